@@ -1,0 +1,352 @@
+"""Benchmark of the BSE hot path: Haydock spectra of the 8x8x8 k-mesh, 100-band,
+12^3 x-mesh 1s-edge workload (Nk=512, Nb=100, Nx=1728, Na=4), one step = one full
+Haydock run (1000 Lanczos iterations, each one H*psi) plus its 2001-point
+continued-fraction spectrum.
+
+Our arm (default):  libocean_gpu.so through its C ABI.
+  value  H*psi/s with psi0 resident in HBM (ocn_haydock_dev), device time from
+         CUDA events on the library's stream.
+  e2e    the same through ocn_haydock + ocn_spectrum_cf with host buffers
+         (pinned psi0 uploaded and coefficients / spectrum read back every step).
+Reference arm (--impl reference): the reference's algorithm restated on the host
+  cores (the oracle, OpenMP, FP64): the reference itself is Fortran+MPI+FFTW+LAPACK
+  and cannot be built in this environment.
+
+Multi-GPU: the path does not shard in this design (replicas only); each rank runs
+an independent replica with its own seed and value sums the ranks' H*psi.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "H*psi/s (Haydock, 8^3 k, 100 bands, 12^3 x-mesh, 1s edge)"
+UNIT = "H*psi/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default=os.environ.get("OCN_BENCH_PRECISION", "fp64"),
+                    choices=["fp64", "mixed"])
+    ap.add_argument("--niter", type=int, default=1000)
+    ap.add_argument("--ne", type=int, default=2000)
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            import torch
+
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        pg = dist
+    return ws, rank, local, pg
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def traffic_summary():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def algorithmic_bytes(w, cls: str, precision: str) -> float:
+    """Bytes one launch of a long-range kernel must move (read + write)."""
+    nb, nk, nx, na = w.nb, w.nk, w.nx, w.na
+    ubytes = nb * nk * nx * w.nspn * (16 if precision == "fp64" else 8)
+    phi = nk * nx * na * (16 if precision == "fp64" else 8)
+    psi = 2 * nb * nk * na * 8
+    if cls == "lr_band_to_x":
+        return ubytes + psi + phi
+    if cls == "lr_x_to_band":
+        return ubytes + phi + psi
+    if cls == "lr_kmesh_transform":
+        return 2 * phi + nk * nx * 8
+    return float("nan")
+
+
+def cpu_baseline(w, seconds: float = 15.0):
+    """Oracle H*psi (FP64, all host cores) on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    cores = os.cpu_count() or 1
+    P = O.OracleProblem(w, nthreads=cores)
+    pr, pi = w.psi_r.copy(), w.psi_i.copy()
+    P.xact(pr, pi)  # warm-up
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        P.xact(pr, pi)
+        n += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} oracle H*psi applications (FP64, OpenMP over x-points) of the same "
+                      f"workload in {dt:.1f} s"}
+
+
+def run_reference(args, ws, rank, pg):
+    from ocean_gb300 import workloads as WL
+
+    if rank != 0:
+        return
+    w = WL.make(args.workload, seed=0)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    cores = os.cpu_count() or 1
+    P = O.OracleProblem(w, nthreads=cores)
+    sample_iters = 3  # Lanczos iterations per step: bounded sample of the 1000-iteration run
+    for _ in range(args.warmup):
+        P.haydock(1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        P.haydock(sample_iters)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = sample_iters * args.steps / tot
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded; u2 QR-orthonormal complex Gaussian, U(0,30) eV bands)",
+            "config": {"workload": f"{args.workload}: Nk=512 (8^3), Nb=100, Nx=1728 (12^3), Na=4",
+                       "step": f"{sample_iters} Lanczos iterations (bounded sample of the "
+                               f"{args.niter}-iteration Haydock run)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{sample_iters} oracle Lanczos iterations per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local, pg):
+    import torch
+
+    from ocean_gb300 import build as B
+    from ocean_gb300 import capi
+    from ocean_gb300 import workloads as WL
+
+    B.build()
+    torch.cuda.set_device(local)
+    prec = capi.OCN_PREC_FP64 if args.precision == "fp64" else capi.OCN_PREC_MIXED
+    w = WL.make(args.workload, seed=rank)
+    ctx = capi.Context(w, precision=prec, device=local)
+    niter, ne = args.niter, args.ne
+    n = w.npsi
+    d_psi = torch.empty(2 * n, dtype=torch.float64, device=f"cuda:{local}")
+    d_psi[:n].copy_(torch.from_numpy(w.psi_r))
+    d_psi[n:].copy_(torch.from_numpy(w.psi_i))
+    torch.cuda.synchronize()
+    pr_ptr = d_psi.data_ptr()
+    pi_ptr = pr_ptr + 8 * n
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
+
+    def step_dev():
+        ra, ia, rb, done = ctx.haydock_dev(niter, pr_ptr, pi_ptr)
+        s = capi.spectrum_cf(ra, ia, rb, done, w.kpref, w.el, w.eh, ne, w.gam0)
+        return ra, rb, s
+
+    for _ in range(args.warmup):
+        step_dev()
+    # ---- timed region (device-resident inputs)
+    ctx.timing(True)
+    ctx.timing_reset()
+    if pg is not None:
+        pg.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    l0 = ctx.launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    last = None
+    for _ in range(args.steps):
+        last = step_dev()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ev1.synchronize()
+    if pg is not None:
+        pg.barrier()
+    clocks = sampler.stop()
+    launches = ctx.launches - l0
+    dev_ms = ev0.elapsed_time(ev1)
+    kt = ctx.timing_read()
+    ctx.timing(False)
+    if pg is not None:
+        t = torch.tensor([dev_ms], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    total_hpsi = niter * args.steps * ws
+    value = total_hpsi / (dev_ms / 1000.0)
+
+    # ---- e2e: pinned host psi0 -> ocn_haydock -> coefficients + spectrum back
+    h_psi = torch.empty(2 * n, dtype=torch.float64).pin_memory()
+    h_psi[:n].copy_(torch.from_numpy(w.psi_r))
+    h_psi[n:].copy_(torch.from_numpy(w.psi_i))
+    hr = h_psi[:n].numpy()
+    hi = h_psi[n:].numpy()
+    ctx.haydock(niter, hr, hi)
+    if pg is not None:
+        pg.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        ra, ia, rb, done = ctx.haydock(niter, hr, hi)
+        capi.spectrum_cf(ra, ia, rb, done, w.kpref, w.el, w.eh, ne, w.gam0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    if pg is not None:
+        t = torch.tensor([e2e_ms], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = total_hpsi / (e2e_ms / 1000.0)
+
+    if rank != 0:
+        ctx.close()
+        return
+    # dominant kernel and its roofline
+    hbm, bf16, src = measured_peaks()
+    lr_classes = {k: v for k, v in kt.items() if v[0] > 0 and k.startswith("lr_")}
+    dom = max(lr_classes, key=lambda k: lr_classes[k][1]) if lr_classes else None
+    roof = None
+    if dom:
+        cnt, ms = lr_classes[dom]
+        per_launch_s = ms / cnt / 1000.0
+        bytes_pl = algorithmic_bytes(w, dom, args.precision)
+        achieved = bytes_pl / per_launch_s / 1e9
+        tr = traffic_summary().get(f"{dom}:{args.precision}:{args.workload}")
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_source": f"{src} hbm_gbs",
+                "traffic": tr, "algorithmic_bytes_per_launch": bytes_pl,
+                "avg_launch_ms": ms / cnt,
+                "kernel_share": {k: round(v[1] / max(1e-9, sum(x[1] for x in kt.values())), 4)
+                                 for k, v in kt.items() if v[0] > 0}}
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(w)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "bf16x2-split/f32/f64",
+            "data": "synthetic (seeded; u2 QR-orthonormal complex Gaussian, U(0,30) eV bands, "
+                    "erf(r/0.5A)/(4r) W table)",
+            "config": {"workload": f"{args.workload}: Nk=512 (8^3), Nb=100, Nx=1728 (12^3), Na=4, "
+                                   f"{niter} Lanczos iterations + {ne + 1}-point spectrum per step",
+                       "precision": args.precision, "parallelism": f"replicas x{ws}",
+                       "l2": "inputs larger than L2 (u2 %.2f GB)" % (
+                           w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
+            "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
+                    "d2h_bytes_per_step": 3 * (niter + 1) * 8 + (ne + 1) * 9 * 8},
+            "gpu_launches": launches, "clocks": clocks, "kernel_ms": kt}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    args = parse()
+    ws, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, ws, rank, pg)
+    else:
+        run_ours(args, ws, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,274 @@
+/*
+ * ocean_gpu.h -- C ABI of libocean_gpu.so, the GB300 (sm_103a) implementation of
+ * OCEAN's core-level BSE Hamiltonian action H*psi and the Haydock / GMRES solvers
+ * that apply it.
+ *
+ * Conventions (mirroring the Fortran module procedures this library replaces):
+ *   - Every entry point returns an int status; 0 = success.  Negative -1 is the
+ *     reference's "NaN in the Lanczos a_n" code (OCEAN2/OCEAN_haydock.f90:913-920);
+ *     positive codes are listed in ocn_status below.  Nothing aborts the process.
+ *   - All arrays are borrowed for the duration of the call.  Arrays with a
+ *     Fortran shape are passed in Fortran (column-major) order, exactly as the
+ *     reference stores them, as separate real and imaginary FP64 planes:
+ *       psi%r / psi%i                (Nb, Nk, Na)          OCEAN2/OCEAN_psi.f90:63-76,4272-4274
+ *       re/im_bloch_state            (Nb, Nk, Nx, nspn)    OCEAN2/long_range.f90:168-179
+ *       W                            (Nk, Nx)              OCEAN2/long_range.f90:1846
+ *       mpcr / mpci                  (Nb, Nk, npmax, 2*lmax+1, lmax-lmin+1, nspn)
+ *                                                          OCEAN2/OCEAN_multiplet.f90:401
+ *       mpm                          (npmax, npmax, lmax-lmin+1)  OCEAN_multiplet.f90:534
+ *       mhr / mhi                    packed blocks, row ii of block l contiguous,
+ *                                    j1 = jbeg(l) + (jj-1) + (ii-1)*mham(l)
+ *                                                          OCEAN_multiplet.f90:1906
+ *       somelr / someli              (Na, Na)              OCEAN_multiplet.f90:666-671
+ *     Energies are in Hartree, as inside ocean.x.
+ *   - One context owns one CUDA stream and the device copies of the operator data
+ *     (the module-global `save` state of the reference).  Calls on one context are
+ *     not thread safe; calls on different contexts are.
+ *   - Entry points ending in _dev take device pointers (FP64 planes laid out as
+ *     above) and run on the context's stream; they do not synchronise unless
+ *     stated.
+ */
+#ifndef OCEAN_GPU_H
+#define OCEAN_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ocn_ctx ocn_ctx;
+
+enum ocn_status {
+  OCN_OK = 0,
+  OCN_ERR_NAN = -1,          /* NaN in a Lanczos coefficient (OCEAN_haydock.f90:917-919) */
+  OCN_ERR_ARG = 1,           /* bad argument / dimension */
+  OCN_ERR_CUDA = 2,          /* CUDA runtime or driver error */
+  OCN_ERR_ALLOC = 3,         /* device or host allocation failed */
+  OCN_ERR_STATE = 4,         /* required operator data not set */
+  OCN_ERR_TIMEOUT = 5,       /* a bounded device wait gave up */
+  OCN_ERR_NOCONV = 6,        /* GMRES hit its restart cap before converging */
+  OCN_ERR_SOLVE = 7,         /* Gram-matrix factorisation failed (LAPACK info analogue) */
+  OCN_ERR_UNSUPPORTED = 9962 /* unsupported flag combination (OCEAN_gmres.f90:539-541) */
+};
+
+enum ocn_precision {
+  OCN_PREC_FP64 = 0,   /* every product and sum in FP64 (reference numerics) */
+  OCN_PREC_MIXED = 1   /* split-BF16 tcgen05 u2 contractions with FP32 accumulation,
+                          FP32 k<->R FFT, FP64 vector/Lanczos/GMRES arithmetic */
+};
+
+/* Problem dimensions.  Replaces the sizes carried by o_system
+ * (OCEAN2/OCEAN_system.f90:14-124) that the hot path reads. */
+typedef struct {
+  int num_bands;   /* Nb   = sys%num_bands                          */
+  int kmesh[3];    /* sys%kmesh; Nk = kmesh[0]*kmesh[1]*kmesh[2]     */
+  int xmesh[3];    /* sys%xmesh; Nx = xmesh[0]*xmesh[1]*xmesh[2]     */
+  int nalpha;      /* Na   = 4*(2*l_c+1) = sys%nalpha                */
+  int nspn;        /* valence spins, 1 or 2 = sys%nspn               */
+  int core_l;      /* l_c  = sys%cur_run%ZNL(3)                      */
+  int precision;   /* enum ocn_precision                             */
+  int device;      /* CUDA device ordinal                            */
+} ocn_dims;
+
+/* Scalars of o_system used by the action (OCEAN_system.f90). */
+typedef struct {
+  double celvol;            /* sys%celvol, Bohr^3                                  */
+  double interaction_scale; /* sys%interactionScale (multiplet mul, OCEAN_multiplet.f90:1641) */
+  int e0;                   /* sys%e0: one-electron energies on                    */
+  int long_range;           /* sys%long_range                                      */
+  int mult;                 /* sys%mult: multiplet (F/G) + spin-orbit terms         */
+  int nhflag[6];            /* sys%nhflag: LR, ladder, bubble, ct, fg, SO switches   */
+} ocn_system;
+
+/* Inputs of lr_populate_W2 / OCEAN_bloch_lrLOAD (long_range.f90:1659-1853,
+ * OCEAN_bloch.f90:54-219). */
+typedef struct {
+  double avec[9];           /* avec(3,3) Fortran order: column i = lattice vector i, Bohr */
+  double tau[3];            /* core-site position, fractional                          */
+  double epsilon0;          /* sys%epsilon0                                            */
+  double interaction_scale; /* sys%interactionScale (W prefactor, long_range.f90:1846)  */
+  int nptab;                /* rpottrim table length                                    */
+  const double* rtab;       /* (nptab) radii, Bohr, ascending                           */
+  const double* ptab;       /* (nptab) screened potential                               */
+  int isolated;             /* isolated.inp present                                     */
+  double iso_cut;           /* its cutoff, Bohr                                         */
+  int pbc[3];               /* pbc.inp (nonzero = periodic); all zero = file absent     */
+  int have_eps3d;           /* sys%have3dEpsilon                                        */
+  double epsilon3d[3];      /* sys%epsilon3D                                            */
+  int xshift_override[3];   /* xshift_override (OCEAN_bloch.f90:113); normally 1,1,1    */
+} ocn_lr_params;
+
+/* Multiplet data loaded by OCEAN_create_central (OCEAN_multiplet.f90:248-570). */
+typedef struct {
+  int lmin, lmax;           /* projector angular momenta                  */
+  const int* nproj;         /* (lmax-lmin+1) radial projectors per l       */
+  const double* mpcr;       /* see layout notes above                      */
+  const double* mpci;
+  const double* mpm;        /* direct (Slater F) matrix, Hartree           */
+  const double* mhr;        /* exchange (G) matrices, Hartree, sum mham^2  */
+  const double* mhi;
+} ocn_mult_data;
+
+/* ---------------------------------------------------------------- context */
+
+/* Allocates device state for one problem.  Replaces the allocations done by
+ * OCEAN_psi_init/new (OCEAN_psi.f90:3867-4060) and lr_init (long_range.f90:108-244). */
+int ocn_ctx_create(const ocn_dims* dims, ocn_ctx** out);
+int ocn_ctx_destroy(ocn_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or timing events against the library's. */
+void* ocn_stream(ocn_ctx* ctx);
+/* Copies the last error message of ctx (or of the last failed create when ctx
+ * is NULL) into buf. */
+int ocn_last_error(const ocn_ctx* ctx, char* buf, size_t len);
+/* Library version string and the compute capability it was built for. */
+const char* ocn_version(void);
+
+/* ---------------------------------------------------------- operator data */
+
+/* o_system scalars and term switches (OCEAN_system.f90:149-614). */
+int ocn_set_system(ocn_ctx* ctx, const ocn_system* sys);
+
+/* p_energy%r/%i after stubby (OCEAN_energies.f90:829-888): complex band energies
+ * epsilon + i Sigma'' on the (Nb,Nk,Na) grid.  im may be NULL (zero). */
+int ocn_set_energies(ocn_ctx* ctx, const double* re, const double* im);
+
+/* allow%r (OCEAN_energies.f90:371-417): real occupation mask on (Nb,Nk,Na). */
+int ocn_set_allow(ocn_ctx* ctx, const double* allow);
+
+/* Raw Bloch functions as read by OCEAN_bloch_load (OCEAN_bloch.f90:395-694),
+ * before the core-hole phase.  (Nb,Nk,Nx,nspn). */
+int ocn_set_bloch(ocn_ctx* ctx, const double* re, const double* im);
+
+/* lr_init step (4): OCEAN_bloch_lrLOAD phase + xshift (OCEAN_bloch.f90:54-219)
+ * applied to the stored Bloch functions, then lr_populate_W2
+ * (long_range.f90:1659-1853).  Requires ocn_set_bloch first. */
+int ocn_lr_init(ocn_ctx* ctx, const ocn_lr_params* p);
+
+/* Direct replacement of W(Nk,Nx) (e.g. from a caller that built it itself). */
+int ocn_set_W(ocn_ctx* ctx, const double* W);
+
+/* Reads back W(Nk,Nx), the xshift and the shifted tau computed by ocn_lr_init.
+ * Any output pointer may be NULL. */
+int ocn_get_W(ocn_ctx* ctx, double* W, int xshift[3], double tau_shifted[3]);
+
+/* Host-only pieces of ocn_lr_init, usable without a GPU or a context:
+ * the xshift / shifted tau of OCEAN_bloch_lrLOAD (OCEAN_bloch.f90:94-123) and
+ * the W(Nk,Nx) table of lr_populate_W2 (long_range.f90:1659-1853).  Only the
+ * kmesh and xmesh fields of dims are read. */
+int ocn_w2_host(const ocn_dims* dims, const ocn_lr_params* p, double* W, int xshift[3],
+                double tau_shifted[3]);
+/* The core-hole phase e^{i phi(x,k)} of OCEAN_bloch_lrLOAD (OCEAN_bloch.f90:141-204)
+ * as cos/sin tables, index x*Nk + k, for the given xshift. */
+int ocn_phase_table_host(const ocn_dims* dims, const int xshift[3], double* cos_tab, double* sin_tab);
+
+/* Reads back the phased Bloch functions (Nb,Nk,Nx,nspn) produced by ocn_lr_init
+ * (the re/im_bloch_state arrays after OCEAN_bloch_lrLOAD). */
+int ocn_get_bloch(ocn_ctx* ctx, double* re, double* im);
+
+/* Multiplet projector data (OCEAN_multiplet.f90:248-570). */
+int ocn_set_mult(ocn_ctx* ctx, const ocn_mult_data* m);
+
+/* Spin-orbit matrix somelr + i someli, (Na,Na) (OCEAN_multiplet.f90:572-690). */
+int ocn_set_spin_orbit(ocn_ctx* ctx, const double* somelr, const double* someli);
+
+/* OCEAN_soprep (OCEAN_multiplet.f90:572-690) without core_broaden.ipt: builds
+ * somelr/someli from xi (Hartree) for core angular momentum dims.core_l and
+ * installs them. */
+int ocn_soprep(ocn_ctx* ctx, double xi);
+
+/* ------------------------------------------------------------------ action */
+
+/* OCEAN_xact (OCEAN_action.f90:286-618), core branch:
+ *   out = E o in + A o [H_fg + H_lr](A o in) + H_so in
+ * hflag may be NULL (use the system's nhflag).  backwards conjugates E and the
+ * spin-orbit matrix as the reference does.  Host buffers; synchronous. */
+int ocn_apply_H(ocn_ctx* ctx, const double* in_r, const double* in_i,
+                double* out_r, double* out_i, const int* hflag, int backwards);
+
+/* Same on device buffers (each (Nb,Nk,Na) FP64), on the context stream. */
+int ocn_apply_H_dev(ocn_ctx* ctx, const double* d_in_r, const double* d_in_i,
+                    double* d_out_r, double* d_out_i, const int* hflag, int backwards);
+
+/* ----------------------------------------------------------------- Haydock */
+
+/* OCEAN_haydock_do -> OCEAN_haydock_Herm_do (OCEAN_haydock.f90:167-320) with
+ * ocean_hay_ab_twoterm (:824-938).  psi0 must already be normalised (core_pnorm,
+ * OCEAN_psi.f90:5589-5638).  Writes real_a[0..niter], imag_a[0..niter],
+ * real_b[0..niter] (index 0 of b unused = 0, a[niter] = 0 as in the reference's
+ * zero-initialised arrays).  *niter_done = iterations completed.
+ * Returns OCN_ERR_NAN if an a_n is NaN (checked after the loop).  Host buffers. */
+int ocn_haydock(ocn_ctx* ctx, const double* psi0_r, const double* psi0_i, int niter,
+                double* real_a, double* imag_a, double* real_b, int* niter_done);
+
+/* Same with psi0 in device memory; coefficient outputs are host arrays. */
+int ocn_haydock_dev(ocn_ctx* ctx, const double* d_psi0_r, const double* d_psi0_i, int niter,
+                    double* real_a, double* imag_a, double* real_b, int* niter_done);
+
+/* core_pnorm (OCEAN_psi.f90:5589-5638): normalises psi in place (host planes of
+ * n = Nb*Nk*Na values) and returns kpref = 4 pi |psi|^2 / (Nk celvol^2). */
+int ocn_psi_pnorm(int n, int nkpts, double celvol, double* psi_r, double* psi_i, double* kpref);
+
+/* write_core (OCEAN_haydock.f90:1801-1894) or write_core_Voigt (:1896-1989)
+ * when gam_gauss > gam0/10: the continued fraction with square-root terminator on
+ * ne+1 energies e = el + (eh-el)*ie/(2ne), ie = 0,2,..,2ne, evaluated on the GPU
+ * in FP64.  Output rows of 9 columns (Voigt: 5 columns, remaining zero):
+ *   Energy(eV), Spect, Spect(0), SPKK, SPKK(0), sigma, sigma cm^2, sig^2, sig^2 cm^4 s.
+ * imag_a may be NULL.  el, eh, gam0, gam_gauss in Hartree; ebase in eV.
+ * old_broaden selects the gamfcn column (nval, eps as in OCEAN_haydock_setup). */
+typedef struct {
+  double el, eh, gam0, ebase, gam_gauss;
+  int ne;
+  double ucvol;
+  int old_broaden;
+  double nval, eps;
+} ocn_cf_params;
+int ocn_spectrum_cf(const double* real_a, const double* imag_a, const double* real_b,
+                    int iter, double kpref, const ocn_cf_params* p, double* out /* (ne+1)*9 */);
+
+/* redtrid (OCEAN_haydock.f90:2273-2316): eigenvalues (ascending) of the (n+1)x(n+1)
+ * tridiagonal Lanczos matrix; host FP64. */
+int ocn_redtrid(int n, const double* real_a, const double* real_b, double* w /* n+1 */);
+
+/* ------------------------------------------------------------------- GMRES */
+
+typedef struct {
+  int depth;              /* gmres_depth (bse.in)                                */
+  double resolution;      /* gmres_resolution = Gamma, Hartree                    */
+  double preconditioner;  /* gmres_preconditioner (gprc), Hartree                 */
+  double convergence;     /* gmres_convergence (ffff) on |g|^2                    */
+  int max_restarts;       /* cap on restart cycles per energy (the reference loops forever) */
+} ocn_gmres_params;
+
+/* OCEAN_gmres_do_recycle (OCEAN_gmres.f90:508-908) with update_gmres (:241-344),
+ * make_recycle (:207-239), set_initial_vector (:1213-1283) and
+ * OCEAN_psi_min_set_prec (OCEAN_psi.f90:2907-2994).  hay_vec is the normalised
+ * psi0 (host planes); energies[nomega] in eV as in bse.in.  For each energy writes
+ *   out_re[i] = 1 - Re<b|x>*kpref, out_im[i] = -Im<b|x>*kpref,
+ *   rel_err[i] = -|g|^2/Im<b|x>, iters[i] = complete_iter
+ * (the abs.gmres columns, OCEAN_gmres.f90:864-869).  Any output may be NULL. */
+int ocn_gmres(ocn_ctx* ctx, const double* hay_r, const double* hay_i, double kpref,
+              const double* energies_ev, int nomega, const ocn_gmres_params* p,
+              double* out_re, double* out_im, double* rel_err, int* iters);
+
+/* --------------------------------------------------------------- counters */
+
+/* Number of kernels this context launched since creation (for accounting). */
+long long ocn_kernel_launches(const ocn_ctx* ctx);
+
+/* Per-kernel device timing with CUDA events recorded on the context stream
+ * (replaces the wall-clock buckets of OCEAN_timekeeper, OCEAN_timekeeper.f90:13-168).
+ * Classes: 0 LR band->x contraction, 1 LR k-mesh transform x W, 2 LR x->band
+ * contraction, 3 LR operand preparation, 4 multiplet, 5 combine + Lanczos step.
+ * ocn_timing_read synchronises the stream and returns, per class, the launch
+ * count and the summed milliseconds since the last reset. */
+int ocn_timing_enable(ocn_ctx* ctx, int on);
+int ocn_timing_reset(ocn_ctx* ctx);
+int ocn_timing_read(ocn_ctx* ctx, long long counts[6], double ms[6]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OCEAN_GPU_H */

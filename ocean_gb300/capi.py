@@ -1,0 +1,350 @@
+"""ctypes bindings of libocean_gpu.so and a thin host-side mirror of the
+reference's call surface (OCEAN_xact / OCEAN_haydock_do / OCEAN_gmres_do_recycle).
+
+The library is the product: this module only marshals numpy arrays across the
+C ABI declared in include/ocean_gpu.h.  It raises if the library is missing;
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libocean_gpu.so")
+
+DP = C.POINTER(C.c_double)
+IP = C.POINTER(C.c_int)
+
+OCN_PREC_FP64 = 0
+OCN_PREC_MIXED = 1
+
+STATUS = {0: "OK", -1: "NaN in Lanczos a", 1: "bad argument", 2: "CUDA error", 3: "allocation failed",
+          4: "operator data not set", 5: "device wait timed out", 6: "GMRES did not converge",
+          7: "Gram matrix factorisation failed", 9962: "unsupported"}
+
+
+class OcnDims(C.Structure):
+    _fields_ = [("num_bands", C.c_int), ("kmesh", C.c_int * 3), ("xmesh", C.c_int * 3),
+                ("nalpha", C.c_int), ("nspn", C.c_int), ("core_l", C.c_int),
+                ("precision", C.c_int), ("device", C.c_int)]
+
+
+class OcnSystem(C.Structure):
+    _fields_ = [("celvol", C.c_double), ("interaction_scale", C.c_double), ("e0", C.c_int),
+                ("long_range", C.c_int), ("mult", C.c_int), ("nhflag", C.c_int * 6)]
+
+
+class OcnLrParams(C.Structure):
+    _fields_ = [("avec", C.c_double * 9), ("tau", C.c_double * 3), ("epsilon0", C.c_double),
+                ("interaction_scale", C.c_double), ("nptab", C.c_int), ("rtab", DP),
+                ("ptab", DP), ("isolated", C.c_int), ("iso_cut", C.c_double),
+                ("pbc", C.c_int * 3), ("have_eps3d", C.c_int), ("epsilon3d", C.c_double * 3),
+                ("xshift_override", C.c_int * 3)]
+
+
+class OcnMultData(C.Structure):
+    _fields_ = [("lmin", C.c_int), ("lmax", C.c_int), ("nproj", IP), ("mpcr", DP), ("mpci", DP),
+                ("mpm", DP), ("mhr", DP), ("mhi", DP)]
+
+
+class OcnCfParams(C.Structure):
+    _fields_ = [("el", C.c_double), ("eh", C.c_double), ("gam0", C.c_double),
+                ("ebase", C.c_double), ("gam_gauss", C.c_double), ("ne", C.c_int),
+                ("ucvol", C.c_double), ("old_broaden", C.c_int), ("nval", C.c_double),
+                ("eps", C.c_double)]
+
+
+class OcnGmresParams(C.Structure):
+    _fields_ = [("depth", C.c_int), ("resolution", C.c_double), ("preconditioner", C.c_double),
+                ("convergence", C.c_double), ("max_restarts", C.c_int)]
+
+
+# every entry point declared in include/ocean_gpu.h
+EXPORTS = [
+    "ocn_ctx_create", "ocn_ctx_destroy", "ocn_last_error", "ocn_version", "ocn_set_system",
+    "ocn_set_energies", "ocn_set_allow", "ocn_set_bloch", "ocn_lr_init", "ocn_set_W", "ocn_get_W",
+    "ocn_get_bloch", "ocn_set_mult", "ocn_set_spin_orbit", "ocn_soprep", "ocn_apply_H",
+    "ocn_apply_H_dev", "ocn_haydock", "ocn_haydock_dev", "ocn_psi_pnorm", "ocn_spectrum_cf",
+    "ocn_redtrid", "ocn_gmres", "ocn_kernel_launches", "ocn_w2_host", "ocn_phase_table_host",
+    "ocn_timing_enable", "ocn_timing_reset", "ocn_timing_read", "ocn_stream",
+]
+
+TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
+                 "combine_lanczos"]
+
+
+def _lr_params(w):
+    p = OcnLrParams()
+    p.avec[:] = list(w.avec)
+    p.tau[:] = list(w.tau)
+    p.epsilon0 = w.epsilon0
+    p.interaction_scale = w.interaction_scale
+    rtab, ptab = _f64(w.rtab), _f64(w.ptab)
+    p.nptab = len(rtab)
+    p.rtab = _dp(rtab)
+    p.ptab = _dp(ptab)
+    p.pbc[:] = [0, 0, 0]
+    p.epsilon3d[:] = [1.0, 1.0, 1.0]
+    p.xshift_override[:] = [1, 1, 1]
+    return p, (rtab, ptab)
+
+
+def _dims(w, precision=0, device=0):
+    d = OcnDims()
+    d.num_bands = w.nb
+    d.kmesh[:] = list(w.kmesh)
+    d.xmesh[:] = list(w.xmesh)
+    d.nalpha = w.na
+    d.nspn = w.nspn
+    d.core_l = w.core_l
+    d.precision = precision
+    d.device = device
+    return d
+
+
+def w2_host(w):
+    """W(Nk,Nx), xshift and shifted tau computed by the library's host code."""
+    d = _dims(w)
+    p, keep = _lr_params(w)
+    W = np.zeros(w.nk * w.nx)
+    xs = (C.c_int * 3)()
+    tau = (C.c_double * 3)()
+    check(load().ocn_w2_host(C.byref(d), C.byref(p), _dp(W), xs, tau))
+    return W, tuple(xs), tuple(tau)
+
+
+def phase_table_host(w, xshift):
+    d = _dims(w)
+    c, s = np.zeros(w.nk * w.nx), np.zeros(w.nk * w.nx)
+    xs = (C.c_int * 3)(*xshift)
+    check(load().ocn_phase_table_host(C.byref(d), xs, _dp(c), _dp(s)))
+    return c, s
+
+_LIB = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libocean_gpu.so; raises (no fallback) if it is absent."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} missing: run ocean_gb300.build.build() first")
+        lib = C.CDLL(path)
+        lib.ocn_version.restype = C.c_char_p
+        lib.ocn_kernel_launches.restype = C.c_longlong
+        lib.ocn_stream.restype = C.c_void_p
+        _LIB = lib
+    return _LIB
+
+
+class OcnError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ocean_gpu error {code} ({STATUS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous, "float64 contiguous array required"
+    return a.ctypes.data_as(DP)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def last_error(ctx=None) -> str:
+    buf = C.create_string_buffer(1024)
+    load().ocn_last_error(ctx, buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int, ctx=None):
+    if rc != 0:
+        raise OcnError(rc, last_error(ctx))
+
+
+class Context:
+    """One problem on one GPU: mirrors the module state the reference loads in
+    ocean_load_data (OCEAN_load_data.f90:8-173) and the operators that use it."""
+
+    def __init__(self, w, precision: int = OCN_PREC_FP64, device: int = 0,
+                 hflag=(1, 1, 1, 1, 1, 1), set_mult: bool = True):
+        lib = load()
+        self.w = w
+        self.lib = lib
+        d = OcnDims()
+        d.num_bands = w.nb
+        d.kmesh[:] = list(w.kmesh)
+        d.xmesh[:] = list(w.xmesh)
+        d.nalpha = w.na
+        d.nspn = w.nspn
+        d.core_l = w.core_l
+        d.precision = precision
+        d.device = device
+        self.dims = d
+        self.ptr = C.c_void_p()
+        check(lib.ocn_ctx_create(C.byref(d), C.byref(self.ptr)))
+        try:
+            s = OcnSystem()
+            s.celvol = w.celvol
+            s.interaction_scale = w.interaction_scale
+            s.e0 = 1
+            s.long_range = 1
+            s.mult = 1 if (w.mult is not None and set_mult) else 0
+            s.nhflag[:] = list(hflag)
+            self._chk(lib.ocn_set_system(self.ptr, C.byref(s)))
+            self._chk(lib.ocn_set_energies(self.ptr, _dp(_f64(w.er)), _dp(_f64(w.ei))))
+            self._chk(lib.ocn_set_allow(self.ptr, _dp(_f64(w.allow))))
+            self._chk(lib.ocn_set_bloch(self.ptr, _dp(_f64(w.ur)), _dp(_f64(w.ui))))
+            p = OcnLrParams()
+            p.avec[:] = list(w.avec)
+            p.tau[:] = list(w.tau)
+            p.epsilon0 = w.epsilon0
+            p.interaction_scale = w.interaction_scale
+            self._rtab = _f64(w.rtab)
+            self._ptab = _f64(w.ptab)
+            p.nptab = len(self._rtab)
+            p.rtab = _dp(self._rtab)
+            p.ptab = _dp(self._ptab)
+            p.pbc[:] = [0, 0, 0]
+            p.epsilon3d[:] = [1.0, 1.0, 1.0]
+            p.xshift_override[:] = [1, 1, 1]
+            self._chk(lib.ocn_lr_init(self.ptr, C.byref(p)))
+            if w.mult is not None and set_mult:
+                m = w.mult
+                md = OcnMultData()
+                md.lmin, md.lmax = m["lmin"], m["lmax"]
+                self._nproj = np.ascontiguousarray(m["nproj"], dtype=np.int32)
+                md.nproj = self._nproj.ctypes.data_as(IP)
+                md.mpcr, md.mpci = _dp(m["mpcr"]), _dp(m["mpci"])
+                md.mpm, md.mhr, md.mhi = _dp(m["mpm"]), _dp(m["mhr"]), _dp(m["mhi"])
+                self._chk(lib.ocn_set_mult(self.ptr, C.byref(md)))
+                self._chk(lib.ocn_soprep(self.ptr, C.c_double(w.so_xi)))
+        except Exception:
+            self.close()
+            raise
+
+    def _chk(self, rc):
+        check(rc, self.ptr)
+
+    def close(self):
+        if self.ptr:
+            self.lib.ocn_ctx_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.ocn_kernel_launches(self.ptr))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.ocn_stream(self.ptr) or 0)
+
+    def haydock_dev(self, niter: int, d_pr: int, d_pi: int):
+        """Haydock with psi0 already in device memory (raw device addresses)."""
+        ra, ia, rb = np.zeros(niter + 1), np.zeros(niter + 1), np.zeros(niter + 1)
+        done = C.c_int(0)
+        self._chk(self.lib.ocn_haydock_dev(self.ptr, C.c_void_p(d_pr), C.c_void_p(d_pi), niter,
+                                           _dp(ra), _dp(ia), _dp(rb), C.byref(done)))
+        return ra, ia, rb, done.value
+
+    def timing(self, on: bool = True):
+        self._chk(self.lib.ocn_timing_enable(self.ptr, int(on)))
+
+    def timing_reset(self):
+        self._chk(self.lib.ocn_timing_reset(self.ptr))
+
+    def timing_read(self) -> dict:
+        counts = (C.c_longlong * 6)()
+        ms = (C.c_double * 6)()
+        self._chk(self.lib.ocn_timing_read(self.ptr, counts, ms))
+        return {name: (int(counts[i]), float(ms[i])) for i, name in enumerate(TIMED_CLASSES)}
+
+    def get_W(self):
+        W = np.zeros(self.w.nk * self.w.nx)
+        xs = (C.c_int * 3)()
+        tau = (C.c_double * 3)()
+        self._chk(self.lib.ocn_get_W(self.ptr, _dp(W), xs, tau))
+        return W, tuple(xs), tuple(tau)
+
+    def get_bloch(self):
+        n = self.w.nb * self.w.nk * self.w.nx * self.w.nspn
+        r, i = np.zeros(n), np.zeros(n)
+        self._chk(self.lib.ocn_get_bloch(self.ptr, _dp(r), _dp(i)))
+        return r, i
+
+    def apply_H(self, pr, pi, hflag=None, backwards=False):
+        n = self.w.npsi
+        outr, outi = np.zeros(n), np.zeros(n)
+        hf = None if hflag is None else (C.c_int * 6)(*hflag)
+        self._chk(self.lib.ocn_apply_H(self.ptr, _dp(_f64(pr)), _dp(_f64(pi)), _dp(outr), _dp(outi),
+                                       hf, int(bool(backwards))))
+        return outr, outi
+
+    def haydock(self, niter: int, pr=None, pi=None):
+        w = self.w
+        pr = w.psi_r if pr is None else pr
+        pi = w.psi_i if pi is None else pi
+        ra, ia, rb = np.zeros(niter + 1), np.zeros(niter + 1), np.zeros(niter + 1)
+        done = C.c_int(0)
+        rc = self.lib.ocn_haydock(self.ptr, _dp(_f64(pr)), _dp(_f64(pi)), niter, _dp(ra), _dp(ia),
+                                  _dp(rb), C.byref(done))
+        self._chk(rc)
+        return ra, ia, rb, done.value
+
+    def gmres(self, energies_ev, depth=80, resolution=None, preconditioner=None, tol=1e-6,
+              max_restarts=50, kpref=None):
+        w = self.w
+        e = _f64(energies_ev)
+        n = len(e)
+        p = OcnGmresParams()
+        p.depth = depth
+        p.resolution = w.gam0 if resolution is None else resolution
+        p.preconditioner = w.gmres_gprc if preconditioner is None else preconditioner
+        p.convergence = tol
+        p.max_restarts = max_restarts
+        ore, oim, rel = np.zeros(n), np.zeros(n), np.zeros(n)
+        its = np.zeros(n, dtype=np.int32)
+        kp = w.kpref if kpref is None else kpref
+        self._chk(self.lib.ocn_gmres(self.ptr, _dp(_f64(w.psi_r)), _dp(_f64(w.psi_i)), C.c_double(kp),
+                                     _dp(e), n, C.byref(p), _dp(ore), _dp(oim), _dp(rel),
+                                     its.ctypes.data_as(IP)))
+        return ore, oim, rel, its
+
+
+def spectrum_cf(ra, ia, rb, iteration: int, kpref: float, el: float, eh: float, ne: int, gam0: float,
+                ebase: float = 0.0, gam_gauss: float = 0.0, ucvol: float = 1.0,
+                old_broaden: int = 0, nval: float = 0.0, eps: float = 1.0) -> np.ndarray:
+    lib = load()
+    p = OcnCfParams()
+    p.el, p.eh, p.gam0, p.ebase, p.gam_gauss = el, eh, gam0, ebase, gam_gauss
+    p.ne, p.ucvol, p.old_broaden, p.nval, p.eps = ne, ucvol, old_broaden, nval, eps
+    out = np.zeros((ne + 1) * 9)
+    ia_p = None if ia is None else _dp(_f64(ia))
+    check(lib.ocn_spectrum_cf(_dp(_f64(ra)), ia_p, _dp(_f64(rb)), iteration, C.c_double(kpref),
+                              C.byref(p), _dp(out)))
+    return out.reshape(ne + 1, 9)
+
+
+def redtrid(n: int, ra, rb) -> np.ndarray:
+    w = np.zeros(n + 1)
+    check(load().ocn_redtrid(n, _dp(_f64(ra)), _dp(_f64(rb)), _dp(w)))
+    return w
+
+
+def pnorm(pr, pi, nkpts: int, celvol: float):
+    pr = _f64(pr).copy()
+    pi = _f64(pi).copy()
+    kp = C.c_double(0.0)
+    check(load().ocn_psi_pnorm(len(pr), nkpts, C.c_double(celvol), _dp(pr), _dp(pi), C.byref(kp)))
+    return pr, pi, kp.value

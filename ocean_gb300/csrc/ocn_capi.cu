@@ -1,0 +1,882 @@
+// ocn_capi.cu -- the extern "C" boundary of libocean_gpu.so: context and operator
+// data management, the H*psi action, and the Haydock and GMRES drivers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "ocn_internal.h"
+
+namespace {
+std::string g_create_err;
+}
+
+namespace ocn {
+
+int set_err(ocn_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  else g_create_err = msg;
+  return code;
+}
+
+int cuda_fail(ocn_ctx* c, cudaError_t e, const char* what) {
+  return set_err(c, OCN_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int kernels_init(ocn_ctx* c);  // ocn_kernels.cu
+int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const double* psi_r,
+                   const double* psi_i, double* h_r, double* h_i, const double* bprev,
+                   double* a_out, double* ia_out, double* b_out);
+
+namespace {
+
+template <typename T>
+int dev_alloc(ocn_ctx* c, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return OCN_OK;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+  if (e != cudaSuccess) return set_err(c, OCN_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return OCN_OK;
+}
+
+int require(ocn_ctx* c) {
+  if (!c->have_energies && c->sys.e0) return set_err(c, OCN_ERR_STATE, "energies not set");
+  if (!c->have_allow) return set_err(c, OCN_ERR_STATE, "allow mask not set");
+  if (c->sys.long_range && (!c->have_bloch || !c->have_W))
+    return set_err(c, OCN_ERR_STATE, "long-range term on but Bloch functions / W not set");
+  return OCN_OK;
+}
+
+// H*psi on device vectors (OCEAN_xact, OCEAN_action.f90:286-618).
+int apply_H_impl(ocn_ctx* c, const double* ir, const double* ii, double* orr, double* oi,
+                 const int* hflag_in, int backwards) {
+  int hflag[6];
+  for (int i = 0; i < 6; ++i) hflag[i] = hflag_in ? hflag_in[i] : c->sys.nhflag[i];
+  int rc = require(c);
+  if (rc) return rc;
+  if ((rc = zero_acc(c))) return rc;
+  if (c->sys.mult && hflag[4] == 1 && c->have_mult)
+    if ((rc = mult_apply(c, ir, ii))) return rc;
+  if (c->sys.long_range && hflag[0] == 1) {
+    if (c->dims.precision == OCN_PREC_MIXED) rc = lr_apply_mixed(c, ir, ii);
+    else rc = lr_apply_fp64(c, ir, ii);
+    if (rc) return rc;
+  }
+  return combine(c, ir, ii, orr, oi, hflag, backwards);
+}
+
+}  // namespace
+}  // namespace ocn
+
+using namespace ocn;
+
+extern "C" {
+
+const char* ocn_version(void) { return "ocean_gb300 0.1 (sm_103a)"; }
+
+int ocn_last_error(const ocn_ctx* ctx, char* buf, size_t len) {
+  if (!buf || len == 0) return OCN_ERR_ARG;
+  const std::string& s = ctx ? ctx->err : g_create_err;
+  std::snprintf(buf, len, "%s", s.c_str());
+  return OCN_OK;
+}
+
+long long ocn_kernel_launches(const ocn_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+void* ocn_stream(ocn_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
+
+int ocn_timing_enable(ocn_ctx* c, int on) {
+  if (!c) return OCN_ERR_ARG;
+  c->timing.on = on != 0;
+  return OCN_OK;
+}
+
+int ocn_timing_read(ocn_ctx* c, long long counts[6], double ms[6]) {
+  if (!c) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < T_NCLASS; ++k) {
+    for (auto& pr : c->timing.pending[k]) {
+      float t = 0.0f;
+      if (cudaEventElapsedTime(&t, pr.first, pr.second) == cudaSuccess) {
+        c->timing.total_ms[k] += t;
+        c->timing.count[k] += 1;
+      }
+      c->timing.pool.push_back(pr.first);
+      c->timing.pool.push_back(pr.second);
+    }
+    c->timing.pending[k].clear();
+    if (counts) counts[k] = c->timing.count[k];
+    if (ms) ms[k] = c->timing.total_ms[k];
+  }
+  return OCN_OK;
+}
+
+int ocn_timing_reset(ocn_ctx* c) {
+  if (!c) return OCN_ERR_ARG;
+  int rc = ocn_timing_read(c, nullptr, nullptr);
+  for (int k = 0; k < T_NCLASS; ++k) {
+    c->timing.total_ms[k] = 0.0;
+    c->timing.count[k] = 0;
+  }
+  return rc;
+}
+
+int ocn_ctx_create(const ocn_dims* d, ocn_ctx** out) {
+  if (!d || !out) return set_err(nullptr, OCN_ERR_ARG, "null argument");
+  *out = nullptr;
+  const int nk = d->kmesh[0] * d->kmesh[1] * d->kmesh[2];
+  const int nx = d->xmesh[0] * d->xmesh[1] * d->xmesh[2];
+  for (int i = 0; i < 3; ++i) {
+    if (d->kmesh[i] < 1 || d->kmesh[i] > OCN_MAX_KDIM)
+      return set_err(nullptr, OCN_ERR_ARG, "kmesh extent out of range 1..32");
+    if (d->xmesh[i] < 1) return set_err(nullptr, OCN_ERR_ARG, "xmesh extent must be >= 1");
+  }
+  if (d->num_bands < 1 || d->num_bands > 1024)
+    return set_err(nullptr, OCN_ERR_ARG, "num_bands must be in 1..1024");
+  if (d->core_l < 0 || d->core_l > 1) return set_err(nullptr, OCN_ERR_ARG, "core_l must be 0 or 1");
+  if (d->nalpha != 4 * (2 * d->core_l + 1))
+    return set_err(nullptr, OCN_ERR_ARG, "nalpha must equal 4*(2*core_l+1)");
+  if (d->nspn != 1 && d->nspn != 2) return set_err(nullptr, OCN_ERR_ARG, "nspn must be 1 or 2");
+  if (nk > OCN_MAX_NK) return set_err(nullptr, OCN_ERR_ARG, "k-mesh larger than 4096 points");
+  if ((size_t)2 * d->nalpha * nk * sizeof(double2) > 227u * 1024u)
+    return set_err(nullptr, OCN_ERR_ARG, "nalpha*Nk too large for the shared-memory k-mesh transform");
+  if (d->precision != OCN_PREC_FP64 && d->precision != OCN_PREC_MIXED)
+    return set_err(nullptr, OCN_ERR_ARG, "unknown precision");
+  if (d->precision == OCN_PREC_MIXED && d->num_bands > 256)
+    return set_err(nullptr, OCN_ERR_ARG, "mixed precision supports at most 256 bands");
+
+  ocn_ctx* c = new (std::nothrow) ocn_ctx();
+  if (!c) return set_err(nullptr, OCN_ERR_ALLOC, "host allocation failed");
+  c->dims = *d;
+  c->nb = d->num_bands;
+  c->nk = nk;
+  c->nx = nx;
+  c->na = d->nalpha;
+  c->nspn = d->nspn;
+  c->npsi = (size_t)c->nb * nk * c->na;
+  c->device = d->device;
+  c->sys.celvol = 1.0;
+  c->sys.interaction_scale = 1.0;
+  c->sys.e0 = 1;
+  c->sys.long_range = 1;
+  c->sys.mult = 0;
+  for (int i = 0; i < 6; ++i) c->sys.nhflag[i] = 1;
+
+  auto fail = [&](int rc) {
+    std::string m = c->err;
+    ocn_ctx_destroy(c);
+    set_err(nullptr, rc, m);
+    return rc;
+  };
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return fail(cuda_fail(c, e, "cudaSetDevice"));
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  c->sm_count = sms > 0 ? sms : 1;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(cuda_fail(c, e, "cudaStreamCreate"));
+
+  c->red_blocks = 2 * c->sm_count;
+  c->lr_xsplit = std::max(1, std::min((2 * c->sm_count + nk - 1) / nk, std::max(1, nx / 64)));
+  int rc = OCN_OK;
+  if ((rc = dev_alloc(c, &c->d_er, c->npsi)) || (rc = dev_alloc(c, &c->d_ei, c->npsi)) ||
+      (rc = dev_alloc(c, &c->d_allow, c->npsi)) ||
+      (rc = dev_alloc(c, &c->d_u, (size_t)c->nb * nk * nx * c->nspn)) ||
+      (rc = dev_alloc(c, &c->d_W, (size_t)nk * nx)) ||
+      (rc = dev_alloc(c, &c->d_so, (size_t)c->na * c->na)) ||
+      (rc = dev_alloc(c, &c->d_acc, 2 * c->npsi)) ||
+      (rc = dev_alloc(c, &c->d_red, (size_t)8 * c->red_blocks)) ||
+      (rc = dev_alloc(c, &c->d_scal, 64)))
+    return fail(rc);
+  if (d->precision == OCN_PREC_FP64) {
+    if ((rc = dev_alloc(c, &c->d_phi, (size_t)nk * nx * c->na)) ||
+        (rc = dev_alloc(c, &c->d_accpart, (size_t)c->lr_xsplit * 2 * c->npsi)))
+      return fail(rc);
+  }
+  cudaMemsetAsync(c->d_ei, 0, sizeof(double) * c->npsi, c->stream);
+  cudaMemsetAsync(c->d_so, 0, sizeof(double2) * c->na * c->na, c->stream);
+  if ((rc = upload_twiddles(c)) || (rc = kernels_init(c))) return fail(rc);
+  if (d->precision == OCN_PREC_MIXED && (rc = mixed_init(c))) return fail(rc);
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail(cuda_fail(c, e, "ocn_ctx_create"));
+  *out = c;
+  return OCN_OK;
+}
+
+int ocn_ctx_destroy(ocn_ctx* c) {
+  if (!c) return OCN_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->mixed) mixed_free(c);
+  void* bufs[] = {c->d_er, c->d_ei, c->d_allow, c->d_u, c->d_W, c->d_so, c->d_phi, c->d_acc,
+                  c->d_accpart, c->d_vec, c->d_red, c->d_scal, c->mult.mpc, c->mult.mpm, c->mult.mh,
+                  c->mult.p_l, c->mult.p_m, c->mult.p_nu, c->mult.d_pfirst, c->mult.d_nproj,
+                  c->mult.d_jbeg, c->mult.amp, c->mult.amp_part, c->mult.hamp};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  for (int k = 0; k < T_NCLASS; ++k)
+    for (auto& pr : c->timing.pending[k]) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  for (cudaEvent_t e : c->timing.pool) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return OCN_OK;
+}
+
+int ocn_set_system(ocn_ctx* c, const ocn_system* s) {
+  if (!c || !s) return OCN_ERR_ARG;
+  if (s->celvol <= 0.0) return set_err(c, OCN_ERR_ARG, "celvol must be positive");
+  c->sys = *s;
+  return OCN_OK;
+}
+
+int ocn_set_energies(ocn_ctx* c, const double* re, const double* im) {
+  if (!c || !re) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  OCN_CUDA(c, cudaMemcpyAsync(c->d_er, re, sizeof(double) * c->npsi, cudaMemcpyHostToDevice, c->stream));
+  if (im)
+    OCN_CUDA(c, cudaMemcpyAsync(c->d_ei, im, sizeof(double) * c->npsi, cudaMemcpyHostToDevice, c->stream));
+  else
+    OCN_CUDA(c, cudaMemsetAsync(c->d_ei, 0, sizeof(double) * c->npsi, c->stream));
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_energies = true;
+  return OCN_OK;
+}
+
+int ocn_set_allow(ocn_ctx* c, const double* allow) {
+  if (!c || !allow) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  OCN_CUDA(c, cudaMemcpyAsync(c->d_allow, allow, sizeof(double) * c->npsi, cudaMemcpyHostToDevice, c->stream));
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_allow = true;
+  return OCN_OK;
+}
+
+int ocn_set_bloch(ocn_ctx* c, const double* re, const double* im) {
+  if (!c || !re || !im) return OCN_ERR_ARG;
+  const size_t n = (size_t)c->nb * c->nk * c->nx * c->nspn;
+  try {
+    c->h_ur.assign(re, re + n);
+    c->h_ui.assign(im, im + n);
+  } catch (...) {
+    return set_err(c, OCN_ERR_ALLOC, "host copy of the Bloch functions failed");
+  }
+  c->have_bloch = false;  // phased copy produced by ocn_lr_init
+  return OCN_OK;
+}
+
+int ocn_lr_init(ocn_ctx* c, const ocn_lr_params* p) {
+  if (!c || !p || !p->rtab || !p->ptab || p->nptab < 2) return OCN_ERR_ARG;
+  if (c->h_ur.empty()) return set_err(c, OCN_ERR_STATE, "ocn_set_bloch must precede ocn_lr_init");
+  if (p->epsilon0 <= 0.0) return set_err(c, OCN_ERR_ARG, "epsilon0 must be positive");
+  cudaSetDevice(c->device);
+  double tau[3] = {p->tau[0], p->tau[1], p->tau[2]};
+  int xs[3];
+  const int ovr[3] = {p->xshift_override[0], p->xshift_override[1], p->xshift_override[2]};
+  lrload_shift(c->dims, tau, ovr, xs);
+  std::vector<double> pc, ps;
+  lrload_phase_table(c->dims, xs, pc, ps);
+  populate_w2(c->dims, *p, tau, xs, c->h_W);
+  for (int i = 0; i < 3; ++i) {
+    c->xshift[i] = xs[i];
+    c->tau_shifted[i] = tau[i];
+  }
+  const size_t n = c->h_ur.size();
+  double *d_raw = nullptr, *d_tab = nullptr;
+  int rc = dev_alloc(c, &d_raw, 2 * n);
+  if (rc) return rc;
+  rc = dev_alloc(c, &d_tab, 2 * pc.size());
+  if (rc) {
+    cudaFree(d_raw);
+    return rc;
+  }
+  cudaError_t e = cudaMemcpyAsync(d_raw, c->h_ur.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_raw + n, c->h_ui.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_tab, pc.data(), pc.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_tab + pc.size(), ps.data(), ps.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->d_W, c->h_W.data(), c->h_W.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) rc = phase_bloch(c, d_raw, d_raw + n, d_tab, d_tab + pc.size());
+  if (e == cudaSuccess && rc == OCN_OK) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_raw);
+  cudaFree(d_tab);
+  if (e != cudaSuccess) return cuda_fail(c, e, "ocn_lr_init");
+  if (rc) return rc;
+  c->have_bloch = true;
+  c->have_W = true;
+  if (c->dims.precision == OCN_PREC_MIXED) return mixed_set_bloch(c);
+  return OCN_OK;
+}
+
+int ocn_set_W(ocn_ctx* c, const double* W) {
+  if (!c || !W) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  const size_t n = (size_t)c->nk * c->nx;
+  c->h_W.assign(W, W + n);
+  OCN_CUDA(c, cudaMemcpyAsync(c->d_W, W, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_W = true;
+  if (c->dims.precision == OCN_PREC_MIXED && c->have_bloch) return mixed_set_bloch(c);
+  return OCN_OK;
+}
+
+int ocn_get_W(ocn_ctx* c, double* W, int xshift[3], double tau_shifted[3]) {
+  if (!c) return OCN_ERR_ARG;
+  if (W) {
+    if (c->h_W.empty()) return set_err(c, OCN_ERR_STATE, "W not set");
+    std::memcpy(W, c->h_W.data(), c->h_W.size() * sizeof(double));
+  }
+  for (int i = 0; i < 3; ++i) {
+    if (xshift) xshift[i] = c->xshift[i];
+    if (tau_shifted) tau_shifted[i] = c->tau_shifted[i];
+  }
+  return OCN_OK;
+}
+
+int ocn_w2_host(const ocn_dims* d, const ocn_lr_params* p, double* W, int xshift[3],
+                double tau_shifted[3]) {
+  if (!d || !p || !p->rtab || !p->ptab || p->nptab < 2 || p->epsilon0 <= 0.0)
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_w2_host: bad argument");
+  for (int i = 0; i < 3; ++i)
+    if (d->kmesh[i] < 1 || d->xmesh[i] < 1) return set_err(nullptr, OCN_ERR_ARG, "bad mesh");
+  double tau[3] = {p->tau[0], p->tau[1], p->tau[2]};
+  int xs[3];
+  const int ovr[3] = {p->xshift_override[0], p->xshift_override[1], p->xshift_override[2]};
+  lrload_shift(*d, tau, ovr, xs);
+  std::vector<double> w;
+  populate_w2(*d, *p, tau, xs, w);
+  if (W) std::memcpy(W, w.data(), w.size() * sizeof(double));
+  for (int i = 0; i < 3; ++i) {
+    if (xshift) xshift[i] = xs[i];
+    if (tau_shifted) tau_shifted[i] = tau[i];
+  }
+  return OCN_OK;
+}
+
+int ocn_phase_table_host(const ocn_dims* d, const int xshift[3], double* ct, double* st) {
+  if (!d || !xshift || !ct || !st) return set_err(nullptr, OCN_ERR_ARG, "ocn_phase_table_host: null");
+  std::vector<double> c, s;
+  lrload_phase_table(*d, xshift, c, s);
+  std::memcpy(ct, c.data(), c.size() * sizeof(double));
+  std::memcpy(st, s.data(), s.size() * sizeof(double));
+  return OCN_OK;
+}
+
+int ocn_get_bloch(ocn_ctx* c, double* re, double* im) {
+  if (!c || !re || !im) return OCN_ERR_ARG;
+  if (!c->have_bloch) return set_err(c, OCN_ERR_STATE, "Bloch functions not initialised");
+  cudaSetDevice(c->device);
+  const size_t n = (size_t)c->nb * c->nk * c->nx * c->nspn;
+  std::vector<double2> tmp(n);
+  OCN_CUDA(c, cudaMemcpy(tmp.data(), c->d_u, n * sizeof(double2), cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < n; ++i) {
+    re[i] = tmp[i].x;
+    im[i] = tmp[i].y;
+  }
+  return OCN_OK;
+}
+
+int ocn_set_spin_orbit(ocn_ctx* c, const double* r, const double* im) {
+  if (!c || !r || !im) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  const int na = c->na;
+  std::vector<double2> so((size_t)na * na);
+  for (int j = 0; j < na; ++j)
+    for (int i = 0; i < na; ++i) so[(size_t)j * na + i] = make_double2(r[i + na * j], im[i + na * j]);
+  c->h_so_r.assign(r, r + (size_t)na * na);
+  c->h_so_i.assign(im, im + (size_t)na * na);
+  OCN_CUDA(c, cudaMemcpyAsync(c->d_so, so.data(), so.size() * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_so = true;
+  return OCN_OK;
+}
+
+int ocn_soprep(ocn_ctx* c, double xi) {
+  if (!c) return OCN_ERR_ARG;
+  std::vector<double> r, im;
+  soprep(c->dims.core_l, xi, r, im);
+  // have_spin_orbit = .false. when xi < 1e-12 (OCEAN_multiplet.f90:615)
+  if (xi < 1.0e-12) {
+    c->have_so = false;
+    return OCN_OK;
+  }
+  return ocn_set_spin_orbit(c, r.data(), im.data());
+}
+
+int ocn_set_mult(ocn_ctx* c, const ocn_mult_data* m) {
+  if (!c || !m || !m->nproj || !m->mpcr || !m->mpci || !m->mpm || !m->mhr || !m->mhi)
+    return OCN_ERR_ARG;
+  if (m->lmin < 0 || m->lmax < m->lmin) return set_err(c, OCN_ERR_ARG, "bad lmin/lmax");
+  cudaSetDevice(c->device);
+  MultDev& d = c->mult;
+  const int nl = m->lmax - m->lmin + 1;
+  int npmax = 0;
+  for (int i = 0; i < nl; ++i) {
+    if (m->nproj[i] < 0) return set_err(c, OCN_ERR_ARG, "negative nproj");
+    npmax = std::max(npmax, m->nproj[i]);
+  }
+  // valid projector list in the reference's (l, m, nu) order
+  std::vector<int> pl, pm, pnu, pfirst(nl), nproj(m->nproj, m->nproj + nl);
+  std::vector<long long> jbeg(nl);
+  long long jt = 0;
+  for (int l = m->lmin; l <= m->lmax; ++l) {
+    const int li = l - m->lmin;
+    pfirst[li] = (int)pl.size();
+    for (int mm = -l; mm <= l; ++mm)
+      for (int nu = 0; nu < nproj[li]; ++nu) {
+        pl.push_back(l);
+        pm.push_back(mm);
+        pnu.push_back(nu);
+      }
+    jbeg[li] = jt;
+    const long long mham = (long long)c->na * (2 * l + 1) * nproj[li];
+    jt += mham * mham;
+  }
+  const int np = (int)pl.size();
+  const int nbk = c->nb * c->nk;
+  const int nm = 2 * m->lmax + 1;
+  // repack mpc(nb, nk, npmax, 2lmax+1, nl, nspn) -> [s][p][k*nb + n]
+  std::vector<double2> mpc((size_t)c->nspn * np * nbk);
+  for (int s = 0; s < c->nspn; ++s)
+    for (int p = 0; p < np; ++p) {
+      const size_t src = (size_t)nbk * ((size_t)pnu[p] + (size_t)npmax * ((size_t)(pm[p] + m->lmax) +
+                                        (size_t)nm * ((size_t)(pl[p] - m->lmin) + (size_t)nl * s)));
+      double2* dst = mpc.data() + ((size_t)s * np + p) * nbk;
+      for (int e = 0; e < nbk; ++e) dst[e] = make_double2(m->mpcr[src + e], m->mpci[src + e]);
+    }
+  std::vector<double2> mh((size_t)jt);
+  for (long long j = 0; j < jt; ++j) mh[j] = make_double2(m->mhr[j], m->mhi[j]);
+  // free a previous set
+  void* old[] = {d.mpc, d.mpm, d.mh, d.p_l, d.p_m, d.p_nu, d.d_pfirst, d.d_nproj, d.d_jbeg,
+                 d.amp, d.amp_part, d.hamp};
+  for (void* p : old)
+    if (p) cudaFree(p);
+  d = MultDev();
+  d.np = np;
+  d.lmin = m->lmin;
+  d.lmax = m->lmax;
+  d.npmax = npmax;
+  d.nproj = nproj;
+  const int chunk = 256;
+  d.nchunk = (nbk + chunk - 1) / chunk;
+  int rc;
+  if ((rc = dev_alloc(c, &d.mpc, mpc.size())) || (rc = dev_alloc(c, &d.mpm, (size_t)npmax * npmax * nl)) ||
+      (rc = dev_alloc(c, &d.mh, mh.size())) || (rc = dev_alloc(c, &d.p_l, np)) ||
+      (rc = dev_alloc(c, &d.p_m, np)) || (rc = dev_alloc(c, &d.p_nu, np)) ||
+      (rc = dev_alloc(c, &d.d_pfirst, nl)) || (rc = dev_alloc(c, &d.d_nproj, nl)) ||
+      (rc = dev_alloc(c, &d.d_jbeg, nl)) || (rc = dev_alloc(c, &d.amp, (size_t)np * c->na)) ||
+      (rc = dev_alloc(c, &d.hamp, (size_t)np * c->na)) ||
+      (rc = dev_alloc(c, &d.amp_part, (size_t)d.nchunk * np * c->na)))
+    return rc;
+  OCN_CUDA(c, cudaMemcpy(d.mpc, mpc.data(), mpc.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  OCN_CUDA(c, cudaMemcpy(d.mpm, m->mpm, (size_t)npmax * npmax * nl * sizeof(double), cudaMemcpyHostToDevice));
+  OCN_CUDA(c, cudaMemcpy(d.mh, mh.data(), mh.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  OCN_CUDA(c, cudaMemcpy(d.p_l, pl.data(), np * sizeof(int), cudaMemcpyHostToDevice));
+  OCN_CUDA(c, cudaMemcpy(d.p_m, pm.data(), np * sizeof(int), cudaMemcpyHostToDevice));
+  OCN_CUDA(c, cudaMemcpy(d.p_nu, pnu.data(), np * sizeof(int), cudaMemcpyHostToDevice));
+  OCN_CUDA(c, cudaMemcpy(d.d_pfirst, pfirst.data(), nl * sizeof(int), cudaMemcpyHostToDevice));
+  OCN_CUDA(c, cudaMemcpy(d.d_nproj, nproj.data(), nl * sizeof(int), cudaMemcpyHostToDevice));
+  OCN_CUDA(c, cudaMemcpy(d.d_jbeg, jbeg.data(), nl * sizeof(long long), cudaMemcpyHostToDevice));
+  c->have_mult = true;
+  return OCN_OK;
+}
+
+int ocn_apply_H_dev(ocn_ctx* c, const double* ir, const double* ii, double* orr, double* oi,
+                    const int* hflag, int backwards) {
+  if (!c || !ir || !ii || !orr || !oi) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  return apply_H_impl(c, ir, ii, orr, oi, hflag, backwards);
+}
+
+int ocn_apply_H(ocn_ctx* c, const double* ir, const double* ii, double* orr, double* oi,
+                const int* hflag, int backwards) {
+  if (!c || !ir || !ii || !orr || !oi) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  const size_t n = c->npsi;
+  double* buf = nullptr;
+  int rc = dev_alloc(c, &buf, 4 * n);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(buf, ir, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(buf + n, ii, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) rc = apply_H_impl(c, buf, buf + n, buf + 2 * n, buf + 3 * n, hflag, backwards);
+  if (e == cudaSuccess && rc == OCN_OK)
+    e = cudaMemcpyAsync(orr, buf + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && rc == OCN_OK)
+    e = cudaMemcpyAsync(oi, buf + 3 * n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(c, e, "ocn_apply_H");
+  return rc;
+}
+
+// ----------------------------------------------------------------- Haydock
+
+int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter, double* real_a,
+                    double* imag_a, double* real_b, int* niter_done) {
+  if (!c || !p0r || !p0i || niter < 1 || !real_a || !real_b) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  int rc = require(c);
+  if (rc) return rc;
+  const size_t n = c->npsi;
+  double* vec = nullptr;
+  double* coef = nullptr;  // [real_a | imag_a | real_b], each niter+1
+  if ((rc = dev_alloc(c, &vec, 6 * n))) return rc;
+  if ((rc = dev_alloc(c, &coef, 3 * (size_t)(niter + 1)))) {
+    cudaFree(vec);
+    return rc;
+  }
+  double* ra = coef;
+  double* ia = coef + (niter + 1);
+  double* rb = coef + 2 * (niter + 1);
+  double* buf[3] = {vec, vec + 2 * n, vec + 4 * n};  // old, psi, h
+  cudaError_t e = cudaMemsetAsync(coef, 0, 3 * (size_t)(niter + 1) * sizeof(double), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(buf[0], 0, 2 * n * sizeof(double), c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(buf[1], p0r, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(buf[1] + n, p0i, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  int done = 0;
+  for (int it = 1; it <= niter && e == cudaSuccess && rc == OCN_OK; ++it) {
+    double* old = buf[0];
+    double* psi = buf[1];
+    double* h = buf[2];
+    if ((rc = zero_acc(c))) break;
+    if (c->sys.mult && c->sys.nhflag[4] == 1 && c->have_mult && (rc = mult_apply(c, psi, psi + n))) break;
+    if (c->sys.long_range && c->sys.nhflag[0] == 1) {
+      rc = (c->dims.precision == OCN_PREC_MIXED) ? lr_apply_mixed(c, psi, psi + n)
+                                                 : lr_apply_fp64(c, psi, psi + n);
+      if (rc) break;
+    }
+    rc = lanczos_launch(c, old, old + n, psi, psi + n, h, h + n, rb + (it - 1), ra + (it - 1),
+                        ia + (it - 1), rb + it);
+    if (rc) break;
+    buf[0] = psi;  // old <- psi
+    buf[1] = h;    // psi <- h / b
+    buf[2] = old;
+    done = it;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  std::vector<double> host(3 * (size_t)(niter + 1));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(host.data(), coef, host.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(vec);
+  cudaFree(coef);
+  if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock");
+  if (rc) return rc;
+  for (int i = 0; i <= niter; ++i) {
+    real_a[i] = host[i];
+    if (imag_a) imag_a[i] = host[(niter + 1) + i];
+    real_b[i] = host[2 * (niter + 1) + i];
+  }
+  if (niter_done) *niter_done = done;
+  // NaN check on a (OCEAN_haydock.f90:913-920): the reference stops at the first
+  // NaN; report the iteration count up to it.
+  for (int i = 0; i < done; ++i)
+    if (std::isnan(real_a[i])) {
+      if (niter_done) *niter_done = i + 1;
+      return set_err(c, OCN_ERR_NAN, "NaN detected in Lanczos a");
+    }
+  return OCN_OK;
+}
+
+int ocn_haydock(ocn_ctx* c, const double* p0r, const double* p0i, int niter, double* real_a,
+                double* imag_a, double* real_b, int* niter_done) {
+  if (!c || !p0r || !p0i) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  const size_t n = c->npsi;
+  double* d = nullptr;
+  int rc = dev_alloc(c, &d, 2 * n);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(d, p0r, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d + n, p0i, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    return cuda_fail(c, e, "ocn_haydock upload");
+  }
+  rc = ocn_haydock_dev(c, d, d + n, niter, real_a, imag_a, real_b, niter_done);
+  cudaFree(d);
+  return rc;
+}
+
+int ocn_psi_pnorm(int n, int nkpts, double celvol, double* pr, double* pi, double* kpref) {
+  if (n < 1 || !pr || !pi || !kpref || nkpts < 1 || celvol <= 0.0) return OCN_ERR_ARG;
+  double val = 0.0;
+  for (int i = 0; i < n; ++i) val += pr[i] * pr[i] + pi[i] * pi[i];
+  val = std::sqrt(val);
+  const double pi_ = 3.1415926535897932384626433832795028841971693993751;
+  *kpref = 4.0 * pi_ * val * val / ((double)nkpts * celvol * celvol);
+  const double inv = 1.0 / val;
+  for (int i = 0; i < n; ++i) {
+    pr[i] *= inv;
+    pi[i] *= inv;
+  }
+  return OCN_OK;
+}
+
+int ocn_spectrum_cf(const double* real_a, const double* imag_a, const double* real_b, int iter,
+                    double kpref, const ocn_cf_params* p, double* out) {
+  if (!real_a || !real_b || !p || !out) return set_err(nullptr, OCN_ERR_ARG, "null argument");
+  std::string err;
+  int rc = cf_eval(real_a, imag_a, real_b, iter, kpref, p, out, &err);
+  if (rc) set_err(nullptr, rc, err);
+  return rc;
+}
+
+int ocn_redtrid(int n, const double* real_a, const double* real_b, double* w) {
+  if (n < 0 || !real_a || !real_b || !w) return OCN_ERR_ARG;
+  return redtrid_eigs(n, real_a, real_b, w) ? OCN_ERR_SOLVE : OCN_OK;
+}
+
+// ------------------------------------------------------------------- GMRES
+
+namespace {
+
+// Cholesky factorisation and solve of the Hermitian positive-definite Gram
+// matrix C (upper triangle given, C_ij = <au_i|au_j>), for C c = rhs.
+int herm_solve(int n, const std::vector<std::complex<double>>& up, std::vector<std::complex<double>>& b) {
+  typedef std::complex<double> cd;
+  std::vector<cd> L((size_t)n * n, cd(0.0, 0.0));  // lower, L L^H = C
+  auto Cij = [&](int i, int j) -> cd {             // i <= j stored
+    return (i <= j) ? up[(size_t)i + (size_t)j * (j + 1) / 2] : std::conj(up[(size_t)j + (size_t)i * (i + 1) / 2]);
+  };
+  for (int j = 0; j < n; ++j) {
+    double d = Cij(j, j).real();
+    for (int k = 0; k < j; ++k) d -= std::norm(L[(size_t)j * n + k]);
+    if (!(d > 0.0)) return j + 1;
+    const double ljj = std::sqrt(d);
+    L[(size_t)j * n + j] = ljj;
+    for (int i = j + 1; i < n; ++i) {
+      cd s = Cij(i, j);
+      for (int k = 0; k < j; ++k) s -= L[(size_t)i * n + k] * std::conj(L[(size_t)j * n + k]);
+      L[(size_t)i * n + j] = s / ljj;
+    }
+  }
+  for (int i = 0; i < n; ++i) {  // L y = b
+    cd s = b[i];
+    for (int k = 0; k < i; ++k) s -= L[(size_t)i * n + k] * b[k];
+    b[i] = s / L[(size_t)i * n + i].real();
+  }
+  for (int i = n - 1; i >= 0; --i) {  // L^H x = y
+    cd s = b[i];
+    for (int k = i + 1; k < n; ++k) s -= std::conj(L[(size_t)k * n + i]) * b[k];
+    b[i] = s / L[(size_t)i * n + i].real();
+  }
+  return 0;
+}
+
+struct Gmres {
+  ocn_ctx* c;
+  size_t n;
+  int depth;
+  std::vector<double*> u, au;
+  double** d_ul = nullptr;
+  double** d_aul = nullptr;
+  double* d_part = nullptr;
+  double* d_out = nullptr;
+  double2* d_coef = nullptr;
+  std::vector<std::complex<double>> cmat;
+  long long hpsi = 0;
+
+  int H(const double* in, double* out) {
+    ++hpsi;
+    return apply_H_impl(c, in, in + n, out, out + n, nullptr, 0);
+  }
+  int dot(const double* p, const double* q, double* r, double* i) {
+    int rc = vec_dot_dev(c, p, q, c->d_scal);
+    if (rc) return rc;
+    double h[2];
+    OCN_CUDA(c, cudaMemcpyAsync(h, c->d_scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+    *r = h[0];
+    if (i) *i = h[1];
+    return OCN_OK;
+  }
+  // update_gmres (OCEAN_gmres.f90:241-344)
+  int update(int cur, double* g, double* x, double* ax) {
+    int rc = vec_multidot_dev(c, const_cast<const double* const*>(d_aul), cur, au[cur - 1], g, d_part, d_out);
+    if (rc) return rc;
+    std::vector<double> h(4 * (size_t)cur);
+    OCN_CUDA(c, cudaMemcpyAsync(h.data(), d_out, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+    const size_t start = (size_t)cur * (cur - 1) / 2;
+    for (int j = 0; j < cur; ++j) {
+      // c_matrix(iter + iter_start) = conj(<au_cur|au_iter>); the diagonal is the norm
+      if (j == cur - 1) cmat[start + j] = std::complex<double>(h[4 * j], 0.0);
+      else cmat[start + j] = std::complex<double>(h[4 * j], -h[4 * j + 1]);
+    }
+    std::vector<std::complex<double>> coef(cur);
+    for (int j = 0; j < cur; ++j) coef[j] = -std::complex<double>(h[4 * j + 2], h[4 * j + 3]);
+    const int info = herm_solve(cur, cmat, coef);
+    if (info) return set_err(c, OCN_ERR_SOLVE, "GMRES Gram matrix not positive definite");
+    std::vector<double2> hc(cur);
+    for (int j = 0; j < cur; ++j) hc[j] = make_double2(coef[j].real(), coef[j].imag());
+    OCN_CUDA(c, cudaMemcpyAsync(d_coef, hc.data(), cur * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+    return vec_update_dev(c, cur, d_coef, const_cast<const double* const*>(d_ul),
+                          const_cast<const double* const*>(d_aul), x, ax);
+  }
+};
+
+}  // namespace
+
+int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref,
+              const double* elist, int nomega, const ocn_gmres_params* p, double* out_re,
+              double* out_im, double* rel_err, int* iters) {
+  if (!c || !hay_r || !hay_i || !elist || nomega < 1 || !p || p->depth < 1) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  int rc = require(c);
+  if (rc) return rc;
+  const double ev2ha = 0.036749322175666;
+  Gmres G;
+  G.c = c;
+  G.n = c->npsi;
+  G.depth = p->depth;
+  const size_t n = c->npsi;
+  const int nfixed = 8;  // rhs x ax hpsi1 g pcdiv ones spare
+  double* pool = nullptr;
+  if ((rc = dev_alloc(c, &pool, (size_t)(nfixed + 2 * p->depth) * 2 * n))) return rc;
+  auto V = [&](int i) { return pool + (size_t)i * 2 * n; };
+  double *rhs = V(0), *x = V(1), *ax = V(2), *hpsi1 = V(3), *g = V(4), *pcdiv = V(5), *ones = V(6);
+  for (int j = 0; j < p->depth; ++j) {
+    G.u.push_back(V(nfixed + j));
+    G.au.push_back(V(nfixed + p->depth + j));
+  }
+  std::vector<void*> owned{pool};
+  auto cleanup = [&]() {
+    for (void* q : owned) cudaFree(q);
+  };
+  if ((rc = dev_alloc(c, &G.d_ul, p->depth)) || (owned.push_back(G.d_ul), false) ||
+      (rc = dev_alloc(c, &G.d_aul, p->depth)) || (owned.push_back(G.d_aul), false) ||
+      (rc = dev_alloc(c, &G.d_part, (size_t)c->red_blocks * p->depth * 4)) ||
+      (owned.push_back(G.d_part), false) || (rc = dev_alloc(c, &G.d_out, (size_t)p->depth * 4)) ||
+      (owned.push_back(G.d_out), false) || (rc = dev_alloc(c, &G.d_coef, p->depth)) ||
+      (owned.push_back(G.d_coef), false)) {
+    cleanup();
+    return rc;
+  }
+  G.cmat.assign((size_t)p->depth * (p->depth + 1) / 2, std::complex<double>(0.0, 0.0));
+  cudaError_t e = cudaMemcpyAsync(G.d_ul, G.u.data(), p->depth * sizeof(double*), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(G.d_aul, G.au.data(), p->depth * sizeof(double*), cudaMemcpyHostToDevice, c->stream);
+  // psi_rhs = sfact(hay_vec): allow o hay (OCEAN_gmres.f90:586)
+  if (e == cudaSuccess) e = cudaMemcpyAsync(g, hay_r, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(g + n, hay_i, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) {
+    cleanup();
+    return cuda_fail(c, e, "ocn_gmres upload");
+  }
+  auto run = [&]() -> int {
+    int r;
+    if ((r = vec_mask_copy(c, g, rhs))) return r;
+    if ((r = vec_fill(c, ones, 1.0, 0.0))) return r;
+    if ((r = G.H(ones, hpsi1))) return r;  // H * (1,0), :600-608
+    int global_iter = 0, prev_iter = 0;
+    double prev_energy = -1.0e308;
+    double rval = 0.0, ival = 0.0, gval = 0.0;
+    for (int step = 0; step < nomega; ++step) {
+      int complete_iter = 0;
+      const double ener = elist[step] * ev2ha;
+      bool converged = false;
+      if (prev_iter == 0) {
+        prev_energy = ener;
+        if ((r = vec_set_prec(c, ener, p->preconditioner, hpsi1, pcdiv))) return r;
+      }
+      // set_initial_vector: keep x for step > 0 (force_reuse_x, OCEAN_gmres.f90:24-27,1232-1241)
+      auto initial = [&]() -> int {
+        int q;
+        if (step > 0) {
+          if ((q = G.H(x, ax))) return q;
+          if ((q = vec_axmy(c, x, ax, ener, p->resolution))) return q;
+        } else {
+          if ((q = vec_fill(c, x, 0.0, 0.0))) return q;
+          if ((q = vec_fill(c, ax, 0.0, 0.0))) return q;
+        }
+        return vec_axmz(c, ax, g, rhs);
+      };
+      if (prev_iter == 0) {
+        if ((r = initial())) return r;
+        if ((r = G.dot(g, g, &gval, nullptr))) return r;
+        if ((r = G.dot(rhs, x, &rval, &ival))) return r;
+      } else {
+        const double delta = elist[step] * ev2ha - elist[step - 1] * ev2ha;  // make_recycle
+        for (int j = 0; j < prev_iter; ++j)
+          if ((r = vec_axpy(c, delta, 0.0, G.u[j], G.au[j]))) return r;
+        if ((r = initial())) return r;
+        for (int it = 1; it <= prev_iter; ++it) {
+          if ((r = G.update(it, g, x, ax))) return r;
+          if ((r = vec_axmz(c, ax, g, rhs))) return r;
+        }
+        if ((r = G.dot(g, g, &gval, nullptr))) return r;
+        if ((r = G.dot(rhs, x, &rval, &ival))) return r;
+        if (gval < p->convergence) {
+          const double rel = -gval / ival;
+          if (rel < 0.001 || gval < p->convergence / 10.0) converged = true;
+        }
+        if (!converged && std::fabs(prev_energy - ener) > p->preconditioner / 4.0) {
+          prev_iter = 0;
+          prev_energy = ener;
+          if ((r = vec_set_prec(c, ener, p->preconditioner, hpsi1, pcdiv))) return r;
+        }
+      }
+      int restarts = 0;
+      while (!converged) {
+        for (int it = prev_iter + 1; it <= p->depth; ++it) {
+          ++complete_iter;
+          ++global_iter;
+          double* pg = G.u[it - 1];
+          double* apg = G.au[it - 1];
+          if ((r = vec_mul(c, g, pcdiv, pg))) return r;
+          if ((r = G.H(pg, apg))) return r;
+          if ((r = vec_axmy(c, pg, apg, ener, p->resolution))) return r;
+          if ((r = G.update(it, g, x, ax))) return r;
+          if (it == p->depth) {
+            if ((r = G.H(x, ax))) return r;
+            if ((r = vec_axmy(c, x, ax, ener, p->resolution))) return r;
+            if (ener != prev_energy) {
+              if ((r = vec_set_prec(c, ener, p->preconditioner, hpsi1, pcdiv))) return r;
+              prev_energy = ener;
+            }
+            prev_iter = 0;
+          }
+          if ((r = vec_axmz(c, ax, g, rhs))) return r;
+          if ((r = G.dot(g, g, &gval, nullptr))) return r;
+          if ((r = G.dot(rhs, x, &rval, &ival))) return r;
+          if (gval < p->convergence) {
+            const double rel = -gval / ival;
+            if (rel < 0.001 || gval < p->convergence / 10.0) {
+              prev_iter = (it == p->depth) ? 0 : it;
+              converged = true;
+              break;
+            }
+          }
+        }
+        if (converged) break;
+        if (++restarts > std::max(0, p->max_restarts))
+          return set_err(c, OCN_ERR_NOCONV, "GMRES restart cap reached");
+      }
+      if (out_re) out_re[step] = 1.0 - rval * kpref;
+      if (out_im) out_im[step] = -ival * kpref;
+      if (rel_err) rel_err[step] = -gval / ival;
+      if (iters) iters[step] = complete_iter;
+    }
+    return OCN_OK;
+  };
+  rc = run();
+  e = cudaStreamSynchronize(c->stream);
+  cleanup();
+  if (e != cudaSuccess) return cuda_fail(c, e, "ocn_gmres");
+  return rc;
+}
+
+}  // extern "C"

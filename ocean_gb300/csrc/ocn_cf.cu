@@ -1,0 +1,245 @@
+// ocn_cf.cu -- Haydock continued fraction on the GPU (write_core,
+// OCEAN_haydock.f90:1801-1894, and write_core_Voigt, :1896-1989).
+//
+// One thread per energy point, FP64.  The reference builds two of the complex
+// numbers in its recurrence with cmplx(x, y) without a KIND, which Fortran
+// evaluates in default (single) precision: b_j*c_j and (e - a_j) + i(gam + ia_j)
+// are rounded to binary32 before entering the FP64 recurrence (:1837, :1868-1869).
+// The golden spectra in EXAMPLE/Cu_TwoPhoton/Results carry that rounding, so it is
+// restated here.  This file is compiled with -fmad=false so that every product
+// and sum rounds exactly as written.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "ocn_internal.h"
+
+namespace ocn {
+
+namespace {
+
+// OCEAN2/OCEAN_constants.f90:15-30
+constexpr double kEV2Ha = 0.036749322175666;
+constexpr double kHa2eV = 27.211386245980;
+constexpr double kAlpha = 0.0072973525643;
+constexpr double kBohr = 0.529177210544;
+constexpr double kAu2sec = 2.4188843265864e-17;
+constexpr double kPi = 3.1415926535897932384626433832795028841971693993751;
+
+struct cplx {
+  double x, y;
+};
+
+__device__ __forceinline__ cplx cdiv_smith(cplx n, cplx d) {
+  if (fabs(d.x) >= fabs(d.y)) {
+    const double r = d.y / d.x;
+    const double t = 1.0 / (d.x + d.y * r);
+    return {(n.x + n.y * r) * t, (n.y - n.x * r) * t};
+  }
+  const double r = d.x / d.y;
+  const double t = 1.0 / (d.x * r + d.y);
+  return {(n.x * r + n.y) * t, (n.y * r - n.x) * t};
+}
+
+__device__ __forceinline__ cplx csqrt_principal(cplx z) {
+  if (z.x == 0.0 && z.y == 0.0) return {0.0, z.y};
+  const double t = sqrt((fabs(z.x) + sqrt(z.x * z.x + z.y * z.y)) * 0.5);
+  if (z.x >= 0.0) return {t, z.y / (2.0 * t)};
+  return {fabs(z.y) / (2.0 * t), copysign(t, z.y)};
+}
+
+// b_j c_j with c = b real (Hermitian Lanczos), as a binary32 product.
+__device__ __forceinline__ double bsq_sp(double b) {
+  const float f = __double2float_rn(b);
+  return (double)__fmul_rn(f, f);
+}
+
+__device__ cplx cf_delta(const double* __restrict__ ra, const double* __restrict__ ia,
+                         const double* __restrict__ rb, int iter, double e, double gam) {
+  const double ial = ia ? ia[iter - 1] : 0.0;
+  const cplx ct = {e - ra[iter - 1], gam + ial};
+  const double bc4 = (double)__fmul_rn(4.0f, __double2float_rn(bsq_sp(rb[iter])));
+  const cplx sq = {ct.x * ct.x - ct.y * ct.y - bc4, ct.x * ct.y + ct.y * ct.x};
+  const cplx disc = csqrt_principal(sq);
+  cplx delta;
+  if (disc.y > 0.0)
+    delta = {(ct.x + disc.x) * 0.5, (ct.y + disc.y) * 0.5};
+  else
+    delta = {(ct.x - disc.x) * 0.5, (ct.y - disc.y) * 0.5};
+  for (int jj = iter - 1; jj >= 0; --jj) {
+    const cplx c2 = {bsq_sp(rb[jj + 1]), 0.0};
+    const double iaj = ia ? ia[jj] : 0.0;
+    const cplx z = {(double)__double2float_rn(e - ra[jj]), (double)__double2float_rn(gam + iaj)};
+    const cplx q = cdiv_smith(c2, delta);
+    delta = {z.x - q.x, z.y - q.y};
+  }
+  return delta;
+}
+
+__global__ void k_write_core(const double* __restrict__ ra, const double* __restrict__ ia,
+                             const double* __restrict__ rb, int iter, double kpref, double el,
+                             double eh, int ne, double gam0, const double* __restrict__ gam1,
+                             double ebase, double ucvol, double* __restrict__ out) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row > ne) return;
+  const int ie = 2 * row;
+  const double e = el + (eh - el) * (double)ie / (double)(2 * ne);
+  const cplx d = cf_delta(ra, ia, rb, iter, e, gam0);
+  const double dr = d.x, di = fabs(d.y);
+  const double spct = kpref * di / (dr * dr + di * di);
+  const double spkk = kpref * dr / (dr * dr + di * di);
+  double spct1 = spct, spkk1 = spkk;
+  if (gam1) {  // oldXASbroaden: second damping with gamfcn (OCEAN_haydock.f90:1839-1841)
+    const cplx d1 = cf_delta(ra, ia, rb, iter, e, gam1[row]);
+    const double dr1 = d1.x, di1 = fabs(d1.y);
+    spct1 = kpref * di1 / (dr1 * dr1 + di1 * di1);
+    spkk1 = kpref * dr1 / (dr1 * dr1 + di1 * di1);
+  }
+  const double alphaByVolumeHartree = kEV2Ha * kAlpha * ucvol;
+  const double tpa = (kAlpha * kAlpha * 2.0 * kPi) * ucvol;
+  const double bohrSq2CmSq = kBohr * kBohr * 1.0e-16;
+  const double tpacm4 = tpa * bohrSq2CmSq * bohrSq2CmSq * kAu2sec;
+  const double ener = ebase + kHa2eV * e;
+  const double sigma = alphaByVolumeHartree * ener * spct;
+  double* r = out + 9 * (size_t)row;
+  r[0] = ener;
+  r[1] = spct1;
+  r[2] = spct;
+  r[3] = spkk1;
+  r[4] = spkk;
+  r[5] = sigma;
+  r[6] = sigma * bohrSq2CmSq;
+  r[7] = spct * tpa;
+  r[8] = spct * tpacm4;
+}
+
+// Voigt variant: Lorentzian spectrum on the fine grid e_i = el + (i - nstep)*estep
+// (each fine point of write_core_Voigt evaluated once), with damping gam[i].
+__global__ void k_cf_points(const double* __restrict__ ra, const double* __restrict__ ia,
+                            const double* __restrict__ rb, int iter, double kpref, double el,
+                            int nstep, double estep, const double* __restrict__ gam,
+                            double prefactor, double* __restrict__ sp, double* __restrict__ sk,
+                            int npts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npts) return;
+  const double e = el + (double)(i - nstep) * estep;
+  const cplx d = cf_delta(ra, ia, rb, iter, e, gam[i]);
+  const double dr = d.x, di = fabs(d.y);
+  sp[i] = prefactor * kpref * di / (dr * dr + di * di);
+  sk[i] = prefactor * kpref * dr / (dr * dr + di * di);
+}
+
+}  // namespace
+
+int cf_eval(const double* ra, const double* ia, const double* rb, int iter, double kpref,
+            const ocn_cf_params* p, double* out, std::string* err) {
+  if (iter < 1 || p->ne < 1) {
+    if (err) *err = "ocn_spectrum_cf: iter and ne must be >= 1";
+    return OCN_ERR_ARG;
+  }
+  const size_t nco = (size_t)iter + 1;
+  std::vector<void*> owned;
+  cudaError_t e = cudaSuccess;
+  auto cleanup = [&]() {
+    for (void* q : owned) cudaFree(q);
+    owned.clear();
+  };
+  auto dalloc = [&](size_t bytes) -> double* {
+    void* q = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&q, bytes);
+    if (e == cudaSuccess) owned.push_back(q);
+    return static_cast<double*>(q);
+  };
+  auto h2d = [&](double* d, const double* h, size_t n) {
+    if (e == cudaSuccess) e = cudaMemcpy(d, h, n * sizeof(double), cudaMemcpyHostToDevice);
+  };
+  double* d_ra = dalloc(nco * sizeof(double));
+  double* d_rb = dalloc(nco * sizeof(double));
+  double* d_ia = ia ? dalloc(nco * sizeof(double)) : nullptr;
+  h2d(d_ra, ra, nco);
+  h2d(d_rb, rb, nco);
+  if (ia) h2d(d_ia, ia, nco);
+  const int ne = p->ne;
+  if (e == cudaSuccess && p->gam_gauss > p->gam0 / 10.0) {
+    // write_core_Voigt: fine grid shared between neighbouring output rows
+    const double de = (p->eh - p->el) / (double)ne;
+    double estep = fmin(p->gam0, p->gam_gauss) / 2.0;
+    const int nratio = (int)((de - estep) / estep) + 1;
+    estep = de / (double)nratio;
+    const int nstep = (int)((2.99999 * p->gam_gauss) / estep) + 1;
+    const double prefactor = estep / (p->gam_gauss * 2.506628274631);
+    const double inv2s2 = 1.0 / (2.0 * p->gam_gauss * p->gam_gauss);
+    const int npts = ne * nratio + 2 * nstep + 1;
+    std::vector<double> g0(npts, p->gam0), g1(npts);
+    for (int i = 0; i < npts; ++i)
+      g1[i] = p->gam0 + gamfcn(p->el + (double)(i - nstep) * estep, p->nval, p->eps);
+    double* d_g0 = dalloc(npts * sizeof(double));
+    double* d_g1 = dalloc(npts * sizeof(double));
+    double* d_sp = dalloc(2 * (size_t)npts * sizeof(double));
+    double* d_sk = dalloc(2 * (size_t)npts * sizeof(double));
+    h2d(d_g0, g0.data(), npts);
+    h2d(d_g1, g1.data(), npts);
+    if (e == cudaSuccess) {
+      k_cf_points<<<(npts + 127) / 128, 128>>>(d_ra, d_ia, d_rb, iter, kpref, p->el, nstep, estep,
+                                              d_g0, prefactor, d_sp, d_sk, npts);
+      k_cf_points<<<(npts + 127) / 128, 128>>>(d_ra, d_ia, d_rb, iter, kpref, p->el, nstep, estep,
+                                              d_g1, prefactor, d_sp + npts, d_sk + npts, npts);
+      e = cudaGetLastError();
+    }
+    std::vector<double> sp(2 * (size_t)npts), sk(2 * (size_t)npts);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(sp.data(), d_sp, sp.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(sk.data(), d_sk, sk.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) {
+      for (int row = 0; row <= ne; ++row) {
+        double s0 = 0.0, s1 = 0.0, k0 = 0.0, k1 = 0.0;
+        for (int ii = -nstep; ii <= nstep; ++ii) {
+          const double pref = exp(-(double)(ii * ii) * estep * estep * inv2s2);
+          const int idx = row * nratio + ii + nstep;
+          s0 += pref * sp[idx];
+          s1 += pref * sp[npts + idx];
+          k0 += pref * sk[idx];
+          k1 += pref * sk[npts + idx];
+        }
+        const double ee = p->el + (p->eh - p->el) * (double)(2 * row) / (double)(2 * ne);
+        double* r = out + 9 * (size_t)row;
+        r[0] = p->ebase + kHa2eV * (ee + (double)nstep * estep);
+        r[1] = s1;
+        r[2] = s0;
+        r[3] = k1;
+        r[4] = k0;
+        r[5] = r[6] = r[7] = r[8] = 0.0;
+      }
+    }
+  } else if (e == cudaSuccess) {
+    double* d_g1 = nullptr;
+    if (p->old_broaden) {
+      std::vector<double> g1(ne + 1);
+      for (int row = 0; row <= ne; ++row) {
+        const double en = p->el + (p->eh - p->el) * (double)(2 * row) / (double)(2 * ne);
+        g1[row] = p->gam0 + gamfcn(en, p->nval, p->eps);
+      }
+      d_g1 = dalloc((ne + 1) * sizeof(double));
+      h2d(d_g1, g1.data(), ne + 1);
+    }
+    double* d_out = dalloc((size_t)(ne + 1) * 9 * sizeof(double));
+    if (e == cudaSuccess) {
+      k_write_core<<<(ne + 1 + 63) / 64, 64>>>(d_ra, d_ia, d_rb, iter, kpref, p->el, p->eh, ne,
+                                             p->gam0, d_g1, p->ebase, p->ucvol, d_out);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpy(out, d_out, (size_t)(ne + 1) * 9 * sizeof(double), cudaMemcpyDeviceToHost);
+  }
+  cleanup();
+  if (e != cudaSuccess) {
+    if (err) *err = std::string("ocn_spectrum_cf: ") + cudaGetErrorString(e);
+    return OCN_ERR_CUDA;
+  }
+  return OCN_OK;
+}
+
+}  // namespace ocn

@@ -1,0 +1,188 @@
+// ocn_internal.h -- shared definitions of libocean_gpu.so (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/ocean_gpu.h"
+
+#define OCN_MAX_NA 12       // 4*(2*l_c+1) for l_c <= 1 (1s, 2p edges)
+#define OCN_MAX_KDIM 32     // largest k-mesh extent along one axis handled by the FFT kernels
+#define OCN_MAX_NK 4096     // largest k-mesh size (shared-memory FFT)
+
+namespace ocn {
+
+struct MixedLR;  // split-BF16 / tcgen05 state (ocn_mixed.cu)
+
+// Kernel classes timed with CUDA events on the context stream when timing is on.
+enum TimedClass { T_LR_GEMM1 = 0, T_LR_FFT, T_LR_GEMM2, T_LR_PREP, T_MULT, T_LANCZOS, T_NCLASS };
+
+struct Timing {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[T_NCLASS];
+  double total_ms[T_NCLASS] = {0, 0, 0, 0, 0, 0};
+  long long count[T_NCLASS] = {0, 0, 0, 0, 0, 0};
+};
+
+// Multiplet data packed for the device: valid projectors only.
+struct MultDev {
+  int np = 0;                  // number of valid (nu, m, l) projectors
+  int lmin = 0, lmax = -1, npmax = 0;
+  std::vector<int> nproj;
+  double2* mpc = nullptr;      // [s][p][k][n] complex (conjugation applied in kernels)
+  double* mpm = nullptr;       // packed per l blocks as given (npmax,npmax,nl)
+  double2* mh = nullptr;       // concatenated blocks, row ii contiguous
+  int* p_l = nullptr;          // per projector: l, m, nu  (device)
+  int* p_m = nullptr;
+  int* p_nu = nullptr;
+  int* d_pfirst = nullptr;     // per l: first projector index of the block
+  int* d_nproj = nullptr;      // per l: radial projectors
+  long long* d_jbeg = nullptr; // per l: offset of the exchange block in mh
+  double2* amp = nullptr;      // [p][a] amplitudes
+  double2* amp_part = nullptr; // [chunk][p][a]
+  double2* hamp = nullptr;     // [p][a]
+  int nchunk = 0;
+};
+
+}  // namespace ocn
+
+struct ocn_ctx {
+  ocn_dims dims{};
+  int nb = 0, nk = 0, nx = 0, na = 0, nspn = 1;
+  size_t npsi = 0;           // Nb*Nk*Na
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  long long launches = 0;
+
+  ocn_system sys{};
+  bool have_energies = false, have_allow = false, have_bloch = false, have_W = false;
+  bool have_so = false, have_mult = false;
+
+  // operator data (device)
+  double* d_er = nullptr;    // energies (npsi)
+  double* d_ei = nullptr;
+  double* d_allow = nullptr;
+  double2* d_u = nullptr;    // phased Bloch functions, [s][x][k][n] complex (reference order)
+  double* d_W = nullptr;     // (Nk, Nx): W[x*Nk + k]
+  double2* d_so = nullptr;   // (Na,Na) somelr + i someli, [jc*Na + ic]
+  std::vector<double> h_so_r, h_so_i;
+
+  // host copies of setup inputs / results
+  std::vector<double> h_ur, h_ui;  // raw Bloch functions
+  std::vector<double> h_W;
+  int xshift[3] = {0, 0, 0};
+  double tau_shifted[3] = {0, 0, 0};
+
+  // work buffers
+  double2* d_phi = nullptr;        // FP64 path: [k][x][a]
+  double* d_acc = nullptr;         // full-store accumulator: re plane then im plane (npsi each)
+  double* d_accpart = nullptr;     // GEMM2 x-split partials [split][2][npsi]
+  int lr_xsplit = 1;
+  double* d_vec = nullptr;         // general vector pool (see ocn_solvers.cu)
+  size_t vec_pool_n = 0;
+  double* d_red = nullptr;         // reduction partials
+  double* d_scal = nullptr;        // device scalars (a, b, ...)
+  int red_blocks = 0;
+
+  ocn::MultDev mult;
+  ocn::MixedLR* mixed = nullptr;
+
+  ocn::Timing timing;
+};
+
+namespace ocn {
+
+int set_err(ocn_ctx* c, int code, const std::string& msg);
+int cuda_fail(ocn_ctx* c, cudaError_t e, const char* what);
+
+#define OCN_CUDA(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) return ocn::cuda_fail(ctx, _e, #call); \
+  } while (0)
+
+// Event bracket around one timed launch (no-op unless timing is on).
+struct TimedScope {
+  ocn_ctx* c;
+  int cls;
+  cudaEvent_t a = nullptr, b = nullptr;
+  TimedScope(ocn_ctx* ctx, int k) : c(ctx), cls(k) {
+    if (!c->timing.on) return;
+    a = take();
+    b = take();
+    if (a && b) cudaEventRecord(a, c->stream);
+  }
+  ~TimedScope() {
+    if (!a || !b) return;
+    cudaEventRecord(b, c->stream);
+    c->timing.pending[cls].emplace_back(a, b);
+  }
+  cudaEvent_t take() {
+    if (!c->timing.pool.empty()) {
+      cudaEvent_t e = c->timing.pool.back();
+      c->timing.pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+  }
+};
+
+// ---- host setup (ocn_setup.cpp)
+void lrload_shift(const ocn_dims& d, double tau[3], const int ovr[3], int xshift[3]);
+void lrload_phase_table(const ocn_dims& d, const int xshift[3], std::vector<double>& c,
+                        std::vector<double>& s);  // (Nk, Nx) cos/sin, [x*Nk + k]
+void populate_w2(const ocn_dims& d, const ocn_lr_params& p, const double tau[3], const int xshift[3],
+                 std::vector<double>& W);
+void soprep(int core_l, double xi, std::vector<double>& r, std::vector<double>& i);
+int redtrid_eigs(int n, const double* ra, const double* rb, double* w);
+double gamfcn(double e, double n, double e0);
+
+// ---- FP64 kernels (ocn_kernels.cu)
+int upload_twiddles(ocn_ctx* c);
+int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi);  // adds into d_acc
+int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi);     // adds into d_acc
+int phase_bloch(ocn_ctx* c, const double* d_ur, const double* d_ui, const double* d_cos,
+                const double* d_sin);
+// out = E o in + A o acc + SO in   (acc already holds H_fg + H_lr of A o in)
+int combine(ocn_ctx* c, const double* d_pr, const double* d_pi, double* d_or, double* d_oi,
+            const int* hflag, int backwards);
+int zero_acc(ocn_ctx* c);
+
+// Fused Lanczos step (combine + ocean_hay_ab_twoterm); coefficients stay on device.
+int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const double* psi_r,
+                   const double* psi_i, double* h_r, double* h_i, const double* bprev,
+                   double* a_out, double* ia_out, double* b_out);
+
+// BLAS-1 helpers for GMRES (ocn_kernels.cu); vectors are [re plane | im plane]
+int vec_dot_dev(ocn_ctx* c, const double* p, const double* q, double* d_out);
+int vec_multidot_dev(ocn_ctx* c, const double* const* d_vecs, int nvec, const double* au_cur,
+                     const double* g, double* d_part, double* d_out);
+int vec_update_dev(ocn_ctx* c, int nvec, const double2* d_coef, const double* const* d_ul,
+                   const double* const* d_aul, double* x, double* ax);
+int vec_axmy(ocn_ctx* c, const double* x, double* y, double rv, double iv);
+int vec_axmz(ocn_ctx* c, const double* x, double* y, const double* z);
+int vec_axpy(ocn_ctx* c, double ar, double ai, const double* x, double* y);
+int vec_mul(ocn_ctx* c, const double* x, const double* y, double* z);
+int vec_set_prec(ocn_ctx* c, double energy, double gprc, const double* h, double* out);
+int vec_mask_copy(ocn_ctx* c, const double* in, double* out);
+int vec_fill(ocn_ctx* c, double* x, double vr, double vi);
+
+// ---- continued fraction (ocn_cf.cu)
+int cf_eval(const double* ra, const double* ia, const double* rb, int iter, double kpref,
+            const ocn_cf_params* p, double* out, std::string* err);
+
+// ---- mixed precision (ocn_mixed.cu)
+int mixed_init(ocn_ctx* c);
+int mixed_free(ocn_ctx* c);
+int mixed_set_bloch(ocn_ctx* c);   // builds split-BF16 layouts from d_u
+int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi);  // adds into d_acc
+
+}  // namespace ocn

@@ -1,0 +1,965 @@
+// ocn_kernels.cu -- FP64 kernels of the BSE action and the vector steps of the
+// Haydock and GMRES solvers.
+//
+// Device layouts
+//   psi-like vectors  two planes re[npsi], im[npsi], npsi = Nb*Nk*Na, element
+//                     (n,k,a) at n + Nb*(k + Nk*a)  (OCEAN_psi.f90:63-76)
+//   u                 double2 [s][x][k][n]            (long_range.f90:168-179)
+//   W                 double  [x][k]                  (long_range.f90:1846)
+//   phi (FP64 path)   double2 [k][x][a]
+#include <cuda_runtime.h>
+
+#include <cstdio>
+
+#include "ocn_internal.h"
+
+namespace ocn {
+
+namespace {
+
+__constant__ double2 c_tw[3][OCN_MAX_KDIM];  // exp(+2 pi i t / n_axis)
+__constant__ int c_kdim[3];
+
+// ------------------------------------------------------------ phase of u2
+
+// u(n,k,x,s) *= exp(i phi(x,k)) exactly as OCEAN_bloch_lrLOAD writes it
+// (OCEAN_bloch.f90:191-197); explicit _rn intrinsics keep the products unfused.
+__global__ void k_phase_bloch(const double* __restrict__ ur, const double* __restrict__ ui,
+                              const double* __restrict__ pc, const double* __restrict__ ps,
+                              double2* __restrict__ u, long long total, int nb, int nk, int nx) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long q = i / nb;         // k + nk*(x + nx*s)
+    long long xk = q % ((long long)nk * nx);
+    double c = pc[xk], s = ps[xk];
+    double r = ur[i], m = ui[i];
+    u[i] = make_double2(__dsub_rn(__dmul_rn(c, r), __dmul_rn(s, m)),
+                        __dadd_rn(__dmul_rn(c, m), __dmul_rn(s, r)));
+  }
+}
+
+// ---------------------------------------------------- LR: band -> x-mesh
+
+// phi[k][x][a] = sum_n u(n,k,x) * (allow o psi)(n,k,a)   (long_range.f90:897-906)
+// grid (ceil(Nx/128), Nk), 128 threads: thread = x.  u staged through shared
+// memory transposed so each thread reads its own column conflict-free.
+constexpr int G1_X = 128;
+constexpr int G1_N = 32;
+__global__ void __launch_bounds__(G1_X) k_lr_gemm1_fp64(
+    const double2* __restrict__ u, const double* __restrict__ pr, const double* __restrict__ pi,
+    const double* __restrict__ allow, double2* __restrict__ phi, int nb, int nk, int nx, int na,
+    int nspn) {
+  extern __shared__ double2 smem[];
+  double2* us = smem;                          // [nspn][G1_N][G1_X+1]
+  double2* ps = smem + nspn * G1_N * (G1_X + 1);  // [na][G1_N]
+  const int k = blockIdx.y;
+  const int x0 = blockIdx.x * G1_X;
+  const int tx = threadIdx.x;
+  const int x = x0 + tx;
+  double2 acc[OCN_MAX_NA];
+#pragma unroll
+  for (int a = 0; a < OCN_MAX_NA; ++a) acc[a] = make_double2(0.0, 0.0);
+
+  for (int n0 = 0; n0 < nb; n0 += G1_N) {
+    const int nn = min(G1_N, nb - n0);
+    __syncthreads();
+    // stage u[s][x0..x0+127][k][n0..n0+nn): each warp walks x rows, lanes along n
+    for (int s = 0; s < nspn; ++s)
+      for (int e = tx; e < G1_X * G1_N; e += G1_X) {
+        const int xl = e / G1_N, nl = e % G1_N;
+        double2 v = make_double2(0.0, 0.0);
+        if (x0 + xl < nx && nl < nn)
+          v = u[(((size_t)s * nx + (x0 + xl)) * nk + k) * nb + n0 + nl];
+        us[(s * G1_N + nl) * (G1_X + 1) + xl] = v;
+      }
+    for (int e = tx; e < na * G1_N; e += G1_X) {
+      const int a = e / G1_N, nl = e % G1_N;
+      double2 v = make_double2(0.0, 0.0);
+      if (nl < nn) {
+        const size_t idx = (size_t)n0 + nl + (size_t)nb * ((size_t)k + (size_t)nk * a);
+        const double m = allow[idx];
+        v = make_double2(pr[idx] * m, pi[idx] * m);
+      }
+      ps[a * G1_N + nl] = v;
+    }
+    __syncthreads();
+    for (int nl = 0; nl < nn; ++nl) {
+      const double2 u0 = us[nl * (G1_X + 1) + tx];
+      const double2 u1 = (nspn == 2) ? us[(G1_N + nl) * (G1_X + 1) + tx] : u0;
+#pragma unroll
+      for (int a = 0; a < OCN_MAX_NA; ++a) {
+        if (a < na) {
+          const double2 uu = (a & 1) ? u1 : u0;
+          const double2 q = ps[a * G1_N + nl];
+          acc[a].x += uu.x * q.x - uu.y * q.y;
+          acc[a].y += uu.x * q.y + uu.y * q.x;
+        }
+      }
+    }
+  }
+  if (x < nx) {
+    double2* o = phi + ((size_t)k * nx + x) * na;
+#pragma unroll
+    for (int a = 0; a < OCN_MAX_NA; ++a)
+      if (a < na) o[a] = acc[a];
+  }
+}
+
+// ------------------------------------------------ LR: k <-> R and x W(R,x)
+
+// One 1-D DFT pass along axis `ax` of every [a][k] line held in shared memory.
+__device__ void dft_axis(const double2* __restrict__ in, double2* __restrict__ out, int na, int nk,
+                         int ax, double sgn) {
+  const int n = c_kdim[ax];
+  const int st = (ax == 0) ? c_kdim[1] * c_kdim[2] : ((ax == 1) ? c_kdim[2] : 1);
+  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
+    const int a = e / nk, k = e % nk;
+    const int m = (k / st) % n;
+    const int base = k - m * st;
+    const double2* line = in + (size_t)a * nk + base;
+    double sr = 0.0, si = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const int t = (j * m) % n;
+      const double2 w = c_tw[ax][t];
+      const double wy = sgn * w.y;
+      const double2 v = line[j * st];
+      sr += v.x * w.x - v.y * wy;
+      si += v.x * wy + v.y * w.x;
+    }
+    out[e] = make_double2(sr, si);
+  }
+}
+
+// phi'(.,x,a) = FFT_fwd[ W(.,x) o FFT_bwd[ phi(.,x,a) ] ] / Nk   (long_range.f90:928-939,
+// FFTW signs +1 backward / -1 forward, Modules/FFT_wrapper.f90:24-25).  One CTA per x.
+__global__ void k_lr_fft_w_fp64(double2* __restrict__ phi, const double* __restrict__ W, int nk,
+                                int nx, int na) {
+  extern __shared__ double2 smem[];
+  double2* b0 = smem;
+  double2* b1 = smem + (size_t)na * nk;
+  const int x = blockIdx.x;
+  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
+    const int a = e / nk, k = e % nk;
+    b0[e] = phi[((size_t)k * nx + x) * na + a];
+  }
+  __syncthreads();
+  dft_axis(b0, b1, na, nk, 0, +1.0);
+  __syncthreads();
+  dft_axis(b1, b0, na, nk, 1, +1.0);
+  __syncthreads();
+  dft_axis(b0, b1, na, nk, 2, +1.0);
+  __syncthreads();
+  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
+    const double w = W[(size_t)x * nk + (e % nk)];
+    b1[e] = make_double2(b1[e].x * w, b1[e].y * w);
+  }
+  __syncthreads();
+  dft_axis(b1, b0, na, nk, 0, -1.0);
+  __syncthreads();
+  dft_axis(b0, b1, na, nk, 1, -1.0);
+  __syncthreads();
+  dft_axis(b1, b0, na, nk, 2, -1.0);
+  __syncthreads();
+  const double norm = 1.0 / (double)nk;
+  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
+    const int a = e / nk, k = e % nk;
+    phi[((size_t)k * nx + x) * na + a] = make_double2(b0[e].x * norm, b0[e].y * norm);
+  }
+}
+
+// ------------------------------------------------------ LR: x-mesh -> band
+
+// part[split][re|im][a][k][n] = - sum_{x in split} conj(u(n,k,x)) phi'(k,x,a)
+// (long_range.f90:943-961).  grid (Nk, nsplit), one thread per band.
+constexpr int G2_XC = 32;
+__global__ void k_lr_gemm2_fp64(const double2* __restrict__ u, const double2* __restrict__ phi,
+                                double* __restrict__ part, int nb, int nk, int nx, int na, int nspn,
+                                int xper, size_t npsi) {
+  __shared__ double2 fs[G2_XC * OCN_MAX_NA];
+  const int k = blockIdx.x;
+  const int split = blockIdx.y;
+  const int xa = split * xper, xb = min(nx, xa + xper);
+  const int n = threadIdx.x;
+  double2 acc[OCN_MAX_NA];
+#pragma unroll
+  for (int a = 0; a < OCN_MAX_NA; ++a) acc[a] = make_double2(0.0, 0.0);
+  for (int x0 = xa; x0 < xb; x0 += G2_XC) {
+    const int xn = min(G2_XC, xb - x0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < xn * na; e += blockDim.x)
+      fs[e] = phi[((size_t)k * nx + x0) * na + e];
+    __syncthreads();
+    if (n < nb) {
+      for (int xl = 0; xl < xn; ++xl) {
+        const double2 u0 = u[(((size_t)0 * nx + x0 + xl) * nk + k) * nb + n];
+        const double2 u1 = (nspn == 2) ? u[(((size_t)1 * nx + x0 + xl) * nk + k) * nb + n] : u0;
+#pragma unroll
+        for (int a = 0; a < OCN_MAX_NA; ++a) {
+          if (a < na) {
+            const double2 uu = (a & 1) ? u1 : u0;
+            const double2 f = fs[xl * na + a];
+            acc[a].x += uu.x * f.x + uu.y * f.y;
+            acc[a].y += uu.x * f.y - uu.y * f.x;
+          }
+        }
+      }
+    }
+  }
+  if (n < nb) {
+    double* pr = part + (size_t)split * 2 * npsi;
+    double* pim = pr + npsi;
+#pragma unroll
+    for (int a = 0; a < OCN_MAX_NA; ++a)
+      if (a < na) {
+        const size_t idx = (size_t)n + (size_t)nb * ((size_t)k + (size_t)nk * a);
+        pr[idx] = -acc[a].x;
+        pim[idx] = -acc[a].y;
+      }
+  }
+}
+
+// ----------------------------------------------------------- combination
+
+// out(n,k,ic) = E o psi (conj when backwards) + allow o (acc + sum of LR parts)
+//             + sum_jc S(ic,jc) psi(n,k,jc)        (OCEAN_action.f90:337-372,596-608)
+// Optionally fused with the first Lanczos stage (ocean_hay_ab_twoterm,
+// OCEAN_haydock.f90:848-860): out -= b_{i-1} old, partial <out|psi>.
+__global__ void k_combine(const double* __restrict__ pr, const double* __restrict__ pi,
+                          const double* __restrict__ er, const double* __restrict__ ei,
+                          const double* __restrict__ allow, const double* __restrict__ acc,
+                          const double* __restrict__ part, int nparts, const double2* __restrict__ so,
+                          double* __restrict__ outr, double* __restrict__ outi, int nbk, int na,
+                          size_t npsi, int use_e0, int use_so, int backwards,
+                          const double* __restrict__ oldr, const double* __restrict__ oldi,
+                          const double* __restrict__ bprev, double* __restrict__ red) {
+  __shared__ double sh[2][32];
+  double dr = 0.0, di = 0.0;
+  double bm = 0.0;
+  if (oldr) bm = -(*bprev);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nbk; e += gridDim.x * blockDim.x) {
+    double qr[OCN_MAX_NA], qi[OCN_MAX_NA];
+#pragma unroll
+    for (int a = 0; a < OCN_MAX_NA; ++a)
+      if (a < na) {
+        qr[a] = pr[e + (size_t)nbk * a];
+        qi[a] = pi[e + (size_t)nbk * a];
+      }
+#pragma unroll
+    for (int ic = 0; ic < OCN_MAX_NA; ++ic) {
+      if (ic >= na) break;
+      const size_t idx = e + (size_t)nbk * ic;
+      double fr = acc[idx], fi = acc[npsi + idx];
+      for (int s = 0; s < nparts; ++s) {
+        fr += part[(size_t)s * 2 * npsi + idx];
+        fi += part[(size_t)s * 2 * npsi + npsi + idx];
+      }
+      const double m = allow[idx];
+      fr *= m;
+      fi *= m;
+      if (use_so) {
+        for (int jc = 0; jc < na; ++jc) {
+          const double2 sv = so[jc * na + ic];
+          if (backwards) {
+            fr = fr + sv.x * qr[jc] + sv.y * qi[jc];
+            fi = fi + sv.x * qi[jc] - sv.y * qr[jc];
+          } else {
+            fr = fr + sv.x * qr[jc] - sv.y * qi[jc];
+            fi = fi + sv.x * qi[jc] + sv.y * qr[jc];
+          }
+        }
+      }
+      double hr = 0.0, hi = 0.0;
+      if (use_e0) {
+        const double a_ = er[idx], b_ = ei ? ei[idx] : 0.0;
+        if (backwards) {
+          hr = a_ * qr[ic] + b_ * qi[ic];
+          hi = a_ * qi[ic] - b_ * qr[ic];
+        } else {
+          hr = a_ * qr[ic] - b_ * qi[ic];
+          hi = a_ * qi[ic] + b_ * qr[ic];
+        }
+      }
+      hr += fr;
+      hi += fi;
+      if (oldr) {
+        hr += bm * oldr[idx];
+        hi += bm * oldi[idx];
+        // psi_dot(hpsi, psi): sum conj(h) psi  (OCEAN_psi.f90:2029-2034)
+        dr += hr * qr[ic] + hi * qi[ic];
+        di += hr * qi[ic] - hi * qr[ic];
+      }
+      outr[idx] = hr;
+      outi[idx] = hi;
+    }
+  }
+  if (!red) return;
+  // deterministic block reduction
+  for (int o = 16; o > 0; o >>= 1) {
+    dr += __shfl_down_sync(0xffffffffu, dr, o);
+    di += __shfl_down_sync(0xffffffffu, di, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = dr;
+    sh[1][w] = di;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+      s0 += sh[0][i];
+      s1 += sh[1][i];
+    }
+    red[2 * blockIdx.x] = s0;
+    red[2 * blockIdx.x + 1] = s1;
+  }
+}
+
+// Sum of nb partial pairs in a fixed order, done identically by every block.
+__device__ __forceinline__ void reduce_pairs(const double* __restrict__ red, int nblk, double* s0,
+                                             double* s1) {
+  __shared__ double sh[2][32];
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
+    a += red[2 * i];
+    b += red[2 * i + 1];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) {
+    sh[0][w] = a;
+    sh[1][w] = b;
+  }
+  __syncthreads();
+  double ta = 0.0, tb = 0.0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+    ta += sh[0][i];
+    tb += sh[1][i];
+  }
+  *s0 = ta;
+  *s1 = tb;
+}
+
+__device__ __forceinline__ void block_partial(double v0, double v1, double* __restrict__ red) {
+  __shared__ double sh[2][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    v0 += __shfl_down_sync(0xffffffffu, v0, o);
+    v1 += __shfl_down_sync(0xffffffffu, v1, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = v0;
+    sh[1][w] = v1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+      s0 += sh[0][i];
+      s1 += sh[1][i];
+    }
+    red[2 * blockIdx.x] = s0;
+    red[2 * blockIdx.x + 1] = s1;
+  }
+}
+
+// Lanczos stage 2: a_{i-1} = Re<h|psi>; h -= a psi; partial |h|^2.
+__global__ void k_lanczos2(const double* __restrict__ red1, int nblk, double* __restrict__ hr,
+                           double* __restrict__ hi, const double* __restrict__ pr,
+                           const double* __restrict__ pi, size_t n, double* __restrict__ red2,
+                           double* __restrict__ coef_a, double* __restrict__ coef_ia) {
+  double a, ia;
+  reduce_pairs(red1, nblk, &a, &ia);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *coef_a = a;
+    *coef_ia = ia;
+  }
+  const double am = -a;
+  double s = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double r = hr[e] + am * pr[e];
+    const double i = hi[e] + am * pi[e];
+    hr[e] = r;
+    hi[e] = i;
+    s += r * r + i * i;
+  }
+  __syncthreads();
+  block_partial(s, 0.0, red2);
+}
+
+// Lanczos stage 3: b_i = sqrt(sum); psi_new = h / b_i (in place in h).
+__global__ void k_lanczos3(const double* __restrict__ red2, int nblk, double* __restrict__ hr,
+                           double* __restrict__ hi, size_t n, double* __restrict__ coef_b) {
+  double bb, dummy;
+  reduce_pairs(red2, nblk, &bb, &dummy);
+  const double b = sqrt(bb);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *coef_b = b;
+  const double inv = 1.0 / b;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    hr[e] *= inv;
+    hi[e] *= inv;
+  }
+}
+
+// ---------------------------------------------------------------- multiplet
+
+// amp_part[chunk][p][a] = sum_{e in chunk} (allow o psi)(e,a) * mpc_s(p)(e), e = (n,k)
+// (OCEAN_multiplet.f90:1730-1783).  One warp per projector at a time.
+__global__ void k_mult_amp(const double* __restrict__ pr, const double* __restrict__ pi,
+                           const double* __restrict__ allow, const double2* __restrict__ mpc,
+                           double2* __restrict__ amp_part, int nbk, int np, int na, int nspn,
+                           int chunk) {
+  extern __shared__ double2 qs[];  // [a][chunk]
+  const int c0 = blockIdx.x * chunk;
+  const int cn = min(chunk, nbk - c0);
+  for (int e = threadIdx.x; e < na * chunk; e += blockDim.x) {
+    const int a = e / chunk, j = e % chunk;
+    double2 v = make_double2(0.0, 0.0);
+    if (j < cn) {
+      const size_t idx = (size_t)c0 + j + (size_t)nbk * a;
+      const double m = allow[idx];
+      v = make_double2(pr[idx] * m, pi[idx] * m);
+    }
+    qs[e] = v;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int p = warp; p < np; p += nw) {
+    double2 s[OCN_MAX_NA];
+#pragma unroll
+    for (int a = 0; a < OCN_MAX_NA; ++a) s[a] = make_double2(0.0, 0.0);
+    for (int j = lane; j < cn; j += 32) {
+      const double2 m0 = mpc[((size_t)0 * np + p) * nbk + c0 + j];
+      const double2 m1 = (nspn == 2) ? mpc[((size_t)1 * np + p) * nbk + c0 + j] : m0;
+#pragma unroll
+      for (int a = 0; a < OCN_MAX_NA; ++a)
+        if (a < na) {
+          const double2 m = ((a & 1) && nspn == 2) ? m1 : m0;
+          const double2 q = qs[a * chunk + j];
+          s[a].x += q.x * m.x - q.y * m.y;
+          s[a].y += q.x * m.y + q.y * m.x;
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < OCN_MAX_NA; ++a) {
+      if (a >= na) break;
+      for (int o = 16; o > 0; o >>= 1) {
+        s[a].x += __shfl_down_sync(0xffffffffu, s[a].x, o);
+        s[a].y += __shfl_down_sync(0xffffffffu, s[a].y, o);
+      }
+      if (lane == 0) amp_part[((size_t)blockIdx.x * np + p) * na + a] = s[a];
+    }
+  }
+}
+
+__global__ void k_mult_amp_reduce(const double2* __restrict__ part, double2* __restrict__ amp,
+                                  int nchunk, int npa) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npa) return;
+  double2 s = make_double2(0.0, 0.0);
+  for (int c = 0; c < nchunk; ++c) {
+    const double2 v = part[(size_t)c * npa + i];
+    s.x += v.x;
+    s.y += v.y;
+  }
+  amp[i] = s;
+}
+
+// hamp(p,a) = mul * ( -sum_nu' mpm(nu,nu',l) amp((nu',m,l),a)
+//                     + sum_jj MH_l(ii(nu,m,a), jj) pw_l(jj) )
+// (OCEAN_multiplet.f90:1819-1936).  One warp per (p, a).
+__global__ void k_mult_hamp(const double2* __restrict__ amp, double2* __restrict__ hamp,
+                            const int* __restrict__ pl, const int* __restrict__ pm,
+                            const int* __restrict__ pnu, const int* __restrict__ pfirst,
+                            const double* __restrict__ mpm, const double2* __restrict__ mh,
+                            const long long* __restrict__ jbeg, const int* __restrict__ nprojv,
+                            int np, int na, int lmin, int npmax, double mul) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= np * na) return;
+  const int p = gw / na, a = gw % na;
+  const int l = pl[p], m = pm[p], nu = pnu[p];
+  const int li = l - lmin;
+  const int npl = nprojv[li];
+  const int first = pfirst[li];  // first projector index of block l (m = -l, nu = 0)
+  double2 s = make_double2(0.0, 0.0);
+  // direct term
+  for (int nup = lane; nup < npl; nup += 32) {
+    const double mm = mpm[(size_t)nu + (size_t)npmax * ((size_t)nup + (size_t)npmax * li)];
+    const int q = first + (m + l) * npl + nup;
+    const double2 v = amp[(size_t)q * na + a];
+    s.x -= mm * v.x;
+    s.y -= mm * v.y;
+  }
+  // exchange term: pw_l(jj), jj = nu' + (m'+l) npl + a' (2l+1) npl
+  const int mham = na * (2 * l + 1) * npl;
+  const int ii = nu + (m + l) * npl + a * (2 * l + 1) * npl;
+  const double2* row = mh + jbeg[li] + (size_t)ii * mham;
+  for (int jj = lane; jj < mham; jj += 32) {
+    const int nup = jj % npl;
+    const int mp = (jj / npl) % (2 * l + 1);
+    const int ap = jj / (npl * (2 * l + 1));
+    const int q = first + mp * npl + nup;
+    const double2 v = amp[(size_t)q * na + ap];
+    const double2 h = row[jj];
+    s.x += h.x * v.x - h.y * v.y;
+    s.y += h.x * v.y + h.y * v.x;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s.x += __shfl_down_sync(0xffffffffu, s.x, o);
+    s.y += __shfl_down_sync(0xffffffffu, s.y, o);
+  }
+  if (lane == 0) hamp[(size_t)p * na + a] = make_double2(s.x * mul, s.y * mul);
+}
+
+// acc(e,a) += sum_p conj(mpc_s(p)(e)) hamp(p,a)   (OCEAN_multiplet.f90:1943-1998)
+__global__ void k_mult_back(const double2* __restrict__ mpc, const double2* __restrict__ hamp,
+                            double* __restrict__ acc, int nbk, int np, int na, int nspn,
+                            size_t npsi) {
+  extern __shared__ double2 hs[];  // [p][a]
+  for (int i = threadIdx.x; i < np * na; i += blockDim.x) hs[i] = hamp[i];
+  __syncthreads();
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nbk) return;
+  double2 s[OCN_MAX_NA];
+#pragma unroll
+  for (int a = 0; a < OCN_MAX_NA; ++a) s[a] = make_double2(0.0, 0.0);
+  for (int p = 0; p < np; ++p) {
+    const double2 m0 = mpc[((size_t)0 * np + p) * nbk + e];
+    const double2 m1 = (nspn == 2) ? mpc[((size_t)1 * np + p) * nbk + e] : m0;
+#pragma unroll
+    for (int a = 0; a < OCN_MAX_NA; ++a)
+      if (a < na) {
+        const double2 m = ((a & 1) && nspn == 2) ? m1 : m0;
+        const double2 h = hs[p * na + a];
+        s[a].x += m.x * h.x + m.y * h.y;
+        s[a].y += m.x * h.y - m.y * h.x;
+      }
+  }
+#pragma unroll
+  for (int a = 0; a < OCN_MAX_NA; ++a)
+    if (a < na) {
+      acc[e + (size_t)nbk * a] += s[a].x;
+      acc[npsi + e + (size_t)nbk * a] += s[a].y;
+    }
+}
+
+// ------------------------------------------------------------ BLAS-1 (GMRES)
+
+// y = (rv + i iv) x - y   (OCEAN_psi_axmy, OCEAN_psi.f90:1515-1522)
+__global__ void k_axmy(const double* __restrict__ x, double* __restrict__ y, size_t n, double rv,
+                       double iv) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double xr = x[e], xi = x[n + e];
+    const double br = rv * xr - y[e];
+    const double bi = rv * xi - y[n + e];
+    y[e] = br - iv * xi;
+    y[n + e] = bi + iv * xr;
+  }
+}
+// y = x - z
+__global__ void k_axmz(const double* __restrict__ x, double* __restrict__ y,
+                       const double* __restrict__ z, size_t n2) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n2;
+       e += (size_t)gridDim.x * blockDim.x)
+    y[e] = x[e] - z[e];
+}
+// y += (ar + i ai) x
+__global__ void k_axpy(double ar, double ai, const double* __restrict__ x, double* __restrict__ y,
+                       size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double xr = x[e], xi = x[n + e];
+    y[e] += ar * xr - ai * xi;
+    y[n + e] += ar * xi + ai * xr;
+  }
+}
+// z = x o y (complex)
+__global__ void k_cmul(const double* __restrict__ x, const double* __restrict__ y,
+                       double* __restrict__ z, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double a = x[e], b = x[n + e], c = y[e], d = y[n + e];
+    z[e] = a * c - b * d;
+    z[n + e] = a * d + b * c;
+  }
+}
+// pcdiv = (E - (h_r + i(h_i + g))) / ((E - h)^2 + g^2)  (OCEAN_psi.f90:2961-2965)
+__global__ void k_set_prec(double energy, double gprc, const double* __restrict__ h,
+                           double* __restrict__ out, size_t n) {
+  const double g2 = gprc * gprc;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double hr = h[e], hi = h[n + e];
+    const double er = energy - hr, ei = -hi;
+    const double dr = er * er - ei * ei + g2, di = 2.0 * er * ei;
+    const double nr = energy - hr, ni = -(hi + gprc);
+    const double den = dr * dr + di * di;
+    out[e] = (nr * dr + ni * di) / den;
+    out[n + e] = (ni * dr - nr * di) / den;
+  }
+}
+__global__ void k_mask_copy(const double* __restrict__ in, const double* __restrict__ allow,
+                            double* __restrict__ out, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double m = allow[e];
+    out[e] = m * in[e];
+    out[n + e] = m * in[n + e];
+  }
+}
+__global__ void k_fill(double* __restrict__ x, size_t n, double vr, double vi) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    x[e] = vr;
+    x[n + e] = vi;
+  }
+}
+// partial <p|q> = sum conj(p) q
+__global__ void k_dot(const double* __restrict__ p, const double* __restrict__ q, size_t n,
+                      double* __restrict__ red) {
+  double a = 0.0, b = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double pr = p[e], pi = p[n + e], qr = q[e], qi = q[n + e];
+    a += pr * qr + pi * qi;
+    b += pr * qi - pi * qr;
+  }
+  block_partial(a, b, red);
+}
+__global__ void k_reduce_final(const double* __restrict__ red, int nblk, double* __restrict__ out) {
+  double a, b;
+  reduce_pairs(red, nblk, &a, &b);
+  if (threadIdx.x == 0) {
+    out[0] = a;
+    out[1] = b;
+  }
+}
+
+// Gram row of update_gmres (OCEAN_gmres.f90:270-283) in one pass:
+// part[blk][j] = { <au_cur|au_j> (re, im), <au_j|g> (re, im) } for j < nvec.
+__global__ void k_multidot(const double* const* __restrict__ vecs, int nvec,
+                           const double* __restrict__ au_cur, const double* __restrict__ g,
+                           size_t n, double* __restrict__ part) {
+  __shared__ double sh[4][32];
+  for (int j = 0; j < nvec; ++j) {
+    const double* v = vecs[j];
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+         e += (size_t)gridDim.x * blockDim.x) {
+      const double cr = au_cur[e], ci = au_cur[n + e];
+      const double vr = v[e], vi = v[n + e];
+      const double gr = g[e], gi = g[n + e];
+      s0 += cr * vr + ci * vi;
+      s1 += cr * vi - ci * vr;
+      s2 += vr * gr + vi * gi;
+      s3 += vr * gi - vi * gr;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s0 += __shfl_down_sync(0xffffffffu, s0, o);
+      s1 += __shfl_down_sync(0xffffffffu, s1, o);
+      s2 += __shfl_down_sync(0xffffffffu, s2, o);
+      s3 += __shfl_down_sync(0xffffffffu, s3, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) {
+      sh[0][w] = s0;
+      sh[1][w] = s1;
+      sh[2][w] = s2;
+      sh[3][w] = s3;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t[4] = {0, 0, 0, 0};
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i)
+        for (int c = 0; c < 4; ++c) t[c] += sh[c][i];
+      for (int c = 0; c < 4; ++c) part[((size_t)blockIdx.x * nvec + j) * 4 + c] = t[c];
+    }
+  }
+}
+__global__ void k_multidot_reduce(const double* __restrict__ part, int nblk, int nvec,
+                                  double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvec * 4) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += part[(size_t)b * nvec * 4 + i];
+  out[i] = s;
+}
+// x += sum_j c_j u_j, ax += sum_j c_j au_j   (OCEAN_gmres.f90:336-341, in j order)
+__global__ void k_update(int nvec, const double2* __restrict__ coef, const double* const* __restrict__ ul,
+                         const double* const* __restrict__ aul, double* __restrict__ x,
+                         double* __restrict__ ax, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    double xr = x[e], xi = x[n + e], yr = ax[e], yi = ax[n + e];
+    for (int j = 0; j < nvec; ++j) {
+      const double2 c = coef[j];
+      const double* u = ul[j];
+      const double* au = aul[j];
+      const double ur = u[e], ui = u[n + e], vr = au[e], vi = au[n + e];
+      xr += c.x * ur - c.y * ui;
+      xi += c.x * ui + c.y * ur;
+      yr += c.x * vr - c.y * vi;
+      yi += c.x * vi + c.y * vr;
+    }
+    x[e] = xr;
+    x[n + e] = xi;
+    ax[e] = yr;
+    ax[n + e] = yi;
+  }
+}
+
+inline int grid_for(size_t n, int block, int cap) {
+  size_t g = (n + block - 1) / block;
+  if (g > (size_t)cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+}  // namespace
+
+// ======================================================================= host
+
+int upload_twiddles(ocn_ctx* c) {
+  double2 tw[3][OCN_MAX_KDIM];
+  const double pi = 3.1415926535897932384626433832795;
+  for (int a = 0; a < 3; ++a) {
+    const int n = c->dims.kmesh[a];
+    for (int t = 0; t < OCN_MAX_KDIM; ++t) {
+      if (t < n) {
+        const double ang = 2.0 * pi * (double)t / (double)n;
+        tw[a][t] = make_double2(cos(ang), sin(ang));
+      } else {
+        tw[a][t] = make_double2(0.0, 0.0);
+      }
+    }
+  }
+  OCN_CUDA(c, cudaMemcpyToSymbolAsync(c_tw, tw, sizeof(tw), 0, cudaMemcpyHostToDevice, c->stream));
+  OCN_CUDA(c, cudaMemcpyToSymbolAsync(c_kdim, c->dims.kmesh, sizeof(int) * 3, 0,
+                                      cudaMemcpyHostToDevice, c->stream));
+  return OCN_OK;
+}
+
+int kernels_init(ocn_ctx* c) {
+  const size_t g1 = sizeof(double2) * ((size_t)c->nspn * G1_N * (G1_X + 1) + (size_t)c->na * G1_N);
+  OCN_CUDA(c, cudaFuncSetAttribute(k_lr_gemm1_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g1));
+  const size_t ff = sizeof(double2) * 2 * (size_t)c->na * c->nk;
+  OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff));
+  const size_t ma = sizeof(double2) * (size_t)c->na * 256;
+  OCN_CUDA(c, cudaFuncSetAttribute(k_mult_amp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ma));
+  return OCN_OK;
+}
+
+int phase_bloch(ocn_ctx* c, const double* d_ur, const double* d_ui, const double* d_cos,
+                const double* d_sin) {
+  const long long total = (long long)c->nb * c->nk * c->nx * c->nspn;
+  k_phase_bloch<<<grid_for((size_t)total, 256, 8 * c->sm_count), 256, 0, c->stream>>>(
+      d_ur, d_ui, d_cos, d_sin, c->d_u, total, c->nb, c->nk, c->nx);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
+int zero_acc(ocn_ctx* c) {
+  OCN_CUDA(c, cudaMemsetAsync(c->d_acc, 0, sizeof(double) * 2 * c->npsi, c->stream));
+  return OCN_OK;
+}
+
+int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi) {
+  const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na;
+  {
+    const size_t sm = sizeof(double2) * ((size_t)c->nspn * G1_N * (G1_X + 1) + (size_t)na * G1_N);
+    dim3 grid((nx + G1_X - 1) / G1_X, nk);
+    TimedScope ts(c, T_LR_GEMM1);
+    k_lr_gemm1_fp64<<<grid, G1_X, sm, c->stream>>>(c->d_u, d_pr, d_pi, c->d_allow, c->d_phi, nb, nk,
+                                                   nx, na, c->nspn);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  {
+    const size_t sm = sizeof(double2) * 2 * (size_t)na * nk;
+    TimedScope ts(c, T_LR_FFT);
+    k_lr_fft_w_fp64<<<nx, 256, sm, c->stream>>>(c->d_phi, c->d_W, nk, nx, na);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  {
+    const int xs = c->lr_xsplit;
+    const int xper = (nx + xs - 1) / xs;
+    const int block = ((nb + 31) / 32) * 32;
+    dim3 grid(nk, xs);
+    TimedScope ts(c, T_LR_GEMM2);
+    k_lr_gemm2_fp64<<<grid, block, 0, c->stream>>>(c->d_u, c->d_phi, c->d_accpart, nb, nk, nx, na,
+                                                   c->nspn, xper, c->npsi);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  return OCN_OK;
+}
+
+int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi) {
+  MultDev& m = c->mult;
+  TimedScope ts(c, T_MULT);
+  const int nbk = c->nb * c->nk;
+  const int chunk = 256;
+  const int nchunk = (nbk + chunk - 1) / chunk;
+  {
+    const size_t sm = sizeof(double2) * (size_t)c->na * chunk;
+    k_mult_amp<<<nchunk, 256, sm, c->stream>>>(d_pr, d_pi, c->d_allow, m.mpc, m.amp_part, nbk, m.np,
+                                              c->na, c->nspn, chunk);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  const int npa = m.np * c->na;
+  k_mult_amp_reduce<<<(npa + 127) / 128, 128, 0, c->stream>>>(m.amp_part, m.amp, nchunk, npa);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  {
+    const double mul = c->sys.interaction_scale / ((double)c->nk * c->sys.celvol);
+    const int warps = npa;
+    const int threads = 256;
+    const int blocks = (warps * 32 + threads - 1) / threads;
+    k_mult_hamp<<<blocks, threads, 0, c->stream>>>(m.amp, m.hamp, m.p_l, m.p_m, m.p_nu, m.d_pfirst,
+                                                  m.mpm, m.mh, m.d_jbeg, m.d_nproj, m.np, c->na,
+                                                  m.lmin, m.npmax, mul);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  {
+    const size_t sm = sizeof(double2) * (size_t)npa;
+    const int block = 64;
+    k_mult_back<<<(nbk + block - 1) / block, block, sm, c->stream>>>(m.mpc, m.hamp, c->d_acc, nbk,
+                                                                    m.np, c->na, c->nspn, c->npsi);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  return OCN_OK;
+}
+
+int combine(ocn_ctx* c, const double* d_pr, const double* d_pi, double* d_or, double* d_oi,
+            const int* hflag, int backwards) {
+  const int nbk = c->nb * c->nk;
+  const int use_so = (c->sys.mult && hflag[5] == 1 && c->have_so) ? 1 : 0;
+  const int nparts = (c->sys.long_range && hflag[0] == 1) ? c->lr_xsplit : 0;
+  const int lr_mixed = (c->dims.precision == OCN_PREC_MIXED) ? 1 : 0;
+  k_combine<<<grid_for(nbk, 256, 4 * c->sm_count), 256, 0, c->stream>>>(
+      d_pr, d_pi, c->d_er, c->d_ei, c->d_allow, c->d_acc, c->d_accpart, lr_mixed ? 0 : nparts,
+      c->d_so, d_or, d_oi, nbk, c->na, c->npsi, c->sys.e0, use_so, backwards, nullptr, nullptr,
+      nullptr, nullptr);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
+// The Lanczos step is launched from ocn_solvers.cu through this helper, which
+// knows the coefficient array layout.
+int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const double* psi_r,
+                   const double* psi_i, double* h_r, double* h_i, const double* bprev,
+                   double* a_out, double* ia_out, double* b_out) {
+  const int nbk = c->nb * c->nk;
+  const int* hf = c->sys.nhflag;
+  const int use_so = (c->sys.mult && hf[5] == 1 && c->have_so) ? 1 : 0;
+  const int nparts = (c->sys.long_range && hf[0] == 1) ? c->lr_xsplit : 0;
+  const int lr_mixed = (c->dims.precision == OCN_PREC_MIXED) ? 1 : 0;
+  const int nblk = c->red_blocks;
+  TimedScope ts(c, T_LANCZOS);
+  k_combine<<<nblk, 256, 0, c->stream>>>(psi_r, psi_i, c->d_er, c->d_ei, c->d_allow, c->d_acc,
+                                         c->d_accpart, lr_mixed ? 0 : nparts, c->d_so, h_r, h_i, nbk,
+                                         c->na, c->npsi, c->sys.e0, use_so, 0, old_r, old_i, bprev,
+                                         c->d_red);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  k_lanczos2<<<nblk, 256, 0, c->stream>>>(c->d_red, nblk, h_r, h_i, psi_r, psi_i, c->npsi,
+                                          c->d_red + 2 * nblk, a_out, ia_out);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  k_lanczos3<<<nblk, 256, 0, c->stream>>>(c->d_red + 2 * nblk, nblk, h_r, h_i, c->npsi, b_out);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
+int vec_axmy(ocn_ctx* c, const double* x, double* y, double rv, double iv) {
+  k_axmy<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(x, y, c->npsi, rv, iv);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+int vec_axmz(ocn_ctx* c, const double* x, double* y, const double* z) {
+  k_axmz<<<grid_for(2 * c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(x, y, z, 2 * c->npsi);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+int vec_axpy(ocn_ctx* c, double ar, double ai, const double* x, double* y) {
+  k_axpy<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(ar, ai, x, y, c->npsi);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+int vec_mul(ocn_ctx* c, const double* x, const double* y, double* z) {
+  k_cmul<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(x, y, z, c->npsi);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+int vec_set_prec(ocn_ctx* c, double energy, double gprc, const double* h, double* out) {
+  k_set_prec<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(energy, gprc, h, out,
+                                                                              c->npsi);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+int vec_mask_copy(ocn_ctx* c, const double* in, double* out) {
+  k_mask_copy<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(in, c->d_allow, out,
+                                                                               c->npsi);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+int vec_fill(ocn_ctx* c, double* x, double vr, double vi) {
+  k_fill<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(x, c->npsi, vr, vi);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+// Device-resident <p|q>; result pair written to d_out (2 doubles).
+int vec_dot_dev(ocn_ctx* c, const double* p, const double* q, double* d_out) {
+  const int nblk = c->red_blocks;
+  k_dot<<<nblk, 256, 0, c->stream>>>(p, q, c->npsi, c->d_red);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  k_reduce_final<<<1, 256, 0, c->stream>>>(c->d_red, nblk, d_out);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+int vec_multidot_dev(ocn_ctx* c, const double* const* d_vecs, int nvec, const double* au_cur,
+                     const double* g, double* d_part, double* d_out) {
+  const int nblk = c->red_blocks;
+  k_multidot<<<nblk, 256, 0, c->stream>>>(d_vecs, nvec, au_cur, g, c->npsi, d_part);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  k_multidot_reduce<<<(nvec * 4 + 127) / 128, 128, 0, c->stream>>>(d_part, nblk, nvec, d_out);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+int vec_update_dev(ocn_ctx* c, int nvec, const double2* d_coef, const double* const* d_ul,
+                   const double* const* d_aul, double* x, double* ax) {
+  k_update<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(nvec, d_coef, d_ul, d_aul,
+                                                                            x, ax, c->npsi);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
+}  // namespace ocn

@@ -1,0 +1,227 @@
+"""Seeded synthetic workloads for the OCEAN core-level BSE hot path.
+
+The reference ships none of the pipeline files its BSE solver reads (u2.dat,
+rpottrim.*, wvfcninfo, cks*, Slater files), so these generators stand in for
+them with the shapes and value distributions of the five benchmark cases:
+
+  c1  cubic a = 4.0 A, k-mesh 4^3, 32 bands, x-mesh 8^3, 1s edge (Na = 4)
+  c2  k-mesh 8^3, 100 bands, x-mesh 12^3, 1s edge
+  c3  2p edge with multiplets and spin-orbit (Na = 12), k-mesh 6^3, 64 bands,
+      x-mesh 10^3, projectors l = 0..3 x 8 radial
+  c4  uneven batched instances (k-mesh from {4^3,5^3,6^3,8^3}, 24..128 bands)
+  c5  c2 sizes for the adjoint-gradient study
+
+Value recipe (identical bytes are fed to the oracle and the GPU library):
+  * band energies  U(0, 30) eV sorted per k, converted to Hartree, Sigma'' = 0
+  * allow mask     1
+  * u2 per k       QR-orthonormalised complex Gaussian (Nx x Nb), raw (before the
+                   core-hole phase of OCEAN_bloch_lrLOAD)
+  * W(r)           rpottrim-style table of 64 samples of erf(r/0.5 A)/(eps r),
+                   eps = 4, on 0..10 Bohr; beyond the table lr_populate_W2 uses
+                   1/(eps r) itself.  The table is positive: long_range.f90:943-961
+                   subtracts conj(u) phi, which supplies the attraction.
+  * psi0           complex Gaussian normalised by core_pnorm (kpref returned)
+
+Everything is in Hartree / Bohr, the units ocean.x works in.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+# OCEAN2/OCEAN_constants.f90:15-20
+EV2HARTREE = 0.036749322175666
+HARTREE2EV = 27.211386245980
+BOHR = 0.529177210544  # Angstrom per Bohr
+
+
+@dataclass
+class Workload:
+    name: str
+    nb: int
+    kmesh: tuple
+    xmesh: tuple
+    na: int
+    nspn: int
+    core_l: int
+    celvol: float
+    avec: np.ndarray            # (9,) Fortran avec(3,3), Bohr
+    tau: np.ndarray             # (3,)
+    epsilon0: float
+    interaction_scale: float
+    rtab: np.ndarray
+    ptab: np.ndarray
+    er: np.ndarray              # (Nb*Nk*Na,) Fortran order
+    ei: np.ndarray
+    allow: np.ndarray
+    ur: np.ndarray              # raw u2 (Nb*Nk*Nx*nspn,)
+    ui: np.ndarray
+    psi_r: np.ndarray           # normalised psi0
+    psi_i: np.ndarray
+    kpref: float
+    # Haydock / spectrum settings
+    niter: int = 200
+    gam0: float = 0.5 * EV2HARTREE
+    ne: int = 2000
+    el: float = -10.0 * EV2HARTREE
+    eh: float = 40.0 * EV2HARTREE
+    # GMRES settings
+    gmres_nomega: int = 0
+    gmres_tol: float = 1e-6
+    gmres_depth: int = 80
+    gmres_gprc: float = 0.5
+    # multiplet / spin-orbit (None when off)
+    mult: Optional[dict] = None
+    so_xi: float = 0.0
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nk(self) -> int:
+        return int(np.prod(self.kmesh))
+
+    @property
+    def nx(self) -> int:
+        return int(np.prod(self.xmesh))
+
+    @property
+    def npsi(self) -> int:
+        return self.nb * self.nk * self.na
+
+
+def w_table(epsilon0: float = 4.0, width_angstrom: float = 0.5, nptab: int = 64,
+            rmax_bohr: float = 10.0):
+    """rpottrim-style table of the screened core-hole potential erf(r/a)/(eps r)."""
+    a = width_angstrom / BOHR
+    rtab = np.linspace(0.0, rmax_bohr, nptab)
+    ptab = np.empty_like(rtab)
+    for i, r in enumerate(rtab):
+        if r == 0.0:
+            ptab[i] = 2.0 / (a * math.sqrt(math.pi) * epsilon0)
+        else:
+            ptab[i] = math.erf(r / a) / (epsilon0 * r)
+    return rtab, ptab
+
+
+def pnorm(psi_r: np.ndarray, psi_i: np.ndarray, nkpts: int, celvol: float):
+    """core_pnorm (OCEAN_psi.f90:5589-5638): normalise and return kpref."""
+    val = math.sqrt(float(np.sum(psi_r * psi_r + psi_i * psi_i)))
+    kpref = 4.0 * math.pi * val * val / (nkpts * celvol * celvol)
+    return psi_r / val, psi_i / val, kpref
+
+
+def _orthonormal_u2(rng, nk: int, nx: int, nb: int, nspn: int):
+    """u2 per k = Q of a QR of an (Nx x Nb) complex Gaussian; returns Fortran
+    (Nb, Nk, Nx, nspn) planes flattened."""
+    ur = np.empty((nspn, nx, nk, nb), dtype=np.float64)
+    ui = np.empty_like(ur)
+    for s in range(nspn):
+        chunk = 64
+        for k0 in range(0, nk, chunk):
+            k1 = min(nk, k0 + chunk)
+            g = rng.standard_normal((k1 - k0, nx, nb)) + 1j * rng.standard_normal((k1 - k0, nx, nb))
+            q, _ = np.linalg.qr(g)
+            # q[k, x, n] -> u(n, k, x)
+            ur[s, :, k0:k1, :] = np.transpose(q.real, (1, 0, 2))
+            ui[s, :, k0:k1, :] = np.transpose(q.imag, (1, 0, 2))
+    return ur.reshape(-1), ui.reshape(-1)
+
+
+def make(name: str, seed: int = 0, nb: Optional[int] = None, kmesh=None, xmesh=None,
+         core_l: Optional[int] = None, with_mult: Optional[bool] = None) -> Workload:
+    """Build a named workload: 'c1', 'c2', 'c3', 'c5', or 'tiny' (test sizes)."""
+    presets = {
+        "tiny": dict(nb=8, kmesh=(2, 2, 2), xmesh=(3, 3, 3), core_l=0, mult=False, niter=24),
+        "small": dict(nb=12, kmesh=(3, 2, 2), xmesh=(4, 3, 2), core_l=0, mult=False, niter=40),
+        "c1": dict(nb=32, kmesh=(4, 4, 4), xmesh=(8, 8, 8), core_l=0, mult=False, niter=200),
+        "c2": dict(nb=100, kmesh=(8, 8, 8), xmesh=(12, 12, 12), core_l=0, mult=False, niter=1000,
+                   gmres_nomega=200),
+        "c3": dict(nb=64, kmesh=(6, 6, 6), xmesh=(10, 10, 10), core_l=1, mult=True, niter=200),
+        "c3small": dict(nb=16, kmesh=(2, 2, 3), xmesh=(4, 4, 4), core_l=1, mult=True, niter=40),
+        "c5": dict(nb=100, kmesh=(8, 8, 8), xmesh=(12, 12, 12), core_l=0, mult=False, niter=1000,
+                   gmres_nomega=400),
+    }
+    if name not in presets:
+        raise ValueError(f"unknown workload {name!r}")
+    p = dict(presets[name])
+    if nb is not None:
+        p["nb"] = nb
+    if kmesh is not None:
+        p["kmesh"] = tuple(kmesh)
+    if xmesh is not None:
+        p["xmesh"] = tuple(xmesh)
+    if core_l is not None:
+        p["core_l"] = core_l
+    if with_mult is not None:
+        p["mult"] = with_mult
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nbv, km, xm, lc = p["nb"], tuple(p["kmesh"]), tuple(p["xmesh"]), p["core_l"]
+    na = 4 * (2 * lc + 1)
+    nspn = 1
+    nk, nx = int(np.prod(km)), int(np.prod(xm))
+    a_bohr = 4.0 / BOHR
+    avec = np.zeros(9)
+    avec[0] = avec[4] = avec[8] = a_bohr
+    celvol = a_bohr ** 3
+    eps0 = 4.0
+    rtab, ptab = w_table(eps0)
+
+    # energies: U(0,30) eV sorted per k, (Nb, Nk) -> stubby to (Nb, Nk, Na)
+    e = np.sort(rng.uniform(0.0, 30.0, size=(nk, nbv)), axis=1) * EV2HARTREE
+    er = np.broadcast_to(e[None, :, :], (na, nk, nbv)).reshape(-1).copy()
+    ei = np.zeros_like(er)
+    allow = np.ones_like(er)
+
+    ur, ui = _orthonormal_u2(rng, nk, nx, nbv, nspn)
+
+    g_r = rng.standard_normal(na * nk * nbv)
+    g_i = rng.standard_normal(na * nk * nbv)
+    psi_r, psi_i, kpref = pnorm(g_r, g_i, nk, celvol)
+
+    w = Workload(name=name, nb=nbv, kmesh=km, xmesh=xm, na=na, nspn=nspn, core_l=lc,
+                 celvol=celvol, avec=avec, tau=np.zeros(3), epsilon0=eps0,
+                 interaction_scale=1.0, rtab=rtab, ptab=ptab, er=er, ei=ei, allow=allow,
+                 ur=ur, ui=ui, psi_r=psi_r, psi_i=psi_i, kpref=kpref, niter=p["niter"],
+                 gmres_nomega=p.get("gmres_nomega", 0))
+
+    if p["mult"]:
+        lmin, lmax, nproj = 0, 3, [8, 8, 8, 8]
+        if name == "c3small":
+            nproj = [2, 2, 2, 2]
+        npmax = max(nproj)
+        nl = lmax - lmin + 1
+        shape = (nspn, nl, 2 * lmax + 1, npmax, nk, nbv)  # C order of Fortran mpc
+        scale = 1.0 / math.sqrt(nbv * nk)
+        mpcr = rng.standard_normal(shape) * scale
+        mpci = rng.standard_normal(shape) * scale
+        # zero the unused (m, nu) slots so both sides see identical padding
+        for li, l in enumerate(range(lmin, lmax + 1)):
+            for mi in range(2 * lmax + 1):
+                m = mi - lmax
+                if abs(m) > l:
+                    mpcr[:, li, mi] = 0.0
+                    mpci[:, li, mi] = 0.0
+            mpcr[:, li, :, nproj[li]:] = 0.0
+            mpci[:, li, :, nproj[li]:] = 0.0
+        mpm = np.zeros((nl, npmax, npmax))
+        for li in range(nl):
+            npl = nproj[li]
+            f = rng.uniform(0.5, 8.0, size=(npl, npl))
+            mpm[li, :npl, :npl] = 0.5 * (f + f.T) * EV2HARTREE
+        mh_r, mh_i = [], []
+        for li, l in enumerate(range(lmin, lmax + 1)):
+            mham = na * (2 * l + 1) * nproj[li]
+            gmat = (rng.uniform(0.5, 8.0, size=(mham, mham)) *
+                    np.exp(2j * math.pi * rng.uniform(size=(mham, mham))))
+            h = 0.5 * (gmat + gmat.conj().T) * EV2HARTREE / math.sqrt(mham)
+            # row ii contiguous: C order of an (ii, jj) array
+            mh_r.append(h.real.reshape(-1))
+            mh_i.append(h.imag.reshape(-1))
+        w.mult = dict(lmin=lmin, lmax=lmax, nproj=np.array(nproj, dtype=np.int32), npmax=npmax,
+                      mpcr=mpcr.reshape(-1), mpci=mpci.reshape(-1),
+                      mpm=mpm.reshape(-1), mhr=np.concatenate(mh_r), mhi=np.concatenate(mh_i))
+        w.so_xi = 5.0 * EV2HARTREE
+    return w

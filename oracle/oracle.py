@@ -1,0 +1,225 @@
+"""ctypes bindings of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+cpu_baseline / reference legs of bench.py as the checker and the CPU baseline.
+The product package (ocean_gb300) never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+DP = C.POINTER(C.c_double)
+IP = C.POINTER(C.c_int)
+
+
+class OrDims(C.Structure):
+    _fields_ = [("nb", C.c_int), ("kmesh", C.c_int * 3), ("xmesh", C.c_int * 3), ("na", C.c_int),
+                ("nspn", C.c_int), ("core_l", C.c_int)]
+
+
+class OrOps(C.Structure):
+    _fields_ = [("er", DP), ("ei", DP), ("allow", DP), ("ur", DP), ("ui", DP), ("W", DP),
+                ("somelr", DP), ("someli", DP), ("lmin", C.c_int), ("lmax", C.c_int),
+                ("npmax", C.c_int), ("nproj", IP), ("mpcr", DP), ("mpci", DP), ("mpm", DP),
+                ("mhr", DP), ("mhi", DP), ("celvol", C.c_double),
+                ("interaction_scale", C.c_double), ("e0", C.c_int), ("long_range", C.c_int),
+                ("mult", C.c_int), ("nhflag", C.c_int * 6), ("nthreads", C.c_int)]
+
+
+class OrLrIn(C.Structure):
+    _fields_ = [("avec", C.c_double * 9), ("tau", C.c_double * 3), ("epsilon0", C.c_double),
+                ("interaction_scale", C.c_double), ("nptab", C.c_int), ("rtab", DP), ("ptab", DP),
+                ("isolated", C.c_int), ("iso_cut", C.c_double), ("pbc", C.c_int * 3),
+                ("have_eps3d", C.c_int), ("epsilon3d", C.c_double * 3),
+                ("xshift_override", C.c_int * 3)]
+
+
+def build(force: bool = False) -> str:
+    path = os.path.join(_HERE, "liboracle.so")
+    src = os.path.join(_HERE, "ocean_oracle.cpp")
+    if force or not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        subprocess.check_call(["make", "-s", "-C", _HERE, "liboracle.so"])
+    return path
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = C.CDLL(build())
+        L = _LIB
+        L.or_intval.restype = C.c_double
+        L.or_pnorm.restype = C.c_double
+        L.or_gamfcn.restype = C.c_double
+    return _LIB
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(DP)
+
+
+def iptr(a: np.ndarray):
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(IP)
+
+
+def dims_of(w) -> OrDims:
+    d = OrDims()
+    d.nb = w.nb
+    d.kmesh[:] = list(w.kmesh)
+    d.xmesh[:] = list(w.xmesh)
+    d.na = w.na
+    d.nspn = w.nspn
+    d.core_l = w.core_l
+    return d
+
+
+def lr_in_of(w) -> OrLrIn:
+    p = OrLrIn()
+    p.avec[:] = list(w.avec)
+    p.tau[:] = list(w.tau)
+    p.epsilon0 = w.epsilon0
+    p.interaction_scale = w.interaction_scale
+    p.nptab = len(w.rtab)
+    p.rtab = dptr(w.rtab)
+    p.ptab = dptr(w.ptab)
+    p.isolated = 0
+    p.iso_cut = 0.0
+    p.pbc[:] = [0, 0, 0]
+    p.have_eps3d = 0
+    p.epsilon3d[:] = [1.0, 1.0, 1.0]
+    p.xshift_override[:] = [1, 1, 1]
+    return p
+
+
+class OracleProblem:
+    """Operator data of one workload, set up by the oracle's own lrLOAD + W2."""
+
+    def __init__(self, w, nthreads: int = 0, hflag=(1, 1, 1, 1, 1, 1)):
+        L = lib()
+        self.w = w
+        # keep every array whose address is handed to the C side alive
+        self._refs = [w.er, w.ei, w.allow, w.rtab, w.ptab]
+        if w.mult is not None:
+            self._refs += list(w.mult.values())
+        self.d = dims_of(w)
+        self.ur = w.ur.copy()
+        self.ui = w.ui.copy()
+        tau = (C.c_double * 3)(*list(w.tau))
+        ovr = (C.c_int * 3)(1, 1, 1)
+        xs = (C.c_int * 3)()
+        L.or_lrload(C.byref(self.d), tau, ovr, xs, dptr(self.ur), dptr(self.ui))
+        self.xshift = tuple(xs)
+        self.tau_shifted = tuple(tau)
+        self.lr = lr_in_of(w)
+        self.W = np.zeros(w.nk * w.nx)
+        L.or_populate_w2(C.byref(self.d), C.byref(self.lr), tau, xs, dptr(self.W))
+        o = OrOps()
+        o.er = dptr(w.er)
+        o.ei = dptr(w.ei)
+        o.allow = dptr(w.allow)
+        o.ur = dptr(self.ur)
+        o.ui = dptr(self.ui)
+        o.W = dptr(self.W)
+        o.celvol = w.celvol
+        o.interaction_scale = w.interaction_scale
+        o.e0 = 1
+        o.long_range = 1
+        o.mult = 1 if w.mult is not None else 0
+        o.nhflag[:] = list(hflag)
+        o.nthreads = nthreads
+        self._keep = []
+        if w.mult is not None:
+            m = w.mult
+            o.lmin, o.lmax, o.npmax = m["lmin"], m["lmax"], m["npmax"]
+            o.nproj = iptr(m["nproj"])
+            o.mpcr, o.mpci = dptr(m["mpcr"]), dptr(m["mpci"])
+            o.mpm, o.mhr, o.mhi = dptr(m["mpm"]), dptr(m["mhr"]), dptr(m["mhi"])
+            self.somelr = np.zeros(w.na * w.na)
+            self.someli = np.zeros(w.na * w.na)
+            L.or_soprep(w.core_l, C.c_double(w.so_xi), dptr(self.somelr), dptr(self.someli))
+            o.somelr, o.someli = dptr(self.somelr), dptr(self.someli)
+        self.o = o
+
+    def xact(self, pr, pi, hflag=None, backwards=False):
+        out_r = np.zeros(self.w.npsi)
+        out_i = np.zeros(self.w.npsi)
+        hf = None if hflag is None else (C.c_int * 6)(*hflag)
+        lib().or_xact(C.byref(self.d), C.byref(self.o), dptr(np.ascontiguousarray(pr)),
+                      dptr(np.ascontiguousarray(pi)), dptr(out_r), dptr(out_i), hf,
+                      int(bool(backwards)))
+        return out_r, out_i
+
+    def haydock(self, niter, pr=None, pi=None):
+        w = self.w
+        pr = w.psi_r if pr is None else pr
+        pi = w.psi_i if pi is None else pi
+        ra = np.zeros(niter + 1)
+        ia = np.zeros(niter + 1)
+        rb = np.zeros(niter + 1)
+        done = C.c_int(0)
+        rc = lib().or_haydock(C.byref(self.d), C.byref(self.o), dptr(pr), dptr(pi), niter,
+                              dptr(ra), dptr(ia), dptr(rb), C.byref(done))
+        return rc, ra, ia, rb, done.value
+
+    def gmres(self, energies_ev, depth=80, gres=None, gprc=None, ffff=1e-6, max_restarts=50):
+        w = self.w
+        e = np.ascontiguousarray(energies_ev, dtype=np.float64)
+        n = len(e)
+        gres = w.gam0 if gres is None else gres
+        gprc = w.gmres_gprc if gprc is None else gprc
+        ore, oim, rel = np.zeros(n), np.zeros(n), np.zeros(n)
+        its = np.zeros(n, dtype=np.int32)
+        tot = C.c_int(0)
+        rc = lib().or_gmres(C.byref(self.d), C.byref(self.o), dptr(w.psi_r), dptr(w.psi_i),
+                            C.c_double(w.kpref), dptr(e), n, depth, C.c_double(gres),
+                            C.c_double(gprc), C.c_double(ffff), max_restarts, dptr(ore), dptr(oim),
+                            dptr(rel), iptr(its), C.byref(tot))
+        return rc, ore, oim, rel, its, tot.value
+
+
+def write_core(ra, ia, rb, it, kpref, el, eh, ne, gam0, ebase=0.0, gam_gauss=0.0, ucvol=1.0,
+               old_broaden=0, nval=0.0, eps=1.0):
+    out = np.zeros((ne + 1) * 9)
+    ia_p = None if ia is None else dptr(np.ascontiguousarray(ia, dtype=np.float64))
+    lib().or_write_core(dptr(np.ascontiguousarray(ra, dtype=np.float64)), ia_p,
+                        dptr(np.ascontiguousarray(rb, dtype=np.float64)), it, C.c_double(kpref),
+                        C.c_double(el), C.c_double(eh), ne, C.c_double(gam0), C.c_double(ebase),
+                        C.c_double(gam_gauss), C.c_double(ucvol), old_broaden, C.c_double(nval),
+                        C.c_double(eps), dptr(out))
+    return out.reshape(ne + 1, 9)
+
+
+def redtrid(n, ra, rb):
+    w = np.zeros(n + 1)
+    rc = lib().or_redtrid(n, dptr(np.ascontiguousarray(ra, dtype=np.float64)),
+                          dptr(np.ascontiguousarray(rb, dtype=np.float64)), dptr(w))
+    return rc, w
+
+
+def fft3d(kmesh, re, im, sign):
+    re = np.ascontiguousarray(re, dtype=np.float64).copy()
+    im = np.ascontiguousarray(im, dtype=np.float64).copy()
+    km = (C.c_int * 3)(*kmesh)
+    lib().or_fft3d(km, dptr(re), dptr(im), sign)
+    return re, im
+
+
+def zhptrf_solve(ap: np.ndarray, b: np.ndarray):
+    """Factor packed-upper Hermitian ap (complex, n(n+1)/2) and solve for b."""
+    n = len(b)
+    apc = np.ascontiguousarray(ap, dtype=np.complex128).copy()
+    ipiv = np.zeros(n, dtype=np.int32)
+    info = lib().or_zhptrf_u(n, apc.view(np.float64).ctypes.data_as(DP), iptr(ipiv))
+    x = np.ascontiguousarray(b, dtype=np.complex128).copy()
+    if info == 0:
+        lib().or_zhptrs_u(n, apc.view(np.float64).ctypes.data_as(DP), iptr(ipiv),
+                          x.view(np.float64).ctypes.data_as(DP))
+    return info, ipiv, x

@@ -1,0 +1,189 @@
+"""GPU parity tests: libocean_gpu.so (through its C ABI) against the CPU oracle
+on the same seeded inputs.
+
+Tolerances
+  * index bookkeeping (xshift, W, phased u2): bit-exact
+  * FP64 action H*psi:      ||dH|| / ||H psi|| < 1e-12
+  * FP64 Lanczos:           first 10 a_n, b_n relative < 1e-12
+  * continued fraction:     GPU vs oracle < 1e-12 relative; vs golden file 6e-8
+  * GMRES (FP64):           eps2 within 1e-8 relative of the oracle's
+"""
+import os
+
+import numpy as np
+import pytest
+
+from ocean_gb300 import capi
+from ocean_gb300 import workloads as WL
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def built(lib_built, oracle_lib):
+    return capi.load(lib_built), oracle_lib
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+PROBLEMS = {}
+
+
+def problem(name, O, seed=0, **kw):
+    key = (name, seed, tuple(sorted(kw.items())))
+    if key not in PROBLEMS:
+        w = WL.make(name, seed=seed, **kw)
+        PROBLEMS[key] = (w, O.OracleProblem(w))
+    return PROBLEMS[key]
+
+
+@pytest.mark.parametrize("name", ["tiny", "c1"])
+def test_bloch_phase_and_W_bit_exact(built, name):
+    _, O = built
+    w, P = problem(name, O)
+    ctx = capi.Context(w)
+    try:
+        ur, ui = ctx.get_bloch()
+        W, xs, tau = ctx.get_W()
+    finally:
+        ctx.close()
+    assert xs == P.xshift and tau == P.tau_shifted
+    assert np.array_equal(W, P.W)
+    assert np.array_equal(ur, P.ur) and np.array_equal(ui, P.ui)
+
+
+@pytest.mark.parametrize("name", ["tiny", "small", "c1", "c3small"])
+def test_apply_H_fp64_matches_oracle(built, name):
+    _, O = built
+    w, P = problem(name, O, seed=4)
+    ctx = capi.Context(w)
+    try:
+        rng = np.random.default_rng(11)
+        for trial in range(2):
+            pr, pi = rng.standard_normal(w.npsi), rng.standard_normal(w.npsi)
+            hr, hi = ctx.apply_H(pr, pi)
+            orr, oi = P.xact(pr, pi)
+            assert _rel(hr + 1j * hi, orr + 1j * oi) < 1e-12
+        assert ctx.launches > 0
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("hflag", [(0, 1, 1, 1, 1, 1), (1, 1, 1, 1, 0, 1), (1, 1, 1, 1, 1, 0),
+                                   (0, 1, 1, 1, 0, 0)])
+@pytest.mark.parametrize("backwards", [False, True])
+def test_apply_H_term_switches(built, hflag, backwards):
+    _, O = built
+    w = WL.make("c3small", seed=5)
+    w.ei = np.linspace(0.0, 0.01, w.npsi)  # complex energies exercise the backwards conjugate
+    P = O.OracleProblem(w)
+    ctx = capi.Context(w)
+    try:
+        hr, hi = ctx.apply_H(w.psi_r, w.psi_i, hflag=hflag, backwards=backwards)
+        orr, oi = P.xact(w.psi_r, w.psi_i, hflag=hflag, backwards=backwards)
+        assert _rel(hr + 1j * hi, orr + 1j * oi) < 1e-12
+    finally:
+        ctx.close()
+
+
+def test_apply_H_hermitian_on_gpu(built):
+    _, O = built
+    w, _ = problem("c3small", O, seed=6)
+    ctx = capi.Context(w)
+    try:
+        rng = np.random.default_rng(2)
+        a = rng.standard_normal(w.npsi) + 1j * rng.standard_normal(w.npsi)
+        b = rng.standard_normal(w.npsi) + 1j * rng.standard_normal(w.npsi)
+        ha = np.array(ctx.apply_H(a.real.copy(), a.imag.copy()))
+        hb = np.array(ctx.apply_H(b.real.copy(), b.imag.copy()))
+        ha = ha[0] + 1j * ha[1]
+        hb = hb[0] + 1j * hb[1]
+        assert abs(np.vdot(b, ha) - np.vdot(hb, a)) < 1e-12 * abs(np.vdot(b, ha))
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("name,niter", [("small", 30), ("c1", 60), ("c3small", 30)])
+def test_haydock_fp64_matches_oracle(built, name, niter):
+    _, O = built
+    w, P = problem(name, O, seed=7)
+    ctx = capi.Context(w)
+    try:
+        ra, ia, rb, done = ctx.haydock(niter)
+    finally:
+        ctx.close()
+    rc, ora, oia, orb, odone = P.haydock(niter)
+    assert rc == 0 and done == odone == niter
+    assert np.max(np.abs(ra[:10] - ora[:10]) / np.abs(ora[:10])) < 1e-12
+    assert np.max(np.abs(rb[1:11] - orb[1:11]) / np.abs(orb[1:11])) < 1e-12
+    assert np.max(np.abs(ia[:niter])) < 1e-12
+    # spectra from both coefficient sets
+    sg = capi.spectrum_cf(ra, ia, rb, niter, w.kpref, w.el, w.eh, 400, w.gam0)
+    so = O.write_core(ora, oia, orb, niter, w.kpref, w.el, w.eh, 400, w.gam0)
+    assert _rel(sg[:, 2], so[:, 2]) < 1e-9
+
+
+def test_haydock_nan_returns_reference_ierr(built):
+    _, O = built
+    w, _ = problem("tiny", O, seed=8)
+    ctx = capi.Context(w)
+    try:
+        pr = w.psi_r.copy()
+        pr[0] = np.nan
+        with pytest.raises(capi.OcnError) as ei:
+            ctx.haydock(4, pr, w.psi_i)
+        assert ei.value.code == -1
+        # the context stays usable after the error
+        ra, ia, rb, done = ctx.haydock(4)
+        assert done == 4 and np.all(np.isfinite(ra[:4]))
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("photon", [1, 5])
+def test_spectrum_cf_reproduces_reference_golden(built, photon):
+    _, O = built
+    d = np.load(os.path.join(ROOT, "tests", "golden", "cu_twophoton_kat.npz"))
+    p = f"p{photon}"
+    n = int(d[p + "_n"])
+    args = (d[p + "_real_a"], None, d[p + "_real_b"], n, float(d[p + "_kpref"]),
+            -30.0 * WL.EV2HARTREE, 70.0 * WL.EV2HARTREE, 5000, 1.245 * WL.EV2HARTREE)
+    g = capi.spectrum_cf(*args, ucvol=float(d[p + "_vol"]))
+    o = O.write_core(*args, 0.0, 0.0, float(d[p + "_vol"]))
+    assert np.max(np.abs(g - o) / np.maximum(np.abs(o), 1e-300)) < 1e-12
+    ref = d[p + "_spct"]
+    got = g[d[p + "_rows"]]
+    nz = ref != 0
+    assert np.max(np.abs(got[nz] - ref[nz]) / np.abs(ref[nz])) < 6e-8
+
+
+def test_spectrum_voigt_matches_oracle(built):
+    _, O = built
+    d = np.load(os.path.join(ROOT, "tests", "golden", "cu_twophoton_kat.npz"))
+    n = int(d["p3_n"])
+    args = (d["p3_real_a"], None, d["p3_real_b"], n, float(d["p3_kpref"]),
+            -30.0 * WL.EV2HARTREE, 70.0 * WL.EV2HARTREE, 500, 1.245 * WL.EV2HARTREE)
+    gg = 0.8 * WL.EV2HARTREE
+    g = capi.spectrum_cf(*args, gam_gauss=gg, nval=0.05, eps=4.0)
+    o = O.write_core(*args, 0.0, gg, 1.0, 0, 0.05, 4.0)
+    assert np.max(np.abs(g[:, :5] - o[:, :5]) / np.maximum(np.abs(o[:, :5]), 1e-300)) < 1e-9
+
+
+@pytest.mark.parametrize("name", ["tiny", "small"])
+def test_gmres_fp64_matches_oracle(built, name):
+    _, O = built
+    w, P = problem(name, O, seed=9)
+    E = np.array([4.0, 4.1, 4.2, 4.3, 8.0, 8.05])
+    ctx = capi.Context(w)
+    try:
+        ore, oim, rel, its = ctx.gmres(E, depth=16, tol=1e-20, max_restarts=500)
+    finally:
+        ctx.close()
+    rc, ore2, oim2, rel2, its2, tot = P.gmres(E, depth=16, ffff=1e-20, max_restarts=500)
+    assert rc == 0
+    assert np.max(np.abs(oim - oim2) / np.abs(oim2)) < 1e-8
+    assert np.max(np.abs(ore - ore2) / np.abs(ore2)) < 1e-8

@@ -1,0 +1,181 @@
+"""CPU tests of the oracle: pinned against the reference's golden vectors where
+they exist (continued fraction, tridiagonal eigenvalues) and against
+structural properties and numpy/scipy elsewhere."""
+import os
+
+import numpy as np
+import pytest
+
+from ocean_gb300 import workloads as WL
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "cu_twophoton_kat.npz")
+
+
+@pytest.fixture(scope="module")
+def kat():
+    return np.load(GOLD)
+
+
+@pytest.mark.parametrize("photon", range(1, 8))
+def test_write_core_matches_reference_golden(oracle_lib, kat, photon):
+    """write_core (OCEAN_haydock.f90:1801-1894) reproduces absspct_Cu.0001_1s_0P
+    from abslanc_Cu.0001_1s_0P to the 8 significant digits the file holds."""
+    O = oracle_lib
+    p = f"p{photon}"
+    n = int(kat[p + "_n"])
+    ne = int(kat["ne"])
+    out = O.write_core(kat[p + "_real_a"], None, kat[p + "_real_b"], n, float(kat[p + "_kpref"]),
+                       float(kat["el_ev"]) * WL.EV2HARTREE, float(kat["eh_ev"]) * WL.EV2HARTREE, ne,
+                       float(kat["gam0_ev"]) * WL.EV2HARTREE, 0.0, 0.0, float(kat[p + "_vol"]))
+    assert out.shape[0] == int(kat[p + "_nrows"])
+    got = out[kat[p + "_rows"]]
+    ref = kat[p + "_spct"]
+    # E15.8 keeps 8 significant digits: half a unit in the last place is <= 5e-8
+    nz = ref != 0.0
+    rel = np.abs(got[nz] - ref[nz]) / np.abs(ref[nz])
+    assert rel.max() < 6e-8, rel.max()
+    assert np.abs(got[~nz]).max(initial=0.0) < 1e-12  # the 0 eV row: energy and sigma vanish
+
+
+def test_single_precision_cmplx_is_needed(oracle_lib, kat):
+    """The golden spectra carry the binary32 rounding of Fortran cmplx() without
+    KIND; an all-FP64 recurrence misses them by far more than print precision."""
+    ra, rb = kat["p1_real_a"], kat["p1_real_b"]
+    n = int(kat["p1_n"])
+    kp = float(kat["p1_kpref"])
+    gam = float(kat["gam0_ev"]) * WL.EV2HARTREE
+    rows = kat["p1_rows"][::7]
+    ref = kat["p1_spct"][::7, 2]
+    worst = 0.0
+    for r, s in zip(rows, ref):
+        e = -30.0 * WL.EV2HARTREE + 100.0 * WL.EV2HARTREE * (2 * r) / 10000.0
+        ct = complex(e - ra[n - 1], gam)
+        disc = np.sqrt(ct * ct - 4 * rb[n] ** 2)
+        d = (ct + disc) / 2 if disc.imag > 0 else (ct - disc) / 2
+        for j in range(n - 1, -1, -1):
+            d = complex(e - ra[j], gam) - rb[j + 1] ** 2 / d
+        val = kp * abs(d.imag) / abs(d) ** 2
+        worst = max(worst, abs(val - s) / abs(s))
+    assert worst > 1.5e-7
+
+
+@pytest.mark.parametrize("photon", [1, 4, 7])
+def test_redtrid_matches_reference_golden(oracle_lib, kat, photon):
+    p = f"p{photon}"
+    n = int(kat[p + "_n"])
+    rc, w = oracle_lib.redtrid(n, kat[p + "_real_a"], kat[p + "_real_b"])
+    assert rc == 0
+    assert np.abs(w - kat[p + "_eig"]).max() < 6e-11  # printed with 10 decimals
+
+
+@pytest.mark.parametrize("kmesh", [(2, 2, 2), (4, 4, 4), (3, 5, 2), (6, 1, 4), (5, 5, 5)])
+@pytest.mark.parametrize("sign", [1, -1])
+def test_fft_matches_numpy(oracle_lib, kmesh, sign):
+    rng = np.random.default_rng(1)
+    nk = int(np.prod(kmesh))
+    x = rng.standard_normal(nk) + 1j * rng.standard_normal(nk)
+    r, i = oracle_lib.fft3d(kmesh, x.real, x.imag, sign)
+    a = x.reshape(kmesh)  # k3 fastest = C order of (k1, k2, k3)
+    ref = (np.fft.ifftn(a) * nk) if sign > 0 else np.fft.fftn(a)
+    assert np.allclose(r + 1j * i, ref.reshape(-1), rtol=0, atol=1e-12 * nk)
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 17, 40])
+def test_zhptrf_zhptrs_match_scipy(oracle_lib, n):
+    sl = pytest.importorskip("scipy.linalg")
+    rng = np.random.default_rng(n)
+    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    h = a + a.conj().T  # Hermitian indefinite: exercises 2x2 pivots
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ap = np.array([h[i, j] for j in range(n) for i in range(j + 1)])
+    info, ipiv, x = oracle_lib.zhptrf_solve(ap, b)
+    assert info == 0
+    assert np.allclose(h @ x, b, atol=1e-9 * np.abs(b).max() * max(1, np.linalg.cond(h)) ** 0.5)
+    lu, piv, info2 = sl.lapack.zhetrf(h, lower=0)
+    assert info2 == 0
+    if n < 32:  # LAPACK's unblocked path: identical pivot choices
+        assert list(ipiv) == list(piv)
+
+
+@pytest.fixture(scope="module")
+def tiny_problem(oracle_lib):
+    w = WL.make("tiny", seed=1)
+    return w, oracle_lib.OracleProblem(w)
+
+
+def _dense(P, n):
+    H = np.zeros((n, n), complex)
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = 1.0
+        r, i = P.xact(e, np.zeros(n))
+        H[:, j] = r + 1j * i
+    return H
+
+
+def test_action_is_hermitian(tiny_problem):
+    w, P = tiny_problem
+    H = _dense(P, w.npsi)
+    assert np.abs(H - H.conj().T).max() < 1e-14 * np.abs(H).max()
+
+
+def test_action_terms_recombine(tiny_problem):
+    """E o psi + LR part: hflag off for LR leaves exactly E o psi."""
+    w, P = tiny_problem
+    r, i = P.xact(w.psi_r, w.psi_i, hflag=(0, 1, 1, 1, 1, 1))
+    assert np.allclose(r + 1j * i, w.er * (w.psi_r + 1j * w.psi_i), atol=1e-15)
+
+
+def test_multiplet_action_hermitian(oracle_lib):
+    w = WL.make("c3small", seed=2)
+    P = oracle_lib.OracleProblem(w)
+    H = _dense(P, w.npsi)
+    assert np.abs(H - H.conj().T).max() < 1e-13 * np.abs(H).max()
+    # the multiplet + spin-orbit terms are active: switching them off changes H
+    r, i = P.xact(w.psi_r, w.psi_i, hflag=(1, 1, 1, 1, 0, 0))
+    r2, i2 = P.xact(w.psi_r, w.psi_i)
+    assert np.abs((r - r2) + 1j * (i - i2)).max() > 1e-6
+
+
+def test_lanczos_ritz_values_bracket_spectrum(tiny_problem):
+    w, P = tiny_problem
+    H = _dense(P, w.npsi)
+    ev = np.linalg.eigvalsh(0.5 * (H + H.conj().T))
+    rc, ra, ia, rb, done = P.haydock(w.npsi - 1)
+    assert rc == 0 and done == w.npsi - 1
+    psi = w.psi_r + 1j * w.psi_i
+    assert abs(ra[0] - np.vdot(psi, H @ psi).real) < 1e-14
+    T = np.diag(ra[:done]) + np.diag(rb[1:done], 1) + np.diag(rb[1:done], -1)
+    rit = np.linalg.eigvalsh(T)
+    assert rit[0] >= ev[0] - 1e-10 and rit[-1] <= ev[-1] + 1e-10
+    assert abs(rit[0] - ev[0]) < 1e-3 and abs(rit[-1] - ev[-1]) < 1e-3
+
+
+def test_haydock_nan_sets_ierr(tiny_problem):
+    w, P = tiny_problem
+    pr = w.psi_r.copy()
+    pr[3] = np.nan
+    rc, ra, ia, rb, done = P.haydock(5, pr, w.psi_i)
+    assert rc == -1 and done == 1
+
+
+def test_gmres_matches_direct_solve(tiny_problem):
+    w, P = tiny_problem
+    H = _dense(P, w.npsi)
+    E = np.array([5.0, 5.1, 5.2, 9.0])
+    rc, ore, oim, rel, its, tot = P.gmres(E, depth=20, ffff=1e-14)
+    assert rc == 0
+    rhs = w.allow * (w.psi_r + 1j * w.psi_i)
+    for k, e in enumerate(E):
+        z = e * WL.EV2HARTREE + 1j * w.gam0
+        x = np.linalg.solve(z * np.eye(w.npsi) - H, rhs)
+        ex = -np.vdot(rhs, x).imag * w.kpref
+        assert abs(oim[k] - ex) < 1e-5 * abs(ex)
+        assert its[k] >= 0
+
+
+def test_pnorm_kpref():
+    w = WL.make("tiny", seed=3)
+    val = 1.0  # psi already normalised
+    assert abs(np.sum(w.psi_r ** 2 + w.psi_i ** 2) - 1.0) < 1e-12
+    assert w.kpref > 0 and val == 1.0
