@@ -41,12 +41,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default=os.environ.get("OCN_BENCH_PRECISION", "fp64"),
+    ap.add_argument("--precision", default=os.environ.get("OCN_BENCH_PRECISION", "mixed"),
                     choices=["fp64", "mixed"])
     ap.add_argument("--niter", type=int, default=1000)
     ap.add_argument("--ne", type=int, default=2000)
     ap.add_argument("--workload", default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-compare", action="store_true")
     return ap.parse_args()
 
 
@@ -208,6 +209,24 @@ def run_reference(args, ws, rank, pg):
     print(json.dumps(line), flush=True)
 
 
+def _device_steps(ctx, w, niter, ne, pr_ptr, pi_ptr, steps, stream, torch):
+    """steps full Haydock runs (+ spectra) with psi0 in HBM; CUDA-event ms on the
+    library's stream."""
+    from ocean_gb300 import capi
+
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    last = None
+    for _ in range(steps):
+        ra, ia, rb, done = ctx.haydock_dev(niter, pr_ptr, pi_ptr)
+        last = capi.spectrum_cf(ra, ia, rb, done, w.kpref, w.el, w.eh, ne, w.gam0)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ev1.synchronize()
+    return ev0.elapsed_time(ev1), last
+
+
 def run_ours(args, ws, rank, local, pg):
     import torch
 
@@ -217,27 +236,22 @@ def run_ours(args, ws, rank, local, pg):
 
     B.build()
     torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
     prec = capi.OCN_PREC_FP64 if args.precision == "fp64" else capi.OCN_PREC_MIXED
     w = WL.make(args.workload, seed=rank)
     ctx = capi.Context(w, precision=prec, device=local)
     niter, ne = args.niter, args.ne
     n = w.npsi
-    d_psi = torch.empty(2 * n, dtype=torch.float64, device=f"cuda:{local}")
+    d_psi = torch.empty(2 * n, dtype=torch.float64, device=dev)
     d_psi[:n].copy_(torch.from_numpy(w.psi_r))
     d_psi[n:].copy_(torch.from_numpy(w.psi_i))
     torch.cuda.synchronize()
     pr_ptr = d_psi.data_ptr()
     pi_ptr = pr_ptr + 8 * n
-    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
 
-    def step_dev():
-        ra, ia, rb, done = ctx.haydock_dev(niter, pr_ptr, pi_ptr)
-        s = capi.spectrum_cf(ra, ia, rb, done, w.kpref, w.el, w.eh, ne, w.gam0)
-        return ra, rb, s
-
-    for _ in range(args.warmup):
-        step_dev()
-    # ---- timed region (device-resident inputs)
+    _device_steps(ctx, w, niter, ne, pr_ptr, pi_ptr, args.warmup, stream, torch)
+    # ---- timed region (inputs resident in HBM)
     ctx.timing(True)
     ctx.timing_reset()
     if pg is not None:
@@ -246,24 +260,15 @@ def run_ours(args, ws, rank, local, pg):
     sampler = ClockSampler(local)
     sampler.start()
     l0 = ctx.launches
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    last = None
-    for _ in range(args.steps):
-        last = step_dev()
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    ev1.synchronize()
+    dev_ms, spec_main = _device_steps(ctx, w, niter, ne, pr_ptr, pi_ptr, args.steps, stream, torch)
     if pg is not None:
         pg.barrier()
     clocks = sampler.stop()
     launches = ctx.launches - l0
-    dev_ms = ev0.elapsed_time(ev1)
     kt = ctx.timing_read()
     ctx.timing(False)
     if pg is not None:
-        t = torch.tensor([dev_ms], device=f"cuda:{local}")
+        t = torch.tensor([dev_ms], device=dev)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         dev_ms = float(t.item())
     total_hpsi = niter * args.steps * ws
@@ -289,17 +294,30 @@ def run_ours(args, ws, rank, local, pg):
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
     if pg is not None:
-        t = torch.tensor([e2e_ms], device=f"cuda:{local}")
+        t = torch.tensor([e2e_ms], device=dev)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         e2e_ms = float(t.item())
     e2e_value = total_hpsi / (e2e_ms / 1000.0)
+    ctx.close()
 
     if rank != 0:
-        ctx.close()
         return
+    # ---- the project's own FP64 GPU path on the same input: speed and the
+    #      spectral error of the mixed path against it (column Spect(0))
+    fp64 = None
+    if prec == capi.OCN_PREC_MIXED and not args.no_fp64_compare:
+        c64 = capi.Context(w, precision=capi.OCN_PREC_FP64, device=local)
+        s64 = torch.cuda.ExternalStream(c64.stream, device=dev)
+        c64.haydock_dev(50, pr_ptr, pi_ptr)
+        ms64, spec64 = _device_steps(c64, w, niter, ne, pr_ptr, pi_ptr, 1, s64, torch)
+        c64.close()
+        err = float(np.linalg.norm(spec_main[:, 2] - spec64[:, 2]) / np.linalg.norm(spec64[:, 2]))
+        fp64 = {"value": niter / (ms64 / 1000.0), "unit": UNIT, "ms_per_step": ms64,
+                "spectral_error_mixed_vs_fp64": err,
+                "speedup_mixed_vs_fp64": value / ws / (niter / (ms64 / 1000.0))}
     # dominant kernel and its roofline
     hbm, bf16, src = measured_peaks()
-    lr_classes = {k: v for k, v in kt.items() if v[0] > 0 and k.startswith("lr_")}
+    lr_classes = {k: v for k, v in kt.items() if v[0] > 0 and k.startswith("lr_") and k != "lr_prep"}
     dom = max(lr_classes, key=lambda k: lr_classes[k][1]) if lr_classes else None
     roof = None
     if dom:
@@ -308,33 +326,32 @@ def run_ours(args, ws, rank, local, pg):
         bytes_pl = algorithmic_bytes(w, dom, args.precision)
         achieved = bytes_pl / per_launch_s / 1e9
         tr = traffic_summary().get(f"{dom}:{args.precision}:{args.workload}")
+        total_ms = sum(x[1] for x in kt.values())
         roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "peak_source": f"{src} hbm_gbs",
+                "frac": achieved / hbm, "peak_source": f"{src} hbm_gbs (copy bandwidth)",
                 "traffic": tr, "algorithmic_bytes_per_launch": bytes_pl,
                 "avg_launch_ms": ms / cnt,
-                "kernel_share": {k: round(v[1] / max(1e-9, sum(x[1] for x in kt.values())), 4)
-                                 for k, v in kt.items() if v[0] > 0}}
+                "kernel_share": {k: round(v[1] / max(1e-9, total_ms), 4) for k, v in kt.items() if v[0] > 0}}
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(w)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "bf16x2-split/f32/f64",
+            "dtype": "f64" if args.precision == "fp64" else "bf16x2-split+f32 (contractions), f64 (vectors)",
             "data": "synthetic (seeded; u2 QR-orthonormal complex Gaussian, U(0,30) eV bands, "
                     "erf(r/0.5A)/(4r) W table)",
             "config": {"workload": f"{args.workload}: Nk=512 (8^3), Nb=100, Nx=1728 (12^3), Na=4, "
                                    f"{niter} Lanczos iterations + {ne + 1}-point spectrum per step",
                        "precision": args.precision, "parallelism": f"replicas x{ws}",
-                       "l2": "inputs larger than L2 (u2 %.2f GB)" % (
+                       "l2": "inputs larger than L2 (u2 %.2f GB per contraction operand)" % (
                            w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
             "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
-            "roofline": roof, "cpu_baseline": cpu,
+            "fp64_gpu": fp64, "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
                     "d2h_bytes_per_step": 3 * (niter + 1) * 8 + (ne + 1) * 9 * 8},
             "gpu_launches": launches, "clocks": clocks, "kernel_ms": kt}
     print(json.dumps(line), flush=True)
-    ctx.close()
 
 
 def main():

@@ -518,6 +518,7 @@ int ocn_apply_H(ocn_ctx* c, const double* ir, const double* ii, double* orr, dou
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   cudaFree(buf);
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_apply_H");
+  if (rc == OCN_OK && c->mixed) rc = mixed_check(c);
   return rc;
 }
 
@@ -575,6 +576,7 @@ int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter,
   cudaFree(coef);
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock");
   if (rc) return rc;
+  if (c->mixed && (rc = mixed_check(c))) return rc;
   for (int i = 0; i <= niter; ++i) {
     real_a[i] = host[i];
     if (imag_a) imag_a[i] = host[(niter + 1) + i];
@@ -876,6 +878,7 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
   e = cudaStreamSynchronize(c->stream);
   cleanup();
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_gmres");
+  if (rc == OCN_OK && c->mixed) rc = mixed_check(c);
   return rc;
 }
 

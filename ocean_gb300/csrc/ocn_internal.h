@@ -183,6 +183,7 @@ int cf_eval(const double* ra, const double* ia, const double* rb, int iter, doub
 int mixed_init(ocn_ctx* c);
 int mixed_free(ocn_ctx* c);
 int mixed_set_bloch(ocn_ctx* c);   // builds split-BF16 layouts from d_u
-int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi);  // adds into d_acc
+int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi);  // writes d_accpart
+int mixed_check(ocn_ctx* c);       // reads and clears the device timeout flag
 
 }  // namespace ocn

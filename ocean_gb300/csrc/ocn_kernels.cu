@@ -849,9 +849,8 @@ int combine(ocn_ctx* c, const double* d_pr, const double* d_pi, double* d_or, do
   const int nbk = c->nb * c->nk;
   const int use_so = (c->sys.mult && hflag[5] == 1 && c->have_so) ? 1 : 0;
   const int nparts = (c->sys.long_range && hflag[0] == 1) ? c->lr_xsplit : 0;
-  const int lr_mixed = (c->dims.precision == OCN_PREC_MIXED) ? 1 : 0;
   k_combine<<<grid_for(nbk, 256, 4 * c->sm_count), 256, 0, c->stream>>>(
-      d_pr, d_pi, c->d_er, c->d_ei, c->d_allow, c->d_acc, c->d_accpart, lr_mixed ? 0 : nparts,
+      d_pr, d_pi, c->d_er, c->d_ei, c->d_allow, c->d_acc, c->d_accpart, nparts,
       c->d_so, d_or, d_oi, nbk, c->na, c->npsi, c->sys.e0, use_so, backwards, nullptr, nullptr,
       nullptr, nullptr);
   ++c->launches;
@@ -868,11 +867,10 @@ int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const d
   const int* hf = c->sys.nhflag;
   const int use_so = (c->sys.mult && hf[5] == 1 && c->have_so) ? 1 : 0;
   const int nparts = (c->sys.long_range && hf[0] == 1) ? c->lr_xsplit : 0;
-  const int lr_mixed = (c->dims.precision == OCN_PREC_MIXED) ? 1 : 0;
   const int nblk = c->red_blocks;
   TimedScope ts(c, T_LANCZOS);
   k_combine<<<nblk, 256, 0, c->stream>>>(psi_r, psi_i, c->d_er, c->d_ei, c->d_allow, c->d_acc,
-                                         c->d_accpart, lr_mixed ? 0 : nparts, c->d_so, h_r, h_i, nbk,
+                                         c->d_accpart, nparts, c->d_so, h_r, h_i, nbk,
                                          c->na, c->npsi, c->sys.e0, use_so, 0, old_r, old_i, bprev,
                                          c->d_red);
   ++c->launches;

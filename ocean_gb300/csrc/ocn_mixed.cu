@@ -1,30 +1,741 @@
-// ocn_mixed.cu -- mixed-precision long-range term (split-BF16 tcgen05 u2
-// contractions, FP32 k-mesh transform).  Placeholder until the tensor-core path
-// lands: a mixed-precision context reports OCN_ERR_UNSUPPORTED instead of
-// silently running another path.
+// ocn_mixed.cu -- mixed-precision long-range term of the BSE action
+// (long_range.f90:873-963 restated for tensor cores):
+//
+//   phi(k,x,a)  = sum_n u(n,k,x) q(n,k,a),        q = allow o psi        [tcgen05, split-BF16]
+//   phi'(.,x,a) = FFT_fwd[ W(.,x) o FFT_bwd[phi(.,x,a)] ] / Nk                 [FP32, shared memory]
+//   part(n,k,a) = - sum_x conj(u(n,k,x)) phi'(k,x,a)                         [tcgen05, split-BF16]
+//
+// Split-BF16: every FP32 operand v is stored as hi = bf16(v), lo = bf16(v - hi);
+// the MMAs accumulate (A_hi + A_lo)(B_hi + B_lo) in FP32 in tensor memory, which
+// keeps ~16 significant bits of every product.
+//
+// Complex arithmetic is made real by stacking re/im along K (K = (c, n) for the
+// band contraction, K = (c, x) for the x-mesh contraction) and by the output
+// columns j = (split s, part re/im, alpha): D[:, j] + D[:, j + 2Na] is the full
+// product.  The MMA is M = 128 rows x N = 4 Na columns x K = 16 per instruction.
+//
+// Operands live in HBM as bf16 tiles read by TMA with 128-byte swizzling:
+//   UA_s [k][x][K1]  (K1 = 2 Nb)      A of the band -> x contraction, built once
+//   UB_s [k][n][K2]  (K2 = 2 Nx)      A of the x -> band contraction, built once
+//   B1   [k][j][K1]                   psi operand, rebuilt per action
+//   B2   [k][j][K2]                   phi' operand, rebuilt per action
+// The GEMM kernel is persistent and warp-specialised: warp 0 issues TMA loads,
+// warp 1 issues tcgen05.mma and owns the tensor-memory allocation, warps 2-5 drain
+// the double-buffered accumulator.  Every mbarrier wait is bounded in time; on
+// expiry the kernel records an error, drains what it issued, frees its tensor
+// memory and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <string>
+
 #include "ocn_internal.h"
 
 namespace ocn {
 
-struct MixedLR {
-  int dummy = 0;
+namespace {
+
+constexpr int TC_STAGES = 4;
+constexpr int TC_BM = 128;
+constexpr int TC_BK = 64;  // bf16 elements per 128-byte swizzle row
+constexpr int TC_THREADS = 192;
+constexpr long long TC_WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
+
+__constant__ float2 c_twf[3][OCN_MAX_KDIM];
+__constant__ int c_kdimf[3];
+
+struct TcParams {
+  int mode;      // 1: band -> x (GEMM1), 2: x -> band (GEMM2)
+  int ntiles;
+  int nb, nk, nx, na;
+  int n4;        // MMA N = 4 Na
+  int nch;       // K chunks of the full reduction
+  int nxt;       // mode 1: x tiles per k
+  int mt2, ks2, cps2;  // mode 2: M tiles, K splits, chunks per split
+  uint32_t idesc;
+  uint32_t tcols;
+  float2* phi;   // mode 1 output [k][x][a]
+  double* part;  // mode 2 output [split][re|im][npsi]
+  size_t npsi;
+  int* err;
 };
 
+__device__ __forceinline__ uint32_t su32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false when the time limit passed or another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                          long long limit) {
+  const long long t0 = clock64();
+  while (!mbar_test(bar, parity)) {
+    if (*abort_flag) return false;
+    if (clock64() - t0 > limit) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int c0,
+                                            int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// K-major operand tile with 128-byte swizzling: rows of 128 bytes, 8-row core
+// groups 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+struct TileInfo {
+  int k, row0, c0, c1, mt, sp;
+};
+
+__device__ __forceinline__ TileInfo decode(const TcParams& p, int t) {
+  TileInfo ti;
+  if (p.mode == 1) {
+    ti.k = t / p.nxt;
+    ti.row0 = (t % p.nxt) * TC_BM;
+    ti.c0 = 0;
+    ti.c1 = p.nch;
+    ti.mt = 0;
+    ti.sp = 0;
+  } else {
+    const int per_k = p.mt2 * p.ks2;
+    ti.k = t / per_k;
+    const int r = t % per_k;
+    ti.mt = r / p.ks2;
+    ti.sp = r % p.ks2;
+    ti.row0 = ti.mt * TC_BM;
+    ti.c0 = ti.sp * p.cps2;
+    ti.c1 = min(p.nch, ti.c0 + p.cps2);
+  }
+  return ti;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_lr_tc(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
+            const __grid_constant__ CUtensorMap tm_b, const TcParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~static_cast<uintptr_t>(1023));
+  const uint32_t a_bytes = TC_BM * TC_BK * 2;
+  const uint32_t b_bytes = (uint32_t)p.n4 * TC_BK * 2;
+  const uint32_t stage_bytes = 2 * a_bytes + b_bytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TC_STAGES * stage_bytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 4);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  const uint32_t full0 = su32(bars), empty0 = su32(bars + TC_STAGES);
+  const uint32_t tfull0 = su32(bars + 2 * TC_STAGES), tempty0 = su32(bars + 2 * TC_STAGES + 2);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(tfull0 + 8 * b, 1);
+      mbar_init(tempty0 + 8 * b, 128);
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(tmem_slot)),
+                 "r"(p.tcols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ------------------------------------------------------------ producer
+      uint32_t stage = 0, phase = 0;
+      int armed_phase[TC_STAGES];
+      for (int s = 0; s < TC_STAGES; ++s) armed_phase[s] = -1;
+      bool ok = true;
+      for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
+        const TileInfo ti = decode(p, t);
+        for (int c = ti.c0; c < ti.c1; ++c) {
+          if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, TC_WAIT_CYCLES)) {
+            ok = false;
+            break;
+          }
+          const uint32_t sbase = su32(smem + stage * stage_bytes);
+          mbar_expect_tx(full0 + 8 * stage, stage_bytes);
+          tma_load_3d(sbase, &tm_hi, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k);
+          tma_load_3d(sbase + a_bytes, &tm_lo, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k);
+          tma_load_3d(sbase + 2 * a_bytes, &tm_b, full0 + 8 * stage, c * TC_BK, 0, ti.k);
+          armed_phase[stage] = (int)phase;
+          if (++stage == TC_STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      if (!ok) {
+        *abort_flag = 1;
+        atomicOr(p.err, 1);
+      }
+      // drain: never leave a TMA write in flight
+      for (int s = 0; s < TC_STAGES; ++s)
+        if (armed_phase[s] >= 0) {
+          const long long t0 = clock64();
+          while (!mbar_test(full0 + 8 * s, (uint32_t)armed_phase[s]) &&
+                 clock64() - t0 < TC_WAIT_CYCLES) {
+          }
+        }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ------------------------------------------------------------ MMA issuer
+      uint32_t stage = 0, phase = 0, acc = 0, acc_phase = 0;
+      int last_stage = -1;
+      uint32_t last_phase = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
+        const TileInfo ti = decode(p, t);
+        if (!mbar_wait(tempty0 + 8 * acc, acc_phase ^ 1, abort_flag, TC_WAIT_CYCLES)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t dt = tmem_base + acc * (uint32_t)p.n4;
+        for (int c = ti.c0; c < ti.c1; ++c) {
+          if (!mbar_wait(full0 + 8 * stage, phase, abort_flag, TC_WAIT_CYCLES)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = su32(smem + stage * stage_bytes);
+#pragma unroll
+          for (int kk = 0; kk < TC_BK / 16; ++kk) {
+            const uint64_t bd = sw128_desc(sa + 2 * a_bytes + kk * 32);
+            umma_bf16(dt, sw128_desc(sa + kk * 32), bd, p.idesc, (c > ti.c0 || kk > 0) ? 1u : 0u);
+            umma_bf16(dt, sw128_desc(sa + a_bytes + kk * 32), bd, p.idesc, 1u);
+          }
+          umma_commit(empty0 + 8 * stage);
+          last_stage = (int)stage;
+          last_phase = phase;
+          if (++stage == TC_STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+        if (!ok) break;
+        umma_commit(tfull0 + 8 * acc);
+        acc ^= 1;
+        if (acc == 0) acc_phase ^= 1;
+      }
+      if (!ok) {
+        *abort_flag = 1;
+        atomicOr(p.err, 2);
+      }
+      if (last_stage >= 0) {  // drain: every issued MMA finished reading shared memory
+        const long long t0 = clock64();
+        while (!mbar_test(empty0 + 8 * last_stage, last_phase) && clock64() - t0 < TC_WAIT_CYCLES) {
+        }
+      }
+    }
+  } else {
+    // -------------------------------------------------------------- epilogue
+    const int q = warp & 3;  // TMEM lane quadrant this warp may access
+    const int row = q * 32 + lane;
+    uint32_t acc = 0, acc_phase = 0;
+    float v[48];
+    for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+      const TileInfo ti = decode(p, t);
+      if (!mbar_wait(tfull0 + 8 * acc, acc_phase, abort_flag, TC_WAIT_CYCLES)) {
+        *abort_flag = 1;
+        atomicOr(p.err, 4);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t ta = tmem_base + ((uint32_t)(q * 32) << 16) + acc * (uint32_t)p.n4;
+      for (int c16 = 0; c16 < p.n4; c16 += 16) tmem_ld16(ta + c16, v + c16);
+      tmem_ld_wait();
+      tc_fence_before();
+      mbar_arrive(tempty0 + 8 * acc);
+      const int na = p.na;
+      if (p.mode == 1) {
+        const int x = ti.row0 + row;
+        if (x < p.nx) {
+          float2* o = p.phi + ((size_t)ti.k * p.nx + x) * na;
+          for (int a = 0; a < na; ++a)
+            o[a] = make_float2(v[a] + v[2 * na + a], v[na + a] + v[3 * na + a]);
+        }
+      } else {
+        const int n = ti.row0 + row;
+        if (n < p.nb) {
+          double* pr = p.part + (size_t)ti.sp * 2 * p.npsi;
+          double* pim = pr + p.npsi;
+          for (int a = 0; a < na; ++a) {
+            const size_t idx = (size_t)n + (size_t)p.nb * ((size_t)ti.k + (size_t)p.nk * a);
+            pr[idx] = -((double)v[a] + (double)v[2 * na + a]);
+            pim[idx] = -((double)v[na + a] + (double)v[3 * na + a]);
+          }
+        }
+      }
+      acc ^= 1;
+      if (acc == 0) acc_phase ^= 1;
+    }
+  }
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(p.tcols)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------- operand builders
+
+__device__ __forceinline__ void split_bf16(float v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(v);
+  lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+}
+
+// UA_s[k][x][K1]: K < Nb -> Re u(n=K), else Im u(n=K-Nb)   (from u [x][k][n])
+__global__ void k_build_ua(const double2* __restrict__ u, __nv_bfloat16* __restrict__ hi,
+                           __nv_bfloat16* __restrict__ lo, int nb, int nk, int nx, int p1) {
+  const long long total = (long long)nk * nx * 2 * nb;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int K = (int)(i % (2 * nb));
+    const long long r = i / (2 * nb);
+    const int x = (int)(r % nx);
+    const int k = (int)(r / nx);
+    const int n = K < nb ? K : K - nb;
+    const double2 z = u[((size_t)x * nk + k) * nb + n];
+    const float v = (float)(K < nb ? z.x : z.y);
+    __nv_bfloat16 h, l;
+    split_bf16(v, h, l);
+    const size_t o = ((size_t)k * nx + x) * p1 + K;
+    hi[o] = h;
+    lo[o] = l;
+  }
+}
+
+// UB_s[k][n][K2]: K2 < Nx -> Re u(n, x=K2), else Im u(n, x=K2-Nx)
+__global__ void k_build_ub(const double2* __restrict__ u, __nv_bfloat16* __restrict__ hi,
+                           __nv_bfloat16* __restrict__ lo, int nb, int nk, int nx, int p2) {
+  const long long total = (long long)nk * nb * 2 * nx;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int K = (int)(i % (2 * nx));
+    const long long r = i / (2 * nx);
+    const int n = (int)(r % nb);
+    const int k = (int)(r / nb);
+    const int x = K < nx ? K : K - nx;
+    const double2 z = u[((size_t)x * nk + k) * nb + n];
+    const float v = (float)(K < nx ? z.x : z.y);
+    __nv_bfloat16 h, l;
+    split_bf16(v, h, l);
+    const size_t o = ((size_t)k * nb + n) * p2 + K;
+    hi[o] = h;
+    lo[o] = l;
+  }
+}
+
+// B1[k][j][K1], j = s*2Na + part*Na + a, from q = allow o psi:
+//   part 0 (Re phi): K=(0,n) -> qr, K=(1,n) -> -qi;  part 1 (Im phi): (0,n) -> qi, (1,n) -> qr
+__global__ void k_prep_b1(const double* __restrict__ pr, const double* __restrict__ pi,
+                          const double* __restrict__ allow, __nv_bfloat16* __restrict__ b1, int nb,
+                          int nk, int na, int p1) {
+  const int total = nk * 2 * nb;
+  const int n4 = 4 * na;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int K = i % (2 * nb);
+    const int k = i / (2 * nb);
+    const int c = K < nb ? 0 : 1;
+    const int n = K - c * nb;
+    for (int a = 0; a < na; ++a) {
+      const size_t idx = (size_t)n + (size_t)nb * ((size_t)k + (size_t)nk * a);
+      const double m = allow[idx];
+      const float qr = (float)(pr[idx] * m), qi = (float)(pi[idx] * m);
+      const float v0 = c == 0 ? qr : -qi;
+      const float v1 = c == 0 ? qi : qr;
+      __nv_bfloat16 h0, l0, h1, l1;
+      split_bf16(v0, h0, l0);
+      split_bf16(v1, h1, l1);
+      __nv_bfloat16* base = b1 + (size_t)k * n4 * p1 + K;
+      base[(size_t)(0 * 2 * na + 0 * na + a) * p1] = h0;
+      base[(size_t)(0 * 2 * na + 1 * na + a) * p1] = h1;
+      base[(size_t)(1 * 2 * na + 0 * na + a) * p1] = l0;
+      base[(size_t)(1 * 2 * na + 1 * na + a) * p1] = l1;
+    }
+  }
+}
+
+// B2[k][j][K2] from phi'[k][x][a]:
+//   part 0 (Re out): K=(0,x) -> Re phi', K=(1,x) -> Im phi'
+//   part 1 (Im out): K=(0,x) -> Im phi', K=(1,x) -> -Re phi'
+__global__ void k_prep_b2(const float2* __restrict__ phi, __nv_bfloat16* __restrict__ b2, int nk,
+                          int nx, int na, int p2) {
+  const int total = nk * nx;
+  const int n4 = 4 * na;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int x = i % nx;
+    const int k = i / nx;
+    __nv_bfloat16* base = b2 + (size_t)k * n4 * p2;
+    for (int a = 0; a < na; ++a) {
+      const float2 f = phi[((size_t)k * nx + x) * na + a];
+      __nv_bfloat16 hr, lr, hi, li, hn, ln;
+      split_bf16(f.x, hr, lr);
+      split_bf16(f.y, hi, li);
+      split_bf16(-f.x, hn, ln);
+      // part 0
+      base[(size_t)(0 * 2 * na + a) * p2 + x] = hr;
+      base[(size_t)(0 * 2 * na + a) * p2 + nx + x] = hi;
+      base[(size_t)(1 * 2 * na + a) * p2 + x] = lr;
+      base[(size_t)(1 * 2 * na + a) * p2 + nx + x] = li;
+      // part 1
+      base[(size_t)(0 * 2 * na + na + a) * p2 + x] = hi;
+      base[(size_t)(0 * 2 * na + na + a) * p2 + nx + x] = hn;
+      base[(size_t)(1 * 2 * na + na + a) * p2 + x] = li;
+      base[(size_t)(1 * 2 * na + na + a) * p2 + nx + x] = ln;
+    }
+  }
+}
+
+// FP32 k-mesh transform: phi'(.,x,a) = FFT_fwd[W(.,x) o FFT_bwd[phi(.,x,a)]] / Nk
+__device__ void dft_axis_f(const float2* __restrict__ in, float2* __restrict__ out, int na, int nk,
+                           int ax, float sgn) {
+  const int n = c_kdimf[ax];
+  const int st = (ax == 0) ? c_kdimf[1] * c_kdimf[2] : ((ax == 1) ? c_kdimf[2] : 1);
+  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
+    const int a = e / nk, k = e % nk;
+    const int m = (k / st) % n;
+    const float2* line = in + (size_t)a * nk + (k - m * st);
+    float sr = 0.f, si = 0.f;
+    for (int j = 0; j < n; ++j) {
+      const float2 w = c_twf[ax][(j * m) % n];
+      const float wy = sgn * w.y;
+      const float2 v = line[j * st];
+      sr += v.x * w.x - v.y * wy;
+      si += v.x * wy + v.y * w.x;
+    }
+    out[e] = make_float2(sr, si);
+  }
+}
+
+__global__ void k_lr_fft_w_f32(float2* __restrict__ phi, const float* __restrict__ W, int nk, int nx,
+                               int na) {
+  extern __shared__ float2 fsm[];
+  float2* b0 = fsm;
+  float2* b1 = fsm + (size_t)na * nk;
+  const int x = blockIdx.x;
+  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
+    const int a = e / nk, k = e % nk;
+    b0[e] = phi[((size_t)k * nx + x) * na + a];
+  }
+  __syncthreads();
+  dft_axis_f(b0, b1, na, nk, 0, 1.f);
+  __syncthreads();
+  dft_axis_f(b1, b0, na, nk, 1, 1.f);
+  __syncthreads();
+  dft_axis_f(b0, b1, na, nk, 2, 1.f);
+  __syncthreads();
+  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
+    const float w = W[(size_t)x * nk + (e % nk)];
+    b1[e] = make_float2(b1[e].x * w, b1[e].y * w);
+  }
+  __syncthreads();
+  dft_axis_f(b1, b0, na, nk, 0, -1.f);
+  __syncthreads();
+  dft_axis_f(b0, b1, na, nk, 1, -1.f);
+  __syncthreads();
+  dft_axis_f(b1, b0, na, nk, 2, -1.f);
+  __syncthreads();
+  const float norm = 1.0f / (float)nk;
+  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
+    const int a = e / nk, k = e % nk;
+    phi[((size_t)k * nx + x) * na + a] = make_float2(b0[e].x * norm, b0[e].y * norm);
+  }
+}
+
+__global__ void k_w_to_f32(const double* __restrict__ W, float* __restrict__ Wf, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    Wf[i] = (float)W[i];
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+
+}  // namespace
+
+struct MixedLR {
+  int p1 = 0, p2 = 0, n4 = 0;
+  __nv_bfloat16 *ua_hi = nullptr, *ua_lo = nullptr, *ub_hi = nullptr, *ub_lo = nullptr;
+  __nv_bfloat16 *b1 = nullptr, *b2 = nullptr;
+  float2* phi = nullptr;
+  float* Wf = nullptr;
+  int* d_err = nullptr;
+  CUtensorMap tm_ua_hi, tm_ua_lo, tm_b1, tm_ub_hi, tm_ub_lo, tm_b2;
+  TcParams g1{}, g2{};
+  int grid1 = 1, grid2 = 1;
+  size_t smem_bytes = 0;
+  bool ready = false;
+};
+
+namespace {
+
+int encode3d(ocn_ctx* c, EncodeTiledFn fn, CUtensorMap* m, void* base, uint64_t inner, uint64_t rows,
+             uint64_t outer, uint64_t pitch_elems, uint32_t box_rows) {
+  const cuuint64_t dims[3] = {inner, rows, outer};
+  const cuuint64_t strides[2] = {pitch_elems * 2, pitch_elems * 2 * rows};
+  const cuuint32_t box[3] = {(cuuint32_t)TC_BK, box_rows, 1};
+  const cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_err(c, OCN_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return OCN_OK;
+}
+
+template <typename T>
+int alloc(ocn_ctx* c, T** p, size_t n) {
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+  if (e != cudaSuccess) return set_err(c, OCN_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return OCN_OK;
+}
+
+}  // namespace
+
 int mixed_init(ocn_ctx* c) {
-  c->mixed = new MixedLR();
+  if (c->nspn != 1) return set_err(c, OCN_ERR_UNSUPPORTED, "mixed precision requires nspn = 1");
+  MixedLR* m = new (std::nothrow) MixedLR();
+  if (!m) return set_err(c, OCN_ERR_ALLOC, "host allocation failed");
+  c->mixed = m;
+  const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na;
+  m->n4 = 4 * na;
+  m->p1 = (2 * nb + 7) / 8 * 8;
+  m->p2 = (2 * nx + 7) / 8 * 8;
+  int rc;
+  if ((rc = alloc(c, &m->ua_hi, (size_t)nk * nx * m->p1)) || (rc = alloc(c, &m->ua_lo, (size_t)nk * nx * m->p1)) ||
+      (rc = alloc(c, &m->ub_hi, (size_t)nk * nb * m->p2)) || (rc = alloc(c, &m->ub_lo, (size_t)nk * nb * m->p2)) ||
+      (rc = alloc(c, &m->b1, (size_t)nk * m->n4 * m->p1)) || (rc = alloc(c, &m->b2, (size_t)nk * m->n4 * m->p2)) ||
+      (rc = alloc(c, &m->phi, (size_t)nk * nx * na)) || (rc = alloc(c, &m->Wf, (size_t)nk * nx)) ||
+      (rc = alloc(c, &m->d_err, 1)))
+    return rc;
+  OCN_CUDA(c, cudaMemset(m->d_err, 0, sizeof(int)));
+  // pitch padding of the operands is never read (TMA bounds are the logical
+  // extents) but is cleared so the buffers hold defined values
+  OCN_CUDA(c, cudaMemset(m->b1, 0, (size_t)nk * m->n4 * m->p1 * 2));
+  OCN_CUDA(c, cudaMemset(m->b2, 0, (size_t)nk * m->n4 * m->p2 * 2));
+
+  void* fnp = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fnp, 12000, cudaEnableDefault, &q);
+  if (e != cudaSuccess || !fnp) return set_err(c, OCN_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  EncodeTiledFn fn = reinterpret_cast<EncodeTiledFn>(fnp);
+  if ((rc = encode3d(c, fn, &m->tm_ua_hi, m->ua_hi, 2 * nb, nx, nk, m->p1, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_ua_lo, m->ua_lo, 2 * nb, nx, nk, m->p1, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_b1, m->b1, 2 * nb, m->n4, nk, m->p1, m->n4)) ||
+      (rc = encode3d(c, fn, &m->tm_ub_hi, m->ub_hi, 2 * nx, nb, nk, m->p2, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_ub_lo, m->ub_lo, 2 * nx, nb, nk, m->p2, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_b2, m->b2, 2 * nx, m->n4, nk, m->p2, m->n4)))
+    return rc;
+
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(m->n4 >> 3) << 17) |
+                         ((uint32_t)(TC_BM >> 4) << 24);
+  const uint32_t tcols = (2 * m->n4 <= 32) ? 32u : ((2 * m->n4 <= 64) ? 64u : 128u);
+  TcParams& g1 = m->g1;
+  g1.mode = 1;
+  g1.nb = nb; g1.nk = nk; g1.nx = nx; g1.na = na; g1.n4 = m->n4;
+  g1.nch = (2 * nb + TC_BK - 1) / TC_BK;
+  g1.nxt = (nx + TC_BM - 1) / TC_BM;
+  g1.ntiles = nk * g1.nxt;
+  g1.idesc = idesc;
+  g1.tcols = tcols;
+  g1.phi = m->phi;
+  g1.err = m->d_err;
+  g1.npsi = c->npsi;
+  TcParams& g2 = m->g2;
+  g2 = g1;
+  g2.mode = 2;
+  g2.nch = (2 * nx + TC_BK - 1) / TC_BK;
+  g2.mt2 = (nb + TC_BM - 1) / TC_BM;
+  int ks = (4 * c->sm_count + nk * g2.mt2 - 1) / (nk * g2.mt2);
+  ks = std::max(1, std::min(ks, std::max(1, g2.nch / 4)));
+  g2.cps2 = (g2.nch + ks - 1) / ks;
+  g2.ks2 = (g2.nch + g2.cps2 - 1) / g2.cps2;  // no empty split
+  g2.ntiles = nk * g2.mt2 * g2.ks2;
+  c->lr_xsplit = g2.ks2;
+  if ((rc = alloc(c, &c->d_accpart, (size_t)g2.ks2 * 2 * c->npsi))) return rc;
+  g2.part = c->d_accpart;
+  m->smem_bytes = 1024 + TC_STAGES * (size_t)(2 * TC_BM * TC_BK * 2 + m->n4 * TC_BK * 2) + 256;
+  m->grid1 = std::min(g1.ntiles, c->sm_count);
+  m->grid2 = std::min(g2.ntiles, c->sm_count);
+  OCN_CUDA(c, cudaFuncSetAttribute(k_lr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->smem_bytes));
+  const size_t fsm = sizeof(float2) * 2 * (size_t)na * nk;
+  OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+  // FP32 twiddles, rounded from FP64 roots of unity
+  float2 tw[3][OCN_MAX_KDIM];
+  const double pi = 3.1415926535897932384626433832795;
+  for (int a = 0; a < 3; ++a)
+    for (int t = 0; t < OCN_MAX_KDIM; ++t) {
+      const int n = c->dims.kmesh[a];
+      tw[a][t] = t < n ? make_float2((float)cos(2.0 * pi * t / n), (float)sin(2.0 * pi * t / n))
+                       : make_float2(0.f, 0.f);
+    }
+  OCN_CUDA(c, cudaMemcpyToSymbol(c_twf, tw, sizeof(tw)));
+  OCN_CUDA(c, cudaMemcpyToSymbol(c_kdimf, c->dims.kmesh, sizeof(int) * 3));
   return OCN_OK;
 }
 
 int mixed_free(ocn_ctx* c) {
-  delete c->mixed;
+  MixedLR* m = c->mixed;
+  if (!m) return OCN_OK;
+  void* bufs[] = {m->ua_hi, m->ua_lo, m->ub_hi, m->ub_lo, m->b1, m->b2, m->phi, m->Wf, m->d_err};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  delete m;
   c->mixed = nullptr;
   return OCN_OK;
 }
 
-int mixed_set_bloch(ocn_ctx* c) { return OCN_OK; }
+int mixed_set_bloch(ocn_ctx* c) {
+  MixedLR* m = c->mixed;
+  if (!m) return set_err(c, OCN_ERR_STATE, "mixed state missing");
+  const int nb = c->nb, nk = c->nk, nx = c->nx;
+  const int grid = 8 * c->sm_count;
+  k_build_ua<<<grid, 256, 0, c->stream>>>(c->d_u, m->ua_hi, m->ua_lo, nb, nk, nx, m->p1);
+  OCN_CUDA(c, cudaGetLastError());
+  k_build_ub<<<grid, 256, 0, c->stream>>>(c->d_u, m->ub_hi, m->ub_lo, nb, nk, nx, m->p2);
+  OCN_CUDA(c, cudaGetLastError());
+  k_w_to_f32<<<grid, 256, 0, c->stream>>>(c->d_W, m->Wf, (size_t)nk * nx);
+  OCN_CUDA(c, cudaGetLastError());
+  c->launches += 3;
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+  m->ready = true;
+  return OCN_OK;
+}
 
-int lr_apply_mixed(ocn_ctx* c, const double*, const double*) {
-  return set_err(c, OCN_ERR_UNSUPPORTED, "mixed-precision long-range path not built");
+int mixed_check(ocn_ctx* c) {
+  MixedLR* m = c->mixed;
+  if (!m) return OCN_OK;
+  int h = 0;
+  OCN_CUDA(c, cudaMemcpy(&h, m->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    cudaMemset(m->d_err, 0, sizeof(int));
+    return set_err(c, OCN_ERR_TIMEOUT, "tensor-core pipeline wait timed out (code " + std::to_string(h) + ")");
+  }
+  return OCN_OK;
+}
+
+int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi) {
+  MixedLR* m = c->mixed;
+  if (!m || !m->ready) return set_err(c, OCN_ERR_STATE, "mixed-precision operands not built");
+  const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na;
+  {
+    TimedScope ts(c, T_LR_PREP);
+    const int total = nk * 2 * nb;
+    k_prep_b1<<<std::min((total + 255) / 256, 8 * c->sm_count), 256, 0, c->stream>>>(
+        d_pr, d_pi, c->d_allow, m->b1, nb, nk, na, m->p1);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  {
+    TimedScope ts(c, T_LR_GEMM1);
+    k_lr_tc<<<m->grid1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ua_hi, m->tm_ua_lo, m->tm_b1, m->g1);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  {
+    TimedScope ts(c, T_LR_FFT);
+    const size_t fsm = sizeof(float2) * 2 * (size_t)na * nk;
+    k_lr_fft_w_f32<<<nx, 256, fsm, c->stream>>>(m->phi, m->Wf, nk, nx, na);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  {
+    TimedScope ts(c, T_LR_PREP);
+    const int total = nk * nx;
+    k_prep_b2<<<std::min((total + 255) / 256, 8 * c->sm_count), 256, 0, c->stream>>>(m->phi, m->b2, nk,
+                                                                                       nx, na, m->p2);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  {
+    TimedScope ts(c, T_LR_GEMM2);
+    k_lr_tc<<<m->grid2, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ub_hi, m->tm_ub_lo, m->tm_b2, m->g2);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+  }
+  return OCN_OK;
 }
 
 }  // namespace ocn

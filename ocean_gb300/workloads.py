@@ -138,6 +138,8 @@ def make(name: str, seed: int = 0, nb: Optional[int] = None, kmesh=None, xmesh=N
         "c1": dict(nb=32, kmesh=(4, 4, 4), xmesh=(8, 8, 8), core_l=0, mult=False, niter=200),
         "c2": dict(nb=100, kmesh=(8, 8, 8), xmesh=(12, 12, 12), core_l=0, mult=False, niter=1000,
                    gmres_nomega=200),
+        # c2 k-mesh and bands on an 8^3 x-mesh: the profiling case (~1.3 GB on the device)
+        "c2s": dict(nb=100, kmesh=(8, 8, 8), xmesh=(8, 8, 8), core_l=0, mult=False, niter=100),
         "c3": dict(nb=64, kmesh=(6, 6, 6), xmesh=(10, 10, 10), core_l=1, mult=True, niter=200),
         "c3small": dict(nb=16, kmesh=(2, 2, 3), xmesh=(4, 4, 4), core_l=1, mult=True, niter=40),
         "c5": dict(nb=100, kmesh=(8, 8, 8), xmesh=(12, 12, 12), core_l=0, mult=False, niter=1000,

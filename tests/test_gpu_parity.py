@@ -187,3 +187,64 @@ def test_gmres_fp64_matches_oracle(built, name):
     assert rc == 0
     assert np.max(np.abs(oim - oim2) / np.abs(oim2)) < 1e-8
     assert np.max(np.abs(ore - ore2) / np.abs(ore2)) < 1e-8
+
+
+# ------------------------------------------------------------- mixed precision
+# Split-BF16 tensor-core contractions keep ~16 significant bits per product and
+# accumulate in FP32: H*psi is expected within 1e-4 relative of the FP64 oracle,
+# and Haydock spectra within the 1e-4 relative spectral error the path targets.
+
+@pytest.mark.parametrize("name", ["tiny", "small", "c1", "c3small"])
+def test_apply_H_mixed_matches_oracle(built, name):
+    _, O = built
+    w, P = problem(name, O, seed=4)
+    ctx = capi.Context(w, precision=capi.OCN_PREC_MIXED)
+    try:
+        rng = np.random.default_rng(13)
+        pr, pi = rng.standard_normal(w.npsi), rng.standard_normal(w.npsi)
+        hr, hi = ctx.apply_H(pr, pi)
+        orr, oi = P.xact(pr, pi)
+        assert _rel(hr + 1j * hi, orr + 1j * oi) < 1e-4
+        # the long-range part alone (E and multiplet off) still agrees
+        hf = (1, 1, 1, 1, 0, 0)
+        r1, i1 = ctx.apply_H(pr, pi, hflag=hf)
+        r0, i0 = ctx.apply_H(pr, pi, hflag=(0, 1, 1, 1, 0, 0))
+        o1r, o1i = P.xact(pr, pi, hflag=hf)
+        o0r, o0i = P.xact(pr, pi, hflag=(0, 1, 1, 1, 0, 0))
+        lr_gpu = (r1 - r0) + 1j * (i1 - i0)
+        lr_ref = (o1r - o0r) + 1j * (o1i - o0i)
+        assert _rel(lr_gpu, lr_ref) < 2e-4
+    finally:
+        ctx.close()
+
+
+def test_haydock_mixed_spectrum_error(built):
+    _, O = built
+    w, P = problem("c1", O, seed=7)
+    niter = 200
+    ctx = capi.Context(w, precision=capi.OCN_PREC_MIXED)
+    try:
+        ra, ia, rb, done = ctx.haydock(niter)
+    finally:
+        ctx.close()
+    rc, ora, oia, orb, _ = P.haydock(niter)
+    assert done == niter and rc == 0
+    assert np.max(np.abs(ra[:5] - ora[:5]) / np.abs(ora[:5])) < 1e-4
+    sg = capi.spectrum_cf(ra, ia, rb, niter, w.kpref, w.el, w.eh, 2000, w.gam0)
+    so = O.write_core(ora, oia, orb, niter, w.kpref, w.el, w.eh, 2000, w.gam0)
+    assert _rel(sg[:, 2], so[:, 2]) < 1e-4
+
+
+def test_gmres_mixed_matches_oracle(built):
+    _, O = built
+    w, P = problem("small", O, seed=9)
+    E = np.array([4.0, 4.1, 8.0])
+    # |g|^2 threshold above the floor set by the split-BF16 action (~1e-11 here)
+    ctx = capi.Context(w, precision=capi.OCN_PREC_MIXED)
+    try:
+        ore, oim, rel, its = ctx.gmres(E, depth=16, tol=1e-9, max_restarts=200)
+    finally:
+        ctx.close()
+    rc, ore2, oim2, rel2, its2, tot = P.gmres(E, depth=16, ffff=1e-14, max_restarts=200)
+    assert rc == 0
+    assert np.max(np.abs(oim - oim2) / np.abs(oim2)) < 1e-3
