@@ -60,9 +60,12 @@ int apply_H_impl(ocn_ctx* c, const double* ir, const double* ii, double* orr, do
   for (int i = 0; i < 6; ++i) hflag[i] = hflag_in ? hflag_in[i] : c->sys.nhflag[i];
   int rc = require(c);
   if (rc) return rc;
-  if ((rc = zero_acc(c))) return rc;
-  if (c->sys.mult && hflag[4] == 1 && c->have_mult)
+  c->acc_valid = false;
+  if (c->sys.mult && hflag[4] == 1 && c->have_mult) {
+    if ((rc = zero_acc(c))) return rc;
     if ((rc = mult_apply(c, ir, ii))) return rc;
+    c->acc_valid = true;
+  }
   if (c->sys.long_range && hflag[0] == 1) {
     if (c->dims.precision == OCN_PREC_MIXED) rc = lr_apply_mixed(c, ir, ii);
     else rc = lr_apply_fp64(c, ir, ii);
@@ -145,7 +148,8 @@ int ocn_ctx_create(const ocn_dims* d, ocn_ctx** out) {
     return set_err(nullptr, OCN_ERR_ARG, "nalpha must equal 4*(2*core_l+1)");
   if (d->nspn != 1 && d->nspn != 2) return set_err(nullptr, OCN_ERR_ARG, "nspn must be 1 or 2");
   if (nk > OCN_MAX_NK) return set_err(nullptr, OCN_ERR_ARG, "k-mesh larger than 4096 points");
-  if ((size_t)2 * d->nalpha * nk * sizeof(double2) > 227u * 1024u)
+  if (sizeof(double2) * (3 * OCN_MAX_KDIM + (size_t)d->nalpha * d->kmesh[0] * d->kmesh[1] * (d->kmesh[2] + 1)) >
+      227u * 1024u)
     return set_err(nullptr, OCN_ERR_ARG, "nalpha*Nk too large for the shared-memory k-mesh transform");
   if (d->precision != OCN_PREC_FP64 && d->precision != OCN_PREC_MIXED)
     return set_err(nullptr, OCN_ERR_ARG, "unknown precision");
@@ -249,6 +253,13 @@ int ocn_set_energies(ocn_ctx* c, const double* re, const double* im) {
     OCN_CUDA(c, cudaMemsetAsync(c->d_ei, 0, sizeof(double) * c->npsi, c->stream));
   OCN_CUDA(c, cudaStreamSynchronize(c->stream));
   c->have_energies = true;
+  c->ei_nonzero = false;
+  if (im)
+    for (size_t i = 0; i < c->npsi; ++i)
+      if (im[i] != 0.0) {
+        c->ei_nonzero = true;
+        break;
+      }
   return OCN_OK;
 }
 
@@ -553,8 +564,11 @@ int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter,
     double* old = buf[0];
     double* psi = buf[1];
     double* h = buf[2];
-    if ((rc = zero_acc(c))) break;
-    if (c->sys.mult && c->sys.nhflag[4] == 1 && c->have_mult && (rc = mult_apply(c, psi, psi + n))) break;
+    c->acc_valid = false;
+    if (c->sys.mult && c->sys.nhflag[4] == 1 && c->have_mult) {
+      if ((rc = zero_acc(c)) || (rc = mult_apply(c, psi, psi + n))) break;
+      c->acc_valid = true;
+    }
     if (c->sys.long_range && c->sys.nhflag[0] == 1) {
       rc = (c->dims.precision == OCN_PREC_MIXED) ? lr_apply_mixed(c, psi, psi + n)
                                                  : lr_apply_fp64(c, psi, psi + n);

@@ -62,6 +62,8 @@ struct ocn_ctx {
 
   ocn_system sys{};
   bool have_energies = false, have_allow = false, have_bloch = false, have_W = false;
+  bool ei_nonzero = false;   // any Sigma'' != 0 (else the imaginary energy plane is skipped)
+  bool acc_valid = false;    // d_acc holds the multiplet term of the current action
   bool have_so = false, have_mult = false;
 
   // operator data (device)

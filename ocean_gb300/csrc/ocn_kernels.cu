@@ -12,6 +12,7 @@
 #include <cstdio>
 
 #include "ocn_internal.h"
+#include "ocn_kmesh_dft.cuh"
 
 namespace ocn {
 
@@ -107,64 +108,17 @@ __global__ void __launch_bounds__(G1_X) k_lr_gemm1_fp64(
 
 // ------------------------------------------------ LR: k <-> R and x W(R,x)
 
-// One 1-D DFT pass along axis `ax` of every [a][k] line held in shared memory.
-__device__ void dft_axis(const double2* __restrict__ in, double2* __restrict__ out, int na, int nk,
-                         int ax, double sgn) {
-  const int n = c_kdim[ax];
-  const int st = (ax == 0) ? c_kdim[1] * c_kdim[2] : ((ax == 1) ? c_kdim[2] : 1);
-  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
-    const int a = e / nk, k = e % nk;
-    const int m = (k / st) % n;
-    const int base = k - m * st;
-    const double2* line = in + (size_t)a * nk + base;
-    double sr = 0.0, si = 0.0;
-    for (int j = 0; j < n; ++j) {
-      const int t = (j * m) % n;
-      const double2 w = c_tw[ax][t];
-      const double wy = sgn * w.y;
-      const double2 v = line[j * st];
-      sr += v.x * w.x - v.y * wy;
-      si += v.x * wy + v.y * w.x;
-    }
-    out[e] = make_double2(sr, si);
-  }
-}
-
 // phi'(.,x,a) = FFT_fwd[ W(.,x) o FFT_bwd[ phi(.,x,a) ] ] / Nk   (long_range.f90:928-939,
-// FFTW signs +1 backward / -1 forward, Modules/FFT_wrapper.f90:24-25).  One CTA per x.
-__global__ void k_lr_fft_w_fp64(double2* __restrict__ phi, const double* __restrict__ W, int nk,
-                                int nx, int na) {
+// FFTW signs +1 backward / -1 forward, Modules/FFT_wrapper.f90:24-25).  One CTA per x,
+// transform in shared memory (ocn_kmesh_dft.cuh).
+__global__ void k_lr_fft_w_fp64(double2* __restrict__ phi, const double* __restrict__ W, int nx,
+                                const KmeshGeom<double> g) {
   extern __shared__ double2 smem[];
-  double2* b0 = smem;
-  double2* b1 = smem + (size_t)na * nk;
-  const int x = blockIdx.x;
-  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
-    const int a = e / nk, k = e % nk;
-    b0[e] = phi[((size_t)k * nx + x) * na + a];
-  }
+  double2* tw = smem;
+  double2* buf = smem + 3 * OCN_MAX_KDIM;
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_tw[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
   __syncthreads();
-  dft_axis(b0, b1, na, nk, 0, +1.0);
-  __syncthreads();
-  dft_axis(b1, b0, na, nk, 1, +1.0);
-  __syncthreads();
-  dft_axis(b0, b1, na, nk, 2, +1.0);
-  __syncthreads();
-  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
-    const double w = W[(size_t)x * nk + (e % nk)];
-    b1[e] = make_double2(b1[e].x * w, b1[e].y * w);
-  }
-  __syncthreads();
-  dft_axis(b1, b0, na, nk, 0, -1.0);
-  __syncthreads();
-  dft_axis(b0, b1, na, nk, 1, -1.0);
-  __syncthreads();
-  dft_axis(b1, b0, na, nk, 2, -1.0);
-  __syncthreads();
-  const double norm = 1.0 / (double)nk;
-  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
-    const int a = e / nk, k = e % nk;
-    phi[((size_t)k * nx + x) * na + a] = make_double2(b0[e].x * norm, b0[e].y * norm);
-  }
+  kmesh_convolve<double>(phi, W, nx, blockIdx.x, g, buf, tw);
 }
 
 // ------------------------------------------------------ LR: x-mesh -> band
@@ -248,7 +202,11 @@ __global__ void k_combine(const double* __restrict__ pr, const double* __restric
     for (int ic = 0; ic < OCN_MAX_NA; ++ic) {
       if (ic >= na) break;
       const size_t idx = e + (size_t)nbk * ic;
-      double fr = acc[idx], fi = acc[npsi + idx];
+      double fr = 0.0, fi = 0.0;
+      if (acc) {
+        fr = acc[idx];
+        fi = acc[npsi + idx];
+      }
       for (int s = 0; s < nparts; ++s) {
         fr += part[(size_t)s * 2 * npsi + idx];
         fi += part[(size_t)s * 2 * npsi + npsi + idx];
@@ -751,7 +709,7 @@ int upload_twiddles(ocn_ctx* c) {
 int kernels_init(ocn_ctx* c) {
   const size_t g1 = sizeof(double2) * ((size_t)c->nspn * G1_N * (G1_X + 1) + (size_t)c->na * G1_N);
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_gemm1_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g1));
-  const size_t ff = sizeof(double2) * 2 * (size_t)c->na * c->nk;
+  const size_t ff = kmesh_smem(kmesh_geom<double>(c->dims.kmesh, c->na));
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff));
   const size_t ma = sizeof(double2) * (size_t)c->na * 256;
   OCN_CUDA(c, cudaFuncSetAttribute(k_mult_amp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ma));
@@ -785,9 +743,9 @@ int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi) {
     OCN_CUDA(c, cudaGetLastError());
   }
   {
-    const size_t sm = sizeof(double2) * 2 * (size_t)na * nk;
+    const KmeshGeom<double> g = kmesh_geom<double>(c->dims.kmesh, na);
     TimedScope ts(c, T_LR_FFT);
-    k_lr_fft_w_fp64<<<nx, 256, sm, c->stream>>>(c->d_phi, c->d_W, nk, nx, na);
+    k_lr_fft_w_fp64<<<nx, 256, kmesh_smem(g), c->stream>>>(c->d_phi, c->d_W, nx, g);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }
@@ -850,7 +808,8 @@ int combine(ocn_ctx* c, const double* d_pr, const double* d_pi, double* d_or, do
   const int use_so = (c->sys.mult && hflag[5] == 1 && c->have_so) ? 1 : 0;
   const int nparts = (c->sys.long_range && hflag[0] == 1) ? c->lr_xsplit : 0;
   k_combine<<<grid_for(nbk, 256, 4 * c->sm_count), 256, 0, c->stream>>>(
-      d_pr, d_pi, c->d_er, c->d_ei, c->d_allow, c->d_acc, c->d_accpart, nparts,
+      d_pr, d_pi, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow,
+      c->acc_valid ? c->d_acc : nullptr, c->d_accpart, nparts,
       c->d_so, d_or, d_oi, nbk, c->na, c->npsi, c->sys.e0, use_so, backwards, nullptr, nullptr,
       nullptr, nullptr);
   ++c->launches;
@@ -869,7 +828,8 @@ int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const d
   const int nparts = (c->sys.long_range && hf[0] == 1) ? c->lr_xsplit : 0;
   const int nblk = c->red_blocks;
   TimedScope ts(c, T_LANCZOS);
-  k_combine<<<nblk, 256, 0, c->stream>>>(psi_r, psi_i, c->d_er, c->d_ei, c->d_allow, c->d_acc,
+  k_combine<<<nblk, 256, 0, c->stream>>>(psi_r, psi_i, c->d_er, c->ei_nonzero ? c->d_ei : nullptr,
+                                         c->d_allow, c->acc_valid ? c->d_acc : nullptr,
                                          c->d_accpart, nparts, c->d_so, h_r, h_i, nbk,
                                          c->na, c->npsi, c->sys.e0, use_so, 0, old_r, old_i, bprev,
                                          c->d_red);

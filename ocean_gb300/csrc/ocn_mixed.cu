@@ -35,6 +35,7 @@
 #include <string>
 
 #include "ocn_internal.h"
+#include "ocn_kmesh_dft.cuh"
 
 namespace ocn {
 
@@ -468,60 +469,15 @@ __global__ void k_prep_b2(const float2* __restrict__ phi, __nv_bfloat16* __restr
   }
 }
 
-// FP32 k-mesh transform: phi'(.,x,a) = FFT_fwd[W(.,x) o FFT_bwd[phi(.,x,a)]] / Nk
-__device__ void dft_axis_f(const float2* __restrict__ in, float2* __restrict__ out, int na, int nk,
-                           int ax, float sgn) {
-  const int n = c_kdimf[ax];
-  const int st = (ax == 0) ? c_kdimf[1] * c_kdimf[2] : ((ax == 1) ? c_kdimf[2] : 1);
-  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
-    const int a = e / nk, k = e % nk;
-    const int m = (k / st) % n;
-    const float2* line = in + (size_t)a * nk + (k - m * st);
-    float sr = 0.f, si = 0.f;
-    for (int j = 0; j < n; ++j) {
-      const float2 w = c_twf[ax][(j * m) % n];
-      const float wy = sgn * w.y;
-      const float2 v = line[j * st];
-      sr += v.x * w.x - v.y * wy;
-      si += v.x * wy + v.y * w.x;
-    }
-    out[e] = make_float2(sr, si);
-  }
-}
-
-__global__ void k_lr_fft_w_f32(float2* __restrict__ phi, const float* __restrict__ W, int nk, int nx,
-                               int na) {
+// FP32 k-mesh transform, one CTA per x-point (ocn_kmesh_dft.cuh).
+__global__ void k_lr_fft_w_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx,
+                               const KmeshGeom<float> g) {
   extern __shared__ float2 fsm[];
-  float2* b0 = fsm;
-  float2* b1 = fsm + (size_t)na * nk;
-  const int x = blockIdx.x;
-  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
-    const int a = e / nk, k = e % nk;
-    b0[e] = phi[((size_t)k * nx + x) * na + a];
-  }
+  float2* tw = fsm;                   // [3][OCN_MAX_KDIM]
+  float2* buf = fsm + 3 * OCN_MAX_KDIM;
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_twf[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
   __syncthreads();
-  dft_axis_f(b0, b1, na, nk, 0, 1.f);
-  __syncthreads();
-  dft_axis_f(b1, b0, na, nk, 1, 1.f);
-  __syncthreads();
-  dft_axis_f(b0, b1, na, nk, 2, 1.f);
-  __syncthreads();
-  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
-    const float w = W[(size_t)x * nk + (e % nk)];
-    b1[e] = make_float2(b1[e].x * w, b1[e].y * w);
-  }
-  __syncthreads();
-  dft_axis_f(b1, b0, na, nk, 0, -1.f);
-  __syncthreads();
-  dft_axis_f(b0, b1, na, nk, 1, -1.f);
-  __syncthreads();
-  dft_axis_f(b1, b0, na, nk, 2, -1.f);
-  __syncthreads();
-  const float norm = 1.0f / (float)nk;
-  for (int e = threadIdx.x; e < na * nk; e += blockDim.x) {
-    const int a = e / nk, k = e % nk;
-    phi[((size_t)k * nx + x) * na + a] = make_float2(b0[e].x * norm, b0[e].y * norm);
-  }
+  kmesh_convolve<float>(phi, W, nx, blockIdx.x, g, buf, tw);
 }
 
 __global__ void k_w_to_f32(const double* __restrict__ W, float* __restrict__ Wf, size_t n) {
@@ -640,7 +596,7 @@ int mixed_init(ocn_ctx* c) {
   m->grid1 = std::min(g1.ntiles, c->sm_count);
   m->grid2 = std::min(g2.ntiles, c->sm_count);
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->smem_bytes));
-  const size_t fsm = sizeof(float2) * 2 * (size_t)na * nk;
+  const size_t fsm = kmesh_smem(kmesh_geom<float>(c->dims.kmesh, na));
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
   // FP32 twiddles, rounded from FP64 roots of unity
   float2 tw[3][OCN_MAX_KDIM];
@@ -716,8 +672,8 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi) {
   }
   {
     TimedScope ts(c, T_LR_FFT);
-    const size_t fsm = sizeof(float2) * 2 * (size_t)na * nk;
-    k_lr_fft_w_f32<<<nx, 256, fsm, c->stream>>>(m->phi, m->Wf, nk, nx, na);
+    const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na);
+    k_lr_fft_w_f32<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }
