@@ -138,6 +138,12 @@ def traffic_summary():
     return {}
 
 
+def describe(w) -> str:
+    k, x = w.kmesh, w.xmesh
+    return (f"Nk={w.nk} ({k[0]}x{k[1]}x{k[2]}), Nb={w.nb}, Nx={w.nx} ({x[0]}x{x[1]}x{x[2]}), "
+            f"Na={w.na}")
+
+
 def algorithmic_bytes(w, cls: str, precision: str) -> float:
     """Bytes one launch of a long-range kernel must move (read + write)."""
     nb, nk, nx, na = w.nb, w.nk, w.nx, w.na
@@ -200,7 +206,7 @@ def run_reference(args, ws, rank, pg):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded; u2 QR-orthonormal complex Gaussian, U(0,30) eV bands)",
-            "config": {"workload": f"{args.workload}: Nk=512 (8^3), Nb=100, Nx=1728 (12^3), Na=4",
+            "config": {"workload": f"{args.workload}: {describe(w)}",
                        "step": f"{sample_iters} Lanczos iterations (bounded sample of the "
                                f"{args.niter}-iteration Haydock run)"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
@@ -341,7 +347,7 @@ def run_ours(args, ws, rank, local, pg):
             "dtype": "f64" if args.precision == "fp64" else "bf16x2-split+f32 (contractions), f64 (vectors)",
             "data": "synthetic (seeded; u2 QR-orthonormal complex Gaussian, U(0,30) eV bands, "
                     "erf(r/0.5A)/(4r) W table)",
-            "config": {"workload": f"{args.workload}: Nk=512 (8^3), Nb=100, Nx=1728 (12^3), Na=4, "
+            "config": {"workload": f"{args.workload}: {describe(w)}, "
                                    f"{niter} Lanczos iterations + {ne + 1}-point spectrum per step",
                        "precision": args.precision, "parallelism": f"replicas x{ws}",
                        "l2": "inputs larger than L2 (u2 %.2f GB per contraction operand)" % (

@@ -225,6 +225,13 @@ int ocn_ctx_destroy(ocn_ctx* c) {
                   c->mult.d_jbeg, c->mult.amp, c->mult.amp_part, c->mult.hamp};
   for (void* p : bufs)
     if (p) cudaFree(p);
+  if (c->hay_exec) cudaGraphExecDestroy(c->hay_exec);
+  for (void* p : {(void*)c->hay_vec, (void*)c->hay_coef, (void*)c->d_iter})
+    if (p) cudaFree(p);
+  for (auto& ge : c->graph_events) {
+    cudaEventDestroy(ge.second.first);
+    cudaEventDestroy(ge.second.second);
+  }
   for (int k = 0; k < T_NCLASS; ++k)
     for (auto& pr : c->timing.pending[k]) {
       cudaEventDestroy(pr.first);
@@ -469,7 +476,11 @@ int ocn_set_mult(ocn_ctx* c, const ocn_mult_data* m) {
     }
   std::vector<double2> mh((size_t)jt);
   for (long long j = 0; j < jt; ++j) mh[j] = make_double2(m->mhr[j], m->mhi[j]);
-  // free a previous set
+  // free a previous set (a captured Haydock graph refers to the old buffers)
+  if (c->hay_exec) {
+    cudaGraphExecDestroy(c->hay_exec);
+    c->hay_exec = nullptr;
+  }
   void* old[] = {d.mpc, d.mpm, d.mh, d.p_l, d.p_m, d.p_nu, d.d_pfirst, d.d_nproj, d.d_jbeg,
                  d.amp, d.amp_part, d.hamp};
   for (void* p : old)
@@ -535,6 +546,54 @@ int ocn_apply_H(ocn_ctx* c, const double* ir, const double* ii, double* orr, dou
 
 // ----------------------------------------------------------------- Haydock
 
+namespace {
+
+// One Haydock iteration (OCEAN_haydock.f90:250-268): H*psi then the fused
+// two-term Lanczos update, for iteration index *d_iter (advanced first).
+int haydock_iteration(ocn_ctx* c, double* old, double* psi, double* h, double* ra, double* ia,
+                      double* rb) {
+  const size_t n = c->npsi;
+  int rc;
+  if ((rc = advance_iter(c, c->d_iter))) return rc;
+  c->acc_valid = false;
+  if (c->sys.mult && c->sys.nhflag[4] == 1 && c->have_mult) {
+    if ((rc = zero_acc(c)) || (rc = mult_apply(c, psi, psi + n))) return rc;
+    c->acc_valid = true;
+  }
+  if (c->sys.long_range && c->sys.nhflag[0] == 1) {
+    rc = (c->dims.precision == OCN_PREC_MIXED) ? lr_apply_mixed(c, psi, psi + n)
+                                               : lr_apply_fp64(c, psi, psi + n);
+    if (rc) return rc;
+  }
+  return lanczos_launch(c, old, old + n, psi, psi + n, h, h + n, ra, ia, rb, c->d_iter);
+}
+
+void drop_haydock_graph(ocn_ctx* c) {
+  if (c->hay_exec) cudaGraphExecDestroy(c->hay_exec);
+  c->hay_exec = nullptr;
+  for (auto& ge : c->graph_events) {
+    c->timing.pool.push_back(ge.second.first);
+    c->timing.pool.push_back(ge.second.second);
+  }
+  c->graph_events.clear();
+}
+
+unsigned long long haydock_key(const ocn_ctx* c) {
+  unsigned long long k = reinterpret_cast<uintptr_t>(c->hay_vec) ^
+                         (reinterpret_cast<uintptr_t>(c->hay_coef) << 1) ^ ((unsigned long long)c->hay_cap << 40);
+  k ^= (unsigned long long)(c->sys.mult ? 1 : 0) << 1;
+  k ^= (unsigned long long)(c->sys.long_range ? 1 : 0) << 2;
+  k ^= (unsigned long long)(c->sys.e0 ? 1 : 0) << 3;
+  k ^= (unsigned long long)(c->timing.on ? 1 : 0) << 4;
+  k ^= (unsigned long long)(c->have_mult ? 1 : 0) << 5;
+  k ^= (unsigned long long)(c->have_so ? 1 : 0) << 6;
+  k ^= (unsigned long long)(c->ei_nonzero ? 1 : 0) << 7;
+  for (int i = 0; i < 6; ++i) k ^= (unsigned long long)(c->sys.nhflag[i] & 1) << (8 + i);
+  return k;
+}
+
+}  // namespace
+
 int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter, double* real_a,
                     double* imag_a, double* real_b, int* niter_done) {
   if (!c || !p0r || !p0i || niter < 1 || !real_a || !real_b) return OCN_ERR_ARG;
@@ -542,59 +601,100 @@ int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter,
   int rc = require(c);
   if (rc) return rc;
   const size_t n = c->npsi;
-  double* vec = nullptr;
-  double* coef = nullptr;  // [real_a | imag_a | real_b], each niter+1
-  if ((rc = dev_alloc(c, &vec, 6 * n))) return rc;
-  if ((rc = dev_alloc(c, &coef, 3 * (size_t)(niter + 1)))) {
-    cudaFree(vec);
-    return rc;
+  if (!c->hay_vec && (rc = dev_alloc(c, &c->hay_vec, 6 * n))) return rc;
+  if (!c->d_iter && (rc = dev_alloc(c, &c->d_iter, 1))) return rc;
+  if (c->hay_cap < niter) {
+    drop_haydock_graph(c);
+    if (c->hay_coef) cudaFree(c->hay_coef);
+    c->hay_coef = nullptr;
+    c->hay_cap = 0;
+    if ((rc = dev_alloc(c, &c->hay_coef, 3 * (size_t)(niter + 1)))) return rc;
+    c->hay_cap = niter;
   }
-  double* ra = coef;
-  double* ia = coef + (niter + 1);
-  double* rb = coef + 2 * (niter + 1);
-  double* buf[3] = {vec, vec + 2 * n, vec + 4 * n};  // old, psi, h
-  cudaError_t e = cudaMemsetAsync(coef, 0, 3 * (size_t)(niter + 1) * sizeof(double), c->stream);
+  const size_t cap1 = (size_t)c->hay_cap + 1;
+  double* ra = c->hay_coef;
+  double* ia = c->hay_coef + cap1;
+  double* rb = c->hay_coef + 2 * cap1;
+  double* buf[3] = {c->hay_vec, c->hay_vec + 2 * n, c->hay_vec + 4 * n};  // old, psi, h
+  cudaError_t e = cudaMemsetAsync(c->hay_coef, 0, 3 * cap1 * sizeof(double), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d_iter, 0, sizeof(int), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(buf[0], 0, 2 * n * sizeof(double), c->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(buf[1], p0r, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(buf[1] + n, p0i, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  int done = 0;
-  for (int it = 1; it <= niter && e == cudaSuccess && rc == OCN_OK; ++it) {
-    double* old = buf[0];
-    double* psi = buf[1];
-    double* h = buf[2];
-    c->acc_valid = false;
-    if (c->sys.mult && c->sys.nhflag[4] == 1 && c->have_mult) {
-      if ((rc = zero_acc(c)) || (rc = mult_apply(c, psi, psi + n))) break;
-      c->acc_valid = true;
+  if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock setup");
+
+  // Three iterations rotate (old, psi, h) back to their starting roles, so one
+  // captured 3-iteration graph serves every launch.
+  const int ngraph = c->use_graphs ? niter / 3 : 0;
+  if (ngraph > 0) {
+    const unsigned long long key = haydock_key(c);
+    if (!c->hay_exec || key != c->hay_key) {
+      drop_haydock_graph(c);
+      OCN_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      c->capturing = true;
+      const long long l0 = c->launches;
+      double* b[3] = {buf[0], buf[1], buf[2]};
+      for (int r = 0; r < 3 && rc == OCN_OK; ++r) {
+        rc = haydock_iteration(c, b[0], b[1], b[2], ra, ia, rb);
+        double* t = b[0];
+        b[0] = b[1];
+        b[1] = b[2];
+        b[2] = t;
+      }
+      c->capturing = false;
+      cudaGraph_t graph = nullptr;
+      cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+      if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+      }
+      if (ce != cudaSuccess) return cuda_fail(c, ce, "cudaStreamEndCapture");
+      ce = cudaGraphInstantiate(&c->hay_exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) {
+        c->hay_exec = nullptr;
+        return cuda_fail(c, ce, "cudaGraphInstantiate");
+      }
+      c->hay_key = key;
+      c->hay_graph_kernels = c->launches - l0;
+      c->launches = l0;
     }
-    if (c->sys.long_range && c->sys.nhflag[0] == 1) {
-      rc = (c->dims.precision == OCN_PREC_MIXED) ? lr_apply_mixed(c, psi, psi + n)
-                                                 : lr_apply_fp64(c, psi, psi + n);
-      if (rc) break;
+    for (int g = 0; g < ngraph; ++g) {
+      OCN_CUDA(c, cudaGraphLaunch(c->hay_exec, c->stream));
+      c->launches += c->hay_graph_kernels;
     }
-    rc = lanczos_launch(c, old, old + n, psi, psi + n, h, h + n, rb + (it - 1), ra + (it - 1),
-                        ia + (it - 1), rb + it);
+  }
+  int done = 3 * ngraph;
+  for (int it = done + 1; it <= niter && rc == OCN_OK; ++it) {
+    rc = haydock_iteration(c, buf[0], buf[1], buf[2], ra, ia, rb);
     if (rc) break;
-    buf[0] = psi;  // old <- psi
-    buf[1] = h;    // psi <- h / b
-    buf[2] = old;
+    double* t = buf[0];
+    buf[0] = buf[1];  // old <- psi
+    buf[1] = buf[2];  // psi <- h / b
+    buf[2] = t;
     done = it;
   }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  std::vector<double> host(3 * (size_t)(niter + 1));
+  e = cudaStreamSynchronize(c->stream);
+  std::vector<double> host(3 * cap1);
   if (e == cudaSuccess)
-    e = cudaMemcpy(host.data(), coef, host.size() * sizeof(double), cudaMemcpyDeviceToHost);
-  cudaFree(vec);
-  cudaFree(coef);
+    e = cudaMemcpy(host.data(), c->hay_coef, host.size() * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock");
   if (rc) return rc;
+  if (c->timing.on && ngraph > 0)  // event pairs of the last graph replay
+    for (auto& ge : c->graph_events) {
+      float t = 0.0f;
+      if (cudaEventElapsedTime(&t, ge.second.first, ge.second.second) == cudaSuccess) {
+        c->timing.total_ms[ge.first] += t;
+        c->timing.count[ge.first] += 1;
+      }
+    }
   if (c->mixed && (rc = mixed_check(c))) return rc;
   for (int i = 0; i <= niter; ++i) {
     real_a[i] = host[i];
-    if (imag_a) imag_a[i] = host[(niter + 1) + i];
-    real_b[i] = host[2 * (niter + 1) + i];
+    if (imag_a) imag_a[i] = host[cap1 + i];
+    real_b[i] = host[2 * cap1 + i];
   }
   if (niter_done) *niter_done = done;
   // NaN check on a (OCEAN_haydock.f90:913-920): the reference stops at the first

@@ -96,6 +96,18 @@ struct ocn_ctx {
   ocn::MixedLR* mixed = nullptr;
 
   ocn::Timing timing;
+
+  // Haydock loop: persistent buffers and the captured 3-iteration CUDA graph
+  double* hay_vec = nullptr;   // old | psi | h, each 2*npsi
+  double* hay_coef = nullptr;  // real_a | imag_a | real_b, each hay_cap+1
+  int hay_cap = 0;
+  int* d_iter = nullptr;       // device iteration counter
+  cudaGraphExec_t hay_exec = nullptr;
+  unsigned long long hay_key = 0;
+  long long hay_graph_kernels = 0;
+  bool use_graphs = true;
+  bool capturing = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> graph_events;
 };
 
 namespace ocn {
@@ -120,11 +132,7 @@ struct TimedScope {
     b = take();
     if (a && b) cudaEventRecord(a, c->stream);
   }
-  ~TimedScope() {
-    if (!a || !b) return;
-    cudaEventRecord(b, c->stream);
-    c->timing.pending[cls].emplace_back(a, b);
-  }
+  ~TimedScope();
   cudaEvent_t take() {
     if (!c->timing.pool.empty()) {
       cudaEvent_t e = c->timing.pool.back();
@@ -136,6 +144,19 @@ struct TimedScope {
     return e;
   }
 };
+
+}  // namespace ocn
+
+// Closing event of a timed launch: kept for the next ocn_timing_read, or, while a
+// graph is being captured, attached to that graph (read after each replay).
+inline ocn::TimedScope::~TimedScope() {
+  if (!a || !b) return;
+  cudaEventRecord(b, c->stream);
+  if (c->capturing) c->graph_events.push_back({cls, {a, b}});
+  else c->timing.pending[cls].emplace_back(a, b);
+}
+
+namespace ocn {
 
 // ---- host setup (ocn_setup.cpp)
 void lrload_shift(const ocn_dims& d, double tau[3], const int ovr[3], int xshift[3]);
@@ -158,10 +179,12 @@ int combine(ocn_ctx* c, const double* d_pr, const double* d_pi, double* d_or, do
             const int* hflag, int backwards);
 int zero_acc(ocn_ctx* c);
 
-// Fused Lanczos step (combine + ocean_hay_ab_twoterm); coefficients stay on device.
+// Fused Lanczos step (combine + ocean_hay_ab_twoterm); coefficients stay on device,
+// indexed by the device iteration counter *itp (advanced by advance_iter).
 int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const double* psi_r,
-                   const double* psi_i, double* h_r, double* h_i, const double* bprev,
-                   double* a_out, double* ia_out, double* b_out);
+                   const double* psi_i, double* h_r, double* h_i, double* ra, double* ia,
+                   double* rb, const int* itp);
+int advance_iter(ocn_ctx* c, int* itp);
 
 // BLAS-1 helpers for GMRES (ocn_kernels.cu); vectors are [re plane | im plane]
 int vec_dot_dev(ocn_ctx* c, const double* p, const double* q, double* d_out);

@@ -121,6 +121,17 @@ __global__ void k_lr_fft_w_fp64(double2* __restrict__ phi, const double* __restr
   kmesh_convolve<double>(phi, W, nx, blockIdx.x, g, buf, tw);
 }
 
+template <int N, int NA>
+__global__ void k_fft_cube_fp64(double2* __restrict__ phi, const double* __restrict__ W, int nx) {
+  extern __shared__ double2 smem[];
+  double2* tw = smem;
+  double2* buf = smem + 3 * OCN_MAX_KDIM;
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_tw[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
+  __syncthreads();
+  kmesh_convolve_cube<double, N, NA>(phi, W, nx, blockIdx.x, buf, tw);
+}
+typedef void (*CubeFnD)(double2*, const double*, int);
+
 // ------------------------------------------------------ LR: x-mesh -> band
 
 // part[split][re|im][a][k][n] = - sum_{x in split} conj(u(n,k,x)) phi'(k,x,a)
@@ -178,6 +189,7 @@ __global__ void k_lr_gemm2_fp64(const double2* __restrict__ u, const double2* __
 //             + sum_jc S(ic,jc) psi(n,k,jc)        (OCEAN_action.f90:337-372,596-608)
 // Optionally fused with the first Lanczos stage (ocean_hay_ab_twoterm,
 // OCEAN_haydock.f90:848-860): out -= b_{i-1} old, partial <out|psi>.
+template <int NA>
 __global__ void k_combine(const double* __restrict__ pr, const double* __restrict__ pi,
                           const double* __restrict__ er, const double* __restrict__ ei,
                           const double* __restrict__ allow, const double* __restrict__ acc,
@@ -185,22 +197,21 @@ __global__ void k_combine(const double* __restrict__ pr, const double* __restric
                           double* __restrict__ outr, double* __restrict__ outi, int nbk, int na,
                           size_t npsi, int use_e0, int use_so, int backwards,
                           const double* __restrict__ oldr, const double* __restrict__ oldi,
-                          const double* __restrict__ bprev, double* __restrict__ red) {
+                          const double* __restrict__ rb_base, const int* __restrict__ itp,
+                          double* __restrict__ red) {
   __shared__ double sh[2][32];
   double dr = 0.0, di = 0.0;
   double bm = 0.0;
-  if (oldr) bm = -(*bprev);
+  if (oldr) bm = -rb_base[*itp - 1];  // b_{i-1}
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nbk; e += gridDim.x * blockDim.x) {
-    double qr[OCN_MAX_NA], qi[OCN_MAX_NA];
+    double qr[NA], qi[NA];
 #pragma unroll
-    for (int a = 0; a < OCN_MAX_NA; ++a)
-      if (a < na) {
-        qr[a] = pr[e + (size_t)nbk * a];
-        qi[a] = pi[e + (size_t)nbk * a];
-      }
+    for (int a = 0; a < NA; ++a) {
+      qr[a] = pr[e + (size_t)nbk * a];
+      qi[a] = pi[e + (size_t)nbk * a];
+    }
 #pragma unroll
-    for (int ic = 0; ic < OCN_MAX_NA; ++ic) {
-      if (ic >= na) break;
+    for (int ic = 0; ic < NA; ++ic) {
       const size_t idx = e + (size_t)nbk * ic;
       double fr = 0.0, fi = 0.0;
       if (acc) {
@@ -215,8 +226,9 @@ __global__ void k_combine(const double* __restrict__ pr, const double* __restric
       fr *= m;
       fi *= m;
       if (use_so) {
-        for (int jc = 0; jc < na; ++jc) {
-          const double2 sv = so[jc * na + ic];
+#pragma unroll
+        for (int jc = 0; jc < NA; ++jc) {
+          const double2 sv = so[jc * NA + ic];
           if (backwards) {
             fr = fr + sv.x * qr[jc] + sv.y * qi[jc];
             fi = fi + sv.x * qi[jc] - sv.y * qr[jc];
@@ -325,16 +337,21 @@ __device__ __forceinline__ void block_partial(double v0, double v1, double* __re
   }
 }
 
+// Iteration counter of the device-resident Lanczos loop (coefficient index i).
+__global__ void k_advance(int* __restrict__ itp) { *itp += 1; }
+
 // Lanczos stage 2: a_{i-1} = Re<h|psi>; h -= a psi; partial |h|^2.
 __global__ void k_lanczos2(const double* __restrict__ red1, int nblk, double* __restrict__ hr,
                            double* __restrict__ hi, const double* __restrict__ pr,
                            const double* __restrict__ pi, size_t n, double* __restrict__ red2,
-                           double* __restrict__ coef_a, double* __restrict__ coef_ia) {
+                           double* __restrict__ ra_base, double* __restrict__ ia_base,
+                           const int* __restrict__ itp) {
   double a, ia;
   reduce_pairs(red1, nblk, &a, &ia);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    *coef_a = a;
-    *coef_ia = ia;
+    const int it = *itp;
+    ra_base[it - 1] = a;
+    ia_base[it - 1] = ia;
   }
   const double am = -a;
   double s = 0.0;
@@ -352,11 +369,12 @@ __global__ void k_lanczos2(const double* __restrict__ red1, int nblk, double* __
 
 // Lanczos stage 3: b_i = sqrt(sum); psi_new = h / b_i (in place in h).
 __global__ void k_lanczos3(const double* __restrict__ red2, int nblk, double* __restrict__ hr,
-                           double* __restrict__ hi, size_t n, double* __restrict__ coef_b) {
+                           double* __restrict__ hi, size_t n, double* __restrict__ rb_base,
+                           const int* __restrict__ itp) {
   double bb, dummy;
   reduce_pairs(red2, nblk, &bb, &dummy);
   const double b = sqrt(bb);
-  if (blockIdx.x == 0 && threadIdx.x == 0) *coef_b = b;
+  if (blockIdx.x == 0 && threadIdx.x == 0) rb_base[*itp] = b;
   const double inv = 1.0 / b;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
        e += (size_t)gridDim.x * blockDim.x) {
@@ -711,6 +729,11 @@ int kernels_init(ocn_ctx* c) {
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_gemm1_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g1));
   const size_t ff = kmesh_smem(kmesh_geom<double>(c->dims.kmesh, c->na));
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff));
+  if (kmesh_cube_supported(c->dims.kmesh, c->na)) {
+    CubeFnD f;
+    OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], c->na, f);
+    OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff));
+  }
   const size_t ma = sizeof(double2) * (size_t)c->na * 256;
   OCN_CUDA(c, cudaFuncSetAttribute(k_mult_amp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ma));
   return OCN_OK;
@@ -745,7 +768,12 @@ int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi) {
   {
     const KmeshGeom<double> g = kmesh_geom<double>(c->dims.kmesh, na);
     TimedScope ts(c, T_LR_FFT);
-    k_lr_fft_w_fp64<<<nx, 256, kmesh_smem(g), c->stream>>>(c->d_phi, c->d_W, nx, g);
+    CubeFnD f = nullptr;
+    if (kmesh_cube_supported(c->dims.kmesh, na)) OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], na, f);
+    if (f)
+      f<<<nx, 128, kmesh_smem(g), c->stream>>>(c->d_phi, c->d_W, nx);
+    else
+      k_lr_fft_w_fp64<<<nx, 256, kmesh_smem(g), c->stream>>>(c->d_phi, c->d_W, nx, g);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }
@@ -807,39 +835,47 @@ int combine(ocn_ctx* c, const double* d_pr, const double* d_pi, double* d_or, do
   const int nbk = c->nb * c->nk;
   const int use_so = (c->sys.mult && hflag[5] == 1 && c->have_so) ? 1 : 0;
   const int nparts = (c->sys.long_range && hflag[0] == 1) ? c->lr_xsplit : 0;
-  k_combine<<<grid_for(nbk, 256, 4 * c->sm_count), 256, 0, c->stream>>>(
+  auto kern = (c->na == 4) ? k_combine<4> : k_combine<12>;
+  kern<<<grid_for(nbk, 256, 4 * c->sm_count), 256, 0, c->stream>>>(
       d_pr, d_pi, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow,
       c->acc_valid ? c->d_acc : nullptr, c->d_accpart, nparts,
       c->d_so, d_or, d_oi, nbk, c->na, c->npsi, c->sys.e0, use_so, backwards, nullptr, nullptr,
-      nullptr, nullptr);
+      nullptr, nullptr, nullptr);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;
 }
 
-// The Lanczos step is launched from ocn_solvers.cu through this helper, which
-// knows the coefficient array layout.
+// Fused combine + ocean_hay_ab_twoterm for iteration i = *itp: reads b_{i-1} from
+// rb, writes a_{i-1}, Im a_{i-1} and b_i (OCEAN_haydock.f90:848-889).
 int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const double* psi_r,
-                   const double* psi_i, double* h_r, double* h_i, const double* bprev,
-                   double* a_out, double* ia_out, double* b_out) {
+                   const double* psi_i, double* h_r, double* h_i, double* ra, double* ia,
+                   double* rb, const int* itp) {
   const int nbk = c->nb * c->nk;
   const int* hf = c->sys.nhflag;
   const int use_so = (c->sys.mult && hf[5] == 1 && c->have_so) ? 1 : 0;
   const int nparts = (c->sys.long_range && hf[0] == 1) ? c->lr_xsplit : 0;
   const int nblk = c->red_blocks;
   TimedScope ts(c, T_LANCZOS);
-  k_combine<<<nblk, 256, 0, c->stream>>>(psi_r, psi_i, c->d_er, c->ei_nonzero ? c->d_ei : nullptr,
-                                         c->d_allow, c->acc_valid ? c->d_acc : nullptr,
-                                         c->d_accpart, nparts, c->d_so, h_r, h_i, nbk,
-                                         c->na, c->npsi, c->sys.e0, use_so, 0, old_r, old_i, bprev,
-                                         c->d_red);
+  auto kern = (c->na == 4) ? k_combine<4> : k_combine<12>;
+  kern<<<nblk, 256, 0, c->stream>>>(psi_r, psi_i, c->d_er, c->ei_nonzero ? c->d_ei : nullptr,
+                                    c->d_allow, c->acc_valid ? c->d_acc : nullptr, c->d_accpart,
+                                    nparts, c->d_so, h_r, h_i, nbk, c->na, c->npsi, c->sys.e0,
+                                    use_so, 0, old_r, old_i, rb, itp, c->d_red);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   k_lanczos2<<<nblk, 256, 0, c->stream>>>(c->d_red, nblk, h_r, h_i, psi_r, psi_i, c->npsi,
-                                          c->d_red + 2 * nblk, a_out, ia_out);
+                                          c->d_red + 2 * nblk, ra, ia, itp);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
-  k_lanczos3<<<nblk, 256, 0, c->stream>>>(c->d_red + 2 * nblk, nblk, h_r, h_i, c->npsi, b_out);
+  k_lanczos3<<<nblk, 256, 0, c->stream>>>(c->d_red + 2 * nblk, nblk, h_r, h_i, c->npsi, rb, itp);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
+int advance_iter(ocn_ctx* c, int* itp) {
+  k_advance<<<1, 1, 0, c->stream>>>(itp);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;

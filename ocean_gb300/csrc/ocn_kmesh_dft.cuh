@@ -163,6 +163,194 @@ __device__ __forceinline__ void dft_pass(typename C2<R>::T* buf, const KmeshGeom
   }
 }
 
+// --------------------------------------------------------------------------
+// Compile-time specialisation for cubic meshes n^3 and NA transforms per x:
+// every index computation folds to shifts and multiplies, and 2/4/8-point lines
+// use radix-2 butterflies (sgn = +1 backward, -1 forward).
+
+template <typename CT, typename R>
+__device__ __forceinline__ CT cadd(CT a, CT b) {
+  CT r;
+  r.x = a.x + b.x;
+  r.y = a.y + b.y;
+  return r;
+}
+template <typename CT, typename R>
+__device__ __forceinline__ CT csub(CT a, CT b) {
+  CT r;
+  r.x = a.x - b.x;
+  r.y = a.y - b.y;
+  return r;
+}
+// (sgn * i) * z
+template <typename CT, typename R>
+__device__ __forceinline__ CT cmul_si(CT z, R sgn) {
+  CT r;
+  r.x = -sgn * z.y;
+  r.y = sgn * z.x;
+  return r;
+}
+
+template <typename CT, typename R, int N>
+__device__ __forceinline__ void line_dft(CT (&v)[N], const CT* __restrict__ tw, R sgn) {
+  if constexpr (N == 2) {
+    const CT a = v[0], b = v[1];
+    v[0] = cadd<CT, R>(a, b);
+    v[1] = csub<CT, R>(a, b);
+  } else if constexpr (N == 4) {
+    const CT s02 = cadd<CT, R>(v[0], v[2]), d02 = csub<CT, R>(v[0], v[2]);
+    const CT s13 = cadd<CT, R>(v[1], v[3]), d13 = cmul_si<CT, R>(csub<CT, R>(v[1], v[3]), sgn);
+    v[0] = cadd<CT, R>(s02, s13);
+    v[2] = csub<CT, R>(s02, s13);
+    v[1] = cadd<CT, R>(d02, d13);
+    v[3] = csub<CT, R>(d02, d13);
+  } else if constexpr (N == 8) {
+    CT e[4] = {v[0], v[2], v[4], v[6]};
+    CT o[4] = {v[1], v[3], v[5], v[7]};
+    line_dft<CT, R, 4>(e, tw, sgn);
+    line_dft<CT, R, 4>(o, tw, sgn);
+    const R h = (R)0.70710678118654752440;  // cos(pi/4)
+    // w^m = exp(sgn i pi m / 4), m = 1..3
+    CT t1, t2, t3;
+    t1.x = h * (o[1].x - sgn * o[1].y);
+    t1.y = h * (o[1].y + sgn * o[1].x);
+    t2 = cmul_si<CT, R>(o[2], sgn);
+    t3.x = -h * (o[3].x + sgn * o[3].y);
+    t3.y = h * (sgn * o[3].x - o[3].y);
+    v[0] = cadd<CT, R>(e[0], o[0]);
+    v[4] = csub<CT, R>(e[0], o[0]);
+    v[1] = cadd<CT, R>(e[1], t1);
+    v[5] = csub<CT, R>(e[1], t1);
+    v[2] = cadd<CT, R>(e[2], t2);
+    v[6] = csub<CT, R>(e[2], t2);
+    v[3] = cadd<CT, R>(e[3], t3);
+    v[7] = csub<CT, R>(e[3], t3);
+  } else {
+    CT w[N];
+#pragma unroll
+    for (int t = 0; t < N; ++t) {
+      w[t] = tw[t];
+      w[t].y *= sgn;
+    }
+    CT out[N];
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      R sr = v[0].x, si = v[0].y;
+#pragma unroll
+      for (int j = 1; j < N; ++j) {
+        const CT ww = w[(j * m) % N];
+        sr += v[j].x * ww.x - v[j].y * ww.y;
+        si += v[j].x * ww.y + v[j].y * ww.x;
+      }
+      out[m].x = sr;
+      out[m].y = si;
+    }
+#pragma unroll
+    for (int m = 0; m < N; ++m) v[m] = out[m];
+  }
+}
+
+template <typename R, int N, int NA>
+__device__ __forceinline__ void cube_pass(typename C2<R>::T* buf, int ax,
+                                          const typename C2<R>::T* __restrict__ tw, R sgn) {
+  typedef typename C2<R>::T CT;
+  constexpr int P3 = N + 1;
+  constexpr int SLAB = N * N * P3;
+  constexpr int LINES = NA * N * N;
+  const int st = (ax == 2) ? 1 : ((ax == 1) ? P3 : N * P3);
+  for (int l = threadIdx.x; l < LINES; l += blockDim.x) {
+    const int a = l / (N * N);
+    const int r = l % (N * N);
+    const int i1 = r / N, i2 = r % N;
+    int base;
+    if (ax == 0) base = i1 * P3 + i2;
+    else if (ax == 1) base = i1 * N * P3 + i2;
+    else base = (i1 * N + i2) * P3;
+    CT* p = buf + a * SLAB + base;
+    CT v[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) v[j] = p[j * st];
+    line_dft<CT, R, N>(v, tw, sgn);
+#pragma unroll
+    for (int j = 0; j < N; ++j) p[j * st] = v[j];
+  }
+}
+
+template <typename R, int N, int NA>
+__device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R* __restrict__ W, int nx,
+                                    int x, typename C2<R>::T* buf, const typename C2<R>::T* __restrict__ tw) {
+  typedef typename C2<R>::T CT;
+  constexpr int NK = N * N * N;
+  constexpr int P3 = N + 1;
+  constexpr int SLAB = N * N * P3;
+  for (int e = threadIdx.x; e < NA * NK; e += blockDim.x) {
+    const int k = e / NA, a = e % NA;
+    const int k3 = k % N;
+    buf[a * SLAB + (k / N) * P3 + k3] = phi[((size_t)k * nx + x) * NA + a];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    cube_pass<R, N, NA>(buf, ax, tw + ax * OCN_MAX_KDIM, (R)1);
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < NA * NK; e += blockDim.x) {
+    const int a = e / NK, k = e % NK;
+    const R wv = W[(size_t)x * NK + k];
+    CT& v = buf[a * SLAB + (k / N) * P3 + k % N];
+    v.x *= wv;
+    v.y *= wv;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    cube_pass<R, N, NA>(buf, ax, tw + ax * OCN_MAX_KDIM, (R)-1);
+    __syncthreads();
+  }
+  const R norm = (R)1 / (R)NK;
+  for (int e = threadIdx.x; e < NA * NK; e += blockDim.x) {
+    const int k = e / NA, a = e % NA;
+    const CT v = buf[a * SLAB + (k / N) * P3 + k % N];
+    CT o;
+    o.x = v.x * norm;
+    o.y = v.y * norm;
+    phi[((size_t)k * nx + x) * NA + a] = o;
+  }
+}
+
+// A cubic specialisation exists for these extents and transform counts.
+inline bool kmesh_cube_supported(const int kmesh[3], int na) {
+  if (kmesh[0] != kmesh[1] || kmesh[1] != kmesh[2]) return false;
+  const int n = kmesh[0];
+  return (na == 4 || na == 12) && (n == 2 || n == 3 || n == 4 || n == 5 || n == 6 || n == 8);
+}
+
+// Selects the instantiation kern<N, NA> of a kernel template for a supported
+// cubic mesh (kmesh_cube_supported); returns nullptr otherwise.
+#define OCN_CUBE_DISPATCH(KERN, n, na, out)                                      \
+  do {                                                                           \
+    out = nullptr;                                                               \
+    if ((na) == 4) {                                                             \
+      switch (n) {                                                               \
+        case 2: out = KERN<2, 4>; break;                                         \
+        case 3: out = KERN<3, 4>; break;                                         \
+        case 4: out = KERN<4, 4>; break;                                         \
+        case 5: out = KERN<5, 4>; break;                                         \
+        case 6: out = KERN<6, 4>; break;                                         \
+        case 8: out = KERN<8, 4>; break;                                         \
+      }                                                                          \
+    } else if ((na) == 12) {                                                     \
+      switch (n) {                                                               \
+        case 2: out = KERN<2, 12>; break;                                        \
+        case 3: out = KERN<3, 12>; break;                                        \
+        case 4: out = KERN<4, 12>; break;                                        \
+        case 5: out = KERN<5, 12>; break;                                        \
+        case 6: out = KERN<6, 12>; break;                                        \
+        case 8: out = KERN<8, 12>; break;                                        \
+      }                                                                          \
+    }                                                                            \
+  } while (0)
+
 // Whole k-mesh step for the x-point of this CTA.  phi layout [k][x][a].
 // twiddles: tw + ax*OCN_MAX_KDIM.
 template <typename R>

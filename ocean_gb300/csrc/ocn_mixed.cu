@@ -480,6 +480,17 @@ __global__ void k_lr_fft_w_f32(float2* __restrict__ phi, const float* __restrict
   kmesh_convolve<float>(phi, W, nx, blockIdx.x, g, buf, tw);
 }
 
+template <int N, int NA>
+__global__ void k_fft_cube_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx) {
+  extern __shared__ float2 fsm[];
+  float2* tw = fsm;
+  float2* buf = fsm + 3 * OCN_MAX_KDIM;
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_twf[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
+  __syncthreads();
+  kmesh_convolve_cube<float, N, NA>(phi, W, nx, blockIdx.x, buf, tw);
+}
+typedef void (*CubeFnF)(float2*, const float*, int);
+
 __global__ void k_w_to_f32(const double* __restrict__ W, float* __restrict__ Wf, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     Wf[i] = (float)W[i];
@@ -503,6 +514,8 @@ struct MixedLR {
   TcParams g1{}, g2{};
   int grid1 = 1, grid2 = 1;
   size_t smem_bytes = 0;
+  void* cube_fn = nullptr;  // specialised k-mesh kernel (CubeFnF), or null
+  size_t cube_smem = 0;
   bool ready = false;
 };
 
@@ -598,6 +611,13 @@ int mixed_init(ocn_ctx* c) {
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->smem_bytes));
   const size_t fsm = kmesh_smem(kmesh_geom<float>(c->dims.kmesh, na));
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+  if (kmesh_cube_supported(c->dims.kmesh, na)) {
+    CubeFnF f;
+    OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], na, f);
+    m->cube_fn = reinterpret_cast<void*>(f);
+    m->cube_smem = fsm;
+    OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+  }
   // FP32 twiddles, rounded from FP64 roots of unity
   float2 tw[3][OCN_MAX_KDIM];
   const double pi = 3.1415926535897932384626433832795;
@@ -672,8 +692,12 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi) {
   }
   {
     TimedScope ts(c, T_LR_FFT);
-    const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na);
-    k_lr_fft_w_f32<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g);
+    if (m->cube_fn) {
+      reinterpret_cast<CubeFnF>(m->cube_fn)<<<nx, 128, m->cube_smem, c->stream>>>(m->phi, m->Wf, nx);
+    } else {
+      const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na);
+      k_lr_fft_w_f32<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g);
+    }
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }

@@ -144,6 +144,29 @@ def test_haydock_nan_returns_reference_ierr(built):
         ctx.close()
 
 
+@pytest.mark.parametrize("prec", [capi.OCN_PREC_FP64, capi.OCN_PREC_MIXED])
+def test_haydock_graph_replay_deterministic(built, prec):
+    """The captured 3-iteration graph plus the remainder iterations give the same
+    coefficients on every call (deterministic reductions), for counts that are and
+    are not multiples of three, and match the oracle's first coefficients."""
+    _, O = built
+    w, P = problem("small", O, seed=12)
+    ctx = capi.Context(w, precision=prec)
+    try:
+        r1 = ctx.haydock(31)
+        r2 = ctx.haydock(31)
+        r3 = ctx.haydock(30)
+        r4 = ctx.haydock(2)
+    finally:
+        ctx.close()
+    assert all(np.array_equal(a, b) for a, b in zip(r1[:3], r2[:3]))
+    assert np.array_equal(r1[0][:30], r3[0][:30]) and np.array_equal(r1[2][:31], r3[2][:31])
+    assert np.array_equal(r1[0][:2], r4[0][:2])
+    _, ora, oia, orb, _ = P.haydock(31)
+    tol = 1e-12 if prec == capi.OCN_PREC_FP64 else 1e-4
+    assert np.max(np.abs(r1[0][:10] - ora[:10]) / np.abs(ora[:10])) < tol
+
+
 @pytest.mark.parametrize("photon", [1, 5])
 def test_spectrum_cf_reproduces_reference_golden(built, photon):
     _, O = built
