@@ -257,9 +257,7 @@ def run_ours(args, ws, rank, local, pg):
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
 
     _device_steps(ctx, w, niter, ne, pr_ptr, pi_ptr, args.warmup, stream, torch)
-    # ---- timed region (inputs resident in HBM)
-    ctx.timing(True)
-    ctx.timing_reset()
+    # ---- timed region (inputs resident in HBM, no instrumentation)
     if pg is not None:
         pg.barrier()
     torch.cuda.synchronize()
@@ -271,6 +269,11 @@ def run_ours(args, ws, rank, local, pg):
         pg.barrier()
     clocks = sampler.stop()
     launches = ctx.launches - l0
+    # ---- one instrumented step: CUDA events around every timed kernel on the
+    #      library's stream (event-record nodes inside the captured graph)
+    ctx.timing(True)
+    ctx.timing_reset()
+    _device_steps(ctx, w, niter, ne, pr_ptr, pi_ptr, 1, stream, torch)
     kt = ctx.timing_read()
     ctx.timing(False)
     if pg is not None:

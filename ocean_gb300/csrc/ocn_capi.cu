@@ -561,7 +561,8 @@ int haydock_iteration(ocn_ctx* c, double* old, double* psi, double* h, double* r
     c->acc_valid = true;
   }
   if (c->sys.long_range && c->sys.nhflag[0] == 1) {
-    rc = (c->dims.precision == OCN_PREC_MIXED) ? lr_apply_mixed(c, psi, psi + n)
+    // mixed: the psi operand was built by the previous normalisation (or before the loop)
+    rc = (c->dims.precision == OCN_PREC_MIXED) ? lr_apply_mixed(c, psi, psi + n, true)
                                                : lr_apply_fp64(c, psi, psi + n);
     if (rc) return rc;
   }
@@ -624,6 +625,7 @@ int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter,
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(buf[1] + n, p0i, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock setup");
+  if (c->dims.precision == OCN_PREC_MIXED && (rc = mixed_prep_b1(c, buf[1], buf[1] + n))) return rc;
 
   // Three iterations rotate (old, psi, h) back to their starting roles, so one
   // captured 3-iteration graph serves every launch.
@@ -682,7 +684,7 @@ int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter,
     e = cudaMemcpy(host.data(), c->hay_coef, host.size() * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock");
   if (rc) return rc;
-  if (c->timing.on && ngraph > 0)  // event pairs of the last graph replay
+  if (c->timing.on && ngraph > 0) {  // event pairs of the last graph replay
     for (auto& ge : c->graph_events) {
       float t = 0.0f;
       if (cudaEventElapsedTime(&t, ge.second.first, ge.second.second) == cudaSuccess) {
@@ -690,6 +692,8 @@ int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter,
         c->timing.count[ge.first] += 1;
       }
     }
+    (void)cudaGetLastError();  // a failed timing query must not poison later calls
+  }
   if (c->mixed && (rc = mixed_check(c))) return rc;
   for (int i = 0; i <= niter; ++i) {
     real_a[i] = host[i];

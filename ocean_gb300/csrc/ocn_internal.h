@@ -130,7 +130,12 @@ struct TimedScope {
     if (!c->timing.on) return;
     a = take();
     b = take();
-    if (a && b) cudaEventRecord(a, c->stream);
+    if (a && b) record(a);
+  }
+  // Inside stream capture only an "external" record becomes an event-record node.
+  void record(cudaEvent_t e) {
+    if (c->capturing) cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal);
+    else cudaEventRecord(e, c->stream);
   }
   ~TimedScope();
   cudaEvent_t take() {
@@ -151,7 +156,7 @@ struct TimedScope {
 // graph is being captured, attached to that graph (read after each replay).
 inline ocn::TimedScope::~TimedScope() {
   if (!a || !b) return;
-  cudaEventRecord(b, c->stream);
+  record(b);
   if (c->capturing) c->graph_events.push_back({cls, {a, b}});
   else c->timing.pending[cls].emplace_back(a, b);
 }
@@ -208,7 +213,12 @@ int cf_eval(const double* ra, const double* ia, const double* rb, int iter, doub
 int mixed_init(ocn_ctx* c);
 int mixed_free(ocn_ctx* c);
 int mixed_set_bloch(ocn_ctx* c);   // builds split-BF16 layouts from d_u
-int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi);  // writes d_accpart
+// writes d_accpart; b1_ready: the psi operand was already built (fused Lanczos step)
+int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, bool b1_ready = false);
+int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi);
+// b_i = sqrt(partials), psi = h / b_i, and the psi operand of the next action
+int mixed_norm_prep(ocn_ctx* c, const double* red2, int nblk, double* hr, double* hi, double* rb,
+                    const int* itp);
 int mixed_check(ocn_ctx* c);       // reads and clears the device timeout flag
 
 }  // namespace ocn

@@ -868,6 +868,8 @@ int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const d
                                           c->d_red + 2 * nblk, ra, ia, itp);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
+  if (c->dims.precision == OCN_PREC_MIXED && c->mixed)  // also builds the next psi operand
+    return mixed_norm_prep(c, c->d_red + 2 * nblk, nblk, h_r, h_i, rb, itp);
   k_lanczos3<<<nblk, 256, 0, c->stream>>>(c->d_red + 2 * nblk, nblk, h_r, h_i, c->npsi, rb, itp);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());

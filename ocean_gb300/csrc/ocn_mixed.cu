@@ -438,6 +438,55 @@ __global__ void k_prep_b1(const double* __restrict__ pr, const double* __restric
   }
 }
 
+// Lanczos normalisation fused with the next action's psi operand
+// (OCEAN_haydock.f90:880-889 then long_range.f90:897-906): b_i = sqrt(sum of
+// partials), psi = h / b_i written in place, and B1 built from allow o psi.
+// One thread per (n, k) covers both K = n and K = Nb + n for every alpha.
+__global__ void k_norm_prep(const double* __restrict__ red2, int nblk, double* __restrict__ hr,
+                            double* __restrict__ hi, const double* __restrict__ allow,
+                            __nv_bfloat16* __restrict__ b1, int nb, int nk, int na, int p1,
+                            double* __restrict__ rb_base, const int* __restrict__ itp) {
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) s += red2[2 * i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  double bb = 0.0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) bb += sh[i];
+  const double b = sqrt(bb);
+  if (blockIdx.x == 0 && threadIdx.x == 0) rb_base[*itp] = b;
+  const double inv = 1.0 / b;
+  const int n4 = 4 * na;
+  const int total = nb * nk;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int n = i % nb;
+    const int k = i / nb;
+    __nv_bfloat16* base = b1 + (size_t)k * n4 * p1;
+    for (int a = 0; a < na; ++a) {
+      const size_t idx = (size_t)i + (size_t)total * a;
+      const double r = hr[idx] * inv, im = hi[idx] * inv;
+      hr[idx] = r;
+      hi[idx] = im;
+      const double m = allow[idx];
+      const float qr = (float)(r * m), qi = (float)(im * m);
+      __nv_bfloat16 h0, l0, h1, l1, h2, l2;
+      split_bf16(qr, h0, l0);
+      split_bf16(qi, h1, l1);
+      split_bf16(-qi, h2, l2);
+      // K = n (c = 0): part 0 <- qr, part 1 <- qi;  K = Nb + n (c = 1): part 0 <- -qi, part 1 <- qr
+      base[(size_t)(a)*p1 + n] = h0;
+      base[(size_t)(na + a) * p1 + n] = h1;
+      base[(size_t)(2 * na + a) * p1 + n] = l0;
+      base[(size_t)(3 * na + a) * p1 + n] = l1;
+      base[(size_t)(a)*p1 + nb + n] = h2;
+      base[(size_t)(na + a) * p1 + nb + n] = h0;
+      base[(size_t)(2 * na + a) * p1 + nb + n] = l2;
+      base[(size_t)(3 * na + a) * p1 + nb + n] = l0;
+    }
+  }
+}
+
 // B2[k][j][K2] from phi'[k][x][a]:
 //   part 0 (Re out): K=(0,x) -> Re phi', K=(1,x) -> Im phi'
 //   part 1 (Im out): K=(0,x) -> Im phi', K=(1,x) -> -Re phi'
@@ -672,11 +721,32 @@ int mixed_check(ocn_ctx* c) {
   return OCN_OK;
 }
 
-int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi) {
+int mixed_norm_prep(ocn_ctx* c, const double* red2, int nblk, double* hr, double* hi, double* rb,
+                    const int* itp) {
+  MixedLR* m = c->mixed;  // timed as part of the enclosing Lanczos step
+  k_norm_prep<<<nblk, 256, 0, c->stream>>>(red2, nblk, hr, hi, c->d_allow, m->b1, c->nb, c->nk, c->na,
+                                           m->p1, rb, itp);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
+int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi) {
+  MixedLR* m = c->mixed;
+  TimedScope ts(c, T_LR_PREP);
+  const int total = c->nk * 2 * c->nb;
+  k_prep_b1<<<std::min((total + 255) / 256, 8 * c->sm_count), 256, 0, c->stream>>>(
+      d_pr, d_pi, c->d_allow, m->b1, c->nb, c->nk, c->na, m->p1);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
+int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, bool b1_ready) {
   MixedLR* m = c->mixed;
   if (!m || !m->ready) return set_err(c, OCN_ERR_STATE, "mixed-precision operands not built");
   const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na;
-  {
+  if (!b1_ready) {
     TimedScope ts(c, T_LR_PREP);
     const int total = nk * 2 * nb;
     k_prep_b1<<<std::min((total + 255) / 256, 8 * c->sm_count), 256, 0, c->stream>>>(

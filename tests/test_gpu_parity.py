@@ -154,11 +154,17 @@ def test_haydock_graph_replay_deterministic(built, prec):
     ctx = capi.Context(w, precision=prec)
     try:
         r1 = ctx.haydock(31)
+        ctx.timing(True)  # graph re-captured with event-record nodes
         r2 = ctx.haydock(31)
+        kt = ctx.timing_read()
+        ctx.timing(False)
         r3 = ctx.haydock(30)
         r4 = ctx.haydock(2)
+        # no stale CUDA error leaks into the next library call
+        capi.spectrum_cf(r2[0], r2[1], r2[2], 31, w.kpref, w.el, w.eh, 50, w.gam0)
     finally:
         ctx.close()
+    assert kt["combine_lanczos"][0] >= 3 and kt["lr_band_to_x"][1] > 0.0
     assert all(np.array_equal(a, b) for a, b in zip(r1[:3], r2[:3]))
     assert np.array_equal(r1[0][:30], r3[0][:30]) and np.array_equal(r1[2][:31], r3[2][:31])
     assert np.array_equal(r1[0][:2], r4[0][:2])
