@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--workload", default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--gmres-omega", type=int, default=200,
+                    help="energies of the GMRES leg (0 disables it)")
     return ap.parse_args()
 
 
@@ -144,18 +146,31 @@ def describe(w) -> str:
             f"Na={w.na}")
 
 
-def algorithmic_bytes(w, cls: str, precision: str) -> float:
-    """Bytes one launch of a long-range kernel must move (read + write)."""
+def algorithmic_bytes(w, cls: str, precision: str, ksplit: int = 2) -> float:
+    """Bytes one launch of a long-range kernel must move (read + write).
+
+    FP64 path: u2 (16 B/complex), psi in, phi out (16 B/complex).
+    Mixed path: u2 as split-bf16 (8 B/complex); the psi operand B1 and the phi'
+    operand B2 are split-bf16 tiles of 4*Na rows; band->x writes FP32 phi; x->band
+    writes ksplit FP64 partial planes."""
     nb, nk, nx, na = w.nb, w.nk, w.nx, w.na
-    ubytes = nb * nk * nx * w.nspn * (16 if precision == "fp64" else 8)
-    phi = nk * nx * na * (16 if precision == "fp64" else 8)
     psi = 2 * nb * nk * na * 8
+    if precision == "fp64":
+        ubytes = nb * nk * nx * w.nspn * 16
+        phi = nk * nx * na * 16
+        if cls in ("lr_band_to_x", "lr_x_to_band"):
+            return ubytes + psi + phi
+        if cls == "lr_kmesh_transform":
+            return 2 * phi + nk * nx * 8
+        return float("nan")
+    ubytes = nb * nk * nx * 8
+    phi = nk * nx * na * 8
     if cls == "lr_band_to_x":
-        return ubytes + psi + phi
+        return ubytes + nk * 4 * na * 2 * nb * 2 + phi
     if cls == "lr_x_to_band":
-        return ubytes + phi + psi
+        return ubytes + nk * 4 * na * 2 * nx * 2 + ksplit * psi
     if cls == "lr_kmesh_transform":
-        return 2 * phi + nk * nx * 8
+        return 2 * phi + nk * nx * 4
     return float("nan")
 
 
@@ -307,6 +322,27 @@ def run_ours(args, ws, rank, local, pg):
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         e2e_ms = float(t.item())
     e2e_value = total_hpsi / (e2e_ms / 1000.0)
+
+    # ---- GMRES leg: 200 energies across the spectrum, tol 1e-6 on |g|^2, depth 80
+    gm = None
+    if rank == 0 and args.gmres_omega > 0:
+        from ocean_gb300 import workloads as WL2
+
+        energies = np.linspace(w.el, w.eh, args.gmres_omega) * WL2.HARTREE2EV
+        ctx.gmres(energies[:2], depth=80, tol=1e-6, max_restarts=100)  # warm-up
+        l1 = ctx.launches
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        ore, oim, rel, its = ctx.gmres(energies, depth=80, tol=1e-6, max_restarts=100)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        gms = g0.elapsed_time(g1)
+        gm = {"omega_points": int(args.gmres_omega), "tolerance_g2": 1e-6, "depth": 80,
+              "ms": gms, "spectra_per_s": 1000.0 / gms, "inner_iterations": int(its.sum()),
+              "gpu_launches": ctx.launches - l1,
+              "hpsi_per_s": (int(its.sum()) + 2 * args.gmres_omega) / (gms / 1000.0),
+              "max_rel_error": float(np.max(np.abs(rel)))}
     ctx.close()
 
     if rank != 0:
@@ -334,7 +370,7 @@ def run_ours(args, ws, rank, local, pg):
         per_launch_s = ms / cnt / 1000.0
         bytes_pl = algorithmic_bytes(w, dom, args.precision)
         achieved = bytes_pl / per_launch_s / 1e9
-        tr = traffic_summary().get(f"{dom}:{args.precision}:{args.workload}")
+        tr = traffic_summary().get(f"k_lr_tc:{dom}:{args.workload}") if args.precision == "mixed" else None
         total_ms = sum(x[1] for x in kt.values())
         roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_source": f"{src} hbm_gbs (copy bandwidth)",
@@ -356,7 +392,7 @@ def run_ours(args, ws, rank, local, pg):
                        "l2": "inputs larger than L2 (u2 %.2f GB per contraction operand)" % (
                            w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
             "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
-            "fp64_gpu": fp64, "roofline": roof, "cpu_baseline": cpu,
+            "fp64_gpu": fp64, "gmres": gm, "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
                     "d2h_bytes_per_step": 3 * (niter + 1) * 8 + (ne + 1) * 9 * 8},
             "gpu_launches": launches, "clocks": clocks, "kernel_ms": kt}

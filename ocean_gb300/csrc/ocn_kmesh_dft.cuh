@@ -283,10 +283,13 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
   constexpr int NK = N * N * N;
   constexpr int P3 = N + 1;
   constexpr int SLAB = N * N * P3;
-  for (int e = threadIdx.x; e < NA * NK; e += blockDim.x) {
-    const int k = e / NA, a = e % NA;
-    const int k3 = k % N;
-    buf[a * SLAB + (k / N) * P3 + k3] = phi[((size_t)k * nx + x) * NA + a];
+  // one thread per k-point: its NA values are contiguous in phi, and for each
+  // alpha consecutive threads hit consecutive shared-memory words
+  for (int k = threadIdx.x; k < NK; k += blockDim.x) {
+    const CT* src = phi + ((size_t)k * nx + x) * NA;
+    const int pos = (k / N) * P3 + k % N;
+#pragma unroll
+    for (int a = 0; a < NA; ++a) buf[a * SLAB + pos] = src[a];
   }
   __syncthreads();
 #pragma unroll
@@ -308,13 +311,17 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
     __syncthreads();
   }
   const R norm = (R)1 / (R)NK;
-  for (int e = threadIdx.x; e < NA * NK; e += blockDim.x) {
-    const int k = e / NA, a = e % NA;
-    const CT v = buf[a * SLAB + (k / N) * P3 + k % N];
-    CT o;
-    o.x = v.x * norm;
-    o.y = v.y * norm;
-    phi[((size_t)k * nx + x) * NA + a] = o;
+  for (int k = threadIdx.x; k < NK; k += blockDim.x) {
+    CT* dst = phi + ((size_t)k * nx + x) * NA;
+    const int pos = (k / N) * P3 + k % N;
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+      const CT v = buf[a * SLAB + pos];
+      CT o;
+      o.x = v.x * norm;
+      o.y = v.y * norm;
+      dst[a] = o;
+    }
   }
 }
 
@@ -359,9 +366,10 @@ __device__ void kmesh_convolve(typename C2<R>::T* __restrict__ phi, const R* __r
                                const typename C2<R>::T* __restrict__ tw) {
   typedef typename C2<R>::T CT;
   const int tot = g.na * g.nk;
-  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-    const int k = e / g.na, a = e % g.na;
-    buf[a * g.slab + kpad(g, k)] = phi[((size_t)k * nx + x) * g.na + a];
+  for (int k = threadIdx.x; k < g.nk; k += blockDim.x) {
+    const CT* src = phi + ((size_t)k * nx + x) * g.na;
+    const int pos = kpad(g, k);
+    for (int a = 0; a < g.na; ++a) buf[a * g.slab + pos] = src[a];
   }
   __syncthreads();
   for (int ax = 0; ax < 3; ++ax) {
@@ -381,13 +389,16 @@ __device__ void kmesh_convolve(typename C2<R>::T* __restrict__ phi, const R* __r
     __syncthreads();
   }
   const R norm = (R)1 / (R)g.nk;
-  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-    const int k = e / g.na, a = e % g.na;
-    const CT v = buf[a * g.slab + kpad(g, k)];
-    CT o;
-    o.x = v.x * norm;
-    o.y = v.y * norm;
-    phi[((size_t)k * nx + x) * g.na + a] = o;
+  for (int k = threadIdx.x; k < g.nk; k += blockDim.x) {
+    CT* dst = phi + ((size_t)k * nx + x) * g.na;
+    const int pos = kpad(g, k);
+    for (int a = 0; a < g.na; ++a) {
+      const CT v = buf[a * g.slab + pos];
+      CT o;
+      o.x = v.x * norm;
+      o.y = v.y * norm;
+      dst[a] = o;
+    }
   }
 }
 
