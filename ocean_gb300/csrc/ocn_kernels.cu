@@ -732,7 +732,8 @@ int kernels_init(ocn_ctx* c) {
   if (kmesh_cube_supported(c->dims.kmesh, c->na)) {
     CubeFnD f;
     OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], c->na, f);
-    OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff));
+    OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kmesh_cube_smem<double>(c->dims.kmesh[0], c->na)));
   }
   const size_t ma = sizeof(double2) * (size_t)c->na * 256;
   OCN_CUDA(c, cudaFuncSetAttribute(k_mult_amp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ma));
@@ -771,7 +772,7 @@ int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi) {
     CubeFnD f = nullptr;
     if (kmesh_cube_supported(c->dims.kmesh, na)) OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], na, f);
     if (f)
-      f<<<nx, 128, kmesh_smem(g), c->stream>>>(c->d_phi, c->d_W, nx);
+      f<<<nx, 128, kmesh_cube_smem<double>(c->dims.kmesh[0], na), c->stream>>>(c->d_phi, c->d_W, nx);
     else
       k_lr_fft_w_fp64<<<nx, 256, kmesh_smem(g), c->stream>>>(c->d_phi, c->d_W, nx, g);
     ++c->launches;

@@ -250,12 +250,20 @@ __device__ __forceinline__ void line_dft(CT (&v)[N], const CT* __restrict__ tw, 
   }
 }
 
+// Elements per alpha plane of a cubic transform: n*n*(n+1), padded so that
+// consecutive alpha planes start 8 banks apart (float2: 2 words per element,
+// double2: 4 words) -- four alpha values of one k-point then never share a bank.
+template <typename CT>
+__host__ __device__ constexpr int cube_slab(int n) {
+  return ((n * n * (n + 1) + 15) / 16) * 16 + (sizeof(CT) == 8 ? 4 : 2);
+}
+
 template <typename R, int N, int NA>
 __device__ __forceinline__ void cube_pass(typename C2<R>::T* buf, int ax,
                                           const typename C2<R>::T* __restrict__ tw, R sgn) {
   typedef typename C2<R>::T CT;
   constexpr int P3 = N + 1;
-  constexpr int SLAB = N * N * P3;
+  constexpr int SLAB = cube_slab<CT>(N);
   constexpr int LINES = NA * N * N;
   const int st = (ax == 2) ? 1 : ((ax == 1) ? P3 : N * P3);
   for (int l = threadIdx.x; l < LINES; l += blockDim.x) {
@@ -282,14 +290,12 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
   typedef typename C2<R>::T CT;
   constexpr int NK = N * N * N;
   constexpr int P3 = N + 1;
-  constexpr int SLAB = N * N * P3;
-  // one thread per k-point: its NA values are contiguous in phi, and for each
-  // alpha consecutive threads hit consecutive shared-memory words
-  for (int k = threadIdx.x; k < NK; k += blockDim.x) {
-    const CT* src = phi + ((size_t)k * nx + x) * NA;
-    const int pos = (k / N) * P3 + k % N;
-#pragma unroll
-    for (int a = 0; a < NA; ++a) buf[a * SLAB + pos] = src[a];
+  constexpr int SLAB = cube_slab<CT>(N);
+  // alpha fastest across threads: a warp reads whole 32-byte sectors of phi,
+  // and the padded slab puts the alpha planes on different shared-memory banks
+  for (int e = threadIdx.x; e < NA * NK; e += blockDim.x) {
+    const int k = e / NA, a = e % NA;
+    buf[a * SLAB + (k / N) * P3 + k % N] = phi[((size_t)k * nx + x) * NA + a];
   }
   __syncthreads();
 #pragma unroll
@@ -311,18 +317,21 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
     __syncthreads();
   }
   const R norm = (R)1 / (R)NK;
-  for (int k = threadIdx.x; k < NK; k += blockDim.x) {
-    CT* dst = phi + ((size_t)k * nx + x) * NA;
-    const int pos = (k / N) * P3 + k % N;
-#pragma unroll
-    for (int a = 0; a < NA; ++a) {
-      const CT v = buf[a * SLAB + pos];
-      CT o;
-      o.x = v.x * norm;
-      o.y = v.y * norm;
-      dst[a] = o;
-    }
+  for (int e = threadIdx.x; e < NA * NK; e += blockDim.x) {
+    const int k = e / NA, a = e % NA;
+    const CT v = buf[a * SLAB + (k / N) * P3 + k % N];
+    CT o;
+    o.x = v.x * norm;
+    o.y = v.y * norm;
+    phi[((size_t)k * nx + x) * NA + a] = o;
   }
+}
+
+// dynamic shared memory of a kmesh_convolve_cube CTA: twiddles + padded planes
+template <typename R>
+inline size_t kmesh_cube_smem(int n, int na) {
+  typedef typename C2<R>::T CT;
+  return sizeof(CT) * (3 * OCN_MAX_KDIM + (size_t)na * cube_slab<CT>(n));
 }
 
 // A cubic specialisation exists for these extents and transform counts.

@@ -664,8 +664,8 @@ int mixed_init(ocn_ctx* c) {
     CubeFnF f;
     OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], na, f);
     m->cube_fn = reinterpret_cast<void*>(f);
-    m->cube_smem = fsm;
-    OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+    m->cube_smem = kmesh_cube_smem<float>(c->dims.kmesh[0], na);
+    OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->cube_smem));
   }
   // FP32 twiddles, rounded from FP64 roots of unity
   float2 tw[3][OCN_MAX_KDIM];
