@@ -69,6 +69,7 @@ typedef struct {
   int core_l;      /* l_c  = sys%cur_run%ZNL(3)                      */
   int precision;   /* enum ocn_precision                             */
   int device;      /* CUDA device ordinal                            */
+  int nvec;        /* largest block of psi vectors acted on together (0 or 1: single) */
 } ocn_dims;
 
 /* Scalars of o_system used by the action (OCEAN_system.f90). */
@@ -191,6 +192,11 @@ int ocn_apply_H(ocn_ctx* ctx, const double* in_r, const double* in_i,
 int ocn_apply_H_dev(ocn_ctx* ctx, const double* d_in_r, const double* d_in_i,
                     double* d_out_r, double* d_out_i, const int* hflag, int backwards);
 
+/* H applied to nv vectors at once (host buffers: nv consecutive (Nb,Nk,Na) planes
+ * each).  Mixed precision reads the Bloch functions once for the whole block. */
+int ocn_apply_H_block(ocn_ctx* ctx, int nv, const double* in_r, const double* in_i,
+                      double* out_r, double* out_i, const int* hflag, int backwards);
+
 /* ----------------------------------------------------------------- Haydock */
 
 /* OCEAN_haydock_do -> OCEAN_haydock_Herm_do (OCEAN_haydock.f90:167-320) with
@@ -205,6 +211,22 @@ int ocn_haydock(ocn_ctx* ctx, const double* psi0_r, const double* psi0_i, int ni
 /* Same with psi0 in device memory; coefficient outputs are host arrays. */
 int ocn_haydock_dev(ocn_ctx* ctx, const double* d_psi0_r, const double* d_psi0_i, int niter,
                     double* real_a, double* imag_a, double* real_b, int* niter_done);
+
+/* Block Haydock: nv independent Lanczos chains that share H (the polarisations
+ * or photons of one core site, OCEAN.f90:51-83 runs them one after another),
+ * advanced in lockstep so that every read of the Bloch functions serves all nv
+ * vectors.  Each chain is exactly OCEAN_haydock_Herm_do on its own psi0.
+ * psi0_r/psi0_i: nv consecutive (Nb,Nk,Na) planes (host); real_a, imag_a,
+ * real_b: nv consecutive arrays of niter+1; niter_done: nv entries (may be NULL).
+ * nv <= dims.nvec; the FP64 path runs the chains one after another.  Returns
+ * OCN_ERR_NAN if any chain produced a NaN a_n (its niter_done entry stops there). */
+int ocn_haydock_block(ocn_ctx* ctx, int nv, const double* psi0_r, const double* psi0_i, int niter,
+                      double* real_a, double* imag_a, double* real_b, int* niter_done);
+
+/* Same with the nv psi0 vectors in device memory: vector v at d_psi0 + 2*v*npsi
+ * (real plane, then imaginary plane). */
+int ocn_haydock_block_dev(ocn_ctx* ctx, int nv, const double* d_psi0, int niter, double* real_a,
+                          double* imag_a, double* real_b, int* niter_done);
 
 /* core_pnorm (OCEAN_psi.f90:5589-5638): normalises psi in place (host planes of
  * n = Nb*Nk*Na values) and returns kpref = 4 pi |psi|^2 / (Nk celvol^2). */

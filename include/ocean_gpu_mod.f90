@@ -20,6 +20,7 @@ module ocean_gpu_mod
     integer(c_int) :: core_l
     integer(c_int) :: precision
     integer(c_int) :: device
+    integer(c_int) :: nvec
   end type
 
   type, bind(C), public :: ocn_system
@@ -119,6 +120,26 @@ module ocean_gpu_mod
       integer(c_int), value :: niter
       real(c_double), intent(out) :: real_a(0:*), imag_a(0:*), real_b(0:*)
       integer(c_int), intent(out) :: ndone
+    end function
+    integer(c_int) function ocn_haydock_block(ctx, nv, p0r, p0i, niter, real_a, imag_a, real_b, &
+        ndone) bind(C, name="ocn_haydock_block")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nv
+      real(c_double), intent(in) :: p0r(*), p0i(*)
+      integer(c_int), value :: niter
+      real(c_double), intent(out) :: real_a(0:*), imag_a(0:*), real_b(0:*)
+      integer(c_int), intent(out) :: ndone(*)
+    end function
+    integer(c_int) function ocn_apply_H_block(ctx, nv, in_r, in_i, out_r, out_i, hflag, backwards) &
+        bind(C, name="ocn_apply_H_block")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nv
+      real(c_double), intent(in) :: in_r(*), in_i(*)
+      real(c_double), intent(out) :: out_r(*), out_i(*)
+      integer(c_int), intent(in) :: hflag(6)
+      integer(c_int), value :: backwards
     end function
     integer(c_int) function ocn_spectrum_cf(real_a, imag_a, real_b, iter, kpref, p, out) &
         bind(C, name="ocn_spectrum_cf")

@@ -21,6 +21,7 @@ IP = C.POINTER(C.c_int)
 
 OCN_PREC_FP64 = 0
 OCN_PREC_MIXED = 1
+OCN_OK, OCN_ERR_NAN, OCN_ERR_ARG, OCN_ERR_STATE = 0, -1, 1, 4
 
 STATUS = {0: "OK", -1: "NaN in Lanczos a", 1: "bad argument", 2: "CUDA error", 3: "allocation failed",
           4: "operator data not set", 5: "device wait timed out", 6: "GMRES did not converge",
@@ -30,7 +31,7 @@ STATUS = {0: "OK", -1: "NaN in Lanczos a", 1: "bad argument", 2: "CUDA error", 3
 class OcnDims(C.Structure):
     _fields_ = [("num_bands", C.c_int), ("kmesh", C.c_int * 3), ("xmesh", C.c_int * 3),
                 ("nalpha", C.c_int), ("nspn", C.c_int), ("core_l", C.c_int),
-                ("precision", C.c_int), ("device", C.c_int)]
+                ("precision", C.c_int), ("device", C.c_int), ("nvec", C.c_int)]
 
 
 class OcnSystem(C.Structure):
@@ -70,7 +71,8 @@ EXPORTS = [
     "ocn_get_bloch", "ocn_set_mult", "ocn_set_spin_orbit", "ocn_soprep", "ocn_apply_H",
     "ocn_apply_H_dev", "ocn_haydock", "ocn_haydock_dev", "ocn_psi_pnorm", "ocn_spectrum_cf",
     "ocn_redtrid", "ocn_gmres", "ocn_kernel_launches", "ocn_w2_host", "ocn_phase_table_host",
-    "ocn_timing_enable", "ocn_timing_reset", "ocn_timing_read", "ocn_stream",
+    "ocn_timing_enable", "ocn_timing_reset", "ocn_timing_read", "ocn_stream", "ocn_apply_H_block",
+    "ocn_haydock_block", "ocn_haydock_block_dev",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -93,7 +95,7 @@ def _lr_params(w):
     return p, (rtab, ptab)
 
 
-def _dims(w, precision=0, device=0):
+def _dims(w, precision=0, device=0, nvec=1):
     d = OcnDims()
     d.num_bands = w.nb
     d.kmesh[:] = list(w.kmesh)
@@ -103,6 +105,7 @@ def _dims(w, precision=0, device=0):
     d.core_l = w.core_l
     d.precision = precision
     d.device = device
+    d.nvec = nvec
     return d
 
 
@@ -172,19 +175,12 @@ class Context:
     ocean_load_data (OCEAN_load_data.f90:8-173) and the operators that use it."""
 
     def __init__(self, w, precision: int = OCN_PREC_FP64, device: int = 0,
-                 hflag=(1, 1, 1, 1, 1, 1), set_mult: bool = True):
+                 hflag=(1, 1, 1, 1, 1, 1), set_mult: bool = True, nvec: int = 1):
         lib = load()
         self.w = w
         self.lib = lib
-        d = OcnDims()
-        d.num_bands = w.nb
-        d.kmesh[:] = list(w.kmesh)
-        d.xmesh[:] = list(w.xmesh)
-        d.nalpha = w.na
-        d.nspn = w.nspn
-        d.core_l = w.core_l
-        d.precision = precision
-        d.device = device
+        d = _dims(w, precision, device, nvec)
+        self.nvec = max(1, nvec)
         self.dims = d
         self.ptr = C.c_void_p()
         check(lib.ocn_ctx_create(C.byref(d), C.byref(self.ptr)))
@@ -301,6 +297,35 @@ class Context:
                                   _dp(rb), C.byref(done))
         self._chk(rc)
         return ra, ia, rb, done.value
+
+    def apply_H_block(self, pr, pi, hflag=None, backwards=False):
+        """H on a block of vectors: pr/pi of shape (nv, npsi)."""
+        pr, pi = np.ascontiguousarray(pr, dtype=np.float64), np.ascontiguousarray(pi, dtype=np.float64)
+        nv = pr.shape[0]
+        outr, outi = np.zeros_like(pr), np.zeros_like(pi)
+        hf = None if hflag is None else (C.c_int * 6)(*hflag)
+        self._chk(self.lib.ocn_apply_H_block(self.ptr, nv, _dp(pr), _dp(pi), _dp(outr), _dp(outi), hf,
+                                             int(bool(backwards))))
+        return outr, outi
+
+    def haydock_block(self, niter: int, pr, pi):
+        """nv Lanczos chains in lockstep: pr/pi of shape (nv, npsi); returns arrays
+        of shape (nv, niter+1) and the per-chain iteration counts."""
+        pr, pi = np.ascontiguousarray(pr, dtype=np.float64), np.ascontiguousarray(pi, dtype=np.float64)
+        nv = pr.shape[0]
+        ra, ia, rb = (np.zeros((nv, niter + 1)) for _ in range(3))
+        done = np.zeros(nv, dtype=np.int32)
+        self._chk(self.lib.ocn_haydock_block(self.ptr, nv, _dp(pr), _dp(pi), niter, _dp(ra), _dp(ia),
+                                             _dp(rb), done.ctypes.data_as(IP)))
+        return ra, ia, rb, done
+
+    def haydock_block_dev(self, niter: int, nv: int, d_psi0: int):
+        """Block Haydock on device psi0 (vector v at d_psi0 + 2*v*npsi doubles)."""
+        ra, ia, rb = (np.zeros((nv, niter + 1)) for _ in range(3))
+        done = np.zeros(nv, dtype=np.int32)
+        self._chk(self.lib.ocn_haydock_block_dev(self.ptr, nv, C.c_void_p(d_psi0), niter, _dp(ra), _dp(ia),
+                                                 _dp(rb), done.ctypes.data_as(IP)))
+        return ra, ia, rb, done
 
     def gmres(self, energies_ev, depth=80, resolution=None, preconditioner=None, tol=1e-6,
               max_restarts=50, kpref=None):

@@ -30,9 +30,6 @@ int cuda_fail(ocn_ctx* c, cudaError_t e, const char* what) {
 }
 
 int kernels_init(ocn_ctx* c);  // ocn_kernels.cu
-int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const double* psi_r,
-                   const double* psi_i, double* h_r, double* h_i, const double* bprev,
-                   double* a_out, double* ia_out, double* b_out);
 
 namespace {
 
@@ -62,16 +59,45 @@ int apply_H_impl(ocn_ctx* c, const double* ir, const double* ii, double* orr, do
   if (rc) return rc;
   c->acc_valid = false;
   if (c->sys.mult && hflag[4] == 1 && c->have_mult) {
-    if ((rc = zero_acc(c))) return rc;
-    if ((rc = mult_apply(c, ir, ii))) return rc;
+    if ((rc = zero_acc(c, 1))) return rc;
+    if ((rc = mult_apply(c, ir, ii, c->d_acc))) return rc;
     c->acc_valid = true;
   }
   if (c->sys.long_range && hflag[0] == 1) {
-    if (c->dims.precision == OCN_PREC_MIXED) rc = lr_apply_mixed(c, ir, ii);
+    if (c->dims.precision == OCN_PREC_MIXED) rc = lr_apply_mixed(c, ir, ii, 0, 1);
     else rc = lr_apply_fp64(c, ir, ii);
     if (rc) return rc;
   }
-  return combine(c, ir, ii, orr, oi, hflag, backwards);
+  return combine(c, 1, ir, ii, orr, oi, 0, hflag, backwards);
+}
+
+// H on a block of nv vectors (vector v at in + 2*v*npsi) -- mixed precision reads
+// the Bloch functions once for the block; the FP64 path acts vector by vector.
+int apply_H_block_impl(ocn_ctx* c, int nv, const double* in, double* out, const int* hflag_in,
+                       int backwards) {
+  const size_t n = c->npsi;
+  if (nv < 1 || nv > c->nvec) return set_err(c, OCN_ERR_ARG, "block size must be in 1..nvec");
+  if (c->dims.precision != OCN_PREC_MIXED) {
+    for (int v = 0; v < nv; ++v) {
+      int rc = apply_H_impl(c, in + 2 * v * n, in + 2 * v * n + n, out + 2 * v * n, out + 2 * v * n + n,
+                            hflag_in, backwards);
+      if (rc) return rc;
+    }
+    return OCN_OK;
+  }
+  int hflag[6];
+  for (int i = 0; i < 6; ++i) hflag[i] = hflag_in ? hflag_in[i] : c->sys.nhflag[i];
+  int rc = require(c);
+  if (rc) return rc;
+  c->acc_valid = false;
+  if (c->sys.mult && hflag[4] == 1 && c->have_mult) {
+    if ((rc = zero_acc(c, nv))) return rc;
+    for (int v = 0; v < nv; ++v)
+      if ((rc = mult_apply(c, in + 2 * v * n, in + 2 * v * n + n, c->d_acc + 2 * v * n))) return rc;
+    c->acc_valid = true;
+  }
+  if (c->sys.long_range && hflag[0] == 1 && (rc = lr_apply_mixed(c, in, in + n, 2 * n, nv))) return rc;
+  return combine(c, nv, in, in + n, out, out + n, 2 * n, hflag, backwards);
 }
 
 }  // namespace
@@ -155,10 +181,12 @@ int ocn_ctx_create(const ocn_dims* d, ocn_ctx** out) {
     return set_err(nullptr, OCN_ERR_ARG, "unknown precision");
   if (d->precision == OCN_PREC_MIXED && d->num_bands > 256)
     return set_err(nullptr, OCN_ERR_ARG, "mixed precision supports at most 256 bands");
+  if (d->nvec < 0 || d->nvec > 16) return set_err(nullptr, OCN_ERR_ARG, "nvec must be in 0..16");
 
   ocn_ctx* c = new (std::nothrow) ocn_ctx();
   if (!c) return set_err(nullptr, OCN_ERR_ALLOC, "host allocation failed");
   c->dims = *d;
+  c->nvec = d->nvec > 1 ? d->nvec : 1;
   c->nb = d->num_bands;
   c->nk = nk;
   c->nx = nx;
@@ -195,13 +223,14 @@ int ocn_ctx_create(const ocn_dims* d, ocn_ctx** out) {
       (rc = dev_alloc(c, &c->d_u, (size_t)c->nb * nk * nx * c->nspn)) ||
       (rc = dev_alloc(c, &c->d_W, (size_t)nk * nx)) ||
       (rc = dev_alloc(c, &c->d_so, (size_t)c->na * c->na)) ||
-      (rc = dev_alloc(c, &c->d_acc, 2 * c->npsi)) ||
-      (rc = dev_alloc(c, &c->d_red, (size_t)8 * c->red_blocks)) ||
+      (rc = dev_alloc(c, &c->d_acc, 2 * c->npsi * c->nvec)) ||
+      (rc = dev_alloc(c, &c->d_red, (size_t)8 * c->red_blocks * c->nvec)) ||
       (rc = dev_alloc(c, &c->d_scal, 64)))
     return fail(rc);
   if (d->precision == OCN_PREC_FP64) {
+    c->part_stride = 2 * c->npsi;  // the FP64 path acts on one vector at a time
     if ((rc = dev_alloc(c, &c->d_phi, (size_t)nk * nx * c->na)) ||
-        (rc = dev_alloc(c, &c->d_accpart, (size_t)c->lr_xsplit * 2 * c->npsi)))
+        (rc = dev_alloc(c, &c->d_accpart, (size_t)c->lr_xsplit * c->part_stride)))
       return fail(rc);
   }
   cudaMemsetAsync(c->d_ei, 0, sizeof(double) * c->npsi, c->stream);
@@ -548,25 +577,28 @@ int ocn_apply_H(ocn_ctx* c, const double* ir, const double* ii, double* orr, dou
 
 namespace {
 
-// One Haydock iteration (OCEAN_haydock.f90:250-268): H*psi then the fused
-// two-term Lanczos update, for iteration index *d_iter (advanced first).
-int haydock_iteration(ocn_ctx* c, double* old, double* psi, double* h, double* ra, double* ia,
-                      double* rb) {
+// One Haydock iteration (OCEAN_haydock.f90:250-268) of nv chains in lockstep:
+// H*psi then the fused two-term Lanczos update, for iteration index *d_iter
+// (advanced first).  old/psi/h are block bases (vector v at +2*v*npsi).
+int haydock_iteration(ocn_ctx* c, int nv, double* old, double* psi, double* h, double* ra, double* ia,
+                      double* rb, size_t cstride) {
   const size_t n = c->npsi;
   int rc;
   if ((rc = advance_iter(c, c->d_iter))) return rc;
   c->acc_valid = false;
   if (c->sys.mult && c->sys.nhflag[4] == 1 && c->have_mult) {
-    if ((rc = zero_acc(c)) || (rc = mult_apply(c, psi, psi + n))) return rc;
+    if ((rc = zero_acc(c, nv))) return rc;
+    for (int v = 0; v < nv; ++v)
+      if ((rc = mult_apply(c, psi + 2 * v * n, psi + 2 * v * n + n, c->d_acc + 2 * v * n))) return rc;
     c->acc_valid = true;
   }
   if (c->sys.long_range && c->sys.nhflag[0] == 1) {
     // mixed: the psi operand was built by the previous normalisation (or before the loop)
-    rc = (c->dims.precision == OCN_PREC_MIXED) ? lr_apply_mixed(c, psi, psi + n, true)
+    rc = (c->dims.precision == OCN_PREC_MIXED) ? lr_apply_mixed(c, psi, psi + n, 2 * n, nv, true)
                                                : lr_apply_fp64(c, psi, psi + n);
     if (rc) return rc;
   }
-  return lanczos_launch(c, old, old + n, psi, psi + n, h, h + n, ra, ia, rb, c->d_iter);
+  return lanczos_launch(c, nv, old, psi, h, ra, ia, rb, cstride, c->d_iter);
 }
 
 void drop_haydock_graph(ocn_ctx* c) {
@@ -579,7 +611,7 @@ void drop_haydock_graph(ocn_ctx* c) {
   c->graph_events.clear();
 }
 
-unsigned long long haydock_key(const ocn_ctx* c) {
+unsigned long long haydock_key(const ocn_ctx* c, int nv) {
   unsigned long long k = reinterpret_cast<uintptr_t>(c->hay_vec) ^
                          (reinterpret_cast<uintptr_t>(c->hay_coef) << 1) ^ ((unsigned long long)c->hay_cap << 40);
   k ^= (unsigned long long)(c->sys.mult ? 1 : 0) << 1;
@@ -590,48 +622,57 @@ unsigned long long haydock_key(const ocn_ctx* c) {
   k ^= (unsigned long long)(c->have_so ? 1 : 0) << 6;
   k ^= (unsigned long long)(c->ei_nonzero ? 1 : 0) << 7;
   for (int i = 0; i < 6; ++i) k ^= (unsigned long long)(c->sys.nhflag[i] & 1) << (8 + i);
+  k ^= (unsigned long long)nv << 16;
   return k;
 }
 
-}  // namespace
+// Chains held at once by the Haydock buffers: a block in mixed precision, one
+// chain in FP64 (the FP64 block driver runs its chains one after another).
+int haydock_chains(const ocn_ctx* c) { return c->dims.precision == OCN_PREC_MIXED ? c->nvec : 1; }
 
-int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter, double* real_a,
-                    double* imag_a, double* real_b, int* niter_done) {
-  if (!c || !p0r || !p0i || niter < 1 || !real_a || !real_b) return OCN_ERR_ARG;
-  cudaSetDevice(c->device);
+// nv Lanczos chains from device psi0 planes (chain v: p0r + v*vstride, p0i + v*vstride).
+// Coefficients land in host arrays real_a/imag_a/real_b + v*(niter+1).
+int haydock_run(ocn_ctx* c, int nv, const double* p0r, const double* p0i, size_t vstride, int niter,
+                double* real_a, double* imag_a, double* real_b, int* niter_done) {
   int rc = require(c);
   if (rc) return rc;
   const size_t n = c->npsi;
-  if (!c->hay_vec && (rc = dev_alloc(c, &c->hay_vec, 6 * n))) return rc;
+  const int hv = haydock_chains(c);
+  if (nv < 1 || nv > hv) return set_err(c, OCN_ERR_ARG, "block size must be in 1..nvec");
+  if (!c->hay_vec && (rc = dev_alloc(c, &c->hay_vec, 6 * n * hv))) return rc;
   if (!c->d_iter && (rc = dev_alloc(c, &c->d_iter, 1))) return rc;
   if (c->hay_cap < niter) {
     drop_haydock_graph(c);
     if (c->hay_coef) cudaFree(c->hay_coef);
     c->hay_coef = nullptr;
     c->hay_cap = 0;
-    if ((rc = dev_alloc(c, &c->hay_coef, 3 * (size_t)(niter + 1)))) return rc;
+    if ((rc = dev_alloc(c, &c->hay_coef, 3 * (size_t)(niter + 1) * hv))) return rc;
     c->hay_cap = niter;
   }
+  // coefficients: [real_a of each chain | imag_a of each chain | real_b of each chain]
   const size_t cap1 = (size_t)c->hay_cap + 1;
   double* ra = c->hay_coef;
-  double* ia = c->hay_coef + cap1;
-  double* rb = c->hay_coef + 2 * cap1;
-  double* buf[3] = {c->hay_vec, c->hay_vec + 2 * n, c->hay_vec + 4 * n};  // old, psi, h
-  cudaError_t e = cudaMemsetAsync(c->hay_coef, 0, 3 * cap1 * sizeof(double), c->stream);
+  double* ia = c->hay_coef + hv * cap1;
+  double* rb = c->hay_coef + 2 * hv * cap1;
+  double* buf[3] = {c->hay_vec, c->hay_vec + 2 * n * hv, c->hay_vec + 4 * n * hv};  // old, psi, h
+  cudaError_t e = cudaMemsetAsync(c->hay_coef, 0, 3 * hv * cap1 * sizeof(double), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->d_iter, 0, sizeof(int), c->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(buf[0], 0, 2 * n * sizeof(double), c->stream);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(buf[1], p0r, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(buf[1] + n, p0i, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(buf[0], 0, 2 * n * nv * sizeof(double), c->stream);
+  for (int v = 0; v < nv && e == cudaSuccess; ++v) {
+    e = cudaMemcpyAsync(buf[1] + 2 * v * n, p0r + v * vstride, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                        c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(buf[1] + 2 * v * n + n, p0i + v * vstride, n * sizeof(double),
+                          cudaMemcpyDeviceToDevice, c->stream);
+  }
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock setup");
-  if (c->dims.precision == OCN_PREC_MIXED && (rc = mixed_prep_b1(c, buf[1], buf[1] + n))) return rc;
+  if (c->dims.precision == OCN_PREC_MIXED && (rc = mixed_prep_b1(c, buf[1], buf[1] + n, 2 * n, nv))) return rc;
 
   // Three iterations rotate (old, psi, h) back to their starting roles, so one
   // captured 3-iteration graph serves every launch.
   const int ngraph = c->use_graphs ? niter / 3 : 0;
   if (ngraph > 0) {
-    const unsigned long long key = haydock_key(c);
+    const unsigned long long key = haydock_key(c, nv);
     if (!c->hay_exec || key != c->hay_key) {
       drop_haydock_graph(c);
       OCN_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -639,7 +680,7 @@ int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter,
       const long long l0 = c->launches;
       double* b[3] = {buf[0], buf[1], buf[2]};
       for (int r = 0; r < 3 && rc == OCN_OK; ++r) {
-        rc = haydock_iteration(c, b[0], b[1], b[2], ra, ia, rb);
+        rc = haydock_iteration(c, nv, b[0], b[1], b[2], ra, ia, rb, cap1);
         double* t = b[0];
         b[0] = b[1];
         b[1] = b[2];
@@ -670,7 +711,7 @@ int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter,
   }
   int done = 3 * ngraph;
   for (int it = done + 1; it <= niter && rc == OCN_OK; ++it) {
-    rc = haydock_iteration(c, buf[0], buf[1], buf[2], ra, ia, rb);
+    rc = haydock_iteration(c, nv, buf[0], buf[1], buf[2], ra, ia, rb, cap1);
     if (rc) break;
     double* t = buf[0];
     buf[0] = buf[1];  // old <- psi
@@ -679,7 +720,7 @@ int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter,
     done = it;
   }
   e = cudaStreamSynchronize(c->stream);
-  std::vector<double> host(3 * cap1);
+  std::vector<double> host(3 * hv * cap1);
   if (e == cudaSuccess)
     e = cudaMemcpy(host.data(), c->hay_coef, host.size() * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock");
@@ -695,20 +736,55 @@ int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter,
     (void)cudaGetLastError();  // a failed timing query must not poison later calls
   }
   if (c->mixed && (rc = mixed_check(c))) return rc;
-  for (int i = 0; i <= niter; ++i) {
-    real_a[i] = host[i];
-    if (imag_a) imag_a[i] = host[cap1 + i];
-    real_b[i] = host[2 * cap1 + i];
-  }
-  if (niter_done) *niter_done = done;
+  const size_t out1 = (size_t)niter + 1;
+  for (int v = 0; v < nv; ++v)
+    for (int i = 0; i <= niter; ++i) {
+      real_a[v * out1 + i] = host[v * cap1 + i];
+      if (imag_a) imag_a[v * out1 + i] = host[(hv + v) * cap1 + i];
+      real_b[v * out1 + i] = host[(2 * hv + v) * cap1 + i];
+    }
   // NaN check on a (OCEAN_haydock.f90:913-920): the reference stops at the first
   // NaN; report the iteration count up to it.
-  for (int i = 0; i < done; ++i)
-    if (std::isnan(real_a[i])) {
-      if (niter_done) *niter_done = i + 1;
-      return set_err(c, OCN_ERR_NAN, "NaN detected in Lanczos a");
-    }
-  return OCN_OK;
+  rc = OCN_OK;
+  for (int v = 0; v < nv; ++v) {
+    int dv = done;
+    for (int i = 0; i < done; ++i)
+      if (std::isnan(real_a[v * out1 + i])) {
+        dv = i + 1;
+        rc = set_err(c, OCN_ERR_NAN, "NaN detected in Lanczos a");
+        break;
+      }
+    if (niter_done) niter_done[v] = dv;
+  }
+  return rc;
+}
+
+// Block Haydock on device psi0 planes; FP64 contexts run the chains one by one.
+int haydock_block_impl(ocn_ctx* c, int nv, const double* d_psi0, int niter, double* real_a, double* imag_a,
+                       double* real_b, int* niter_done) {
+  const size_t n = c->npsi;
+  if (nv < 1 || nv > std::max(c->nvec, 1)) return set_err(c, OCN_ERR_ARG, "block size must be in 1..nvec");
+  if (haydock_chains(c) >= nv)
+    return haydock_run(c, nv, d_psi0, d_psi0 + n, 2 * n, niter, real_a, imag_a, real_b, niter_done);
+  const size_t out1 = (size_t)niter + 1;
+  int rc = OCN_OK;
+  for (int v = 0; v < nv; ++v) {
+    const int r = haydock_run(c, 1, d_psi0 + 2 * v * n, d_psi0 + 2 * v * n + n, 0, niter, real_a + v * out1,
+                              imag_a ? imag_a + v * out1 : nullptr, real_b + v * out1,
+                              niter_done ? niter_done + v : nullptr);
+    if (r == OCN_ERR_NAN) rc = r;
+    else if (r) return r;
+  }
+  return rc;
+}
+
+}  // namespace
+
+int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter, double* real_a,
+                    double* imag_a, double* real_b, int* niter_done) {
+  if (!c || !p0r || !p0i || niter < 1 || !real_a || !real_b) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  return haydock_run(c, 1, p0r, p0i, 0, niter, real_a, imag_a, real_b, niter_done);
 }
 
 int ocn_haydock(ocn_ctx* c, const double* p0r, const double* p0i, int niter, double* real_a,
@@ -727,6 +803,67 @@ int ocn_haydock(ocn_ctx* c, const double* p0r, const double* p0i, int niter, dou
   }
   rc = ocn_haydock_dev(c, d, d + n, niter, real_a, imag_a, real_b, niter_done);
   cudaFree(d);
+  return rc;
+}
+
+int ocn_haydock_block_dev(ocn_ctx* c, int nv, const double* d_psi0, int niter, double* real_a, double* imag_a,
+                          double* real_b, int* niter_done) {
+  if (!c || !d_psi0 || niter < 1 || !real_a || !real_b) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  return haydock_block_impl(c, nv, d_psi0, niter, real_a, imag_a, real_b, niter_done);
+}
+
+int ocn_haydock_block(ocn_ctx* c, int nv, const double* p0r, const double* p0i, int niter, double* real_a,
+                      double* imag_a, double* real_b, int* niter_done) {
+  if (!c || !p0r || !p0i || niter < 1 || !real_a || !real_b) return OCN_ERR_ARG;
+  if (nv < 1 || nv > std::max(c->nvec, 1)) return set_err(c, OCN_ERR_ARG, "block size must be in 1..nvec");
+  cudaSetDevice(c->device);
+  const size_t n = c->npsi;
+  double* d = nullptr;
+  int rc = dev_alloc(c, &d, 2 * n * nv);
+  if (rc) return rc;
+  cudaError_t e = cudaSuccess;
+  for (int v = 0; v < nv && e == cudaSuccess; ++v) {
+    e = cudaMemcpyAsync(d + 2 * v * n, p0r + v * n, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d + 2 * v * n + n, p0i + v * n, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  }
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    return cuda_fail(c, e, "ocn_haydock_block upload");
+  }
+  rc = haydock_block_impl(c, nv, d, niter, real_a, imag_a, real_b, niter_done);
+  cudaFree(d);
+  return rc;
+}
+
+int ocn_apply_H_block(ocn_ctx* c, int nv, const double* ir, const double* ii, double* orr, double* oi,
+                      const int* hflag, int backwards) {
+  if (!c || !ir || !ii || !orr || !oi) return OCN_ERR_ARG;
+  if (nv < 1 || nv > std::max(c->nvec, 1)) return set_err(c, OCN_ERR_ARG, "block size must be in 1..nvec");
+  cudaSetDevice(c->device);
+  const size_t n = c->npsi;
+  double* buf = nullptr;
+  int rc = dev_alloc(c, &buf, 4 * n * nv);
+  if (rc) return rc;
+  double* in = buf;
+  double* out = buf + 2 * n * nv;
+  cudaError_t e = cudaSuccess;
+  for (int v = 0; v < nv && e == cudaSuccess; ++v) {
+    e = cudaMemcpyAsync(in + 2 * v * n, ir + v * n, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(in + 2 * v * n + n, ii + v * n, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  }
+  if (e == cudaSuccess) rc = apply_H_block_impl(c, nv, in, out, hflag, backwards);
+  for (int v = 0; v < nv && e == cudaSuccess && rc == OCN_OK; ++v) {
+    e = cudaMemcpyAsync(orr + v * n, out + 2 * v * n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(oi + v * n, out + 2 * v * n + n, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(c, e, "ocn_apply_H_block");
+  if (rc == OCN_OK && c->mixed) rc = mixed_check(c);
   return rc;
 }
 

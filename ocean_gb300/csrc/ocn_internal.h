@@ -17,6 +17,14 @@ namespace ocn {
 
 struct MixedLR;  // split-BF16 / tcgen05 state (ocn_mixed.cu)
 
+// Strides between the vectors of a block of psi (chain v = blockIdx.y).
+struct BlockStrides {
+  size_t vec;   // between vectors: 2*npsi (real plane, imaginary plane)
+  size_t part;  // between K-splits of the long-range partial sums
+  size_t coef;  // between the coefficient arrays of two chains
+  size_t red;   // between the reduction-partial arrays of two chains
+};
+
 // Kernel classes timed with CUDA events on the context stream when timing is on.
 enum TimedClass { T_LR_GEMM1 = 0, T_LR_FFT, T_LR_GEMM2, T_LR_PREP, T_MULT, T_LANCZOS, T_NCLASS };
 
@@ -84,8 +92,10 @@ struct ocn_ctx {
   // work buffers
   double2* d_phi = nullptr;        // FP64 path: [k][x][a]
   double* d_acc = nullptr;         // full-store accumulator: re plane then im plane (npsi each)
-  double* d_accpart = nullptr;     // GEMM2 x-split partials [split][2][npsi]
+  double* d_accpart = nullptr;     // long-range partials [split][vector][re|im][npsi]
   int lr_xsplit = 1;
+  size_t part_stride = 0;          // elements between two splits of d_accpart
+  int nvec = 1;                    // largest psi block
   double* d_vec = nullptr;         // general vector pool (see ocn_solvers.cu)
   size_t vec_pool_n = 0;
   double* d_red = nullptr;         // reduction partials
@@ -176,19 +186,19 @@ double gamfcn(double e, double n, double e0);
 // ---- FP64 kernels (ocn_kernels.cu)
 int upload_twiddles(ocn_ctx* c);
 int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi);  // adds into d_acc
-int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi);     // adds into d_acc
+int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi, double* acc);  // adds into acc
 int phase_bloch(ocn_ctx* c, const double* d_ur, const double* d_ui, const double* d_cos,
                 const double* d_sin);
-// out = E o in + A o acc + SO in   (acc already holds H_fg + H_lr of A o in)
-int combine(ocn_ctx* c, const double* d_pr, const double* d_pi, double* d_or, double* d_oi,
-            const int* hflag, int backwards);
-int zero_acc(ocn_ctx* c);
+// out = E o in + A o acc + SO in   (acc already holds H_fg + H_lr of A o in), for nv
+// vectors at stride vstride (vector v: planes at d_pr + v*vstride, d_pi + v*vstride)
+int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* d_or, double* d_oi,
+            size_t vstride, const int* hflag, int backwards);
+int zero_acc(ocn_ctx* c, int nv);
 
-// Fused Lanczos step (combine + ocean_hay_ab_twoterm); coefficients stay on device,
-// indexed by the device iteration counter *itp (advanced by advance_iter).
-int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const double* psi_r,
-                   const double* psi_i, double* h_r, double* h_i, double* ra, double* ia,
-                   double* rb, const int* itp);
+// Fused Lanczos step (combine + ocean_hay_ab_twoterm) of nv chains; coefficients stay
+// on device, indexed by the device iteration counter *itp (advanced by advance_iter).
+int lanczos_launch(ocn_ctx* c, int nv, const double* old, const double* psi, double* h, double* ra,
+                   double* ia, double* rb, size_t cstride, const int* itp);
 int advance_iter(ocn_ctx* c, int* itp);
 
 // BLAS-1 helpers for GMRES (ocn_kernels.cu); vectors are [re plane | im plane]
@@ -213,12 +223,14 @@ int cf_eval(const double* ra, const double* ia, const double* rb, int iter, doub
 int mixed_init(ocn_ctx* c);
 int mixed_free(ocn_ctx* c);
 int mixed_set_bloch(ocn_ctx* c);   // builds split-BF16 layouts from d_u
-// writes d_accpart; b1_ready: the psi operand was already built (fused Lanczos step)
-int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, bool b1_ready = false);
-int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi);
-// b_i = sqrt(partials), psi = h / b_i, and the psi operand of the next action
-int mixed_norm_prep(ocn_ctx* c, const double* red2, int nblk, double* hr, double* hi, double* rb,
-                    const int* itp);
+// Long-range term of nv vectors (vector v: planes d_pr + v*vstride, d_pi + v*vstride)
+// into d_accpart; b1_ready: the psi operand was already built (fused Lanczos step)
+int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vstride, int nv,
+                   bool b1_ready = false);
+int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vstride, int nv);
+// b_i = sqrt(partials), psi = h / b_i, and the psi operand of the next action (nv chains)
+int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rstride, double* h,
+                    double* rb, size_t cstride, const int* itp);
 int mixed_check(ocn_ctx* c);       // reads and clears the device timeout flag
 
 }  // namespace ocn

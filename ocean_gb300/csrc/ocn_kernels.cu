@@ -121,16 +121,16 @@ __global__ void k_lr_fft_w_fp64(double2* __restrict__ phi, const double* __restr
   kmesh_convolve<double>(phi, W, nx, blockIdx.x, g, buf, tw);
 }
 
-template <int N, int NA>
-__global__ void k_fft_cube_fp64(double2* __restrict__ phi, const double* __restrict__ W, int nx) {
+template <int N>
+__global__ void k_fft_cube_fp64(double2* __restrict__ phi, const double* __restrict__ W, int nx, int nt) {
   extern __shared__ double2 smem[];
   double2* tw = smem;
   double2* buf = smem + 3 * OCN_MAX_KDIM;
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_tw[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
   __syncthreads();
-  kmesh_convolve_cube<double, N, NA>(phi, W, nx, blockIdx.x, buf, tw);
+  kmesh_convolve_cube<double, N>(phi, W, nx, blockIdx.x, nt, buf, tw);
 }
-typedef void (*CubeFnD)(double2*, const double*, int);
+typedef void (*CubeFnD)(double2*, const double*, int, int);
 
 // ------------------------------------------------------ LR: x-mesh -> band
 
@@ -198,8 +198,22 @@ __global__ void k_combine(const double* __restrict__ pr, const double* __restric
                           size_t npsi, int use_e0, int use_so, int backwards,
                           const double* __restrict__ oldr, const double* __restrict__ oldi,
                           const double* __restrict__ rb_base, const int* __restrict__ itp,
-                          double* __restrict__ red) {
+                          double* __restrict__ red, const BlockStrides bs) {
   __shared__ double sh[2][32];
+  // chain / vector v = blockIdx.y of a block of psi vectors
+  const size_t v = blockIdx.y;
+  pr += v * bs.vec;
+  pi += v * bs.vec;
+  outr += v * bs.vec;
+  outi += v * bs.vec;
+  if (acc) acc += v * bs.vec;
+  part += v * 2 * npsi;
+  if (oldr) {
+    oldr += v * bs.vec;
+    oldi += v * bs.vec;
+    rb_base += v * bs.coef;
+  }
+  if (red) red += v * bs.red;
   double dr = 0.0, di = 0.0;
   double bm = 0.0;
   if (oldr) bm = -rb_base[*itp - 1];  // b_{i-1}
@@ -219,8 +233,8 @@ __global__ void k_combine(const double* __restrict__ pr, const double* __restric
         fi = acc[npsi + idx];
       }
       for (int s = 0; s < nparts; ++s) {
-        fr += part[(size_t)s * 2 * npsi + idx];
-        fi += part[(size_t)s * 2 * npsi + npsi + idx];
+        fr += part[(size_t)s * bs.part + idx];
+        fi += part[(size_t)s * bs.part + npsi + idx];
       }
       const double m = allow[idx];
       fr *= m;
@@ -345,7 +359,16 @@ __global__ void k_lanczos2(const double* __restrict__ red1, int nblk, double* __
                            double* __restrict__ hi, const double* __restrict__ pr,
                            const double* __restrict__ pi, size_t n, double* __restrict__ red2,
                            double* __restrict__ ra_base, double* __restrict__ ia_base,
-                           const int* __restrict__ itp) {
+                           const int* __restrict__ itp, const BlockStrides bs) {
+  const size_t v = blockIdx.y;
+  red1 += v * bs.red;
+  red2 += v * bs.red;
+  hr += v * bs.vec;
+  hi += v * bs.vec;
+  pr += v * bs.vec;
+  pi += v * bs.vec;
+  ra_base += v * bs.coef;
+  ia_base += v * bs.coef;
   double a, ia;
   reduce_pairs(red1, nblk, &a, &ia);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -370,7 +393,12 @@ __global__ void k_lanczos2(const double* __restrict__ red1, int nblk, double* __
 // Lanczos stage 3: b_i = sqrt(sum); psi_new = h / b_i (in place in h).
 __global__ void k_lanczos3(const double* __restrict__ red2, int nblk, double* __restrict__ hr,
                            double* __restrict__ hi, size_t n, double* __restrict__ rb_base,
-                           const int* __restrict__ itp) {
+                           const int* __restrict__ itp, const BlockStrides bs) {
+  const size_t v = blockIdx.y;
+  red2 += v * bs.red;
+  hr += v * bs.vec;
+  hi += v * bs.vec;
+  rb_base += v * bs.coef;
   double bb, dummy;
   reduce_pairs(red2, nblk, &bb, &dummy);
   const double b = sqrt(bb);
@@ -729,9 +757,9 @@ int kernels_init(ocn_ctx* c) {
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_gemm1_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g1));
   const size_t ff = kmesh_smem(kmesh_geom<double>(c->dims.kmesh, c->na));
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff));
-  if (kmesh_cube_supported(c->dims.kmesh, c->na)) {
+  if (kmesh_cube_supported(c->dims.kmesh)) {
     CubeFnD f;
-    OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], c->na, f);
+    OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], f);
     OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kmesh_cube_smem<double>(c->dims.kmesh[0], c->na)));
   }
@@ -750,8 +778,8 @@ int phase_bloch(ocn_ctx* c, const double* d_ur, const double* d_ui, const double
   return OCN_OK;
 }
 
-int zero_acc(ocn_ctx* c) {
-  OCN_CUDA(c, cudaMemsetAsync(c->d_acc, 0, sizeof(double) * 2 * c->npsi, c->stream));
+int zero_acc(ocn_ctx* c, int nv) {
+  OCN_CUDA(c, cudaMemsetAsync(c->d_acc, 0, sizeof(double) * 2 * c->npsi * nv, c->stream));
   return OCN_OK;
 }
 
@@ -770,9 +798,9 @@ int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi) {
     const KmeshGeom<double> g = kmesh_geom<double>(c->dims.kmesh, na);
     TimedScope ts(c, T_LR_FFT);
     CubeFnD f = nullptr;
-    if (kmesh_cube_supported(c->dims.kmesh, na)) OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], na, f);
+    if (kmesh_cube_supported(c->dims.kmesh)) OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], f);
     if (f)
-      f<<<nx, 128, kmesh_cube_smem<double>(c->dims.kmesh[0], na), c->stream>>>(c->d_phi, c->d_W, nx);
+      f<<<nx, 128, kmesh_cube_smem<double>(c->dims.kmesh[0], na), c->stream>>>(c->d_phi, c->d_W, nx, na);
     else
       k_lr_fft_w_fp64<<<nx, 256, kmesh_smem(g), c->stream>>>(c->d_phi, c->d_W, nx, g);
     ++c->launches;
@@ -792,7 +820,7 @@ int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi) {
   return OCN_OK;
 }
 
-int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi) {
+int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi, double* acc) {
   MultDev& m = c->mult;
   TimedScope ts(c, T_MULT);
   const int nbk = c->nb * c->nk;
@@ -823,55 +851,61 @@ int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi) {
   {
     const size_t sm = sizeof(double2) * (size_t)npa;
     const int block = 64;
-    k_mult_back<<<(nbk + block - 1) / block, block, sm, c->stream>>>(m.mpc, m.hamp, c->d_acc, nbk,
-                                                                    m.np, c->na, c->nspn, c->npsi);
+    k_mult_back<<<(nbk + block - 1) / block, block, sm, c->stream>>>(m.mpc, m.hamp, acc, nbk, m.np,
+                                                                    c->na, c->nspn, c->npsi);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }
   return OCN_OK;
 }
 
-int combine(ocn_ctx* c, const double* d_pr, const double* d_pi, double* d_or, double* d_oi,
-            const int* hflag, int backwards) {
+int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* d_or, double* d_oi,
+            size_t vstride, const int* hflag, int backwards) {
   const int nbk = c->nb * c->nk;
   const int use_so = (c->sys.mult && hflag[5] == 1 && c->have_so) ? 1 : 0;
   const int nparts = (c->sys.long_range && hflag[0] == 1) ? c->lr_xsplit : 0;
+  const BlockStrides bs = {vstride, c->part_stride, 0, 0};
   auto kern = (c->na == 4) ? k_combine<4> : k_combine<12>;
-  kern<<<grid_for(nbk, 256, 4 * c->sm_count), 256, 0, c->stream>>>(
+  dim3 grid(grid_for(nbk, 256, 4 * c->sm_count), nv);
+  kern<<<grid, 256, 0, c->stream>>>(
       d_pr, d_pi, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow,
       c->acc_valid ? c->d_acc : nullptr, c->d_accpart, nparts,
       c->d_so, d_or, d_oi, nbk, c->na, c->npsi, c->sys.e0, use_so, backwards, nullptr, nullptr,
-      nullptr, nullptr, nullptr);
+      nullptr, nullptr, nullptr, bs);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;
 }
 
-// Fused combine + ocean_hay_ab_twoterm for iteration i = *itp: reads b_{i-1} from
-// rb, writes a_{i-1}, Im a_{i-1} and b_i (OCEAN_haydock.f90:848-889).
-int lanczos_launch(ocn_ctx* c, const double* old_r, const double* old_i, const double* psi_r,
-                   const double* psi_i, double* h_r, double* h_i, double* ra, double* ia,
-                   double* rb, const int* itp) {
+// Fused combine + ocean_hay_ab_twoterm for iteration i = *itp of nv chains:
+// reads b_{i-1} from rb, writes a_{i-1}, Im a_{i-1} and b_i
+// (OCEAN_haydock.f90:848-889).  old/psi/h are block bases (vector stride 2*npsi),
+// ra/ia/rb coefficient bases with cstride between chains.
+int lanczos_launch(ocn_ctx* c, int nv, const double* old, const double* psi, double* h, double* ra,
+                   double* ia, double* rb, size_t cstride, const int* itp) {
   const int nbk = c->nb * c->nk;
+  const size_t n = c->npsi;
   const int* hf = c->sys.nhflag;
   const int use_so = (c->sys.mult && hf[5] == 1 && c->have_so) ? 1 : 0;
   const int nparts = (c->sys.long_range && hf[0] == 1) ? c->lr_xsplit : 0;
   const int nblk = c->red_blocks;
+  const BlockStrides bs = {2 * n, c->part_stride, cstride, (size_t)4 * nblk};
   TimedScope ts(c, T_LANCZOS);
+  dim3 grid(nblk, nv);
   auto kern = (c->na == 4) ? k_combine<4> : k_combine<12>;
-  kern<<<nblk, 256, 0, c->stream>>>(psi_r, psi_i, c->d_er, c->ei_nonzero ? c->d_ei : nullptr,
+  kern<<<grid, 256, 0, c->stream>>>(psi, psi + n, c->d_er, c->ei_nonzero ? c->d_ei : nullptr,
                                     c->d_allow, c->acc_valid ? c->d_acc : nullptr, c->d_accpart,
-                                    nparts, c->d_so, h_r, h_i, nbk, c->na, c->npsi, c->sys.e0,
-                                    use_so, 0, old_r, old_i, rb, itp, c->d_red);
+                                    nparts, c->d_so, h, h + n, nbk, c->na, n, c->sys.e0, use_so, 0,
+                                    old, old + n, rb, itp, c->d_red, bs);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
-  k_lanczos2<<<nblk, 256, 0, c->stream>>>(c->d_red, nblk, h_r, h_i, psi_r, psi_i, c->npsi,
-                                          c->d_red + 2 * nblk, ra, ia, itp);
+  k_lanczos2<<<grid, 256, 0, c->stream>>>(c->d_red, nblk, h, h + n, psi, psi + n, n, c->d_red + 2 * nblk,
+                                          ra, ia, itp, bs);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   if (c->dims.precision == OCN_PREC_MIXED && c->mixed)  // also builds the next psi operand
-    return mixed_norm_prep(c, c->d_red + 2 * nblk, nblk, h_r, h_i, rb, itp);
-  k_lanczos3<<<nblk, 256, 0, c->stream>>>(c->d_red + 2 * nblk, nblk, h_r, h_i, c->npsi, rb, itp);
+    return mixed_norm_prep(c, nv, c->d_red + 2 * nblk, nblk, bs.red, h, rb, cstride, itp);
+  k_lanczos3<<<grid, 256, 0, c->stream>>>(c->d_red + 2 * nblk, nblk, h, h + n, n, rb, itp, bs);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;

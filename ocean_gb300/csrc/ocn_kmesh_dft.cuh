@@ -258,15 +258,15 @@ __host__ __device__ constexpr int cube_slab(int n) {
   return ((n * n * (n + 1) + 15) / 16) * 16 + (sizeof(CT) == 8 ? 4 : 2);
 }
 
-template <typename R, int N, int NA>
-__device__ __forceinline__ void cube_pass(typename C2<R>::T* buf, int ax,
+template <typename R, int N>
+__device__ __forceinline__ void cube_pass(typename C2<R>::T* buf, int nt, int ax,
                                           const typename C2<R>::T* __restrict__ tw, R sgn) {
   typedef typename C2<R>::T CT;
   constexpr int P3 = N + 1;
   constexpr int SLAB = cube_slab<CT>(N);
-  constexpr int LINES = NA * N * N;
+  const int lines = nt * N * N;
   const int st = (ax == 2) ? 1 : ((ax == 1) ? P3 : N * P3);
-  for (int l = threadIdx.x; l < LINES; l += blockDim.x) {
+  for (int l = threadIdx.x; l < lines; l += blockDim.x) {
     const int a = l / (N * N);
     const int r = l % (N * N);
     const int i1 = r / N, i2 = r % N;
@@ -284,26 +284,39 @@ __device__ __forceinline__ void cube_pass(typename C2<R>::T* buf, int ax,
   }
 }
 
-template <typename R, int N, int NA>
+// nt transforms per x-point (alpha, or (vector, alpha) for a block of psi),
+// phi layout [k][x][t].
+template <typename R, int N>
 __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R* __restrict__ W, int nx,
-                                    int x, typename C2<R>::T* buf, const typename C2<R>::T* __restrict__ tw) {
+                                    int x, int nt, typename C2<R>::T* buf,
+                                    const typename C2<R>::T* __restrict__ tw) {
   typedef typename C2<R>::T CT;
   constexpr int NK = N * N * N;
   constexpr int P3 = N + 1;
   constexpr int SLAB = cube_slab<CT>(N);
-  // alpha fastest across threads: a warp reads whole 32-byte sectors of phi,
-  // and the padded slab puts the alpha planes on different shared-memory banks
-  for (int e = threadIdx.x; e < NA * NK; e += blockDim.x) {
-    const int k = e / NA, a = e % NA;
-    buf[a * SLAB + (k / N) * P3 + k % N] = phi[((size_t)k * nx + x) * NA + a];
+  // t fastest across threads: a warp reads whole 32-byte sectors of phi, and the
+  // padded slab puts neighbouring transforms on different shared-memory banks.
+  // (k, t) advance incrementally to avoid a runtime division per element.
+  const int dt = blockDim.x % nt, dk = blockDim.x / nt;
+  {
+    int t = threadIdx.x % nt, k = threadIdx.x / nt;
+    while (k < NK) {
+      buf[t * SLAB + (k / N) * P3 + k % N] = phi[((size_t)k * nx + x) * nt + t];
+      t += dt;
+      k += dk;
+      if (t >= nt) {
+        t -= nt;
+        ++k;
+      }
+    }
   }
   __syncthreads();
 #pragma unroll
   for (int ax = 0; ax < 3; ++ax) {
-    cube_pass<R, N, NA>(buf, ax, tw + ax * OCN_MAX_KDIM, (R)1);
+    cube_pass<R, N>(buf, nt, ax, tw + ax * OCN_MAX_KDIM, (R)1);
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < NA * NK; e += blockDim.x) {
+  for (int e = threadIdx.x; e < nt * NK; e += blockDim.x) {
     const int a = e / NK, k = e % NK;
     const R wv = W[(size_t)x * NK + k];
     CT& v = buf[a * SLAB + (k / N) * P3 + k % N];
@@ -313,58 +326,55 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
   __syncthreads();
 #pragma unroll
   for (int ax = 0; ax < 3; ++ax) {
-    cube_pass<R, N, NA>(buf, ax, tw + ax * OCN_MAX_KDIM, (R)-1);
+    cube_pass<R, N>(buf, nt, ax, tw + ax * OCN_MAX_KDIM, (R)-1);
     __syncthreads();
   }
   const R norm = (R)1 / (R)NK;
-  for (int e = threadIdx.x; e < NA * NK; e += blockDim.x) {
-    const int k = e / NA, a = e % NA;
-    const CT v = buf[a * SLAB + (k / N) * P3 + k % N];
-    CT o;
-    o.x = v.x * norm;
-    o.y = v.y * norm;
-    phi[((size_t)k * nx + x) * NA + a] = o;
+  {
+    int t = threadIdx.x % nt, k = threadIdx.x / nt;
+    while (k < NK) {
+      const CT v = buf[t * SLAB + (k / N) * P3 + k % N];
+      CT o;
+      o.x = v.x * norm;
+      o.y = v.y * norm;
+      phi[((size_t)k * nx + x) * nt + t] = o;
+      t += dt;
+      k += dk;
+      if (t >= nt) {
+        t -= nt;
+        ++k;
+      }
+    }
   }
 }
 
 // dynamic shared memory of a kmesh_convolve_cube CTA: twiddles + padded planes
 template <typename R>
-inline size_t kmesh_cube_smem(int n, int na) {
+inline size_t kmesh_cube_smem(int n, int nt) {
   typedef typename C2<R>::T CT;
-  return sizeof(CT) * (3 * OCN_MAX_KDIM + (size_t)na * cube_slab<CT>(n));
+  return sizeof(CT) * (3 * OCN_MAX_KDIM + (size_t)nt * cube_slab<CT>(n));
 }
 
-// A cubic specialisation exists for these extents and transform counts.
-inline bool kmesh_cube_supported(const int kmesh[3], int na) {
+// A cubic specialisation exists for these extents.
+inline bool kmesh_cube_supported(const int kmesh[3]) {
   if (kmesh[0] != kmesh[1] || kmesh[1] != kmesh[2]) return false;
   const int n = kmesh[0];
-  return (na == 4 || na == 12) && (n == 2 || n == 3 || n == 4 || n == 5 || n == 6 || n == 8);
+  return n == 2 || n == 3 || n == 4 || n == 5 || n == 6 || n == 8;
 }
 
-// Selects the instantiation kern<N, NA> of a kernel template for a supported
-// cubic mesh (kmesh_cube_supported); returns nullptr otherwise.
-#define OCN_CUBE_DISPATCH(KERN, n, na, out)                                      \
-  do {                                                                           \
-    out = nullptr;                                                               \
-    if ((na) == 4) {                                                             \
-      switch (n) {                                                               \
-        case 2: out = KERN<2, 4>; break;                                         \
-        case 3: out = KERN<3, 4>; break;                                         \
-        case 4: out = KERN<4, 4>; break;                                         \
-        case 5: out = KERN<5, 4>; break;                                         \
-        case 6: out = KERN<6, 4>; break;                                         \
-        case 8: out = KERN<8, 4>; break;                                         \
-      }                                                                          \
-    } else if ((na) == 12) {                                                     \
-      switch (n) {                                                               \
-        case 2: out = KERN<2, 12>; break;                                        \
-        case 3: out = KERN<3, 12>; break;                                        \
-        case 4: out = KERN<4, 12>; break;                                        \
-        case 5: out = KERN<5, 12>; break;                                        \
-        case 6: out = KERN<6, 12>; break;                                        \
-        case 8: out = KERN<8, 12>; break;                                        \
-      }                                                                          \
-    }                                                                            \
+// Selects the instantiation kern<N> of a kernel template for a supported cubic
+// mesh (kmesh_cube_supported); returns nullptr otherwise.
+#define OCN_CUBE_DISPATCH(KERN, n, out) \
+  do {                                  \
+    out = nullptr;                      \
+    switch (n) {                        \
+      case 2: out = KERN<2>; break;     \
+      case 3: out = KERN<3>; break;     \
+      case 4: out = KERN<4>; break;     \
+      case 5: out = KERN<5>; break;     \
+      case 6: out = KERN<6>; break;     \
+      case 8: out = KERN<8>; break;     \
+    }                                   \
   } while (0)
 
 // Whole k-mesh step for the x-point of this CTA.  phi layout [k][x][a].

@@ -1,18 +1,20 @@
 // ocn_mixed.cu -- mixed-precision long-range term of the BSE action
-// (long_range.f90:873-963 restated for tensor cores):
+// (long_range.f90:873-963 restated for tensor cores), for a block of nv psi
+// vectors that share H:
 //
-//   phi(k,x,a)  = sum_n u(n,k,x) q(n,k,a),        q = allow o psi        [tcgen05, split-BF16]
-//   phi'(.,x,a) = FFT_fwd[ W(.,x) o FFT_bwd[phi(.,x,a)] ] / Nk                 [FP32, shared memory]
-//   part(n,k,a) = - sum_x conj(u(n,k,x)) phi'(k,x,a)                         [tcgen05, split-BF16]
+//   phi(k,x,v,a)  = sum_n u(n,k,x) q_v(n,k,a),     q = allow o psi_v     [tcgen05, split-BF16]
+//   phi'(.,x,v,a) = FFT_fwd[ W(.,x) o FFT_bwd[phi(.,x,v,a)] ] / Nk            [FP32, shared memory]
+//   part(n,k,v,a) = - sum_x conj(u(n,k,x)) phi'(k,x,v,a)                    [tcgen05, split-BF16]
 //
-// Split-BF16: every FP32 operand v is stored as hi = bf16(v), lo = bf16(v - hi);
-// the MMAs accumulate (A_hi + A_lo)(B_hi + B_lo) in FP32 in tensor memory, which
-// keeps ~16 significant bits of every product.
+// Split-BF16: every FP32 operand value is stored as hi = bf16(v), lo =
+// bf16(v - hi); the MMAs accumulate (A_hi + A_lo)(B_hi + B_lo) in FP32 in tensor
+// memory, which keeps ~16 significant bits of every product.
 //
 // Complex arithmetic is made real by stacking re/im along K (K = (c, n) for the
 // band contraction, K = (c, x) for the x-mesh contraction) and by the output
-// columns j = (split s, part re/im, alpha): D[:, j] + D[:, j + 2Na] is the full
-// product.  The MMA is M = 128 rows x N = 4 Na columns x K = 16 per instruction.
+// columns j = v*4Na + (split s)*2Na + (part re/im)*Na + alpha: D[:, j] +
+// D[:, j + 2Na] is the full product.  MMA shape: M = 128 rows, N = 4 Na nvmax,
+// K = 16 per instruction.  Every byte of u2 read from HBM serves all nv vectors.
 //
 // Operands live in HBM as bf16 tiles read by TMA with 128-byte swizzling:
 //   UA_s [k][x][K1]  (K1 = 2 Nb)      A of the band -> x contraction, built once
@@ -41,27 +43,31 @@ namespace ocn {
 
 namespace {
 
-constexpr int TC_STAGES = 4;
+constexpr int TC_MAX_STAGES = 4;
 constexpr int TC_BM = 128;
 constexpr int TC_BK = 64;  // bf16 elements per 128-byte swizzle row
 constexpr int TC_THREADS = 192;
+constexpr int TC_MAX_NCOL = 256;  // MMA N limit for M = 128
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
+constexpr size_t TC_SMEM_BUDGET = 220 * 1024;
 
 __constant__ float2 c_twf[3][OCN_MAX_KDIM];
-__constant__ int c_kdimf[3];
 
 struct TcParams {
   int mode;      // 1: band -> x (GEMM1), 2: x -> band (GEMM2)
   int ntiles;
   int nb, nk, nx, na;
-  int n4;        // MMA N = 4 Na
+  int ncol;      // MMA N = 4 Na nvmax
+  int nv;        // vectors whose outputs are written
+  int stages;    // shared-memory pipeline depth (<= TC_MAX_STAGES)
   int nch;       // K chunks of the full reduction
   int nxt;       // mode 1: x tiles per k
   int mt2, ks2, cps2;  // mode 2: M tiles, K splits, chunks per split
+  int nvmax;     // partial-buffer vector stride
   uint32_t idesc;
   uint32_t tcols;
-  float2* phi;   // mode 1 output [k][x][a]
-  double* part;  // mode 2 output [split][re|im][npsi]
+  float2* phi;   // mode 1 output [k][x][v*Na + a]
+  double* part;  // mode 2 output [split][v][re|im][npsi]
   size_t npsi;
   int* err;
 };
@@ -186,17 +192,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
   const uint32_t a_bytes = TC_BM * TC_BK * 2;
-  const uint32_t b_bytes = (uint32_t)p.n4 * TC_BK * 2;
+  const uint32_t b_bytes = (uint32_t)p.ncol * TC_BK * 2;
   const uint32_t stage_bytes = 2 * a_bytes + b_bytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + TC_STAGES * stage_bytes);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * TC_STAGES + 4);
+  const int S = p.stages;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * stage_bytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * TC_MAX_STAGES + 4);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-  const uint32_t full0 = su32(bars), empty0 = su32(bars + TC_STAGES);
-  const uint32_t tfull0 = su32(bars + 2 * TC_STAGES), tempty0 = su32(bars + 2 * TC_STAGES + 2);
+  const uint32_t full0 = su32(bars), empty0 = su32(bars + TC_MAX_STAGES);
+  const uint32_t tfull0 = su32(bars + 2 * TC_MAX_STAGES), tempty0 = su32(bars + 2 * TC_MAX_STAGES + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < TC_STAGES; ++s) {
+    for (int s = 0; s < S; ++s) {
       mbar_init(full0 + 8 * s, 1);
       mbar_init(empty0 + 8 * s, 1);
     }
@@ -222,8 +229,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (lane == 0) {
       // ------------------------------------------------------------ producer
       uint32_t stage = 0, phase = 0;
-      int armed_phase[TC_STAGES];
-      for (int s = 0; s < TC_STAGES; ++s) armed_phase[s] = -1;
+      int armed_phase[TC_MAX_STAGES];
+      for (int s = 0; s < TC_MAX_STAGES; ++s) armed_phase[s] = -1;
       bool ok = true;
       for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
         const TileInfo ti = decode(p, t);
@@ -238,7 +245,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           tma_load_3d(sbase + a_bytes, &tm_lo, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k);
           tma_load_3d(sbase + 2 * a_bytes, &tm_b, full0 + 8 * stage, c * TC_BK, 0, ti.k);
           armed_phase[stage] = (int)phase;
-          if (++stage == TC_STAGES) {
+          if (++stage == (uint32_t)S) {
             stage = 0;
             phase ^= 1;
           }
@@ -249,7 +256,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         atomicOr(p.err, 1);
       }
       // drain: never leave a TMA write in flight
-      for (int s = 0; s < TC_STAGES; ++s)
+      for (int s = 0; s < S; ++s)
         if (armed_phase[s] >= 0) {
           const long long t0 = clock64();
           while (!mbar_test(full0 + 8 * s, (uint32_t)armed_phase[s]) &&
@@ -271,7 +278,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           break;
         }
         tc_fence_after();
-        const uint32_t dt = tmem_base + acc * (uint32_t)p.n4;
+        const uint32_t dt = tmem_base + acc * (uint32_t)p.ncol;
         for (int c = ti.c0; c < ti.c1; ++c) {
           if (!mbar_wait(full0 + 8 * stage, phase, abort_flag, TC_WAIT_CYCLES)) {
             ok = false;
@@ -288,7 +295,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           umma_commit(empty0 + 8 * stage);
           last_stage = (int)stage;
           last_phase = phase;
-          if (++stage == TC_STAGES) {
+          if (++stage == (uint32_t)S) {
             stage = 0;
             phase ^= 1;
           }
@@ -312,8 +319,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // -------------------------------------------------------------- epilogue
     const int q = warp & 3;  // TMEM lane quadrant this warp may access
     const int row = q * 32 + lane;
+    const int na = p.na, g4 = 4 * na;
     uint32_t acc = 0, acc_phase = 0;
-    float v[48];
+    float v[48];  // one vector's 4 Na columns
     for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
       const TileInfo ti = decode(p, t);
       if (!mbar_wait(tfull0 + 8 * acc, acc_phase, abort_flag, TC_WAIT_CYCLES)) {
@@ -322,31 +330,32 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         break;
       }
       tc_fence_after();
-      const uint32_t ta = tmem_base + ((uint32_t)(q * 32) << 16) + acc * (uint32_t)p.n4;
-      for (int c16 = 0; c16 < p.n4; c16 += 16) tmem_ld16(ta + c16, v + c16);
-      tmem_ld_wait();
-      tc_fence_before();
-      mbar_arrive(tempty0 + 8 * acc);
-      const int na = p.na;
-      if (p.mode == 1) {
-        const int x = ti.row0 + row;
-        if (x < p.nx) {
-          float2* o = p.phi + ((size_t)ti.k * p.nx + x) * na;
-          for (int a = 0; a < na; ++a)
-            o[a] = make_float2(v[a] + v[2 * na + a], v[na + a] + v[3 * na + a]);
-        }
-      } else {
-        const int n = ti.row0 + row;
-        if (n < p.nb) {
-          double* pr = p.part + (size_t)ti.sp * 2 * p.npsi;
-          double* pim = pr + p.npsi;
-          for (int a = 0; a < na; ++a) {
-            const size_t idx = (size_t)n + (size_t)p.nb * ((size_t)ti.k + (size_t)p.nk * a);
-            pr[idx] = -((double)v[a] + (double)v[2 * na + a]);
-            pim[idx] = -((double)v[na + a] + (double)v[3 * na + a]);
+      const uint32_t ta = tmem_base + ((uint32_t)(q * 32) << 16) + acc * (uint32_t)p.ncol;
+      for (int vv = 0; vv < p.nv; ++vv) {
+        for (int c16 = 0; c16 < g4; c16 += 16) tmem_ld16(ta + vv * g4 + c16, v + c16);
+        tmem_ld_wait();
+        if (p.mode == 1) {
+          const int x = ti.row0 + row;
+          if (x < p.nx) {
+            float2* o = p.phi + ((size_t)ti.k * p.nx + x) * (p.nv * na) + vv * na;
+            for (int a = 0; a < na; ++a)
+              o[a] = make_float2(v[a] + v[2 * na + a], v[na + a] + v[3 * na + a]);
+          }
+        } else {
+          const int n = ti.row0 + row;
+          if (n < p.nb) {
+            double* pr = p.part + ((size_t)ti.sp * p.nvmax + vv) * 2 * p.npsi;
+            double* pim = pr + p.npsi;
+            for (int a = 0; a < na; ++a) {
+              const size_t idx = (size_t)n + (size_t)p.nb * ((size_t)ti.k + (size_t)p.nk * a);
+              pr[idx] = -((double)v[a] + (double)v[2 * na + a]);
+              pim[idx] = -((double)v[na + a] + (double)v[3 * na + a]);
+            }
           }
         }
       }
+      tc_fence_before();
+      mbar_arrive(tempty0 + 8 * acc);
       acc ^= 1;
       if (acc == 0) acc_phase ^= 1;
     }
@@ -408,61 +417,71 @@ __global__ void k_build_ub(const double2* __restrict__ u, __nv_bfloat16* __restr
   }
 }
 
-// B1[k][j][K1], j = s*2Na + part*Na + a, from q = allow o psi:
+// B1[k][v*4Na + j][K1], j = s*2Na + part*Na + a, from q = allow o psi_v:
 //   part 0 (Re phi): K=(0,n) -> qr, K=(1,n) -> -qi;  part 1 (Im phi): (0,n) -> qi, (1,n) -> qr
-__global__ void k_prep_b1(const double* __restrict__ pr, const double* __restrict__ pi,
-                          const double* __restrict__ allow, __nv_bfloat16* __restrict__ b1, int nb,
-                          int nk, int na, int p1) {
-  const int total = nk * 2 * nb;
-  const int n4 = 4 * na;
+// Vector v of the block starts at pr + v*vstride (imaginary plane at +npsi).
+__global__ void k_prep_b1(const double* __restrict__ pr, const double* __restrict__ pi, size_t vstride,
+                          int nv, const double* __restrict__ allow, __nv_bfloat16* __restrict__ b1,
+                          int nb, int nk, int na, int ncol, int p1) {
+  const int total = nv * nk * 2 * nb;
+  const int g4 = 4 * na;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
     const int K = i % (2 * nb);
-    const int k = i / (2 * nb);
+    const int k = (i / (2 * nb)) % nk;
+    const int vv = i / (2 * nb * nk);
     const int c = K < nb ? 0 : 1;
     const int n = K - c * nb;
+    const double* vr = pr + (size_t)vv * vstride;
+    const double* vi = pi + (size_t)vv * vstride;
+    __nv_bfloat16* base = b1 + (size_t)k * ncol * p1 + (size_t)vv * g4 * p1 + K;
     for (int a = 0; a < na; ++a) {
       const size_t idx = (size_t)n + (size_t)nb * ((size_t)k + (size_t)nk * a);
       const double m = allow[idx];
-      const float qr = (float)(pr[idx] * m), qi = (float)(pi[idx] * m);
+      const float qr = (float)(vr[idx] * m), qi = (float)(vi[idx] * m);
       const float v0 = c == 0 ? qr : -qi;
       const float v1 = c == 0 ? qi : qr;
       __nv_bfloat16 h0, l0, h1, l1;
       split_bf16(v0, h0, l0);
       split_bf16(v1, h1, l1);
-      __nv_bfloat16* base = b1 + (size_t)k * n4 * p1 + K;
-      base[(size_t)(0 * 2 * na + 0 * na + a) * p1] = h0;
-      base[(size_t)(0 * 2 * na + 1 * na + a) * p1] = h1;
-      base[(size_t)(1 * 2 * na + 0 * na + a) * p1] = l0;
-      base[(size_t)(1 * 2 * na + 1 * na + a) * p1] = l1;
+      base[(size_t)(a)*p1] = h0;
+      base[(size_t)(na + a) * p1] = h1;
+      base[(size_t)(2 * na + a) * p1] = l0;
+      base[(size_t)(3 * na + a) * p1] = l1;
     }
   }
 }
 
 // Lanczos normalisation fused with the next action's psi operand
-// (OCEAN_haydock.f90:880-889 then long_range.f90:897-906): b_i = sqrt(sum of
-// partials), psi = h / b_i written in place, and B1 built from allow o psi.
-// One thread per (n, k) covers both K = n and K = Nb + n for every alpha.
-__global__ void k_norm_prep(const double* __restrict__ red2, int nblk, double* __restrict__ hr,
-                            double* __restrict__ hi, const double* __restrict__ allow,
-                            __nv_bfloat16* __restrict__ b1, int nb, int nk, int na, int p1,
-                            double* __restrict__ rb_base, const int* __restrict__ itp) {
+// (OCEAN_haydock.f90:880-889 then long_range.f90:897-906): for chain v =
+// blockIdx.y, b_i = sqrt(sum of partials), psi = h / b_i written in place, and
+// B1 rows of vector v built from allow o psi.  One thread per (n, k) covers
+// both K = n and K = Nb + n for every alpha.
+__global__ void k_norm_prep(const double* __restrict__ red2, int nblk, size_t rstride,
+                            double* __restrict__ hbase, size_t vstride, size_t npsi,
+                            const double* __restrict__ allow, __nv_bfloat16* __restrict__ b1, int nb,
+                            int nk, int na, int ncol, int p1, double* __restrict__ rb_base,
+                            size_t cstride, const int* __restrict__ itp) {
   __shared__ double sh[32];
+  const int vv = blockIdx.y;
+  const double* red = red2 + (size_t)vv * rstride;
   double s = 0.0;
-  for (int i = threadIdx.x; i < nblk; i += blockDim.x) s += red2[2 * i];
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) s += red[2 * i];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
   __syncthreads();
   double bb = 0.0;
   for (int i = 0; i < (int)(blockDim.x >> 5); ++i) bb += sh[i];
   const double b = sqrt(bb);
-  if (blockIdx.x == 0 && threadIdx.x == 0) rb_base[*itp] = b;
+  if (blockIdx.x == 0 && threadIdx.x == 0) rb_base[(size_t)vv * cstride + *itp] = b;
   const double inv = 1.0 / b;
-  const int n4 = 4 * na;
+  double* hr = hbase + (size_t)vv * vstride;
+  double* hi = hr + npsi;
+  const int g4 = 4 * na;
   const int total = nb * nk;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
     const int n = i % nb;
     const int k = i / nb;
-    __nv_bfloat16* base = b1 + (size_t)k * n4 * p1;
+    __nv_bfloat16* base = b1 + (size_t)k * ncol * p1 + (size_t)vv * g4 * p1;
     for (int a = 0; a < na; ++a) {
       const size_t idx = (size_t)i + (size_t)total * a;
       const double r = hr[idx] * inv, im = hi[idx] * inv;
@@ -487,58 +506,61 @@ __global__ void k_norm_prep(const double* __restrict__ red2, int nblk, double* _
   }
 }
 
-// B2[k][j][K2] from phi'[k][x][a]:
+// B2[k][v*4Na + j][K2] from phi'[k][x][v*Na + a]:
 //   part 0 (Re out): K=(0,x) -> Re phi', K=(1,x) -> Im phi'
 //   part 1 (Im out): K=(0,x) -> Im phi', K=(1,x) -> -Re phi'
 __global__ void k_prep_b2(const float2* __restrict__ phi, __nv_bfloat16* __restrict__ b2, int nk,
-                          int nx, int na, int p2) {
+                          int nx, int na, int nv, int ncol, int p2) {
   const int total = nk * nx;
-  const int n4 = 4 * na;
+  const int g4 = 4 * na;
+  const int nt = na * nv;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
     const int x = i % nx;
     const int k = i / nx;
-    __nv_bfloat16* base = b2 + (size_t)k * n4 * p2;
-    for (int a = 0; a < na; ++a) {
-      const float2 f = phi[((size_t)k * nx + x) * na + a];
+    for (int t = 0; t < nt; ++t) {
+      const int vv = t / na, a = t % na;
+      __nv_bfloat16* base = b2 + (size_t)k * ncol * p2 + (size_t)vv * g4 * p2;
+      const float2 f = phi[((size_t)k * nx + x) * nt + t];
       __nv_bfloat16 hr, lr, hi, li, hn, ln;
       split_bf16(f.x, hr, lr);
       split_bf16(f.y, hi, li);
       split_bf16(-f.x, hn, ln);
       // part 0
-      base[(size_t)(0 * 2 * na + a) * p2 + x] = hr;
-      base[(size_t)(0 * 2 * na + a) * p2 + nx + x] = hi;
-      base[(size_t)(1 * 2 * na + a) * p2 + x] = lr;
-      base[(size_t)(1 * 2 * na + a) * p2 + nx + x] = li;
+      base[(size_t)(a)*p2 + x] = hr;
+      base[(size_t)(a)*p2 + nx + x] = hi;
+      base[(size_t)(2 * na + a) * p2 + x] = lr;
+      base[(size_t)(2 * na + a) * p2 + nx + x] = li;
       // part 1
-      base[(size_t)(0 * 2 * na + na + a) * p2 + x] = hi;
-      base[(size_t)(0 * 2 * na + na + a) * p2 + nx + x] = hn;
-      base[(size_t)(1 * 2 * na + na + a) * p2 + x] = li;
-      base[(size_t)(1 * 2 * na + na + a) * p2 + nx + x] = ln;
+      base[(size_t)(na + a) * p2 + x] = hi;
+      base[(size_t)(na + a) * p2 + nx + x] = hn;
+      base[(size_t)(3 * na + a) * p2 + x] = li;
+      base[(size_t)(3 * na + a) * p2 + nx + x] = ln;
     }
   }
 }
 
-// FP32 k-mesh transform, one CTA per x-point (ocn_kmesh_dft.cuh).
+// FP32 k-mesh transform, one CTA per x-point (ocn_kmesh_dft.cuh): generic meshes
 __global__ void k_lr_fft_w_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx,
                                const KmeshGeom<float> g) {
   extern __shared__ float2 fsm[];
-  float2* tw = fsm;                   // [3][OCN_MAX_KDIM]
+  float2* tw = fsm;
   float2* buf = fsm + 3 * OCN_MAX_KDIM;
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_twf[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
   __syncthreads();
   kmesh_convolve<float>(phi, W, nx, blockIdx.x, g, buf, tw);
 }
 
-template <int N, int NA>
-__global__ void k_fft_cube_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx) {
+// cubic meshes, nt transforms per x-point
+template <int N>
+__global__ void k_fft_cube_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx, int nt) {
   extern __shared__ float2 fsm[];
   float2* tw = fsm;
   float2* buf = fsm + 3 * OCN_MAX_KDIM;
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_twf[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
   __syncthreads();
-  kmesh_convolve_cube<float, N, NA>(phi, W, nx, blockIdx.x, buf, tw);
+  kmesh_convolve_cube<float, N>(phi, W, nx, blockIdx.x, nt, buf, tw);
 }
-typedef void (*CubeFnF)(float2*, const float*, int);
+typedef void (*CubeFnF)(float2*, const float*, int, int);
 
 __global__ void k_w_to_f32(const double* __restrict__ W, float* __restrict__ Wf, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -553,7 +575,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
 }  // namespace
 
 struct MixedLR {
-  int p1 = 0, p2 = 0, n4 = 0;
+  int p1 = 0, p2 = 0, ncol = 0, nvmax = 1;
   __nv_bfloat16 *ua_hi = nullptr, *ua_lo = nullptr, *ub_hi = nullptr, *ub_lo = nullptr;
   __nv_bfloat16 *b1 = nullptr, *b2 = nullptr;
   float2* phi = nullptr;
@@ -564,7 +586,6 @@ struct MixedLR {
   int grid1 = 1, grid2 = 1;
   size_t smem_bytes = 0;
   void* cube_fn = nullptr;  // specialised k-mesh kernel (CubeFnF), or null
-  size_t cube_smem = 0;
   bool ready = false;
 };
 
@@ -594,25 +615,33 @@ int alloc(ocn_ctx* c, T** p, size_t n) {
 
 int mixed_init(ocn_ctx* c) {
   if (c->nspn != 1) return set_err(c, OCN_ERR_UNSUPPORTED, "mixed precision requires nspn = 1");
+  const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na, nvmax = c->nvec;
+  const int ncol = 4 * na * nvmax;
+  if (ncol > TC_MAX_NCOL)
+    return set_err(c, OCN_ERR_ARG, "nvec too large: 4*nalpha*nvec must be <= 256");
+  const bool cube = kmesh_cube_supported(c->dims.kmesh);
+  const size_t fsm = cube ? kmesh_cube_smem<float>(c->dims.kmesh[0], na * nvmax)
+                          : kmesh_smem(kmesh_geom<float>(c->dims.kmesh, na * nvmax));
+  if (fsm > 227u * 1024u)
+    return set_err(c, OCN_ERR_ARG, "nvec*nalpha*Nk too large for the shared-memory k-mesh transform");
   MixedLR* m = new (std::nothrow) MixedLR();
   if (!m) return set_err(c, OCN_ERR_ALLOC, "host allocation failed");
   c->mixed = m;
-  const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na;
-  m->n4 = 4 * na;
+  m->nvmax = nvmax;
+  m->ncol = ncol;
   m->p1 = (2 * nb + 7) / 8 * 8;
   m->p2 = (2 * nx + 7) / 8 * 8;
   int rc;
   if ((rc = alloc(c, &m->ua_hi, (size_t)nk * nx * m->p1)) || (rc = alloc(c, &m->ua_lo, (size_t)nk * nx * m->p1)) ||
       (rc = alloc(c, &m->ub_hi, (size_t)nk * nb * m->p2)) || (rc = alloc(c, &m->ub_lo, (size_t)nk * nb * m->p2)) ||
-      (rc = alloc(c, &m->b1, (size_t)nk * m->n4 * m->p1)) || (rc = alloc(c, &m->b2, (size_t)nk * m->n4 * m->p2)) ||
-      (rc = alloc(c, &m->phi, (size_t)nk * nx * na)) || (rc = alloc(c, &m->Wf, (size_t)nk * nx)) ||
+      (rc = alloc(c, &m->b1, (size_t)nk * ncol * m->p1)) || (rc = alloc(c, &m->b2, (size_t)nk * ncol * m->p2)) ||
+      (rc = alloc(c, &m->phi, (size_t)nk * nx * na * nvmax)) || (rc = alloc(c, &m->Wf, (size_t)nk * nx)) ||
       (rc = alloc(c, &m->d_err, 1)))
     return rc;
   OCN_CUDA(c, cudaMemset(m->d_err, 0, sizeof(int)));
-  // pitch padding of the operands is never read (TMA bounds are the logical
-  // extents) but is cleared so the buffers hold defined values
-  OCN_CUDA(c, cudaMemset(m->b1, 0, (size_t)nk * m->n4 * m->p1 * 2));
-  OCN_CUDA(c, cudaMemset(m->b2, 0, (size_t)nk * m->n4 * m->p2 * 2));
+  // operand rows of vectors outside the current block keep finite (zero) values
+  OCN_CUDA(c, cudaMemset(m->b1, 0, (size_t)nk * ncol * m->p1 * 2));
+  OCN_CUDA(c, cudaMemset(m->b2, 0, (size_t)nk * ncol * m->p2 * 2));
 
   void* fnp = nullptr;
   cudaDriverEntryPointQueryResult q;
@@ -621,18 +650,25 @@ int mixed_init(ocn_ctx* c) {
   EncodeTiledFn fn = reinterpret_cast<EncodeTiledFn>(fnp);
   if ((rc = encode3d(c, fn, &m->tm_ua_hi, m->ua_hi, 2 * nb, nx, nk, m->p1, TC_BM)) ||
       (rc = encode3d(c, fn, &m->tm_ua_lo, m->ua_lo, 2 * nb, nx, nk, m->p1, TC_BM)) ||
-      (rc = encode3d(c, fn, &m->tm_b1, m->b1, 2 * nb, m->n4, nk, m->p1, m->n4)) ||
+      (rc = encode3d(c, fn, &m->tm_b1, m->b1, 2 * nb, ncol, nk, m->p1, ncol)) ||
       (rc = encode3d(c, fn, &m->tm_ub_hi, m->ub_hi, 2 * nx, nb, nk, m->p2, TC_BM)) ||
       (rc = encode3d(c, fn, &m->tm_ub_lo, m->ub_lo, 2 * nx, nb, nk, m->p2, TC_BM)) ||
-      (rc = encode3d(c, fn, &m->tm_b2, m->b2, 2 * nx, m->n4, nk, m->p2, m->n4)))
+      (rc = encode3d(c, fn, &m->tm_b2, m->b2, 2 * nx, ncol, nk, m->p2, ncol)))
     return rc;
 
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(m->n4 >> 3) << 17) |
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(ncol >> 3) << 17) |
                          ((uint32_t)(TC_BM >> 4) << 24);
-  const uint32_t tcols = (2 * m->n4 <= 32) ? 32u : ((2 * m->n4 <= 64) ? 64u : 128u);
+  uint32_t tcols = 32;
+  while ((int)tcols < 2 * ncol) tcols <<= 1;
+  const size_t stage_bytes = 2 * (size_t)TC_BM * TC_BK * 2 + (size_t)ncol * TC_BK * 2;
+  const int stages = (int)std::min<size_t>(TC_MAX_STAGES, (TC_SMEM_BUDGET - 1024 - 256) / stage_bytes);
   TcParams& g1 = m->g1;
   g1.mode = 1;
-  g1.nb = nb; g1.nk = nk; g1.nx = nx; g1.na = na; g1.n4 = m->n4;
+  g1.nb = nb; g1.nk = nk; g1.nx = nx; g1.na = na;
+  g1.ncol = ncol;
+  g1.nv = 1;
+  g1.nvmax = nvmax;
+  g1.stages = stages;
   g1.nch = (2 * nb + TC_BK - 1) / TC_BK;
   g1.nxt = (nx + TC_BM - 1) / TC_BM;
   g1.ntiles = nk * g1.nxt;
@@ -652,20 +688,19 @@ int mixed_init(ocn_ctx* c) {
   g2.ks2 = (g2.nch + g2.cps2 - 1) / g2.cps2;  // no empty split
   g2.ntiles = nk * g2.mt2 * g2.ks2;
   c->lr_xsplit = g2.ks2;
-  if ((rc = alloc(c, &c->d_accpart, (size_t)g2.ks2 * 2 * c->npsi))) return rc;
+  c->part_stride = (size_t)nvmax * 2 * c->npsi;
+  if ((rc = alloc(c, &c->d_accpart, (size_t)g2.ks2 * c->part_stride))) return rc;
   g2.part = c->d_accpart;
-  m->smem_bytes = 1024 + TC_STAGES * (size_t)(2 * TC_BM * TC_BK * 2 + m->n4 * TC_BK * 2) + 256;
+  m->smem_bytes = 1024 + stages * stage_bytes + 256;
   m->grid1 = std::min(g1.ntiles, c->sm_count);
   m->grid2 = std::min(g2.ntiles, c->sm_count);
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->smem_bytes));
-  const size_t fsm = kmesh_smem(kmesh_geom<float>(c->dims.kmesh, na));
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
-  if (kmesh_cube_supported(c->dims.kmesh, na)) {
+  if (cube) {
     CubeFnF f;
-    OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], na, f);
+    OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], f);
     m->cube_fn = reinterpret_cast<void*>(f);
-    m->cube_smem = kmesh_cube_smem<float>(c->dims.kmesh[0], na);
-    OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->cube_smem));
+    OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
   }
   // FP32 twiddles, rounded from FP64 roots of unity
   float2 tw[3][OCN_MAX_KDIM];
@@ -677,7 +712,6 @@ int mixed_init(ocn_ctx* c) {
                        : make_float2(0.f, 0.f);
     }
   OCN_CUDA(c, cudaMemcpyToSymbol(c_twf, tw, sizeof(tw)));
-  OCN_CUDA(c, cudaMemcpyToSymbol(c_kdimf, c->dims.kmesh, sizeof(int) * 3));
   return OCN_OK;
 }
 
@@ -721,51 +755,52 @@ int mixed_check(ocn_ctx* c) {
   return OCN_OK;
 }
 
-int mixed_norm_prep(ocn_ctx* c, const double* red2, int nblk, double* hr, double* hi, double* rb,
-                    const int* itp) {
+int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rstride, double* h,
+                    double* rb, size_t cstride, const int* itp) {
   MixedLR* m = c->mixed;  // timed as part of the enclosing Lanczos step
-  k_norm_prep<<<nblk, 256, 0, c->stream>>>(red2, nblk, hr, hi, c->d_allow, m->b1, c->nb, c->nk, c->na,
-                                           m->p1, rb, itp);
+  dim3 grid(nblk, nv);
+  k_norm_prep<<<grid, 256, 0, c->stream>>>(red2, nblk, rstride, h, 2 * c->npsi, c->npsi, c->d_allow, m->b1,
+                                           c->nb, c->nk, c->na, m->ncol, m->p1, rb, cstride, itp);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;
 }
 
-int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi) {
+int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vstride, int nv) {
   MixedLR* m = c->mixed;
   TimedScope ts(c, T_LR_PREP);
-  const int total = c->nk * 2 * c->nb;
+  const int total = nv * c->nk * 2 * c->nb;
   k_prep_b1<<<std::min((total + 255) / 256, 8 * c->sm_count), 256, 0, c->stream>>>(
-      d_pr, d_pi, c->d_allow, m->b1, c->nb, c->nk, c->na, m->p1);
+      d_pr, d_pi, vstride, nv, c->d_allow, m->b1, c->nb, c->nk, c->na, m->ncol, m->p1);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;
 }
 
-int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, bool b1_ready) {
+int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vstride, int nv,
+                   bool b1_ready) {
   MixedLR* m = c->mixed;
   if (!m || !m->ready) return set_err(c, OCN_ERR_STATE, "mixed-precision operands not built");
-  const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na;
-  if (!b1_ready) {
-    TimedScope ts(c, T_LR_PREP);
-    const int total = nk * 2 * nb;
-    k_prep_b1<<<std::min((total + 255) / 256, 8 * c->sm_count), 256, 0, c->stream>>>(
-        d_pr, d_pi, c->d_allow, m->b1, nb, nk, na, m->p1);
-    ++c->launches;
-    OCN_CUDA(c, cudaGetLastError());
-  }
+  if (nv < 1 || nv > m->nvmax) return set_err(c, OCN_ERR_ARG, "block size exceeds nvec");
+  const int nk = c->nk, nx = c->nx, na = c->na;
+  int rc;
+  if (!b1_ready && (rc = mixed_prep_b1(c, d_pr, d_pi, vstride, nv))) return rc;
+  TcParams g1 = m->g1, g2 = m->g2;
+  g1.nv = nv;
+  g2.nv = nv;
   {
     TimedScope ts(c, T_LR_GEMM1);
-    k_lr_tc<<<m->grid1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ua_hi, m->tm_ua_lo, m->tm_b1, m->g1);
+    k_lr_tc<<<m->grid1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ua_hi, m->tm_ua_lo, m->tm_b1, g1);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }
   {
     TimedScope ts(c, T_LR_FFT);
     if (m->cube_fn) {
-      reinterpret_cast<CubeFnF>(m->cube_fn)<<<nx, 128, m->cube_smem, c->stream>>>(m->phi, m->Wf, nx);
+      reinterpret_cast<CubeFnF>(m->cube_fn)<<<nx, 128, kmesh_cube_smem<float>(c->dims.kmesh[0], na * nv),
+                                               c->stream>>>(m->phi, m->Wf, nx, na * nv);
     } else {
-      const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na);
+      const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na * nv);
       k_lr_fft_w_f32<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g);
     }
     ++c->launches;
@@ -774,14 +809,14 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, bool b1_r
   {
     TimedScope ts(c, T_LR_PREP);
     const int total = nk * nx;
-    k_prep_b2<<<std::min((total + 255) / 256, 8 * c->sm_count), 256, 0, c->stream>>>(m->phi, m->b2, nk,
-                                                                                       nx, na, m->p2);
+    k_prep_b2<<<std::min((total + 255) / 256, 8 * c->sm_count), 256, 0, c->stream>>>(m->phi, m->b2, nk, nx,
+                                                                                       na, nv, m->ncol, m->p2);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }
   {
     TimedScope ts(c, T_LR_GEMM2);
-    k_lr_tc<<<m->grid2, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ub_hi, m->tm_ub_lo, m->tm_b2, m->g2);
+    k_lr_tc<<<m->grid2, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ub_hi, m->tm_ub_lo, m->tm_b2, g2);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }
