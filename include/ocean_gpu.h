@@ -249,6 +249,23 @@ typedef struct {
 int ocn_spectrum_cf(const double* real_a, const double* imag_a, const double* real_b,
                     int iter, double kpref, const ocn_cf_params* p, double* out /* (ne+1)*9 */);
 
+/* ocn_spectrum_cf (write_core path only) without any device allocation: no
+ * counterpart in the reference, which evaluates the fraction on the host.  For
+ * callers that cannot allocate device memory at that point (HBM held by a
+ * caching allocator or by the vectors of a large run) or must not stall the
+ * device with cudaFree.  Its buffers live in one static device array of
+ * 3*(OCN_CF_NOALLOC_MAX_ITER+1) + 10*(OCN_CF_NOALLOC_MAX_NE+1) doubles (736 KiB).
+ * Runs on the calling thread's current device; the first call on a device looks
+ * up that array's address (set-up), so make it before any stream capture.
+ * iter > OCN_CF_NOALLOC_MAX_ITER, ne > OCN_CF_NOALLOC_MAX_NE and Voigt broadening
+ * (gam_gauss > gam0/10) return OCN_ERR_ARG.  Nothing must be zeroed first.  Calls
+ * that overlap on one device share the array and race: serialise them.  Same
+ * output as ocn_spectrum_cf; on error the contents of out are unspecified. */
+#define OCN_CF_NOALLOC_MAX_ITER 4096
+#define OCN_CF_NOALLOC_MAX_NE 8192
+int ocn_spectrum_cf_noalloc(const double* real_a, const double* imag_a, const double* real_b,
+                            int iter, double kpref, const ocn_cf_params* p, double* out);
+
 /* redtrid (OCEAN_haydock.f90:2273-2316): eigenvalues (ascending) of the (n+1)x(n+1)
  * tridiagonal Lanczos matrix; host FP64. */
 int ocn_redtrid(int n, const double* real_a, const double* real_b, double* w /* n+1 */);

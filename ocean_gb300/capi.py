@@ -72,7 +72,7 @@ EXPORTS = [
     "ocn_apply_H_dev", "ocn_haydock", "ocn_haydock_dev", "ocn_psi_pnorm", "ocn_spectrum_cf",
     "ocn_redtrid", "ocn_gmres", "ocn_kernel_launches", "ocn_w2_host", "ocn_phase_table_host",
     "ocn_timing_enable", "ocn_timing_reset", "ocn_timing_read", "ocn_stream", "ocn_apply_H_block",
-    "ocn_haydock_block", "ocn_haydock_block_dev",
+    "ocn_haydock_block", "ocn_haydock_block_dev", "ocn_spectrum_cf_noalloc",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -358,6 +358,21 @@ def spectrum_cf(ra, ia, rb, iteration: int, kpref: float, el: float, eh: float, 
     ia_p = None if ia is None else _dp(_f64(ia))
     check(lib.ocn_spectrum_cf(_dp(_f64(ra)), ia_p, _dp(_f64(rb)), iteration, C.c_double(kpref),
                               C.byref(p), _dp(out)))
+    return out.reshape(ne + 1, 9)
+
+
+def spectrum_cf_noalloc(ra, ia, rb, iteration: int, kpref: float, el: float, eh: float, ne: int,
+                        gam0: float, ebase: float = 0.0, ucvol: float = 1.0, old_broaden: int = 0,
+                        nval: float = 0.0, eps: float = 1.0) -> np.ndarray:
+    """write_core through ocn_spectrum_cf_noalloc (static device scratch, no allocation)."""
+    lib = load()
+    p = OcnCfParams()
+    p.el, p.eh, p.gam0, p.ebase, p.gam_gauss = el, eh, gam0, ebase, 0.0
+    p.ne, p.ucvol, p.old_broaden, p.nval, p.eps = ne, ucvol, old_broaden, nval, eps
+    out = np.zeros((ne + 1) * 9)
+    ia_p = None if ia is None else _dp(_f64(ia))
+    check(lib.ocn_spectrum_cf_noalloc(_dp(_f64(ra)), ia_p, _dp(_f64(rb)), iteration, C.c_double(kpref),
+                                      C.byref(p), _dp(out)))
     return out.reshape(ne + 1, 9)
 
 

@@ -891,6 +891,15 @@ int ocn_spectrum_cf(const double* real_a, const double* imag_a, const double* re
   return rc;
 }
 
+int ocn_spectrum_cf_noalloc(const double* real_a, const double* imag_a, const double* real_b, int iter,
+                            double kpref, const ocn_cf_params* p, double* out) {
+  if (!real_a || !real_b || !p || !out) return set_err(nullptr, OCN_ERR_ARG, "null argument");
+  std::string err;
+  int rc = cf_eval_noalloc(real_a, imag_a, real_b, iter, kpref, p, out, &err);
+  if (rc) set_err(nullptr, rc, err);
+  return rc;
+}
+
 int ocn_redtrid(int n, const double* real_a, const double* real_b, double* w) {
   if (n < 0 || !real_a || !real_b || !w) return OCN_ERR_ARG;
   return redtrid_eigs(n, real_a, real_b, w) ? OCN_ERR_SOLVE : OCN_OK;

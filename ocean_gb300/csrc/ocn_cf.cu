@@ -10,6 +10,7 @@
 // and sum rounds exactly as written.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -239,6 +240,112 @@ int cf_eval(const double* ra, const double* ia, const double* rb, int iter, doub
     if (err) *err = std::string("ocn_spectrum_cf: ") + cudaGetErrorString(e);
     return OCN_ERR_CUDA;
   }
+  return OCN_OK;
+}
+
+// ---- write_core without allocation (ocn_spectrum_cf_noalloc) ----------------
+//
+// Some callers cannot allocate device memory at the moment they want a spectrum:
+// a run whose HBM is held by a caching allocator or by the Lanczos / Krylov
+// buffers of a large problem (cudaMalloc then fails, or makes the pool hand
+// memory back), and callers that must not stall the device, because cudaFree
+// waits for all work on it, including other streams' Haydock chains.  For them
+// this variant keeps every device buffer of k_write_core in one fixed array.
+//
+// Scratch layout, in doubles: real_a | imag_a | real_b (kNaCoef each) | damping
+// column (kNaRows) | output rows (9 * kNaRows).  No part of it has to start at
+// zero: each call uploads every coefficient and damping value that the kernel
+// reads before it launches, and the kernel writes every output row that is
+// copied back.  Calls that overlap on one device (two host threads of one
+// process) share the array and race; a caller serialises them.  Each process
+// and each device has its own copy.
+namespace {
+
+constexpr size_t kNaCoef = (size_t)OCN_CF_NOALLOC_MAX_ITER + 1;
+constexpr size_t kNaRows = (size_t)OCN_CF_NOALLOC_MAX_NE + 1;
+constexpr size_t kNaDoubles = 3 * kNaCoef + 10 * kNaRows;  // 94,221 doubles = 736 KiB
+
+static __device__ __align__(256) double g_cf_scratch[kNaDoubles];
+
+// Device address of g_cf_scratch per device, looked up once with that device
+// current (the first call on a device does the set-up).
+constexpr int kNaMaxDevices = 64;
+std::atomic<double*> g_cf_scratch_ptr[kNaMaxDevices] = {};
+
+int noalloc_scratch(double** out, std::string* err) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    if (err) *err = std::string("ocn_spectrum_cf_noalloc: cudaGetDevice: ") + cudaGetErrorString(e);
+    return OCN_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= kNaMaxDevices) {
+    if (err) *err = "ocn_spectrum_cf_noalloc: device ordinal beyond the set-up table (64 devices)";
+    return OCN_ERR_ARG;
+  }
+  double* p = g_cf_scratch_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    void* q = nullptr;
+    e = cudaGetSymbolAddress(&q, g_cf_scratch);
+    if (e != cudaSuccess || !q) {
+      if (err)
+        *err = std::string("ocn_spectrum_cf_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+      return OCN_ERR_CUDA;
+    }
+    p = static_cast<double*>(q);
+    g_cf_scratch_ptr[dev].store(p, std::memory_order_release);
+  }
+  *out = p;
+  return OCN_OK;
+}
+
+}  // namespace
+
+int cf_eval_noalloc(const double* ra, const double* ia, const double* rb, int iter, double kpref,
+                    const ocn_cf_params* p, double* out, std::string* err) {
+  auto fail = [&](int code, const std::string& msg) {
+    if (err) *err = "ocn_spectrum_cf_noalloc: " + msg;
+    return code;
+  };
+  if (iter < 1 || p->ne < 1) return fail(OCN_ERR_ARG, "iter and ne must be >= 1");
+  if (iter > OCN_CF_NOALLOC_MAX_ITER)
+    return fail(OCN_ERR_ARG, "iter = " + std::to_string(iter) + " exceeds the static scratch limit of " +
+                                 std::to_string(OCN_CF_NOALLOC_MAX_ITER) + "; use ocn_spectrum_cf");
+  if (p->ne > OCN_CF_NOALLOC_MAX_NE)
+    return fail(OCN_ERR_ARG, "ne = " + std::to_string(p->ne) + " exceeds the static scratch limit of " +
+                                 std::to_string(OCN_CF_NOALLOC_MAX_NE) + "; use ocn_spectrum_cf");
+  if (p->gam_gauss > p->gam0 / 10.0)
+    return fail(OCN_ERR_ARG, "Voigt broadening (gam_gauss > gam0/10) is not available here; use ocn_spectrum_cf");
+  double* s = nullptr;
+  int rc = noalloc_scratch(&s, err);
+  if (rc) return rc;
+  double* d_ra = s;
+  double* d_ia = s + kNaCoef;
+  double* d_rb = s + 2 * kNaCoef;
+  double* d_g1 = s + 3 * kNaCoef;
+  double* d_out = d_g1 + kNaRows;
+  const int ne = p->ne;
+  const size_t nco = (size_t)iter + 1;
+  cudaError_t e = cudaMemcpy(d_ra, ra, nco * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_rb, rb, nco * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && ia) e = cudaMemcpy(d_ia, ia, nco * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && p->old_broaden) {
+    // the damping column is staged in the caller's output array, overwritten below
+    for (int row = 0; row <= ne; ++row) {
+      const double en = p->el + (p->eh - p->el) * (double)(2 * row) / (double)(2 * ne);
+      out[row] = p->gam0 + gamfcn(en, p->nval, p->eps);
+    }
+    e = cudaMemcpy(d_g1, out, (size_t)(ne + 1) * sizeof(double), cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) {
+    k_write_core<<<(ne + 1 + 63) / 64, 64>>>(d_ra, ia ? d_ia : nullptr, d_rb, iter, kpref, p->el, p->eh, ne,
+                                           p->gam0, p->old_broaden ? d_g1 : nullptr, p->ebase, p->ucvol,
+                                           d_out);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpy(out, d_out, (size_t)(ne + 1) * 9 * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail(OCN_ERR_CUDA, cudaGetErrorString(e));
   return OCN_OK;
 }
 

@@ -218,6 +218,8 @@ int vec_fill(ocn_ctx* c, double* x, double vr, double vi);
 // ---- continued fraction (ocn_cf.cu)
 int cf_eval(const double* ra, const double* ia, const double* rb, int iter, double kpref,
             const ocn_cf_params* p, double* out, std::string* err);
+int cf_eval_noalloc(const double* ra, const double* ia, const double* rb, int iter, double kpref,
+                    const ocn_cf_params* p, double* out, std::string* err);
 
 // ---- mixed precision (ocn_mixed.cu)
 int mixed_init(ocn_ctx* c);
