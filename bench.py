@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--workload", default="c2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--block", type=int, default=3,
+                    help="chains of the block-Haydock leg (polarisations sharing H); 0 = off")
     ap.add_argument("--gmres-omega", type=int, default=200,
                     help="energies of the GMRES leg (0 disables it)")
     return ap.parse_args()
@@ -345,6 +347,38 @@ def run_ours(args, ws, rank, local, pg):
               "max_rel_error": float(np.max(np.abs(rel)))}
     ctx.close()
 
+    # ---- block leg: nb chains (polarisations of one site) in lockstep, psi0 in HBM
+    blk = None
+    if rank == 0 and args.block > 1 and prec == capi.OCN_PREC_MIXED:
+        nvb = args.block
+        cb = capi.Context(w, precision=prec, device=local, nvec=nvb)
+        rng = np.random.default_rng(1000 + rank)
+        d_blk = torch.empty(2 * n * nvb, dtype=torch.float64, device=dev)
+        for v in range(nvb):
+            r = w.psi_r if v == 0 else rng.standard_normal(n)
+            i = w.psi_i if v == 0 else rng.standard_normal(n)
+            nrm = np.sqrt(np.sum(r * r + i * i))
+            d_blk[2 * v * n:(2 * v + 1) * n].copy_(torch.from_numpy(r / nrm))
+            d_blk[(2 * v + 1) * n:(2 * v + 2) * n].copy_(torch.from_numpy(i / nrm))
+        torch.cuda.synchronize()
+        sb = torch.cuda.ExternalStream(cb.stream, device=dev)
+        cb.haydock_block_dev(niter, nvb, d_blk.data_ptr())  # warm-up (graph capture)
+        b0 = torch.cuda.Event(enable_timing=True)
+        b1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        b0.record(sb)
+        for _ in range(args.steps):
+            ra, ia, rb, done = cb.haydock_block_dev(niter, nvb, d_blk.data_ptr())
+            for v in range(nvb):
+                capi.spectrum_cf(ra[v], ia[v], rb[v], int(done[v]), w.kpref, w.el, w.eh, ne, w.gam0)
+        b1.record(sb)
+        torch.cuda.synchronize()
+        bms = b0.elapsed_time(b1)
+        cb.close()
+        blk = {"chains": nvb, "value": nvb * niter * args.steps / (bms / 1000.0), "unit": UNIT,
+               "ms_per_step": bms / args.steps,
+               "spectra_per_s": nvb * args.steps / (bms / 1000.0)}
+
     if rank != 0:
         return
     # ---- the project's own FP64 GPU path on the same input: speed and the
@@ -392,7 +426,7 @@ def run_ours(args, ws, rank, local, pg):
                        "l2": "inputs larger than L2 (u2 %.2f GB per contraction operand)" % (
                            w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
             "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
-            "fp64_gpu": fp64, "gmres": gm, "roofline": roof, "cpu_baseline": cpu,
+            "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
                     "d2h_bytes_per_step": 3 * (niter + 1) * 8 + (ne + 1) * 9 * 8},
             "gpu_launches": launches, "clocks": clocks, "kernel_ms": kt}

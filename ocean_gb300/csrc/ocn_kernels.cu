@@ -121,14 +121,14 @@ __global__ void k_lr_fft_w_fp64(double2* __restrict__ phi, const double* __restr
   kmesh_convolve<double>(phi, W, nx, blockIdx.x, g, buf, tw);
 }
 
-template <int N>
+template <int N, int NTC>
 __global__ void k_fft_cube_fp64(double2* __restrict__ phi, const double* __restrict__ W, int nx, int nt) {
   extern __shared__ double2 smem[];
   double2* tw = smem;
   double2* buf = smem + 3 * OCN_MAX_KDIM;
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_tw[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
   __syncthreads();
-  kmesh_convolve_cube<double, N>(phi, W, nx, blockIdx.x, nt, buf, tw);
+  kmesh_convolve_cube<double, N, NTC>(phi, W, nx, blockIdx.x, nt, buf, tw);
 }
 typedef void (*CubeFnD)(double2*, const double*, int, int);
 
@@ -759,7 +759,7 @@ int kernels_init(ocn_ctx* c) {
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff));
   if (kmesh_cube_supported(c->dims.kmesh)) {
     CubeFnD f;
-    OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], f);
+    OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], c->na, f);
     OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kmesh_cube_smem<double>(c->dims.kmesh[0], c->na)));
   }
@@ -798,7 +798,7 @@ int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi) {
     const KmeshGeom<double> g = kmesh_geom<double>(c->dims.kmesh, na);
     TimedScope ts(c, T_LR_FFT);
     CubeFnD f = nullptr;
-    if (kmesh_cube_supported(c->dims.kmesh)) OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], f);
+    if (kmesh_cube_supported(c->dims.kmesh)) OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], na, f);
     if (f)
       f<<<nx, 128, kmesh_cube_smem<double>(c->dims.kmesh[0], na), c->stream>>>(c->d_phi, c->d_W, nx, na);
     else

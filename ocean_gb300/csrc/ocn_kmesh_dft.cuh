@@ -258,12 +258,14 @@ __host__ __device__ constexpr int cube_slab(int n) {
   return ((n * n * (n + 1) + 15) / 16) * 16 + (sizeof(CT) == 8 ? 4 : 2);
 }
 
-template <typename R, int N>
-__device__ __forceinline__ void cube_pass(typename C2<R>::T* buf, int nt, int ax,
+// NTC: the transform count when it is known at compile time (0: runtime nt).
+template <typename R, int N, int NTC>
+__device__ __forceinline__ void cube_pass(typename C2<R>::T* buf, int nt_rt, int ax,
                                           const typename C2<R>::T* __restrict__ tw, R sgn) {
   typedef typename C2<R>::T CT;
   constexpr int P3 = N + 1;
   constexpr int SLAB = cube_slab<CT>(N);
+  const int nt = NTC ? NTC : nt_rt;
   const int lines = nt * N * N;
   const int st = (ax == 2) ? 1 : ((ax == 1) ? P3 : N * P3);
   for (int l = threadIdx.x; l < lines; l += blockDim.x) {
@@ -286,19 +288,26 @@ __device__ __forceinline__ void cube_pass(typename C2<R>::T* buf, int nt, int ax
 
 // nt transforms per x-point (alpha, or (vector, alpha) for a block of psi),
 // phi layout [k][x][t].
-template <typename R, int N>
+template <typename R, int N, int NTC>
 __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R* __restrict__ W, int nx,
-                                    int x, int nt, typename C2<R>::T* buf,
+                                    int x, int nt_rt, typename C2<R>::T* buf,
                                     const typename C2<R>::T* __restrict__ tw) {
   typedef typename C2<R>::T CT;
+  const int nt = NTC ? NTC : nt_rt;
   constexpr int NK = N * N * N;
   constexpr int P3 = N + 1;
   constexpr int SLAB = cube_slab<CT>(N);
   // t fastest across threads: a warp reads whole 32-byte sectors of phi, and the
   // padded slab puts neighbouring transforms on different shared-memory banks.
-  // (k, t) advance incrementally to avoid a runtime division per element.
+  // A compile-time count keeps a plain unrollable loop (several loads in
+  // flight); a runtime count advances (k, t) incrementally instead of dividing.
   const int dt = blockDim.x % nt, dk = blockDim.x / nt;
-  {
+  if (NTC) {
+    for (int e = threadIdx.x; e < NTC * NK; e += blockDim.x) {
+      const int k = e / NTC, t = e % NTC;
+      buf[t * SLAB + (k / N) * P3 + k % N] = phi[((size_t)k * nx + x) * NTC + t];
+    }
+  } else {
     int t = threadIdx.x % nt, k = threadIdx.x / nt;
     while (k < NK) {
       buf[t * SLAB + (k / N) * P3 + k % N] = phi[((size_t)k * nx + x) * nt + t];
@@ -313,7 +322,7 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
   __syncthreads();
 #pragma unroll
   for (int ax = 0; ax < 3; ++ax) {
-    cube_pass<R, N>(buf, nt, ax, tw + ax * OCN_MAX_KDIM, (R)1);
+    cube_pass<R, N, NTC>(buf, nt, ax, tw + ax * OCN_MAX_KDIM, (R)1);
     __syncthreads();
   }
   for (int e = threadIdx.x; e < nt * NK; e += blockDim.x) {
@@ -326,11 +335,20 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
   __syncthreads();
 #pragma unroll
   for (int ax = 0; ax < 3; ++ax) {
-    cube_pass<R, N>(buf, nt, ax, tw + ax * OCN_MAX_KDIM, (R)-1);
+    cube_pass<R, N, NTC>(buf, nt, ax, tw + ax * OCN_MAX_KDIM, (R)-1);
     __syncthreads();
   }
   const R norm = (R)1 / (R)NK;
-  {
+  if (NTC) {
+    for (int e = threadIdx.x; e < NTC * NK; e += blockDim.x) {
+      const int k = e / NTC, t = e % NTC;
+      const CT v = buf[t * SLAB + (k / N) * P3 + k % N];
+      CT o;
+      o.x = v.x * norm;
+      o.y = v.y * norm;
+      phi[((size_t)k * nx + x) * NTC + t] = o;
+    }
+  } else {
     int t = threadIdx.x % nt, k = threadIdx.x / nt;
     while (k < NK) {
       const CT v = buf[t * SLAB + (k / N) * P3 + k % N];
@@ -362,19 +380,23 @@ inline bool kmesh_cube_supported(const int kmesh[3]) {
   return n == 2 || n == 3 || n == 4 || n == 5 || n == 6 || n == 8;
 }
 
-// Selects the instantiation kern<N> of a kernel template for a supported cubic
-// mesh (kmesh_cube_supported); returns nullptr otherwise.
-#define OCN_CUBE_DISPATCH(KERN, n, out) \
-  do {                                  \
-    out = nullptr;                      \
-    switch (n) {                        \
-      case 2: out = KERN<2>; break;     \
-      case 3: out = KERN<3>; break;     \
-      case 4: out = KERN<4>; break;     \
-      case 5: out = KERN<5>; break;     \
-      case 6: out = KERN<6>; break;     \
-      case 8: out = KERN<8>; break;     \
-    }                                   \
+// Selects the instantiation kern<N, NTC> of a kernel template for a supported
+// cubic mesh (kmesh_cube_supported) and nt transforms per x-point: NTC = nt for
+// the common counts 4 (1s edge) and 12 (2p edge, or three 1s vectors), where
+// the index arithmetic folds at compile time, else 0 (runtime nt).  nullptr if
+// the mesh is not supported.
+#define OCN_CUBE_NT(KERN, N, nt) (((nt) == 4) ? KERN<N, 4> : ((nt) == 12) ? KERN<N, 12> : KERN<N, 0>)
+#define OCN_CUBE_DISPATCH(KERN, n, nt, out)          \
+  do {                                               \
+    out = nullptr;                                   \
+    switch (n) {                                     \
+      case 2: out = OCN_CUBE_NT(KERN, 2, nt); break; \
+      case 3: out = OCN_CUBE_NT(KERN, 3, nt); break; \
+      case 4: out = OCN_CUBE_NT(KERN, 4, nt); break; \
+      case 5: out = OCN_CUBE_NT(KERN, 5, nt); break; \
+      case 6: out = OCN_CUBE_NT(KERN, 6, nt); break; \
+      case 8: out = OCN_CUBE_NT(KERN, 8, nt); break; \
+    }                                                \
   } while (0)
 
 // Whole k-mesh step for the x-point of this CTA.  phi layout [k][x][a].

@@ -550,15 +550,15 @@ __global__ void k_lr_fft_w_f32(float2* __restrict__ phi, const float* __restrict
   kmesh_convolve<float>(phi, W, nx, blockIdx.x, g, buf, tw);
 }
 
-// cubic meshes, nt transforms per x-point
-template <int N>
+// cubic meshes, nt transforms per x-point (NTC: nt fixed at compile time, or 0)
+template <int N, int NTC>
 __global__ void k_fft_cube_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx, int nt) {
   extern __shared__ float2 fsm[];
   float2* tw = fsm;
   float2* buf = fsm + 3 * OCN_MAX_KDIM;
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_twf[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
   __syncthreads();
-  kmesh_convolve_cube<float, N>(phi, W, nx, blockIdx.x, nt, buf, tw);
+  kmesh_convolve_cube<float, N, NTC>(phi, W, nx, blockIdx.x, nt, buf, tw);
 }
 typedef void (*CubeFnF)(float2*, const float*, int, int);
 
@@ -585,7 +585,7 @@ struct MixedLR {
   TcParams g1{}, g2{};
   int grid1 = 1, grid2 = 1;
   size_t smem_bytes = 0;
-  void* cube_fn = nullptr;  // specialised k-mesh kernel (CubeFnF), or null
+  bool cube = false;        // cubic k-mesh: k_fft_cube_f32 instantiations apply
   bool ready = false;
 };
 
@@ -697,10 +697,13 @@ int mixed_init(ocn_ctx* c) {
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->smem_bytes));
   OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
   if (cube) {
-    CubeFnF f;
-    OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], f);
-    m->cube_fn = reinterpret_cast<void*>(f);
-    OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+    // the three instantiations a call can select (nt = 4, 12, other)
+    for (int nt : {4, 12, 1}) {
+      CubeFnF f;
+      OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], nt, f);
+      OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+    }
+    m->cube = true;
   }
   // FP32 twiddles, rounded from FP64 roots of unity
   float2 tw[3][OCN_MAX_KDIM];
@@ -796,9 +799,10 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
   }
   {
     TimedScope ts(c, T_LR_FFT);
-    if (m->cube_fn) {
-      reinterpret_cast<CubeFnF>(m->cube_fn)<<<nx, 128, kmesh_cube_smem<float>(c->dims.kmesh[0], na * nv),
-                                               c->stream>>>(m->phi, m->Wf, nx, na * nv);
+    if (m->cube) {
+      CubeFnF f;
+      OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], na * nv, f);
+      f<<<nx, 128, kmesh_cube_smem<float>(c->dims.kmesh[0], na * nv), c->stream>>>(m->phi, m->Wf, nx, na * nv);
     } else {
       const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na * nv);
       k_lr_fft_w_f32<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g);
