@@ -909,38 +909,49 @@ int ocn_redtrid(int n, const double* real_a, const double* real_b, double* w) {
 
 namespace {
 
-// Cholesky factorisation and solve of the Hermitian positive-definite Gram
-// matrix C (upper triangle given, C_ij = <au_i|au_j>), for C c = rhs.
-int herm_solve(int n, const std::vector<std::complex<double>>& up, std::vector<std::complex<double>>& b) {
+// Cholesky factor L (L L^H = C) of the Hermitian positive-definite Gram matrix
+// C_ij = <au_i|au_j>, grown one row at a time: update_gmres appends row cur-1
+// of C on each call (OCEAN_gmres.f90:262-300) and restarts from row 0 whenever
+// the basis changes, so rows 0..cur-2 of L stay valid.  Each entry follows
+// L_ij = (C_ij - sum_{k<j} L_ik conj(L_jk)) / L_jj with k ascending, the same
+// arithmetic as a full factorisation.
+struct GramCholesky {
   typedef std::complex<double> cd;
-  std::vector<cd> L((size_t)n * n, cd(0.0, 0.0));  // lower, L L^H = C
-  auto Cij = [&](int i, int j) -> cd {             // i <= j stored
-    return (i <= j) ? up[(size_t)i + (size_t)j * (j + 1) / 2] : std::conj(up[(size_t)j + (size_t)i * (i + 1) / 2]);
-  };
-  for (int j = 0; j < n; ++j) {
-    double d = Cij(j, j).real();
-    for (int k = 0; k < j; ++k) d -= std::norm(L[(size_t)j * n + k]);
-    if (!(d > 0.0)) return j + 1;
-    const double ljj = std::sqrt(d);
-    L[(size_t)j * n + j] = ljj;
-    for (int i = j + 1; i < n; ++i) {
-      cd s = Cij(i, j);
-      for (int k = 0; k < j; ++k) s -= L[(size_t)i * n + k] * std::conj(L[(size_t)j * n + k]);
-      L[(size_t)i * n + j] = s / ljj;
+  int depth = 0;
+  std::vector<cd> L;  // row-major depth x depth, lower
+  void init(int d) {
+    depth = d;
+    L.assign((size_t)d * d, cd(0.0, 0.0));
+  }
+  // up: packed upper triangle of C (C_ij, i <= j, at i + j(j+1)/2)
+  int add_row(int i, const std::vector<cd>& up) {
+    cd* Li = L.data() + (size_t)i * depth;
+    for (int j = 0; j < i; ++j) {
+      cd v = std::conj(up[(size_t)j + (size_t)i * (i + 1) / 2]);  // C_ij, i > j
+      const cd* Lj = L.data() + (size_t)j * depth;
+      for (int k = 0; k < j; ++k) v -= Li[k] * std::conj(Lj[k]);
+      Li[j] = v / Lj[j].real();
+    }
+    double d = up[(size_t)i + (size_t)i * (i + 1) / 2].real();
+    for (int k = 0; k < i; ++k) d -= std::norm(Li[k]);
+    if (!(d > 0.0)) return i + 1;
+    Li[i] = std::sqrt(d);
+    return 0;
+  }
+  // C x = b with the first n rows of L
+  void solve(int n, std::vector<cd>& b) const {
+    for (int i = 0; i < n; ++i) {  // L y = b
+      cd s = b[i];
+      for (int k = 0; k < i; ++k) s -= L[(size_t)i * depth + k] * b[k];
+      b[i] = s / L[(size_t)i * depth + i].real();
+    }
+    for (int i = n - 1; i >= 0; --i) {  // L^H x = y
+      cd s = b[i];
+      for (int k = i + 1; k < n; ++k) s -= std::conj(L[(size_t)k * depth + i]) * b[k];
+      b[i] = s / L[(size_t)i * depth + i].real();
     }
   }
-  for (int i = 0; i < n; ++i) {  // L y = b
-    cd s = b[i];
-    for (int k = 0; k < i; ++k) s -= L[(size_t)i * n + k] * b[k];
-    b[i] = s / L[(size_t)i * n + i].real();
-  }
-  for (int i = n - 1; i >= 0; --i) {  // L^H x = y
-    cd s = b[i];
-    for (int k = i + 1; k < n; ++k) s -= std::conj(L[(size_t)k * n + i]) * b[k];
-    b[i] = s / L[(size_t)i * n + i].real();
-  }
-  return 0;
-}
+};
 
 struct Gmres {
   ocn_ctx* c;
@@ -953,20 +964,23 @@ struct Gmres {
   double* d_out = nullptr;
   double2* d_coef = nullptr;
   std::vector<std::complex<double>> cmat;
+  GramCholesky chol;
   long long hpsi = 0;
 
   int H(const double* in, double* out) {
     ++hpsi;
     return apply_H_impl(c, in, in + n, out, out + n, nullptr, 0);
   }
-  int dot(const double* p, const double* q, double* r, double* i) {
-    int rc = vec_dot_dev(c, p, q, c->d_scal);
-    if (rc) return rc;
-    double h[2];
-    OCN_CUDA(c, cudaMemcpyAsync(h, c->d_scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  // |g|^2 and <rhs|x> with one read-back (the convergence test of OCEAN_gmres.f90:820-842)
+  int residual(const double* g, const double* rhs, const double* x, double* gval, double* rval, double* ival) {
+    int rc;
+    if ((rc = vec_dot_dev(c, g, g, c->d_scal)) || (rc = vec_dot_dev(c, rhs, x, c->d_scal + 2))) return rc;
+    double h[4];
+    OCN_CUDA(c, cudaMemcpyAsync(h, c->d_scal, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     OCN_CUDA(c, cudaStreamSynchronize(c->stream));
-    *r = h[0];
-    if (i) *i = h[1];
+    *gval = h[0];
+    *rval = h[2];
+    *ival = h[3];
     return OCN_OK;
   }
   // update_gmres (OCEAN_gmres.f90:241-344)
@@ -984,8 +998,8 @@ struct Gmres {
     }
     std::vector<std::complex<double>> coef(cur);
     for (int j = 0; j < cur; ++j) coef[j] = -std::complex<double>(h[4 * j + 2], h[4 * j + 3]);
-    const int info = herm_solve(cur, cmat, coef);
-    if (info) return set_err(c, OCN_ERR_SOLVE, "GMRES Gram matrix not positive definite");
+    if (chol.add_row(cur - 1, cmat)) return set_err(c, OCN_ERR_SOLVE, "GMRES Gram matrix not positive definite");
+    chol.solve(cur, coef);
     std::vector<double2> hc(cur);
     for (int j = 0; j < cur; ++j) hc[j] = make_double2(coef[j].real(), coef[j].imag());
     OCN_CUDA(c, cudaMemcpyAsync(d_coef, hc.data(), cur * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
@@ -1000,6 +1014,7 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
               const double* elist, int nomega, const ocn_gmres_params* p, double* out_re,
               double* out_im, double* rel_err, int* iters) {
   if (!c || !hay_r || !hay_i || !elist || nomega < 1 || !p || p->depth < 1) return OCN_ERR_ARG;
+  if (p->depth > 1024) return set_err(c, OCN_ERR_ARG, "gmres depth must be <= 1024");
   cudaSetDevice(c->device);
   int rc = require(c);
   if (rc) return rc;
@@ -1032,6 +1047,7 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
     return rc;
   }
   G.cmat.assign((size_t)p->depth * (p->depth + 1) / 2, std::complex<double>(0.0, 0.0));
+  G.chol.init(p->depth);
   cudaError_t e = cudaMemcpyAsync(G.d_ul, G.u.data(), p->depth * sizeof(double*), cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(G.d_aul, G.au.data(), p->depth * sizeof(double*), cudaMemcpyHostToDevice, c->stream);
@@ -1072,8 +1088,7 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
       };
       if (prev_iter == 0) {
         if ((r = initial())) return r;
-        if ((r = G.dot(g, g, &gval, nullptr))) return r;
-        if ((r = G.dot(rhs, x, &rval, &ival))) return r;
+        if ((r = G.residual(g, rhs, x, &gval, &rval, &ival))) return r;
       } else {
         const double delta = elist[step] * ev2ha - elist[step - 1] * ev2ha;  // make_recycle
         for (int j = 0; j < prev_iter; ++j)
@@ -1083,8 +1098,7 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
           if ((r = G.update(it, g, x, ax))) return r;
           if ((r = vec_axmz(c, ax, g, rhs))) return r;
         }
-        if ((r = G.dot(g, g, &gval, nullptr))) return r;
-        if ((r = G.dot(rhs, x, &rval, &ival))) return r;
+        if ((r = G.residual(g, rhs, x, &gval, &rval, &ival))) return r;
         if (gval < p->convergence) {
           const double rel = -gval / ival;
           if (rel < 0.001 || gval < p->convergence / 10.0) converged = true;
@@ -1116,8 +1130,7 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
             prev_iter = 0;
           }
           if ((r = vec_axmz(c, ax, g, rhs))) return r;
-          if ((r = G.dot(g, g, &gval, nullptr))) return r;
-          if ((r = G.dot(rhs, x, &rval, &ival))) return r;
+          if ((r = G.residual(g, rhs, x, &gval, &rval, &ival))) return r;
           if (gval < p->convergence) {
             const double rel = -gval / ival;
             if (rel < 0.001 || gval < p->convergence / 10.0) {
