@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--block", type=int, default=3,
                     help="chains of the block-Haydock leg (polarisations sharing H); 0 = off")
+    ap.add_argument("--adjoint-omega", type=int, default=400,
+                    help="energies of the adjoint-gradient leg (GMRES forward + reverse); 0 = off")
     ap.add_argument("--gmres-omega", type=int, default=200,
                     help="energies of the GMRES leg (0 disables it)")
     return ap.parse_args()
@@ -347,6 +349,40 @@ def run_ours(args, ws, rank, local, pg):
               "max_rel_error": float(np.max(np.abs(rel)))}
     ctx.close()
 
+    # ---- adjoint leg: d(spectrum)/d(W scale, W(r) table, Gamma, scissor) through
+    #      GmresSpectrum, 400 energies at Gamma = 0.3 eV on the same sizes
+    adj = None
+    if rank == 0 and args.adjoint_omega > 0:
+        import time
+
+        from ocean_gb300 import adjoint
+
+        gam = 0.3 * WL.EV2HARTREE
+        energies = np.linspace(w.el, w.eh, args.adjoint_omega) * WL.HARTREE2EV
+        prob = adjoint.GmresProblem(w, energies, precision=prec, device=local, depth=80, tol=1e-6,
+                                    max_restarts=100)
+        pt = [torch.tensor(w.interaction_scale, dtype=torch.float64, requires_grad=True),
+              torch.tensor(w.ptab, dtype=torch.float64, requires_grad=True),
+              torch.tensor(gam, dtype=torch.float64, requires_grad=True),
+              torch.tensor(0.0, dtype=torch.float64, requires_grad=True)]
+        l2 = prob.ctx.launches
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ore, oim = adjoint.gmres_spectrum(prob, *pt)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        oim.sum().backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        adj = {"omega_points": int(args.adjoint_omega), "gamma_ev": 0.3, "tolerance_g2": 1e-6, "depth": 80,
+               "forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
+               "backward_over_forward": (t2 - t1) / (t1 - t0),
+               "gpu_launches": prob.ctx.launches - l2,
+               "loss": "sum over energies of out_im (the eps2-like column)",
+               "grad": {"scale": float(pt[0].grad), "ptab_norm": float(pt[1].grad.norm()),
+                        "gamma": float(pt[2].grad), "scissor": float(pt[3].grad)}}
+        prob.close()
+
     # ---- block leg: nb chains (polarisations of one site) in lockstep, psi0 in HBM
     blk = None
     if rank == 0 and args.block > 1 and prec == capi.OCN_PREC_MIXED:
@@ -426,7 +462,7 @@ def run_ours(args, ws, rank, local, pg):
                        "l2": "inputs larger than L2 (u2 %.2f GB per contraction operand)" % (
                            w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
             "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
-            "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "roofline": roof, "cpu_baseline": cpu,
+            "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "adjoint": adj, "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
                     "d2h_bytes_per_step": 3 * (niter + 1) * 8 + (ne + 1) * 9 * 8},
             "gpu_launches": launches, "clocks": clocks, "kernel_ms": kt}

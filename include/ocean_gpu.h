@@ -291,6 +291,38 @@ int ocn_gmres(ocn_ctx* ctx, const double* hay_r, const double* hay_i, double kpr
               const double* energies_ev, int nomega, const ocn_gmres_params* p,
               double* out_re, double* out_im, double* rel_err, int* iters);
 
+/* Same with psi0 in device memory (d_hay: real plane then imaginary plane, npsi
+ * each).  d_x (device, may be NULL) receives the solution x of every energy:
+ * nomega consecutive blocks of 2*npsi doubles (the input of ocn_gmres_vjp). */
+int ocn_gmres_dev(ocn_ctx* ctx, const double* d_hay, double kpref, const double* energies_ev,
+                  int nomega, const ocn_gmres_params* p, double* out_re, double* out_im,
+                  double* rel_err, int* iters, double* d_x);
+
+/* Adjoint (reverse-mode) derivatives of the ocn_gmres spectrum; no counterpart
+ * in the reference.  With F(w) = <b|x(w)>, x = (w + i Gamma - H)^-1 b, and the
+ * adjoint y = (w - i Gamma - H)^-1 b (the same recycled GMRES at -Gamma), a
+ * parameter t of H or of the resolvent gives dF/dt = <y| dH/dt |x>.  For the
+ * loss L = sum_w grad_re[w]*out_re[w] + grad_im[w]*out_im[w] (either grad
+ * array may be NULL = 0) this returns
+ *   *g_gamma   = dL/dGamma            (dF/dGamma = -i <y|x>)
+ *   *g_scissor = dL/ds for E -> E + s (dF/ds = <y|x>)
+ *   d_gW       = dL/dW(R, x) on the device, Nk*Nx doubles at [x*Nk + k]
+ *                (dF/dW = -(1/Nk) sum_alpha conj(A^y) A^x, A^v the band-to-x
+ *                 transform of allow o v taken back over the k-mesh).
+ * d_x: the forward solutions from ocn_gmres_dev.  Needs real energies, no
+ * multiplet or spin-orbit term, and a cubic k-mesh of extent 2,3,4,5,6 or 8
+ * (else OCN_ERR_UNSUPPORTED).  ocn_w2_vjp maps d_gW to the W(r) table. */
+int ocn_gmres_vjp(ocn_ctx* ctx, const double* d_hay, double kpref, const double* energies_ev,
+                  int nomega, const ocn_gmres_params* p, const double* d_x,
+                  const double* grad_re, const double* grad_im, double* g_gamma,
+                  double* g_scissor, double* d_gW);
+
+/* Chain rule through lr_populate_W2 (long_range.f90:1659-1853) on the host:
+ * from G = dL/dW (Nk*Nx, [x*Nk + k]) returns dL/dptab[nptab] (the radial table
+ * samples, linear interpolation of intval) and dL/d(interaction_scale). */
+int ocn_w2_vjp(const ocn_dims* dims, const ocn_lr_params* p, const double* G, double* g_ptab,
+               double* g_scale);
+
 /* --------------------------------------------------------------- counters */
 
 /* Number of kernels this context launched since creation (for accounting). */

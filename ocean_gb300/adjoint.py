@@ -1,0 +1,97 @@
+"""Reverse-mode derivatives of the GMRES core-level spectrum.
+
+The spectrum that OCEAN_gmres_do_recycle writes (OCEAN2/OCEAN_gmres.f90:864-869)
+is, per energy w,
+
+    out_re(w) = 1 - kpref Re F(w),   out_im(w) = -kpref Im F(w),
+    F(w) = <b|x(w)>,  (w + i Gamma - H) x = b,  b = allow o psi0.
+
+GmresSpectrum is a torch.autograd.Function over libocean_gpu.so with four
+parameters:
+
+  scale    interactionScale as it multiplies W(R, x) in lr_populate_W2
+           (OCEAN2/long_range.f90:1840); the multiplet term is off here, so this
+           is the "W scale"
+  ptab     the radial table W(r) that lr_populate_W2 interpolates (64 samples)
+  gamma    the resolution Gamma of the resolvent (Hartree)
+  scissor  a shift s of every energy E -> E + s (the core_offset shift of
+           OCEAN2/OCEAN_energies.f90:859-866; Hartree)
+
+forward runs ocn_gmres_dev and keeps every solution x(w) on the device;
+backward runs ocn_gmres_vjp (one adjoint GMRES at -Gamma plus one dL/dW map)
+and ocn_w2_vjp (the chain rule through the W(r) interpolation).  Nothing here
+computes the spectrum itself: every number comes from the library.
+"""
+import dataclasses
+
+import numpy as np
+import torch
+
+from . import capi
+
+
+class GmresProblem:
+    """One site on one GPU with the settings of a GMRES spectrum run."""
+
+    def __init__(self, w, energies_ev, precision=capi.OCN_PREC_FP64, device: int = 0, depth: int = 80,
+                 tol: float = 1e-6, preconditioner=None, max_restarts: int = 100):
+        self.w = w
+        self.energies = np.ascontiguousarray(energies_ev, dtype=np.float64)
+        self.ctx = capi.Context(w, precision=precision, device=device, set_mult=False)
+        self.dev = torch.device(f"cuda:{device}")
+        n = w.npsi
+        self.d_hay = torch.empty(2 * n, dtype=torch.float64, device=self.dev)
+        self.d_hay[:n].copy_(torch.from_numpy(np.ascontiguousarray(w.psi_r)))
+        self.d_hay[n:].copy_(torch.from_numpy(np.ascontiguousarray(w.psi_i)))
+        self.kw = dict(depth=depth, preconditioner=preconditioner, tol=tol, max_restarts=max_restarts)
+        torch.cuda.synchronize(self.dev)
+
+    def set_parameters(self, scale: float, ptab: np.ndarray, scissor: float):
+        """Installs W(scale, ptab) and the shifted energies; returns the workload
+        view whose ptab / interaction_scale the W table was built from."""
+        wv = dataclasses.replace(self.w, ptab=np.ascontiguousarray(ptab, dtype=np.float64),
+                                 interaction_scale=float(scale))
+        W, _, _ = capi.w2_host(wv)
+        self.ctx.set_W(W)
+        self.ctx.set_energies(self.w.er + float(scissor), self.w.ei)
+        return wv
+
+    def close(self):
+        self.ctx.close()
+
+
+class GmresSpectrum(torch.autograd.Function):
+    """(scale, ptab, gamma, scissor) -> (out_re, out_im) of the GMRES spectrum."""
+
+    @staticmethod
+    def forward(fctx, scale, ptab, gamma, scissor, prob: GmresProblem):
+        n = prob.w.npsi
+        nw = len(prob.energies)
+        wv = prob.set_parameters(float(scale), ptab.detach().cpu().numpy(), float(scissor))
+        d_x = torch.empty(nw * 2 * n, dtype=torch.float64, device=prob.dev)
+        ore, oim, rel, its = prob.ctx.gmres_dev(prob.d_hay.data_ptr(), prob.energies, resolution=float(gamma),
+                                                d_x=d_x.data_ptr(), **prob.kw)
+        fctx.prob, fctx.wv, fctx.gamma, fctx.d_x = prob, wv, float(gamma), d_x
+        fctx.iterations = its
+        return torch.from_numpy(ore), torch.from_numpy(oim)
+
+    @staticmethod
+    def backward(fctx, g_re, g_im):
+        prob, wv = fctx.prob, fctx.wv
+        w = prob.w
+        d_gW = torch.empty(w.nk * w.nx, dtype=torch.float64, device=prob.dev)
+        gr = None if g_re is None else g_re.detach().cpu().numpy().astype(np.float64)
+        gi = None if g_im is None else g_im.detach().cpu().numpy().astype(np.float64)
+        g_gamma, g_scissor = prob.ctx.gmres_vjp(prob.d_hay.data_ptr(), prob.energies, fctx.d_x.data_ptr(),
+                                                d_gW.data_ptr(), grad_re=gr, grad_im=gi,
+                                                resolution=fctx.gamma, **prob.kw)
+        G = d_gW.cpu().numpy()
+        g_ptab, g_scale = capi.w2_vjp(wv, G)
+        dt = torch.float64
+        return (torch.tensor(g_scale, dtype=dt), torch.from_numpy(g_ptab), torch.tensor(g_gamma, dtype=dt),
+                torch.tensor(g_scissor, dtype=dt), None)
+
+
+def gmres_spectrum(prob: GmresProblem, scale, ptab, gamma, scissor):
+    """Differentiable (out_re, out_im) over prob.energies."""
+    return GmresSpectrum.apply(scale, ptab, gamma, scissor, prob)

@@ -72,7 +72,8 @@ EXPORTS = [
     "ocn_apply_H_dev", "ocn_haydock", "ocn_haydock_dev", "ocn_psi_pnorm", "ocn_spectrum_cf",
     "ocn_redtrid", "ocn_gmres", "ocn_kernel_launches", "ocn_w2_host", "ocn_phase_table_host",
     "ocn_timing_enable", "ocn_timing_reset", "ocn_timing_read", "ocn_stream", "ocn_apply_H_block",
-    "ocn_haydock_block", "ocn_haydock_block_dev", "ocn_spectrum_cf_noalloc",
+    "ocn_haydock_block", "ocn_haydock_block_dev", "ocn_spectrum_cf_noalloc", "ocn_gmres_dev",
+    "ocn_gmres_vjp", "ocn_w2_vjp",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -118,6 +119,16 @@ def w2_host(w):
     tau = (C.c_double * 3)()
     check(load().ocn_w2_host(C.byref(d), C.byref(p), _dp(W), xs, tau))
     return W, tuple(xs), tuple(tau)
+
+
+def w2_vjp(w, G):
+    """dL/dptab and dL/d(interaction_scale) from dL/dW (Nk*Nx, [x*Nk + k])."""
+    d = _dims(w)
+    p, keep = _lr_params(w)
+    gp = np.zeros(len(keep[1]))
+    gs = C.c_double(0.0)
+    check(load().ocn_w2_vjp(C.byref(d), C.byref(p), _dp(_f64(G)), _dp(gp), C.byref(gs)))
+    return gp, gs.value
 
 
 def phase_table_host(w, xshift):
@@ -326,6 +337,50 @@ class Context:
         self._chk(self.lib.ocn_haydock_block_dev(self.ptr, nv, C.c_void_p(d_psi0), niter, _dp(ra), _dp(ia),
                                                  _dp(rb), done.ctypes.data_as(IP)))
         return ra, ia, rb, done
+
+    def set_W(self, W):
+        self._chk(self.lib.ocn_set_W(self.ptr, _dp(_f64(W))))
+
+    def set_energies(self, er, ei=None):
+        self._chk(self.lib.ocn_set_energies(self.ptr, _dp(_f64(er)), None if ei is None else _dp(_f64(ei))))
+
+    def _gmres_params(self, depth, resolution, preconditioner, tol, max_restarts):
+        p = OcnGmresParams()
+        p.depth = depth
+        p.resolution = self.w.gam0 if resolution is None else resolution
+        p.preconditioner = self.w.gmres_gprc if preconditioner is None else preconditioner
+        p.convergence = tol
+        p.max_restarts = max_restarts
+        return p
+
+    def gmres_dev(self, d_hay: int, energies_ev, depth=80, resolution=None, preconditioner=None, tol=1e-6,
+                  max_restarts=50, kpref=None, d_x: int = 0):
+        """GMRES with psi0 at device address d_hay (re plane, im plane); the
+        solutions go to device address d_x (nomega blocks of 2*npsi) when given."""
+        e = _f64(energies_ev)
+        n = len(e)
+        p = self._gmres_params(depth, resolution, preconditioner, tol, max_restarts)
+        ore, oim, rel = np.zeros(n), np.zeros(n), np.zeros(n)
+        its = np.zeros(n, dtype=np.int32)
+        kp = self.w.kpref if kpref is None else kpref
+        self._chk(self.lib.ocn_gmres_dev(self.ptr, C.c_void_p(d_hay), C.c_double(kp), _dp(e), n, C.byref(p),
+                                         _dp(ore), _dp(oim), _dp(rel), its.ctypes.data_as(IP),
+                                         C.c_void_p(d_x) if d_x else None))
+        return ore, oim, rel, its
+
+    def gmres_vjp(self, d_hay: int, energies_ev, d_x: int, d_gW: int, grad_re=None, grad_im=None, depth=80,
+                  resolution=None, preconditioner=None, tol=1e-6, max_restarts=50, kpref=None):
+        """Adjoint GMRES: returns (dL/dGamma, dL/dscissor); dL/dW lands at device address d_gW."""
+        e = _f64(energies_ev)
+        n = len(e)
+        p = self._gmres_params(depth, resolution, preconditioner, tol, max_restarts)
+        kp = self.w.kpref if kpref is None else kpref
+        gg, gs = C.c_double(0.0), C.c_double(0.0)
+        gr = None if grad_re is None else _dp(_f64(grad_re))
+        gi = None if grad_im is None else _dp(_f64(grad_im))
+        self._chk(self.lib.ocn_gmres_vjp(self.ptr, C.c_void_p(d_hay), C.c_double(kp), _dp(e), n, C.byref(p),
+                                         C.c_void_p(d_x), gr, gi, C.byref(gg), C.byref(gs), C.c_void_p(d_gW)))
+        return gg.value, gs.value
 
     def gmres(self, energies_ev, depth=80, resolution=None, preconditioner=None, tol=1e-6,
               max_restarts=50, kpref=None):

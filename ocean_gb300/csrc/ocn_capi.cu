@@ -7,6 +7,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <new>
 #include <string>
 #include <vector>
@@ -1008,11 +1009,17 @@ struct Gmres {
   }
 };
 
-}  // namespace
+// Called with each energy's solution x (device, re|im planes) once it has converged.
+typedef std::function<int(int step, const double* x)> GmresHook;
 
-int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref,
-              const double* elist, int nomega, const ocn_gmres_params* p, double* out_re,
-              double* out_im, double* rel_err, int* iters) {
+// OCEAN_gmres_do_recycle over the energy list; hay_r/hay_i are host or device
+// planes as `kind` says.  adjoint: solve (w - i Gamma - H) y = b instead, with
+// the preconditioner's damping and the convergence test's sign flipped to match.
+int gmres_run(ocn_ctx* c, const double* hay_r, const double* hay_i, cudaMemcpyKind kind, double kpref,
+              const double* elist, int nomega, const ocn_gmres_params* p, double* out_re, double* out_im,
+              double* rel_err, int* iters, const GmresHook* on_x, bool adjoint = false) {
+  const double zs = adjoint ? -1.0 : 1.0;
+  const double res = zs * p->resolution, gprc = zs * p->preconditioner;
   if (!c || !hay_r || !hay_i || !elist || nomega < 1 || !p || p->depth < 1) return OCN_ERR_ARG;
   if (p->depth > 1024) return set_err(c, OCN_ERR_ARG, "gmres depth must be <= 1024");
   cudaSetDevice(c->device);
@@ -1052,8 +1059,8 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(G.d_aul, G.au.data(), p->depth * sizeof(double*), cudaMemcpyHostToDevice, c->stream);
   // psi_rhs = sfact(hay_vec): allow o hay (OCEAN_gmres.f90:586)
-  if (e == cudaSuccess) e = cudaMemcpyAsync(g, hay_r, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(g + n, hay_i, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(g, hay_r, n * sizeof(double), kind, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(g + n, hay_i, n * sizeof(double), kind, c->stream);
   if (e != cudaSuccess) {
     cleanup();
     return cuda_fail(c, e, "ocn_gmres upload");
@@ -1072,14 +1079,14 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
       bool converged = false;
       if (prev_iter == 0) {
         prev_energy = ener;
-        if ((r = vec_set_prec(c, ener, p->preconditioner, hpsi1, pcdiv))) return r;
+        if ((r = vec_set_prec(c, ener, gprc, hpsi1, pcdiv))) return r;
       }
       // set_initial_vector: keep x for step > 0 (force_reuse_x, OCEAN_gmres.f90:24-27,1232-1241)
       auto initial = [&]() -> int {
         int q;
         if (step > 0) {
           if ((q = G.H(x, ax))) return q;
-          if ((q = vec_axmy(c, x, ax, ener, p->resolution))) return q;
+          if ((q = vec_axmy(c, x, ax, ener, res))) return q;
         } else {
           if ((q = vec_fill(c, x, 0.0, 0.0))) return q;
           if ((q = vec_fill(c, ax, 0.0, 0.0))) return q;
@@ -1100,13 +1107,13 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
         }
         if ((r = G.residual(g, rhs, x, &gval, &rval, &ival))) return r;
         if (gval < p->convergence) {
-          const double rel = -gval / ival;
+          const double rel = -zs * gval / ival;
           if (rel < 0.001 || gval < p->convergence / 10.0) converged = true;
         }
         if (!converged && std::fabs(prev_energy - ener) > p->preconditioner / 4.0) {
           prev_iter = 0;
           prev_energy = ener;
-          if ((r = vec_set_prec(c, ener, p->preconditioner, hpsi1, pcdiv))) return r;
+          if ((r = vec_set_prec(c, ener, gprc, hpsi1, pcdiv))) return r;
         }
       }
       int restarts = 0;
@@ -1118,13 +1125,13 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
           double* apg = G.au[it - 1];
           if ((r = vec_mul(c, g, pcdiv, pg))) return r;
           if ((r = G.H(pg, apg))) return r;
-          if ((r = vec_axmy(c, pg, apg, ener, p->resolution))) return r;
+          if ((r = vec_axmy(c, pg, apg, ener, res))) return r;
           if ((r = G.update(it, g, x, ax))) return r;
           if (it == p->depth) {
             if ((r = G.H(x, ax))) return r;
-            if ((r = vec_axmy(c, x, ax, ener, p->resolution))) return r;
+            if ((r = vec_axmy(c, x, ax, ener, res))) return r;
             if (ener != prev_energy) {
-              if ((r = vec_set_prec(c, ener, p->preconditioner, hpsi1, pcdiv))) return r;
+              if ((r = vec_set_prec(c, ener, gprc, hpsi1, pcdiv))) return r;
               prev_energy = ener;
             }
             prev_iter = 0;
@@ -1132,7 +1139,7 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
           if ((r = vec_axmz(c, ax, g, rhs))) return r;
           if ((r = G.residual(g, rhs, x, &gval, &rval, &ival))) return r;
           if (gval < p->convergence) {
-            const double rel = -gval / ival;
+            const double rel = -zs * gval / ival;
             if (rel < 0.001 || gval < p->convergence / 10.0) {
               prev_iter = (it == p->depth) ? 0 : it;
               converged = true;
@@ -1148,6 +1155,7 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
       if (out_im) out_im[step] = -ival * kpref;
       if (rel_err) rel_err[step] = -gval / ival;
       if (iters) iters[step] = complete_iter;
+      if (on_x && (r = (*on_x)(step, x))) return r;
     }
     return OCN_OK;
   };
@@ -1157,6 +1165,88 @@ int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_gmres");
   if (rc == OCN_OK && c->mixed) rc = mixed_check(c);
   return rc;
+}
+
+}  // namespace
+
+int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref, const double* elist,
+              int nomega, const ocn_gmres_params* p, double* out_re, double* out_im, double* rel_err,
+              int* iters) {
+  return gmres_run(c, hay_r, hay_i, cudaMemcpyHostToDevice, kpref, elist, nomega, p, out_re, out_im, rel_err,
+                   iters, nullptr);
+}
+
+int ocn_gmres_dev(ocn_ctx* c, const double* d_hay, double kpref, const double* elist, int nomega,
+                  const ocn_gmres_params* p, double* out_re, double* out_im, double* rel_err, int* iters,
+                  double* d_x) {
+  if (!c || !d_hay) return OCN_ERR_ARG;
+  const size_t n = c->npsi;
+  GmresHook keep = [&](int step, const double* x) -> int {
+    OCN_CUDA(c, cudaMemcpyAsync(d_x + (size_t)step * 2 * n, x, 2 * n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                c->stream));
+    return OCN_OK;
+  };
+  return gmres_run(c, d_hay, d_hay + n, cudaMemcpyDeviceToDevice, kpref, elist, nomega, p, out_re, out_im,
+                   rel_err, iters, d_x ? &keep : nullptr);
+}
+
+int ocn_gmres_vjp(ocn_ctx* c, const double* d_hay, double kpref, const double* elist, int nomega,
+                  const ocn_gmres_params* p, const double* d_x, const double* grad_re, const double* grad_im,
+                  double* g_gamma, double* g_scissor, double* d_gW) {
+  if (!c || !d_hay || !elist || nomega < 1 || !p || !d_x || !g_gamma || !g_scissor || !d_gW) return OCN_ERR_ARG;
+  if (c->ei_nonzero || c->have_so || c->have_mult)
+    return set_err(c, OCN_ERR_UNSUPPORTED, "ocn_gmres_vjp: needs real energies and no multiplet / spin-orbit term");
+  if (!lr_wgrad_supported(c))
+    return set_err(c, OCN_ERR_UNSUPPORTED, "ocn_gmres_vjp: W gradient needs a cubic k-mesh of 2,3,4,5,6 or 8");
+  cudaSetDevice(c->device);
+  const size_t n = c->npsi;
+  const size_t nkx = (size_t)c->nk * c->nx;
+  double2* phi = nullptr;
+  int rc = dev_alloc(c, &phi, 2 * nkx * c->na);
+  if (rc) return rc;
+  cudaError_t e = cudaMemsetAsync(d_gW, 0, nkx * sizeof(double), c->stream);
+  if (e != cudaSuccess) {
+    cudaFree(phi);
+    return cuda_fail(c, e, "ocn_gmres_vjp");
+  }
+  double gg = 0.0, gs = 0.0;
+  // adjoint solve (conj(z) - H) y = rhs: the same recycled GMRES at -Gamma
+  GmresHook pair = [&](int step, const double* y) -> int {
+    const double* x = d_x + (size_t)step * 2 * n;
+    const double a = -kpref * (grad_re ? grad_re[step] : 0.0);
+    const double b = -kpref * (grad_im ? grad_im[step] : 0.0);
+    int q;
+    if ((q = vec_dot_dev(c, y, x, c->d_scal))) return q;
+    double yx[2];
+    OCN_CUDA(c, cudaMemcpyAsync(yx, c->d_scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+    // dF/dGamma = -i <y|x>, dF/d(scissor) = <y|x>  (F = <rhs|x>)
+    gg += a * yx[1] - b * yx[0];
+    gs += a * yx[0] + b * yx[1];
+    return lr_wgrad_fp64(c, x, y, phi, a, b, d_gW);
+  };
+  rc = gmres_run(c, d_hay, d_hay + n, cudaMemcpyDeviceToDevice, kpref, elist, nomega, p, nullptr, nullptr,
+                 nullptr, nullptr, &pair, true);
+  e = cudaStreamSynchronize(c->stream);
+  cudaFree(phi);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(c, e, "ocn_gmres_vjp");
+  *g_gamma = gg;
+  *g_scissor = gs;
+  return OCN_OK;
+}
+
+int ocn_w2_vjp(const ocn_dims* d, const ocn_lr_params* p, const double* G, double* g_ptab, double* g_scale) {
+  if (!d || !p || !p->rtab || !p->ptab || p->nptab < 2 || p->epsilon0 <= 0.0 || !G || !g_ptab || !g_scale)
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_w2_vjp: bad argument");
+  for (int i = 0; i < 3; ++i)
+    if (d->kmesh[i] < 1 || d->xmesh[i] < 1) return set_err(nullptr, OCN_ERR_ARG, "bad mesh");
+  double tau[3] = {p->tau[0], p->tau[1], p->tau[2]};
+  int xs[3];
+  const int ovr[3] = {p->xshift_override[0], p->xshift_override[1], p->xshift_override[2]};
+  lrload_shift(*d, tau, ovr, xs);
+  w2_vjp(*d, *p, tau, xs, G, g_ptab, g_scale);
+  return OCN_OK;
 }
 
 }  // extern "C"

@@ -179,6 +179,9 @@ void lrload_phase_table(const ocn_dims& d, const int xshift[3], std::vector<doub
                         std::vector<double>& s);  // (Nk, Nx) cos/sin, [x*Nk + k]
 void populate_w2(const ocn_dims& d, const ocn_lr_params& p, const double tau[3], const int xshift[3],
                  std::vector<double>& W);
+// dL/dptab and dL/d(interactionScale) from dL/dW (index x*Nk + k)
+void w2_vjp(const ocn_dims& d, const ocn_lr_params& p, const double tau[3], const int xshift[3],
+            const double* G, double* g_ptab, double* g_scale);
 void soprep(int core_l, double xi, std::vector<double>& r, std::vector<double>& i);
 int redtrid_eigs(int n, const double* ra, const double* rb, double* w);
 double gamfcn(double e, double n, double e0);
@@ -191,6 +194,12 @@ int phase_bloch(ocn_ctx* c, const double* d_ur, const double* d_ui, const double
                 const double* d_sin);
 // out = E o in + A o acc + SO in   (acc already holds H_fg + H_lr of A o in), for nv
 // vectors at stride vstride (vector v: planes at d_pr + v*vstride, d_pi + v*vstride)
+// dL/dW accumulation for one (x, y) pair of GMRES solutions (FP64):
+// gW[x*Nk + R] += a Re(D) + b Im(D), D = -(1/Nk) sum_alpha conj(A^y) A^x with
+// A^v the band-to-x result of allow o v transformed back over the k-mesh.
+// phi: scratch of 2*Nk*Nx*Na complex values.
+int lr_wgrad_fp64(ocn_ctx* c, const double* x, const double* y, double2* phi, double a, double b, double* gW);
+bool lr_wgrad_supported(const ocn_ctx* c);
 int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* d_or, double* d_oi,
             size_t vstride, const int* hflag, int backwards);
 int zero_acc(ocn_ctx* c, int nv);

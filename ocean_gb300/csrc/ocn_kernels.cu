@@ -134,6 +134,30 @@ __global__ void k_fft_cube_fp64(double2* __restrict__ phi, const double* __restr
 }
 typedef void (*CubeFnD)(double2*, const double*, int, int);
 
+template <int N>
+__global__ void k_wgrad_cube_fp64(const double2* __restrict__ phx, const double2* __restrict__ phy, int nx,
+                                  int nt, double* __restrict__ gW, double ca, double cb) {
+  extern __shared__ double2 smem[];
+  double2* tw = smem;
+  double2* buf = smem + 3 * OCN_MAX_KDIM;
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_tw[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
+  __syncthreads();
+  kmesh_wgrad_cube<double, N>(phx, phy, nx, blockIdx.x, nt, buf, tw, gW, ca, cb);
+}
+typedef void (*WgradFnD)(const double2*, const double2*, int, int, double*, double, double);
+
+WgradFnD wgrad_fn(int n) {
+  switch (n) {
+    case 2: return k_wgrad_cube_fp64<2>;
+    case 3: return k_wgrad_cube_fp64<3>;
+    case 4: return k_wgrad_cube_fp64<4>;
+    case 5: return k_wgrad_cube_fp64<5>;
+    case 6: return k_wgrad_cube_fp64<6>;
+    case 8: return k_wgrad_cube_fp64<8>;
+  }
+  return nullptr;
+}
+
 // ------------------------------------------------------ LR: x-mesh -> band
 
 // part[split][re|im][a][k][n] = - sum_{x in split} conj(u(n,k,x)) phi'(k,x,a)
@@ -837,6 +861,32 @@ int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi) {
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }
+  return OCN_OK;
+}
+
+bool lr_wgrad_supported(const ocn_ctx* c) {
+  return kmesh_cube_supported(c->dims.kmesh) &&
+         kmesh_cube_smem<double>(c->dims.kmesh[0], 2 * c->na) <= (size_t)227 * 1024;
+}
+
+int lr_wgrad_fp64(ocn_ctx* c, const double* x, const double* y, double2* phi, double a, double b, double* gW) {
+  if (!lr_wgrad_supported(c)) return set_err(c, OCN_ERR_UNSUPPORTED, "W gradient needs a supported cubic k-mesh");
+  const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na;
+  const size_t n = c->npsi;
+  double2* phx = phi;
+  double2* phy = phi + (size_t)nk * nx * na;
+  const size_t sm = sizeof(double2) * ((size_t)c->nspn * G1_N * (G1_X + 1) + (size_t)na * G1_N);
+  const dim3 grid((nx + G1_X - 1) / G1_X, nk);
+  k_lr_gemm1_fp64<<<grid, G1_X, sm, c->stream>>>(c->d_u, x, x + n, c->d_allow, phx, nb, nk, nx, na, c->nspn);
+  k_lr_gemm1_fp64<<<grid, G1_X, sm, c->stream>>>(c->d_u, y, y + n, c->d_allow, phy, nb, nk, nx, na, c->nspn);
+  c->launches += 2;
+  OCN_CUDA(c, cudaGetLastError());
+  WgradFnD f = wgrad_fn(c->dims.kmesh[0]);
+  const size_t wsm = kmesh_cube_smem<double>(c->dims.kmesh[0], 2 * na);
+  OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
+  f<<<nx, 128, wsm, c->stream>>>(phx, phy, nx, na, gW, a, b);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;
 }
 

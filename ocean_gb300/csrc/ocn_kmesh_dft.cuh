@@ -302,7 +302,7 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
   // A compile-time count keeps a plain unrollable loop (several loads in
   // flight); a runtime count advances (k, t) incrementally instead of dividing.
   const int dt = blockDim.x % nt, dk = blockDim.x / nt;
-  if (NTC) {
+  if constexpr (NTC > 0) {
     for (int e = threadIdx.x; e < NTC * NK; e += blockDim.x) {
       const int k = e / NTC, t = e % NTC;
       buf[t * SLAB + (k / N) * P3 + k % N] = phi[((size_t)k * nx + x) * NTC + t];
@@ -339,7 +339,7 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
     __syncthreads();
   }
   const R norm = (R)1 / (R)NK;
-  if (NTC) {
+  if constexpr (NTC > 0) {
     for (int e = threadIdx.x; e < NTC * NK; e += blockDim.x) {
       const int k = e / NTC, t = e % NTC;
       const CT v = buf[t * SLAB + (k / N) * P3 + k % N];
@@ -363,6 +363,46 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
         ++k;
       }
     }
+  }
+}
+
+// dL/dW of the long-range term for the x-point of this CTA, from the band-to-x
+// results of a solution pair (phx: x, phy: the adjoint y; layout [k][x][t]):
+// both are transformed back over the k-mesh (the F_b half of the convolution),
+// then gW[x*NK + R] += ca Re(D) + cb Im(D) with D = -(1/NK) sum_t conj(Y_t) X_t.
+template <typename R, int N>
+__device__ void kmesh_wgrad_cube(const typename C2<R>::T* __restrict__ phx, const typename C2<R>::T* __restrict__ phy,
+                                 int nx, int x, int nt, typename C2<R>::T* buf,
+                                 const typename C2<R>::T* __restrict__ tw, double* __restrict__ gW, double ca,
+                                 double cb) {
+  typedef typename C2<R>::T CT;
+  constexpr int NK = N * N * N;
+  constexpr int P3 = N + 1;
+  constexpr int SLAB = cube_slab<CT>(N);
+  for (int e = threadIdx.x; e < 2 * nt * NK; e += blockDim.x) {
+    const int half = e / (nt * NK);
+    const int r = e % (nt * NK);
+    const int k = r / nt, t = r % nt;
+    const CT* src = half ? phy : phx;
+    buf[(half * nt + t) * SLAB + (k / N) * P3 + k % N] = src[((size_t)k * nx + x) * nt + t];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    cube_pass<R, N, 0>(buf, 2 * nt, ax, tw + ax * OCN_MAX_KDIM, (R)1);
+    __syncthreads();
+  }
+  for (int k = threadIdx.x; k < NK; k += blockDim.x) {
+    double sr = 0.0, si = 0.0;
+    const int o = (k / N) * P3 + k % N;
+    for (int t = 0; t < nt; ++t) {
+      const CT X = buf[t * SLAB + o];
+      const CT Y = buf[(nt + t) * SLAB + o];
+      sr += (double)Y.x * (double)X.x + (double)Y.y * (double)X.y;
+      si += (double)Y.x * (double)X.y - (double)Y.y * (double)X.x;
+    }
+    const double inv = -1.0 / (double)NK;
+    gW[(size_t)x * NK + k] += ca * (sr * inv) + cb * (si * inv);
   }
 }
 

@@ -78,14 +78,15 @@ void lrload_phase_table(const ocn_dims& d, const int xshift[3], std::vector<doub
   }
 }
 
-// W(R, x) of lr_populate_W2 (long_range.f90:1659-1853): the screened core-hole
-// potential between supercell vector R (k-mesh index, k3 fastest) and x-mesh
-// point x (x fastest, z slowest) relative to the shifted core site, times
-// interactionScale.  Stored at [x*Nk + k] (the Fortran W(k, x)).
-void populate_w2(const ocn_dims& d, const ocn_lr_params& p, const double tau[3], const int xshift[3],
-                 std::vector<double>& W) {
+namespace {
+
+// Geometry of lr_populate_W2 (long_range.f90:1659-1853): for every supercell
+// vector R (k-mesh index, k3 fastest) and x-mesh point x (x fastest, z slowest)
+// calls f(index x*Nk + k, r, pbc prefactor, alf) with r = |R + x_frac - tau| in
+// the metric of avec and alf the lattice coordinates of that separation.
+template <class F>
+void w2_visit(const ocn_dims& d, const ocn_lr_params& p, const double tau[3], const int xshift[3], F f) {
   const int nk = prod3(d.kmesh), nx = prod3(d.xmesh);
-  W.assign((size_t)nk * nx, 0.0);
   double metric[3][3];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
@@ -96,9 +97,6 @@ void populate_w2(const ocn_dims& d, const ocn_lr_params& p, const double tau[3],
   const bool any_pbc = (p.pbc[0] | p.pbc[1] | p.pbc[2]) != 0;
   int pbc[3];
   for (int i = 0; i < 3; ++i) pbc[i] = any_pbc ? (p.pbc[i] != 0 ? d.kmesh[i] : 0) : d.kmesh[i];
-  const double epsi = 1.0 / p.epsilon0;
-  const double rlast = p.rtab[p.nptab - 1];
-
   for (int xi = 0; xi < nx; ++xi) {
     const int pos[3] = {xi % d.xmesh[0] + 1, (xi / d.xmesh[0]) % d.xmesh[1] + 1,
                         xi / (d.xmesh[0] * d.xmesh[1]) + 1};
@@ -122,38 +120,92 @@ void populate_w2(const ocn_dims& d, const ocn_lr_params& p, const double tau[3],
         for (int j = 0; j < 3; ++j) m += metric[i][j] * alf[j];
         r2 += alf[i] * m;
       }
-      const double r = std::sqrt(r2);
-      double v;
-      if (p.isolated && r > p.iso_cut) {
-        v = 0.0;
-      } else if (r > rlast) {
-        if (p.have_eps3d) {
-          double dir[3];
-          for (int c = 0; c < 3; ++c) {
-            double acc = 0.0;
-            for (int j = 0; j < 3; ++j) acc += p.avec[c + 3 * j] * alf[j];
-            dir[c] = acc / r;
-          }
-          v = (dir[0] * dir[0] / p.epsilon3d[0] + dir[1] * dir[1] / p.epsilon3d[1] +
-               dir[2] * dir[2] / p.epsilon3d[2]) / r;
-          if (r < rlast + 5.0) v = v * (r - rlast) / 5.0 + (rlast + 5.0 - r) * epsi / (5.0 * r);
-        } else {
-          v = epsi / r;
-        }
-      } else {
-        // linear interpolation, capped below the first radius (intval 'cap','cap')
-        if (r < p.rtab[0]) {
-          v = p.ptab[0];
-        } else {
-          int i = 0;
-          while (p.rtab[i + 1] < r) ++i;
-          const double t = (r - p.rtab[i]) / (p.rtab[i + 1] - p.rtab[i]);
-          v = p.ptab[i] + t * (p.ptab[i + 1] - p.ptab[i]);
-        }
-      }
-      W[(size_t)xi * nk + k] = v * pref * p.interaction_scale;
+      f((size_t)xi * nk + k, std::sqrt(r2), pref, alf);
     }
   }
+}
+
+// Table interval of r for the linear interpolation of intval ('cap', 'cap'):
+// W = (1 - t) ptab[i] + t ptab[i+1]; below the first radius t = 0, i = 0.
+inline void w2_interval(const ocn_lr_params& p, double r, int* i_out, double* t_out) {
+  if (r < p.rtab[0]) {
+    *i_out = 0;
+    *t_out = 0.0;
+    return;
+  }
+  int i = 0;
+  while (p.rtab[i + 1] < r) ++i;
+  *i_out = i;
+  *t_out = (r - p.rtab[i]) / (p.rtab[i + 1] - p.rtab[i]);
+}
+
+}  // namespace
+
+// W(R, x) of lr_populate_W2 (long_range.f90:1659-1853): the screened core-hole
+// potential between supercell vector R and x-mesh point x relative to the
+// shifted core site, times interactionScale.  Stored at [x*Nk + k] (the Fortran
+// W(k, x)).
+void populate_w2(const ocn_dims& d, const ocn_lr_params& p, const double tau[3], const int xshift[3],
+                 std::vector<double>& W) {
+  W.assign((size_t)prod3(d.kmesh) * prod3(d.xmesh), 0.0);
+  const double epsi = 1.0 / p.epsilon0;
+  const double rlast = p.rtab[p.nptab - 1];
+  w2_visit(d, p, tau, xshift, [&](size_t idx, double r, double pref, const double alf[3]) {
+    double v;
+    if (p.isolated && r > p.iso_cut) {
+      v = 0.0;
+    } else if (r > rlast) {
+      if (p.have_eps3d) {
+        double dir[3];
+        for (int c = 0; c < 3; ++c) {
+          double acc = 0.0;
+          for (int j = 0; j < 3; ++j) acc += p.avec[c + 3 * j] * alf[j];
+          dir[c] = acc / r;
+        }
+        v = (dir[0] * dir[0] / p.epsilon3d[0] + dir[1] * dir[1] / p.epsilon3d[1] +
+             dir[2] * dir[2] / p.epsilon3d[2]) / r;
+        if (r < rlast + 5.0) v = v * (r - rlast) / 5.0 + (rlast + 5.0 - r) * epsi / (5.0 * r);
+      } else {
+        v = epsi / r;
+      }
+    } else if (r < p.rtab[0]) {
+      v = p.ptab[0];
+    } else {
+      int i;
+      double t;
+      w2_interval(p, r, &i, &t);
+      v = p.ptab[i] + t * (p.ptab[i + 1] - p.ptab[i]);
+    }
+    W[idx] = v * pref * p.interaction_scale;
+  });
+}
+
+// Vector-Jacobian product of populate_w2: given G = dL/dW (at [x*Nk + k]),
+// g_ptab[m] = sum G dW/dptab_m (only entries with r inside the table depend on
+// it) and g_scale = sum G dW/d(interactionScale) = sum G W / interactionScale.
+void w2_vjp(const ocn_dims& d, const ocn_lr_params& p, const double tau[3], const int xshift[3],
+            const double* G, double* g_ptab, double* g_scale) {
+  std::vector<double> W;
+  populate_w2(d, p, tau, xshift, W);
+  const double rlast = p.rtab[p.nptab - 1];
+  for (int m = 0; m < p.nptab; ++m) g_ptab[m] = 0.0;
+  double gs = 0.0;
+  w2_visit(d, p, tau, xshift, [&](size_t idx, double r, double pref, const double*) {
+    const double gw = G[idx];
+    gs += gw * W[idx];
+    if ((p.isolated && r > p.iso_cut) || r > rlast) return;
+    const double f = gw * pref * p.interaction_scale;
+    if (r < p.rtab[0]) {
+      g_ptab[0] += f;
+      return;
+    }
+    int i;
+    double t;
+    w2_interval(p, r, &i, &t);
+    g_ptab[i] += f * (1.0 - t);
+    g_ptab[i + 1] += f * t;
+  });
+  *g_scale = (p.interaction_scale != 0.0) ? gs / p.interaction_scale : 0.0;
 }
 
 // Spin-orbit matrix of OCEAN_soprep (OCEAN_multiplet.f90:572-690) without the

@@ -141,3 +141,34 @@ def test_pnorm_matches_reference_formula(lib_built):
     r, i, kp = capi.pnorm(a, b, 64, 432.0)
     r2, i2, kp2 = WL.pnorm(a, b, 64, 432.0)
     assert np.allclose(r, r2, rtol=1e-15) and abs(kp - kp2) < 1e-15 * kp
+
+
+def test_w2_vjp_is_the_exact_chain_rule_of_w2(lib_built):
+    """ocn_w2_vjp against finite differences of ocn_w2_host: W is linear in the
+    W(r) table and in interactionScale, so central differences are exact up to
+    rounding."""
+    import dataclasses
+
+    from ocean_gb300 import capi
+    from ocean_gb300 import workloads as WL
+
+    capi.load(lib_built)
+    w = WL.make("c1", seed=2)
+    rng = np.random.default_rng(7)
+    G = rng.standard_normal(w.nk * w.nx)
+    gp, gs = capi.w2_vjp(w, G)
+
+    def L(ptab, scale):
+        W, _, _ = capi.w2_host(dataclasses.replace(w, ptab=np.ascontiguousarray(ptab), interaction_scale=scale))
+        return float(np.dot(G, W))
+
+    p0 = np.asarray(w.ptab, dtype=np.float64)
+    for m in (0, 1, 17, len(p0) - 1):
+        e = np.zeros_like(p0)
+        e[m] = 1e-3
+        fd = (L(p0 + e, 1.0) - L(p0 - e, 1.0)) / 2e-3
+        assert abs(gp[m] - fd) <= 1e-9 * max(1.0, abs(fd)), (m, gp[m], fd)
+    fd_s = (L(p0, 1.0 + 1e-3) - L(p0, 1.0 - 1e-3)) / 2e-3
+    assert abs(gs - fd_s) <= 1e-9 * abs(fd_s)
+    # entries beyond the table (the 1/(eps r) tail) do not depend on it
+    assert np.count_nonzero(gp) <= len(p0)
