@@ -228,6 +228,18 @@ int ocn_haydock_block(ocn_ctx* ctx, int nv, const double* psi0_r, const double* 
 int ocn_haydock_block_dev(ocn_ctx* ctx, int nv, const double* d_psi0, int niter, double* real_a,
                           double* imag_a, double* real_b, int* niter_done);
 
+/* Batched Haydock over independent problems: context i runs nv[i] chains
+ * (ocn_haydock_block_dev on d_psi0[i]) for niter iterations.  Three iterations
+ * of every context are captured into one CUDA graph as independent branches and
+ * the graph is replayed niter/3 times, so one launch advances all problems and
+ * small ones share the SMs.  The reference runs such problems one after another
+ * (OCEAN.f90:51-83, one ocean.x run per site and photon).  Contexts must share
+ * one device; outputs per context as for ocn_haydock_block_dev (niter_done may be
+ * NULL).  Returns the first hard error, else OCN_ERR_NAN if a chain hit a NaN. */
+int ocn_haydock_batch(ocn_ctx* const* ctxs, int nctx, const int* nv, const double* const* d_psi0,
+                      int niter, double* const* real_a, double* const* imag_a,
+                      double* const* real_b, int* const* niter_done);
+
 /* core_pnorm (OCEAN_psi.f90:5589-5638): normalises psi in place (host planes of
  * n = Nb*Nk*Na values) and returns kpref = 4 pi |psi|^2 / (Nk celvol^2). */
 int ocn_psi_pnorm(int n, int nkpts, double celvol, double* psi_r, double* psi_i, double* kpref);

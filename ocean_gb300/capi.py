@@ -73,7 +73,7 @@ EXPORTS = [
     "ocn_redtrid", "ocn_gmres", "ocn_kernel_launches", "ocn_w2_host", "ocn_phase_table_host",
     "ocn_timing_enable", "ocn_timing_reset", "ocn_timing_read", "ocn_stream", "ocn_apply_H_block",
     "ocn_haydock_block", "ocn_haydock_block_dev", "ocn_spectrum_cf_noalloc", "ocn_gmres_dev",
-    "ocn_gmres_vjp", "ocn_w2_vjp",
+    "ocn_gmres_vjp", "ocn_w2_vjp", "ocn_haydock_batch",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -119,6 +119,28 @@ def w2_host(w):
     tau = (C.c_double * 3)()
     check(load().ocn_w2_host(C.byref(d), C.byref(p), _dp(W), xs, tau))
     return W, tuple(xs), tuple(tau)
+
+
+def haydock_batch(contexts, d_psi0, nvs, niter: int):
+    """ocn_haydock_batch: context i runs nvs[i] chains from device address
+    d_psi0[i] (vector v at + 2*v*npsi doubles).  Returns per context arrays
+    (ra, ia, rb) of shape (nv, niter+1) and the iteration counts."""
+    lib = load()
+    k = len(contexts)
+    outs = [tuple(np.zeros((nv, niter + 1)) for _ in range(3)) for nv in nvs]
+    dones = [np.zeros(nv, dtype=np.int32) for nv in nvs]
+    ctxs = (C.c_void_p * k)(*[c.ptr.value for c in contexts])
+    nvarr = (C.c_int * k)(*nvs)
+    psi = (C.c_void_p * k)(*d_psi0)
+    ra = (DP * k)(*[_dp(o[0]) for o in outs])
+    ia = (DP * k)(*[_dp(o[1]) for o in outs])
+    rb = (DP * k)(*[_dp(o[2]) for o in outs])
+    nd = (IP * k)(*[d.ctypes.data_as(IP) for d in dones])
+    rc = lib.ocn_haydock_batch(ctxs, k, nvarr, psi, niter, ra, ia, rb, nd)
+    if rc:
+        bad = next((c for c in contexts if last_error(c.ptr)), None)
+        raise OcnError(rc, last_error(bad.ptr) if bad else "")
+    return [(o[0], o[1], o[2], d) for o, d in zip(outs, dones)]
 
 
 def w2_vjp(w, G):

@@ -249,7 +249,7 @@ int ocn_ctx_destroy(ocn_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->mixed) mixed_free(c);
-  void* bufs[] = {c->d_er, c->d_ei, c->d_allow, c->d_u, c->d_W, c->d_so, c->d_phi, c->d_acc,
+  void* bufs[] = {c->d_er, c->d_ei, c->d_allow, c->d_u, c->d_W, c->d_tw, c->d_so, c->d_phi, c->d_acc,
                   c->d_accpart, c->d_vec, c->d_red, c->d_scal, c->mult.mpc, c->mult.mpm, c->mult.mh,
                   c->mult.p_l, c->mult.p_m, c->mult.p_nu, c->mult.d_pfirst, c->mult.d_nproj,
                   c->mult.d_jbeg, c->mult.amp, c->mult.amp_part, c->mult.hamp};
@@ -631,10 +631,18 @@ unsigned long long haydock_key(const ocn_ctx* c, int nv) {
 // chain in FP64 (the FP64 block driver runs its chains one after another).
 int haydock_chains(const ocn_ctx* c) { return c->dims.precision == OCN_PREC_MIXED ? c->nvec : 1; }
 
-// nv Lanczos chains from device psi0 planes (chain v: p0r + v*vstride, p0i + v*vstride).
-// Coefficients land in host arrays real_a/imag_a/real_b + v*(niter+1).
-int haydock_run(ocn_ctx* c, int nv, const double* p0r, const double* p0i, size_t vstride, int niter,
-                double* real_a, double* imag_a, double* real_b, int* niter_done) {
+// Buffers of one Haydock run of nv chains on a context (see haydock_prepare).
+struct HayRun {
+  int nv = 0, niter = 0, hv = 0;
+  size_t cap1 = 0;
+  double *ra = nullptr, *ia = nullptr, *rb = nullptr;
+  double* buf[3] = {nullptr, nullptr, nullptr};  // old, psi, h
+};
+
+// Allocates (once) and initialises the Haydock buffers of nv chains from device
+// psi0 planes (chain v: p0r + v*vstride, p0i + v*vstride), on the context stream.
+int haydock_prepare(ocn_ctx* c, int nv, const double* p0r, const double* p0i, size_t vstride, int niter,
+                    HayRun* R) {
   int rc = require(c);
   if (rc) return rc;
   const size_t n = c->npsi;
@@ -651,82 +659,89 @@ int haydock_run(ocn_ctx* c, int nv, const double* p0r, const double* p0i, size_t
     c->hay_cap = niter;
   }
   // coefficients: [real_a of each chain | imag_a of each chain | real_b of each chain]
-  const size_t cap1 = (size_t)c->hay_cap + 1;
-  double* ra = c->hay_coef;
-  double* ia = c->hay_coef + hv * cap1;
-  double* rb = c->hay_coef + 2 * hv * cap1;
-  double* buf[3] = {c->hay_vec, c->hay_vec + 2 * n * hv, c->hay_vec + 4 * n * hv};  // old, psi, h
-  cudaError_t e = cudaMemsetAsync(c->hay_coef, 0, 3 * hv * cap1 * sizeof(double), c->stream);
+  R->nv = nv;
+  R->niter = niter;
+  R->hv = hv;
+  R->cap1 = (size_t)c->hay_cap + 1;
+  R->ra = c->hay_coef;
+  R->ia = c->hay_coef + hv * R->cap1;
+  R->rb = c->hay_coef + 2 * hv * R->cap1;
+  R->buf[0] = c->hay_vec;
+  R->buf[1] = c->hay_vec + 2 * n * hv;
+  R->buf[2] = c->hay_vec + 4 * n * hv;
+  cudaError_t e = cudaMemsetAsync(c->hay_coef, 0, 3 * hv * R->cap1 * sizeof(double), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(c->d_iter, 0, sizeof(int), c->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(buf[0], 0, 2 * n * nv * sizeof(double), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(R->buf[0], 0, 2 * n * nv * sizeof(double), c->stream);
   for (int v = 0; v < nv && e == cudaSuccess; ++v) {
-    e = cudaMemcpyAsync(buf[1] + 2 * v * n, p0r + v * vstride, n * sizeof(double), cudaMemcpyDeviceToDevice,
+    e = cudaMemcpyAsync(R->buf[1] + 2 * v * n, p0r + v * vstride, n * sizeof(double), cudaMemcpyDeviceToDevice,
                         c->stream);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(buf[1] + 2 * v * n + n, p0i + v * vstride, n * sizeof(double),
+      e = cudaMemcpyAsync(R->buf[1] + 2 * v * n + n, p0i + v * vstride, n * sizeof(double),
                           cudaMemcpyDeviceToDevice, c->stream);
   }
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock setup");
-  if (c->dims.precision == OCN_PREC_MIXED && (rc = mixed_prep_b1(c, buf[1], buf[1] + n, 2 * n, nv))) return rc;
+  if (c->dims.precision == OCN_PREC_MIXED && (rc = mixed_prep_b1(c, R->buf[1], R->buf[1] + n, 2 * n, nv)))
+    return rc;
+  return OCN_OK;
+}
 
-  // Three iterations rotate (old, psi, h) back to their starting roles, so one
-  // captured 3-iteration graph serves every launch.
-  const int ngraph = c->use_graphs ? niter / 3 : 0;
-  if (ngraph > 0) {
-    const unsigned long long key = haydock_key(c, nv);
-    if (!c->hay_exec || key != c->hay_key) {
-      drop_haydock_graph(c);
-      OCN_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      c->capturing = true;
-      const long long l0 = c->launches;
-      double* b[3] = {buf[0], buf[1], buf[2]};
-      for (int r = 0; r < 3 && rc == OCN_OK; ++r) {
-        rc = haydock_iteration(c, nv, b[0], b[1], b[2], ra, ia, rb, cap1);
-        double* t = b[0];
-        b[0] = b[1];
-        b[1] = b[2];
-        b[2] = t;
-      }
-      c->capturing = false;
-      cudaGraph_t graph = nullptr;
-      cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
-      if (rc) {
-        if (graph) cudaGraphDestroy(graph);
-        return rc;
-      }
-      if (ce != cudaSuccess) return cuda_fail(c, ce, "cudaStreamEndCapture");
-      ce = cudaGraphInstantiate(&c->hay_exec, graph, 0);
-      cudaGraphDestroy(graph);
-      if (ce != cudaSuccess) {
-        c->hay_exec = nullptr;
-        return cuda_fail(c, ce, "cudaGraphInstantiate");
-      }
-      c->hay_key = key;
-      c->hay_graph_kernels = c->launches - l0;
-      c->launches = l0;
-    }
-    for (int g = 0; g < ngraph; ++g) {
-      OCN_CUDA(c, cudaGraphLaunch(c->hay_exec, c->stream));
-      c->launches += c->hay_graph_kernels;
-    }
+// Captures three iterations, which rotate (old, psi, h) back to their starting
+// roles, into a graph: one graph serves every launch.
+int haydock_capture(ocn_ctx* c, const HayRun& R, cudaGraph_t* out) {
+  *out = nullptr;
+  OCN_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  c->capturing = true;
+  const long long l0 = c->launches;
+  double* b[3] = {R.buf[0], R.buf[1], R.buf[2]};
+  int rc = OCN_OK;
+  for (int r = 0; r < 3 && rc == OCN_OK; ++r) {
+    rc = haydock_iteration(c, R.nv, b[0], b[1], b[2], R.ra, R.ia, R.rb, R.cap1);
+    double* t = b[0];
+    b[0] = b[1];
+    b[1] = b[2];
+    b[2] = t;
   }
-  int done = 3 * ngraph;
-  for (int it = done + 1; it <= niter && rc == OCN_OK; ++it) {
-    rc = haydock_iteration(c, nv, buf[0], buf[1], buf[2], ra, ia, rb, cap1);
-    if (rc) break;
+  c->capturing = false;
+  cudaGraph_t graph = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+  c->hay_graph_kernels = c->launches - l0;
+  c->launches = l0;
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (ce != cudaSuccess) return cuda_fail(c, ce, "cudaStreamEndCapture");
+  *out = graph;
+  return OCN_OK;
+}
+
+// Iterations first+1 .. niter launched directly (after 3*k graph iterations the
+// buffers are back in their starting roles).
+int haydock_remainder(ocn_ctx* c, const HayRun& R, int first, int* done) {
+  double* buf[3] = {R.buf[0], R.buf[1], R.buf[2]};
+  *done = first;
+  for (int it = first + 1; it <= R.niter; ++it) {
+    int rc = haydock_iteration(c, R.nv, buf[0], buf[1], buf[2], R.ra, R.ia, R.rb, R.cap1);
+    if (rc) return rc;
     double* t = buf[0];
     buf[0] = buf[1];  // old <- psi
     buf[1] = buf[2];  // psi <- h / b
     buf[2] = t;
-    done = it;
+    *done = it;
   }
-  e = cudaStreamSynchronize(c->stream);
-  std::vector<double> host(3 * hv * cap1);
+  return OCN_OK;
+}
+
+// Waits for the run, copies the coefficients of each chain into the host
+// arrays (+ v*(niter+1)) and applies the reference's NaN check per chain.
+int haydock_finish(ocn_ctx* c, const HayRun& R, int done, bool graph_timing, double* real_a, double* imag_a,
+                   double* real_b, int* niter_done) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  std::vector<double> host(3 * R.hv * R.cap1);
   if (e == cudaSuccess)
     e = cudaMemcpy(host.data(), c->hay_coef, host.size() * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock");
-  if (rc) return rc;
-  if (c->timing.on && ngraph > 0) {  // event pairs of the last graph replay
+  if (c->timing.on && graph_timing) {  // event pairs of the last graph replay
     for (auto& ge : c->graph_events) {
       float t = 0.0f;
       if (cudaEventElapsedTime(&t, ge.second.first, ge.second.second) == cudaSuccess) {
@@ -736,18 +751,19 @@ int haydock_run(ocn_ctx* c, int nv, const double* p0r, const double* p0i, size_t
     }
     (void)cudaGetLastError();  // a failed timing query must not poison later calls
   }
+  int rc;
   if (c->mixed && (rc = mixed_check(c))) return rc;
-  const size_t out1 = (size_t)niter + 1;
-  for (int v = 0; v < nv; ++v)
-    for (int i = 0; i <= niter; ++i) {
-      real_a[v * out1 + i] = host[v * cap1 + i];
-      if (imag_a) imag_a[v * out1 + i] = host[(hv + v) * cap1 + i];
-      real_b[v * out1 + i] = host[(2 * hv + v) * cap1 + i];
+  const size_t out1 = (size_t)R.niter + 1;
+  for (int v = 0; v < R.nv; ++v)
+    for (int i = 0; i <= R.niter; ++i) {
+      real_a[v * out1 + i] = host[v * R.cap1 + i];
+      if (imag_a) imag_a[v * out1 + i] = host[(R.hv + v) * R.cap1 + i];
+      real_b[v * out1 + i] = host[(2 * R.hv + v) * R.cap1 + i];
     }
   // NaN check on a (OCEAN_haydock.f90:913-920): the reference stops at the first
   // NaN; report the iteration count up to it.
   rc = OCN_OK;
-  for (int v = 0; v < nv; ++v) {
+  for (int v = 0; v < R.nv; ++v) {
     int dv = done;
     for (int i = 0; i < done; ++i)
       if (std::isnan(real_a[v * out1 + i])) {
@@ -758,6 +774,39 @@ int haydock_run(ocn_ctx* c, int nv, const double* p0r, const double* p0i, size_t
     if (niter_done) niter_done[v] = dv;
   }
   return rc;
+}
+
+// nv Lanczos chains from device psi0 planes (chain v: p0r + v*vstride, p0i + v*vstride).
+// Coefficients land in host arrays real_a/imag_a/real_b + v*(niter+1).
+int haydock_run(ocn_ctx* c, int nv, const double* p0r, const double* p0i, size_t vstride, int niter,
+                double* real_a, double* imag_a, double* real_b, int* niter_done) {
+  HayRun R;
+  int rc = haydock_prepare(c, nv, p0r, p0i, vstride, niter, &R);
+  if (rc) return rc;
+  const int ngraph = c->use_graphs ? niter / 3 : 0;
+  if (ngraph > 0) {
+    const unsigned long long key = haydock_key(c, nv);
+    if (!c->hay_exec || key != c->hay_key) {
+      drop_haydock_graph(c);
+      cudaGraph_t graph = nullptr;
+      if ((rc = haydock_capture(c, R, &graph))) return rc;
+      cudaError_t ce = cudaGraphInstantiate(&c->hay_exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ce != cudaSuccess) {
+        c->hay_exec = nullptr;
+        return cuda_fail(c, ce, "cudaGraphInstantiate");
+      }
+      c->hay_key = key;
+    }
+    for (int g = 0; g < ngraph; ++g) {
+      OCN_CUDA(c, cudaGraphLaunch(c->hay_exec, c->stream));
+      c->launches += c->hay_graph_kernels;
+    }
+  }
+  int done = 3 * ngraph;
+  rc = haydock_remainder(c, R, done, &done);
+  const int rf = haydock_finish(c, R, done, ngraph > 0, real_a, imag_a, real_b, niter_done);
+  return rc ? rc : rf;
 }
 
 // Block Haydock on device psi0 planes; FP64 contexts run the chains one by one.
@@ -836,6 +885,85 @@ int ocn_haydock_block(ocn_ctx* c, int nv, const double* p0r, const double* p0i, 
   rc = haydock_block_impl(c, nv, d, niter, real_a, imag_a, real_b, niter_done);
   cudaFree(d);
   return rc;
+}
+
+int ocn_haydock_batch(ocn_ctx* const* ctxs, int nctx, const int* nv, const double* const* d_psi0, int niter,
+                      double* const* real_a, double* const* imag_a, double* const* real_b,
+                      int* const* niter_done) {
+  if (!ctxs || nctx < 1 || !nv || !d_psi0 || niter < 1 || !real_a || !real_b) return OCN_ERR_ARG;
+  for (int i = 0; i < nctx; ++i) {
+    if (!ctxs[i] || !d_psi0[i] || !real_a[i] || !real_b[i]) return OCN_ERR_ARG;
+    if (ctxs[i]->device != ctxs[0]->device)
+      return set_err(ctxs[i], OCN_ERR_ARG, "ocn_haydock_batch: contexts must share one device");
+    for (int j = 0; j < i; ++j)
+      if (ctxs[j] == ctxs[i]) return set_err(ctxs[i], OCN_ERR_ARG, "ocn_haydock_batch: context listed twice");
+  }
+  cudaSetDevice(ctxs[0]->device);
+  std::vector<HayRun> R(nctx);
+  for (int i = 0; i < nctx; ++i) {
+    ocn_ctx* c = ctxs[i];
+    const int rc = haydock_prepare(c, nv[i], d_psi0[i], d_psi0[i] + c->npsi, 2 * c->npsi, niter, &R[i]);
+    if (rc) return rc;
+  }
+  // One graph holds three iterations of every context as independent branches,
+  // so a single launch advances all of them and the device overlaps their kernels.
+  const int ngraph = niter / 3;
+  ocn_ctx* c0 = ctxs[0];
+  std::vector<cudaEvent_t> ev(nctx, nullptr);
+  cudaGraph_t parent = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<long long> kernels(nctx, 0);
+  auto cleanup = [&]() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (parent) cudaGraphDestroy(parent);
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+  };
+  int rc = OCN_OK;
+  if (ngraph > 0) {
+    cudaError_t e = cudaGraphCreate(&parent, 0);
+    for (int i = 0; i < nctx && e == cudaSuccess && rc == OCN_OK; ++i) {
+      ocn_ctx* c = ctxs[i];
+      const bool timing = c->timing.on;  // event-record nodes stay out of the batch graph
+      const long long saved = c->hay_graph_kernels;
+      c->timing.on = false;
+      cudaGraph_t child = nullptr;
+      rc = haydock_capture(c, R[i], &child);
+      c->timing.on = timing;
+      kernels[i] = c->hay_graph_kernels;
+      c->hay_graph_kernels = saved;
+      if (rc == OCN_OK) {
+        cudaGraphNode_t node;
+        e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, child);
+        cudaGraphDestroy(child);
+      }
+    }
+    if (rc == OCN_OK && e == cudaSuccess) e = cudaGraphInstantiate(&exec, parent, 0);
+    // the launch stream (context 0's) waits for every context's set-up
+    for (int i = 0; i < nctx && rc == OCN_OK && e == cudaSuccess; ++i) {
+      e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[i], ctxs[i]->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(c0->stream, ev[i], 0);
+    }
+    for (int g = 0; g < ngraph && rc == OCN_OK && e == cudaSuccess; ++g) e = cudaGraphLaunch(exec, c0->stream);
+    // and every context continues after the last replay
+    if (rc == OCN_OK && e == cudaSuccess) e = cudaEventRecord(ev[0], c0->stream);
+    for (int i = 1; i < nctx && rc == OCN_OK && e == cudaSuccess; ++i) e = cudaStreamWaitEvent(ctxs[i]->stream, ev[0], 0);
+    if (rc == OCN_OK && e != cudaSuccess) rc = cuda_fail(c0, e, "ocn_haydock_batch graph");
+    if (rc == OCN_OK)
+      for (int i = 0; i < nctx; ++i) ctxs[i]->launches += (long long)ngraph * kernels[i];
+  }
+  // remaining iterations on each context's own stream, then the read-backs
+  std::vector<int> done(nctx, 3 * ngraph);
+  for (int i = 0; i < nctx && rc == OCN_OK; ++i) rc = haydock_remainder(ctxs[i], R[i], 3 * ngraph, &done[i]);
+  int worst = rc;
+  for (int i = 0; i < nctx; ++i) {
+    const int rf = haydock_finish(ctxs[i], R[i], done[i], false, real_a[i], imag_a ? imag_a[i] : nullptr,
+                                  real_b[i], niter_done ? niter_done[i] : nullptr);
+    if (rf && (worst == OCN_OK || worst == OCN_ERR_NAN)) worst = rf;  // a NaN yields to a harder error
+  }
+  cleanup();
+  return worst;
 }
 
 int ocn_apply_H_block(ocn_ctx* c, int nv, const double* ir, const double* ii, double* orr, double* oi,

@@ -80,6 +80,7 @@ struct ocn_ctx {
   double* d_allow = nullptr;
   double2* d_u = nullptr;    // phased Bloch functions, [s][x][k][n] complex (reference order)
   double* d_W = nullptr;     // (Nk, Nx): W[x*Nk + k]
+  double2* d_tw = nullptr;   // k-mesh twiddles exp(+2 pi i t / n_axis), [axis][t] (3 x OCN_MAX_KDIM)
   double2* d_so = nullptr;   // (Na,Na) somelr + i someli, [jc*Na + ic]
   std::vector<double> h_so_r, h_so_i;
 
@@ -130,6 +131,18 @@ int cuda_fail(ocn_ctx* c, cudaError_t e, const char* what);
     cudaError_t _e = (call);                                  \
     if (_e != cudaSuccess) return ocn::cuda_fail(ctx, _e, #call); \
   } while (0)
+
+// Lets kernel f use up to the device's opt-in shared memory per block.  The
+// attribute belongs to the function, process-wide: a context of one size must
+// not lower it under a live context of another, so it is always set to the
+// device maximum (the launch's own request still decides occupancy).
+template <class F>
+int allow_max_smem(ocn_ctx* c, F* f) {
+  int optin = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  return e == cudaSuccess ? 0 : cuda_fail(c, e, "cudaFuncSetAttribute");
+}
 
 // Event bracket around one timed launch (no-op unless timing is on).
 struct TimedScope {

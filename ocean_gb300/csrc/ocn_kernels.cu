@@ -20,8 +20,6 @@ namespace ocn {
 
 namespace {
 
-__constant__ double2 c_tw[3][OCN_MAX_KDIM];  // exp(+2 pi i t / n_axis)
-__constant__ int c_kdim[3];
 
 // ------------------------------------------------------------ phase of u2
 
@@ -114,37 +112,39 @@ __global__ void __launch_bounds__(G1_X) k_lr_gemm1_fp64(
 // FFTW signs +1 backward / -1 forward, Modules/FFT_wrapper.f90:24-25).  One CTA per x,
 // transform in shared memory (ocn_kmesh_dft.cuh).
 __global__ void k_lr_fft_w_fp64(double2* __restrict__ phi, const double* __restrict__ W, int nx,
-                                const KmeshGeom<double> g) {
+                                const KmeshGeom<double> g, const double2* __restrict__ twg) {
   extern __shared__ double2 smem[];
   double2* tw = smem;
   double2* buf = smem + 3 * OCN_MAX_KDIM;
-  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_tw[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
   __syncthreads();
   kmesh_convolve<double>(phi, W, nx, blockIdx.x, g, buf, tw);
 }
 
 template <int N, int NTC>
-__global__ void k_fft_cube_fp64(double2* __restrict__ phi, const double* __restrict__ W, int nx, int nt) {
+__global__ void k_fft_cube_fp64(double2* __restrict__ phi, const double* __restrict__ W, int nx, int nt,
+                                const double2* __restrict__ twg) {
   extern __shared__ double2 smem[];
   double2* tw = smem;
   double2* buf = smem + 3 * OCN_MAX_KDIM;
-  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_tw[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
   __syncthreads();
   kmesh_convolve_cube<double, N, NTC>(phi, W, nx, blockIdx.x, nt, buf, tw);
 }
-typedef void (*CubeFnD)(double2*, const double*, int, int);
+typedef void (*CubeFnD)(double2*, const double*, int, int, const double2*);
 
 template <int N>
 __global__ void k_wgrad_cube_fp64(const double2* __restrict__ phx, const double2* __restrict__ phy, int nx,
-                                  int nt, double* __restrict__ gW, double ca, double cb) {
+                                  int nt, double* __restrict__ gW, double ca, double cb,
+                                  const double2* __restrict__ twg) {
   extern __shared__ double2 smem[];
   double2* tw = smem;
   double2* buf = smem + 3 * OCN_MAX_KDIM;
-  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_tw[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
   __syncthreads();
   kmesh_wgrad_cube<double, N>(phx, phy, nx, blockIdx.x, nt, buf, tw, gW, ca, cb);
 }
-typedef void (*WgradFnD)(const double2*, const double2*, int, int, double*, double, double);
+typedef void (*WgradFnD)(const double2*, const double2*, int, int, double*, double, double, const double2*);
 
 WgradFnD wgrad_fn(int n) {
   switch (n) {
@@ -790,25 +790,31 @@ int upload_twiddles(ocn_ctx* c) {
       }
     }
   }
-  OCN_CUDA(c, cudaMemcpyToSymbolAsync(c_tw, tw, sizeof(tw), 0, cudaMemcpyHostToDevice, c->stream));
-  OCN_CUDA(c, cudaMemcpyToSymbolAsync(c_kdim, c->dims.kmesh, sizeof(int) * 3, 0,
-                                      cudaMemcpyHostToDevice, c->stream));
+  // per context: contexts with different k-meshes coexist in one process
+  if (!c->d_tw) OCN_CUDA(c, cudaMalloc(reinterpret_cast<void**>(&c->d_tw), sizeof(tw)));
+  OCN_CUDA(c, cudaMemcpyAsync(c->d_tw, tw, sizeof(tw), cudaMemcpyHostToDevice, c->stream));
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
   return OCN_OK;
 }
 
 int kernels_init(ocn_ctx* c) {
+  int optin = 0;
+  OCN_CUDA(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
   const size_t g1 = sizeof(double2) * ((size_t)c->nspn * G1_N * (G1_X + 1) + (size_t)c->na * G1_N);
-  OCN_CUDA(c, cudaFuncSetAttribute(k_lr_gemm1_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g1));
-  const size_t ff = kmesh_smem(kmesh_geom<double>(c->dims.kmesh, c->na));
-  OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff));
-  if (kmesh_cube_supported(c->dims.kmesh)) {
+  const size_t ma = sizeof(double2) * (size_t)c->na * 256;
+  const bool cube = kmesh_cube_supported(c->dims.kmesh);
+  const size_t ff = cube ? kmesh_cube_smem<double>(c->dims.kmesh[0], c->na)
+                         : kmesh_smem(kmesh_geom<double>(c->dims.kmesh, c->na));
+  if (g1 > (size_t)optin || ma > (size_t)optin || ff > (size_t)optin)
+    return set_err(c, OCN_ERR_ARG, "k-mesh or nalpha too large for the shared-memory kernels");
+  if (int rc_ = allow_max_smem(c, k_lr_gemm1_fp64)) return rc_;
+  if (int rc_ = allow_max_smem(c, k_lr_fft_w_fp64)) return rc_;
+  if (cube) {
     CubeFnD f;
     OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], c->na, f);
-    OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kmesh_cube_smem<double>(c->dims.kmesh[0], c->na)));
+    if (int rc_ = allow_max_smem(c, f)) return rc_;
   }
-  const size_t ma = sizeof(double2) * (size_t)c->na * 256;
-  OCN_CUDA(c, cudaFuncSetAttribute(k_mult_amp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ma));
+  if (int rc_ = allow_max_smem(c, k_mult_amp)) return rc_;
   return OCN_OK;
 }
 
@@ -844,9 +850,10 @@ int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi) {
     CubeFnD f = nullptr;
     if (kmesh_cube_supported(c->dims.kmesh)) OCN_CUBE_DISPATCH(k_fft_cube_fp64, c->dims.kmesh[0], na, f);
     if (f)
-      f<<<nx, 128, kmesh_cube_smem<double>(c->dims.kmesh[0], na), c->stream>>>(c->d_phi, c->d_W, nx, na);
+      f<<<nx, 128, kmesh_cube_smem<double>(c->dims.kmesh[0], na), c->stream>>>(c->d_phi, c->d_W, nx, na,
+                                                                               c->d_tw);
     else
-      k_lr_fft_w_fp64<<<nx, 256, kmesh_smem(g), c->stream>>>(c->d_phi, c->d_W, nx, g);
+      k_lr_fft_w_fp64<<<nx, 256, kmesh_smem(g), c->stream>>>(c->d_phi, c->d_W, nx, g, c->d_tw);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }
@@ -883,8 +890,8 @@ int lr_wgrad_fp64(ocn_ctx* c, const double* x, const double* y, double2* phi, do
   OCN_CUDA(c, cudaGetLastError());
   WgradFnD f = wgrad_fn(c->dims.kmesh[0]);
   const size_t wsm = kmesh_cube_smem<double>(c->dims.kmesh[0], 2 * na);
-  OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm));
-  f<<<nx, 128, wsm, c->stream>>>(phx, phy, nx, na, gW, a, b);
+  if (int rc_ = allow_max_smem(c, f)) return rc_;
+  f<<<nx, 128, wsm, c->stream>>>(phx, phy, nx, na, gW, a, b, c->d_tw);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;

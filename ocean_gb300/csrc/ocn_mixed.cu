@@ -51,7 +51,6 @@ constexpr int TC_MAX_NCOL = 256;  // MMA N limit for M = 128
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 constexpr size_t TC_SMEM_BUDGET = 220 * 1024;
 
-__constant__ float2 c_twf[3][OCN_MAX_KDIM];
 
 struct TcParams {
   int mode;      // 1: band -> x (GEMM1), 2: x -> band (GEMM2)
@@ -541,26 +540,27 @@ __global__ void k_prep_b2(const float2* __restrict__ phi, __nv_bfloat16* __restr
 
 // FP32 k-mesh transform, one CTA per x-point (ocn_kmesh_dft.cuh): generic meshes
 __global__ void k_lr_fft_w_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx,
-                               const KmeshGeom<float> g) {
+                               const KmeshGeom<float> g, const float2* __restrict__ twg) {
   extern __shared__ float2 fsm[];
   float2* tw = fsm;
   float2* buf = fsm + 3 * OCN_MAX_KDIM;
-  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_twf[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
   __syncthreads();
   kmesh_convolve<float>(phi, W, nx, blockIdx.x, g, buf, tw);
 }
 
 // cubic meshes, nt transforms per x-point (NTC: nt fixed at compile time, or 0)
 template <int N, int NTC>
-__global__ void k_fft_cube_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx, int nt) {
+__global__ void k_fft_cube_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx, int nt,
+                               const float2* __restrict__ twg) {
   extern __shared__ float2 fsm[];
   float2* tw = fsm;
   float2* buf = fsm + 3 * OCN_MAX_KDIM;
-  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = c_twf[i / OCN_MAX_KDIM][i % OCN_MAX_KDIM];
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
   __syncthreads();
   kmesh_convolve_cube<float, N, NTC>(phi, W, nx, blockIdx.x, nt, buf, tw);
 }
-typedef void (*CubeFnF)(float2*, const float*, int, int);
+typedef void (*CubeFnF)(float2*, const float*, int, int, const float2*);
 
 __global__ void k_w_to_f32(const double* __restrict__ W, float* __restrict__ Wf, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -580,6 +580,7 @@ struct MixedLR {
   __nv_bfloat16 *b1 = nullptr, *b2 = nullptr;
   float2* phi = nullptr;
   float* Wf = nullptr;
+  float2* twf = nullptr;  // FP32 twiddles exp(+2 pi i t / n_axis), [axis][t]
   int* d_err = nullptr;
   CUtensorMap tm_ua_hi, tm_ua_lo, tm_b1, tm_ub_hi, tm_ub_lo, tm_b2;
   TcParams g1{}, g2{};
@@ -694,14 +695,14 @@ int mixed_init(ocn_ctx* c) {
   m->smem_bytes = 1024 + stages * stage_bytes + 256;
   m->grid1 = std::min(g1.ntiles, c->sm_count);
   m->grid2 = std::min(g2.ntiles, c->sm_count);
-  OCN_CUDA(c, cudaFuncSetAttribute(k_lr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->smem_bytes));
-  OCN_CUDA(c, cudaFuncSetAttribute(k_lr_fft_w_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+  if (int rc_ = allow_max_smem(c, k_lr_tc)) return rc_;
+  if (int rc_ = allow_max_smem(c, k_lr_fft_w_f32)) return rc_;
   if (cube) {
     // the three instantiations a call can select (nt = 4, 12, other)
     for (int nt : {4, 12, 1}) {
       CubeFnF f;
       OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], nt, f);
-      OCN_CUDA(c, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+      if (int rc_ = allow_max_smem(c, f)) return rc_;
     }
     m->cube = true;
   }
@@ -714,14 +715,15 @@ int mixed_init(ocn_ctx* c) {
       tw[a][t] = t < n ? make_float2((float)cos(2.0 * pi * t / n), (float)sin(2.0 * pi * t / n))
                        : make_float2(0.f, 0.f);
     }
-  OCN_CUDA(c, cudaMemcpyToSymbol(c_twf, tw, sizeof(tw)));
+  if ((rc = alloc(c, &m->twf, (size_t)3 * OCN_MAX_KDIM))) return rc;
+  OCN_CUDA(c, cudaMemcpy(m->twf, tw, sizeof(tw), cudaMemcpyHostToDevice));
   return OCN_OK;
 }
 
 int mixed_free(ocn_ctx* c) {
   MixedLR* m = c->mixed;
   if (!m) return OCN_OK;
-  void* bufs[] = {m->ua_hi, m->ua_lo, m->ub_hi, m->ub_lo, m->b1, m->b2, m->phi, m->Wf, m->d_err};
+  void* bufs[] = {m->ua_hi, m->ua_lo, m->ub_hi, m->ub_lo, m->b1, m->b2, m->phi, m->Wf, m->d_err, m->twf};
   for (void* p : bufs)
     if (p) cudaFree(p);
   delete m;
@@ -802,10 +804,11 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
     if (m->cube) {
       CubeFnF f;
       OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], na * nv, f);
-      f<<<nx, 128, kmesh_cube_smem<float>(c->dims.kmesh[0], na * nv), c->stream>>>(m->phi, m->Wf, nx, na * nv);
+      f<<<nx, 128, kmesh_cube_smem<float>(c->dims.kmesh[0], na * nv), c->stream>>>(m->phi, m->Wf, nx, na * nv,
+                                                                                    m->twf);
     } else {
       const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na * nv);
-      k_lr_fft_w_f32<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g);
+      k_lr_fft_w_f32<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g, m->twf);
     }
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());

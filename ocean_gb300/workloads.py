@@ -129,9 +129,45 @@ def _orthonormal_u2(rng, nk: int, nx: int, nb: int, nspn: int):
     return ur.reshape(-1), ui.reshape(-1)
 
 
+def _orthonormal_u2_torch(seed: int, nk: int, nx: int, nb: int, nspn: int, device: str):
+    """Same distribution as _orthonormal_u2, drawn and factorised on a GPU with
+    torch (the batched-instance sets are too large for host QR in a benchmark)."""
+    import torch
+
+    gen = torch.Generator(device=device)
+    gen.manual_seed(1_000_003 * seed + 17)
+    ur = np.empty((nspn, nx, nk, nb), dtype=np.float64)
+    ui = np.empty_like(ur)
+    chunk = max(1, min(nk, (1 << 27) // max(1, nx * nb)))
+    for s in range(nspn):
+        for k0 in range(0, nk, chunk):
+            k1 = min(nk, k0 + chunk)
+            g = torch.complex(torch.randn((k1 - k0, nx, nb), generator=gen, device=device, dtype=torch.float64),
+                              torch.randn((k1 - k0, nx, nb), generator=gen, device=device, dtype=torch.float64))
+            q, _ = torch.linalg.qr(g)
+            q = q.permute(1, 0, 2).contiguous()
+            ur[s, :, k0:k1, :] = q.real.cpu().numpy()
+            ui[s, :, k0:k1, :] = q.imag.cpu().numpy()
+    return ur.reshape(-1), ui.reshape(-1)
+
+
+def batch_instance(i: int, u2_device: Optional[str] = None) -> "Workload":
+    """Instance i of the batched uneven set: k-mesh n^3 with n in {4,5,6,8},
+    bands U{24..128}, 1s or 2p edge, x-mesh m^3 with m in 8..12, seed i."""
+    rng = np.random.Generator(np.random.PCG64(10_000 + i))
+    n = int(rng.choice([4, 5, 6, 8]))
+    nb = int(rng.integers(24, 129))
+    lc = int(rng.integers(0, 2))
+    m = int(rng.integers(8, 13))
+    return make("batch", seed=i, nb=nb, kmesh=(n, n, n), xmesh=(m, m, m), core_l=lc, with_mult=False,
+                u2_device=u2_device)
+
+
 def make(name: str, seed: int = 0, nb: Optional[int] = None, kmesh=None, xmesh=None,
-         core_l: Optional[int] = None, with_mult: Optional[bool] = None) -> Workload:
-    """Build a named workload: 'c1', 'c2', 'c3', 'c5', or 'tiny' (test sizes)."""
+         core_l: Optional[int] = None, with_mult: Optional[bool] = None,
+         u2_device: Optional[str] = None) -> Workload:
+    """Build a named workload: 'c1', 'c2', 'c3', 'c5', 'batch' (shape given by the
+    caller), or 'tiny' (test sizes).  u2_device: draw u2 on that torch device."""
     presets = {
         "tiny": dict(nb=8, kmesh=(2, 2, 2), xmesh=(3, 3, 3), core_l=0, mult=False, niter=24),
         "small": dict(nb=12, kmesh=(3, 2, 2), xmesh=(4, 3, 2), core_l=0, mult=False, niter=40),
@@ -144,6 +180,7 @@ def make(name: str, seed: int = 0, nb: Optional[int] = None, kmesh=None, xmesh=N
         "c3small": dict(nb=16, kmesh=(2, 2, 3), xmesh=(4, 4, 4), core_l=1, mult=True, niter=40),
         "c5": dict(nb=100, kmesh=(8, 8, 8), xmesh=(12, 12, 12), core_l=0, mult=False, niter=1000,
                    gmres_nomega=400),
+        "batch": dict(nb=32, kmesh=(4, 4, 4), xmesh=(8, 8, 8), core_l=0, mult=False, niter=500),
     }
     if name not in presets:
         raise ValueError(f"unknown workload {name!r}")
@@ -177,7 +214,10 @@ def make(name: str, seed: int = 0, nb: Optional[int] = None, kmesh=None, xmesh=N
     ei = np.zeros_like(er)
     allow = np.ones_like(er)
 
-    ur, ui = _orthonormal_u2(rng, nk, nx, nbv, nspn)
+    if u2_device is None:
+        ur, ui = _orthonormal_u2(rng, nk, nx, nbv, nspn)
+    else:
+        ur, ui = _orthonormal_u2_torch(seed, nk, nx, nbv, nspn, u2_device)
 
     g_r = rng.standard_normal(na * nk * nbv)
     g_i = rng.standard_normal(na * nk * nbv)
