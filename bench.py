@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--block", type=int, default=3,
                     help="chains of the block-Haydock leg (polarisations sharing H); 0 = off")
+    ap.add_argument("--batch", type=int, default=64,
+                    help="instances of the batched uneven-Haydock leg (3 polarisations each); 0 = off")
     ap.add_argument("--adjoint-omega", type=int, default=400,
                     help="energies of the adjoint-gradient leg (GMRES forward + reverse); 0 = off")
     ap.add_argument("--gmres-omega", type=int, default=200,
@@ -252,6 +254,56 @@ def _device_steps(ctx, w, niter, ne, pr_ptr, pi_ptr, steps, stream, torch):
     return ev0.elapsed_time(ev1), last
 
 
+def run_batch(args, torch, capi, WL, local, dev, niter: int = 500, nv: int = 3):
+    """Batched uneven instances: autotuned tiles per instance, one batched run
+    (ocn_haydock_batch) against the same instances run one after another."""
+    import time
+
+    ctxs, bufs, shapes, tuned = [], [], [], []
+    t0 = time.perf_counter()
+    for i in range(args.batch):
+        w = WL.batch_instance(i, u2_device=dev)
+        ctx = capi.Context(w, precision=capi.OCN_PREC_MIXED, device=local, nvec=nv)
+        w.ur = w.ui = None  # the context holds its own copy
+        rng = np.random.default_rng(500 + i)
+        d = torch.empty(2 * w.npsi * nv, dtype=torch.float64, device=dev)
+        for v in range(nv):
+            r = w.psi_r if v == 0 else rng.standard_normal(w.npsi)
+            im = w.psi_i if v == 0 else rng.standard_normal(w.npsi)
+            s = np.sqrt(np.sum(r * r + im * im))
+            d[2 * v * w.npsi:(2 * v + 1) * w.npsi].copy_(torch.from_numpy(r / s))
+            d[(2 * v + 1) * w.npsi:(2 * v + 2) * w.npsi].copy_(torch.from_numpy(im / s))
+        default_tiles = ctx.tiles()
+        ms_best, best = ctx.autotune(nv=nv, reps=3)
+        tuned.append({"tiles": list(best), "default": list(default_tiles), "lr_ms": ms_best,
+                      "default_lr_ms": ctx.last_tune_current_ms})
+        ctxs.append(ctx)
+        bufs.append(d)
+        shapes.append({"nb": w.nb, "kmesh": w.kmesh[0], "xmesh": w.xmesh[0], "na": w.na})
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    ptrs = [d.data_ptr() for d in bufs]
+    nvs = [nv] * len(ctxs)
+    capi.haydock_batch(ctxs, ptrs, nvs, 30)  # warm-up
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    capi.haydock_batch(ctxs, ptrs, nvs, niter)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    for c, p in zip(ctxs, ptrs):
+        c.haydock_block_dev(niter, nv, p)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    total = len(ctxs) * nv * niter
+    for c in ctxs:
+        c.close()
+    torch.cuda.empty_cache()
+    return {"instances": len(ctxs), "chains_each": nv, "lanczos_steps": niter,
+            "value": total / (t2 - t1), "unit": UNIT, "ms": (t2 - t1) * 1e3,
+            "sequential_value": total / (t3 - t2), "sequential_ms": (t3 - t2) * 1e3,
+            "setup_s": setup_s, "shapes": shapes, "tiles": tuned}
+
+
 def run_ours(args, ws, rank, local, pg):
     import torch
 
@@ -383,6 +435,13 @@ def run_ours(args, ws, rank, local, pg):
                         "gamma": float(pt[2].grad), "scissor": float(pt[3].grad)}}
         prob.close()
 
+    # ---- batched leg: independent uneven instances (k-mesh n^3, n in {4,5,6,8};
+    #      bands U{24..128}; 1s or 2p; x-mesh 8^3..12^3), 3 polarisations each,
+    #      500 Lanczos steps, all advanced by one graph launch per 3 steps
+    bat = None
+    if rank == 0 and args.batch > 0 and prec == capi.OCN_PREC_MIXED:
+        bat = run_batch(args, torch, capi, WL, local, dev)
+
     # ---- block leg: nb chains (polarisations of one site) in lockstep, psi0 in HBM
     blk = None
     if rank == 0 and args.block > 1 and prec == capi.OCN_PREC_MIXED:
@@ -462,7 +521,7 @@ def run_ours(args, ws, rank, local, pg):
                        "l2": "inputs larger than L2 (u2 %.2f GB per contraction operand)" % (
                            w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
             "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
-            "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "adjoint": adj, "roofline": roof, "cpu_baseline": cpu,
+            "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "adjoint": adj, "batch": bat, "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
                     "d2h_bytes_per_step": 3 * (niter + 1) * 8 + (ne + 1) * 9 * 8},
             "gpu_launches": launches, "clocks": clocks, "kernel_ms": kt}

@@ -73,7 +73,7 @@ EXPORTS = [
     "ocn_redtrid", "ocn_gmres", "ocn_kernel_launches", "ocn_w2_host", "ocn_phase_table_host",
     "ocn_timing_enable", "ocn_timing_reset", "ocn_timing_read", "ocn_stream", "ocn_apply_H_block",
     "ocn_haydock_block", "ocn_haydock_block_dev", "ocn_spectrum_cf_noalloc", "ocn_gmres_dev",
-    "ocn_gmres_vjp", "ocn_w2_vjp", "ocn_haydock_batch",
+    "ocn_gmres_vjp", "ocn_w2_vjp", "ocn_haydock_batch", "ocn_autotune", "ocn_set_tiles", "ocn_get_tiles",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -359,6 +359,23 @@ class Context:
         self._chk(self.lib.ocn_haydock_block_dev(self.ptr, nv, C.c_void_p(d_psi0), niter, _dp(ra), _dp(ia),
                                                  _dp(rb), done.ctypes.data_as(IP)))
         return ra, ia, rb, done
+
+    def autotune(self, nv: int = 1, reps: int = 3):
+        """Times the candidate tilings of the tensor-core contractions and keeps
+        the fastest; returns (ms per long-range application, tiles)."""
+        ms, cur = C.c_double(0.0), C.c_double(0.0)
+        t = (C.c_int * 5)()
+        self._chk(self.lib.ocn_autotune(self.ptr, nv, reps, C.byref(ms), C.byref(cur), t))
+        self.last_tune_current_ms = cur.value
+        return ms.value, tuple(t)
+
+    def tiles(self):
+        t = (C.c_int * 5)()
+        self._chk(self.lib.ocn_get_tiles(self.ptr, t))
+        return tuple(t)
+
+    def set_tiles(self, tiles):
+        self._chk(self.lib.ocn_set_tiles(self.ptr, (C.c_int * 5)(*tiles)))
 
     def set_W(self, W):
         self._chk(self.lib.ocn_set_W(self.ptr, _dp(_f64(W))))

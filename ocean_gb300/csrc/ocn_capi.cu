@@ -121,6 +121,34 @@ long long ocn_kernel_launches(const ocn_ctx* ctx) { return ctx ? ctx->launches :
 
 void* ocn_stream(ocn_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
 
+namespace {
+void drop_haydock_graph(ocn_ctx* c);
+}
+
+int ocn_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int tiles[5]) {
+  if (!c) return OCN_ERR_ARG;
+  if (c->dims.precision != OCN_PREC_MIXED || !c->mixed)
+    return set_err(c, OCN_ERR_UNSUPPORTED, "ocn_autotune: tiles exist on the mixed-precision path only");
+  cudaSetDevice(c->device);
+  drop_haydock_graph(c);  // a captured graph holds the old tiling
+  return mixed_autotune(c, nv, reps, best_ms, current_ms, tiles);
+}
+
+int ocn_set_tiles(ocn_ctx* c, const int tiles[5]) {
+  if (!c || !tiles) return OCN_ERR_ARG;
+  if (c->dims.precision != OCN_PREC_MIXED || !c->mixed)
+    return set_err(c, OCN_ERR_UNSUPPORTED, "ocn_set_tiles: tiles exist on the mixed-precision path only");
+  cudaSetDevice(c->device);
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+  drop_haydock_graph(c);
+  return mixed_configure(c, tiles);
+}
+
+int ocn_get_tiles(const ocn_ctx* c, int tiles[5]) {
+  if (!c || !tiles) return OCN_ERR_ARG;
+  return c->mixed ? mixed_config(c, tiles) : OCN_ERR_UNSUPPORTED;
+}
+
 int ocn_timing_enable(ocn_ctx* c, int on) {
   if (!c) return OCN_ERR_ARG;
   c->timing.on = on != 0;

@@ -256,5 +256,10 @@ int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vst
 int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rstride, double* h,
                     double* rb, size_t cstride, const int* itp);
 int mixed_check(ocn_ctx* c);       // reads and clears the device timeout flag
+// tile configuration {stages, GEMM2 K splits, GEMM1 grid cap, GEMM2 grid cap,
+// k-mesh transforms per CTA}
+int mixed_configure(ocn_ctx* c, const int cfg[5]);
+int mixed_config(const ocn_ctx* c, int cfg[5]);
+int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int best_cfg[5]);
 
 }  // namespace ocn

@@ -129,7 +129,7 @@ __global__ void k_fft_cube_fp64(double2* __restrict__ phi, const double* __restr
   double2* buf = smem + 3 * OCN_MAX_KDIM;
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
   __syncthreads();
-  kmesh_convolve_cube<double, N, NTC>(phi, W, nx, blockIdx.x, nt, buf, tw);
+  kmesh_convolve_cube<double, N, NTC>(phi, W, nx, blockIdx.x, nt, nt, buf, tw);
 }
 typedef void (*CubeFnD)(double2*, const double*, int, int, const double2*);
 

@@ -286,11 +286,12 @@ __device__ __forceinline__ void cube_pass(typename C2<R>::T* buf, int nt_rt, int
   }
 }
 
-// nt transforms per x-point (alpha, or (vector, alpha) for a block of psi),
-// phi layout [k][x][t].
+// nt transforms of the x-point (alpha, or (vector, alpha) for a block of psi):
+// transform t of k-point k at phi[(k*nx + x)*ld + t], ld >= nt (a CTA may own a
+// slice of the transforms of its x-point).
 template <typename R, int N, int NTC>
 __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R* __restrict__ W, int nx,
-                                    int x, int nt_rt, typename C2<R>::T* buf,
+                                    int x, int nt_rt, int ld, typename C2<R>::T* buf,
                                     const typename C2<R>::T* __restrict__ tw) {
   typedef typename C2<R>::T CT;
   const int nt = NTC ? NTC : nt_rt;
@@ -305,12 +306,12 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
   if constexpr (NTC > 0) {
     for (int e = threadIdx.x; e < NTC * NK; e += blockDim.x) {
       const int k = e / NTC, t = e % NTC;
-      buf[t * SLAB + (k / N) * P3 + k % N] = phi[((size_t)k * nx + x) * NTC + t];
+      buf[t * SLAB + (k / N) * P3 + k % N] = phi[((size_t)k * nx + x) * ld + t];
     }
   } else {
     int t = threadIdx.x % nt, k = threadIdx.x / nt;
     while (k < NK) {
-      buf[t * SLAB + (k / N) * P3 + k % N] = phi[((size_t)k * nx + x) * nt + t];
+      buf[t * SLAB + (k / N) * P3 + k % N] = phi[((size_t)k * nx + x) * ld + t];
       t += dt;
       k += dk;
       if (t >= nt) {
@@ -346,7 +347,7 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
       CT o;
       o.x = v.x * norm;
       o.y = v.y * norm;
-      phi[((size_t)k * nx + x) * NTC + t] = o;
+      phi[((size_t)k * nx + x) * ld + t] = o;
     }
   } else {
     int t = threadIdx.x % nt, k = threadIdx.x / nt;
@@ -355,7 +356,7 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
       CT o;
       o.x = v.x * norm;
       o.y = v.y * norm;
-      phi[((size_t)k * nx + x) * nt + t] = o;
+      phi[((size_t)k * nx + x) * ld + t] = o;
       t += dt;
       k += dk;
       if (t >= nt) {

@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdint>
 #include <cstring>
 #include <new>
@@ -551,16 +552,17 @@ __global__ void k_lr_fft_w_f32(float2* __restrict__ phi, const float* __restrict
 
 // cubic meshes, nt transforms per x-point (NTC: nt fixed at compile time, or 0)
 template <int N, int NTC>
-__global__ void k_fft_cube_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx, int nt,
+__global__ void k_fft_cube_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx, int nt, int ld,
                                const float2* __restrict__ twg) {
   extern __shared__ float2 fsm[];
   float2* tw = fsm;
   float2* buf = fsm + 3 * OCN_MAX_KDIM;
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
   __syncthreads();
-  kmesh_convolve_cube<float, N, NTC>(phi, W, nx, blockIdx.x, nt, buf, tw);
+  // blockIdx.y: which slice of nt transforms (of ld per x-point) this CTA owns
+  kmesh_convolve_cube<float, N, NTC>(phi + (size_t)blockIdx.y * nt, W, nx, blockIdx.x, nt, ld, buf, tw);
 }
-typedef void (*CubeFnF)(float2*, const float*, int, int, const float2*);
+typedef void (*CubeFnF)(float2*, const float*, int, int, int, const float2*);
 
 __global__ void k_w_to_f32(const double* __restrict__ W, float* __restrict__ Wf, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -587,6 +589,11 @@ struct MixedLR {
   int grid1 = 1, grid2 = 1;
   size_t smem_bytes = 0;
   bool cube = false;        // cubic k-mesh: k_fft_cube_f32 instantiations apply
+  size_t stage_bytes = 0;   // shared memory of one pipeline stage
+  int max_stages = 1;       // deepest pipeline that fits the shared-memory budget
+  int cfg[5] = {0, 0, 0, 0, 0};  // stages, GEMM2 K splits (requested), grid caps of GEMM1 / GEMM2,
+                                // k-mesh transforms per CTA (0: all of an x-point)
+  size_t part_cap = 0;      // splits the partial-sum buffer holds
   bool ready = false;
 };
 
@@ -683,18 +690,15 @@ int mixed_init(ocn_ctx* c) {
   g2.mode = 2;
   g2.nch = (2 * nx + TC_BK - 1) / TC_BK;
   g2.mt2 = (nb + TC_BM - 1) / TC_BM;
+  m->stage_bytes = stage_bytes;
+  m->max_stages = stages;
+  c->part_stride = (size_t)nvmax * 2 * c->npsi;
+  // default tiling: K splits of GEMM2 so that about four tiles per SM exist,
+  // full pipeline depth, one persistent CTA per SM at most
   int ks = (4 * c->sm_count + nk * g2.mt2 - 1) / (nk * g2.mt2);
   ks = std::max(1, std::min(ks, std::max(1, g2.nch / 4)));
-  g2.cps2 = (g2.nch + ks - 1) / ks;
-  g2.ks2 = (g2.nch + g2.cps2 - 1) / g2.cps2;  // no empty split
-  g2.ntiles = nk * g2.mt2 * g2.ks2;
-  c->lr_xsplit = g2.ks2;
-  c->part_stride = (size_t)nvmax * 2 * c->npsi;
-  if ((rc = alloc(c, &c->d_accpart, (size_t)g2.ks2 * c->part_stride))) return rc;
-  g2.part = c->d_accpart;
-  m->smem_bytes = 1024 + stages * stage_bytes + 256;
-  m->grid1 = std::min(g1.ntiles, c->sm_count);
-  m->grid2 = std::min(g2.ntiles, c->sm_count);
+  const int cfg[5] = {stages, ks, c->sm_count, c->sm_count, 0};
+  if ((rc = mixed_configure(c, cfg))) return rc;
   if (int rc_ = allow_max_smem(c, k_lr_tc)) return rc_;
   if (int rc_ = allow_max_smem(c, k_lr_fft_w_f32)) return rc_;
   if (cube) {
@@ -717,6 +721,115 @@ int mixed_init(ocn_ctx* c) {
     }
   if ((rc = alloc(c, &m->twf, (size_t)3 * OCN_MAX_KDIM))) return rc;
   OCN_CUDA(c, cudaMemcpy(m->twf, tw, sizeof(tw), cudaMemcpyHostToDevice));
+  return OCN_OK;
+}
+
+// Tile configuration: cfg = {pipeline stages, K splits of GEMM2, persistent
+// grid cap of GEMM1, of GEMM2, k-mesh transforms per CTA (0 = all of an
+// x-point; a value that does not divide a block's count means all)}.  Grows the
+// partial-sum buffer when a configuration needs more splits.
+int mixed_configure(ocn_ctx* c, const int cfg[5]) {
+  MixedLR* m = c->mixed;
+  if (!m) return set_err(c, OCN_ERR_STATE, "mixed-precision state missing");
+  if (cfg[0] < 1 || cfg[0] > m->max_stages || cfg[1] < 1 || cfg[2] < 1 || cfg[3] < 1 || cfg[4] < 0)
+    return set_err(c, OCN_ERR_ARG, "bad tile configuration");
+  TcParams& g1 = m->g1;
+  TcParams& g2 = m->g2;
+  g1.stages = g2.stages = cfg[0];
+  const int ks = std::max(1, std::min(cfg[1], g2.nch));
+  g2.cps2 = (g2.nch + ks - 1) / ks;
+  g2.ks2 = (g2.nch + g2.cps2 - 1) / g2.cps2;  // no empty split
+  g2.ntiles = c->nk * g2.mt2 * g2.ks2;
+  if ((size_t)g2.ks2 > m->part_cap) {
+    double* np = nullptr;
+    int rc = alloc(c, &np, (size_t)g2.ks2 * c->part_stride);
+    if (rc) return rc;
+    if (c->d_accpart) cudaFree(c->d_accpart);
+    c->d_accpart = np;
+    m->part_cap = (size_t)g2.ks2;
+  }
+  g2.part = c->d_accpart;
+  c->lr_xsplit = g2.ks2;
+  m->smem_bytes = 1024 + (size_t)cfg[0] * m->stage_bytes + 256;
+  m->grid1 = std::min(g1.ntiles, std::min(cfg[2], c->sm_count));
+  m->grid2 = std::min(g2.ntiles, std::min(cfg[3], c->sm_count));
+  for (int i = 0; i < 5; ++i) m->cfg[i] = cfg[i];
+  return OCN_OK;
+}
+
+int mixed_config(const ocn_ctx* c, int cfg[5]) {
+  if (!c->mixed) return OCN_ERR_STATE;
+  for (int i = 0; i < 5; ++i) cfg[i] = c->mixed->cfg[i];
+  return OCN_OK;
+}
+
+// Times the long-range term of an nv-vector block under candidate tile
+// configurations (CUDA events on the context stream, reps launches each after
+// one warm-up) and keeps the fastest.  Two rounds: pipeline depth 2..max x
+// GEMM2 K splits {1, 2, 4, 8, current} x persistent grids of all SMs or half,
+// then the k-mesh transforms per CTA {all, 4, 12} under the round-one winner.
+int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int best_cfg[5]) {
+  MixedLR* m = c->mixed;
+  if (!m || !m->ready) return set_err(c, OCN_ERR_STATE, "mixed-precision operands not built");
+  if (nv < 1 || nv > m->nvmax) return set_err(c, OCN_ERR_ARG, "block size exceeds nvec");
+  reps = std::max(1, reps);
+  const size_t n = c->npsi;
+  double* v = nullptr;
+  int rc = alloc(c, &v, 2 * n * nv);
+  if (rc) return rc;
+  for (int j = 0; j < nv && rc == OCN_OK; ++j) rc = vec_fill(c, v + 2 * j * n, 1.0, 0.5);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  typedef std::array<int, 5> Cfg;
+  const Cfg def = {m->cfg[0], m->cfg[1], m->cfg[2], m->cfg[3], m->cfg[4]};
+  double best = 1e300, dms = 0.0;
+  Cfg bc = def;
+  auto time_cfg = [&](const Cfg& a) -> int {
+    int q;
+    if ((q = mixed_configure(c, a.data()))) return q;
+    if ((q = lr_apply_mixed(c, v, v + n, 2 * n, nv))) return q;  // warm-up
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < reps && q == OCN_OK; ++r) q = lr_apply_mixed(c, v, v + n, 2 * n, nv);
+    cudaEventRecord(e1, c->stream);
+    cudaError_t ce = cudaEventSynchronize(e1);
+    if (ce != cudaSuccess) return cuda_fail(c, ce, "autotune");
+    if (q || (q = mixed_check(c))) return q;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (a == def) dms = ms / reps;
+    if (ms / reps < best) {
+      best = ms / reps;
+      bc = a;
+    }
+    return OCN_OK;
+  };
+  std::vector<Cfg> cand{def};  // the configuration in force, timed first
+  for (int st = std::min(2, m->max_stages); st <= m->max_stages; ++st)
+    for (int ks : {1, 2, 4, 8, def[1]})
+      for (int gc : {c->sm_count, std::max(1, c->sm_count / 2)}) {
+        const Cfg a = {st, ks, gc, gc, def[4]};
+        if (std::find(cand.begin(), cand.end(), a) == cand.end()) cand.push_back(a);
+      }
+  for (size_t i = 0; i < cand.size() && rc == OCN_OK; ++i) rc = time_cfg(cand[i]);
+  if (m->cube && rc == OCN_OK) {
+    const Cfg r1 = bc;
+    for (int tc : {0, 4, 12}) {
+      Cfg a = r1;
+      a[4] = tc;
+      if (tc != r1[4] && rc == OCN_OK) rc = time_cfg(a);
+    }
+  }
+  const int rf = mixed_configure(c, rc ? def.data() : bc.data());
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(v);
+  if (rc) return rc;
+  if (rf) return rf;
+  if (best_ms) *best_ms = best;
+  if (current_ms) *current_ms = dms;
+  if (best_cfg)
+    for (int i = 0; i < 5; ++i) best_cfg[i] = bc[i];
   return OCN_OK;
 }
 
@@ -802,10 +915,13 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
   {
     TimedScope ts(c, T_LR_FFT);
     if (m->cube) {
+      // transforms per CTA: all of the x-point, or a slice (tile parameter 5)
+      const int ntot = na * nv;
+      const int tc = (m->cfg[4] > 0 && ntot % m->cfg[4] == 0) ? m->cfg[4] : ntot;
       CubeFnF f;
-      OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], na * nv, f);
-      f<<<nx, 128, kmesh_cube_smem<float>(c->dims.kmesh[0], na * nv), c->stream>>>(m->phi, m->Wf, nx, na * nv,
-                                                                                    m->twf);
+      OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], tc, f);
+      f<<<dim3(nx, ntot / tc), 128, kmesh_cube_smem<float>(c->dims.kmesh[0], tc), c->stream>>>(m->phi, m->Wf, nx,
+                                                                                              tc, ntot, m->twf);
     } else {
       const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na * nv);
       k_lr_fft_w_f32<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g, m->twf);

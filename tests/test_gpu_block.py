@@ -146,3 +146,37 @@ def test_block_size_checked(built):
         assert list(done) == [6, 6]
     finally:
         ctx.close()
+
+
+def test_autotune_and_tilings_keep_the_action(built):
+    """Every tiling of the contractions gives the same H*psi to FP32 round-off,
+    and the autotuner leaves a working, reported configuration."""
+    _, O = built
+    w = WL.make("c1", seed=12)
+    P = O.OracleProblem(w)
+    rng = np.random.default_rng(5)
+    pr, pi = rng.standard_normal((2, w.npsi)), rng.standard_normal((2, w.npsi))
+    ctx = capi.Context(w, precision=capi.OCN_PREC_MIXED, nvec=2)
+    try:
+        default = ctx.tiles()
+        base_r, base_i = ctx.apply_H_block(pr, pi)
+        for tiles in [(2, 1, 152, 152, 0), (3, 4, 76, 76, 4), (default[0], 8, 152, 76, 0)]:
+            ctx.set_tiles(tiles)
+            assert ctx.tiles() == tiles
+            r, i = ctx.apply_H_block(pr, pi)
+            assert _rel(r + 1j * i, base_r + 1j * base_i) < 1e-6
+        ms, best = ctx.autotune(nv=2, reps=2)
+        assert ms > 0 and ctx.tiles() == best
+        r, i = ctx.apply_H_block(pr, pi)
+        for v in range(2):
+            orr, oi = P.xact(pr[v], pi[v])
+            assert _rel(r[v] + 1j * i[v], orr + 1j * oi) < 1e-4
+        with pytest.raises(capi.OcnError) as e:
+            ctx.set_tiles((0, 1, 1, 1, 0))
+        assert e.value.code == capi.OCN_ERR_ARG
+        # the Haydock graph is rebuilt for the new tiling
+        ra, ia, rb, done = ctx.haydock_block(9, pr / np.linalg.norm(pr[0] + 1j * pi[0]),
+                                             pi / np.linalg.norm(pr[0] + 1j * pi[0]))
+        assert list(done) == [9, 9]
+    finally:
+        ctx.close()
