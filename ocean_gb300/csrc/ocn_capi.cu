@@ -59,12 +59,20 @@ int apply_H_impl(ocn_ctx* c, const double* ir, const double* ii, double* orr, do
   int rc = require(c);
   if (rc) return rc;
   c->acc_valid = false;
-  if (c->sys.mult && hflag[4] == 1 && c->have_mult) {
+  const bool mult_on = c->sys.mult && hflag[4] == 1 && c->have_mult;
+  const bool lr_on = c->sys.long_range && hflag[0] == 1;
+  if (c->mult_parts > 0) {  // mixed precision with tensor-core multiplet: one psi operand for both
+    if ((mult_on || lr_on) && (rc = mixed_prep_b1(c, ir, ii, 0, 1))) return rc;
+    if (mult_on && (rc = mult_apply_mixed(c, ir, ii, 0, 1, true))) return rc;
+    if (lr_on && (rc = lr_apply_mixed(c, ir, ii, 0, 1, true))) return rc;
+    return combine(c, 1, ir, ii, orr, oi, 0, hflag, backwards);
+  }
+  if (mult_on) {
     if ((rc = zero_acc(c, 1))) return rc;
     if ((rc = mult_apply(c, ir, ii, c->d_acc))) return rc;
     c->acc_valid = true;
   }
-  if (c->sys.long_range && hflag[0] == 1) {
+  if (lr_on) {
     if (c->dims.precision == OCN_PREC_MIXED) rc = lr_apply_mixed(c, ir, ii, 0, 1);
     else rc = lr_apply_fp64(c, ir, ii);
     if (rc) return rc;
@@ -91,13 +99,20 @@ int apply_H_block_impl(ocn_ctx* c, int nv, const double* in, double* out, const 
   int rc = require(c);
   if (rc) return rc;
   c->acc_valid = false;
-  if (c->sys.mult && hflag[4] == 1 && c->have_mult) {
+  const bool mult_on = c->sys.mult && hflag[4] == 1 && c->have_mult;
+  const bool lr_on = c->sys.long_range && hflag[0] == 1;
+  bool b1_ready = false;
+  if (c->mult_parts > 0 && mult_on) {
+    if ((rc = mixed_prep_b1(c, in, in + n, 2 * n, nv)) || (rc = mult_apply_mixed(c, in, in + n, 2 * n, nv, true)))
+      return rc;
+    b1_ready = true;
+  } else if (mult_on) {
     if ((rc = zero_acc(c, nv))) return rc;
     for (int v = 0; v < nv; ++v)
       if ((rc = mult_apply(c, in + 2 * v * n, in + 2 * v * n + n, c->d_acc + 2 * v * n))) return rc;
     c->acc_valid = true;
   }
-  if (c->sys.long_range && hflag[0] == 1 && (rc = lr_apply_mixed(c, in, in + n, 2 * n, nv))) return rc;
+  if (lr_on && (rc = lr_apply_mixed(c, in, in + n, 2 * n, nv, b1_ready))) return rc;
   return combine(c, nv, in, in + n, out, out + n, 2 * n, hflag, backwards);
 }
 
@@ -570,6 +585,8 @@ int ocn_set_mult(ocn_ctx* c, const ocn_mult_data* m) {
   OCN_CUDA(c, cudaMemcpy(d.d_nproj, nproj.data(), nl * sizeof(int), cudaMemcpyHostToDevice));
   OCN_CUDA(c, cudaMemcpy(d.d_jbeg, jbeg.data(), nl * sizeof(long long), cudaMemcpyHostToDevice));
   c->have_mult = true;
+  // mixed precision: the projector contractions run on the tensor cores
+  if (c->mixed && (rc = mixed_set_mult(c))) return rc;
   return OCN_OK;
 }
 
@@ -616,10 +633,14 @@ int haydock_iteration(ocn_ctx* c, int nv, double* old, double* psi, double* h, d
   if ((rc = advance_iter(c, c->d_iter))) return rc;
   c->acc_valid = false;
   if (c->sys.mult && c->sys.nhflag[4] == 1 && c->have_mult) {
-    if ((rc = zero_acc(c, nv))) return rc;
-    for (int v = 0; v < nv; ++v)
-      if ((rc = mult_apply(c, psi + 2 * v * n, psi + 2 * v * n + n, c->d_acc + 2 * v * n))) return rc;
-    c->acc_valid = true;
+    if (c->mult_parts > 0) {  // tensor cores; the psi operand was built with the last normalisation
+      if ((rc = mult_apply_mixed(c, psi, psi + n, 2 * n, nv, true))) return rc;
+    } else {
+      if ((rc = zero_acc(c, nv))) return rc;
+      for (int v = 0; v < nv; ++v)
+        if ((rc = mult_apply(c, psi + 2 * v * n, psi + 2 * v * n + n, c->d_acc + 2 * v * n))) return rc;
+      c->acc_valid = true;
+    }
   }
   if (c->sys.long_range && c->sys.nhflag[0] == 1) {
     // mixed: the psi operand was built by the previous normalisation (or before the loop)

@@ -95,6 +95,7 @@ struct ocn_ctx {
   double* d_acc = nullptr;         // full-store accumulator: re plane then im plane (npsi each)
   double* d_accpart = nullptr;     // long-range partials [split][vector][re|im][npsi]
   int lr_xsplit = 1;
+  int mult_parts = 0;              // multiplet partial slices after the LR ones (mixed precision)
   size_t part_stride = 0;          // elements between two splits of d_accpart
   int nvec = 1;                    // largest psi block
   double* d_vec = nullptr;         // general vector pool (see ocn_solvers.cu)
@@ -203,6 +204,8 @@ double gamfcn(double e, double n, double e0);
 int upload_twiddles(ocn_ctx* c);
 int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi);  // adds into d_acc
 int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi, double* acc);  // adds into acc
+int mult_hamp(ocn_ctx* c, const double2* amp, double2* hamp);  // one vector, [p][a]
+void active_parts(const ocn_ctx* c, const int* hflag, const double** base, int* count);
 int phase_bloch(ocn_ctx* c, const double* d_ur, const double* d_ui, const double* d_cos,
                 const double* d_sin);
 // out = E o in + A o acc + SO in   (acc already holds H_fg + H_lr of A o in), for nv
@@ -256,6 +259,11 @@ int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vst
 int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rstride, double* h,
                     double* rb, size_t cstride, const int* itp);
 int mixed_check(ocn_ctx* c);       // reads and clears the device timeout flag
+// multiplet on the tensor cores: operands from c->mult (after ocn_set_mult), and
+// the action's multiplet term of nv vectors into its d_accpart slices
+int mixed_set_mult(ocn_ctx* c);
+int mult_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vstride, int nv,
+                     bool b1_ready);
 // tile configuration {stages, GEMM2 K splits, GEMM1 grid cap, GEMM2 grid cap,
 // k-mesh transforms per CTA}
 int mixed_configure(ocn_ctx* c, const int cfg[5]);

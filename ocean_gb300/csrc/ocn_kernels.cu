@@ -897,6 +897,29 @@ int lr_wgrad_fp64(ocn_ctx* c, const double* x, const double* y, double2* phi, do
   return OCN_OK;
 }
 
+// hamp = mul (-mpm amp + MH amp) of one vector (k_mult_hamp), amp/hamp [p][a]
+int mult_hamp(ocn_ctx* c, const double2* amp, double2* hamp) {
+  MultDev& m = c->mult;
+  const double mul = c->sys.interaction_scale / ((double)c->nk * c->sys.celvol);
+  const int npa = m.np * c->na;
+  const int threads = 256;
+  const int blocks = (npa * 32 + threads - 1) / threads;
+  k_mult_hamp<<<blocks, threads, 0, c->stream>>>(amp, hamp, m.p_l, m.p_m, m.p_nu, m.d_pfirst, m.mpm, m.mh,
+                                                m.d_jbeg, m.d_nproj, m.np, c->na, m.lmin, m.npmax, mul);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
+// Slices of d_accpart that hold terms of the current action: the long-range
+// K-split partials, followed (mixed precision) by the multiplet's.
+void active_parts(const ocn_ctx* c, const int* hf, const double** base, int* count) {
+  const bool lr = c->sys.long_range && hf[0] == 1;
+  const bool mm = c->mult_parts > 0 && c->sys.mult && hf[4] == 1 && c->have_mult;
+  *base = c->d_accpart + (lr ? 0 : (size_t)c->lr_xsplit * c->part_stride);
+  *count = (lr ? c->lr_xsplit : 0) + (mm ? c->mult_parts : 0);
+}
+
 int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi, double* acc) {
   MultDev& m = c->mult;
   TimedScope ts(c, T_MULT);
@@ -940,13 +963,15 @@ int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* 
             size_t vstride, const int* hflag, int backwards) {
   const int nbk = c->nb * c->nk;
   const int use_so = (c->sys.mult && hflag[5] == 1 && c->have_so) ? 1 : 0;
-  const int nparts = (c->sys.long_range && hflag[0] == 1) ? c->lr_xsplit : 0;
+  const double* parts;
+  int nparts;
+  active_parts(c, hflag, &parts, &nparts);
   const BlockStrides bs = {vstride, c->part_stride, 0, 0};
   auto kern = (c->na == 4) ? k_combine<4> : k_combine<12>;
   dim3 grid(grid_for(nbk, 256, 4 * c->sm_count), nv);
   kern<<<grid, 256, 0, c->stream>>>(
       d_pr, d_pi, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow,
-      c->acc_valid ? c->d_acc : nullptr, c->d_accpart, nparts,
+      c->acc_valid ? c->d_acc : nullptr, parts, nparts,
       c->d_so, d_or, d_oi, nbk, c->na, c->npsi, c->sys.e0, use_so, backwards, nullptr, nullptr,
       nullptr, nullptr, nullptr, bs);
   ++c->launches;
@@ -964,14 +989,16 @@ int lanczos_launch(ocn_ctx* c, int nv, const double* old, const double* psi, dou
   const size_t n = c->npsi;
   const int* hf = c->sys.nhflag;
   const int use_so = (c->sys.mult && hf[5] == 1 && c->have_so) ? 1 : 0;
-  const int nparts = (c->sys.long_range && hf[0] == 1) ? c->lr_xsplit : 0;
+  const double* parts;
+  int nparts;
+  active_parts(c, hf, &parts, &nparts);
   const int nblk = c->red_blocks;
   const BlockStrides bs = {2 * n, c->part_stride, cstride, (size_t)4 * nblk};
   TimedScope ts(c, T_LANCZOS);
   dim3 grid(nblk, nv);
   auto kern = (c->na == 4) ? k_combine<4> : k_combine<12>;
   kern<<<grid, 256, 0, c->stream>>>(psi, psi + n, c->d_er, c->ei_nonzero ? c->d_ei : nullptr,
-                                    c->d_allow, c->acc_valid ? c->d_acc : nullptr, c->d_accpart,
+                                    c->d_allow, c->acc_valid ? c->d_acc : nullptr, parts,
                                     nparts, c->d_so, h, h + n, nbk, c->na, n, c->sys.e0, use_so, 0,
                                     old, old + n, rb, itp, c->d_red, bs);
   ++c->launches;

@@ -70,6 +70,7 @@ struct TcParams {
   double* part;  // mode 2 output [split][v][re|im][npsi]
   size_t npsi;
   int* err;
+  int bshared;   // B operand has one k slice shared by every k (multiplet back-projection)
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
@@ -243,7 +244,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           mbar_expect_tx(full0 + 8 * stage, stage_bytes);
           tma_load_3d(sbase, &tm_hi, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k);
           tma_load_3d(sbase + a_bytes, &tm_lo, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k);
-          tma_load_3d(sbase + 2 * a_bytes, &tm_b, full0 + 8 * stage, c * TC_BK, 0, ti.k);
+          tma_load_3d(sbase + 2 * a_bytes, &tm_b, full0 + 8 * stage, c * TC_BK, 0, p.bshared ? 0 : ti.k);
           armed_phase[stage] = (int)phase;
           if (++stage == (uint32_t)S) {
             stage = 0;
@@ -451,6 +452,95 @@ __global__ void k_prep_b1(const double* __restrict__ pr, const double* __restric
   }
 }
 
+// Multiplet amplitude operand MA[k][p][K1]: K < Nb -> Re mpc(p, n=K, k), else
+// Im mpc(p, n=K-Nb, k) -- the layout of UA with the projector p in place of x,
+// so amp(p, a) = sum_{k,n} mpc q (OCEAN_multiplet.f90:1730-1783) is the band->x
+// contraction against the same psi operand B1, summed over k afterwards.
+__global__ void k_build_ma(const double2* __restrict__ mpc, __nv_bfloat16* __restrict__ hi,
+                           __nv_bfloat16* __restrict__ lo, int nb, int nk, int np, int p1) {
+  const long long total = (long long)nk * np * 2 * nb;
+  const size_t nbk = (size_t)nb * nk;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int K = (int)(i % (2 * nb));
+    const long long r = i / (2 * nb);
+    const int p = (int)(r % np);
+    const int k = (int)(r / np);
+    const int n = K < nb ? K : K - nb;
+    const double2 z = mpc[(size_t)p * nbk + (size_t)k * nb + n];
+    __nv_bfloat16 h, l;
+    split_bf16((float)(K < nb ? z.x : z.y), h, l);
+    const size_t o = ((size_t)k * np + p) * p1 + K;
+    hi[o] = h;
+    lo[o] = l;
+  }
+}
+
+// Back-projection operand MB[k][n][K3]: K3 < Np -> Re mpc(p=K3, n, k), else
+// Im mpc(p=K3-Np, n, k) -- the layout of UB with p in place of x, so that
+// acc(n,k,a) += sum_p conj(mpc) hamp (OCEAN_multiplet.f90:1943-1998) is the
+// x->band contraction against B3 built from hamp.
+__global__ void k_build_mb(const double2* __restrict__ mpc, __nv_bfloat16* __restrict__ hi,
+                           __nv_bfloat16* __restrict__ lo, int nb, int nk, int np, int p3) {
+  const long long total = (long long)nk * nb * 2 * np;
+  const size_t nbk = (size_t)nb * nk;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int K = (int)(i % (2 * np));
+    const long long r = i / (2 * np);
+    const int n = (int)(r % nb);
+    const int k = (int)(r / nb);
+    const int p = K < np ? K : K - np;
+    const double2 z = mpc[(size_t)p * nbk + (size_t)k * nb + n];
+    __nv_bfloat16 h, l;
+    split_bf16((float)(K < np ? z.x : z.y), h, l);
+    const size_t o = ((size_t)k * nb + n) * p3 + K;
+    hi[o] = h;
+    lo[o] = l;
+  }
+}
+
+// amp[v][p][a] = sum_k amp_part[k][p][v*Na + a], summed in FP64
+__global__ void k_amp_reduce_f32(const float2* __restrict__ part, double2* __restrict__ amp, int nk, int np,
+                                 int na, int nv) {
+  const int nt = na * nv;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np * nt) return;
+  const int p = i / nt, t = i % nt;
+  double sr = 0.0, si = 0.0;
+  for (int k = 0; k < nk; ++k) {
+    const float2 f = part[((size_t)k * np + p) * nt + t];
+    sr += (double)f.x;
+    si += (double)f.y;
+  }
+  const int v = t / na, a = t % na;
+  amp[((size_t)v * np + p) * na + a] = make_double2(sr, si);
+}
+
+// B3[v*4Na + j][K3] from h = -hamp[v][p][a] (the x->band epilogue negates):
+//   part 0: K=(0,p) -> Re h, K=(1,p) -> Im h;  part 1: (0,p) -> Im h, (1,p) -> -Re h
+__global__ void k_prep_b3(const double2* __restrict__ hamp, __nv_bfloat16* __restrict__ b3, int np, int na,
+                          int nv, int p3) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nv * np * na) return;
+  const int a = i % na, p = (i / na) % np, v = i / (na * np);
+  const double2 hz = hamp[i];
+  const float hr = (float)(-hz.x), hi_ = (float)(-hz.y);
+  __nv_bfloat16* base = b3 + (size_t)v * 4 * na * p3;
+  __nv_bfloat16 rh, rl, ih, il, nh, nl;
+  split_bf16(hr, rh, rl);
+  split_bf16(hi_, ih, il);
+  split_bf16(-hr, nh, nl);
+  base[(size_t)a * p3 + p] = rh;
+  base[(size_t)a * p3 + np + p] = ih;
+  base[(size_t)(2 * na + a) * p3 + p] = rl;
+  base[(size_t)(2 * na + a) * p3 + np + p] = il;
+  base[(size_t)(na + a) * p3 + p] = ih;
+  base[(size_t)(na + a) * p3 + np + p] = nh;
+  base[(size_t)(3 * na + a) * p3 + p] = il;
+  base[(size_t)(3 * na + a) * p3 + np + p] = nl;
+}
+
 // Lanczos normalisation fused with the next action's psi operand
 // (OCEAN_haydock.f90:880-889 then long_range.f90:897-906): for chain v =
 // blockIdx.y, b_i = sqrt(sum of partials), psi = h / b_i written in place, and
@@ -594,6 +684,17 @@ struct MixedLR {
   int cfg[5] = {0, 0, 0, 0, 0};  // stages, GEMM2 K splits (requested), grid caps of GEMM1 / GEMM2,
                                 // k-mesh transforms per CTA (0: all of an x-point)
   size_t part_cap = 0;      // splits the partial-sum buffer holds
+  // multiplet projector contractions (fg_combo) on the tensor cores
+  bool mult_ready = false;
+  int np = 0, p3 = 0;
+  __nv_bfloat16 *ma_hi = nullptr, *ma_lo = nullptr;  // [k][p][p1]: amplitude contraction A
+  __nv_bfloat16 *mb_hi = nullptr, *mb_lo = nullptr;  // [k][n][p3]: back-projection A
+  __nv_bfloat16* b3 = nullptr;                        // [col][p3]: back-projection B (all k)
+  float2* amp_part = nullptr;                         // [k][p][v*Na + a]
+  double2 *amp = nullptr, *hamp = nullptr;            // [v][p][a]
+  CUtensorMap tm_ma_hi, tm_ma_lo, tm_mb_hi, tm_mb_lo, tm_b3;
+  TcParams gm1{}, gm2{};
+  int gridm1 = 0, gridm2 = 0;
   bool ready = false;
 };
 
@@ -740,19 +841,24 @@ int mixed_configure(ocn_ctx* c, const int cfg[5]) {
   g2.cps2 = (g2.nch + ks - 1) / ks;
   g2.ks2 = (g2.nch + g2.cps2 - 1) / g2.cps2;  // no empty split
   g2.ntiles = c->nk * g2.mt2 * g2.ks2;
-  if ((size_t)g2.ks2 > m->part_cap) {
+  const size_t need = (size_t)g2.ks2 + (size_t)c->mult_parts;  // LR splits, then the multiplet's
+  if (need > m->part_cap) {
     double* np = nullptr;
-    int rc = alloc(c, &np, (size_t)g2.ks2 * c->part_stride);
+    int rc = alloc(c, &np, need * c->part_stride);
     if (rc) return rc;
     if (c->d_accpart) cudaFree(c->d_accpart);
     c->d_accpart = np;
-    m->part_cap = (size_t)g2.ks2;
+    m->part_cap = need;
   }
   g2.part = c->d_accpart;
   c->lr_xsplit = g2.ks2;
+  m->gm2.part = c->d_accpart + (size_t)g2.ks2 * c->part_stride;
   m->smem_bytes = 1024 + (size_t)cfg[0] * m->stage_bytes + 256;
   m->grid1 = std::min(g1.ntiles, std::min(cfg[2], c->sm_count));
   m->grid2 = std::min(g2.ntiles, std::min(cfg[3], c->sm_count));
+  m->gm1.stages = m->gm2.stages = cfg[0];
+  m->gridm1 = std::min(m->gm1.ntiles, std::min(cfg[2], c->sm_count));
+  m->gridm2 = std::min(m->gm2.ntiles, std::min(cfg[3], c->sm_count));
   for (int i = 0; i < 5; ++i) m->cfg[i] = cfg[i];
   return OCN_OK;
 }
@@ -833,10 +939,104 @@ int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* curren
   return OCN_OK;
 }
 
+// Split-BF16 operands and tiling of the multiplet projector contractions, from
+// the projector coefficients of ocn_set_mult (c->mult.mpc, nspn = 1).
+int mixed_set_mult(ocn_ctx* c) {
+  MixedLR* m = c->mixed;
+  if (!m) return OCN_OK;
+  MultDev& d = c->mult;
+  void* old[] = {m->ma_hi, m->ma_lo, m->mb_hi, m->mb_lo, m->b3, m->amp_part, m->amp, m->hamp};
+  for (void* q : old)
+    if (q) cudaFree(q);
+  m->ma_hi = m->ma_lo = m->mb_hi = m->mb_lo = m->b3 = nullptr;
+  m->amp_part = nullptr;
+  m->amp = m->hamp = nullptr;
+  m->mult_ready = false;
+  c->mult_parts = 0;
+  const int np = d.np, nb = c->nb, nk = c->nk, na = c->na, nvmax = m->nvmax;
+  if (np < 1) return OCN_OK;
+  m->np = np;
+  m->p3 = (2 * np + 7) / 8 * 8;
+  int rc;
+  if ((rc = alloc(c, &m->ma_hi, (size_t)nk * np * m->p1)) || (rc = alloc(c, &m->ma_lo, (size_t)nk * np * m->p1)) ||
+      (rc = alloc(c, &m->mb_hi, (size_t)nk * nb * m->p3)) || (rc = alloc(c, &m->mb_lo, (size_t)nk * nb * m->p3)) ||
+      (rc = alloc(c, &m->b3, (size_t)m->ncol * m->p3)) ||
+      (rc = alloc(c, &m->amp_part, (size_t)nk * np * na * nvmax)) ||
+      (rc = alloc(c, &m->amp, (size_t)nvmax * np * na)) || (rc = alloc(c, &m->hamp, (size_t)nvmax * np * na)))
+    return rc;
+  OCN_CUDA(c, cudaMemsetAsync(m->b3, 0, (size_t)m->ncol * m->p3 * 2, c->stream));
+  const int grid = 8 * c->sm_count;
+  k_build_ma<<<grid, 256, 0, c->stream>>>(d.mpc, m->ma_hi, m->ma_lo, nb, nk, np, m->p1);
+  k_build_mb<<<grid, 256, 0, c->stream>>>(d.mpc, m->mb_hi, m->mb_lo, nb, nk, np, m->p3);
+  c->launches += 2;
+  OCN_CUDA(c, cudaGetLastError());
+  void* fnp = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fnp, 12000, cudaEnableDefault, &q);
+  if (e != cudaSuccess || !fnp) return set_err(c, OCN_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  EncodeTiledFn fn = reinterpret_cast<EncodeTiledFn>(fnp);
+  if ((rc = encode3d(c, fn, &m->tm_ma_hi, m->ma_hi, 2 * nb, np, nk, m->p1, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_ma_lo, m->ma_lo, 2 * nb, np, nk, m->p1, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_mb_hi, m->mb_hi, 2 * np, nb, nk, m->p3, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_mb_lo, m->mb_lo, 2 * np, nb, nk, m->p3, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_b3, m->b3, 2 * np, m->ncol, 1, m->p3, m->ncol)))
+    return rc;
+  TcParams& a = m->gm1;  // amplitudes: band->x form with Np rows per k
+  a = m->g1;
+  a.nx = np;
+  a.nxt = (np + TC_BM - 1) / TC_BM;
+  a.ntiles = nk * a.nxt;
+  a.phi = m->amp_part;
+  a.bshared = 0;
+  TcParams& b = m->gm2;  // back-projection: x->band form over 2 Np, B shared by every k
+  b = m->g2;
+  b.nx = np;
+  b.nch = (2 * np + TC_BK - 1) / TC_BK;
+  b.cps2 = b.nch;
+  b.ks2 = 1;
+  b.ntiles = nk * b.mt2;
+  b.bshared = 1;
+  c->mult_parts = 1;
+  if ((rc = mixed_configure(c, m->cfg))) return rc;  // partial-sum room, multiplet grids
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+  m->mult_ready = true;
+  return OCN_OK;
+}
+
+// Multiplet term of nv vectors (OCEAN_fg_combo, OCEAN_multiplet.f90:1617-2005):
+// amplitudes on the tensor cores, the direct / exchange matrices in FP64
+// (k_mult_hamp), the back-projection on the tensor cores into the multiplet
+// slice of d_accpart.  b1_ready: the psi operand B1 already holds these vectors.
+int mult_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vstride, int nv, bool b1_ready) {
+  MixedLR* m = c->mixed;
+  if (!m || !m->mult_ready) return set_err(c, OCN_ERR_STATE, "mixed-precision multiplet operands not built");
+  if (nv < 1 || nv > m->nvmax) return set_err(c, OCN_ERR_ARG, "block size exceeds nvec");
+  int rc;
+  if (!b1_ready && (rc = mixed_prep_b1(c, d_pr, d_pi, vstride, nv))) return rc;
+  TimedScope ts(c, T_MULT);
+  const int np = m->np, na = c->na;
+  TcParams a = m->gm1, b = m->gm2;
+  a.nv = nv;
+  b.nv = nv;
+  k_lr_tc<<<m->gridm1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ma_hi, m->tm_ma_lo, m->tm_b1, a);
+  k_amp_reduce_f32<<<(np * na * nv + 127) / 128, 128, 0, c->stream>>>(m->amp_part, m->amp, c->nk, np, na, nv);
+  c->launches += 2;
+  OCN_CUDA(c, cudaGetLastError());
+  for (int v = 0; v < nv; ++v)
+    if ((rc = mult_hamp(c, m->amp + (size_t)v * np * na, m->hamp + (size_t)v * np * na))) return rc;
+  k_prep_b3<<<(nv * np * na + 127) / 128, 128, 0, c->stream>>>(m->hamp, m->b3, np, na, nv, m->p3);
+  k_lr_tc<<<m->gridm2, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_mb_hi, m->tm_mb_lo, m->tm_b3, b);
+  c->launches += 2;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
 int mixed_free(ocn_ctx* c) {
   MixedLR* m = c->mixed;
   if (!m) return OCN_OK;
-  void* bufs[] = {m->ua_hi, m->ua_lo, m->ub_hi, m->ub_lo, m->b1, m->b2, m->phi, m->Wf, m->d_err, m->twf};
+  void* bufs[] = {m->ua_hi, m->ua_lo, m->ub_hi, m->ub_lo, m->b1,     m->b2,       m->phi,  m->Wf,
+                  m->d_err, m->twf,   m->ma_hi, m->ma_lo, m->mb_hi, m->mb_lo, m->b3, m->amp_part,
+                  m->amp,   m->hamp};
   for (void* p : bufs)
     if (p) cudaFree(p);
   delete m;

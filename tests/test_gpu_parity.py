@@ -277,3 +277,27 @@ def test_gmres_mixed_matches_oracle(built):
     rc, ore2, oim2, rel2, its2, tot = P.gmres(E, depth=16, ffff=1e-14, max_restarts=200)
     assert rc == 0
     assert np.max(np.abs(oim - oim2) / np.abs(oim2)) < 1e-3
+
+
+@pytest.mark.parametrize("name", ["c3small"])
+def test_multiplet_mixed_tensor_core_term(built, name):
+    """The multiplet term alone (long range off): split-BF16 tcgen05 projector
+    contractions with the FP64 direct/exchange matrices, against the oracle."""
+    _, O = built
+    w, P = problem(name, O, seed=6)
+    rng = np.random.default_rng(17)
+    pr, pi = rng.standard_normal(w.npsi), rng.standard_normal(w.npsi)
+    ctx = capi.Context(w, precision=capi.OCN_PREC_MIXED)
+    try:
+        m1 = (0, 1, 1, 1, 1, 0)
+        m0 = (0, 1, 1, 1, 0, 0)
+        r1, i1 = ctx.apply_H(pr, pi, hflag=m1)
+        r0, i0 = ctx.apply_H(pr, pi, hflag=m0)
+        o1r, o1i = P.xact(pr, pi, hflag=m1)
+        o0r, o0i = P.xact(pr, pi, hflag=m0)
+        got = (r1 - r0) + 1j * (i1 - i0)
+        ref = (o1r - o0r) + 1j * (o1i - o0i)
+        assert np.linalg.norm(ref) > 0
+        assert _rel(got, ref) < 2e-4
+    finally:
+        ctx.close()
