@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--block", type=int, default=3,
                     help="chains of the block-Haydock leg (polarisations sharing H); 0 = off")
+    ap.add_argument("--multiplet-steps", type=int, default=200,
+                    help="Lanczos steps of the 2p-edge multiplet leg (c3 sizes); 0 = off")
     ap.add_argument("--batch", type=int, default=64,
                     help="instances of the batched uneven-Haydock leg (3 polarisations each); 0 = off")
     ap.add_argument("--adjoint-omega", type=int, default=400,
@@ -254,6 +256,35 @@ def _device_steps(ctx, w, niter, ne, pr_ptr, pi_ptr, steps, stream, torch):
     return ev0.elapsed_time(ev1), last
 
 
+def run_multiplet(args, torch, capi, WL, local, dev):
+    """c3: Haydock with the multiplet (tcgen05 projector contractions) and
+    spin-orbit terms; H*psi/s of both precisions and the spectral error."""
+    import time
+
+    w = WL.make("c3", seed=0)
+    niter = args.multiplet_steps
+    out = {"workload": f"c3: {describe(w)}, multiplet l=0..3 x 8 projectors + spin-orbit", "steps": niter}
+    spec = {}
+    for name, prec in (("mixed", capi.OCN_PREC_MIXED), ("fp64", capi.OCN_PREC_FP64)):
+        ctx = capi.Context(w, precision=prec, device=local)
+        ctx.haydock(9)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ra, ia, rb, done = ctx.haydock(niter)
+        dt = time.perf_counter() - t0
+        ctx.timing(True)
+        ctx.timing_reset()
+        ctx.haydock(30)
+        kt = ctx.timing_read()
+        ctx.close()
+        spec[name] = capi.spectrum_cf(ra, ia, rb, done, w.kpref, w.el, w.eh, args.ne, w.gam0)
+        out[name] = {"value": niter / dt, "unit": UNIT, "ms_per_hpsi": dt * 1e3 / niter, "kernel_ms_30_steps": kt}
+    out["spectral_error_mixed_vs_fp64"] = float(np.linalg.norm(spec["mixed"][:, 2] - spec["fp64"][:, 2]) /
+                                                np.linalg.norm(spec["fp64"][:, 2]))
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def run_batch(args, torch, capi, WL, local, dev, niter: int = 500, nv: int = 3):
     """Batched uneven instances: autotuned tiles per instance, one batched run
     (ocn_haydock_batch) against the same instances run one after another."""
@@ -435,6 +466,12 @@ def run_ours(args, ws, rank, local, pg):
                         "gamma": float(pt[2].grad), "scissor": float(pt[3].grad)}}
         prob.close()
 
+    # ---- multiplet leg: 2p edge with multiplet and spin-orbit terms (6^3 k, 64 bands,
+    #      10^3 x-mesh, 128 projectors), mixed precision against the FP64 path
+    mlt = None
+    if rank == 0 and args.multiplet_steps > 0 and prec == capi.OCN_PREC_MIXED:
+        mlt = run_multiplet(args, torch, capi, WL, local, dev)
+
     # ---- batched leg: independent uneven instances (k-mesh n^3, n in {4,5,6,8};
     #      bands U{24..128}; 1s or 2p; x-mesh 8^3..12^3), 3 polarisations each,
     #      500 Lanczos steps, all advanced by one graph launch per 3 steps
@@ -521,7 +558,8 @@ def run_ours(args, ws, rank, local, pg):
                        "l2": "inputs larger than L2 (u2 %.2f GB per contraction operand)" % (
                            w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
             "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
-            "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "adjoint": adj, "batch": bat, "roofline": roof, "cpu_baseline": cpu,
+            "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "adjoint": adj, "batch": bat,
+            "multiplet": mlt, "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
                     "d2h_bytes_per_step": 3 * (niter + 1) * 8 + (ne + 1) * 9 * 8},
             "gpu_launches": launches, "clocks": clocks, "kernel_ms": kt}
