@@ -61,6 +61,17 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(pg, value: float, device="cpu") -> float:
+    """The slowest rank's value (the whole job's clock); value itself at N=1."""
+    if pg is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_setup(args):
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -378,10 +389,7 @@ def run_ours(args, ws, rank, local, pg):
     _device_steps(ctx, w, niter, ne, pr_ptr, pi_ptr, 1, stream, torch)
     kt = ctx.timing_read()
     ctx.timing(False)
-    if pg is not None:
-        t = torch.tensor([dev_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        dev_ms = float(t.item())
+    dev_ms = max_over_ranks(pg, dev_ms, dev)
     total_hpsi = niter * args.steps * ws
     value = total_hpsi / (dev_ms / 1000.0)
 
@@ -404,10 +412,7 @@ def run_ours(args, ws, rank, local, pg):
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
-    if pg is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(pg, e2e_ms, dev)
     e2e_value = total_hpsi / (e2e_ms / 1000.0)
 
     # ---- GMRES leg: 200 energies across the spectrum, tol 1e-6 on |g|^2, depth 80
