@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--block", type=int, default=3,
                     help="chains of the block-Haydock leg (polarisations sharing H); 0 = off")
+    ap.add_argument("--c1-steps", type=int, default=200,
+                    help="Lanczos steps of the 4^3 k / 32-band / 8^3 x leg, with the oracle's full run beside it; 0 = off")
     ap.add_argument("--multiplet-steps", type=int, default=200,
                     help="Lanczos steps of the 2p-edge multiplet leg (c3 sizes); 0 = off")
     ap.add_argument("--batch", type=int, default=64,
@@ -267,6 +269,42 @@ def _device_steps(ctx, w, niter, ne, pr_ptr, pi_ptr, steps, stream, torch):
     return ev0.elapsed_time(ev1), last
 
 
+def run_small(args, torch, capi, WL, local):
+    """c1 (4^3 k, 32 bands, 8^3 x, 1s): 200 Lanczos steps + 2001-point spectrum on
+    the GPU (both precisions) and the same run by the oracle on all host cores."""
+    import time
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    w = WL.make("c1", seed=0)
+    niter = args.c1_steps
+    out = {"workload": f"c1: {describe(w)}", "steps": niter}
+    spec = {}
+    for name, prec in (("mixed", capi.OCN_PREC_MIXED), ("fp64", capi.OCN_PREC_FP64)):
+        ctx = capi.Context(w, precision=prec, device=local)
+        ctx.haydock(niter)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ra, ia, rb, done = ctx.haydock(niter)
+        spec[name] = capi.spectrum_cf(ra, ia, rb, done, w.kpref, w.el, w.eh, args.ne, w.gam0)
+        dt = time.perf_counter() - t0
+        ctx.close()
+        out[name] = {"value": niter / dt, "unit": UNIT, "spectra_per_s": 1.0 / dt}
+    cores = os.cpu_count() or 1
+    P = O.OracleProblem(w, nthreads=cores)
+    t0 = time.perf_counter()
+    rc, ora, oia, orb, odone = P.haydock(niter)
+    so = O.write_core(ora, oia, orb, odone, w.kpref, w.el, w.eh, args.ne, w.gam0)
+    dt = time.perf_counter() - t0
+    out["cpu_oracle"] = {"value": niter / dt, "unit": UNIT, "spectra_per_s": 1.0 / dt, "cores": cores,
+                         "kind": "port"}
+    for name in ("mixed", "fp64"):
+        out[name]["spectral_error_vs_oracle"] = float(np.linalg.norm(spec[name][:, 2] - so[:, 2]) /
+                                                      np.linalg.norm(so[:, 2]))
+    return out
+
+
 def run_multiplet(args, torch, capi, WL, local, dev):
     """c3: Haydock with the multiplet (tcgen05 projector contractions) and
     spin-orbit terms; H*psi/s of both precisions and the spectral error."""
@@ -471,6 +509,12 @@ def run_ours(args, ws, rank, local, pg):
                         "gamma": float(pt[2].grad), "scissor": float(pt[3].grad)}}
         prob.close()
 
+    # ---- small-case leg (the CPU-runnable configuration): GPU precisions and the
+    #      oracle's whole Haydock run on all host cores
+    small = None
+    if rank == 0 and args.c1_steps > 0:
+        small = run_small(args, torch, capi, WL, local)
+
     # ---- multiplet leg: 2p edge with multiplet and spin-orbit terms (6^3 k, 64 bands,
     #      10^3 x-mesh, 128 projectors), mixed precision against the FP64 path
     mlt = None
@@ -564,7 +608,7 @@ def run_ours(args, ws, rank, local, pg):
                            w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
             "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
             "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "adjoint": adj, "batch": bat,
-            "multiplet": mlt, "roofline": roof, "cpu_baseline": cpu,
+            "multiplet": mlt, "c1": small, "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
                     "d2h_bytes_per_step": 3 * (niter + 1) * 8 + (ne + 1) * 9 * 8},
             "gpu_launches": launches, "clocks": clocks, "kernel_ms": kt}
