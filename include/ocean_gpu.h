@@ -335,6 +335,58 @@ int ocn_gmres_vjp(ocn_ctx* ctx, const double* d_hay, double kpref, const double*
 int ocn_w2_vjp(const ocn_dims* dims, const ocn_lr_params* p, const double* G, double* g_ptab,
                double* g_scale);
 
+/* ----------------------------------------------------- reference text files */
+
+/* The solver settings of bse.in as ocean.x reads them (list-directed input):
+ * record 1 an integer, record 2 a real (OCEAN_driver.f90:67-68), record 3 the
+ * style; for 'hay' (OCEAN_haydock.f90:2118) niter ne el eh gam0 ebase; for 'inv'
+ * (OCEAN_gmres.f90:89-124) depth resolution preconditioner convergence, then
+ * 'list' (count, one energy per record) or 'loop' (start stop step, count
+ * 1 + ceiling((stop - start - step*1e-4)/step)).  Energies stay in eV as written;
+ * a non-positive gam0 / resolution means "core-hole lifetime" to the reference
+ * and is returned unchanged. */
+typedef struct {
+  int dumi;
+  double dumf;
+  char style[8];        /* 'hay', 'inv', 'exa' or 'dia' */
+  int niter, ne;        /* hay */
+  double el, eh, gam0, ebase;
+  int depth;            /* inv */
+  double resolution, preconditioner, convergence;
+  char inv_style[8];    /* 'list' or 'loop' */
+  int nomega;
+} ocn_bse_in;
+/* energies (may be NULL): receives up to cap GMRES energies in eV; returns
+ * OCN_ERR_ARG if the list is longer than cap (out->nomega is still set). */
+int ocn_read_bse_in(const char* path, ocn_bse_in* out, double* energies, int cap);
+
+/* write_lanczos (OCEAN_haydock.f90:2318-2358), byte for byte: '(1i8,1x,1ES24.17)'
+ * n, kpref; the coefficients ('(2x,ES24.17)' / '(2(2x,ES24.17))', or six per
+ * record when imag_a is given: the complex Haydock form with real_c/imag_c,
+ * which default to the b arrays); then, when eigs (n+1 values) is given, the
+ * redtrid eigenvalues '(2x,2i5,1f20.10)'.  Arrays are (0:n). */
+int ocn_write_abslanc(const char* path, int n, double kpref, const double* real_a,
+                      const double* imag_a, const double* real_b, const double* imag_b,
+                      const double* real_c, const double* imag_c, const double* eigs);
+
+/* write_core / write_core_Voigt output (OCEAN_haydock.f90:1831-1892,1922-1985),
+ * byte for byte: header, column names, then ne+1 rows of the 9 (Voigt: first 5)
+ * columns of ocn_spectrum_cf's output, '(9(1e15.8,1x))'.  gam0 in Hartree. */
+int ocn_write_absspct(const char* path, int iter, double gam0, double kpref, double ucvol,
+                      int ne, const double* rows /* (ne+1)*9 */, int voigt);
+
+/* abs.gmres (OCEAN_gmres.f90:864-869): per energy '(1p,4(1e15.8,1x),1i6,1x,i10)'
+ * energy (eV, through Hartree and back as the reference does), out_re, out_im,
+ * rel_err, iterations, running total of iterations. */
+int ocn_write_abs_gmres(const char* path, int nomega, const double* energies_ev,
+                        const double* out_re, const double* out_im, const double* rel_err,
+                        const int* iters);
+
+/* OCEAN_filenames_spectrum / _lanc (OCEAN_filenames.f90:21-107) for XAS / XES
+ * runs: kind "spct" or "lanc", e.g. absspct_Cu.0001_1s_01. */
+int ocn_output_filename(const char* kind, const char* calc_type, const char* elname, int indx,
+                        const char* corelevel, int photon, char* buf, size_t len);
+
 /* --------------------------------------------------------------- counters */
 
 /* Number of kernels this context launched since creation (for accounting). */

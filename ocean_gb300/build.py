@@ -28,6 +28,7 @@ SOURCES = {
     "ocn_cf.cu": ["-fmad=false"],
     "ocn_mixed.cu": [],
     "ocn_setup.cpp": [],
+    "ocn_io.cpp": [],
 }
 
 
@@ -44,7 +45,8 @@ def nvcc() -> str:
 def _compile(src: str, extra: list[str], verbose: bool) -> str:
     obj = os.path.join(BUILD, src + ".o")
     srcp = os.path.join(CSRC, src)
-    deps = [srcp, os.path.join(CSRC, "ocn_internal.h"), os.path.join(ROOT, "include", "ocean_gpu.h")]
+    deps = [srcp, os.path.join(CSRC, "ocn_internal.h"), os.path.join(CSRC, "ocn_kmesh_dft.cuh"),
+            os.path.join(ROOT, "include", "ocean_gpu.h")]
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc()] + ARCH + COMMON + extra + ["-c", srcp, "-o", obj]

@@ -64,6 +64,14 @@ class OcnGmresParams(C.Structure):
                 ("convergence", C.c_double), ("max_restarts", C.c_int)]
 
 
+class OcnBseIn(C.Structure):
+    _fields_ = [("dumi", C.c_int), ("dumf", C.c_double), ("style", C.c_char * 8), ("niter", C.c_int),
+                ("ne", C.c_int), ("el", C.c_double), ("eh", C.c_double), ("gam0", C.c_double),
+                ("ebase", C.c_double), ("depth", C.c_int), ("resolution", C.c_double),
+                ("preconditioner", C.c_double), ("convergence", C.c_double), ("inv_style", C.c_char * 8),
+                ("nomega", C.c_int)]
+
+
 # every entry point declared in include/ocean_gpu.h
 EXPORTS = [
     "ocn_ctx_create", "ocn_ctx_destroy", "ocn_last_error", "ocn_version", "ocn_set_system",
@@ -74,6 +82,7 @@ EXPORTS = [
     "ocn_timing_enable", "ocn_timing_reset", "ocn_timing_read", "ocn_stream", "ocn_apply_H_block",
     "ocn_haydock_block", "ocn_haydock_block_dev", "ocn_spectrum_cf_noalloc", "ocn_gmres_dev",
     "ocn_gmres_vjp", "ocn_w2_vjp", "ocn_haydock_batch", "ocn_autotune", "ocn_set_tiles", "ocn_get_tiles",
+    "ocn_read_bse_in", "ocn_write_abslanc", "ocn_write_absspct", "ocn_write_abs_gmres", "ocn_output_filename",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -468,6 +477,46 @@ def spectrum_cf_noalloc(ra, ia, rb, iteration: int, kpref: float, el: float, eh:
     check(lib.ocn_spectrum_cf_noalloc(_dp(_f64(ra)), ia_p, _dp(_f64(rb)), iteration, C.c_double(kpref),
                                       C.byref(p), _dp(out)))
     return out.reshape(ne + 1, 9)
+
+
+def read_bse_in(path: str) -> dict:
+    """bse.in as ocean.x reads it; energies (eV) of a GMRES run under 'energies'."""
+    lib = load()
+    b = OcnBseIn()
+    check(lib.ocn_read_bse_in(path.encode(), C.byref(b), None, 0))
+    e = np.zeros(max(b.nomega, 1))
+    if b.nomega > 0:
+        check(lib.ocn_read_bse_in(path.encode(), C.byref(b), _dp(e), len(e)))
+    d = {k: getattr(b, k) for k, _ in OcnBseIn._fields_}
+    d["style"], d["inv_style"] = b.style.decode(), b.inv_style.decode()
+    d["energies"] = e[:b.nomega]
+    return d
+
+
+def write_abslanc(path: str, n: int, kpref: float, ra, rb, ia=None, ib=None, rc=None, ic=None, eigs=None):
+    opt = [None if a is None else _dp(_f64(a)) for a in (ia, ib, rc, ic, eigs)]
+    check(load().ocn_write_abslanc(path.encode(), n, C.c_double(kpref), _dp(_f64(ra)), opt[0], _dp(_f64(rb)),
+                                   opt[1], opt[2], opt[3], opt[4]))
+
+
+def write_absspct(path: str, iteration: int, gam0: float, kpref: float, ucvol: float, rows, voigt: bool = False):
+    rows = np.ascontiguousarray(rows, dtype=np.float64)
+    ne = rows.shape[0] - 1
+    check(load().ocn_write_absspct(path.encode(), iteration, C.c_double(gam0), C.c_double(kpref),
+                                   C.c_double(ucvol), ne, _dp(rows.reshape(-1)), int(bool(voigt))))
+
+
+def write_abs_gmres(path: str, energies_ev, out_re, out_im, rel_err, iters):
+    it = np.ascontiguousarray(iters, dtype=np.int32)
+    check(load().ocn_write_abs_gmres(path.encode(), len(it), _dp(_f64(energies_ev)), _dp(_f64(out_re)),
+                                     _dp(_f64(out_im)), _dp(_f64(rel_err)), it.ctypes.data_as(IP)))
+
+
+def output_filename(kind: str, calc_type: str, elname: str, indx: int, corelevel: str, photon: int) -> str:
+    buf = C.create_string_buffer(64)
+    check(load().ocn_output_filename(kind.encode(), calc_type.encode(), elname.encode(), indx,
+                                     corelevel.encode(), photon, buf, 64))
+    return buf.value.decode()
 
 
 def redtrid(n: int, ra, rb) -> np.ndarray:

@@ -7,6 +7,10 @@ For each of the 7 photon files:
                           (OCEAN2/OCEAN_haydock.f90:2273-2358)
   absspct_Cu.0001_1s_0P : write_core output (OCEAN_haydock.f90:1801-1894); every
                           10th row (plus the last) of the 5001 is kept.
+Text fixtures (verbatim bytes, for the byte-compatibility tests of the writers):
+  cu_abslanc_01.txt       : abslanc_Cu.0001_1s_01 whole
+  cu_absspct_01_rows.txt  : absspct_Cu.0001_1s_01, its two header records and
+                            the same kept rows
 Run from the repository root: python tests/golden/make_golden.py [reference_root]
 """
 import os
@@ -77,6 +81,17 @@ def main():
     data["eh_ev"] = np.array(70.0)
     np.savez_compressed(OUT, **data)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
+    here = os.path.dirname(OUT)
+    with open(os.path.join(RES, "abslanc_Cu.0001_1s_01"), "rb") as f:
+        lanc = f.read()
+    with open(os.path.join(here, "cu_abslanc_01.txt"), "wb") as f:
+        f.write(lanc)
+    with open(os.path.join(RES, "absspct_Cu.0001_1s_01"), "rb") as f:
+        lines = f.read().split(b"\n")
+    body = [l for l in lines[2:] if l]
+    keep = np.unique(np.concatenate([np.arange(0, len(body), 10), [len(body) - 1]]))
+    with open(os.path.join(here, "cu_absspct_01_rows.txt"), "wb") as f:
+        f.write(b"\n".join(lines[:2] + [body[i] for i in keep]) + b"\n")
 
 
 if __name__ == "__main__":
