@@ -393,18 +393,19 @@ int ocn_output_filename(const char* kind, const char* calc_type, const char* eln
 long long ocn_kernel_launches(const ocn_ctx* ctx);
 
 /* Tile configuration of the mixed-precision tensor-core contractions (no
- * counterpart in the reference, whose BLAS calls have none): tiles[5] =
+ * counterpart in the reference, whose BLAS calls have none): tiles[6] =
  * {shared-memory pipeline stages, K splits of the x->band contraction,
  *  persistent grid cap of the band->x contraction, of the x->band one,
- *  k-mesh transforms per CTA (0 = all of an x-point)}.
+ *  k-mesh transforms per CTA (0 = all of an x-point), threads of a k-mesh
+ *  transform CTA (128, 256 or 512; 0 = 128)}.
  * ocn_autotune times the long-range term of an nv-vector block under each
  * candidate (reps launches each, CUDA events) and keeps the fastest; returns
  * its time in ms, the time of the tiling in force before the call, and the
  * chosen tiles (any output may be NULL).  Tilings change only the order of
  * FP32 partial sums.  Mixed precision only (else OCN_ERR_UNSUPPORTED). */
-int ocn_autotune(ocn_ctx* ctx, int nv, int reps, double* best_ms, double* current_ms, int tiles[5]);
-int ocn_set_tiles(ocn_ctx* ctx, const int tiles[5]);
-int ocn_get_tiles(const ocn_ctx* ctx, int tiles[5]);
+int ocn_autotune(ocn_ctx* ctx, int nv, int reps, double* best_ms, double* current_ms, int tiles[6]);
+int ocn_set_tiles(ocn_ctx* ctx, const int tiles[6]);
+int ocn_get_tiles(const ocn_ctx* ctx, int tiles[6]);
 
 /* Per-kernel device timing with CUDA events recorded on the context stream
  * (replaces the wall-clock buckets of OCEAN_timekeeper, OCEAN_timekeeper.f90:13-168).

@@ -140,7 +140,7 @@ namespace {
 void drop_haydock_graph(ocn_ctx* c);
 }
 
-int ocn_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int tiles[5]) {
+int ocn_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int tiles[6]) {
   if (!c) return OCN_ERR_ARG;
   if (c->dims.precision != OCN_PREC_MIXED || !c->mixed)
     return set_err(c, OCN_ERR_UNSUPPORTED, "ocn_autotune: tiles exist on the mixed-precision path only");
@@ -149,7 +149,7 @@ int ocn_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_
   return mixed_autotune(c, nv, reps, best_ms, current_ms, tiles);
 }
 
-int ocn_set_tiles(ocn_ctx* c, const int tiles[5]) {
+int ocn_set_tiles(ocn_ctx* c, const int tiles[6]) {
   if (!c || !tiles) return OCN_ERR_ARG;
   if (c->dims.precision != OCN_PREC_MIXED || !c->mixed)
     return set_err(c, OCN_ERR_UNSUPPORTED, "ocn_set_tiles: tiles exist on the mixed-precision path only");
@@ -159,7 +159,7 @@ int ocn_set_tiles(ocn_ctx* c, const int tiles[5]) {
   return mixed_configure(c, tiles);
 }
 
-int ocn_get_tiles(const ocn_ctx* c, int tiles[5]) {
+int ocn_get_tiles(const ocn_ctx* c, int tiles[6]) {
   if (!c || !tiles) return OCN_ERR_ARG;
   return c->mixed ? mixed_config(c, tiles) : OCN_ERR_UNSUPPORTED;
 }

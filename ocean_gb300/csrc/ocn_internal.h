@@ -265,9 +265,9 @@ int mixed_set_mult(ocn_ctx* c);
 int mult_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vstride, int nv,
                      bool b1_ready);
 // tile configuration {stages, GEMM2 K splits, GEMM1 grid cap, GEMM2 grid cap,
-// k-mesh transforms per CTA}
-int mixed_configure(ocn_ctx* c, const int cfg[5]);
-int mixed_config(const ocn_ctx* c, int cfg[5]);
-int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int best_cfg[5]);
+// k-mesh transforms per CTA, k-mesh transform threads}
+int mixed_configure(ocn_ctx* c, const int cfg[6]);
+int mixed_config(const ocn_ctx* c, int cfg[6]);
+int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int best_cfg[6]);
 
 }  // namespace ocn

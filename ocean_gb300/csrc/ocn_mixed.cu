@@ -681,8 +681,8 @@ struct MixedLR {
   bool cube = false;        // cubic k-mesh: k_fft_cube_f32 instantiations apply
   size_t stage_bytes = 0;   // shared memory of one pipeline stage
   int max_stages = 1;       // deepest pipeline that fits the shared-memory budget
-  int cfg[5] = {0, 0, 0, 0, 0};  // stages, GEMM2 K splits (requested), grid caps of GEMM1 / GEMM2,
-                                // k-mesh transforms per CTA (0: all of an x-point)
+  int cfg[6] = {0, 0, 0, 0, 0, 0};  // stages, GEMM2 K splits (requested), grid caps of GEMM1 / GEMM2,
+                                   // k-mesh transforms per CTA (0: all of an x-point), its threads (0: 128)
   size_t part_cap = 0;      // splits the partial-sum buffer holds
   // multiplet projector contractions (fg_combo) on the tensor cores
   bool mult_ready = false;
@@ -798,7 +798,7 @@ int mixed_init(ocn_ctx* c) {
   // full pipeline depth, one persistent CTA per SM at most
   int ks = (4 * c->sm_count + nk * g2.mt2 - 1) / (nk * g2.mt2);
   ks = std::max(1, std::min(ks, std::max(1, g2.nch / 4)));
-  const int cfg[5] = {stages, ks, c->sm_count, c->sm_count, 0};
+  const int cfg[6] = {stages, ks, c->sm_count, c->sm_count, 0, 256};  // 256-thread transforms: measured best on 8^3
   if ((rc = mixed_configure(c, cfg))) return rc;
   if (int rc_ = allow_max_smem(c, k_lr_tc)) return rc_;
   if (int rc_ = allow_max_smem(c, k_lr_fft_w_f32)) return rc_;
@@ -827,12 +827,14 @@ int mixed_init(ocn_ctx* c) {
 
 // Tile configuration: cfg = {pipeline stages, K splits of GEMM2, persistent
 // grid cap of GEMM1, of GEMM2, k-mesh transforms per CTA (0 = all of an
-// x-point; a value that does not divide a block's count means all)}.  Grows the
-// partial-sum buffer when a configuration needs more splits.
-int mixed_configure(ocn_ctx* c, const int cfg[5]) {
+// x-point; a value that does not divide a block's count means all), threads of a
+// k-mesh transform CTA (128, 256 or 512; 0 = 128)}.  Grows the partial-sum
+// buffer when a configuration needs more splits.
+int mixed_configure(ocn_ctx* c, const int cfg[6]) {
   MixedLR* m = c->mixed;
   if (!m) return set_err(c, OCN_ERR_STATE, "mixed-precision state missing");
-  if (cfg[0] < 1 || cfg[0] > m->max_stages || cfg[1] < 1 || cfg[2] < 1 || cfg[3] < 1 || cfg[4] < 0)
+  if (cfg[0] < 1 || cfg[0] > m->max_stages || cfg[1] < 1 || cfg[2] < 1 || cfg[3] < 1 || cfg[4] < 0 ||
+      (cfg[5] != 0 && cfg[5] != 128 && cfg[5] != 256 && cfg[5] != 512))
     return set_err(c, OCN_ERR_ARG, "bad tile configuration");
   TcParams& g1 = m->g1;
   TcParams& g2 = m->g2;
@@ -859,13 +861,13 @@ int mixed_configure(ocn_ctx* c, const int cfg[5]) {
   m->gm1.stages = m->gm2.stages = cfg[0];
   m->gridm1 = std::min(m->gm1.ntiles, std::min(cfg[2], c->sm_count));
   m->gridm2 = std::min(m->gm2.ntiles, std::min(cfg[3], c->sm_count));
-  for (int i = 0; i < 5; ++i) m->cfg[i] = cfg[i];
+  for (int i = 0; i < 6; ++i) m->cfg[i] = cfg[i];
   return OCN_OK;
 }
 
-int mixed_config(const ocn_ctx* c, int cfg[5]) {
+int mixed_config(const ocn_ctx* c, int cfg[6]) {
   if (!c->mixed) return OCN_ERR_STATE;
-  for (int i = 0; i < 5; ++i) cfg[i] = c->mixed->cfg[i];
+  for (int i = 0; i < 6; ++i) cfg[i] = c->mixed->cfg[i];
   return OCN_OK;
 }
 
@@ -874,7 +876,7 @@ int mixed_config(const ocn_ctx* c, int cfg[5]) {
 // one warm-up) and keeps the fastest.  Two rounds: pipeline depth 2..max x
 // GEMM2 K splits {1, 2, 4, 8, current} x persistent grids of all SMs or half,
 // then the k-mesh transforms per CTA {all, 4, 12} under the round-one winner.
-int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int best_cfg[5]) {
+int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int best_cfg[6]) {
   MixedLR* m = c->mixed;
   if (!m || !m->ready) return set_err(c, OCN_ERR_STATE, "mixed-precision operands not built");
   if (nv < 1 || nv > m->nvmax) return set_err(c, OCN_ERR_ARG, "block size exceeds nvec");
@@ -887,8 +889,8 @@ int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* curren
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  typedef std::array<int, 5> Cfg;
-  const Cfg def = {m->cfg[0], m->cfg[1], m->cfg[2], m->cfg[3], m->cfg[4]};
+  typedef std::array<int, 6> Cfg;
+  const Cfg def = {m->cfg[0], m->cfg[1], m->cfg[2], m->cfg[3], m->cfg[4], m->cfg[5]};
   double best = 1e300, dms = 0.0;
   Cfg bc = def;
   auto time_cfg = [&](const Cfg& a) -> int {
@@ -914,17 +916,20 @@ int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* curren
   for (int st = std::min(2, m->max_stages); st <= m->max_stages; ++st)
     for (int ks : {1, 2, 4, 8, def[1]})
       for (int gc : {c->sm_count, std::max(1, c->sm_count / 2)}) {
-        const Cfg a = {st, ks, gc, gc, def[4]};
+        const Cfg a = {st, ks, gc, gc, def[4], def[5]};
         if (std::find(cand.begin(), cand.end(), a) == cand.end()) cand.push_back(a);
       }
   for (size_t i = 0; i < cand.size() && rc == OCN_OK; ++i) rc = time_cfg(cand[i]);
   if (m->cube && rc == OCN_OK) {
     const Cfg r1 = bc;
-    for (int tc : {0, 4, 12}) {
-      Cfg a = r1;
-      a[4] = tc;
-      if (tc != r1[4] && rc == OCN_OK) rc = time_cfg(a);
-    }
+    for (int tc : {0, 4, 12})
+      for (int th : {128, 256, 512}) {
+        Cfg a = r1;
+        a[4] = tc;
+        a[5] = th;
+        const bool same = (tc == r1[4]) && (th == (r1[5] ? r1[5] : 128));
+        if (!same && rc == OCN_OK) rc = time_cfg(a);
+      }
   }
   const int rf = mixed_configure(c, rc ? def.data() : bc.data());
   cudaEventDestroy(e0);
@@ -935,7 +940,7 @@ int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* curren
   if (best_ms) *best_ms = best;
   if (current_ms) *current_ms = dms;
   if (best_cfg)
-    for (int i = 0; i < 5; ++i) best_cfg[i] = bc[i];
+    for (int i = 0; i < 6; ++i) best_cfg[i] = bc[i];
   return OCN_OK;
 }
 
@@ -1120,8 +1125,9 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
       const int tc = (m->cfg[4] > 0 && ntot % m->cfg[4] == 0) ? m->cfg[4] : ntot;
       CubeFnF f;
       OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], tc, f);
-      f<<<dim3(nx, ntot / tc), 128, kmesh_cube_smem<float>(c->dims.kmesh[0], tc), c->stream>>>(m->phi, m->Wf, nx,
-                                                                                              tc, ntot, m->twf);
+      const int th = m->cfg[5] ? m->cfg[5] : 128;
+      f<<<dim3(nx, ntot / tc), th, kmesh_cube_smem<float>(c->dims.kmesh[0], tc), c->stream>>>(m->phi, m->Wf, nx, tc,
+                                                                                             ntot, m->twf);
     } else {
       const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na * nv);
       k_lr_fft_w_f32<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g, m->twf);

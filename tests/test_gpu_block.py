@@ -160,7 +160,7 @@ def test_autotune_and_tilings_keep_the_action(built):
     try:
         default = ctx.tiles()
         base_r, base_i = ctx.apply_H_block(pr, pi)
-        for tiles in [(2, 1, 152, 152, 0), (3, 4, 76, 76, 4), (default[0], 8, 152, 76, 0)]:
+        for tiles in [(2, 1, 152, 152, 0, 0), (3, 4, 76, 76, 4, 256), (default[0], 8, 152, 76, 0, 512)]:
             ctx.set_tiles(tiles)
             assert ctx.tiles() == tiles
             r, i = ctx.apply_H_block(pr, pi)
@@ -172,7 +172,7 @@ def test_autotune_and_tilings_keep_the_action(built):
             orr, oi = P.xact(pr[v], pi[v])
             assert _rel(r[v] + 1j * i[v], orr + 1j * oi) < 1e-4
         with pytest.raises(capi.OcnError) as e:
-            ctx.set_tiles((0, 1, 1, 1, 0))
+            ctx.set_tiles((0, 1, 1, 1, 0, 0))
         assert e.value.code == capi.OCN_ERR_ARG
         # the Haydock graph is rebuilt for the new tiling
         ra, ia, rb, done = ctx.haydock_block(9, pr / np.linalg.norm(pr[0] + 1j * pi[0]),
