@@ -12,6 +12,7 @@
 #define OCN_MAX_NA 12       // 4*(2*l_c+1) for l_c <= 1 (1s, 2p edges)
 #define OCN_MAX_KDIM 32     // largest k-mesh extent along one axis handled by the FFT kernels
 #define OCN_MAX_NK 4096     // largest k-mesh size (shared-memory FFT)
+#define LZ_THREADS 256      // threads of the Lanczos-step kernels
 
 namespace ocn {
 

@@ -215,8 +215,9 @@ __global__ void k_lr_gemm2_fp64(const double2* __restrict__ u, const double2* __
 //             + sum_jc S(ic,jc) psi(n,k,jc)        (OCEAN_action.f90:337-372,596-608)
 // Optionally fused with the first Lanczos stage (ocean_hay_ab_twoterm,
 // OCEAN_haydock.f90:848-860): out -= b_{i-1} old, partial <out|psi>.
-template <int NA>
-__global__ void k_combine(const double* __restrict__ pr, const double* __restrict__ pi,
+template <int NA, bool SO>
+__global__ void __launch_bounds__(LZ_THREADS)
+    k_combine(const double* __restrict__ pr, const double* __restrict__ pi,
                           const double* __restrict__ er, const double* __restrict__ ei,
                           const double* __restrict__ allow, const double* __restrict__ acc,
                           const double* __restrict__ part, int nparts, const double2* __restrict__ so,
@@ -265,7 +266,7 @@ __global__ void k_combine(const double* __restrict__ pr, const double* __restric
       const double m = allow[idx];
       fr *= m;
       fi *= m;
-      if (use_so) {
+      if (SO) {  // spin-orbit (use_so selects the instantiation)
 #pragma unroll
         for (int jc = 0; jc < NA; ++jc) {
           const double2 sv = so[jc * NA + ic];
@@ -381,7 +382,7 @@ __device__ __forceinline__ void block_partial(double v0, double v1, double* __re
 __global__ void k_advance(int* __restrict__ itp) { *itp += 1; }
 
 // Lanczos stage 2: a_{i-1} = Re<h|psi>; h -= a psi; partial |h|^2.
-__global__ void k_lanczos2(const double* __restrict__ red1, int nblk, double* __restrict__ hr,
+__global__ void __launch_bounds__(LZ_THREADS) k_lanczos2(const double* __restrict__ red1, int nblk, double* __restrict__ hr,
                            double* __restrict__ hi, const double* __restrict__ pr,
                            const double* __restrict__ pi, size_t n, double* __restrict__ red2,
                            double* __restrict__ ra_base, double* __restrict__ ia_base,
@@ -417,7 +418,7 @@ __global__ void k_lanczos2(const double* __restrict__ red1, int nblk, double* __
 }
 
 // Lanczos stage 3: b_i = sqrt(sum); psi_new = h / b_i (in place in h).
-__global__ void k_lanczos3(const double* __restrict__ red2, int nblk, double* __restrict__ hr,
+__global__ void __launch_bounds__(LZ_THREADS) k_lanczos3(const double* __restrict__ red2, int nblk, double* __restrict__ hr,
                            double* __restrict__ hi, size_t n, double* __restrict__ rb_base,
                            const int* __restrict__ itp, const BlockStrides bs) {
   const size_t v = blockIdx.y;
@@ -765,6 +766,12 @@ __global__ void k_update(int nvec, const double2* __restrict__ coef, const doubl
   }
 }
 
+typedef decltype(&k_combine<4, false>) CombineFn;
+CombineFn combine_kernel(int na, int use_so) {
+  if (na == 4) return use_so ? k_combine<4, true> : k_combine<4, false>;
+  return use_so ? k_combine<12, true> : k_combine<12, false>;
+}
+
 inline int grid_for(size_t n, int block, int cap) {
   size_t g = (n + block - 1) / block;
   if (g > (size_t)cap) g = cap;
@@ -967,9 +974,9 @@ int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* 
   int nparts;
   active_parts(c, hflag, &parts, &nparts);
   const BlockStrides bs = {vstride, c->part_stride, 0, 0};
-  auto kern = (c->na == 4) ? k_combine<4> : k_combine<12>;
-  dim3 grid(grid_for(nbk, 256, 4 * c->sm_count), nv);
-  kern<<<grid, 256, 0, c->stream>>>(
+  auto kern = combine_kernel(c->na, use_so);
+  dim3 grid(grid_for(nbk, LZ_THREADS, 4 * c->sm_count), nv);
+  kern<<<grid, LZ_THREADS, 0, c->stream>>>(
       d_pr, d_pi, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow,
       c->acc_valid ? c->d_acc : nullptr, parts, nparts,
       c->d_so, d_or, d_oi, nbk, c->na, c->npsi, c->sys.e0, use_so, backwards, nullptr, nullptr,
@@ -996,20 +1003,20 @@ int lanczos_launch(ocn_ctx* c, int nv, const double* old, const double* psi, dou
   const BlockStrides bs = {2 * n, c->part_stride, cstride, (size_t)4 * nblk};
   TimedScope ts(c, T_LANCZOS);
   dim3 grid(nblk, nv);
-  auto kern = (c->na == 4) ? k_combine<4> : k_combine<12>;
-  kern<<<grid, 256, 0, c->stream>>>(psi, psi + n, c->d_er, c->ei_nonzero ? c->d_ei : nullptr,
+  auto kern = combine_kernel(c->na, use_so);
+  kern<<<grid, LZ_THREADS, 0, c->stream>>>(psi, psi + n, c->d_er, c->ei_nonzero ? c->d_ei : nullptr,
                                     c->d_allow, c->acc_valid ? c->d_acc : nullptr, parts,
                                     nparts, c->d_so, h, h + n, nbk, c->na, n, c->sys.e0, use_so, 0,
                                     old, old + n, rb, itp, c->d_red, bs);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
-  k_lanczos2<<<grid, 256, 0, c->stream>>>(c->d_red, nblk, h, h + n, psi, psi + n, n, c->d_red + 2 * nblk,
+  k_lanczos2<<<grid, LZ_THREADS, 0, c->stream>>>(c->d_red, nblk, h, h + n, psi, psi + n, n, c->d_red + 2 * nblk,
                                           ra, ia, itp, bs);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   if (c->dims.precision == OCN_PREC_MIXED && c->mixed)  // also builds the next psi operand
     return mixed_norm_prep(c, nv, c->d_red + 2 * nblk, nblk, bs.red, h, rb, cstride, itp);
-  k_lanczos3<<<grid, 256, 0, c->stream>>>(c->d_red + 2 * nblk, nblk, h, h + n, n, rb, itp, bs);
+  k_lanczos3<<<grid, LZ_THREADS, 0, c->stream>>>(c->d_red + 2 * nblk, nblk, h, h + n, n, rb, itp, bs);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;

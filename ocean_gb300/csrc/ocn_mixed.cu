@@ -546,7 +546,7 @@ __global__ void k_prep_b3(const double2* __restrict__ hamp, __nv_bfloat16* __res
 // blockIdx.y, b_i = sqrt(sum of partials), psi = h / b_i written in place, and
 // B1 rows of vector v built from allow o psi.  One thread per (n, k) covers
 // both K = n and K = Nb + n for every alpha.
-__global__ void k_norm_prep(const double* __restrict__ red2, int nblk, size_t rstride,
+__global__ void __launch_bounds__(LZ_THREADS) k_norm_prep(const double* __restrict__ red2, int nblk, size_t rstride,
                             double* __restrict__ hbase, size_t vstride, size_t npsi,
                             const double* __restrict__ allow, __nv_bfloat16* __restrict__ b1, int nb,
                             int nk, int na, int ncol, int p1, double* __restrict__ rb_base,
@@ -1082,7 +1082,7 @@ int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rst
                     double* rb, size_t cstride, const int* itp) {
   MixedLR* m = c->mixed;  // timed as part of the enclosing Lanczos step
   dim3 grid(nblk, nv);
-  k_norm_prep<<<grid, 256, 0, c->stream>>>(red2, nblk, rstride, h, 2 * c->npsi, c->npsi, c->d_allow, m->b1,
+  k_norm_prep<<<grid, LZ_THREADS, 0, c->stream>>>(red2, nblk, rstride, h, 2 * c->npsi, c->npsi, c->d_allow, m->b1,
                                            c->nb, c->nk, c->na, m->ncol, m->p1, rb, cstride, itp);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
