@@ -244,64 +244,63 @@ __global__ void __launch_bounds__(LZ_THREADS)
   double dr = 0.0, di = 0.0;
   double bm = 0.0;
   if (oldr) bm = -rb_base[*itp - 1];  // b_{i-1}
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nbk; e += gridDim.x * blockDim.x) {
-    double qr[NA], qi[NA];
-#pragma unroll
-    for (int a = 0; a < NA; ++a) {
-      qr[a] = pr[e + (size_t)nbk * a];
-      qi[a] = pi[e + (size_t)nbk * a];
+  // one thread per psi element idx = e + Nb*Nk*ic: the spin-orbit sum reads the
+  // other channels of the same (n, k), which neighbouring threads also load
+  const size_t nall = (size_t)nbk * NA;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < nall;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int ic = (int)(idx / (size_t)nbk);
+    const size_t e = idx - (size_t)ic * nbk;
+    const double qrc = pr[idx], qic = pi[idx];
+    double fr = 0.0, fi = 0.0;
+    if (acc) {
+      fr = acc[idx];
+      fi = acc[npsi + idx];
     }
+    for (int s = 0; s < nparts; ++s) {
+      fr += part[(size_t)s * bs.part + idx];
+      fi += part[(size_t)s * bs.part + npsi + idx];
+    }
+    const double m = allow[idx];
+    fr *= m;
+    fi *= m;
+    if (SO) {  // spin-orbit (use_so selects the instantiation)
 #pragma unroll
-    for (int ic = 0; ic < NA; ++ic) {
-      const size_t idx = e + (size_t)nbk * ic;
-      double fr = 0.0, fi = 0.0;
-      if (acc) {
-        fr = acc[idx];
-        fi = acc[npsi + idx];
-      }
-      for (int s = 0; s < nparts; ++s) {
-        fr += part[(size_t)s * bs.part + idx];
-        fi += part[(size_t)s * bs.part + npsi + idx];
-      }
-      const double m = allow[idx];
-      fr *= m;
-      fi *= m;
-      if (SO) {  // spin-orbit (use_so selects the instantiation)
-#pragma unroll
-        for (int jc = 0; jc < NA; ++jc) {
-          const double2 sv = so[jc * NA + ic];
-          if (backwards) {
-            fr = fr + sv.x * qr[jc] + sv.y * qi[jc];
-            fi = fi + sv.x * qi[jc] - sv.y * qr[jc];
-          } else {
-            fr = fr + sv.x * qr[jc] - sv.y * qi[jc];
-            fi = fi + sv.x * qi[jc] + sv.y * qr[jc];
-          }
-        }
-      }
-      double hr = 0.0, hi = 0.0;
-      if (use_e0) {
-        const double a_ = er[idx], b_ = ei ? ei[idx] : 0.0;
+      for (int jc = 0; jc < NA; ++jc) {
+        const double2 sv = so[jc * NA + ic];
+        const size_t j = e + (size_t)nbk * jc;
+        const double qr = pr[j], qi = pi[j];
         if (backwards) {
-          hr = a_ * qr[ic] + b_ * qi[ic];
-          hi = a_ * qi[ic] - b_ * qr[ic];
+          fr = fr + sv.x * qr + sv.y * qi;
+          fi = fi + sv.x * qi - sv.y * qr;
         } else {
-          hr = a_ * qr[ic] - b_ * qi[ic];
-          hi = a_ * qi[ic] + b_ * qr[ic];
+          fr = fr + sv.x * qr - sv.y * qi;
+          fi = fi + sv.x * qi + sv.y * qr;
         }
       }
-      hr += fr;
-      hi += fi;
-      if (oldr) {
-        hr += bm * oldr[idx];
-        hi += bm * oldi[idx];
-        // psi_dot(hpsi, psi): sum conj(h) psi  (OCEAN_psi.f90:2029-2034)
-        dr += hr * qr[ic] + hi * qi[ic];
-        di += hr * qi[ic] - hi * qr[ic];
-      }
-      outr[idx] = hr;
-      outi[idx] = hi;
     }
+    double hr = 0.0, hi = 0.0;
+    if (use_e0) {
+      const double a_ = er[idx], b_ = ei ? ei[idx] : 0.0;
+      if (backwards) {
+        hr = a_ * qrc + b_ * qic;
+        hi = a_ * qic - b_ * qrc;
+      } else {
+        hr = a_ * qrc - b_ * qic;
+        hi = a_ * qic + b_ * qrc;
+      }
+    }
+    hr += fr;
+    hi += fi;
+    if (oldr) {
+      hr += bm * oldr[idx];
+      hi += bm * oldi[idx];
+      // psi_dot(hpsi, psi): sum conj(h) psi  (OCEAN_psi.f90:2029-2034)
+      dr += hr * qrc + hi * qic;
+      di += hr * qic - hi * qrc;
+    }
+    outr[idx] = hr;
+    outi[idx] = hi;
   }
   if (!red) return;
   // deterministic block reduction
@@ -975,7 +974,7 @@ int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* 
   active_parts(c, hflag, &parts, &nparts);
   const BlockStrides bs = {vstride, c->part_stride, 0, 0};
   auto kern = combine_kernel(c->na, use_so);
-  dim3 grid(grid_for(nbk, LZ_THREADS, 4 * c->sm_count), nv);
+  dim3 grid(grid_for(c->npsi, LZ_THREADS, 4 * c->sm_count), nv);
   kern<<<grid, LZ_THREADS, 0, c->stream>>>(
       d_pr, d_pi, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow,
       c->acc_valid ? c->d_acc : nullptr, parts, nparts,

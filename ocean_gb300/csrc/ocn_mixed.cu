@@ -500,21 +500,34 @@ __global__ void k_build_mb(const double2* __restrict__ mpc, __nv_bfloat16* __res
   }
 }
 
-// amp[v][p][a] = sum_k amp_part[k][p][v*Na + a], summed in FP64
+// amp[v][p][a] = sum_k amp_part[k][p][v*Na + a], summed in FP64: a CTA owns
+// 32 consecutive (p, t) outputs (coalesced along t) and its 8 warps split the
+// k range (warp w takes k = w, w+8, ...); the 8 partials are added in order.
 __global__ void k_amp_reduce_f32(const float2* __restrict__ part, double2* __restrict__ amp, int nk, int np,
                                  int na, int nv) {
+  __shared__ double2 sh[8][32];
   const int nt = na * nv;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= np * nt) return;
-  const int p = i / nt, t = i % nt;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lane;
   double sr = 0.0, si = 0.0;
-  for (int k = 0; k < nk; ++k) {
-    const float2 f = part[((size_t)k * np + p) * nt + t];
-    sr += (double)f.x;
-    si += (double)f.y;
+  if (i < np * nt)
+    for (int k = w; k < nk; k += 8) {
+      const float2 f = part[(size_t)k * np * nt + i];
+      sr += (double)f.x;
+      si += (double)f.y;
+    }
+  sh[w][lane] = make_double2(sr, si);
+  __syncthreads();
+  if (w == 0 && i < np * nt) {
+    double tr = 0.0, ti = 0.0;
+    for (int g = 0; g < 8; ++g) {
+      tr += sh[g][lane].x;
+      ti += sh[g][lane].y;
+    }
+    const int p = i / nt, t = i % nt;
+    const int v = t / na, a = t % na;
+    amp[((size_t)v * np + p) * na + a] = make_double2(tr, ti);
   }
-  const int v = t / na, a = t % na;
-  amp[((size_t)v * np + p) * na + a] = make_double2(sr, si);
 }
 
 // B3[v*4Na + j][K3] from h = -hamp[v][p][a] (the x->band epilogue negates):
@@ -1024,7 +1037,7 @@ int mult_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t 
   a.nv = nv;
   b.nv = nv;
   k_lr_tc<<<m->gridm1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ma_hi, m->tm_ma_lo, m->tm_b1, a);
-  k_amp_reduce_f32<<<(np * na * nv + 127) / 128, 128, 0, c->stream>>>(m->amp_part, m->amp, c->nk, np, na, nv);
+  k_amp_reduce_f32<<<(np * na * nv + 31) / 32, 256, 0, c->stream>>>(m->amp_part, m->amp, c->nk, np, na, nv);
   c->launches += 2;
   OCN_CUDA(c, cudaGetLastError());
   for (int v = 0; v < nv; ++v)
