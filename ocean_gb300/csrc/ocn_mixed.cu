@@ -71,6 +71,8 @@ struct TcParams {
   size_t npsi;
   int* err;
   int bshared;   // B operand has one k slice shared by every k (multiplet back-projection)
+  int koff;      // added to k for the A operand: spin s of a spin-polarised problem at s*Nk
+  int spin;      // -1: write every alpha; 0/1: only alpha with alpha mod 2 == spin
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
@@ -242,8 +244,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           }
           const uint32_t sbase = su32(smem + stage * stage_bytes);
           mbar_expect_tx(full0 + 8 * stage, stage_bytes);
-          tma_load_3d(sbase, &tm_hi, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k);
-          tma_load_3d(sbase + a_bytes, &tm_lo, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k);
+          tma_load_3d(sbase, &tm_hi, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + p.koff);
+          tma_load_3d(sbase + a_bytes, &tm_lo, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + p.koff);
           tma_load_3d(sbase + 2 * a_bytes, &tm_b, full0 + 8 * stage, c * TC_BK, 0, p.bshared ? 0 : ti.k);
           armed_phase[stage] = (int)phase;
           if (++stage == (uint32_t)S) {
@@ -340,7 +342,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           if (x < p.nx) {
             float2* o = p.phi + ((size_t)ti.k * p.nx + x) * (p.nv * na) + vv * na;
             for (int a = 0; a < na; ++a)
-              o[a] = make_float2(v[a] + v[2 * na + a], v[na + a] + v[3 * na + a]);
+              if (p.spin < 0 || (a & 1) == p.spin)
+                o[a] = make_float2(v[a] + v[2 * na + a], v[na + a] + v[3 * na + a]);
           }
         } else {
           const int n = ti.row0 + row;
@@ -348,6 +351,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             double* pr = p.part + ((size_t)ti.sp * p.nvmax + vv) * 2 * p.npsi;
             double* pim = pr + p.npsi;
             for (int a = 0; a < na; ++a) {
+              if (p.spin >= 0 && (a & 1) != p.spin) continue;
               const size_t idx = (size_t)n + (size_t)p.nb * ((size_t)ti.k + (size_t)p.nk * a);
               pr[idx] = -((double)v[a] + (double)v[2 * na + a]);
               pim[idx] = -((double)v[na + a] + (double)v[3 * na + a]);
@@ -736,8 +740,8 @@ int alloc(ocn_ctx* c, T** p, size_t n) {
 }  // namespace
 
 int mixed_init(ocn_ctx* c) {
-  if (c->nspn != 1) return set_err(c, OCN_ERR_UNSUPPORTED, "mixed precision requires nspn = 1");
-  const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na, nvmax = c->nvec;
+  if (c->nspn != 1 && c->nspn != 2) return set_err(c, OCN_ERR_UNSUPPORTED, "nspn must be 1 or 2");
+  const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na, nvmax = c->nvec, ns = c->nspn;
   const int ncol = 4 * na * nvmax;
   if (ncol > TC_MAX_NCOL)
     return set_err(c, OCN_ERR_ARG, "nvec too large: 4*nalpha*nvec must be <= 256");
@@ -754,8 +758,11 @@ int mixed_init(ocn_ctx* c) {
   m->p1 = (2 * nb + 7) / 8 * 8;
   m->p2 = (2 * nx + 7) / 8 * 8;
   int rc;
-  if ((rc = alloc(c, &m->ua_hi, (size_t)nk * nx * m->p1)) || (rc = alloc(c, &m->ua_lo, (size_t)nk * nx * m->p1)) ||
-      (rc = alloc(c, &m->ub_hi, (size_t)nk * nb * m->p2)) || (rc = alloc(c, &m->ub_lo, (size_t)nk * nb * m->p2)) ||
+  // u2 operands of both valence spins, spin-major: spin s at outer index s*Nk + k
+  if ((rc = alloc(c, &m->ua_hi, (size_t)ns * nk * nx * m->p1)) ||
+      (rc = alloc(c, &m->ua_lo, (size_t)ns * nk * nx * m->p1)) ||
+      (rc = alloc(c, &m->ub_hi, (size_t)ns * nk * nb * m->p2)) ||
+      (rc = alloc(c, &m->ub_lo, (size_t)ns * nk * nb * m->p2)) ||
       (rc = alloc(c, &m->b1, (size_t)nk * ncol * m->p1)) || (rc = alloc(c, &m->b2, (size_t)nk * ncol * m->p2)) ||
       (rc = alloc(c, &m->phi, (size_t)nk * nx * na * nvmax)) || (rc = alloc(c, &m->Wf, (size_t)nk * nx)) ||
       (rc = alloc(c, &m->d_err, 1)))
@@ -770,11 +777,11 @@ int mixed_init(ocn_ctx* c) {
   cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fnp, 12000, cudaEnableDefault, &q);
   if (e != cudaSuccess || !fnp) return set_err(c, OCN_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
   EncodeTiledFn fn = reinterpret_cast<EncodeTiledFn>(fnp);
-  if ((rc = encode3d(c, fn, &m->tm_ua_hi, m->ua_hi, 2 * nb, nx, nk, m->p1, TC_BM)) ||
-      (rc = encode3d(c, fn, &m->tm_ua_lo, m->ua_lo, 2 * nb, nx, nk, m->p1, TC_BM)) ||
+  if ((rc = encode3d(c, fn, &m->tm_ua_hi, m->ua_hi, 2 * nb, nx, (uint64_t)ns * nk, m->p1, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_ua_lo, m->ua_lo, 2 * nb, nx, (uint64_t)ns * nk, m->p1, TC_BM)) ||
       (rc = encode3d(c, fn, &m->tm_b1, m->b1, 2 * nb, ncol, nk, m->p1, ncol)) ||
-      (rc = encode3d(c, fn, &m->tm_ub_hi, m->ub_hi, 2 * nx, nb, nk, m->p2, TC_BM)) ||
-      (rc = encode3d(c, fn, &m->tm_ub_lo, m->ub_lo, 2 * nx, nb, nk, m->p2, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_ub_hi, m->ub_hi, 2 * nx, nb, (uint64_t)ns * nk, m->p2, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_ub_lo, m->ub_lo, 2 * nx, nb, (uint64_t)ns * nk, m->p2, TC_BM)) ||
       (rc = encode3d(c, fn, &m->tm_b2, m->b2, 2 * nx, ncol, nk, m->p2, ncol)))
     return rc;
 
@@ -799,6 +806,9 @@ int mixed_init(ocn_ctx* c) {
   g1.phi = m->phi;
   g1.err = m->d_err;
   g1.npsi = c->npsi;
+  g1.bshared = 0;
+  g1.koff = 0;
+  g1.spin = -1;  // set per launch on spin-polarised problems
   TcParams& g2 = m->g2;
   g2 = g1;
   g2.mode = 2;
@@ -958,7 +968,8 @@ int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* curren
 }
 
 // Split-BF16 operands and tiling of the multiplet projector contractions, from
-// the projector coefficients of ocn_set_mult (c->mult.mpc, nspn = 1).
+// the projector coefficients of ocn_set_mult (c->mult.mpc [s][p][k*Nb + n]; the
+// operands of both spins are stored spin-major, spin s at outer index s*Nk + k).
 int mixed_set_mult(ocn_ctx* c) {
   MixedLR* m = c->mixed;
   if (!m) return OCN_OK;
@@ -976,27 +987,34 @@ int mixed_set_mult(ocn_ctx* c) {
   m->np = np;
   m->p3 = (2 * np + 7) / 8 * 8;
   int rc;
-  if ((rc = alloc(c, &m->ma_hi, (size_t)nk * np * m->p1)) || (rc = alloc(c, &m->ma_lo, (size_t)nk * np * m->p1)) ||
-      (rc = alloc(c, &m->mb_hi, (size_t)nk * nb * m->p3)) || (rc = alloc(c, &m->mb_lo, (size_t)nk * nb * m->p3)) ||
+  const int ns = c->nspn;
+  if ((rc = alloc(c, &m->ma_hi, (size_t)ns * nk * np * m->p1)) ||
+      (rc = alloc(c, &m->ma_lo, (size_t)ns * nk * np * m->p1)) ||
+      (rc = alloc(c, &m->mb_hi, (size_t)ns * nk * nb * m->p3)) ||
+      (rc = alloc(c, &m->mb_lo, (size_t)ns * nk * nb * m->p3)) ||
       (rc = alloc(c, &m->b3, (size_t)m->ncol * m->p3)) ||
       (rc = alloc(c, &m->amp_part, (size_t)nk * np * na * nvmax)) ||
       (rc = alloc(c, &m->amp, (size_t)nvmax * np * na)) || (rc = alloc(c, &m->hamp, (size_t)nvmax * np * na)))
     return rc;
   OCN_CUDA(c, cudaMemsetAsync(m->b3, 0, (size_t)m->ncol * m->p3 * 2, c->stream));
   const int grid = 8 * c->sm_count;
-  k_build_ma<<<grid, 256, 0, c->stream>>>(d.mpc, m->ma_hi, m->ma_lo, nb, nk, np, m->p1);
-  k_build_mb<<<grid, 256, 0, c->stream>>>(d.mpc, m->mb_hi, m->mb_lo, nb, nk, np, m->p3);
-  c->launches += 2;
+  for (int s = 0; s < ns; ++s) {
+    const double2* ms = d.mpc + (size_t)s * np * nb * nk;
+    const size_t oa = (size_t)s * nk * np * m->p1, ob = (size_t)s * nk * nb * m->p3;
+    k_build_ma<<<grid, 256, 0, c->stream>>>(ms, m->ma_hi + oa, m->ma_lo + oa, nb, nk, np, m->p1);
+    k_build_mb<<<grid, 256, 0, c->stream>>>(ms, m->mb_hi + ob, m->mb_lo + ob, nb, nk, np, m->p3);
+    c->launches += 2;
+  }
   OCN_CUDA(c, cudaGetLastError());
   void* fnp = nullptr;
   cudaDriverEntryPointQueryResult q;
   cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fnp, 12000, cudaEnableDefault, &q);
   if (e != cudaSuccess || !fnp) return set_err(c, OCN_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
   EncodeTiledFn fn = reinterpret_cast<EncodeTiledFn>(fnp);
-  if ((rc = encode3d(c, fn, &m->tm_ma_hi, m->ma_hi, 2 * nb, np, nk, m->p1, TC_BM)) ||
-      (rc = encode3d(c, fn, &m->tm_ma_lo, m->ma_lo, 2 * nb, np, nk, m->p1, TC_BM)) ||
-      (rc = encode3d(c, fn, &m->tm_mb_hi, m->mb_hi, 2 * np, nb, nk, m->p3, TC_BM)) ||
-      (rc = encode3d(c, fn, &m->tm_mb_lo, m->mb_lo, 2 * np, nb, nk, m->p3, TC_BM)) ||
+  if ((rc = encode3d(c, fn, &m->tm_ma_hi, m->ma_hi, 2 * nb, np, (uint64_t)ns * nk, m->p1, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_ma_lo, m->ma_lo, 2 * nb, np, (uint64_t)ns * nk, m->p1, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_mb_hi, m->mb_hi, 2 * np, nb, (uint64_t)ns * nk, m->p3, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_mb_lo, m->mb_lo, 2 * np, nb, (uint64_t)ns * nk, m->p3, TC_BM)) ||
       (rc = encode3d(c, fn, &m->tm_b3, m->b3, 2 * np, m->ncol, 1, m->p3, m->ncol)))
     return rc;
   TcParams& a = m->gm1;  // amplitudes: band->x form with Np rows per k
@@ -1036,15 +1054,26 @@ int mult_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t 
   TcParams a = m->gm1, b = m->gm2;
   a.nv = nv;
   b.nv = nv;
-  k_lr_tc<<<m->gridm1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ma_hi, m->tm_ma_lo, m->tm_b1, a);
+  const int ns = c->nspn;  // spin-polarised: per spin, each launch writes its own alphas
+  for (int s = 0; s < ns; ++s) {
+    a.koff = s * c->nk;
+    a.spin = ns == 2 ? s : -1;
+    k_lr_tc<<<m->gridm1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ma_hi, m->tm_ma_lo, m->tm_b1, a);
+    ++c->launches;
+  }
   k_amp_reduce_f32<<<(np * na * nv + 31) / 32, 256, 0, c->stream>>>(m->amp_part, m->amp, c->nk, np, na, nv);
-  c->launches += 2;
+  ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   for (int v = 0; v < nv; ++v)
     if ((rc = mult_hamp(c, m->amp + (size_t)v * np * na, m->hamp + (size_t)v * np * na))) return rc;
   k_prep_b3<<<(nv * np * na + 127) / 128, 128, 0, c->stream>>>(m->hamp, m->b3, np, na, nv, m->p3);
-  k_lr_tc<<<m->gridm2, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_mb_hi, m->tm_mb_lo, m->tm_b3, b);
-  c->launches += 2;
+  ++c->launches;
+  for (int s = 0; s < ns; ++s) {
+    b.koff = s * c->nk;
+    b.spin = ns == 2 ? s : -1;
+    k_lr_tc<<<m->gridm2, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_mb_hi, m->tm_mb_lo, m->tm_b3, b);
+    ++c->launches;
+  }
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;
 }
@@ -1067,13 +1096,18 @@ int mixed_set_bloch(ocn_ctx* c) {
   if (!m) return set_err(c, OCN_ERR_STATE, "mixed state missing");
   const int nb = c->nb, nk = c->nk, nx = c->nx;
   const int grid = 8 * c->sm_count;
-  k_build_ua<<<grid, 256, 0, c->stream>>>(c->d_u, m->ua_hi, m->ua_lo, nb, nk, nx, m->p1);
-  OCN_CUDA(c, cudaGetLastError());
-  k_build_ub<<<grid, 256, 0, c->stream>>>(c->d_u, m->ub_hi, m->ub_lo, nb, nk, nx, m->p2);
-  OCN_CUDA(c, cudaGetLastError());
+  for (int s = 0; s < c->nspn; ++s) {  // u [s][x][k][n] -> spin-major operands
+    const size_t us = (size_t)s * nx * nk * nb;
+    const size_t oa = (size_t)s * nk * nx * m->p1, ob = (size_t)s * nk * nb * m->p2;
+    k_build_ua<<<grid, 256, 0, c->stream>>>(c->d_u + us, m->ua_hi + oa, m->ua_lo + oa, nb, nk, nx, m->p1);
+    OCN_CUDA(c, cudaGetLastError());
+    k_build_ub<<<grid, 256, 0, c->stream>>>(c->d_u + us, m->ub_hi + ob, m->ub_lo + ob, nb, nk, nx, m->p2);
+    OCN_CUDA(c, cudaGetLastError());
+    c->launches += 2;
+  }
   k_w_to_f32<<<grid, 256, 0, c->stream>>>(c->d_W, m->Wf, (size_t)nk * nx);
   OCN_CUDA(c, cudaGetLastError());
-  c->launches += 3;
+  c->launches += 1;
   OCN_CUDA(c, cudaStreamSynchronize(c->stream));
   m->ready = true;
   return OCN_OK;
@@ -1124,11 +1158,16 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
   TcParams g1 = m->g1, g2 = m->g2;
   g1.nv = nv;
   g2.nv = nv;
+  const int ns = c->nspn;  // spin-polarised: one launch per valence spin, each writes its own alphas
   {
     TimedScope ts(c, T_LR_GEMM1);
-    k_lr_tc<<<m->grid1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ua_hi, m->tm_ua_lo, m->tm_b1, g1);
-    ++c->launches;
-    OCN_CUDA(c, cudaGetLastError());
+    for (int s = 0; s < ns; ++s) {
+      g1.koff = s * nk;
+      g1.spin = ns == 2 ? s : -1;
+      k_lr_tc<<<m->grid1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ua_hi, m->tm_ua_lo, m->tm_b1, g1);
+      ++c->launches;
+      OCN_CUDA(c, cudaGetLastError());
+    }
   }
   {
     TimedScope ts(c, T_LR_FFT);
@@ -1158,9 +1197,13 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
   }
   {
     TimedScope ts(c, T_LR_GEMM2);
-    k_lr_tc<<<m->grid2, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ub_hi, m->tm_ub_lo, m->tm_b2, g2);
-    ++c->launches;
-    OCN_CUDA(c, cudaGetLastError());
+    for (int s = 0; s < ns; ++s) {
+      g2.koff = s * nk;
+      g2.spin = ns == 2 ? s : -1;
+      k_lr_tc<<<m->grid2, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ub_hi, m->tm_ub_lo, m->tm_b2, g2);
+      ++c->launches;
+      OCN_CUDA(c, cudaGetLastError());
+    }
   }
   return OCN_OK;
 }

@@ -165,9 +165,10 @@ def batch_instance(i: int, u2_device: Optional[str] = None) -> "Workload":
 
 def make(name: str, seed: int = 0, nb: Optional[int] = None, kmesh=None, xmesh=None,
          core_l: Optional[int] = None, with_mult: Optional[bool] = None,
-         u2_device: Optional[str] = None) -> Workload:
+         u2_device: Optional[str] = None, nspn: int = 1) -> Workload:
     """Build a named workload: 'c1', 'c2', 'c3', 'c5', 'batch' (shape given by the
-    caller), or 'tiny' (test sizes).  u2_device: draw u2 on that torch device."""
+    caller), or 'tiny' (test sizes).  u2_device: draw u2 on that torch device;
+    nspn = 2 gives spin-polarised Bloch functions (valence spin = alpha mod 2)."""
     presets = {
         "tiny": dict(nb=8, kmesh=(2, 2, 2), xmesh=(3, 3, 3), core_l=0, mult=False, niter=24),
         "small": dict(nb=12, kmesh=(3, 2, 2), xmesh=(4, 3, 2), core_l=0, mult=False, niter=40),
@@ -199,7 +200,8 @@ def make(name: str, seed: int = 0, nb: Optional[int] = None, kmesh=None, xmesh=N
     rng = np.random.Generator(np.random.PCG64(seed))
     nbv, km, xm, lc = p["nb"], tuple(p["kmesh"]), tuple(p["xmesh"]), p["core_l"]
     na = 4 * (2 * lc + 1)
-    nspn = 1
+    if nspn not in (1, 2):
+        raise ValueError("nspn must be 1 or 2")
     nk, nx = int(np.prod(km)), int(np.prod(xm))
     a_bohr = 4.0 / BOHR
     avec = np.zeros(9)

@@ -301,3 +301,46 @@ def test_multiplet_mixed_tensor_core_term(built, name):
         assert _rel(got, ref) < 2e-4
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("name", ["tiny", "small", "c3small"])
+def test_spin_polarised_fp64_matches_oracle(built, name):
+    """nspn = 2: every term picks the Bloch functions / projectors of the
+    valence spin alpha mod 2 (long_range.f90:788-801, OCEAN_multiplet.f90)."""
+    _, O = built
+    w, P = problem(name, O, seed=11, nspn=2)
+    rng = np.random.default_rng(3)
+    pr, pi = rng.standard_normal(w.npsi), rng.standard_normal(w.npsi)
+    ctx = capi.Context(w)
+    try:
+        hr, hi = ctx.apply_H(pr, pi)
+        ra, ia, rb, done = ctx.haydock(20)
+    finally:
+        ctx.close()
+    orr, oi = P.xact(pr, pi)
+    assert _rel(hr + 1j * hi, orr + 1j * oi) < 1e-12
+    rc, ora, oia, orb, _ = P.haydock(20)
+    assert rc == 0 and done == 20
+    assert np.max(np.abs(ra[:10] - ora[:10]) / np.abs(ora[:10])) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["small", "c3small"])
+def test_spin_polarised_mixed_matches_oracle(built, name):
+    """nspn = 2 on the tensor cores: one contraction per valence spin, each
+    writing the channels of its spin, for the long-range and multiplet terms."""
+    _, O = built
+    w, P = problem(name, O, seed=11, nspn=2)
+    rng = np.random.default_rng(4)
+    pr, pi = rng.standard_normal(w.npsi), rng.standard_normal(w.npsi)
+    ctx = capi.Context(w, precision=capi.OCN_PREC_MIXED)
+    try:
+        hr, hi = ctx.apply_H(pr, pi)
+        ra, ia, rb, done = ctx.haydock(30)
+    finally:
+        ctx.close()
+    orr, oi = P.xact(pr, pi)
+    assert _rel(hr + 1j * hi, orr + 1j * oi) < 1e-4
+    rc, ora, oia, orb, _ = P.haydock(30)
+    sg = capi.spectrum_cf(ra, ia, rb, 30, w.kpref, w.el, w.eh, 500, w.gam0)
+    so = O.write_core(ora, oia, orb, 30, w.kpref, w.el, w.eh, 500, w.gam0)
+    assert _rel(sg[:, 2], so[:, 2]) < 1e-4

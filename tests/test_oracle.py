@@ -179,3 +179,19 @@ def test_pnorm_kpref():
     val = 1.0  # psi already normalised
     assert abs(np.sum(w.psi_r ** 2 + w.psi_i ** 2) - 1.0) < 1e-12
     assert w.kpref > 0 and val == 1.0
+
+
+def test_spin_polarised_action_hermitian(oracle_lib):
+    """nspn = 2 (valence spin alpha mod 2 picks the Bloch functions and the
+    projector coefficients): the dense action stays Hermitian and differs from
+    the action built from the spin-up functions alone."""
+    w = WL.make("c3small", seed=5, nspn=2)
+    P = oracle_lib.OracleProblem(w)
+    H = _dense(P, w.npsi)
+    assert np.abs(H - H.conj().T).max() < 1e-13 * np.abs(H).max()
+    n = w.nb * w.nk * w.nx
+    w1 = WL.make("c3small", seed=5, nspn=2)
+    w1.ur[n:], w1.ui[n:] = w1.ur[:n], w1.ui[:n]
+    r, i = oracle_lib.OracleProblem(w1).xact(w.psi_r, w.psi_i)
+    r2, i2 = P.xact(w.psi_r, w.psi_i)
+    assert np.abs((r - r2) + 1j * (i - i2)).max() > 1e-6
