@@ -60,6 +60,12 @@ def parse():
                     help="energies of the adjoint-gradient leg (GMRES forward + reverse); 0 = off")
     ap.add_argument("--gmres-omega", type=int, default=200,
                     help="energies of the GMRES leg (0 disables it)")
+    ap.add_argument("--gmres-fp64-omega", type=int, default=8,
+                    help="energies (a spread subset of the GMRES leg's) solved by both precisions for the "
+                         "FP64 comparison; 0 = off")
+    ap.add_argument("--batch-fp64", type=int, default=8,
+                    help="instances of the batched set run by both precisions (100 steps) for the FP64 "
+                         "comparison; 0 = off")
     return ap.parse_args()
 
 
@@ -375,13 +381,48 @@ def run_batch(args, torch, capi, WL, local, dev, niter: int = 500, nv: int = 3):
     torch.cuda.synchronize()
     t3 = time.perf_counter()
     total = len(ctxs) * nv * niter
+    cmp64 = None
+    m = min(args.batch_fp64, len(ctxs))
+    if m > 0:
+        # The same first m instances through both precisions for fp64_steps
+        # Lanczos steps: mixed as one batched launch, FP64 one context after
+        # another (its kernels are FP64-pipe bound, batching would not change
+        # that); spectra compared chain by chain.
+        fp64_steps = 100
+        mres = capi.haydock_batch(ctxs[:m], ptrs[:m], nvs[:m], fp64_steps)  # warm-up of this subset
+        torch.cuda.synchronize()
+        t4 = time.perf_counter()
+        mres = capi.haydock_batch(ctxs[:m], ptrs[:m], nvs[:m], fp64_steps)
+        torch.cuda.synchronize()
+        t5 = time.perf_counter()
+        err, t64 = 0.0, 0.0
+        for i in range(m):
+            w = WL.batch_instance(i, u2_device=dev)
+            c64 = capi.Context(w, precision=capi.OCN_PREC_FP64, device=local, nvec=nv)
+            w.ur = w.ui = None
+            c64.haydock_block_dev(3, nv, ptrs[i])  # warm-up
+            torch.cuda.synchronize()
+            t6 = time.perf_counter()
+            ra, ia, rb, _ = c64.haydock_block_dev(fp64_steps, nv, ptrs[i])
+            torch.cuda.synchronize()
+            t64 += time.perf_counter() - t6
+            c64.close()
+            for v in range(nv):
+                s64 = capi.spectrum_cf(ra[v], ia[v], rb[v], fp64_steps, w.kpref, w.el, w.eh, 1000, w.gam0)
+                smx = capi.spectrum_cf(mres[i][0][v], mres[i][1][v], mres[i][2][v], fp64_steps, w.kpref,
+                                       w.el, w.eh, 1000, w.gam0)
+                err = max(err, float(np.linalg.norm(smx[:, 2] - s64[:, 2]) / np.linalg.norm(s64[:, 2])))
+        sub = m * nv * fp64_steps
+        cmp64 = {"instances": m, "lanczos_steps": fp64_steps, "mixed_batched_value": sub / (t5 - t4),
+                 "fp64_value": sub / t64, "speedup_mixed_vs_fp64": (t64 / (t5 - t4)),
+                 "max_spectral_error_mixed_vs_fp64": err}
     for c in ctxs:
         c.close()
     torch.cuda.empty_cache()
     return {"instances": len(ctxs), "chains_each": nv, "lanczos_steps": niter,
             "value": total / (t2 - t1), "unit": UNIT, "ms": (t2 - t1) * 1e3,
             "sequential_value": total / (t3 - t2), "sequential_ms": (t3 - t2) * 1e3,
-            "setup_s": setup_s, "shapes": shapes, "tiles": tuned}
+            "fp64_subset": cmp64, "setup_s": setup_s, "shapes": shapes, "tiles": tuned}
 
 
 def run_ours(args, ws, rank, local, pg):
@@ -473,6 +514,15 @@ def run_ours(args, ws, rank, local, pg):
               "gpu_launches": ctx.launches - l1,
               "hpsi_per_s": (int(its.sum()) + 2 * args.gmres_omega) / (gms / 1000.0),
               "max_rel_error": float(np.max(np.abs(rel)))}
+        if args.gmres_fp64_omega > 0:
+            # a spread subset of the energies, solved here and again by the FP64 path below
+            sub_e = energies[np.linspace(0, len(energies) - 1, args.gmres_fp64_omega).round().astype(int)]
+            g0.record(stream)
+            sre, sim, _, sits = ctx.gmres(sub_e, depth=80, tol=1e-6, max_restarts=100)
+            g1.record(stream)
+            torch.cuda.synchronize()
+            gm["fp64_subset"] = {"energies_ev": sub_e, "mixed_ms": g0.elapsed_time(g1),
+                                 "mixed_re": sre, "mixed_im": sim, "mixed_iterations": int(sits.sum())}
     ctx.close()
 
     # ---- adjoint leg: d(spectrum)/d(W scale, W(r) table, Gamma, scissor) through
@@ -570,11 +620,29 @@ def run_ours(args, ws, rank, local, pg):
         s64 = torch.cuda.ExternalStream(c64.stream, device=dev)
         c64.haydock_dev(50, pr_ptr, pi_ptr)
         ms64, spec64 = _device_steps(c64, w, niter, ne, pr_ptr, pi_ptr, 1, s64, torch)
-        c64.close()
         err = float(np.linalg.norm(spec_main[:, 2] - spec64[:, 2]) / np.linalg.norm(spec64[:, 2]))
         fp64 = {"value": niter / (ms64 / 1000.0), "unit": UNIT, "ms_per_step": ms64,
                 "spectral_error_mixed_vs_fp64": err,
                 "speedup_mixed_vs_fp64": value / ws / (niter / (ms64 / 1000.0))}
+        if gm is not None and "fp64_subset" in gm:
+            sub = gm.pop("fp64_subset")
+            h0 = torch.cuda.Event(enable_timing=True)
+            h1 = torch.cuda.Event(enable_timing=True)
+            h0.record(s64)
+            re64, im64, _, its64 = c64.gmres(sub["energies_ev"], depth=80, tol=1e-6, max_restarts=100)
+            h1.record(s64)
+            torch.cuda.synchronize()
+            ms_g64 = h0.elapsed_time(h1)
+            # out_im is the absorption (1 - kpref Re F is out_re): both columns compared
+            e_im = float(np.linalg.norm(sub["mixed_im"] - im64) / np.linalg.norm(im64))
+            e_re = float(np.linalg.norm(sub["mixed_re"] - re64) / np.linalg.norm(re64))
+            gm["fp64_subset"] = {"omega_points": len(sub["energies_ev"]), "mixed_ms": sub["mixed_ms"],
+                                 "fp64_ms": ms_g64, "speedup_mixed_vs_fp64": ms_g64 / sub["mixed_ms"],
+                                 "mixed_iterations": sub["mixed_iterations"], "fp64_iterations": int(its64.sum()),
+                                 "spectral_error_im": e_im, "spectral_error_re": e_re}
+        c64.close()
+    if gm is not None and "mixed_re" in gm.get("fp64_subset", {}):
+        gm.pop("fp64_subset")  # no FP64 run to compare with
     # dominant kernel and its roofline
     hbm, bf16, src = measured_peaks()
     lr_classes = {k: v for k, v in kt.items() if v[0] > 0 and k.startswith("lr_") and k != "lr_prep"}

@@ -159,3 +159,35 @@ def test_vjp_rejects_unsupported_terms(built):
         assert e.value.code == 9962
     finally:
         ctx.close()
+
+
+def test_windowed_recomputation_gives_the_stored_gradient(built):
+    """With a memory cap below the solutions' size the energies are taken in
+    windows, forward keeps nothing and backward solves each window again: the
+    spectrum and every gradient equal, bit for bit, those of the same windows
+    with the solutions stored."""
+    from ocean_gb300 import adjoint
+
+    w, E, c, d, v = _setup("tiny", 7, seed=8)
+    per_x = 2 * w.npsi * 8
+    kw = dict(depth=24, tol=TOL_G2, max_restarts=400)
+    stored = adjoint.GmresProblem(w, E, window=3, **kw)
+    recomp = adjoint.GmresProblem(w, E, max_stored_bytes=3.5 * per_x, **kw)
+    try:
+        assert (stored.recompute, stored.window) == (False, 3)
+        assert (recomp.recompute, recomp.window) == (True, 3)
+        L1, g1 = _autograd(stored, w, c, d)
+        L2, g2 = _autograd(recomp, w, c, d)
+    finally:
+        stored.close()
+        recomp.close()
+    assert L1 == L2
+    assert g1["scale"] == g2["scale"] and g1["gamma"] == g2["gamma"] and g1["scissor"] == g2["scissor"]
+    assert np.array_equal(g1["ptab"], g2["ptab"])
+    # and the windowed gradient is the gradient: central differences of the library
+    prob = adjoint.GmresProblem(w, E, **kw)
+    try:
+        fd = _fd(lambda *a: _eval_lib(prob, w, E, c, d, *a), w, v)
+    finally:
+        prob.close()
+    _compare(g2, fd, v, 2e-5)
