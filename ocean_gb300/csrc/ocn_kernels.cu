@@ -719,13 +719,17 @@ __global__ void k_multidot(const double* const* __restrict__ vecs, int nvec,
     part[((size_t)blockIdx.x * nvec + j) * 4 + threadIdx.x] = t;
   }
 }
+// One warp per output: lane l sums chunks l, l+32, ... in order, then a fixed
+// shuffle tree (deterministic; the chunk partials are L2-resident).
 __global__ void k_multidot_reduce(const double* __restrict__ part, int nblk, int nvec,
                                   double* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (i >= nvec * 4) return;
   double s = 0.0;
-  for (int b = 0; b < nblk; ++b) s += part[(size_t)b * nvec * 4 + i];
-  out[i] = s;
+  for (int b = lane; b < nblk; b += 32) s += part[(size_t)b * nvec * 4 + i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) out[i] = s;
 }
 // x += sum_j c_j u_j, ax += sum_j c_j au_j   (OCEAN_gmres.f90:336-341, in j order)
 // x += sum_j c_j u_j, ax += sum_j c_j au_j (OCEAN_gmres.f90:312-322).  The
@@ -1090,7 +1094,7 @@ int vec_multidot_dev(ocn_ctx* c, const double* const* d_vecs, int nvec, const do
   k_multidot<<<dim3(nblk, nvec), 256, 0, c->stream>>>(d_vecs, nvec, au_cur, g, c->npsi, d_part);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
-  k_multidot_reduce<<<(nvec * 4 + 127) / 128, 128, 0, c->stream>>>(d_part, nblk, nvec, d_out);
+  k_multidot_reduce<<<(nvec * 4 + 7) / 8, 256, 0, c->stream>>>(d_part, nblk, nvec, d_out);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;

@@ -505,17 +505,19 @@ __global__ void k_build_mb(const double2* __restrict__ mpc, __nv_bfloat16* __res
 }
 
 // amp[v][p][a] = sum_k amp_part[k][p][v*Na + a], summed in FP64: a CTA owns
-// 32 consecutive (p, t) outputs (coalesced along t) and its 8 warps split the
-// k range (warp w takes k = w, w+8, ...); the 8 partials are added in order.
-__global__ void k_amp_reduce_f32(const float2* __restrict__ part, double2* __restrict__ amp, int nk, int np,
-                                 int na, int nv) {
-  __shared__ double2 sh[8][32];
+// 32 consecutive (p, t) outputs (coalesced along t) and its AMP_KGROUPS warps
+// split the k range (warp w takes k = w, w + AMP_KGROUPS, ...); warp 0 adds
+// the group partials in order (deterministic).
+constexpr int AMP_KGROUPS = 32;
+__global__ void __launch_bounds__(32 * AMP_KGROUPS)
+    k_amp_reduce_f32(const float2* __restrict__ part, double2* __restrict__ amp, int nk, int np, int na, int nv) {
+  __shared__ double2 sh[AMP_KGROUPS][32];
   const int nt = na * nv;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int i = blockIdx.x * 32 + lane;
   double sr = 0.0, si = 0.0;
   if (i < np * nt)
-    for (int k = w; k < nk; k += 8) {
+    for (int k = w; k < nk; k += AMP_KGROUPS) {
       const float2 f = part[(size_t)k * np * nt + i];
       sr += (double)f.x;
       si += (double)f.y;
@@ -524,7 +526,7 @@ __global__ void k_amp_reduce_f32(const float2* __restrict__ part, double2* __res
   __syncthreads();
   if (w == 0 && i < np * nt) {
     double tr = 0.0, ti = 0.0;
-    for (int g = 0; g < 8; ++g) {
+    for (int g = 0; g < AMP_KGROUPS; ++g) {
       tr += sh[g][lane].x;
       ti += sh[g][lane].y;
     }
@@ -1061,7 +1063,8 @@ int mult_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t 
     k_lr_tc<<<m->gridm1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ma_hi, m->tm_ma_lo, m->tm_b1, a);
     ++c->launches;
   }
-  k_amp_reduce_f32<<<(np * na * nv + 31) / 32, 256, 0, c->stream>>>(m->amp_part, m->amp, c->nk, np, na, nv);
+  k_amp_reduce_f32<<<(np * na * nv + 31) / 32, 32 * AMP_KGROUPS, 0, c->stream>>>(m->amp_part, m->amp, c->nk,
+                                                                                 np, na, nv);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   for (int v = 0; v < nv; ++v)
