@@ -230,12 +230,18 @@ int ocn_haydock_block_dev(ocn_ctx* ctx, int nv, const double* d_psi0, int niter,
 
 /* Batched Haydock over independent problems: context i runs nv[i] chains
  * (ocn_haydock_block_dev on d_psi0[i]) for niter iterations.  Three iterations
- * of every context are captured into one CUDA graph as independent branches and
- * the graph is replayed niter/3 times, so one launch advances all problems and
- * small ones share the SMs.  The reference runs such problems one after another
- * (OCEAN.f90:51-83, one ocean.x run per site and photon).  Contexts must share
- * one device; outputs per context as for ocn_haydock_block_dev (niter_done may be
- * NULL).  Returns the first hard error, else OCN_ERR_NAN if a chain hit a NaN. */
+ * of every context are captured into one CUDA graph that is replayed niter/3
+ * times, so one launch advances all problems.  Mixed-precision contexts with the
+ * long-range term and without the multiplet term share grouped launches: each
+ * stage of a step (the two tensor-core contractions, the k-mesh transforms, the
+ * operand builders, the Lanczos kernels) is one persistent launch over the tiles
+ * or vectors of all of them, each context keeping its own tiling, so its results
+ * equal those of its own launches bit for bit.  Other contexts run as branches
+ * of their own (also with the environment variable OCN_BATCH_BRANCHES=1).  The
+ * reference runs such problems one after another (OCEAN.f90:51-83, one ocean.x
+ * run per site and photon).  Contexts must share one device; outputs per
+ * context as for ocn_haydock_block_dev (niter_done may be NULL).  Returns the
+ * first hard error, else OCN_ERR_NAN if a chain hit a NaN. */
 int ocn_haydock_batch(ocn_ctx* const* ctxs, int nctx, const int* nv, const double* const* d_psi0,
                       int niter, double* const* real_a, double* const* imag_a,
                       double* const* real_b, int* const* niter_done);
@@ -393,19 +399,21 @@ int ocn_output_filename(const char* kind, const char* calc_type, const char* eln
 long long ocn_kernel_launches(const ocn_ctx* ctx);
 
 /* Tile configuration of the mixed-precision tensor-core contractions (no
- * counterpart in the reference, whose BLAS calls have none): tiles[6] =
+ * counterpart in the reference, whose BLAS calls have none): tiles[7] =
  * {shared-memory pipeline stages, K splits of the x->band contraction,
  *  persistent grid cap of the band->x contraction, of the x->band one,
  *  k-mesh transforms per CTA (0 = all of an x-point), threads of a k-mesh
- *  transform CTA (128, 256 or 512; 0 = 128)}.
+ *  transform CTA (128, 256 or 512; 0 = 128), band->x output staging (1: the
+ *  contraction's outputs go through shared memory and are stored coalesced,
+ *  when the pipeline leaves room; 0: stored directly)}.
  * ocn_autotune times the long-range term of an nv-vector block under each
  * candidate (reps launches each, CUDA events) and keeps the fastest; returns
  * its time in ms, the time of the tiling in force before the call, and the
  * chosen tiles (any output may be NULL).  Tilings change only the order of
  * FP32 partial sums.  Mixed precision only (else OCN_ERR_UNSUPPORTED). */
-int ocn_autotune(ocn_ctx* ctx, int nv, int reps, double* best_ms, double* current_ms, int tiles[6]);
-int ocn_set_tiles(ocn_ctx* ctx, const int tiles[6]);
-int ocn_get_tiles(const ocn_ctx* ctx, int tiles[6]);
+int ocn_autotune(ocn_ctx* ctx, int nv, int reps, double* best_ms, double* current_ms, int tiles[7]);
+int ocn_set_tiles(ocn_ctx* ctx, const int tiles[7]);
+int ocn_get_tiles(const ocn_ctx* ctx, int tiles[7]);
 
 /* Per-kernel device timing with CUDA events recorded on the context stream
  * (replaces the wall-clock buckets of OCEAN_timekeeper, OCEAN_timekeeper.f90:13-168).

@@ -373,18 +373,18 @@ class Context:
         """Times the candidate tilings of the tensor-core contractions and keeps
         the fastest; returns (ms per long-range application, tiles)."""
         ms, cur = C.c_double(0.0), C.c_double(0.0)
-        t = (C.c_int * 6)()
+        t = (C.c_int * 7)()
         self._chk(self.lib.ocn_autotune(self.ptr, nv, reps, C.byref(ms), C.byref(cur), t))
         self.last_tune_current_ms = cur.value
         return ms.value, tuple(t)
 
     def tiles(self):
-        t = (C.c_int * 6)()
+        t = (C.c_int * 7)()
         self._chk(self.lib.ocn_get_tiles(self.ptr, t))
         return tuple(t)
 
     def set_tiles(self, tiles):
-        self._chk(self.lib.ocn_set_tiles(self.ptr, (C.c_int * 6)(*tiles)))
+        self._chk(self.lib.ocn_set_tiles(self.ptr, (C.c_int * 7)(*tiles)))
 
     def set_W(self, W):
         self._chk(self.lib.ocn_set_W(self.ptr, _dp(_f64(W))))

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <new>
@@ -140,7 +141,7 @@ namespace {
 void drop_haydock_graph(ocn_ctx* c);
 }
 
-int ocn_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int tiles[6]) {
+int ocn_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int tiles[7]) {
   if (!c) return OCN_ERR_ARG;
   if (c->dims.precision != OCN_PREC_MIXED || !c->mixed)
     return set_err(c, OCN_ERR_UNSUPPORTED, "ocn_autotune: tiles exist on the mixed-precision path only");
@@ -149,7 +150,7 @@ int ocn_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_
   return mixed_autotune(c, nv, reps, best_ms, current_ms, tiles);
 }
 
-int ocn_set_tiles(ocn_ctx* c, const int tiles[6]) {
+int ocn_set_tiles(ocn_ctx* c, const int tiles[7]) {
   if (!c || !tiles) return OCN_ERR_ARG;
   if (c->dims.precision != OCN_PREC_MIXED || !c->mixed)
     return set_err(c, OCN_ERR_UNSUPPORTED, "ocn_set_tiles: tiles exist on the mixed-precision path only");
@@ -159,7 +160,7 @@ int ocn_set_tiles(ocn_ctx* c, const int tiles[6]) {
   return mixed_configure(c, tiles);
 }
 
-int ocn_get_tiles(const ocn_ctx* c, int tiles[6]) {
+int ocn_get_tiles(const ocn_ctx* c, int tiles[7]) {
   if (!c || !tiles) return OCN_ERR_ARG;
   return c->mixed ? mixed_config(c, tiles) : OCN_ERR_UNSUPPORTED;
 }
@@ -259,7 +260,10 @@ int ocn_ctx_create(const ocn_dims* d, ocn_ctx** out) {
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return fail(cuda_fail(c, e, "cudaStreamCreate"));
 
-  c->red_blocks = 2 * c->sm_count;
+  // Blocks of the Lanczos-step and dot-product kernels: two per SM, or fewer for
+  // small vectors (about two elements per thread); each block's partial is
+  // re-reduced by every block of the next stage, so extra blocks cost.
+  c->red_blocks = (int)std::min<size_t>(2 * (size_t)c->sm_count, std::max<size_t>(1, (c->npsi + 511) / 512));
   c->lr_xsplit = std::max(1, std::min((2 * c->sm_count + nk - 1) / nk, std::max(1, nx / 64)));
   int rc = OCN_OK;
   if ((rc = dev_alloc(c, &c->d_er, c->npsi)) || (rc = dev_alloc(c, &c->d_ei, c->npsi)) ||
@@ -954,24 +958,65 @@ int ocn_haydock_batch(ocn_ctx* const* ctxs, int nctx, const int* nv, const doubl
     const int rc = haydock_prepare(c, nv[i], d_psi0[i], d_psi0[i] + c->npsi, 2 * c->npsi, niter, &R[i]);
     if (rc) return rc;
   }
-  // One graph holds three iterations of every context as independent branches,
-  // so a single launch advances all of them and the device overlaps their kernels.
+  // One graph holds three iterations of every context, so a single launch
+  // advances all of them.  Contexts that can share launches (mixed precision,
+  // long-range term, no multiplet; batch_group_refusal) run as one branch of
+  // grouped launches: each stage of the step is one persistent launch over the
+  // tiles or vectors of all of them.  The others run as their own branches.
   const int ngraph = niter / 3;
   ocn_ctx* c0 = ctxs[0];
   std::vector<cudaEvent_t> ev(nctx, nullptr);
   cudaGraph_t parent = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<long long> kernels(nctx, 0);
+  std::vector<int> grouped, own;
+  for (int i = 0; i < nctx; ++i) (batch_group_refusal(ctxs[i]).empty() ? grouped : own).push_back(i);
+  const char* nogroup = std::getenv("OCN_BATCH_BRANCHES");  // "1": every context as its own branch
+  if (grouped.size() < 2 || (nogroup && nogroup[0] == '1')) {  // one context gains nothing from grouping
+    own.insert(own.end(), grouped.begin(), grouped.end());
+    grouped.clear();
+  }
+  LzGroup* lz = nullptr;
+  LrGroup* lr = nullptr;
   auto cleanup = [&]() {
     if (exec) cudaGraphExecDestroy(exec);
     if (parent) cudaGraphDestroy(parent);
     for (cudaEvent_t e : ev)
       if (e) cudaEventDestroy(e);
+    lz_group_destroy(lz);
+    lr_group_destroy(lr);
   };
   int rc = OCN_OK;
   if (ngraph > 0) {
     cudaError_t e = cudaGraphCreate(&parent, 0);
-    for (int i = 0; i < nctx && e == cudaSuccess && rc == OCN_OK; ++i) {
+    if (!grouped.empty() && e == cudaSuccess) {
+      std::vector<BatchMember> mem;
+      for (int i : grouped)
+        mem.push_back(BatchMember{ctxs[i], nv[i], {R[i].buf[0], R[i].buf[1], R[i].buf[2]}, R[i].ra, R[i].ia,
+                                  R[i].rb, R[i].cap1});
+      ocn_ctx* cg = ctxs[grouped[0]];
+      rc = lz_group_create(mem, &lz);
+      if (rc == OCN_OK) rc = lr_group_create(mem, &lr);
+      if (rc == OCN_OK) {
+        cudaGraph_t child = nullptr;
+        e = cudaStreamBeginCapture(cg->stream, cudaStreamCaptureModeThreadLocal);
+        for (int r = 0; r < 3 && e == cudaSuccess && rc == OCN_OK; ++r) {
+          if ((rc = lz_group_advance(lz, cg->stream)) || (rc = lr_group_apply(lr, cg->stream)) ||
+              (rc = lz_group_step(lz, r, cg->stream)) || (rc = lr_group_norm(lr, r, cg->stream)))
+            rc = set_err(cg, rc, "grouped batched launch failed");
+        }
+        const cudaError_t ee = cudaStreamEndCapture(cg->stream, &child);
+        if (e == cudaSuccess) e = ee;
+        if (e == cudaSuccess && rc == OCN_OK) {
+          cudaGraphNode_t node;
+          e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, child);
+          kernels[grouped[0]] = 3 * (3 + lr_group_launches(lr));
+        }
+        if (child) cudaGraphDestroy(child);
+      }
+    }
+    for (int i : own) {
+      if (e != cudaSuccess || rc != OCN_OK) break;
       ocn_ctx* c = ctxs[i];
       const bool timing = c->timing.on;  // event-record nodes stay out of the batch graph
       const long long saved = c->hay_graph_kernels;

@@ -26,6 +26,36 @@ struct BlockStrides {
   size_t red;   // between the reduction-partial arrays of two chains
 };
 
+// Argument records of the Lanczos-step kernels of one context, for launches
+// that serve several contexts at once (batched Haydock).
+struct CombineArgs {
+  const double *pr, *pi, *er, *ei, *allow, *acc, *part;
+  int nparts;
+  const double2* so;
+  double *outr, *outi;
+  int nbk, na;
+  size_t npsi;
+  int use_e0, use_so, backwards;
+  const double *oldr, *oldi, *rb_base;
+  const int* itp;
+  double* red;
+  BlockStrides bs;
+  int nv;    // vectors of this context; blocks beyond it return at once
+  int nblk;  // blocks per vector of this context (its own launches' grid); blocks beyond return
+};
+struct Lanczos2Args {
+  const double* red1;
+  int nblk;
+  double *hr, *hi;
+  const double *pr, *pi;
+  size_t n;
+  double* red2;
+  double *ra_base, *ia_base;
+  const int* itp;
+  BlockStrides bs;
+  int nv;
+};
+
 // Kernel classes timed with CUDA events on the context stream when timing is on.
 enum TimedClass { T_LR_GEMM1 = 0, T_LR_FFT, T_LR_GEMM2, T_LR_PREP, T_MULT, T_LANCZOS, T_NCLASS };
 
@@ -227,6 +257,29 @@ int lanczos_launch(ocn_ctx* c, int nv, const double* old, const double* psi, dou
                    double* ia, double* rb, size_t cstride, const int* itp);
 int advance_iter(ocn_ctx* c, int* itp);
 
+// ---- batched Haydock with grouped launches (one launch per stage for all
+// member contexts; ocn_kernels.cu / ocn_mixed.cu)
+struct BatchMember {
+  ocn_ctx* c;
+  int nv;
+  double* buf[3];  // Haydock vectors: iteration r uses old = buf[r], psi = buf[r+1], h = buf[r+2] (mod 3)
+  double *ra, *ia, *rb;
+  size_t cstride;
+};
+struct LzGroup;  // combine + Lanczos stage 2 + iteration counters
+struct LrGroup;  // long-range term (tensor-core contractions, transforms, operands) + normalisation
+// Why a context cannot join a grouped batch (empty: it can).
+std::string batch_group_refusal(const ocn_ctx* c);
+int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out);
+int lz_group_advance(LzGroup* g, cudaStream_t s);
+int lz_group_step(LzGroup* g, int rot, cudaStream_t s);
+void lz_group_destroy(LzGroup* g);
+int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out);
+int lr_group_apply(LrGroup* g, cudaStream_t s);
+int lr_group_norm(LrGroup* g, int rot, cudaStream_t s);
+int lr_group_launches(const LrGroup* g);
+void lr_group_destroy(LrGroup* g);
+
 // BLAS-1 helpers for GMRES (ocn_kernels.cu); vectors are [re plane | im plane]
 int vec_dot_dev(ocn_ctx* c, const double* p, const double* q, double* d_out);
 int vec_multidot_dev(ocn_ctx* c, const double* const* d_vecs, int nvec, const double* au_cur,
@@ -267,8 +320,8 @@ int mult_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t 
                      bool b1_ready);
 // tile configuration {stages, GEMM2 K splits, GEMM1 grid cap, GEMM2 grid cap,
 // k-mesh transforms per CTA, k-mesh transform threads}
-int mixed_configure(ocn_ctx* c, const int cfg[6]);
-int mixed_config(const ocn_ctx* c, int cfg[6]);
-int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int best_cfg[6]);
+int mixed_configure(ocn_ctx* c, const int cfg[7]);
+int mixed_config(const ocn_ctx* c, int cfg[7]);
+int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int best_cfg[7]);
 
 }  // namespace ocn

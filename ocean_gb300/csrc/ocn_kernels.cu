@@ -12,6 +12,7 @@
 #include <algorithm>
 
 #include <cstdio>
+#include <new>
 
 #include "ocn_internal.h"
 #include "ocn_kmesh_dft.cuh"
@@ -216,8 +217,7 @@ __global__ void k_lr_gemm2_fp64(const double2* __restrict__ u, const double2* __
 // Optionally fused with the first Lanczos stage (ocean_hay_ab_twoterm,
 // OCEAN_haydock.f90:848-860): out -= b_{i-1} old, partial <out|psi>.
 template <int NA, bool SO>
-__global__ void __launch_bounds__(LZ_THREADS)
-    k_combine(const double* __restrict__ pr, const double* __restrict__ pi,
+__device__ __forceinline__ void combine_body(const double* __restrict__ pr, const double* __restrict__ pi,
                           const double* __restrict__ er, const double* __restrict__ ei,
                           const double* __restrict__ allow, const double* __restrict__ acc,
                           const double* __restrict__ part, int nparts, const double2* __restrict__ so,
@@ -225,10 +225,10 @@ __global__ void __launch_bounds__(LZ_THREADS)
                           size_t npsi, int use_e0, int use_so, int backwards,
                           const double* __restrict__ oldr, const double* __restrict__ oldi,
                           const double* __restrict__ rb_base, const int* __restrict__ itp,
-                          double* __restrict__ red, const BlockStrides bs) {
+                          double* __restrict__ red, const BlockStrides bs, int bx, int by, int nbx) {
   __shared__ double sh[2][32];
-  // chain / vector v = blockIdx.y of a block of psi vectors
-  const size_t v = blockIdx.y;
+  // chain / vector v = by of a block of psi vectors
+  const size_t v = by;
   pr += v * bs.vec;
   pi += v * bs.vec;
   outr += v * bs.vec;
@@ -247,8 +247,8 @@ __global__ void __launch_bounds__(LZ_THREADS)
   // one thread per psi element idx = e + Nb*Nk*ic: the spin-orbit sum reads the
   // other channels of the same (n, k), which neighbouring threads also load
   const size_t nall = (size_t)nbk * NA;
-  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < nall;
-       idx += (size_t)gridDim.x * blockDim.x) {
+  for (size_t idx = bx * (size_t)blockDim.x + threadIdx.x; idx < nall;
+       idx += (size_t)nbx * blockDim.x) {
     const int ic = (int)(idx / (size_t)nbk);
     const size_t e = idx - (size_t)ic * nbk;
     const double qrc = pr[idx], qic = pi[idx];
@@ -320,9 +320,42 @@ __global__ void __launch_bounds__(LZ_THREADS)
       s0 += sh[0][i];
       s1 += sh[1][i];
     }
-    red[2 * blockIdx.x] = s0;
-    red[2 * blockIdx.x + 1] = s1;
+    red[2 * bx] = s0;
+    red[2 * bx + 1] = s1;
   }
+}
+
+
+template <int NA, bool SO>
+__global__ void __launch_bounds__(LZ_THREADS)
+    k_combine(const double* __restrict__ pr, const double* __restrict__ pi, const double* __restrict__ er,
+              const double* __restrict__ ei, const double* __restrict__ allow, const double* __restrict__ acc,
+              const double* __restrict__ part, int nparts, const double2* __restrict__ so,
+              double* __restrict__ outr, double* __restrict__ outi, int nbk, int na, size_t npsi, int use_e0,
+              int use_so, int backwards, const double* __restrict__ oldr, const double* __restrict__ oldi,
+              const double* __restrict__ rb_base, const int* __restrict__ itp, double* __restrict__ red,
+              const BlockStrides bs) {
+  combine_body<NA, SO>(pr, pi, er, ei, allow, acc, part, nparts, so, outr, outi, nbk, na, npsi, use_e0, use_so,
+                       backwards, oldr, oldi, rb_base, itp, red, bs, blockIdx.x, blockIdx.y, gridDim.x);
+}
+
+// The combine + first Lanczos stage of several contexts in one launch: grid
+// (blocks per context, largest block of vectors, contexts); every context keeps
+// the block partition (and so the reduction order) of its own launches.
+__global__ void __launch_bounds__(LZ_THREADS) k_combine_group(const CombineArgs* __restrict__ tab) {
+  const CombineArgs& a = tab[blockIdx.z];
+  if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
+#define OCN_COMBINE_ARGS                                                                                    \
+  a.pr, a.pi, a.er, a.ei, a.allow, a.acc, a.part, a.nparts, a.so, a.outr, a.outi, a.nbk, a.na, a.npsi, a.use_e0, \
+      a.use_so, a.backwards, a.oldr, a.oldi, a.rb_base, a.itp, a.red, a.bs, blockIdx.x, blockIdx.y, a.nblk
+  if (a.na == 4) {
+    if (a.use_so) combine_body<4, true>(OCN_COMBINE_ARGS);
+    else combine_body<4, false>(OCN_COMBINE_ARGS);
+  } else {
+    if (a.use_so) combine_body<12, true>(OCN_COMBINE_ARGS);
+    else combine_body<12, false>(OCN_COMBINE_ARGS);
+  }
+#undef OCN_COMBINE_ARGS
 }
 
 // Sum of nb partial pairs in a fixed order, done identically by every block.
@@ -354,7 +387,9 @@ __device__ __forceinline__ void reduce_pairs(const double* __restrict__ red, int
   *s1 = tb;
 }
 
-__device__ __forceinline__ void block_partial(double v0, double v1, double* __restrict__ red) {
+__device__ __forceinline__ void block_partial(double v0, double v1, double* __restrict__ red,
+                                              int bx = -1) {
+  if (bx < 0) bx = blockIdx.x;
   __shared__ double sh[2][32];
   for (int o = 16; o > 0; o >>= 1) {
     v0 += __shfl_down_sync(0xffffffffu, v0, o);
@@ -372,21 +407,26 @@ __device__ __forceinline__ void block_partial(double v0, double v1, double* __re
       s0 += sh[0][i];
       s1 += sh[1][i];
     }
-    red[2 * blockIdx.x] = s0;
-    red[2 * blockIdx.x + 1] = s1;
+    red[2 * bx] = s0;
+    red[2 * bx + 1] = s1;
   }
 }
 
 // Iteration counter of the device-resident Lanczos loop (coefficient index i).
 __global__ void k_advance(int* __restrict__ itp) { *itp += 1; }
+__global__ void k_advance_group(int* const* __restrict__ itps, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) *itps[i] += 1;
+}
 
 // Lanczos stage 2: a_{i-1} = Re<h|psi>; h -= a psi; partial |h|^2.
-__global__ void __launch_bounds__(LZ_THREADS) k_lanczos2(const double* __restrict__ red1, int nblk, double* __restrict__ hr,
+__device__ __forceinline__ void lanczos2_body(const double* __restrict__ red1, int nblk, double* __restrict__ hr,
                            double* __restrict__ hi, const double* __restrict__ pr,
                            const double* __restrict__ pi, size_t n, double* __restrict__ red2,
                            double* __restrict__ ra_base, double* __restrict__ ia_base,
-                           const int* __restrict__ itp, const BlockStrides bs) {
-  const size_t v = blockIdx.y;
+                           const int* __restrict__ itp, const BlockStrides bs, int bx, int by,
+                           int nbx) {
+  const size_t v = by;
   red1 += v * bs.red;
   red2 += v * bs.red;
   hr += v * bs.vec;
@@ -397,15 +437,14 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lanczos2(const double* __restric
   ia_base += v * bs.coef;
   double a, ia;
   reduce_pairs(red1, nblk, &a, &ia);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (bx == 0 && threadIdx.x == 0) {
     const int it = *itp;
     ra_base[it - 1] = a;
     ia_base[it - 1] = ia;
   }
   const double am = -a;
   double s = 0.0;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x) {
+  for (size_t e = bx * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)nbx * blockDim.x) {
     const double r = hr[e] + am * pr[e];
     const double i = hi[e] + am * pi[e];
     hr[e] = r;
@@ -413,7 +452,22 @@ __global__ void __launch_bounds__(LZ_THREADS) k_lanczos2(const double* __restric
     s += r * r + i * i;
   }
   __syncthreads();
-  block_partial(s, 0.0, red2);
+  block_partial(s, 0.0, red2, bx);
+}
+
+__global__ void __launch_bounds__(LZ_THREADS)
+    k_lanczos2(const double* __restrict__ red1, int nblk, double* __restrict__ hr, double* __restrict__ hi,
+               const double* __restrict__ pr, const double* __restrict__ pi, size_t n,
+               double* __restrict__ red2, double* __restrict__ ra_base, double* __restrict__ ia_base,
+               const int* __restrict__ itp, const BlockStrides bs) {
+  lanczos2_body(red1, nblk, hr, hi, pr, pi, n, red2, ra_base, ia_base, itp, bs, blockIdx.x, blockIdx.y, gridDim.x);
+}
+
+__global__ void __launch_bounds__(LZ_THREADS) k_lanczos2_group(const Lanczos2Args* __restrict__ tab) {
+  const Lanczos2Args& a = tab[blockIdx.z];
+  if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
+  lanczos2_body(a.red1, a.nblk, a.hr, a.hi, a.pr, a.pi, a.n, a.red2, a.ra_base, a.ia_base, a.itp, a.bs,
+                blockIdx.x, blockIdx.y, a.nblk);
 }
 
 // Lanczos stage 3: b_i = sqrt(sum); psi_new = h / b_i (in place in h).
@@ -1107,6 +1161,133 @@ int vec_update_dev(ocn_ctx* c, int nvec, const double2* d_coef, const double* co
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;
+}
+
+// ---------------------------------------------------- grouped Lanczos steps
+
+struct LzGroup {
+  int n = 0, nvmax = 1, nblk = 0;
+  CombineArgs* d_comb[3] = {nullptr, nullptr, nullptr};
+  Lanczos2Args* d_lz2[3] = {nullptr, nullptr, nullptr};
+  int** d_iters = nullptr;
+};
+
+void lz_group_destroy(LzGroup* g) {
+  if (!g) return;
+  for (int r = 0; r < 3; ++r) {
+    if (g->d_comb[r]) cudaFree(g->d_comb[r]);
+    if (g->d_lz2[r]) cudaFree(g->d_lz2[r]);
+  }
+  if (g->d_iters) cudaFree(g->d_iters);
+  delete g;
+}
+
+// The records of lanczos_launch for every member and each of the three buffer
+// rotations of a captured three-iteration graph.
+int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out) {
+  *out = nullptr;
+  if (mem.empty()) return OCN_ERR_ARG;
+  ocn_ctx* c0 = mem[0].c;
+  LzGroup* g = new (std::nothrow) LzGroup();
+  if (!g) return set_err(c0, OCN_ERR_ALLOC, "host allocation failed");
+  g->n = (int)mem.size();
+  g->nblk = c0->red_blocks;
+  std::vector<int*> iters;
+  std::vector<CombineArgs> ca(mem.size());
+  std::vector<Lanczos2Args> la(mem.size());
+  int rc = OCN_OK;
+  for (const BatchMember& b : mem) {
+    g->nvmax = std::max(g->nvmax, b.nv);
+    g->nblk = std::max(g->nblk, b.c->red_blocks);
+    iters.push_back(b.c->d_iter);
+  }
+  for (int r = 0; r < 3 && rc == OCN_OK; ++r) {
+    for (size_t i = 0; i < mem.size(); ++i) {
+      const BatchMember& b = mem[i];
+      ocn_ctx* c = b.c;
+      const size_t n = c->npsi;
+      const double* old = b.buf[r % 3];
+      const double* psi = b.buf[(r + 1) % 3];
+      double* h = b.buf[(r + 2) % 3];
+      const int* hf = c->sys.nhflag;
+      const double* parts;
+      int nparts;
+      active_parts(c, hf, &parts, &nparts);
+      const int nblk = c->red_blocks;
+      const BlockStrides bs = {2 * n, c->part_stride, b.cstride, (size_t)4 * nblk};
+      CombineArgs& a = ca[i];
+      a.pr = psi;
+      a.pi = psi + n;
+      a.er = c->d_er;
+      a.ei = c->ei_nonzero ? c->d_ei : nullptr;
+      a.allow = c->d_allow;
+      a.acc = nullptr;  // grouped members have no multiplet term
+      a.part = parts;
+      a.nparts = nparts;
+      a.so = c->d_so;
+      a.outr = h;
+      a.outi = h + n;
+      a.nbk = c->nb * c->nk;
+      a.na = c->na;
+      a.npsi = n;
+      a.use_e0 = c->sys.e0;
+      a.use_so = (c->sys.mult && hf[5] == 1 && c->have_so) ? 1 : 0;
+      a.backwards = 0;
+      a.oldr = old;
+      a.oldi = old + n;
+      a.rb_base = b.rb;
+      a.itp = c->d_iter;
+      a.red = c->d_red;
+      a.bs = bs;
+      a.nv = b.nv;
+      a.nblk = nblk;
+      Lanczos2Args& l = la[i];
+      l.red1 = c->d_red;
+      l.nblk = nblk;
+      l.hr = h;
+      l.hi = h + n;
+      l.pr = psi;
+      l.pi = psi + n;
+      l.n = n;
+      l.red2 = c->d_red + 2 * nblk;
+      l.ra_base = b.ra;
+      l.ia_base = b.ia;
+      l.itp = c->d_iter;
+      l.bs = bs;
+      l.nv = b.nv;
+    }
+    cudaError_t e = cudaMalloc(&g->d_comb[r], ca.size() * sizeof(CombineArgs));
+    if (e == cudaSuccess) e = cudaMalloc(&g->d_lz2[r], la.size() * sizeof(Lanczos2Args));
+    if (e == cudaSuccess) e = cudaMemcpy(g->d_comb[r], ca.data(), ca.size() * sizeof(CombineArgs), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(g->d_lz2[r], la.data(), la.size() * sizeof(Lanczos2Args), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = cuda_fail(c0, e, "batched Lanczos tables");
+  }
+  if (rc == OCN_OK) {
+    cudaError_t e = cudaMalloc(&g->d_iters, iters.size() * sizeof(int*));
+    if (e == cudaSuccess) e = cudaMemcpy(g->d_iters, iters.data(), iters.size() * sizeof(int*), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) rc = cuda_fail(c0, e, "batched Lanczos tables");
+  }
+  if (rc != OCN_OK) {
+    lz_group_destroy(g);
+    return rc;
+  }
+  *out = g;
+  return OCN_OK;
+}
+
+int lz_group_advance(LzGroup* g, cudaStream_t s) {
+  k_advance_group<<<(g->n + 127) / 128, 128, 0, s>>>(g->d_iters, g->n);
+  return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
+}
+
+// combine (E, masks, long-range parts, -b psi_old, <h|psi>) and stage 2 for
+// every member, buffer rotation rot
+int lz_group_step(LzGroup* g, int rot, cudaStream_t s) {
+  const dim3 grid(g->nblk, g->nvmax, g->n);
+  k_combine_group<<<grid, LZ_THREADS, 0, s>>>(g->d_comb[rot]);
+  if (cudaGetLastError() != cudaSuccess) return OCN_ERR_CUDA;
+  k_lanczos2_group<<<grid, LZ_THREADS, 0, s>>>(g->d_lz2[rot]);
+  return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
 }
 
 }  // namespace ocn

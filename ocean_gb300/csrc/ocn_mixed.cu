@@ -73,6 +73,13 @@ struct TcParams {
   int bshared;   // B operand has one k slice shared by every k (multiplet back-projection)
   int koff;      // added to k for the A operand: spin s of a spin-polarised problem at s*Nk
   int spin;      // -1: write every alpha; 0/1: only alpha with alpha mod 2 == spin
+  int estg;      // launch-wide: mode-1 outputs staged per warp in shared memory, stored coalesced
+};
+
+// Tensor maps of a group launch (kernel parameter space, 384 bytes per problem).
+constexpr int TC_GROUP_MAX = 64;
+struct TcGroupMaps {
+  CUtensorMap m[TC_GROUP_MAX][3];  // A hi, A lo, B
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
@@ -188,9 +195,43 @@ __device__ __forceinline__ TileInfo decode(const TcParams& p, int t) {
   return ti;
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    k_lr_tc(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
-            const __grid_constant__ CUtensorMap tm_b, const TcParams p) {
+// Operand source of one launch: one problem (three tensor maps and p), or a
+// group of problems whose tile lists are concatenated (instance i owns tiles
+// tile0[i] .. tile0[i+1]-1 and has its own tensor maps and parameters).  The
+// per-tile work is the same either way.
+struct TcSingle {
+  const CUtensorMap *h, *l, *b;
+  const TcParams* p;
+  __device__ __forceinline__ int inst(int t, int* lt) const {
+    *lt = t;
+    return 0;
+  }
+  __device__ __forceinline__ const TcParams& par(int) const { return *p; }
+  __device__ __forceinline__ const CUtensorMap* map(int, int w) const { return w == 0 ? h : (w == 1 ? l : b); }
+};
+struct TcGroup {
+  const TcGroupMaps* maps;
+  const TcParams* tab;
+  const int* tile0;
+  int n;
+  __device__ __forceinline__ int inst(int t, int* lt) const {
+    int lo = 0, hi = n - 1;  // the last instance whose first tile is <= t
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tile0[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    *lt = t - tile0[lo];
+    return lo;
+  }
+  __device__ __forceinline__ const TcParams& par(int i) const { return tab[i]; }
+  __device__ __forceinline__ const CUtensorMap* map(int i, int w) const { return &maps->m[i][w]; }
+};
+
+// p: launch-wide values (tile count, pipeline depth, shared-memory stage layout
+// and accumulator stride for the largest N, tensor-memory columns, error flag).
+template <class Src>
+__device__ __forceinline__ void lr_tc_body(const TcParams& p, const Src& src) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
@@ -236,17 +277,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for (int s = 0; s < TC_MAX_STAGES; ++s) armed_phase[s] = -1;
       bool ok = true;
       for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
-        const TileInfo ti = decode(p, t);
+        int lt;
+        const int ii = src.inst(t, &lt);
+        const TcParams& tp = src.par(ii);
+        const TileInfo ti = decode(tp, lt);
         for (int c = ti.c0; c < ti.c1; ++c) {
           if (!mbar_wait(empty0 + 8 * stage, phase ^ 1, abort_flag, TC_WAIT_CYCLES)) {
             ok = false;
             break;
           }
           const uint32_t sbase = su32(smem + stage * stage_bytes);
-          mbar_expect_tx(full0 + 8 * stage, stage_bytes);
-          tma_load_3d(sbase, &tm_hi, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + p.koff);
-          tma_load_3d(sbase + a_bytes, &tm_lo, full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + p.koff);
-          tma_load_3d(sbase + 2 * a_bytes, &tm_b, full0 + 8 * stage, c * TC_BK, 0, p.bshared ? 0 : ti.k);
+          mbar_expect_tx(full0 + 8 * stage, 2 * a_bytes + (uint32_t)tp.ncol * TC_BK * 2);
+          tma_load_3d(sbase, src.map(ii, 0), full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + tp.koff);
+          tma_load_3d(sbase + a_bytes, src.map(ii, 1), full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + tp.koff);
+          tma_load_3d(sbase + 2 * a_bytes, src.map(ii, 2), full0 + 8 * stage, c * TC_BK, 0, tp.bshared ? 0 : ti.k);
           armed_phase[stage] = (int)phase;
           if (++stage == (uint32_t)S) {
             stage = 0;
@@ -275,7 +319,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       uint32_t last_phase = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
-        const TileInfo ti = decode(p, t);
+        int lt;
+        const int ii = src.inst(t, &lt);
+        const TcParams& tp = src.par(ii);
+        const TileInfo ti = decode(tp, lt);
         if (!mbar_wait(tempty0 + 8 * acc, acc_phase ^ 1, abort_flag, TC_WAIT_CYCLES)) {
           ok = false;
           break;
@@ -292,8 +339,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
           for (int kk = 0; kk < TC_BK / 16; ++kk) {
             const uint64_t bd = sw128_desc(sa + 2 * a_bytes + kk * 32);
-            umma_bf16(dt, sw128_desc(sa + kk * 32), bd, p.idesc, (c > ti.c0 || kk > 0) ? 1u : 0u);
-            umma_bf16(dt, sw128_desc(sa + a_bytes + kk * 32), bd, p.idesc, 1u);
+            umma_bf16(dt, sw128_desc(sa + kk * 32), bd, tp.idesc, (c > ti.c0 || kk > 0) ? 1u : 0u);
+            umma_bf16(dt, sw128_desc(sa + a_bytes + kk * 32), bd, tp.idesc, 1u);
           }
           umma_commit(empty0 + 8 * stage);
           last_stage = (int)stage;
@@ -322,11 +369,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // -------------------------------------------------------------- epilogue
     const int q = warp & 3;  // TMEM lane quadrant this warp may access
     const int row = q * 32 + lane;
-    const int na = p.na, g4 = 4 * na;
     uint32_t acc = 0, acc_phase = 0;
     float v[48];  // one vector's 4 Na columns
+    // mode-1 staging: this warp's 32 rows of (vector, alpha) values, row pitch wld
+    const int wld = p.ncol / 4 + 1;
+    float2* wst = reinterpret_cast<float2*>(smem + S * stage_bytes + 256) + (size_t)(warp - 2) * 32 * wld;
     for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-      const TileInfo ti = decode(p, t);
+      int lt;
+      const int ii = src.inst(t, &lt);
+      const TcParams& tp = src.par(ii);
+      const TileInfo ti = decode(tp, lt);
+      const int na = tp.na, g4 = 4 * na;
       if (!mbar_wait(tfull0 + 8 * acc, acc_phase, abort_flag, TC_WAIT_CYCLES)) {
         *abort_flag = 1;
         atomicOr(p.err, 4);
@@ -334,25 +387,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       tc_fence_after();
       const uint32_t ta = tmem_base + ((uint32_t)(q * 32) << 16) + acc * (uint32_t)p.ncol;
-      for (int vv = 0; vv < p.nv; ++vv) {
+      for (int vv = 0; vv < tp.nv; ++vv) {
         for (int c16 = 0; c16 < g4; c16 += 16) tmem_ld16(ta + vv * g4 + c16, v + c16);
         tmem_ld_wait();
-        if (p.mode == 1) {
+        if (tp.mode == 1) {
           const int x = ti.row0 + row;
-          if (x < p.nx) {
-            float2* o = p.phi + ((size_t)ti.k * p.nx + x) * (p.nv * na) + vv * na;
+          if (p.estg && tp.spin < 0) {
+            float2* wr = wst + lane * wld + vv * na;
+            for (int a = 0; a < na; ++a) wr[a] = make_float2(v[a] + v[2 * na + a], v[na + a] + v[3 * na + a]);
+          } else if (x < tp.nx) {
+            float2* o = tp.phi + ((size_t)ti.k * tp.nx + x) * (tp.nv * na) + vv * na;
             for (int a = 0; a < na; ++a)
-              if (p.spin < 0 || (a & 1) == p.spin)
+              if (tp.spin < 0 || (a & 1) == tp.spin)
                 o[a] = make_float2(v[a] + v[2 * na + a], v[na + a] + v[3 * na + a]);
           }
         } else {
           const int n = ti.row0 + row;
-          if (n < p.nb) {
-            double* pr = p.part + ((size_t)ti.sp * p.nvmax + vv) * 2 * p.npsi;
-            double* pim = pr + p.npsi;
+          if (n < tp.nb) {
+            double* pr = tp.part + ((size_t)ti.sp * tp.nvmax + vv) * 2 * tp.npsi;
+            double* pim = pr + tp.npsi;
             for (int a = 0; a < na; ++a) {
-              if (p.spin >= 0 && (a & 1) != p.spin) continue;
-              const size_t idx = (size_t)n + (size_t)p.nb * ((size_t)ti.k + (size_t)p.nk * a);
+              if (tp.spin >= 0 && (a & 1) != tp.spin) continue;
+              const size_t idx = (size_t)n + (size_t)tp.nb * ((size_t)ti.k + (size_t)tp.nk * a);
               pr[idx] = -((double)v[a] + (double)v[2 * na + a]);
               pim[idx] = -((double)v[na + a] + (double)v[3 * na + a]);
             }
@@ -361,6 +417,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       tc_fence_before();
       mbar_arrive(tempty0 + 8 * acc);
+      if (tp.mode == 1 && p.estg && tp.spin < 0) {
+        // the warp's rows are one contiguous run of phi: consecutive lanes store
+        // consecutive values
+        __syncwarp();
+        const int nt = tp.nv * na;
+        const int r0 = ti.row0 + q * 32;
+        const int rows = min(32, tp.nx - r0);
+        if (rows > 0) {
+          float2* dst = tp.phi + ((size_t)ti.k * tp.nx + r0) * nt;
+          const int dr = 32 / nt, dc = 32 - dr * nt;  // (row, column) step of 32 elements
+          int r = lane / nt, cc = lane - r * nt;
+          for (int e = lane; e < rows * nt; e += 32) {
+            dst[e] = wst[r * wld + cc];
+            r += dr;
+            cc += dc;
+            if (cc >= nt) {
+              cc -= nt;
+              ++r;
+            }
+          }
+        }
+        __syncwarp();
+      }
       acc ^= 1;
       if (acc == 0) acc_phase ^= 1;
     }
@@ -371,6 +450,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(p.tcols)
                  : "memory");
   }
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_lr_tc(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
+            const __grid_constant__ CUtensorMap tm_b, const __grid_constant__ TcParams p) {
+  const TcSingle src{&tm_hi, &tm_lo, &tm_b, &p};
+  lr_tc_body(p, src);
+}
+
+// All tiles of up to TC_GROUP_MAX problems in one persistent launch.
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_lr_tc_group(const __grid_constant__ TcGroupMaps maps, const __grid_constant__ TcParams p,
+                  const TcParams* __restrict__ tab, const int* __restrict__ tile0, int n) {
+  const TcGroup src{&maps, tab, tile0, n};
+  lr_tc_body(p, src);
 }
 
 // ---------------------------------------------------------- operand builders
@@ -565,13 +659,13 @@ __global__ void k_prep_b3(const double2* __restrict__ hamp, __nv_bfloat16* __res
 // blockIdx.y, b_i = sqrt(sum of partials), psi = h / b_i written in place, and
 // B1 rows of vector v built from allow o psi.  One thread per (n, k) covers
 // both K = n and K = Nb + n for every alpha.
-__global__ void __launch_bounds__(LZ_THREADS) k_norm_prep(const double* __restrict__ red2, int nblk, size_t rstride,
+__device__ __forceinline__ void norm_prep_body(const double* __restrict__ red2, int nblk, size_t rstride,
                             double* __restrict__ hbase, size_t vstride, size_t npsi,
                             const double* __restrict__ allow, __nv_bfloat16* __restrict__ b1, int nb,
                             int nk, int na, int ncol, int p1, double* __restrict__ rb_base,
-                            size_t cstride, const int* __restrict__ itp) {
+                            size_t cstride, const int* __restrict__ itp, int bx, int by, int nbx) {
   __shared__ double sh[32];
-  const int vv = blockIdx.y;
+  const int vv = by;
   const double* red = red2 + (size_t)vv * rstride;
   double s = 0.0;
   for (int i = threadIdx.x; i < nblk; i += blockDim.x) s += red[2 * i];
@@ -581,13 +675,13 @@ __global__ void __launch_bounds__(LZ_THREADS) k_norm_prep(const double* __restri
   double bb = 0.0;
   for (int i = 0; i < (int)(blockDim.x >> 5); ++i) bb += sh[i];
   const double b = sqrt(bb);
-  if (blockIdx.x == 0 && threadIdx.x == 0) rb_base[(size_t)vv * cstride + *itp] = b;
+  if (bx == 0 && threadIdx.x == 0) rb_base[(size_t)vv * cstride + *itp] = b;
   const double inv = 1.0 / b;
   double* hr = hbase + (size_t)vv * vstride;
   double* hi = hr + npsi;
   const int g4 = 4 * na;
   const int total = nb * nk;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+  for (int i = bx * blockDim.x + threadIdx.x; i < total; i += nbx * blockDim.x) {
     const int n = i % nb;
     const int k = i / nb;
     __nv_bfloat16* base = b1 + (size_t)k * ncol * p1 + (size_t)vv * g4 * p1;
@@ -615,15 +709,46 @@ __global__ void __launch_bounds__(LZ_THREADS) k_norm_prep(const double* __restri
   }
 }
 
+__global__ void __launch_bounds__(LZ_THREADS)
+    k_norm_prep(const double* __restrict__ red2, int nblk, size_t rstride, double* __restrict__ hbase,
+                size_t vstride, size_t npsi, const double* __restrict__ allow, __nv_bfloat16* __restrict__ b1,
+                int nb, int nk, int na, int ncol, int p1, double* __restrict__ rb_base, size_t cstride,
+                const int* __restrict__ itp) {
+  norm_prep_body(red2, nblk, rstride, hbase, vstride, npsi, allow, b1, nb, nk, na, ncol, p1, rb_base, cstride, itp,
+                 blockIdx.x, blockIdx.y, gridDim.x);
+}
+
+struct NormGroupArgs {
+  const double* red2;
+  int nblk;
+  size_t rstride;
+  double* hbase;
+  size_t vstride, npsi;
+  const double* allow;
+  __nv_bfloat16* b1;
+  int nb, nk, na, ncol, p1;
+  double* rb_base;
+  size_t cstride;
+  const int* itp;
+  int nv;
+};
+// grid (blocks per context, largest block of vectors, contexts)
+__global__ void __launch_bounds__(LZ_THREADS) k_norm_prep_group(const NormGroupArgs* __restrict__ tab) {
+  const NormGroupArgs& a = tab[blockIdx.z];
+  if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
+  norm_prep_body(a.red2, a.nblk, a.rstride, a.hbase, a.vstride, a.npsi, a.allow, a.b1, a.nb, a.nk, a.na, a.ncol,
+                 a.p1, a.rb_base, a.cstride, a.itp, blockIdx.x, blockIdx.y, a.nblk);
+}
+
 // B2[k][v*4Na + j][K2] from phi'[k][x][v*Na + a]:
 //   part 0 (Re out): K=(0,x) -> Re phi', K=(1,x) -> Im phi'
 //   part 1 (Im out): K=(0,x) -> Im phi', K=(1,x) -> -Re phi'
-__global__ void k_prep_b2(const float2* __restrict__ phi, __nv_bfloat16* __restrict__ b2, int nk,
-                          int nx, int na, int nv, int ncol, int p2) {
+__device__ __forceinline__ void prep_b2_body(const float2* __restrict__ phi, __nv_bfloat16* __restrict__ b2,
+                                             int nk, int nx, int na, int nv, int ncol, int p2, int bx, int nbx) {
   const int total = nk * nx;
   const int g4 = 4 * na;
   const int nt = na * nv;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+  for (int i = bx * blockDim.x + threadIdx.x; i < total; i += nbx * blockDim.x) {
     const int x = i % nx;
     const int k = i / nx;
     for (int t = 0; t < nt; ++t) {
@@ -646,6 +771,33 @@ __global__ void k_prep_b2(const float2* __restrict__ phi, __nv_bfloat16* __restr
       base[(size_t)(3 * na + a) * p2 + nx + x] = ln;
     }
   }
+}
+
+__global__ void k_prep_b2(const float2* __restrict__ phi, __nv_bfloat16* __restrict__ b2, int nk, int nx,
+                          int na, int nv, int ncol, int p2) {
+  prep_b2_body(phi, b2, nk, nx, na, nv, ncol, p2, blockIdx.x, gridDim.x);
+}
+
+struct B2GroupArgs {
+  const float2* phi;
+  __nv_bfloat16* b2;
+  int nk, nx, na, nv, ncol, p2;
+  int cta0, nctas;  // this context's CTAs in the grouped grid
+};
+// The last of n records whose first CTA is <= b (records ordered by cta0).
+template <class A>
+__device__ __forceinline__ int group_find(const A* __restrict__ tab, int n, int b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tab[mid].cta0 <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+__global__ void k_prep_b2_group(const B2GroupArgs* __restrict__ tab, int n) {
+  const B2GroupArgs& a = tab[group_find(tab, n, blockIdx.x)];
+  prep_b2_body(a.phi, a.b2, a.nk, a.nx, a.na, a.nv, a.ncol, a.p2, blockIdx.x - a.cta0, a.nctas);
 }
 
 // FP32 k-mesh transform, one CTA per x-point (ocn_kmesh_dft.cuh): generic meshes
@@ -672,6 +824,27 @@ __global__ void k_fft_cube_f32(float2* __restrict__ phi, const float* __restrict
   kmesh_convolve_cube<float, N, NTC>(phi + (size_t)blockIdx.y * nt, W, nx, blockIdx.x, nt, ld, buf, tw);
 }
 typedef void (*CubeFnF)(float2*, const float*, int, int, int, const float2*);
+
+struct FftGroupArgs {
+  float2* phi;
+  const float* W;
+  int nx, nt, ld;  // x-points, transforms per CTA, transforms per x-point
+  const float2* tw;
+  int cta0;        // first CTA of this context; its CTAs are (slice, x) = divmod(local, nx)
+};
+template <int N, int NTC>
+__global__ void k_fft_cube_f32_group(const FftGroupArgs* __restrict__ tab, int n) {
+  const FftGroupArgs& a = tab[group_find(tab, n, blockIdx.x)];
+  const int local = blockIdx.x - a.cta0;
+  const int x = local % a.nx, slice = local / a.nx;
+  extern __shared__ float2 fsm[];
+  float2* tw = fsm;
+  float2* buf = fsm + 3 * OCN_MAX_KDIM;
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = a.tw[i];
+  __syncthreads();
+  kmesh_convolve_cube<float, N, NTC>(a.phi + (size_t)slice * a.nt, a.W, a.nx, x, a.nt, a.ld, buf, tw);
+}
+typedef void (*CubeFnGroupF)(const FftGroupArgs*, int);
 
 __global__ void k_w_to_f32(const double* __restrict__ W, float* __restrict__ Wf, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -700,8 +873,9 @@ struct MixedLR {
   bool cube = false;        // cubic k-mesh: k_fft_cube_f32 instantiations apply
   size_t stage_bytes = 0;   // shared memory of one pipeline stage
   int max_stages = 1;       // deepest pipeline that fits the shared-memory budget
-  int cfg[6] = {0, 0, 0, 0, 0, 0};  // stages, GEMM2 K splits (requested), grid caps of GEMM1 / GEMM2,
-                                   // k-mesh transforms per CTA (0: all of an x-point), its threads (0: 128)
+  int cfg[7] = {0, 0, 0, 0, 0, 0, 0};  // stages, GEMM2 K splits (requested), grid caps of GEMM1 / GEMM2,
+                                      // k-mesh transforms per CTA (0: all of an x-point), its threads (0: 128),
+                                      // band->x output staging (1: when shared memory allows)
   size_t part_cap = 0;      // splits the partial-sum buffer holds
   // multiplet projector contractions (fg_combo) on the tensor cores
   bool mult_ready = false;
@@ -718,6 +892,16 @@ struct MixedLR {
 };
 
 namespace {
+
+// Shared memory of the band->x output staging: four epilogue warps, 32 rows of
+// ncol/4 + 1 complex values each.
+size_t estg_bytes(int ncol) { return (size_t)4 * 32 * (ncol / 4 + 1) * sizeof(float2); }
+
+size_t device_smem_optin(const ocn_ctx* c) {
+  int v = 0;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device) != cudaSuccess) return 0;
+  return (size_t)v;
+}
 
 int encode3d(ocn_ctx* c, EncodeTiledFn fn, CUtensorMap* m, void* base, uint64_t inner, uint64_t rows,
              uint64_t outer, uint64_t pitch_elems, uint32_t box_rows) {
@@ -823,7 +1007,13 @@ int mixed_init(ocn_ctx* c) {
   // full pipeline depth, one persistent CTA per SM at most
   int ks = (4 * c->sm_count + nk * g2.mt2 - 1) / (nk * g2.mt2);
   ks = std::max(1, std::min(ks, std::max(1, g2.nch / 4)));
-  const int cfg[6] = {stages, ks, c->sm_count, c->sm_count, 0, 256};  // 256-thread transforms: measured best on 8^3
+  // pipeline depth: the deepest that leaves room for the band->x output staging (when that is >= 2)
+  const int st_room = (int)((std::min<size_t>(TC_SMEM_BUDGET, device_smem_optin(c) - estg_bytes(ncol)) - 1024 - 256) /
+                            stage_bytes);
+  const int st_def = st_room >= 2 ? std::min(stages, st_room) : stages;
+  // 256-thread transforms: measured best on 8^3; output staging: measured faster for blocks of vectors,
+  // slightly slower for one vector
+  const int cfg[7] = {st_def, ks, c->sm_count, c->sm_count, 0, 256, nvmax > 1 ? 1 : 0};
   if ((rc = mixed_configure(c, cfg))) return rc;
   if (int rc_ = allow_max_smem(c, k_lr_tc)) return rc_;
   if (int rc_ = allow_max_smem(c, k_lr_fft_w_f32)) return rc_;
@@ -853,13 +1043,14 @@ int mixed_init(ocn_ctx* c) {
 // Tile configuration: cfg = {pipeline stages, K splits of GEMM2, persistent
 // grid cap of GEMM1, of GEMM2, k-mesh transforms per CTA (0 = all of an
 // x-point; a value that does not divide a block's count means all), threads of a
-// k-mesh transform CTA (128, 256 or 512; 0 = 128)}.  Grows the partial-sum
-// buffer when a configuration needs more splits.
-int mixed_configure(ocn_ctx* c, const int cfg[6]) {
+// k-mesh transform CTA (128, 256 or 512; 0 = 128), band->x output staging (0 or
+// 1; applied when the pipeline leaves the shared memory)}.  Grows the
+// partial-sum buffer when a configuration needs more splits.
+int mixed_configure(ocn_ctx* c, const int cfg[7]) {
   MixedLR* m = c->mixed;
   if (!m) return set_err(c, OCN_ERR_STATE, "mixed-precision state missing");
   if (cfg[0] < 1 || cfg[0] > m->max_stages || cfg[1] < 1 || cfg[2] < 1 || cfg[3] < 1 || cfg[4] < 0 ||
-      (cfg[5] != 0 && cfg[5] != 128 && cfg[5] != 256 && cfg[5] != 512))
+      (cfg[5] != 0 && cfg[5] != 128 && cfg[5] != 256 && cfg[5] != 512) || cfg[6] < 0 || cfg[6] > 1)
     return set_err(c, OCN_ERR_ARG, "bad tile configuration");
   TcParams& g1 = m->g1;
   TcParams& g2 = m->g2;
@@ -881,18 +1072,24 @@ int mixed_configure(ocn_ctx* c, const int cfg[6]) {
   c->lr_xsplit = g2.ks2;
   m->gm2.part = c->d_accpart + (size_t)g2.ks2 * c->part_stride;
   m->smem_bytes = 1024 + (size_t)cfg[0] * m->stage_bytes + 256;
+  {  // band->x outputs staged for coalesced stores when the pipeline leaves room
+    const size_t eb = estg_bytes(m->ncol);
+    const int on = (cfg[6] && m->smem_bytes + eb <= device_smem_optin(c)) ? 1 : 0;
+    g1.estg = g2.estg = m->gm1.estg = m->gm2.estg = on;
+    if (on) m->smem_bytes += eb;
+  }
   m->grid1 = std::min(g1.ntiles, std::min(cfg[2], c->sm_count));
   m->grid2 = std::min(g2.ntiles, std::min(cfg[3], c->sm_count));
   m->gm1.stages = m->gm2.stages = cfg[0];
   m->gridm1 = std::min(m->gm1.ntiles, std::min(cfg[2], c->sm_count));
   m->gridm2 = std::min(m->gm2.ntiles, std::min(cfg[3], c->sm_count));
-  for (int i = 0; i < 6; ++i) m->cfg[i] = cfg[i];
+  for (int i = 0; i < 7; ++i) m->cfg[i] = cfg[i];
   return OCN_OK;
 }
 
-int mixed_config(const ocn_ctx* c, int cfg[6]) {
+int mixed_config(const ocn_ctx* c, int cfg[7]) {
   if (!c->mixed) return OCN_ERR_STATE;
-  for (int i = 0; i < 6; ++i) cfg[i] = c->mixed->cfg[i];
+  for (int i = 0; i < 7; ++i) cfg[i] = c->mixed->cfg[i];
   return OCN_OK;
 }
 
@@ -900,8 +1097,9 @@ int mixed_config(const ocn_ctx* c, int cfg[6]) {
 // configurations (CUDA events on the context stream, reps launches each after
 // one warm-up) and keeps the fastest.  Two rounds: pipeline depth 2..max x
 // GEMM2 K splits {1, 2, 4, 8, current} x persistent grids of all SMs or half,
-// then the k-mesh transforms per CTA {all, 4, 12} under the round-one winner.
-int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int best_cfg[6]) {
+// then the k-mesh transforms per CTA {all, 4, 12} x their threads under the
+// round-one winner, then the band->x output staging switched.
+int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* current_ms, int best_cfg[7]) {
   MixedLR* m = c->mixed;
   if (!m || !m->ready) return set_err(c, OCN_ERR_STATE, "mixed-precision operands not built");
   if (nv < 1 || nv > m->nvmax) return set_err(c, OCN_ERR_ARG, "block size exceeds nvec");
@@ -914,8 +1112,8 @@ int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* curren
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  typedef std::array<int, 6> Cfg;
-  const Cfg def = {m->cfg[0], m->cfg[1], m->cfg[2], m->cfg[3], m->cfg[4], m->cfg[5]};
+  typedef std::array<int, 7> Cfg;
+  const Cfg def = {m->cfg[0], m->cfg[1], m->cfg[2], m->cfg[3], m->cfg[4], m->cfg[5], m->cfg[6]};
   double best = 1e300, dms = 0.0;
   Cfg bc = def;
   auto time_cfg = [&](const Cfg& a) -> int {
@@ -941,7 +1139,7 @@ int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* curren
   for (int st = std::min(2, m->max_stages); st <= m->max_stages; ++st)
     for (int ks : {1, 2, 4, 8, def[1]})
       for (int gc : {c->sm_count, std::max(1, c->sm_count / 2)}) {
-        const Cfg a = {st, ks, gc, gc, def[4], def[5]};
+        const Cfg a = {st, ks, gc, gc, def[4], def[5], def[6]};
         if (std::find(cand.begin(), cand.end(), a) == cand.end()) cand.push_back(a);
       }
   for (size_t i = 0; i < cand.size() && rc == OCN_OK; ++i) rc = time_cfg(cand[i]);
@@ -956,6 +1154,11 @@ int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* curren
         if (!same && rc == OCN_OK) rc = time_cfg(a);
       }
   }
+  if (rc == OCN_OK) {  // output staging on / off under the winner
+    Cfg a = bc;
+    a[6] = 1 - a[6];
+    rc = time_cfg(a);
+  }
   const int rf = mixed_configure(c, rc ? def.data() : bc.data());
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -965,7 +1168,7 @@ int mixed_autotune(ocn_ctx* c, int nv, int reps, double* best_ms, double* curren
   if (best_ms) *best_ms = best;
   if (current_ms) *current_ms = dms;
   if (best_cfg)
-    for (int i = 0; i < 6; ++i) best_cfg[i] = bc[i];
+    for (int i = 0; i < 7; ++i) best_cfg[i] = bc[i];
   return OCN_OK;
 }
 
@@ -1209,6 +1412,236 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
     }
   }
   return OCN_OK;
+}
+
+// ------------------------------------------------- grouped long-range term
+
+struct LrGroup {
+  struct TcLaunch {
+    TcGroupMaps maps;
+    TcParams p{};
+    TcParams* d_tab = nullptr;
+    int* d_tile0 = nullptr;
+    int ninst = 0, grid = 0;
+    size_t smem = 0;
+  };
+  struct FftClass {
+    CubeFnGroupF f = nullptr;
+    int kn = 0, tc = 0, th = 0;
+    size_t smem = 0;
+    std::vector<FftGroupArgs> h;
+    FftGroupArgs* d = nullptr;
+    int nctas = 0;
+  };
+  std::vector<TcLaunch> g1, g2;
+  std::vector<FftClass> fft;
+  B2GroupArgs* d_b2 = nullptr;
+  int b2ctas = 0;
+  NormGroupArgs* d_norm[3] = {nullptr, nullptr, nullptr};
+  int n = 0, nvmax = 1, nblk = 0;
+};
+
+std::string batch_group_refusal(const ocn_ctx* c) {
+  if (c->dims.precision != OCN_PREC_MIXED || !c->mixed || !c->mixed->ready) return "not mixed precision";
+  if (c->nspn != 1) return "spin-polarised";
+  if (!c->mixed->cube) return "k-mesh without a cubic transform";
+  if (!(c->sys.long_range && c->sys.nhflag[0] == 1)) return "long-range term off";
+  if (c->sys.mult && c->sys.nhflag[4] == 1 && c->have_mult) return "multiplet term on";
+  if (c->timing.on) return "timing on";
+  return "";
+}
+
+void lr_group_destroy(LrGroup* g) {
+  if (!g) return;
+  for (auto* v : {&g->g1, &g->g2})
+    for (auto& L : *v) {
+      if (L.d_tab) cudaFree(L.d_tab);
+      if (L.d_tile0) cudaFree(L.d_tile0);
+    }
+  for (auto& f : g->fft)
+    if (f.d) cudaFree(f.d);
+  if (g->d_b2) cudaFree(g->d_b2);
+  for (int r = 0; r < 3; ++r)
+    if (g->d_norm[r]) cudaFree(g->d_norm[r]);
+  delete g;
+}
+
+namespace {
+
+template <typename T>
+int upload(ocn_ctx* c, T** d, const std::vector<T>& h) {
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(d), h.size() * sizeof(T));
+  if (e == cudaSuccess) e = cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? OCN_OK : cuda_fail(c, e, "batched launch tables");
+}
+
+}  // namespace
+
+// Launch plan of the long-range term and the normalisation of every member:
+// the two contractions as persistent launches over the concatenated tile
+// lists (TC_GROUP_MAX members each), the k-mesh transforms as one launch per
+// (mesh, transforms per CTA, threads) class, the operand builders as one
+// launch.  Every member keeps its own tiling, so its results are those of its
+// own launches.
+int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out) {
+  *out = nullptr;
+  if (mem.empty()) return OCN_ERR_ARG;
+  ocn_ctx* c0 = mem[0].c;
+  LrGroup* g = new (std::nothrow) LrGroup();
+  if (!g) return set_err(c0, OCN_ERR_ALLOC, "host allocation failed");
+  g->n = (int)mem.size();
+  int ncol_max = 0;
+  for (const BatchMember& b : mem) {
+    ncol_max = std::max(ncol_max, b.c->mixed->ncol);
+    g->nvmax = std::max(g->nvmax, b.nv);
+    g->nblk = std::max(g->nblk, b.c->red_blocks);
+  }
+  const size_t a_bytes = (size_t)TC_BM * TC_BK * 2;
+  const size_t stage_bytes = 2 * a_bytes + (size_t)ncol_max * TC_BK * 2;
+  // deepest pipeline that still leaves room for the output staging
+  const size_t room = std::min<size_t>(TC_SMEM_BUDGET, device_smem_optin(c0) - estg_bytes(ncol_max));
+  int S = (int)std::min<size_t>(TC_MAX_STAGES, (room - 1024 - 256) / stage_bytes);
+  if (S < 2) S = (int)std::min<size_t>(TC_MAX_STAGES, (TC_SMEM_BUDGET - 1024 - 256) / stage_bytes);
+  uint32_t tcols = 32;
+  while ((int)tcols < 2 * ncol_max) tcols <<= 1;
+  int rc = OCN_OK;
+  if ((rc = allow_max_smem(c0, k_lr_tc_group))) {
+    lr_group_destroy(g);
+    return rc;
+  }
+  for (int mode = 1; mode <= 2 && rc == OCN_OK; ++mode) {
+    std::vector<LrGroup::TcLaunch>& dst = mode == 1 ? g->g1 : g->g2;
+    for (size_t c0i = 0; c0i < mem.size() && rc == OCN_OK; c0i += TC_GROUP_MAX) {
+      dst.emplace_back();
+      LrGroup::TcLaunch& L = dst.back();
+      std::vector<TcParams> tab;
+      std::vector<int> tile0;
+      int total = 0;
+      const size_t end = std::min(mem.size(), c0i + TC_GROUP_MAX);
+      for (size_t i = c0i; i < end; ++i) {
+        const MixedLR* m = mem[i].c->mixed;
+        TcParams q = mode == 1 ? m->g1 : m->g2;
+        q.nv = mem[i].nv;
+        q.koff = 0;
+        q.spin = -1;
+        tile0.push_back(total);
+        total += q.ntiles;
+        tab.push_back(q);
+        const int j = (int)(i - c0i);
+        L.maps.m[j][0] = mode == 1 ? m->tm_ua_hi : m->tm_ub_hi;
+        L.maps.m[j][1] = mode == 1 ? m->tm_ua_lo : m->tm_ub_lo;
+        L.maps.m[j][2] = mode == 1 ? m->tm_b1 : m->tm_b2;
+      }
+      tile0.push_back(total);
+      L.ninst = (int)tab.size();
+      L.p = tab[0];
+      L.p.ntiles = total;
+      L.p.ncol = ncol_max;
+      L.p.stages = S;
+      L.p.tcols = tcols;
+      L.p.err = mem[c0i].c->mixed->d_err;
+      L.grid = std::min(total, c0->sm_count);
+      L.smem = 1024 + (size_t)S * stage_bytes + 256;
+      bool want = false;
+      for (size_t i = c0i; i < end; ++i) want = want || mem[i].c->mixed->cfg[6] != 0;
+      L.p.estg = (want && L.smem + estg_bytes(ncol_max) <= device_smem_optin(c0)) ? 1 : 0;
+      if (L.p.estg) L.smem += estg_bytes(ncol_max);
+      if ((rc = upload(c0, &L.d_tab, tab)) == OCN_OK) rc = upload(c0, &L.d_tile0, tile0);
+    }
+  }
+  // k-mesh transforms, by instantiation class
+  for (size_t i = 0; i < mem.size() && rc == OCN_OK; ++i) {
+    ocn_ctx* c = mem[i].c;
+    const MixedLR* m = c->mixed;
+    const int ntot = c->na * mem[i].nv;
+    const int tc = (m->cfg[4] > 0 && ntot % m->cfg[4] == 0) ? m->cfg[4] : ntot;
+    const int th = m->cfg[5] ? m->cfg[5] : 128;
+    const int kn = c->dims.kmesh[0];
+    LrGroup::FftClass* cls = nullptr;
+    for (auto& f : g->fft)
+      if (f.kn == kn && f.tc == tc && f.th == th) cls = &f;
+    if (!cls) {
+      g->fft.emplace_back();
+      cls = &g->fft.back();
+      cls->kn = kn;
+      cls->tc = tc;
+      cls->th = th;
+      cls->smem = kmesh_cube_smem<float>(kn, tc);
+      OCN_CUBE_DISPATCH(k_fft_cube_f32_group, kn, tc, cls->f);
+      if (!cls->f) rc = set_err(c0, OCN_ERR_UNSUPPORTED, "no cubic transform for this k-mesh");
+      else rc = allow_max_smem(c0, cls->f);
+    }
+    FftGroupArgs a{m->phi, m->Wf, c->nx, tc, ntot, m->twf, cls->nctas};
+    cls->h.push_back(a);
+    cls->nctas += c->nx * (ntot / tc);
+  }
+  for (auto& f : g->fft)
+    if (rc == OCN_OK) rc = upload(c0, &f.d, f.h);
+  // phi' -> split-BF16 operand of the x->band contraction
+  if (rc == OCN_OK) {
+    std::vector<B2GroupArgs> b2;
+    for (const BatchMember& b : mem) {
+      const ocn_ctx* c = b.c;
+      const MixedLR* m = c->mixed;
+      const int total = c->nk * c->nx;
+      const int ctas = std::min((total + 255) / 256, 8 * c->sm_count);
+      b2.push_back(B2GroupArgs{m->phi, m->b2, c->nk, c->nx, c->na, b.nv, m->ncol, m->p2, g->b2ctas, ctas});
+      g->b2ctas += ctas;
+    }
+    rc = upload(c0, &g->d_b2, b2);
+  }
+  // normalisation + next psi operand, per buffer rotation
+  for (int r = 0; r < 3 && rc == OCN_OK; ++r) {
+    std::vector<NormGroupArgs> nt;
+    for (const BatchMember& b : mem) {
+      const ocn_ctx* c = b.c;
+      const MixedLR* m = c->mixed;
+      NormGroupArgs a;
+      a.red2 = c->d_red + 2 * c->red_blocks;
+      a.nblk = c->red_blocks;
+      a.rstride = (size_t)4 * c->red_blocks;
+      a.hbase = b.buf[(r + 2) % 3];
+      a.vstride = 2 * c->npsi;
+      a.npsi = c->npsi;
+      a.allow = c->d_allow;
+      a.b1 = m->b1;
+      a.nb = c->nb;
+      a.nk = c->nk;
+      a.na = c->na;
+      a.ncol = m->ncol;
+      a.p1 = m->p1;
+      a.rb_base = b.rb;
+      a.cstride = b.cstride;
+      a.itp = c->d_iter;
+      a.nv = b.nv;
+      nt.push_back(a);
+    }
+    rc = upload(c0, &g->d_norm[r], nt);
+  }
+  if (rc != OCN_OK) {
+    lr_group_destroy(g);
+    return rc;
+  }
+  *out = g;
+  return OCN_OK;
+}
+
+// Kernels one lr_group_apply + lr_group_norm launch.
+int lr_group_launches(const LrGroup* g) { return (int)(g->g1.size() + g->g2.size() + g->fft.size()) + 2; }
+
+int lr_group_apply(LrGroup* g, cudaStream_t s) {
+  for (auto& L : g->g1)
+    k_lr_tc_group<<<L.grid, TC_THREADS, L.smem, s>>>(L.maps, L.p, L.d_tab, L.d_tile0, L.ninst);
+  for (auto& f : g->fft) f.f<<<f.nctas, f.th, f.smem, s>>>(f.d, (int)f.h.size());
+  k_prep_b2_group<<<g->b2ctas, 256, 0, s>>>(g->d_b2, g->n);
+  for (auto& L : g->g2)
+    k_lr_tc_group<<<L.grid, TC_THREADS, L.smem, s>>>(L.maps, L.p, L.d_tab, L.d_tile0, L.ninst);
+  return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
+}
+
+int lr_group_norm(LrGroup* g, int rot, cudaStream_t s) {
+  k_norm_prep_group<<<dim3(g->nblk, g->nvmax, g->n), LZ_THREADS, 0, s>>>(g->d_norm[rot]);
+  return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
 }
 
 }  // namespace ocn

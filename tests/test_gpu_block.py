@@ -148,6 +148,26 @@ def test_block_size_checked(built):
         ctx.close()
 
 
+def test_output_staging_is_bit_identical(built):
+    """The band->x contraction's outputs stored through shared memory (tile
+    parameter 6) are the same values as stored directly."""
+    for name, nv in (("c1", 2), ("c3small", 2), ("tiny", 1)):
+        w = WL.make(name, seed=17)
+        rng = np.random.default_rng(8)
+        pr, pi = rng.standard_normal((nv, w.npsi)), rng.standard_normal((nv, w.npsi))
+        ctx = capi.Context(w, precision=capi.OCN_PREC_MIXED, nvec=nv)
+        try:
+            t = list(ctx.tiles())
+            out = []
+            for stg in (0, 1):
+                t[6] = stg
+                ctx.set_tiles(tuple(t))
+                out.append(ctx.apply_H_block(pr, pi))
+        finally:
+            ctx.close()
+        assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1]), name
+
+
 def test_autotune_and_tilings_keep_the_action(built):
     """Every tiling of the contractions gives the same H*psi to FP32 round-off,
     and the autotuner leaves a working, reported configuration."""
@@ -160,7 +180,7 @@ def test_autotune_and_tilings_keep_the_action(built):
     try:
         default = ctx.tiles()
         base_r, base_i = ctx.apply_H_block(pr, pi)
-        for tiles in [(2, 1, 152, 152, 0, 0), (3, 4, 76, 76, 4, 256), (default[0], 8, 152, 76, 0, 512)]:
+        for tiles in [(2, 1, 152, 152, 0, 0, 0), (3, 4, 76, 76, 4, 256, 1), (default[0], 8, 152, 76, 0, 512, 1)]:
             ctx.set_tiles(tiles)
             assert ctx.tiles() == tiles
             r, i = ctx.apply_H_block(pr, pi)
@@ -172,7 +192,7 @@ def test_autotune_and_tilings_keep_the_action(built):
             orr, oi = P.xact(pr[v], pi[v])
             assert _rel(r[v] + 1j * i[v], orr + 1j * oi) < 1e-4
         with pytest.raises(capi.OcnError) as e:
-            ctx.set_tiles((0, 1, 1, 1, 0, 0))
+            ctx.set_tiles((0, 1, 1, 1, 0, 0, 0))
         assert e.value.code == capi.OCN_ERR_ARG
         # the Haydock graph is rebuilt for the new tiling
         ra, ia, rb, done = ctx.haydock_block(9, pr / np.linalg.norm(pr[0] + 1j * pi[0]),
