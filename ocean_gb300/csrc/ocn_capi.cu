@@ -1010,7 +1010,7 @@ int ocn_haydock_batch(ocn_ctx* const* ctxs, int nctx, const int* nv, const doubl
         if (e == cudaSuccess && rc == OCN_OK) {
           cudaGraphNode_t node;
           e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, child);
-          kernels[grouped[0]] = 3 * (3 + lr_group_launches(lr));
+          kernels[grouped[0]] = 3 * (lz_group_launches(lz) + lr_group_launches(lr));
         }
         if (child) cudaGraphDestroy(child);
       }

@@ -273,6 +273,7 @@ std::string batch_group_refusal(const ocn_ctx* c);
 int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out);
 int lz_group_advance(LzGroup* g, cudaStream_t s);
 int lz_group_step(LzGroup* g, int rot, cudaStream_t s);
+int lz_group_launches(const LzGroup* g);
 void lz_group_destroy(LzGroup* g);
 int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out);
 int lr_group_apply(LrGroup* g, cudaStream_t s);

@@ -339,23 +339,17 @@ __global__ void __launch_bounds__(LZ_THREADS)
                        backwards, oldr, oldi, rb_base, itp, red, bs, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
-// The combine + first Lanczos stage of several contexts in one launch: grid
-// (blocks per context, largest block of vectors, contexts); every context keeps
-// the block partition (and so the reduction order) of its own launches.
+// The combine + first Lanczos stage of several contexts of one (Na, spin-orbit)
+// class in one launch: grid (blocks per context, largest block of vectors,
+// contexts); every context keeps the block partition (and so the reduction
+// order) of its own launches.
+template <int NA, bool SO>
 __global__ void __launch_bounds__(LZ_THREADS) k_combine_group(const CombineArgs* __restrict__ tab) {
   const CombineArgs& a = tab[blockIdx.z];
   if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
-#define OCN_COMBINE_ARGS                                                                                    \
-  a.pr, a.pi, a.er, a.ei, a.allow, a.acc, a.part, a.nparts, a.so, a.outr, a.outi, a.nbk, a.na, a.npsi, a.use_e0, \
-      a.use_so, a.backwards, a.oldr, a.oldi, a.rb_base, a.itp, a.red, a.bs, blockIdx.x, blockIdx.y, a.nblk
-  if (a.na == 4) {
-    if (a.use_so) combine_body<4, true>(OCN_COMBINE_ARGS);
-    else combine_body<4, false>(OCN_COMBINE_ARGS);
-  } else {
-    if (a.use_so) combine_body<12, true>(OCN_COMBINE_ARGS);
-    else combine_body<12, false>(OCN_COMBINE_ARGS);
-  }
-#undef OCN_COMBINE_ARGS
+  combine_body<NA, SO>(a.pr, a.pi, a.er, a.ei, a.allow, a.acc, a.part, a.nparts, a.so, a.outr, a.outi, a.nbk,
+                       a.na, a.npsi, a.use_e0, a.use_so, a.backwards, a.oldr, a.oldi, a.rb_base, a.itp, a.red,
+                       a.bs, blockIdx.x, blockIdx.y, a.nblk);
 }
 
 // Sum of nb partial pairs in a fixed order, done identically by every block.
@@ -1167,6 +1161,12 @@ int vec_update_dev(ocn_ctx* c, int nvec, const double2* d_coef, const double* co
 
 struct LzGroup {
   int n = 0, nvmax = 1, nblk = 0;
+  // members ordered by (Na, spin-orbit) class; class c covers records cls[c].first ..
+  struct Cls {
+    int na, so, first, count;
+  };
+  std::vector<Cls> cls;
+  std::vector<int> order;  // member index of each record
   CombineArgs* d_comb[3] = {nullptr, nullptr, nullptr};
   Lanczos2Args* d_lz2[3] = {nullptr, nullptr, nullptr};
   int** d_iters = nullptr;
@@ -1201,9 +1201,23 @@ int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out) {
     g->nblk = std::max(g->nblk, b.c->red_blocks);
     iters.push_back(b.c->d_iter);
   }
+  for (int na : {4, 12})
+    for (int so : {0, 1}) {
+      LzGroup::Cls k{na, so, (int)g->order.size(), 0};
+      for (size_t i = 0; i < mem.size(); ++i) {
+        const ocn_ctx* c = mem[i].c;
+        const int cso = (c->sys.mult && c->sys.nhflag[5] == 1 && c->have_so) ? 1 : 0;
+        if (c->na == na && cso == so) {
+          g->order.push_back((int)i);
+          ++k.count;
+        }
+      }
+      if (k.count) g->cls.push_back(k);
+    }
+  if (g->order.size() != mem.size()) rc = set_err(c0, OCN_ERR_UNSUPPORTED, "batched context with Na other than 4, 12");
   for (int r = 0; r < 3 && rc == OCN_OK; ++r) {
-    for (size_t i = 0; i < mem.size(); ++i) {
-      const BatchMember& b = mem[i];
+    for (size_t i = 0; i < g->order.size(); ++i) {
+      const BatchMember& b = mem[g->order[i]];
       ocn_ctx* c = b.c;
       const size_t n = c->npsi;
       const double* old = b.buf[r % 3];
@@ -1275,6 +1289,9 @@ int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out) {
   return OCN_OK;
 }
 
+// Kernels of one lz_group_advance + lz_group_step.
+int lz_group_launches(const LzGroup* g) { return 2 + (int)g->cls.size(); }
+
 int lz_group_advance(LzGroup* g, cudaStream_t s) {
   k_advance_group<<<(g->n + 127) / 128, 128, 0, s>>>(g->d_iters, g->n);
   return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
@@ -1283,9 +1300,19 @@ int lz_group_advance(LzGroup* g, cudaStream_t s) {
 // combine (E, masks, long-range parts, -b psi_old, <h|psi>) and stage 2 for
 // every member, buffer rotation rot
 int lz_group_step(LzGroup* g, int rot, cudaStream_t s) {
+  for (const LzGroup::Cls& k : g->cls) {
+    const dim3 gc(g->nblk, g->nvmax, k.count);
+    const CombineArgs* t = g->d_comb[rot] + k.first;
+    if (k.na == 4) {
+      if (k.so) k_combine_group<4, true><<<gc, LZ_THREADS, 0, s>>>(t);
+      else k_combine_group<4, false><<<gc, LZ_THREADS, 0, s>>>(t);
+    } else {
+      if (k.so) k_combine_group<12, true><<<gc, LZ_THREADS, 0, s>>>(t);
+      else k_combine_group<12, false><<<gc, LZ_THREADS, 0, s>>>(t);
+    }
+    if (cudaGetLastError() != cudaSuccess) return OCN_ERR_CUDA;
+  }
   const dim3 grid(g->nblk, g->nvmax, g->n);
-  k_combine_group<<<grid, LZ_THREADS, 0, s>>>(g->d_comb[rot]);
-  if (cudaGetLastError() != cudaSuccess) return OCN_ERR_CUDA;
   k_lanczos2_group<<<grid, LZ_THREADS, 0, s>>>(g->d_lz2[rot]);
   return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
 }
