@@ -393,6 +393,56 @@ int ocn_write_abs_gmres(const char* path, int nomega, const double* energies_ev,
 int ocn_output_filename(const char* kind, const char* calc_type, const char* elname, int indx,
                         const char* corelevel, int photon, char* buf, size_t len);
 
+/* ------------------------------------------------ pipeline input files */
+
+/* Files written by the OCEAN pipeline for ocean.x, read as ocean.x reads them.
+ * Sequential unformatted files are read with 4-byte record frames (gfortran,
+ * ifort).  All return OCN_ERR_ARG on a missing, short or malformed file. */
+
+/* u2.dat (OCEAN_bloch.f90:515-575, the 'old' Bloch-state format): per spin, per
+ * k-point (kmesh loops iq1, iq2, iq3), nband_file bands of nx*ny*nz records
+ * (ix, iy, iz with iz fastest), each three integers and the real and imaginary
+ * part.  first[] is the first band read per (k-point, spin) (0-based: the
+ * occupied bands the reference skips, ivh2 - ivl + 1 in its notation; nfirst = 1
+ * for one value everywhere, else nkpts*nspn values, k fastest); nbd bands are
+ * read from there.  re/im receive re_bloch_state(nbd, nkpts, nx*ny*nz, nspn)
+ * with x = ix + nx*(iy + ny*iz), before the lrLOAD phase (ocn_set_bloch). */
+int ocn_read_u2dat(const char* path, int nx, int ny, int nz, int nkpts, int nspn, int nband_file,
+                   const int* first, int nfirst, int nbd, double* re, double* im);
+
+/* rpottrim.z<El><idx>_n<nn>l<ll> (long_range.f90:1689-1698): a header record
+ * (a word, nptab) then nptab records ptab rtab.  With ptab and rtab NULL only
+ * *nptab is returned; otherwise up to cap samples (OCN_ERR_ARG if more). */
+int ocn_read_rpottrim(const char* path, int* nptab, double* ptab, double* rtab, int cap);
+
+/* wvfcninfo / wvfvainfo (OCEAN_energies.f90:629-689): header (nbd, nq) or, with
+ * two spins, (nbd, nq, nspn); then energies(nbd, nq, nspn) as written (the
+ * pipeline's units; stubby, OCEAN_energies.f90:829-888, turns them into the
+ * energies of ocn_set_energies).  e NULL: header only. */
+int ocn_read_energies(const char* path, int nspn, int* nbd, int* nq, double* e, size_t cap);
+
+/* Projector coefficients (OCEAN_multiplet.f90:414-463): stream = 1 for the
+ * parallel file parcksc.* (three integers, the second nbd*nkpts, then complex
+ * pcTemp(nptot, nbd, nkpts, nspn); bands beyond nb are dropped), stream = 0 for
+ * the legacy cksc.* (two records skipped, then pcr and pci).  pcr/pci receive
+ * (nptot, nb, nkpts, nspn). */
+int ocn_read_cks(const char* path, int stream, int nptot, int nb, int nkpts, int nspn, double* pcr,
+                 double* pci);
+/* The reordering of OCEAN_multiplet.f90:466-481 into the mpcr/mpci layout of
+ * ocn_mult_data (Nb, Nk, npmax, 2*lmax+1, lmax-lmin+1, nspn); projector ip runs
+ * over l, m = -l..l, nu.  Unused (nu, m) slots are zero. */
+int ocn_cks_to_mpc(int lmin, int lmax, const int* nproj, int nb, int nkpts, int nspn, const double* pcr,
+                   const double* pci, double* mpcr, double* mpci);
+/* cmel<l> (OCEAN_multiplet.f90:489-500): nproj*nproj list-directed values into
+ * mpm(1:nproj, 1:nproj) of that l, column-major as the reference fills it. */
+int ocn_read_cmel(const char* path, int nproj, double* mpm);
+
+/* Input file names as ocean.x forms them: kind "rpottrim" (uses n, l),
+ * "cks" / "parcks" (calc_type "XES" gives cksv.), "cmel" (uses l), "energies"
+ * (calc_type "VAL" gives wvfvainfo). */
+int ocn_input_filename(const char* kind, const char* calc_type, const char* elname, int indx, int n, int l,
+                       char* buf, size_t len);
+
 /* --------------------------------------------------------------- counters */
 
 /* Number of kernels this context launched since creation (for accounting). */

@@ -83,6 +83,8 @@ EXPORTS = [
     "ocn_haydock_block", "ocn_haydock_block_dev", "ocn_spectrum_cf_noalloc", "ocn_gmres_dev",
     "ocn_gmres_vjp", "ocn_w2_vjp", "ocn_haydock_batch", "ocn_autotune", "ocn_set_tiles", "ocn_get_tiles",
     "ocn_read_bse_in", "ocn_write_abslanc", "ocn_write_absspct", "ocn_write_abs_gmres", "ocn_output_filename",
+    "ocn_read_u2dat", "ocn_read_rpottrim", "ocn_read_energies", "ocn_read_cks", "ocn_cks_to_mpc", "ocn_read_cmel",
+    "ocn_input_filename",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -517,6 +519,71 @@ def output_filename(kind: str, calc_type: str, elname: str, indx: int, corelevel
     check(load().ocn_output_filename(kind.encode(), calc_type.encode(), elname.encode(), indx,
                                      corelevel.encode(), photon, buf, 64))
     return buf.value.decode()
+
+
+def input_filename(kind: str, elname: str, indx: int, n: int = 0, l: int = 0, calc_type: str = "XAS") -> str:
+    buf = C.create_string_buffer(64)
+    check(load().ocn_input_filename(kind.encode(), calc_type.encode(), elname.encode(), indx, n, l, buf, 64))
+    return buf.value.decode()
+
+
+def read_u2dat(path: str, nx: int, ny: int, nz: int, nkpts: int, nspn: int, nband_file: int, first, nbd: int):
+    """u2.dat -> (re, im) of shape (nspn, Nx, nkpts, nbd) in C order, i.e. the
+    Fortran re_bloch_state(nbd, nkpts, Nx, nspn).  first: one int or one per
+    (k-point, spin), k fastest."""
+    f = np.ascontiguousarray(np.atleast_1d(first), dtype=np.int32)
+    nxyz = nx * ny * nz
+    re = np.zeros((nspn, nxyz, nkpts, nbd))
+    im = np.zeros_like(re)
+    check(load().ocn_read_u2dat(path.encode(), nx, ny, nz, nkpts, nspn, nband_file, f.ctypes.data_as(IP), len(f),
+                                nbd, _dp(re), _dp(im)))
+    return re, im
+
+
+def read_rpottrim(path: str):
+    lib = load()
+    n = C.c_int(0)
+    check(lib.ocn_read_rpottrim(path.encode(), C.byref(n), None, None, 0))
+    p, r = np.zeros(n.value), np.zeros(n.value)
+    check(lib.ocn_read_rpottrim(path.encode(), C.byref(n), _dp(p), _dp(r), n.value))
+    return p, r
+
+
+def read_energies(path: str, nspn: int = 1):
+    """wvfcninfo -> energies of shape (nspn, nq, nbd) in C order (Fortran (nbd, nq, nspn))."""
+    lib = load()
+    nbd, nq = C.c_int(0), C.c_int(0)
+    check(lib.ocn_read_energies(path.encode(), nspn, C.byref(nbd), C.byref(nq), None, C.c_size_t(0)))
+    e = np.zeros((nspn, nq.value, nbd.value))
+    check(lib.ocn_read_energies(path.encode(), nspn, C.byref(nbd), C.byref(nq), _dp(e), C.c_size_t(e.size)))
+    return e
+
+
+def read_cks(path: str, stream: bool, nptot: int, nb: int, nkpts: int, nspn: int = 1):
+    """cksc / parcksc -> (pcr, pci) of shape (nspn, nkpts, nb, nptot) in C order."""
+    pr, pi = np.zeros((nspn, nkpts, nb, nptot)), np.zeros((nspn, nkpts, nb, nptot))
+    check(load().ocn_read_cks(path.encode(), int(stream), nptot, nb, nkpts, nspn, _dp(pr), _dp(pi)))
+    return pr, pi
+
+
+def cks_to_mpc(lmin: int, lmax: int, nproj, pcr, pci):
+    """(nspn, nkpts, nb, nptot) coefficients -> mpcr/mpci of shape
+    (nspn, lmax-lmin+1, 2*lmax+1, npmax, nkpts, nb) in C order."""
+    nspn, nkpts, nb, _ = pcr.shape
+    npj = np.ascontiguousarray(nproj, dtype=np.int32)
+    npmax = int(npj.max())
+    shape = (nspn, lmax - lmin + 1, 2 * lmax + 1, npmax, nkpts, nb)
+    mr, mi = np.zeros(shape), np.zeros(shape)
+    check(load().ocn_cks_to_mpc(lmin, lmax, npj.ctypes.data_as(IP), nb, nkpts, nspn, _dp(_f64(pcr)), _dp(_f64(pci)),
+                                _dp(mr), _dp(mi)))
+    return mr, mi
+
+
+def read_cmel(path: str, nproj: int) -> np.ndarray:
+    """cmel<l> -> mpm block (nproj, nproj) as mpm[nu', nu] (C index [nu][nu'] of the Fortran column-major fill)."""
+    m = np.zeros((nproj, nproj))
+    check(load().ocn_read_cmel(path.encode(), nproj, _dp(m)))
+    return m
 
 
 def redtrid(n: int, ra, rb) -> np.ndarray:

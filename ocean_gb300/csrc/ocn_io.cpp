@@ -1,10 +1,16 @@
-// ocn_io.cpp -- the reference's text interface for this path: the bse.in
+// ocn_io.cpp -- the reference's file interface for this path: the bse.in
 // solver settings (OCEAN2/OCEAN_driver.f90:66-70, OCEAN_haydock.f90:2109-2118,
 // OCEAN_gmres.f90:84-124) and the abslanc / absspct / abs.gmres outputs
 // (OCEAN_haydock.f90:1831-1892,1922-1985,2318-2358; OCEAN_gmres.f90:864-869),
 // written byte for byte as the Fortran edit descriptors there produce them, so
-// that existing post-processing reads the GPU results unchanged.
+// that existing post-processing reads the GPU results unchanged; and the
+// pipeline files the hot path's operator data come from: u2.dat
+// (OCEAN_bloch.f90:515-575), rpottrim.z* (long_range.f90:1689-1698),
+// wvfcninfo / wvfvainfo (OCEAN_energies.f90:629-689), cksc.* / parcksc.*
+// (OCEAN_multiplet.f90:414-481) and cmel<l> (OCEAN_multiplet.f90:489-500).
+#include <algorithm>
 #include <cctype>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -203,6 +209,82 @@ void put(FILE* f, const std::string& s) {
   std::fputc('\n', f);
 }
 
+// Fortran sequential unformatted file as gfortran and ifort write it: each
+// record is framed by its payload length as a 4-byte little-endian integer,
+// before and after.  Read through a large buffer (u2.dat holds one record per
+// (band, k-point, x-point)).
+class SeqFile {
+ public:
+  explicit SeqFile(const char* path) : f_(std::fopen(path, "rb")), buf_(1 << 22) {}
+  ~SeqFile() {
+    if (f_) std::fclose(f_);
+  }
+  bool ok() const { return f_ != nullptr; }
+  // next record's payload: pointer valid until the next call; false at the end
+  // of the file or on a broken frame
+  bool next(const unsigned char** data, uint32_t* n) {
+    uint32_t n1 = 0, n2 = 0;
+    if (!take(&n1, 4)) return false;
+    if (n1 > (1u << 31)) return false;  // not a record length
+    const unsigned char* p = view(n1);
+    if (!p) return false;
+    if (!take(&n2, 4) || n1 != n2) return false;
+    *data = p;
+    *n = n1;
+    return true;
+  }
+  bool skip() {
+    const unsigned char* d;
+    uint32_t n;
+    return next(&d, &n);
+  }
+
+ private:
+  bool fill(size_t need) {  // at least need bytes buffered
+    if (end_ - pos_ >= need) return true;
+    std::memmove(buf_.data(), buf_.data() + pos_, end_ - pos_);
+    end_ -= pos_;
+    pos_ = 0;
+    if (need > buf_.size()) buf_.resize(need);
+    while (end_ < need) {
+      const size_t got = std::fread(buf_.data() + end_, 1, buf_.size() - end_, f_);
+      if (got == 0) return false;
+      end_ += got;
+    }
+    return true;
+  }
+  bool take(void* out, size_t n) {
+    if (!fill(n)) return false;
+    std::memcpy(out, buf_.data() + pos_, n);
+    pos_ += n;
+    return true;
+  }
+  const unsigned char* view(size_t n) {
+    if (!fill(n)) return nullptr;
+    const unsigned char* p = buf_.data() + pos_;
+    pos_ += n;
+    return p;
+  }
+  FILE* f_;
+  std::vector<unsigned char> buf_;
+  size_t pos_ = 0, end_ = 0;
+};
+
+template <typename T>
+T load(const unsigned char* p) {
+  T v;
+  std::memcpy(&v, p, sizeof v);
+  return v;
+}
+
+// Fortran A2 of a character(len=2) variable: short names padded on the right.
+std::string a2(const char* s) {
+  std::string t(s);
+  t.resize(2, ' ');
+  return t;
+}
+
+
 }  // namespace
 
 extern "C" {
@@ -347,6 +429,216 @@ int ocn_output_filename(const char* kind, const char* calc_type, const char* eln
     return set_err(nullptr, OCN_ERR_ARG, "site index or photon out of the I4.4 / I2.2 range");
   std::snprintf(tail, sizeof tail, ".%04d_%s_%02d", indx, fmt_a(corelevel, 2).c_str(), photon);
   const std::string name = pre + fmt_a(elname, 2) + tail;
+  if (name.size() + 1 > len) return set_err(nullptr, OCN_ERR_ARG, "buffer too small");
+  std::memcpy(buf, name.c_str(), name.size() + 1);
+  return OCN_OK;
+}
+
+int ocn_read_u2dat(const char* path, int nx, int ny, int nz, int nkpts, int nspn, int nband_file,
+                   const int* first, int nfirst, int nbd, double* re, double* im) {
+  if (!path || !first || !re || !im) return set_err(nullptr, OCN_ERR_ARG, "ocn_read_u2dat: null argument");
+  if (nx < 1 || ny < 1 || nz < 1 || nkpts < 1 || nspn < 1 || nbd < 1 || nband_file < nbd ||
+      (nfirst != 1 && nfirst != nkpts * nspn))
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_read_u2dat: bad dimensions");
+  for (int i = 0; i < nfirst; ++i)
+    if (first[i] < 0 || first[i] + nbd > nband_file)
+      return set_err(nullptr, OCN_ERR_ARG, "ocn_read_u2dat: band window outside the file's bands");
+  SeqFile f(path);
+  if (!f.ok()) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  const size_t nxyz = (size_t)nx * ny * nz;
+  // OCEAN_bloch.f90:534-575: per spin, per k-point (iq1, iq2, iq3 nested), the
+  // skipped bands, then nbd bands of records (ix, iy, iz with iz fastest) each
+  // holding three integers and the real and imaginary parts, then the rest
+  for (int s = 0; s < nspn; ++s)
+    for (int iq = 0; iq < nkpts; ++iq) {
+      const int f0 = first[nfirst == 1 ? 0 : iq + nkpts * s];
+      for (size_t r = 0; r < (size_t)f0 * nxyz; ++r)
+        if (!f.skip()) return set_err(nullptr, OCN_ERR_ARG, "u2.dat ends early or a record frame is broken");
+      for (int b = 0; b < nbd; ++b)
+        for (int ix = 0; ix < nx; ++ix)
+          for (int iy = 0; iy < ny; ++iy)
+            for (int iz = 0; iz < nz; ++iz) {
+              const unsigned char* d;
+              uint32_t n;
+              if (!f.next(&d, &n)) return set_err(nullptr, OCN_ERR_ARG, "u2.dat ends early or a record frame is broken");
+              if (n < 28) return set_err(nullptr, OCN_ERR_ARG, "u2.dat record shorter than 3 integers + 2 reals");
+              // re_bloch_state(band, k, x, spin), x = ix + nx*(iy + ny*iz) (the transpose loop, :577-587)
+              const size_t x = (size_t)ix + (size_t)nx * ((size_t)iy + (size_t)ny * iz);
+              const size_t o = (size_t)b + (size_t)nbd * ((size_t)iq + (size_t)nkpts * (x + nxyz * s));
+              re[o] = load<double>(d + 12);
+              im[o] = load<double>(d + 20);
+            }
+      for (size_t r = 0; r < (size_t)(nband_file - f0 - nbd) * nxyz; ++r)
+        if (!f.skip()) return set_err(nullptr, OCN_ERR_ARG, "u2.dat ends early or a record frame is broken");
+    }
+  return OCN_OK;
+}
+
+int ocn_read_rpottrim(const char* path, int* nptab, double* ptab, double* rtab, int cap) {
+  if (!path || !nptab) return set_err(nullptr, OCN_ERR_ARG, "ocn_read_rpottrim: null argument");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  // long_range.f90:1694-1698: read(99,*) dumc, nptab; then nptab records ptab, rtab
+  std::vector<std::string> v;
+  int n = 0;
+  int rc = OCN_OK;
+  if (!ld_read(f, 2, &v) || !ld_int(v[1], &n) || n < 1) rc = set_err(nullptr, OCN_ERR_ARG, "rpottrim: bad header");
+  if (rc == OCN_OK) {
+    *nptab = n;
+    if (ptab || rtab) {
+      if (n > cap) rc = set_err(nullptr, OCN_ERR_ARG, "rpottrim: table longer than cap");
+      for (int i = 0; i < n && rc == OCN_OK; ++i) {
+        double p = 0.0, r = 0.0;
+        if (!ld_read(f, 2, &v) || !ld_real(v[0], &p) || !ld_real(v[1], &r))
+          rc = set_err(nullptr, OCN_ERR_ARG, "rpottrim: bad table record");
+        if (ptab) ptab[i] = p;
+        if (rtab) rtab[i] = r;
+      }
+    }
+  }
+  std::fclose(f);
+  return rc;
+}
+
+int ocn_read_energies(const char* path, int nspn, int* nbd, int* nq, double* e, size_t cap) {
+  if (!path || !nbd || !nq || (nspn != 1 && nspn != 2))
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_read_energies: bad argument");
+  SeqFile f(path);
+  if (!f.ok()) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  // OCEAN_energies.f90:657-676: (nbd, nq) or, with two spins, (nbd, nq, nspn); then energies(nbd, nq, nspn)
+  const unsigned char* d;
+  uint32_t n;
+  if (!f.next(&d, &n) || n < (nspn == 2 ? 12u : 8u)) return set_err(nullptr, OCN_ERR_ARG, "energy file: bad header");
+  *nbd = load<int32_t>(d);
+  *nq = load<int32_t>(d + 4);
+  if (nspn == 2 && load<int32_t>(d + 8) != 2) return set_err(nullptr, OCN_ERR_ARG, "energy file: spin mismatch");
+  if (*nbd < 1 || *nq < 1) return set_err(nullptr, OCN_ERR_ARG, "energy file: bad header");
+  if (!e) return OCN_OK;
+  const size_t cnt = (size_t)*nbd * *nq * nspn;
+  if (cnt > cap) return set_err(nullptr, OCN_ERR_ARG, "energy file: more values than cap");
+  if (!f.next(&d, &n) || n < cnt * sizeof(double)) return set_err(nullptr, OCN_ERR_ARG, "energy file: bad energy record");
+  std::memcpy(e, d, cnt * sizeof(double));
+  return OCN_OK;
+}
+
+int ocn_read_cks(const char* path, int stream, int nptot, int nb, int nkpts, int nspn, double* pcr, double* pci) {
+  if (!path || !pcr || !pci || nptot < 1 || nb < 1 || nkpts < 1 || nspn < 1)
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_read_cks: bad argument");
+  const size_t per_b = (size_t)nptot;
+  if (stream) {
+    // parcksc.*: stream access, three integers (the second nbd*nkpts) then
+    // complex(DP) pcTemp(nptot, nbd, nkpts, nspn) (OCEAN_multiplet.f90:430-452)
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+    int32_t h[3];
+    int rc = OCN_OK;
+    if (std::fread(h, 4, 3, f) != 3) rc = set_err(nullptr, OCN_ERR_ARG, "cks: short header");
+    const int nbd = rc == OCN_OK ? h[1] / nkpts : 0;
+    if (rc == OCN_OK && (h[1] != nbd * nkpts || nbd < nb)) rc = set_err(nullptr, OCN_ERR_ARG, "Badly formed cks");
+    std::vector<double> band(2 * per_b);
+    for (int s = 0; s < nspn && rc == OCN_OK; ++s)
+      for (int k = 0; k < nkpts && rc == OCN_OK; ++k)
+        for (int b = 0; b < nbd && rc == OCN_OK; ++b) {
+          if (std::fread(band.data(), sizeof(double), 2 * per_b, f) != 2 * per_b) {
+            rc = set_err(nullptr, OCN_ERR_ARG, "cks: file ends early");
+            break;
+          }
+          if (b >= nb) continue;  // only the first num_bands are used (:444-450)
+          const size_t o = per_b * ((size_t)b + (size_t)nb * ((size_t)k + (size_t)nkpts * s));
+          for (size_t p = 0; p < per_b; ++p) {
+            pcr[o + p] = band[2 * p];
+            pci[o + p] = band[2 * p + 1];
+          }
+        }
+    std::fclose(f);
+    return rc;
+  }
+  // cksc.*: two records skipped, then pcr and pci (nptot, nb, nkpts, nspn) (:456-461)
+  SeqFile f(path);
+  if (!f.ok()) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  const size_t cnt = per_b * nb * nkpts * nspn;
+  if (!f.skip() || !f.skip()) return set_err(nullptr, OCN_ERR_ARG, "cks: missing header records");
+  const unsigned char* d;
+  uint32_t n;
+  for (double* out : {pcr, pci}) {
+    if (!f.next(&d, &n) || n < cnt * sizeof(double)) return set_err(nullptr, OCN_ERR_ARG, "cks: bad coefficient record");
+    std::memcpy(out, d, cnt * sizeof(double));
+  }
+  return OCN_OK;
+}
+
+int ocn_cks_to_mpc(int lmin, int lmax, const int* nproj, int nb, int nkpts, int nspn, const double* pcr,
+                   const double* pci, double* mpcr, double* mpci) {
+  if (!nproj || !pcr || !pci || !mpcr || !mpci || lmin < 0 || lmax < lmin)
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_cks_to_mpc: bad argument");
+  int npmax = 0, nptot = 0;
+  for (int l = lmin; l <= lmax; ++l) {
+    if (nproj[l - lmin] < 0) return set_err(nullptr, OCN_ERR_ARG, "ocn_cks_to_mpc: negative projector count");
+    npmax = std::max(npmax, nproj[l - lmin]);
+    nptot += (2 * l + 1) * nproj[l - lmin];
+  }
+  const int nm = 2 * lmax + 1, nl = lmax - lmin + 1;
+  const size_t total = (size_t)nb * nkpts * npmax * nm * nl * nspn;
+  std::fill(mpcr, mpcr + total, 0.0);
+  std::fill(mpci, mpci + total, 0.0);
+  // OCEAN_multiplet.f90:466-481: ip runs over l, m = -l..l, nu
+  for (int s = 0; s < nspn; ++s)
+    for (int k = 0; k < nkpts; ++k)
+      for (int b = 0; b < nb; ++b) {
+        int ip = 0;
+        const size_t src = (size_t)nptot * ((size_t)b + (size_t)nb * ((size_t)k + (size_t)nkpts * s));
+        for (int l = lmin; l <= lmax; ++l)
+          for (int m = -l; m <= l; ++m)
+            for (int nu = 0; nu < nproj[l - lmin]; ++nu, ++ip) {
+              const size_t dst = (size_t)b + (size_t)nb * ((size_t)k + (size_t)nkpts * ((size_t)nu + (size_t)npmax *
+                                 ((size_t)(m + lmax) + (size_t)nm * ((size_t)(l - lmin) + (size_t)nl * s))));
+              mpcr[dst] = pcr[src + ip];
+              mpci[dst] = pci[src + ip];
+            }
+      }
+  return OCN_OK;
+}
+
+int ocn_read_cmel(const char* path, int nproj, double* mpm) {
+  if (!path || !mpm || nproj < 1) return set_err(nullptr, OCN_ERR_ARG, "ocn_read_cmel: bad argument");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  // OCEAN_multiplet.f90:493-499: list-directed nproj*nproj values; column nu of
+  // mpm(:, :, l) takes values nu*nproj .. nu*nproj + nproj - 1
+  std::vector<std::string> v;
+  int rc = OCN_OK;
+  if (!ld_read(f, (size_t)nproj * nproj, &v)) rc = set_err(nullptr, OCN_ERR_ARG, "cmel: too few values");
+  for (int i = 0; i < nproj * nproj && rc == OCN_OK; ++i)
+    if (!ld_real(v[i], &mpm[i])) rc = set_err(nullptr, OCN_ERR_ARG, "cmel: bad value");
+  std::fclose(f);
+  return rc;
+}
+
+int ocn_input_filename(const char* kind, const char* calc_type, const char* elname, int indx, int n, int l,
+                       char* buf, size_t len) {
+  if (!kind || !elname || !buf || len == 0) return set_err(nullptr, OCN_ERR_ARG, "ocn_input_filename: null argument");
+  if (indx < 0 || indx > 9999 || n < 0 || n > 99 || l < 0 || l > 99)
+    return set_err(nullptr, OCN_ERR_ARG, "index outside the I4.4 / I2.2 range");
+  const std::string k(kind), ct(calc_type ? calc_type : "XAS");
+  char tail[32];
+  std::string name;
+  if (k == "rpottrim") {
+    // long_range.f90:1689-1690: '(A10,A2,I4.4,A2,I2.2,A1,I2.2)'
+    std::snprintf(tail, sizeof tail, "%04d_n%02dl%02d", indx, n, l);
+    name = "rpottrim.z" + a2(elname) + tail;
+  } else if (k == "cks" || k == "parcks") {
+    // OCEAN_multiplet.f90:417-428,454: 'cksc.' (cksv. for XES) + '(A2,I4.4)', 'par' in front for the stream file
+    std::snprintf(tail, sizeof tail, "%04d", indx);
+    name = std::string(k == "parcks" ? "par" : "") + (ct == "XES" ? "cksv." : "cksc.") + a2(elname) + tail;
+  } else if (k == "cmel") {
+    if (l > 9) return set_err(nullptr, OCN_ERR_ARG, "l exceeds 9 in multip");  // :491
+    std::snprintf(tail, sizeof tail, "cmel%d", l);
+    name = tail;
+  } else if (k == "energies") {
+    name = ct == "VAL" ? "wvfvainfo" : "wvfcninfo";  // OCEAN_energies.f90:650-654 (conduct)
+  } else {
+    return set_err(nullptr, OCN_ERR_ARG, "kind must be rpottrim, cks, parcks, cmel or energies");
+  }
   if (name.size() + 1 > len) return set_err(nullptr, OCN_ERR_ARG, "buffer too small");
   std::memcpy(buf, name.c_str(), name.size() + 1);
   return OCN_OK;
