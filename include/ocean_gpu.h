@@ -228,6 +228,26 @@ int ocn_haydock_block(ocn_ctx* ctx, int nv, const double* psi0_r, const double* 
 int ocn_haydock_block_dev(ocn_ctx* ctx, int nv, const double* d_psi0, int niter, double* real_a,
                           double* imag_a, double* real_b, int* niter_done);
 
+/* Non-Hermitian Haydock: the two-sided Lanczos of OCEAN_haydock_nonHerm_do
+ * (OCEAN_haydock.f90:53-164, selected there by complex_haydock), for an H
+ * made non-Hermitian by complex band energies or a broadened spin-orbit term.
+ * Right vectors see H, left vectors H^dagger (the action with backwards set,
+ * OCEAN_action.f90:286); both start from psi0 under the allow mask.  The step
+ * follows the algorithm that haydock_abc_1 (:1250-1433) cites (Saad):
+ * alpha_j = <w_j|H v_j>, z = <w^|v^>, delta = sqrt(z) (principal, as :1373-1374),
+ * beta = z/delta, v_{j+1} = (H v_j - alpha_j v_j - beta_j v_{j-1}) / delta,
+ * w_{j+1} = (H^dagger w_j - conj(alpha_j) w_j - conj(delta_j) w_{j-1}) / conj(beta).
+ * (haydock_abc_1 itself, never called in the reference, subtracts conj(beta_j)
+ * and divides by beta; its tridiagonal then fails the moment test beyond k = 2.)
+ * Stored as write_core reads them (e - real_a, gam + imag_a, products b*c):
+ * a = alpha, b = conj(beta), c = conj(delta), so ocn_spectrum_cf_bc gives
+ * kpref |Im <psi0|(z - H^dagger)^-1|psi0>|, the Hermitian run's convention.
+ * Arrays (0:niter); b and c from index 1.  Host planes in, FP64 recurrence in
+ * both precisions (the action in the context's precision). */
+int ocn_haydock_nonherm(ocn_ctx* ctx, const double* psi0_r, const double* psi0_i, int niter, double* real_a,
+                        double* imag_a, double* real_b, double* imag_b, double* real_c, double* imag_c,
+                        int* niter_done);
+
 /* Batched Haydock over independent problems: context i runs nv[i] chains
  * (ocn_haydock_block_dev on d_psi0[i]) for niter iterations.  Three iterations
  * of every context are captured into one CUDA graph that is replayed niter/3
@@ -266,6 +286,14 @@ typedef struct {
 } ocn_cf_params;
 int ocn_spectrum_cf(const double* real_a, const double* imag_a, const double* real_b,
                     int iter, double kpref, const ocn_cf_params* p, double* out /* (ne+1)*9 */);
+
+/* ocn_spectrum_cf with the complex b and c of ocn_haydock_nonherm: write_core's
+ * products cmplx(real_b, imag_b) * cmplx(real_c, imag_c) (binary32, as the
+ * reference forms them, OCEAN_haydock.f90:1846-1870).  imag_b, real_c, imag_c
+ * NULL: the Hermitian run (c = b real). */
+int ocn_spectrum_cf_bc(const double* real_a, const double* imag_a, const double* real_b, const double* imag_b,
+                       const double* real_c, const double* imag_c, int iter, double kpref,
+                       const ocn_cf_params* p, double* out);
 
 /* ocn_spectrum_cf (write_core path only) without any device allocation: no
  * counterpart in the reference, which evaluates the fraction on the host.  For

@@ -84,7 +84,7 @@ EXPORTS = [
     "ocn_gmres_vjp", "ocn_w2_vjp", "ocn_haydock_batch", "ocn_autotune", "ocn_set_tiles", "ocn_get_tiles",
     "ocn_read_bse_in", "ocn_write_abslanc", "ocn_write_absspct", "ocn_write_abs_gmres", "ocn_output_filename",
     "ocn_read_u2dat", "ocn_read_rpottrim", "ocn_read_energies", "ocn_read_cks", "ocn_cks_to_mpc", "ocn_read_cmel",
-    "ocn_input_filename",
+    "ocn_input_filename", "ocn_haydock_nonherm", "ocn_spectrum_cf_bc",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -352,6 +352,17 @@ class Context:
                                              int(bool(backwards))))
         return outr, outi
 
+    def haydock_nonherm(self, niter: int, pr=None, pi=None):
+        """Two-sided Lanczos (ocn_haydock_nonherm): returns ([a_r, a_i, b_r, b_i, c_r, c_i], done)."""
+        w = self.w
+        pr = _f64(w.psi_r if pr is None else pr)
+        pi = _f64(w.psi_i if pi is None else pi)
+        co = [np.zeros(niter + 1) for _ in range(6)]
+        done = C.c_int(0)
+        self._chk(self.lib.ocn_haydock_nonherm(self.ptr, _dp(pr), _dp(pi), niter, *[_dp(x) for x in co],
+                                               C.byref(done)))
+        return co, done.value
+
     def haydock_block(self, niter: int, pr, pi):
         """nv Lanczos chains in lockstep: pr/pi of shape (nv, npsi); returns arrays
         of shape (nv, niter+1) and the per-chain iteration counts."""
@@ -450,6 +461,19 @@ class Context:
                                      _dp(e), n, C.byref(p), _dp(ore), _dp(oim), _dp(rel),
                                      its.ctypes.data_as(IP)))
         return ore, oim, rel, its
+
+
+def spectrum_cf_bc(ra, ia, rb, ib, rc, ic, iteration: int, kpref: float, el: float, eh: float, ne: int,
+                   gam0: float, ebase: float = 0.0, ucvol: float = 1.0) -> np.ndarray:
+    """write_core rows for the complex b and c of a non-Hermitian run."""
+    lib = load()
+    p = OcnCfParams()
+    p.el, p.eh, p.gam0, p.ebase, p.gam_gauss = el, eh, gam0, ebase, 0.0
+    p.ne, p.ucvol, p.old_broaden, p.nval, p.eps = ne, ucvol, 0, 0.0, 1.0
+    out = np.zeros((ne + 1) * 9)
+    arrs = [None if x is None else _dp(_f64(x)) for x in (ra, ia, rb, ib, rc, ic)]
+    check(lib.ocn_spectrum_cf_bc(*arrs, iteration, C.c_double(kpref), C.byref(p), _dp(out)))
+    return out.reshape(ne + 1, 9)
 
 
 def spectrum_cf(ra, ia, rb, iteration: int, kpref: float, el: float, eh: float, ne: int, gam0: float,

@@ -1105,6 +1105,108 @@ int ocn_psi_pnorm(int n, int nkpts, double celvol, double* pr, double* pi, doubl
   return OCN_OK;
 }
 
+// The two-sided Lanczos of OCEAN_haydock_nonHerm_do (OCEAN_haydock.f90:53-164),
+// its step (haydock_abc_1, :1250-1433) written as Saad's algorithm that the
+// routine's comments cite; see the header for the stored convention.
+int ocn_haydock_nonherm(ocn_ctx* c, const double* psi0_r, const double* psi0_i, int niter, double* real_a,
+                        double* imag_a, double* real_b, double* imag_b, double* real_c, double* imag_c,
+                        int* niter_done) {
+  if (!c || !psi0_r || !psi0_i || niter < 1 || !real_a || !imag_a || !real_b || !imag_b || !real_c || !imag_c)
+    return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  int rc = require(c);
+  if (rc) return rc;
+  const size_t n = c->npsi;
+  double* pool = nullptr;
+  if ((rc = dev_alloc(c, &pool, 6 * 2 * n))) return rc;
+  double *v = pool, *w = pool + 2 * n, *ov = pool + 4 * n, *ow = pool + 6 * n, *hv = pool + 8 * n,
+         *hw = pool + 10 * n;
+  for (int i = 0; i <= niter; ++i) real_a[i] = imag_a[i] = real_b[i] = imag_b[i] = real_c[i] = imag_c[i] = 0.0;
+  if (niter_done) *niter_done = 0;
+  cudaError_t e = cudaMemcpyAsync(v, psi0_r, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(v + n, psi0_i, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(w, v, 2 * n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ov, 0, 4 * n * sizeof(double), c->stream);  // ov, ow
+  if (e != cudaSuccess) {
+    cudaFree(pool);
+    return cuda_fail(c, e, "ocn_haydock_nonherm setup");
+  }
+  auto dot = [&](const double* p, const double* q, double* r, double* i) -> int {  // sum conj(p) q
+    int q_ = vec_dot_dev(c, p, q, c->d_scal);
+    if (q_) return q_;
+    double h[2];
+    OCN_CUDA(c, cudaMemcpyAsync(h, c->d_scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+    *r = h[0];
+    *i = h[1];
+    return OCN_OK;
+  };
+  int done = 0;
+  for (int it = 1; it <= niter && rc == OCN_OK; ++it) {
+    double ar = 0, ai = 0, zr = 0, zi = 0;
+    if ((rc = vec_mask_inplace(c, v)) || (rc = vec_mask_inplace(c, w)) ||
+        (rc = apply_H_impl(c, v, v + n, hv, hv + n, nullptr, 0)) ||
+        (rc = apply_H_impl(c, w, w + n, hw, hw + n, nullptr, 1)) ||  // A^H
+        (rc = vec_mask_inplace(c, hv)) || (rc = vec_mask_inplace(c, hw)) || (rc = dot(w, hv, &ar, &ai)))
+      break;
+    // beta_j = conj(b_j), conj(delta_j) = c_j
+    if ((rc = vec_axpy(c, -real_b[it - 1], imag_b[it - 1], ov, hv)) ||
+        (rc = vec_axpy(c, -real_c[it - 1], -imag_c[it - 1], ow, hw)) || (rc = vec_axpy(c, -ar, -ai, v, hv)) ||
+        (rc = vec_axpy(c, -ar, ai, w, hw)))
+      break;
+    real_a[it - 1] = ar;
+    imag_a[it - 1] = ai;
+    if ((rc = vec_mask_inplace(c, hv)) || (rc = vec_mask_inplace(c, hw)) || (rc = dot(hw, hv, &zr, &zi))) break;
+    const double az = std::sqrt(zr * zr + zi * zi);
+    const double dr = std::sqrt((az + zr) / 2.0), di = std::copysign(std::sqrt((az - zr) / 2.0), zi);
+    // beta = z / delta (Smith's division)
+    double br, bi;
+    if (std::fabs(dr) >= std::fabs(di)) {
+      const double r = di / dr, t = 1.0 / (dr + di * r);
+      br = (zr + zi * r) * t;
+      bi = (zi - zr * r) * t;
+    } else {
+      const double r = dr / di, t = 1.0 / (dr * r + di);
+      br = (zr * r + zi) * t;
+      bi = (zi * r - zr) * t;
+    }
+    real_b[it] = br;
+    imag_b[it] = -bi;
+    real_c[it] = dr;
+    imag_c[it] = -di;
+    if ((rc = vec_divide(c, hw, br, -bi)) || (rc = vec_divide(c, hv, dr, di))) break;  // w^/conj(beta), v^/delta
+    double* t = ov;  // old <- current, current <- new
+    ov = v;
+    v = hv;
+    hv = t;
+    t = ow;
+    ow = w;
+    w = hw;
+    hw = t;
+    done = it;
+    if (std::isnan(ar)) {
+      rc = set_err(c, OCN_ERR_NAN, "NaN in the Lanczos a_n");
+      break;
+    }
+  }
+  e = cudaStreamSynchronize(c->stream);
+  cudaFree(pool);
+  if (niter_done) *niter_done = done;
+  if (rc == OCN_OK && e != cudaSuccess) rc = cuda_fail(c, e, "ocn_haydock_nonherm");
+  if (rc == OCN_OK && c->mixed) rc = mixed_check(c);
+  return rc;
+}
+
+int ocn_spectrum_cf_bc(const double* real_a, const double* imag_a, const double* real_b, const double* imag_b,
+                       const double* real_c, const double* imag_c, int iter, double kpref,
+                       const ocn_cf_params* p, double* out) {
+  if (!real_a || !real_b || !p || !out) return set_err(nullptr, OCN_ERR_ARG, "null argument");
+  std::string err;
+  int rc = cf_eval(real_a, imag_a, real_b, iter, kpref, p, out, &err, imag_b, real_c, imag_c);
+  if (rc) set_err(nullptr, rc, err);
+  return rc;
+}
+
 int ocn_spectrum_cf(const double* real_a, const double* imag_a, const double* real_b, int iter,
                     double kpref, const ocn_cf_params* p, double* out) {
   if (!real_a || !real_b || !p || !out) return set_err(nullptr, OCN_ERR_ARG, "null argument");

@@ -57,12 +57,29 @@ __device__ __forceinline__ double bsq_sp(double b) {
   return (double)__fmul_rn(f, f);
 }
 
+// Imaginary parts of b and the c coefficients of a non-Hermitian run (all NULL:
+// the Hermitian run, c = b real).
+struct BcArrays {
+  const double *ib, *rc, *ic;
+};
+
+// b_j c_j as write_core forms it: cmplx(real_b, imag_b) * cmplx(real_c, imag_c)
+// without a KIND, a binary32 complex product (OCEAN_haydock.f90:1847-1848,1868).
+__device__ __forceinline__ cplx bc_sp(const double* __restrict__ rb, const BcArrays& q, int j) {
+  if (!q.ib && !q.rc && !q.ic) return {bsq_sp(rb[j]), 0.0};
+  const float a = __double2float_rn(rb[j]), b = q.ib ? __double2float_rn(q.ib[j]) : 0.0f;
+  const float c = q.rc ? __double2float_rn(q.rc[j]) : a, d = q.ic ? __double2float_rn(q.ic[j]) : 0.0f;
+  return {(double)__fsub_rn(__fmul_rn(a, c), __fmul_rn(b, d)), (double)__fadd_rn(__fmul_rn(a, d), __fmul_rn(b, c))};
+}
+
 __device__ cplx cf_delta(const double* __restrict__ ra, const double* __restrict__ ia,
-                         const double* __restrict__ rb, int iter, double e, double gam) {
+                         const double* __restrict__ rb, const BcArrays& q, int iter, double e, double gam) {
   const double ial = ia ? ia[iter - 1] : 0.0;
   const cplx ct = {e - ra[iter - 1], gam + ial};
-  const double bc4 = (double)__fmul_rn(4.0f, __double2float_rn(bsq_sp(rb[iter])));
-  const cplx sq = {ct.x * ct.x - ct.y * ct.y - bc4, ct.x * ct.y + ct.y * ct.x};
+  const cplx bcl = bc_sp(rb, q, iter);
+  const double bc4 = (double)__fmul_rn(4.0f, __double2float_rn(bcl.x));
+  const double bc4i = (double)__fmul_rn(4.0f, __double2float_rn(bcl.y));
+  const cplx sq = {ct.x * ct.x - ct.y * ct.y - bc4, ct.x * ct.y + ct.y * ct.x - bc4i};
   const cplx disc = csqrt_principal(sq);
   cplx delta;
   if (disc.y > 0.0)
@@ -70,7 +87,7 @@ __device__ cplx cf_delta(const double* __restrict__ ra, const double* __restrict
   else
     delta = {(ct.x - disc.x) * 0.5, (ct.y - disc.y) * 0.5};
   for (int jj = iter - 1; jj >= 0; --jj) {
-    const cplx c2 = {bsq_sp(rb[jj + 1]), 0.0};
+    const cplx c2 = bc_sp(rb, q, jj + 1);
     const double iaj = ia ? ia[jj] : 0.0;
     const cplx z = {(double)__double2float_rn(e - ra[jj]), (double)__double2float_rn(gam + iaj)};
     const cplx q = cdiv_smith(c2, delta);
@@ -80,20 +97,20 @@ __device__ cplx cf_delta(const double* __restrict__ ra, const double* __restrict
 }
 
 __global__ void k_write_core(const double* __restrict__ ra, const double* __restrict__ ia,
-                             const double* __restrict__ rb, int iter, double kpref, double el,
+                             const double* __restrict__ rb, const BcArrays q, int iter, double kpref, double el,
                              double eh, int ne, double gam0, const double* __restrict__ gam1,
                              double ebase, double ucvol, double* __restrict__ out) {
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row > ne) return;
   const int ie = 2 * row;
   const double e = el + (eh - el) * (double)ie / (double)(2 * ne);
-  const cplx d = cf_delta(ra, ia, rb, iter, e, gam0);
+  const cplx d = cf_delta(ra, ia, rb, q, iter, e, gam0);
   const double dr = d.x, di = fabs(d.y);
   const double spct = kpref * di / (dr * dr + di * di);
   const double spkk = kpref * dr / (dr * dr + di * di);
   double spct1 = spct, spkk1 = spkk;
   if (gam1) {  // oldXASbroaden: second damping with gamfcn (OCEAN_haydock.f90:1839-1841)
-    const cplx d1 = cf_delta(ra, ia, rb, iter, e, gam1[row]);
+    const cplx d1 = cf_delta(ra, ia, rb, q, iter, e, gam1[row]);
     const double dr1 = d1.x, di1 = fabs(d1.y);
     spct1 = kpref * di1 / (dr1 * dr1 + di1 * di1);
     spkk1 = kpref * dr1 / (dr1 * dr1 + di1 * di1);
@@ -119,14 +136,14 @@ __global__ void k_write_core(const double* __restrict__ ra, const double* __rest
 // Voigt variant: Lorentzian spectrum on the fine grid e_i = el + (i - nstep)*estep
 // (each fine point of write_core_Voigt evaluated once), with damping gam[i].
 __global__ void k_cf_points(const double* __restrict__ ra, const double* __restrict__ ia,
-                            const double* __restrict__ rb, int iter, double kpref, double el,
+                            const double* __restrict__ rb, const BcArrays q, int iter, double kpref, double el,
                             int nstep, double estep, const double* __restrict__ gam,
                             double prefactor, double* __restrict__ sp, double* __restrict__ sk,
                             int npts) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= npts) return;
   const double e = el + (double)(i - nstep) * estep;
-  const cplx d = cf_delta(ra, ia, rb, iter, e, gam[i]);
+  const cplx d = cf_delta(ra, ia, rb, q, iter, e, gam[i]);
   const double dr = d.x, di = fabs(d.y);
   sp[i] = prefactor * kpref * di / (dr * dr + di * di);
   sk[i] = prefactor * kpref * dr / (dr * dr + di * di);
@@ -135,7 +152,8 @@ __global__ void k_cf_points(const double* __restrict__ ra, const double* __restr
 }  // namespace
 
 int cf_eval(const double* ra, const double* ia, const double* rb, int iter, double kpref,
-            const ocn_cf_params* p, double* out, std::string* err) {
+            const ocn_cf_params* p, double* out, std::string* err, const double* ib, const double* rc,
+            const double* ic) {
   if (iter < 1 || p->ne < 1) {
     if (err) *err = "ocn_spectrum_cf: iter and ne must be >= 1";
     return OCN_ERR_ARG;
@@ -162,6 +180,17 @@ int cf_eval(const double* ra, const double* ia, const double* rb, int iter, doub
   h2d(d_ra, ra, nco);
   h2d(d_rb, rb, nco);
   if (ia) h2d(d_ia, ia, nco);
+  BcArrays dq{nullptr, nullptr, nullptr};
+  double* d_bc[3] = {nullptr, nullptr, nullptr};
+  const double* h_bc[3] = {ib, rc, ic};
+  for (int i = 0; i < 3; ++i)
+    if (h_bc[i]) {
+      d_bc[i] = dalloc(nco * sizeof(double));
+      h2d(d_bc[i], h_bc[i], nco);
+    }
+  dq.ib = d_bc[0];
+  dq.rc = d_bc[1];
+  dq.ic = d_bc[2];
   const int ne = p->ne;
   if (e == cudaSuccess && p->gam_gauss > p->gam0 / 10.0) {
     // write_core_Voigt: fine grid shared between neighbouring output rows
@@ -183,9 +212,9 @@ int cf_eval(const double* ra, const double* ia, const double* rb, int iter, doub
     h2d(d_g0, g0.data(), npts);
     h2d(d_g1, g1.data(), npts);
     if (e == cudaSuccess) {
-      k_cf_points<<<(npts + 127) / 128, 128>>>(d_ra, d_ia, d_rb, iter, kpref, p->el, nstep, estep,
+      k_cf_points<<<(npts + 127) / 128, 128>>>(d_ra, d_ia, d_rb, dq, iter, kpref, p->el, nstep, estep,
                                               d_g0, prefactor, d_sp, d_sk, npts);
-      k_cf_points<<<(npts + 127) / 128, 128>>>(d_ra, d_ia, d_rb, iter, kpref, p->el, nstep, estep,
+      k_cf_points<<<(npts + 127) / 128, 128>>>(d_ra, d_ia, d_rb, dq, iter, kpref, p->el, nstep, estep,
                                               d_g1, prefactor, d_sp + npts, d_sk + npts, npts);
       e = cudaGetLastError();
     }
@@ -228,7 +257,7 @@ int cf_eval(const double* ra, const double* ia, const double* rb, int iter, doub
     }
     double* d_out = dalloc((size_t)(ne + 1) * 9 * sizeof(double));
     if (e == cudaSuccess) {
-      k_write_core<<<(ne + 1 + 63) / 64, 64>>>(d_ra, d_ia, d_rb, iter, kpref, p->el, p->eh, ne,
+      k_write_core<<<(ne + 1 + 63) / 64, 64>>>(d_ra, d_ia, d_rb, dq, iter, kpref, p->el, p->eh, ne,
                                              p->gam0, d_g1, p->ebase, p->ucvol, d_out);
       e = cudaGetLastError();
     }
@@ -338,7 +367,8 @@ int cf_eval_noalloc(const double* ra, const double* ia, const double* rb, int it
     e = cudaMemcpy(d_g1, out, (size_t)(ne + 1) * sizeof(double), cudaMemcpyHostToDevice);
   }
   if (e == cudaSuccess) {
-    k_write_core<<<(ne + 1 + 63) / 64, 64>>>(d_ra, ia ? d_ia : nullptr, d_rb, iter, kpref, p->el, p->eh, ne,
+    k_write_core<<<(ne + 1 + 63) / 64, 64>>>(d_ra, ia ? d_ia : nullptr, d_rb, BcArrays{nullptr, nullptr, nullptr},
+                                             iter, kpref, p->el, p->eh, ne,
                                            p->gam0, p->old_broaden ? d_g1 : nullptr, p->ebase, p->ucvol,
                                            d_out);
     e = cudaGetLastError();

@@ -291,13 +291,16 @@ int vec_axmy(ocn_ctx* c, const double* x, double* y, double rv, double iv);
 int vec_axmz(ocn_ctx* c, const double* x, double* y, const double* z);
 int vec_axpy(ocn_ctx* c, double ar, double ai, const double* x, double* y);
 int vec_mul(ocn_ctx* c, const double* x, const double* y, double* z);
+int vec_mask_inplace(ocn_ctx* c, double* x);
+int vec_divide(ocn_ctx* c, double* x, double rv, double iv);  // x /= rv + i iv
 int vec_set_prec(ocn_ctx* c, double energy, double gprc, const double* h, double* out);
 int vec_mask_copy(ocn_ctx* c, const double* in, double* out);
 int vec_fill(ocn_ctx* c, double* x, double vr, double vi);
 
 // ---- continued fraction (ocn_cf.cu)
 int cf_eval(const double* ra, const double* ia, const double* rb, int iter, double kpref,
-            const ocn_cf_params* p, double* out, std::string* err);
+            const ocn_cf_params* p, double* out, std::string* err,
+            const double* ib = nullptr, const double* rc = nullptr, const double* ic = nullptr);
 int cf_eval_noalloc(const double* ra, const double* ia, const double* rb, int iter, double kpref,
                     const ocn_cf_params* p, double* out, std::string* err);
 

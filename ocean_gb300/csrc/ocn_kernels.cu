@@ -693,6 +693,25 @@ __global__ void k_mask_copy(const double* __restrict__ in, const double* __restr
     out[n + e] = m * in[n + e];
   }
 }
+// x = allow o x in place (OCEAN_energies_allow)
+__global__ void k_mask_inplace(double* __restrict__ x, const double* __restrict__ allow, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double m = allow[e];
+    x[e] *= m;
+    x[n + e] *= m;
+  }
+}
+// x /= (rv + i iv) as OCEAN_psi_divide does it (OCEAN_psi.f90:1797-1808)
+__global__ void k_cdivide(double* __restrict__ x, size_t n, double rn, double in) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const double xr = x[e], xi = x[n + e];
+    const double buf = -in * xr;
+    x[e] = rn * xr + in * xi;
+    x[n + e] = buf + rn * xi;
+  }
+}
 __global__ void k_fill(double* __restrict__ x, size_t n, double vr, double vi) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
        e += (size_t)gridDim.x * blockDim.x) {
@@ -1114,6 +1133,19 @@ int vec_set_prec(ocn_ctx* c, double energy, double gprc, const double* h, double
 int vec_mask_copy(ocn_ctx* c, const double* in, double* out) {
   k_mask_copy<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(in, c->d_allow, out,
                                                                                c->npsi);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+int vec_mask_inplace(ocn_ctx* c, double* x) {
+  k_mask_inplace<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(x, c->d_allow, c->npsi);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+int vec_divide(ocn_ctx* c, double* x, double rv, double iv) {
+  const double denom = rv * rv + iv * iv;
+  k_cdivide<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, 0, c->stream>>>(x, c->npsi, rv / denom, iv / denom);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;

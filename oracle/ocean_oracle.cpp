@@ -610,6 +610,107 @@ int or_haydock(const or_dims* d, const or_ops* o, const double* p0r, const doubl
   return 0;
 }
 
+// The two-sided Lanczos of OCEAN_haydock_nonHerm_do (OCEAN_haydock.f90:53-164)
+// with the step of haydock_abc_1 (:1250-1433) written as the algorithm its
+// comments cite (Saad, two-sided Lanczos; (x, y) = sum x conj(y) = <y|x>):
+//   alpha_j = <w_j|A v_j>,  delta_{j+1} = sqrt(z) (principal, as :1373-1374),
+//   beta_{j+1} = z / delta_{j+1},  z = <w^_{j+1}|v^_{j+1}>,
+//   v^_{j+1} = A v_j - alpha_j v_j - beta_j v_{j-1},
+//   w^_{j+1} = A^H w_j - conj(alpha_j) w_j - conj(delta_j) w_{j-1},
+//   v_{j+1} = v^ / delta,  w_{j+1} = w^ / conj(beta).
+// haydock_abc_1 itself subtracts conj(beta_j) v_{j-1} and divides w^ by beta,
+// so its tridiagonal matches the moments <w_1|A^k v_1> only for k <= 2 (the
+// routine is not called: complex_haydock is .false., :47,181).  Stored as
+// write_core reads them (z - conj(a), products b*c, :1846-1870): a = alpha,
+// b = conj(beta), c = conj(delta), so that the continued fraction is
+// <psi|(z - A^H)^-1|psi>, the Hermitian run's convention.
+int or_haydock_nonherm(const or_dims* d, const or_ops* o, const double* p0r, const double* p0i, int niter,
+                       double* real_a, double* imag_a, double* real_b, double* imag_b, double* real_c,
+                       double* imag_c, int* niter_done) {
+  const size_t n = (size_t)d->nb * nk_of(d) * d->na;
+  std::vector<double> vr(p0r, p0r + n), vi(p0i, p0i + n), wr(vr), wi(vi);
+  std::vector<double> ovr(n, 0.0), ovi(n, 0.0), owr(n, 0.0), owi(n, 0.0);
+  std::vector<double> hvr(n), hvi(n), hwr(n), hwi(n);
+  for (int i = 0; i <= niter; ++i) real_a[i] = imag_a[i] = real_b[i] = imag_b[i] = real_c[i] = imag_c[i] = 0.0;
+  auto allow = [&](std::vector<double>& r, std::vector<double>& im) {  // OCEAN_energies_allow
+    for (size_t i = 0; i < n; ++i) {
+      r[i] *= o->allow[i];
+      im[i] *= o->allow[i];
+    }
+  };
+  auto dot = [&](const std::vector<double>& pr, const std::vector<double>& pi, const std::vector<double>& qr,
+                 const std::vector<double>& qi, double* rr, double* ii) {  // sum conj(p) q
+    double a = 0.0, b = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+      a += pr[i] * qr[i] + pi[i] * qi[i];
+      b += pr[i] * qi[i] - pi[i] * qr[i];
+    }
+    *rr = a;
+    *ii = b;
+  };
+  auto axpy = [&](double ar, double ai, const std::vector<double>& xr, const std::vector<double>& xi,
+                  std::vector<double>& yr, std::vector<double>& yi) {  // y += (ar + i ai) x
+    for (size_t i = 0; i < n; ++i) {
+      yr[i] += ar * xr[i] - ai * xi[i];
+      yi[i] += ar * xi[i] + ai * xr[i];
+    }
+  };
+  auto divide = [&](std::vector<double>& xr, std::vector<double>& xi, double rv, double iv) {  // OCEAN_psi_divide
+    const double denom = rv * rv + iv * iv, rn = rv / denom, in = iv / denom;
+    for (size_t i = 0; i < n; ++i) {
+      const double buf = -in * xr[i];
+      xr[i] = rn * xr[i] + in * xi[i];
+      xi[i] = buf + rn * xi[i];
+    }
+  };
+  int done = 0;
+  for (int iter = 1; iter <= niter; ++iter) {
+    allow(vr, vi);
+    allow(wr, wi);
+    or_xact(d, o, vr.data(), vi.data(), hvr.data(), hvi.data(), nullptr, 0);
+    or_xact(d, o, wr.data(), wi.data(), hwr.data(), hwi.data(), nullptr, 1);  // A^H
+    allow(hvr, hvi);
+    allow(hwr, hwi);
+    double ar, ai;
+    dot(wr, wi, hvr, hvi, &ar, &ai);  // alpha = <w|A v>
+    // beta_j = conj(b_j), conj(delta_j) = c_j
+    axpy(-real_b[iter - 1], imag_b[iter - 1], ovr, ovi, hvr, hvi);
+    axpy(-real_c[iter - 1], -imag_c[iter - 1], owr, owi, hwr, hwi);
+    axpy(-ar, -ai, vr, vi, hvr, hvi);
+    axpy(-ar, ai, wr, wi, hwr, hwi);
+    real_a[iter - 1] = ar;
+    imag_a[iter - 1] = ai;
+    allow(hvr, hvi);
+    allow(hwr, hwi);
+    double zr, zi;
+    dot(hwr, hwi, hvr, hvi, &zr, &zi);
+    ovr = vr;
+    ovi = vi;
+    owr = wr;
+    owi = wi;
+    const double az = std::sqrt(zr * zr + zi * zi);
+    const double dr = std::sqrt((az + zr) / 2.0), di = std::copysign(std::sqrt((az - zr) / 2.0), zi);
+    const cd beta = cdiv(cd(zr, zi), cd(dr, di));
+    real_b[iter] = beta.real();
+    imag_b[iter] = -beta.imag();
+    real_c[iter] = dr;
+    imag_c[iter] = -di;
+    divide(hwr, hwi, beta.real(), -beta.imag());  // w^ / conj(beta)
+    divide(hvr, hvi, dr, di);                      // v^ / delta
+    vr = hvr;
+    vi = hvi;
+    wr = hwr;
+    wi = hwi;
+    done = iter;
+    if (std::isnan(real_a[iter - 1])) {
+      *niter_done = done;
+      return -1;
+    }
+  }
+  *niter_done = done;
+  return 0;
+}
+
 // gamfcn, CNBSE/zcmsnmult/zf90/gamfcn.f90:8-42.
 double or_gamfcn(double e, double n, double e0) {
   const double pi = 3.14159265358979;
@@ -648,15 +749,22 @@ double or_gamfcn(double e, double n, double e0) {
 namespace {
 // Continued fraction at one energy, write_core inner loops
 // (OCEAN_haydock.f90:1831-1873), single-precision cmplx() quirk included.
-cd cf_delta(const double* ra, const double* ia, const double* rb, int iter, double e, double gam) {
+// b_j c_j: cmplx(real_b, imag_b) * cmplx(real_c, imag_c), binary32; without
+// imag_b / real_c / imag_c the Hermitian run's c = b, imag parts zero
+cd bc_sp(const double* rb, const double* ib, const double* rc, const double* ic, int j) {
+  return cmul_sp(rb[j], ib ? ib[j] : 0.0, rc ? rc[j] : rb[j], ic ? ic[j] : 0.0);
+}
+
+cd cf_delta(const double* ra, const double* ia, const double* rb, const double* ib, const double* rc,
+            const double* ic, int iter, double e, double gam) {
   double ia_last = ia ? ia[iter - 1] : 0.0;
   cd ctmp(e - ra[iter - 1], gam + ia_last);
-  cd bc = cmul_sp(rb[iter], 0.0, rb[iter], 0.0);  // real_c = real_b, imag_b = imag_c = 0
+  cd bc = bc_sp(rb, ib, rc, ic, iter);
   cd four_bc((double)(4.0f * (float)bc.real()), (double)(4.0f * (float)bc.imag()));
   cd disc = csqrt_p(cmul(ctmp, ctmp) - four_bc);
   cd delta = (disc.imag() > 0.0) ? (ctmp + disc) * 0.5 : (ctmp - disc) * 0.5;
   for (int jj = iter - 1; jj >= 0; --jj) {
-    cd c2 = cmul_sp(rb[jj + 1], 0.0, rb[jj + 1], 0.0);
+    cd c2 = bc_sp(rb, ib, rc, ic, jj + 1);
     double iaj = ia ? ia[jj] : 0.0;
     delta = cmplx_sp(e - ra[jj], gam + iaj) - cdiv(c2, delta);
   }
@@ -698,7 +806,7 @@ int or_write_core(const double* ra, const double* ia, const double* rb, int iter
         e = ee + (double)ii * estep;
         for (int jd = 0; jd <= 1; ++jd) {
           double gam = gam0 + (jd ? or_gamfcn(e, nval, eps) : 0.0);
-          cd delta = cf_delta(ra, ia, rb, iter, e, gam);
+          cd delta = cf_delta(ra, ia, rb, nullptr, nullptr, nullptr, iter, e, gam);
           double dr = delta.real(), di = std::fabs(delta.imag());
           double sp = prefactor * kpref * di / (dr * dr + di * di);
           double sk = prefactor * kpref * dr / (dr * dr + di * di);
@@ -734,7 +842,7 @@ int or_write_core(const double* ra, const double* ia, const double* rb, int iter
     for (int jd = 0; jd <= jdstop; ++jd) {
       // gam0 + gamfcn(...)*dble(jdamp): the product is zero for jdamp = 0
       double gam = gam0 + (jd ? or_gamfcn(e, nval, eps) : 0.0);
-      cd delta = cf_delta(ra, ia, rb, iter, e, gam);
+      cd delta = cf_delta(ra, ia, rb, nullptr, nullptr, nullptr, iter, e, gam);
       double dr = delta.real(), di = std::fabs(delta.imag());
       spct[jd] = kpref * di / (dr * dr + di * di);
       spkk[jd] = kpref * dr / (dr * dr + di * di);
@@ -753,12 +861,36 @@ int or_write_core(const double* ra, const double* ia, const double* rb, int iter
   return 0;
 }
 
+// write_core's rows for complex b and c (no Voigt, no second damping).
+int or_write_core_bc(const double* ra, const double* ia, const double* rb, const double* ib,
+                     const double* rc, const double* ic, int iter, double kpref, double el, double eh,
+                     int ne, double gam0, double ebase, double ucvol, double* out) {
+  const double alphaByVolumeHartree = kEV2Ha * kAlpha * ucvol;
+  const double tpa = (kAlpha * kAlpha * 2.0 * kPi) * ucvol;
+  const double bohrSq2CmSq = kBohr * kBohr * 1.0e-16;
+  const double tpacm4 = tpa * bohrSq2CmSq * bohrSq2CmSq * kAu2sec;
+  int row = 0;
+  for (int ie = 0; ie <= 2 * ne; ie += 2) {
+    double e = el + (eh - el) * (double)ie / (double)(2 * ne);
+    cd delta = cf_delta(ra, ia, rb, ib, rc, ic, iter, e, gam0);
+    double dr = delta.real(), di = std::fabs(delta.imag());
+    double sp = kpref * di / (dr * dr + di * di), sk = kpref * dr / (dr * dr + di * di);
+    double ener = ebase + kHa2eV * e;
+    double sigma = alphaByVolumeHartree * ener * sp;
+    double* r = out + 9 * (size_t)row;
+    r[0] = ener; r[1] = sp; r[2] = sp; r[3] = sk; r[4] = sk;
+    r[5] = sigma; r[6] = sigma * bohrSq2CmSq; r[7] = sp * tpa; r[8] = sp * tpacm4;
+    ++row;
+  }
+  return 0;
+}
+
 // calc_spect_core, OCEAN_haydock.f90:1991-2027.
 int or_calc_spect_core(const double* ra, const double* ia, const double* rb, int iter, double kpref,
                        double el, double eh, int ne, double gam0, double ebase, double* out) {
   for (int ie = 1; ie <= ne; ++ie) {
     double e = el + (eh - el) * (double)(2 * (ie - 1) + 1) / (double)(2 * ne);
-    cd delta = cf_delta(ra, ia, rb, iter, e, gam0);
+    cd delta = cf_delta(ra, ia, rb, nullptr, nullptr, nullptr, iter, e, gam0);
     double dr = delta.real(), di = std::fabs(delta.imag());
     out[3 * (ie - 1) + 0] = ebase + kHa2eV * e;
     out[3 * (ie - 1) + 1] = kpref * dr / (dr * dr + di * di);

@@ -89,6 +89,12 @@ int or_xact(const or_dims* d, const or_ops* o, const double* pr, const double* p
 /* OCEAN_haydock_Herm_do + ocean_hay_ab_twoterm (OCEAN_haydock.f90:190-320,824-938). */
 int or_haydock(const or_dims* d, const or_ops* o, const double* p0r, const double* p0i, int niter,
                double* real_a, double* imag_a, double* real_b, int* niter_done);
+/* OCEAN_haydock_nonHerm_do + haydock_abc_1 (OCEAN_haydock.f90:53-164,1250-1433):
+ * two-sided Lanczos with H on the right vectors and H^dagger (xact backwards) on
+ * the left ones; complex a (0:niter), b and c (1:niter). */
+int or_haydock_nonherm(const or_dims* d, const or_ops* o, const double* p0r, const double* p0i, int niter,
+                       double* real_a, double* imag_a, double* real_b, double* imag_b, double* real_c,
+                       double* imag_c, int* niter_done);
 /* core_pnorm (OCEAN_psi.f90:5589-5638). */
 double or_pnorm(int n, int nkpts, double celvol, double* pr, double* pi);
 /* write_core / write_core_Voigt (OCEAN_haydock.f90:1801-1989). out (ne+1)*9. */
@@ -96,6 +102,11 @@ int or_write_core(const double* real_a, const double* imag_a, const double* real
                   double kpref, double el, double eh, int ne, double gam0, double ebase,
                   double gam_gauss, double ucvol, int old_broaden, double nval, double eps,
                   double* out);
+/* write_core with complex b and c (OCEAN_haydock.f90:1846-1870, the products
+ * cmplx(real_b, imag_b) * cmplx(real_c, imag_c) of the non-Hermitian run). */
+int or_write_core_bc(const double* real_a, const double* imag_a, const double* real_b, const double* imag_b,
+                     const double* real_c, const double* imag_c, int iter, double kpref, double el, double eh,
+                     int ne, double gam0, double ebase, double ucvol, double* out);
 /* calc_spect_core (OCEAN_haydock.f90:1991-2027). out ne*3. */
 int or_calc_spect_core(const double* real_a, const double* imag_a, const double* real_b, int iter,
                        double kpref, double el, double eh, int ne, double gam0, double ebase,

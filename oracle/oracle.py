@@ -169,6 +169,18 @@ class OracleProblem:
                               dptr(ra), dptr(ia), dptr(rb), C.byref(done))
         return rc, ra, ia, rb, done.value
 
+    def haydock_nonherm(self, niter, pr=None, pi=None):
+        """Two-sided Lanczos (OCEAN_haydock.f90:53-164,1250-1433): complex a, b, c."""
+        w = self.w
+        pr = w.psi_r if pr is None else pr
+        pi = w.psi_i if pi is None else pi
+        co = [np.zeros(niter + 1) for _ in range(6)]
+        done = C.c_int(0)
+        rc = lib().or_haydock_nonherm(C.byref(self.d), C.byref(self.o), dptr(np.ascontiguousarray(pr)),
+                                      dptr(np.ascontiguousarray(pi)), niter, *[dptr(x) for x in co],
+                                      C.byref(done))
+        return rc, co, done.value
+
     def gmres(self, energies_ev, depth=80, gres=None, gprc=None, ffff=1e-6, max_restarts=50):
         w = self.w
         e = np.ascontiguousarray(energies_ev, dtype=np.float64)
@@ -194,6 +206,15 @@ def write_core(ra, ia, rb, it, kpref, el, eh, ne, gam0, ebase=0.0, gam_gauss=0.0
                         C.c_double(el), C.c_double(eh), ne, C.c_double(gam0), C.c_double(ebase),
                         C.c_double(gam_gauss), C.c_double(ucvol), old_broaden, C.c_double(nval),
                         C.c_double(eps), dptr(out))
+    return out.reshape(ne + 1, 9)
+
+
+def write_core_bc(ra, ia, rb, ib, rc, ic, it, kpref, el, eh, ne, gam0, ebase=0.0, ucvol=1.0):
+    """write_core rows for complex b and c (non-Hermitian runs)."""
+    out = np.zeros((ne + 1) * 9)
+    arrs = [dptr(np.ascontiguousarray(x, dtype=np.float64)) for x in (ra, ia, rb, ib, rc, ic)]
+    lib().or_write_core_bc(*arrs, it, C.c_double(kpref), C.c_double(el), C.c_double(eh), ne, C.c_double(gam0),
+                           C.c_double(ebase), C.c_double(ucvol), dptr(out))
     return out.reshape(ne + 1, 9)
 
 

@@ -195,3 +195,81 @@ def test_spin_polarised_action_hermitian(oracle_lib):
     r, i = oracle_lib.OracleProblem(w1).xact(w.psi_r, w.psi_i)
     r2, i2 = P.xact(w.psi_r, w.psi_i)
     assert np.abs((r - r2) + 1j * (i - i2)).max() > 1e-6
+
+
+def _nonherm(w, seed=5):
+    """The tiny workload with a core-hole lifetime Sigma'' on the band energies:
+    H becomes non-Hermitian (complex diagonal)."""
+    import dataclasses
+
+    rng = np.random.default_rng(seed)
+    return dataclasses.replace(w, ei=rng.uniform(0.005, 0.05, w.npsi))
+
+
+def test_backwards_action_is_the_adjoint(oracle_lib):
+    w = _nonherm(WL.make("tiny", seed=1))
+    P = oracle_lib.OracleProblem(w)
+    n = w.npsi
+    H = _dense(P, n)
+    Hb = np.zeros((n, n), complex)
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = 1.0
+        r, i = P.xact(e, np.zeros(n), backwards=True)
+        Hb[:, j] = r + 1j * i
+    assert np.abs(H - H.conj().T).max() > 1e-4  # not Hermitian
+    assert np.abs(Hb - H.conj().T).max() < 1e-14 * np.abs(H).max()
+
+
+def test_two_sided_lanczos_reduces_to_lanczos_when_hermitian(tiny_problem, oracle_lib):
+    w, P = tiny_problem
+    rc, (ra, ia, rb, ib, rc_, ic), done = P.haydock_nonherm(30)
+    assert rc == 0 and done == 30
+    rh, ha, hia, hb, hdone = P.haydock(30)
+    assert np.allclose(ra, ha, rtol=0, atol=1e-12 * np.abs(ha).max())
+    assert np.allclose(rb * rc_ - ib * ic, hb * hb, rtol=1e-10)  # b c = b^2
+    s1 = oracle_lib.write_core_bc(ra, ia, rb, ib, rc_, ic, 30, w.kpref, w.el, w.eh, 400, w.gam0)
+    s0 = oracle_lib.write_core(ha, None, hb, 30, w.kpref, w.el, w.eh, 400, w.gam0)
+    assert np.abs(s1[:, 2] - s0[:, 2]).max() < 1e-9 * np.abs(s0[:, 2]).max()
+
+
+def test_two_sided_lanczos_moments(oracle_lib):
+    """The tridiagonal T of the two-sided recurrence (A v_j = delta_{j+1} v_{j+1}
+    + a_j v_j + beta_j v_{j-1}, stored as b = conj(beta), c = conj(delta))
+    reproduces the moments w0^H A^k v0 of the non-Hermitian action for k < 2m."""
+    w = _nonherm(WL.make("tiny", seed=1))
+    P = oracle_lib.OracleProblem(w)
+    n = w.npsi
+    A = _dense(P, n)
+    m = 8
+    rc, (ra, ia, rb, ib, rc_, ic), done = P.haydock_nonherm(m)
+    assert rc == 0 and done == m
+    a = ra[:m] + 1j * ia[:m]
+    b = rb[1:m] + 1j * ib[1:m]
+    c = rc_[1:m] + 1j * ic[1:m]
+    T = np.diag(a) + np.diag(np.conj(b), 1) + np.diag(np.conj(c), -1)
+    v0 = w.allow * (w.psi_r + 1j * w.psi_i)
+    for k in range(2 * m):
+        exact = np.vdot(v0, np.linalg.matrix_power(A, k) @ v0)
+        got = np.linalg.matrix_power(T, k)[0, 0]
+        assert abs(got - exact) < 1e-9 * max(1.0, abs(exact)), (k, got, exact)
+
+
+def test_two_sided_lanczos_spectrum_is_the_adjoint_resolvent(oracle_lib):
+    """write_core on the stored coefficients (z - conj(a), b*c) gives
+    kpref |Im <psi|(z - A^H)^-1|psi>| of the dense non-Hermitian action."""
+    w = _nonherm(WL.make("tiny", seed=1))
+    P = oracle_lib.OracleProblem(w)
+    n = w.npsi
+    A = _dense(P, n)
+    m = 120
+    rc, (ra, ia, rb, ib, rc_, ic), done = P.haydock_nonherm(m)
+    assert rc == 0
+    ne = 200
+    s = oracle_lib.write_core_bc(ra, ia, rb, ib, rc_, ic, m, w.kpref, w.el, w.eh, ne, w.gam0)
+    v0 = w.allow * (w.psi_r + 1j * w.psi_i)
+    ex = np.zeros(ne + 1)
+    for r in range(ne + 1):
+        z = w.el + (w.eh - w.el) * r / ne + 1j * w.gam0
+        ex[r] = w.kpref * abs(np.vdot(v0, np.linalg.solve(z * np.eye(n) - A.conj().T, v0)).imag)
+    assert np.linalg.norm(s[:, 2] - ex) < 1e-5 * np.linalg.norm(ex)
