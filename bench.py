@@ -54,6 +54,9 @@ def parse():
                     help="Lanczos steps of the 4^3 k / 32-band / 8^3 x leg, with the oracle's full run beside it; 0 = off")
     ap.add_argument("--multiplet-steps", type=int, default=200,
                     help="Lanczos steps of the 2p-edge multiplet leg (c3 sizes); 0 = off")
+    ap.add_argument("--nonherm-steps", type=int, default=60,
+                    help="steps of the non-Hermitian (two-sided Lanczos) leg on the main workload with a "
+                         "lifetime Sigma'' on the bands, both precisions; 0 = off")
     ap.add_argument("--batch", type=int, default=64,
                     help="instances of the batched uneven-Haydock leg (3 polarisations each); 0 = off")
     ap.add_argument("--adjoint-omega", type=int, default=400,
@@ -308,6 +311,35 @@ def run_small(args, torch, capi, WL, local):
     for name in ("mixed", "fp64"):
         out[name]["spectral_error_vs_oracle"] = float(np.linalg.norm(spec[name][:, 2] - so[:, 2]) /
                                                       np.linalg.norm(so[:, 2]))
+    return out
+
+
+def run_nonherm(args, torch, capi, w, local):
+    """Two-sided Lanczos (ocn_haydock_nonherm) on the main workload made
+    non-Hermitian by a band lifetime Sigma'' ~ U(0.005, 0.05) Ha: H*psi/s (two
+    actions per step, H and H^dagger) of both precisions and the spectral error."""
+    import dataclasses
+    import time
+
+    rng = np.random.default_rng(77)
+    wn = dataclasses.replace(w, ei=rng.uniform(0.005, 0.05, w.npsi))
+    niter = args.nonherm_steps
+    out = {"steps": niter, "sigma2_ha": [0.005, 0.05]}
+    spec = {}
+    for name, prec in (("mixed", capi.OCN_PREC_MIXED), ("fp64", capi.OCN_PREC_FP64)):
+        # two vectors per context: the mixed path applies H and H^dagger as one block
+        ctx = capi.Context(wn, precision=prec, device=local, nvec=2)
+        ctx.haydock_nonherm(3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        co, done = ctx.haydock_nonherm(niter)
+        dt = time.perf_counter() - t0
+        ctx.close()
+        spec[name] = capi.spectrum_cf_bc(*co, done, wn.kpref, wn.el, wn.eh, args.ne, wn.gam0)
+        out[name] = {"value": 2 * niter / dt, "unit": UNIT, "ms_per_step": dt * 1e3 / niter}
+    out["spectral_error_mixed_vs_fp64"] = float(np.linalg.norm(spec["mixed"][:, 2] - spec["fp64"][:, 2]) /
+                                                np.linalg.norm(spec["fp64"][:, 2]))
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     return out
 
 
@@ -571,6 +603,11 @@ def run_ours(args, ws, rank, local, pg):
     if rank == 0 and args.multiplet_steps > 0 and prec == capi.OCN_PREC_MIXED:
         mlt = run_multiplet(args, torch, capi, WL, local, dev)
 
+    # ---- non-Hermitian leg: two-sided Lanczos on the main workload with a band lifetime
+    nh = None
+    if rank == 0 and args.nonherm_steps > 0 and prec == capi.OCN_PREC_MIXED:
+        nh = run_nonherm(args, torch, capi, w, local)
+
     # ---- batched leg: independent uneven instances (k-mesh n^3, n in {4,5,6,8};
     #      bands U{24..128}; 1s or 2p; x-mesh 8^3..12^3), 3 polarisations each,
     #      500 Lanczos steps, all advanced by one graph launch per 3 steps
@@ -676,7 +713,7 @@ def run_ours(args, ws, rank, local, pg):
                            w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
             "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
             "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "adjoint": adj, "batch": bat,
-            "multiplet": mlt, "c1": small, "roofline": roof, "cpu_baseline": cpu,
+            "multiplet": mlt, "nonherm": nh, "c1": small, "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
                     "d2h_bytes_per_step": 3 * (niter + 1) * 8 + (ne + 1) * 9 * 8},
             "gpu_launches": launches, "clocks": clocks, "kernel_ms": kt}

@@ -83,14 +83,15 @@ int apply_H_impl(ocn_ctx* c, const double* ir, const double* ii, double* orr, do
 
 // H on a block of nv vectors (vector v at in + 2*v*npsi) -- mixed precision reads
 // the Bloch functions once for the block; the FP64 path acts vector by vector.
+// back_each (may be NULL): the backwards switch of each vector (H or H^dagger).
 int apply_H_block_impl(ocn_ctx* c, int nv, const double* in, double* out, const int* hflag_in,
-                       int backwards) {
+                       int backwards, const int* back_each = nullptr) {
   const size_t n = c->npsi;
   if (nv < 1 || nv > c->nvec) return set_err(c, OCN_ERR_ARG, "block size must be in 1..nvec");
   if (c->dims.precision != OCN_PREC_MIXED) {
     for (int v = 0; v < nv; ++v) {
       int rc = apply_H_impl(c, in + 2 * v * n, in + 2 * v * n + n, out + 2 * v * n, out + 2 * v * n + n,
-                            hflag_in, backwards);
+                            hflag_in, back_each ? back_each[v] : backwards);
       if (rc) return rc;
     }
     return OCN_OK;
@@ -114,7 +115,11 @@ int apply_H_block_impl(ocn_ctx* c, int nv, const double* in, double* out, const 
     c->acc_valid = true;
   }
   if (lr_on && (rc = lr_apply_mixed(c, in, in + n, 2 * n, nv, b1_ready))) return rc;
-  return combine(c, nv, in, in + n, out, out + n, 2 * n, hflag, backwards);
+  if (!back_each) return combine(c, nv, in, in + n, out, out + n, 2 * n, hflag, backwards);
+  for (int v = 0; v < nv && rc == OCN_OK; ++v)  // the shared terms are Hermitian; E and SO conjugate per vector
+    rc = combine(c, 1, in + 2 * v * n, in + 2 * v * n + n, out + 2 * v * n, out + 2 * v * n + n, 2 * n, hflag,
+                 back_each[v], v);
+  return rc;
 }
 
 }  // namespace
@@ -1119,14 +1124,18 @@ int ocn_haydock_nonherm(ocn_ctx* c, const double* psi0_r, const double* psi0_i, 
   const size_t n = c->npsi;
   double* pool = nullptr;
   if ((rc = dev_alloc(c, &pool, 6 * 2 * n))) return rc;
-  double *v = pool, *w = pool + 2 * n, *ov = pool + 4 * n, *ow = pool + 6 * n, *hv = pool + 8 * n,
-         *hw = pool + 10 * n;
+  // three blocks of two adjacent vectors (right, left): current, old, new;
+  // with nvec >= 2 the mixed path applies H and H^dagger as one block
+  double *cur = pool, *old = pool + 4 * n, *nxt = pool + 8 * n;
+  const bool pair = c->dims.precision == OCN_PREC_MIXED && c->mixed && c->nvec >= 2;
+  const int back_each[2] = {0, 1};
   for (int i = 0; i <= niter; ++i) real_a[i] = imag_a[i] = real_b[i] = imag_b[i] = real_c[i] = imag_c[i] = 0.0;
   if (niter_done) *niter_done = 0;
-  cudaError_t e = cudaMemcpyAsync(v, psi0_r, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(v + n, psi0_i, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(w, v, 2 * n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ov, 0, 4 * n * sizeof(double), c->stream);  // ov, ow
+  cudaError_t e = cudaMemcpyAsync(cur, psi0_r, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cur + n, psi0_i, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(cur + 2 * n, cur, 2 * n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(old, 0, 4 * n * sizeof(double), c->stream);
   if (e != cudaSuccess) {
     cudaFree(pool);
     return cuda_fail(c, e, "ocn_haydock_nonherm setup");
@@ -1143,11 +1152,20 @@ int ocn_haydock_nonherm(ocn_ctx* c, const double* psi0_r, const double* psi0_i, 
   };
   int done = 0;
   for (int it = 1; it <= niter && rc == OCN_OK; ++it) {
+    double* v = cur;
+    double* w = cur + 2 * n;
+    double* ov = old;
+    double* ow = old + 2 * n;
+    double* hv = nxt;
+    double* hw = nxt + 2 * n;
     double ar = 0, ai = 0, zr = 0, zi = 0;
-    if ((rc = vec_mask_inplace(c, v)) || (rc = vec_mask_inplace(c, w)) ||
-        (rc = apply_H_impl(c, v, v + n, hv, hv + n, nullptr, 0)) ||
-        (rc = apply_H_impl(c, w, w + n, hw, hw + n, nullptr, 1)) ||  // A^H
-        (rc = vec_mask_inplace(c, hv)) || (rc = vec_mask_inplace(c, hw)) || (rc = dot(w, hv, &ar, &ai)))
+    if ((rc = vec_mask_inplace(c, v)) || (rc = vec_mask_inplace(c, w))) break;
+    if (pair) {
+      rc = apply_H_block_impl(c, 2, cur, nxt, nullptr, 0, back_each);
+    } else if ((rc = apply_H_impl(c, v, v + n, hv, hv + n, nullptr, 0)) == OCN_OK) {
+      rc = apply_H_impl(c, w, w + n, hw, hw + n, nullptr, 1);  // A^H
+    }
+    if (rc || (rc = vec_mask_inplace(c, hv)) || (rc = vec_mask_inplace(c, hw)) || (rc = dot(w, hv, &ar, &ai)))
       break;
     // beta_j = conj(b_j), conj(delta_j) = c_j
     if ((rc = vec_axpy(c, -real_b[it - 1], imag_b[it - 1], ov, hv)) ||
@@ -1175,14 +1193,10 @@ int ocn_haydock_nonherm(ocn_ctx* c, const double* psi0_r, const double* psi0_i, 
     real_c[it] = dr;
     imag_c[it] = -di;
     if ((rc = vec_divide(c, hw, br, -bi)) || (rc = vec_divide(c, hv, dr, di))) break;  // w^/conj(beta), v^/delta
-    double* t = ov;  // old <- current, current <- new
-    ov = v;
-    v = hv;
-    hv = t;
-    t = ow;
-    ow = w;
-    w = hw;
-    hw = t;
+    double* t = old;  // old <- current, current <- new
+    old = cur;
+    cur = nxt;
+    nxt = t;
     done = it;
     if (std::isnan(ar)) {
       rc = set_err(c, OCN_ERR_NAN, "NaN in the Lanczos a_n");

@@ -248,7 +248,7 @@ int phase_bloch(ocn_ctx* c, const double* d_ur, const double* d_ui, const double
 int lr_wgrad_fp64(ocn_ctx* c, const double* x, const double* y, double2* phi, double a, double b, double* gW);
 bool lr_wgrad_supported(const ocn_ctx* c);
 int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* d_or, double* d_oi,
-            size_t vstride, const int* hflag, int backwards);
+            size_t vstride, const int* hflag, int backwards, int v0 = 0);
 int zero_acc(ocn_ctx* c, int nv);
 
 // Fused Lanczos step (combine + ocean_hay_ab_twoterm) of nv chains; coefficients stay

@@ -1037,7 +1037,7 @@ int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi, double* acc) 
 }
 
 int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* d_or, double* d_oi,
-            size_t vstride, const int* hflag, int backwards) {
+            size_t vstride, const int* hflag, int backwards, int v0) {
   const int nbk = c->nb * c->nk;
   const int use_so = (c->sys.mult && hflag[5] == 1 && c->have_so) ? 1 : 0;
   const double* parts;
@@ -1046,9 +1046,11 @@ int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* 
   const BlockStrides bs = {vstride, c->part_stride, 0, 0};
   auto kern = combine_kernel(c->na, use_so);
   dim3 grid(grid_for(c->npsi, LZ_THREADS, 4 * c->sm_count), nv);
+  // vector v0 of the block: its long-range partials and multiplet accumulator
+  parts += (size_t)v0 * 2 * c->npsi;
   kern<<<grid, LZ_THREADS, 0, c->stream>>>(
       d_pr, d_pi, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow,
-      c->acc_valid ? c->d_acc : nullptr, parts, nparts,
+      c->acc_valid ? c->d_acc + (size_t)v0 * vstride : nullptr, parts, nparts,
       c->d_so, d_or, d_oi, nbk, c->na, c->npsi, c->sys.e0, use_so, backwards, nullptr, nullptr,
       nullptr, nullptr, nullptr, bs);
   ++c->launches;

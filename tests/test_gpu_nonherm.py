@@ -74,16 +74,22 @@ def test_hermitian_problem_gives_the_haydock_spectrum(built):
     assert np.linalg.norm(s2[:, 2] - s1[:, 2]) < 1e-9 * np.linalg.norm(s1[:, 2])
 
 
-def test_mixed_precision_spectrum(built):
-    w = _nonherm("c1")
+@pytest.mark.parametrize("name", ["c1", "c3small"])
+def test_mixed_precision_spectrum(built, name):
+    """Mixed precision against FP64; with nvec = 2 the mixed path applies H and
+    H^dagger as one block (one read of the operator data)."""
+    w = _nonherm(name)
     out = {}
-    for prec in (capi.OCN_PREC_FP64, capi.OCN_PREC_MIXED):
-        ctx = capi.Context(w, precision=prec)
+    for key, prec, nvec in (("fp64", capi.OCN_PREC_FP64, 1), ("mixed", capi.OCN_PREC_MIXED, 1),
+                            ("pair", capi.OCN_PREC_MIXED, 2)):
+        ctx = capi.Context(w, precision=prec, nvec=nvec)
         try:
-            co, done = ctx.haydock_nonherm(80)
+            co, done = ctx.haydock_nonherm(60)
         finally:
             ctx.close()
-        assert done == 80
-        out[prec] = _spec(co, 80, w)[:, 2]
-    ref = out[capi.OCN_PREC_FP64]
-    assert np.linalg.norm(out[capi.OCN_PREC_MIXED] - ref) < 1e-4 * np.linalg.norm(ref)
+        assert done == 60
+        out[key] = _spec(co, 60, w)[:, 2]
+    ref = out["fp64"]
+    assert np.linalg.norm(out["mixed"] - ref) < 1e-4 * np.linalg.norm(ref)
+    assert np.linalg.norm(out["pair"] - ref) < 1e-4 * np.linalg.norm(ref)
+    assert np.linalg.norm(out["pair"] - out["mixed"]) < 1e-5 * np.linalg.norm(ref)
