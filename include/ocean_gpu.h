@@ -503,6 +503,75 @@ int ocn_timing_enable(ocn_ctx* ctx, int on);
 int ocn_timing_reset(ocn_ctx* ctx);
 int ocn_timing_read(ocn_ctx* ctx, long long counts[6], double ms[6]);
 
+/* ------------------------------------------------------- valence BSE
+ * The valence branch of OCEAN_xact (OCEAN_action.f90:521-600) for one spin
+ * channel (valence_ham_spin = 1, nspn = 1) and resonant pairs (nbw = 1):
+ *   H psi = E o psi + allow o [ 2 X(allow o psi) - D(allow o psi) ]
+ * X: AI_bubble_act (OCEAN_bubble.f90:420-796); D: OCEAN_ladder_act_single
+ * (OCEAN_ladder.f90:155-1004).  Replaces those routines and the module state
+ * they read (re/im_con, re/im_val of OCEAN_val_states, p_energy and allow of
+ * OCEAN_energies, bubble of OCEAN_bubble, ladder of OCEAN_ladder).
+ * Layouts are the reference's Fortran orders:
+ *   psi, energies, allow  (Nc, Nv, Nk)   psi%valr / valr(c, v, k)
+ *   con                   (Nx, Nc, Nk)   re_con / im_con(x, c, k)
+ *   val                   (Nx, Nv, Nk)   re_val / im_val(x, v, k)
+ *   bubble                (Nx)
+ *   ladder                (Nk, Nx, Nx)   ladder(k, x, y) after resort_ladder
+ * with the flat k index k3 fastest and the flat x index x3 fastest (the FFT
+ * orders of OCEAN_ladder_init, OCEAN_ladder.f90:1599-1695, and AI_bubble_prep,
+ * OCEAN_bubble.f90:67-157).  OCN_PREC_MIXED computes the direct term's
+ * O(Nx^2 Nk) part (A, val, ladder, k-mesh transforms, B) in FP32; the rest,
+ * and all Lanczos vectors, stay FP64. */
+typedef struct ocn_val_ctx ocn_val_ctx;
+
+typedef struct {
+  int nc, nv;     /* conduction / valence bands (1 <= nv <= 32) */
+  int kmesh[3];   /* k-mesh (each 1..32) */
+  int xmesh[3];   /* x-mesh of the states, bubble and ladder (each 1..32) */
+  int precision;  /* OCN_PREC_FP64 or OCN_PREC_MIXED */
+  int device;     /* CUDA device ordinal */
+} ocn_val_dims;
+
+int ocn_val_create(const ocn_val_dims* dims, ocn_val_ctx** out);
+int ocn_val_destroy(ocn_val_ctx* ctx);
+int ocn_val_last_error(const ocn_val_ctx* ctx, char* buf, size_t len);
+long long ocn_val_kernel_launches(const ocn_val_ctx* ctx);
+void* ocn_val_stream(ocn_val_ctx* ctx);
+
+/* Operator data (host buffers; the _dev variants take device pointers). */
+int ocn_val_set_energies(ocn_val_ctx* ctx, const double* re, const double* im /* may be NULL */);
+int ocn_val_set_allow(ocn_val_ctx* ctx, const double* allow);
+int ocn_val_set_states(ocn_val_ctx* ctx, const double* con_r, const double* con_i, const double* val_r,
+                       const double* val_i);
+int ocn_val_set_states_dev(ocn_val_ctx* ctx, const double* con_r, const double* con_i, const double* val_r,
+                           const double* val_i);
+int ocn_val_set_bubble(ocn_val_ctx* ctx, const double* bubble);
+int ocn_val_set_ladder(ocn_val_ctx* ctx, const double* ladder);
+int ocn_val_set_ladder_dev(ocn_val_ctx* ctx, const double* d_ladder);
+
+/* bubble(x) from the cell (AI_bubble_populate with wall_search_old_way,
+ * OCEAN_bubble.f90:238-407): bvec column-major (bvec[i + 3 j] = bvec(i+1, j+1),
+ * Bohr^-1), qinb = sys%qinunitsofbvectors, celvol in Bohr^3; *ngvec (may be
+ * NULL) = retained G-vectors - 1 as the reference prints it.  Host only. */
+int ocn_val_bubble_populate(const int xmesh[3], const double bvec[9], const double qinb[3], double celvol,
+                            int nkpts, double* bubble, int* ngvec);
+
+/* H psi.  flags[3] = {bande (energies), bflag & hflag(3) (exchange),
+ * lflag & hflag(2) (direct)}; backwards conjugates E (OCEAN_energies.f90:890-906).
+ * Host buffers (in/out planes of Nc*Nv*Nk); _dev: device vectors, real plane
+ * then imaginary plane (2*Nc*Nv*Nk doubles), on the context stream. */
+int ocn_val_apply_H(ocn_val_ctx* ctx, const double* in_r, const double* in_i, double* out_r, double* out_i,
+                    const int flags[3], int backwards);
+int ocn_val_apply_H_dev(ocn_val_ctx* ctx, const double* d_in, double* d_out, const int flags[3], int backwards);
+
+/* OCEAN_haydock_Herm_do with ocean_hay_ab_twoterm over the valence action
+ * (OCEAN_haydock.f90:190-320, 824-938): arrays of niter+1; OCN_ERR_NAN on a NaN
+ * a_n.  psi0 is used as given (normalise it first, core_pnorm). */
+int ocn_val_haydock(ocn_val_ctx* ctx, const double* psi0_r, const double* psi0_i, int niter, const int flags[3],
+                    double* real_a, double* imag_a, double* real_b, int* niter_done);
+int ocn_val_haydock_dev(ocn_val_ctx* ctx, const double* d_psi0, int niter, const int flags[3], double* real_a,
+                        double* imag_a, double* real_b, int* niter_done);
+
 #ifdef __cplusplus
 }
 #endif

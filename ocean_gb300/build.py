@@ -27,6 +27,7 @@ SOURCES = {
     "ocn_kernels.cu": [],
     "ocn_cf.cu": ["-fmad=false"],
     "ocn_mixed.cu": [],
+    "ocn_valence.cu": [],
     "ocn_setup.cpp": [],
     "ocn_io.cpp": [],
 }

@@ -85,6 +85,10 @@ EXPORTS = [
     "ocn_read_bse_in", "ocn_write_abslanc", "ocn_write_absspct", "ocn_write_abs_gmres", "ocn_output_filename",
     "ocn_read_u2dat", "ocn_read_rpottrim", "ocn_read_energies", "ocn_read_cks", "ocn_cks_to_mpc", "ocn_read_cmel",
     "ocn_input_filename", "ocn_haydock_nonherm", "ocn_spectrum_cf_bc",
+    "ocn_val_create", "ocn_val_destroy", "ocn_val_last_error", "ocn_val_kernel_launches", "ocn_val_stream",
+    "ocn_val_set_energies", "ocn_val_set_allow", "ocn_val_set_states", "ocn_val_set_states_dev",
+    "ocn_val_set_bubble", "ocn_val_set_ladder", "ocn_val_set_ladder_dev", "ocn_val_bubble_populate",
+    "ocn_val_apply_H", "ocn_val_apply_H_dev", "ocn_val_haydock", "ocn_val_haydock_dev",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -184,6 +188,8 @@ def load(path: str = LIB_PATH):
         lib.ocn_version.restype = C.c_char_p
         lib.ocn_kernel_launches.restype = C.c_longlong
         lib.ocn_stream.restype = C.c_void_p
+        lib.ocn_val_kernel_launches.restype = C.c_longlong
+        lib.ocn_val_stream.restype = C.c_void_p
         _LIB = lib
     return _LIB
 
@@ -622,3 +628,116 @@ def pnorm(pr, pi, nkpts: int, celvol: float):
     kp = C.c_double(0.0)
     check(load().ocn_psi_pnorm(len(pr), nkpts, C.c_double(celvol), _dp(pr), _dp(pi), C.byref(kp)))
     return pr, pi, kp.value
+
+
+# ---------------------------------------------------------------- valence BSE
+
+class OcnValDims(C.Structure):
+    _fields_ = [("nc", C.c_int), ("nv", C.c_int), ("kmesh", C.c_int * 3), ("xmesh", C.c_int * 3),
+                ("precision", C.c_int), ("device", C.c_int)]
+
+
+def val_last_error(ctx=None) -> str:
+    buf = C.create_string_buffer(1024)
+    load().ocn_val_last_error(ctx, buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def val_bubble(xmesh, bvec, qinb, celvol: float, nkpts: int):
+    """bubble(x) of AI_bubble_populate (host code of the library); returns (bubble, ngvec)."""
+    out = np.zeros(int(np.prod(xmesh)))
+    ng = C.c_int(0)
+    rc = load().ocn_val_bubble_populate((C.c_int * 3)(*xmesh), (C.c_double * 9)(*list(bvec)),
+                                        (C.c_double * 3)(*list(qinb)), C.c_double(celvol), int(nkpts), _dp(out),
+                                        C.byref(ng))
+    if rc != 0:
+        raise OcnError(rc, val_last_error())
+    return out, ng.value
+
+
+class ValContext:
+    """One valence BSE problem on one GPU: the module state of OCEAN_val_states,
+    OCEAN_val_energy, OCEAN_bubble and OCEAN_ladder, and the valence action."""
+
+    def __init__(self, w, precision: int = OCN_PREC_FP64, device: int = 0):
+        lib = load()
+        self.w = w
+        self.lib = lib
+        d = OcnValDims()
+        d.nc, d.nv = w.nc, w.nv
+        d.kmesh[:] = list(w.kmesh)
+        d.xmesh[:] = list(w.xmesh)
+        d.precision = precision
+        d.device = device
+        self.ptr = C.c_void_p()
+        rc = lib.ocn_val_create(C.byref(d), C.byref(self.ptr))
+        if rc != 0:
+            raise OcnError(rc, val_last_error())
+        try:
+            self._chk(lib.ocn_val_set_energies(self.ptr, _dp(_f64(w.er)), _dp(_f64(w.ei))))
+            self._chk(lib.ocn_val_set_allow(self.ptr, _dp(_f64(w.allow))))
+            self.bubble, self.ngvec = val_bubble(w.xmesh, w.bvec, w.qinb, w.celvol, w.nk)
+            self._chk(lib.ocn_val_set_bubble(self.ptr, _dp(self.bubble)))
+            if w.conr is not None:
+                self._chk(lib.ocn_val_set_states(self.ptr, _dp(_f64(w.conr)), _dp(_f64(w.coni)),
+                                                 _dp(_f64(w.valr)), _dp(_f64(w.vali))))
+                self._chk(lib.ocn_val_set_ladder(self.ptr, _dp(_f64(w.ladder))))
+            else:
+                a = w.device_arrays
+                self._chk(lib.ocn_val_set_states_dev(self.ptr, *[C.c_void_p(a[k].data_ptr()) for k in
+                                                                 ("conr", "coni", "valr", "vali")]))
+                self._chk(lib.ocn_val_set_ladder_dev(self.ptr, C.c_void_p(a["ladder"].data_ptr())))
+        except Exception:
+            self.close()
+            raise
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise OcnError(rc, val_last_error(self.ptr))
+
+    def close(self):
+        if self.ptr:
+            self.lib.ocn_val_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.ocn_val_kernel_launches(self.ptr))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.ocn_val_stream(self.ptr) or 0)
+
+    def apply_H(self, pr, pi, flags=(1, 1, 1), backwards=False):
+        n = self.w.npsi
+        hr, hi = np.zeros(n), np.zeros(n)
+        self._chk(self.lib.ocn_val_apply_H(self.ptr, _dp(_f64(pr)), _dp(_f64(pi)), _dp(hr), _dp(hi),
+                                           (C.c_int * 3)(*flags), int(bool(backwards))))
+        return hr, hi
+
+    def apply_H_dev(self, d_in: int, d_out: int, flags=(1, 1, 1), backwards=False):
+        self._chk(self.lib.ocn_val_apply_H_dev(self.ptr, C.c_void_p(d_in), C.c_void_p(d_out),
+                                               (C.c_int * 3)(*flags), int(bool(backwards))))
+
+    def haydock(self, niter: int, pr=None, pi=None, flags=(1, 1, 1)):
+        w = self.w
+        pr = _f64(w.psi_r if pr is None else pr)
+        pi = _f64(w.psi_i if pi is None else pi)
+        ra, ia, rb = np.zeros(niter + 1), np.zeros(niter + 1), np.zeros(niter + 1)
+        done = C.c_int(0)
+        self._chk(self.lib.ocn_val_haydock(self.ptr, _dp(pr), _dp(pi), niter, (C.c_int * 3)(*flags), _dp(ra),
+                                           _dp(ia), _dp(rb), C.byref(done)))
+        return ra, ia, rb, done.value
+
+    def haydock_dev(self, niter: int, d_psi0: int, flags=(1, 1, 1)):
+        ra, ia, rb = np.zeros(niter + 1), np.zeros(niter + 1), np.zeros(niter + 1)
+        done = C.c_int(0)
+        self._chk(self.lib.ocn_val_haydock_dev(self.ptr, C.c_void_p(d_psi0), niter, (C.c_int * 3)(*flags),
+                                               _dp(ra), _dp(ia), _dp(rb), C.byref(done)))
+        return ra, ia, rb, done.value

@@ -1,0 +1,1065 @@
+// ocn_valence.cu -- the valence BSE action and its Haydock recursion on one GPU.
+//
+//   H psi = E o psi + allow o [ 2 X(allow o psi) - D(allow o psi) ]
+//
+// X: exchange ("bubble", OCEAN2/OCEAN_bubble.f90:420-796); D: screened direct
+// ("ladder", OCEAN2/OCEAN_ladder.f90:155-1004); order of OCEAN_xact's valence
+// branch (OCEAN2/OCEAN_action.f90:521-600).  One spin channel
+// (valence_ham_spin = 1) and resonant pairs (nbw = 1).
+//
+// Both terms start from A(x,v,k) = sum_c con(x,c,k) psi(c,v,k) and end with
+// out(c,v,k) = sum_x conj(con(x,c,k)) M(x,v,k), so one kernel builds A (and the
+// exchange partials l_k(x) = sum_v conj(val) A), one projects
+// M = 2 s(x) val - B back onto the pairs, and in between
+//   exchange: l(x) = sum_k l_k(x); s = FFT_fwd[bubble o FFT_bwd[l]] on the x-mesh
+//   direct:   per x (one CTA) and a range of y: T(y,k) = sum_v A(x,v,k)
+//             conj(val(y,v,k)), FFT_fwd over k, times ladder(k,x,y), FFT_bwd,
+//             and B(x,v,k) += sum_y T(y,k) val(y,v,k) -- T never leaves shared
+//             memory (the reference stores all Nx*Ny*Nk of it).
+// The direct term is the O(Nx^2 Nk) part: FP64 in OCN_PREC_FP64, FP32 (A, val,
+// ladder, transforms, B) in OCN_PREC_MIXED; everything else is FP64.
+//
+// Device layouts: psi/E/allow (Nc,Nv,Nk) planes as in the reference;
+// con [k][c][x] and val [k][v][x] interleaved complex (the reference's (x,c,k)
+// order); valT [y][v][k] and the ladder [y][x][k] (the reference's
+// ladder(k,x,y)) with k fastest for the transforms.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "ocn_internal.h"
+#include "ocn_kmesh_dft.cuh"
+
+namespace {
+
+using ocn::C2;
+using ocn::KmeshGeom;
+
+constexpr int VAL_MAX_NV = 32;
+constexpr int VAL_CC = 16;        // conduction bands staged per pass of kv_amat
+constexpr int VAL_THREADS = 256;
+constexpr int VAL_FIN_WARPS = VAL_THREADS / 32;
+
+std::string g_val_create_err;
+
+}  // namespace
+
+struct ocn_val_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  size_t smem_optin = 0;
+  ocn_val_dims dims{};
+  int nc = 0, nv = 0, nk = 0, nx = 0;
+  size_t npsi = 0;
+  int mixed = 0;
+  bool have_e = false, have_allow = false, have_states = false, have_bubble = false, have_ladder = false;
+  bool ei_nonzero = false;
+  double* d_er = nullptr;
+  double* d_ei = nullptr;
+  double* d_allow = nullptr;
+  double2* d_con = nullptr;   // [k][c][x]
+  double2* d_val = nullptr;   // [k][v][x]
+  void* d_valT = nullptr;     // [y][v][k], double2 or float2
+  void* d_lad = nullptr;      // [y][x][k], double or float
+  double* d_bub = nullptr;    // [x]
+  double2* d_twk = nullptr;   // exp(+2 pi i t / n_axis) for the k-mesh, [axis][t]
+  float2* d_twk32 = nullptr;
+  double2* d_twx = nullptr;   // same for the x-mesh
+  double2* d_lp = nullptr;    // exchange partials [k][x]
+  double2* d_s = nullptr;     // s(x)
+  void* d_A = nullptr;        // [x][v][k] in the direct term's precision
+  void* d_Bp = nullptr;       // [ys][k][v][x] in the direct term's precision
+  double* d_vec = nullptr;    // 4 vectors of 2*npsi: in/psi, out/h, old, spare
+  double* d_red = nullptr;
+  double* d_coef = nullptr;
+  int coef_cap = 0;
+  int red_blocks = 1;
+  int ytile = 1, ysplit = 1, yper = 1;
+  size_t lad_smem = 0;
+  long long launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int vset_err(ocn_val_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  else g_val_create_err = msg;
+  return code;
+}
+
+int vcuda(ocn_val_ctx* c, cudaError_t e, const char* what) {
+  return vset_err(c, OCN_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define VCUDA(c, call)                                   \
+  do {                                                   \
+    cudaError_t _e = (call);                             \
+    if (_e != cudaSuccess) return vcuda(c, _e, #call);   \
+  } while (0)
+
+template <typename T>
+int valloc(ocn_val_ctx* c, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return OCN_OK;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+  if (e != cudaSuccess) return vset_err(c, OCN_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return OCN_OK;
+}
+
+// ------------------------------------------------------------------ kernels
+
+// A(x,v,k) = sum_c con(x,c,k) (allow o psi)(c,v,k) (OCEAN_bubble.f90:521-530,
+// OCEAN_ladder.f90:317-326) and the exchange partial
+// l_k(x) = sum_v conj(val(x,v,k)) A(x,v,k) (OCEAN_bubble.f90:568-580).
+// Block: 32 x-points by 8 k-points; lanes along x read con rows coalesced.
+template <typename R, int MAXV>
+__global__ void __launch_bounds__(VAL_THREADS)
+    kv_amat(const double* __restrict__ pr, const double* __restrict__ pi, const double* __restrict__ allow,
+            const double2* __restrict__ con, const double2* __restrict__ val, int nc, int nv, int nk, int nx,
+            double2* __restrict__ lp, typename C2<R>::T* __restrict__ A) {
+  typedef typename C2<R>::T CT;
+  extern __shared__ double2 qs[];  // [kl][cl][v]
+  const int xl = threadIdx.x, kl = threadIdx.y;
+  const int tid = kl * 32 + xl;
+  const int x = blockIdx.x * 32 + xl, k0 = blockIdx.y * 8, k = k0 + kl;
+  double2 acc[MAXV];
+#pragma unroll
+  for (int v = 0; v < MAXV; ++v) acc[v] = make_double2(0.0, 0.0);
+  for (int c0 = 0; c0 < nc; c0 += VAL_CC) {
+    const int cn = min(VAL_CC, nc - c0);
+    __syncthreads();
+    for (int e = tid; e < 8 * VAL_CC * nv; e += VAL_THREADS) {
+      const int kk = e / (VAL_CC * nv), r = e % (VAL_CC * nv);
+      const int cl = r / nv, v = r % nv;
+      double2 q = make_double2(0.0, 0.0);
+      if (k0 + kk < nk && cl < cn) {
+        const size_t idx = (size_t)(c0 + cl) + (size_t)nc * (v + (size_t)nv * (k0 + kk));
+        const double m = allow[idx];
+        q = make_double2(pr[idx] * m, pi[idx] * m);
+      }
+      qs[e] = q;
+    }
+    __syncthreads();
+    if (x < nx && k < nk) {
+      for (int cl = 0; cl < cn; ++cl) {
+        const double2 cv = con[((size_t)k * nc + c0 + cl) * nx + x];
+        const double2* q = qs + (kl * VAL_CC + cl) * nv;
+#pragma unroll
+        for (int v = 0; v < MAXV; ++v)
+          if (v < nv) {
+            const double2 qq = q[v];
+            acc[v].x += cv.x * qq.x - cv.y * qq.y;
+            acc[v].y += cv.y * qq.x + cv.x * qq.y;
+          }
+      }
+    }
+  }
+  if (x < nx && k < nk) {
+    double lr = 0.0, li = 0.0;
+#pragma unroll
+    for (int v = 0; v < MAXV; ++v)
+      if (v < nv) {
+        const double2 vv = val[((size_t)k * nv + v) * nx + x];
+        lr += vv.x * acc[v].x + vv.y * acc[v].y;
+        li += vv.x * acc[v].y - vv.y * acc[v].x;
+        CT a;
+        a.x = (R)acc[v].x;
+        a.y = (R)acc[v].y;
+        A[((size_t)x * nv + v) * nk + k] = a;
+      }
+    lp[(size_t)k * nx + x] = make_double2(lr, li);
+  }
+}
+
+// l(x) = sum_k l_k(x), k in order.
+__global__ void kv_bub_reduce(const double2* __restrict__ lp, int nk, int nx, double2* __restrict__ l) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= nx) return;
+  double sr = 0.0, si = 0.0;
+  for (int k = 0; k < nk; ++k) {
+    const double2 t = lp[(size_t)k * nx + x];
+    sr += t.x;
+    si += t.y;
+  }
+  l[x] = make_double2(sr, si);
+}
+
+// s = FFT_fwd[ bubble o FFT_bwd[ l ] ] on the x-mesh, neither normalised
+// (OCEAN_bubble.f90:663-665; FFTW signs +1 backward, -1 forward,
+// Modules/FFT_wrapper.f90:24-25).  One CTA; the mesh is a few thousand points.
+__global__ void kv_bub_fft(double2* __restrict__ l, const double* __restrict__ bub, int nx,
+                           const KmeshGeom<double> g, const double2* __restrict__ twg) {
+  extern __shared__ double2 sm[];
+  double2* tw = sm;
+  double2* buf = sm + 3 * OCN_MAX_KDIM;
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) buf[ocn::kpad(g, x)] = l[x];
+  __syncthreads();
+  for (int ax = 0; ax < 3; ++ax) {
+    ocn::dft_pass<double>(buf, g, ax, tw + ax * OCN_MAX_KDIM, 1.0);
+    __syncthreads();
+  }
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) {
+    double2& v = buf[ocn::kpad(g, x)];
+    v.x *= bub[x];
+    v.y *= bub[x];
+  }
+  __syncthreads();
+  for (int ax = 0; ax < 3; ++ax) {
+    ocn::dft_pass<double>(buf, g, ax, tw + ax * OCN_MAX_KDIM, -1.0);
+    __syncthreads();
+  }
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) l[x] = buf[ocn::kpad(g, x)];
+}
+
+// Direct term for the x-point of this CTA and the y-range blockIdx.y
+// (OCEAN_ladder.f90:438-449 T, :596-624 transforms and ladder, :711-720 B).
+// N > 0: cubic k-mesh N^3 (radix butterflies); N == 0: any mesh.
+template <typename R, int N>
+__global__ void __launch_bounds__(VAL_THREADS)
+    kv_ladder(const typename C2<R>::T* __restrict__ A, const typename C2<R>::T* __restrict__ valT,
+              const R* __restrict__ lad, typename C2<R>::T* __restrict__ Bp, int nv, int nk, int nx, int ytile,
+              int yper, const KmeshGeom<R> g, int slab, const typename C2<R>::T* __restrict__ twg) {
+  typedef typename C2<R>::T CT;
+  extern __shared__ __align__(16) unsigned char vsm[];
+  CT* tw = reinterpret_cast<CT*>(vsm);
+  CT* As = tw + 3 * OCN_MAX_KDIM;
+  CT* Bs = As + (size_t)nv * nk;
+  CT* T = Bs + (size_t)nv * nk;
+  const int x = blockIdx.x, ys = blockIdx.y;
+  const int ybeg = ys * yper, yend = min(nx, ybeg + yper);
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
+  const CT* Ax = A + (size_t)x * nv * nk;
+  for (int e = threadIdx.x; e < nv * nk; e += blockDim.x) {
+    As[e] = Ax[e];
+    CT z;
+    z.x = (R)0;
+    z.y = (R)0;
+    Bs[e] = z;
+  }
+  auto kp = [&](int k) -> int {
+    if constexpr (N > 0) return (k / N) * (N + 1) + k % N;
+    else return ocn::kpad(g, k);
+  };
+  __syncthreads();
+  for (int y0 = ybeg; y0 < yend; y0 += ytile) {
+    const int ny = min(ytile, yend - y0);
+    for (int e = threadIdx.x; e < ny * nk; e += blockDim.x) {
+      const int yl = e / nk, k = e % nk;
+      const CT* vt = valT + (size_t)(y0 + yl) * nv * nk + k;
+      R sr = (R)0, si = (R)0;
+      for (int v = 0; v < nv; ++v) {
+        const CT a = As[v * nk + k], b = vt[(size_t)v * nk];
+        sr += a.x * b.x + a.y * b.y;
+        si += a.y * b.x - a.x * b.y;
+      }
+      CT t;
+      t.x = sr;
+      t.y = si;
+      T[yl * slab + kp(k)] = t;
+    }
+    __syncthreads();
+    KmeshGeom<R> gg = g;
+    gg.na = ny;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      if constexpr (N > 0) ocn::cube_pass<R, N, 0>(T, ny, ax, tw + ax * OCN_MAX_KDIM, (R)-1);
+      else ocn::dft_pass<R>(T, gg, ax, tw + ax * OCN_MAX_KDIM, (R)-1);
+      __syncthreads();
+    }
+    for (int e = threadIdx.x; e < ny * nk; e += blockDim.x) {
+      const int yl = e / nk, k = e % nk;
+      const R w = lad[((size_t)(y0 + yl) * nx + x) * nk + k];
+      CT& t = T[yl * slab + kp(k)];
+      t.x *= w;
+      t.y *= w;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      if constexpr (N > 0) ocn::cube_pass<R, N, 0>(T, ny, ax, tw + ax * OCN_MAX_KDIM, (R)1);
+      else ocn::dft_pass<R>(T, gg, ax, tw + ax * OCN_MAX_KDIM, (R)1);
+      __syncthreads();
+    }
+    for (int e = threadIdx.x; e < nv * nk; e += blockDim.x) {
+      const int v = e / nk, k = e % nk;
+      CT acc = Bs[e];
+      const CT* vt = valT + ((size_t)y0 * nv + v) * nk + k;
+      for (int yl = 0; yl < ny; ++yl) {
+        const CT t = T[yl * slab + kp(k)];
+        const CT b = vt[(size_t)yl * nv * nk];
+        acc.x += t.x * b.x - t.y * b.y;
+        acc.y += t.y * b.x + t.x * b.y;
+      }
+      Bs[e] = acc;
+    }
+    __syncthreads();
+  }
+  const R inv = (R)1 / (R)nk;  // FFT_wrapper_single's backward normalisation
+  for (int e = threadIdx.x; e < nv * nk; e += blockDim.x) {
+    const int v = e / nk, k = e % nk;
+    CT o = Bs[e];
+    o.x *= inv;
+    o.y *= inv;
+    Bp[(((size_t)ys * nk + k) * nv + v) * nx + x] = o;
+  }
+}
+
+// out(c,v,k) = E o psi (conj E when backwards) + allow o sum_x conj(con(x,c,k))
+// M(x,v,k), M = 2 s(x) val(x,v,k) - sum_ys B_ys(x,v,k) (OCEAN_bubble.f90:742-757
+// with spin_prefac 2, OCEAN_ladder.f90:900-911 with -1, OCEAN_energies.f90:890-906).
+// One CTA per k; a warp owns (c,v) outputs and its lanes run over x.
+template <typename R>
+__global__ void __launch_bounds__(VAL_THREADS)
+    kv_final(const double* __restrict__ pr, const double* __restrict__ pi, const double* __restrict__ er,
+             const double* __restrict__ ei, const double* __restrict__ allow, const double2* __restrict__ con,
+             const double2* __restrict__ val, const double2* __restrict__ s, const typename C2<R>::T* __restrict__ Bp,
+             int nysplit, int nc, int nv, int nk, int nx, int xchunk, int use_e, int use_x, int use_d, int backwards,
+             double* __restrict__ outr, double* __restrict__ outi) {
+  typedef typename C2<R>::T CT;
+  extern __shared__ double2 fsm[];
+  double2* accs = fsm;               // [c + nc v]
+  double2* M = fsm + (size_t)nc * nv;  // [v][xl]
+  const int k = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nout = nc * nv;
+  for (int o = threadIdx.x; o < nout; o += blockDim.x) accs[o] = make_double2(0.0, 0.0);
+  if (use_x || use_d) {
+    for (int x0 = 0; x0 < nx; x0 += xchunk) {
+      const int xn = min(xchunk, nx - x0);
+      __syncthreads();
+      for (int e = threadIdx.x; e < nv * xn; e += blockDim.x) {
+        const int v = e / xn, xl = e % xn, x = x0 + xl;
+        double mr = 0.0, mi = 0.0;
+        if (use_x) {
+          const double2 vv = val[((size_t)k * nv + v) * nx + x];
+          const double2 ss = s[x];
+          mr = 2.0 * (ss.x * vv.x - ss.y * vv.y);
+          mi = 2.0 * (ss.y * vv.x + ss.x * vv.y);
+        }
+        if (use_d)
+          for (int ys = 0; ys < nysplit; ++ys) {
+            const CT b = Bp[(((size_t)ys * nk + k) * nv + v) * nx + x];
+            mr -= (double)b.x;
+            mi -= (double)b.y;
+          }
+        M[(size_t)v * xchunk + xl] = make_double2(mr, mi);
+      }
+      __syncthreads();
+      for (int o = warp; o < nout; o += VAL_FIN_WARPS) {
+        const int c = o % nc, v = o / nc;
+        const double2* cr = con + ((size_t)k * nc + c) * nx + x0;
+        const double2* mv = M + (size_t)v * xchunk;
+        double sr = 0.0, si = 0.0;
+        for (int xl = lane; xl < xn; xl += 32) {
+          const double2 cc = cr[xl], m = mv[xl];
+          sr += cc.x * m.x + cc.y * m.y;
+          si += cc.x * m.y - cc.y * m.x;
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+          sr += __shfl_down_sync(0xffffffffu, sr, off);
+          si += __shfl_down_sync(0xffffffffu, si, off);
+        }
+        if (lane == 0) {
+          accs[o].x += sr;
+          accs[o].y += si;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int o = threadIdx.x; o < nout; o += blockDim.x) {
+    const int c = o % nc, v = o / nc;
+    const size_t idx = (size_t)c + (size_t)nc * (v + (size_t)nv * k);
+    double hr = 0.0, hi = 0.0;
+    if (use_e) {
+      const double a = er[idx], b = ei ? ei[idx] : 0.0, qr = pr[idx], qi = pi[idx];
+      if (backwards) {
+        hr = a * qr + b * qi;
+        hi = a * qi - b * qr;
+      } else {
+        hr = a * qr - b * qi;
+        hi = a * qi + b * qr;
+      }
+    }
+    const double m = allow[idx];
+    outr[idx] = hr + m * accs[o].x;
+    outi[idx] = hi + m * accs[o].y;
+  }
+}
+
+// planes (x, i, k) -> interleaved [k][i][x] (same order) and, for val, the
+// transposed copy [x][i][k] used by the direct term.
+__global__ void kv_interleave(const double* __restrict__ re, const double* __restrict__ im, size_t n,
+                              double2* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = make_double2(re[i], im[i]);
+}
+
+template <typename R>
+__global__ void kv_transpose_val(const double2* __restrict__ val, int nv, int nk, int nx,
+                                 typename C2<R>::T* __restrict__ valT) {
+  const size_t n = (size_t)nx * nv * nk;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i % nk);
+    const size_t r = i / nk;
+    const int v = (int)(r % nv);
+    const int y = (int)(r / nv);
+    const double2 t = val[((size_t)k * nv + v) * nx + y];
+    typename C2<R>::T o;
+    o.x = (R)t.x;
+    o.y = (R)t.y;
+    valT[i] = o;
+  }
+}
+
+__global__ void kv_to_float(const double* __restrict__ in, size_t n, float* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+// ------------------------------------------------------- Lanczos kernels
+// ocean_hay_ab_twoterm (OCEAN_haydock.f90:824-938) in three stages; every block
+// re-adds the block partials in the same fixed order.
+
+__device__ __forceinline__ void kv_block_pair(double a, double b, double* red) {
+  __shared__ double sh[2][32];
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = a;
+    sh[1][w] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+      s0 += sh[0][i];
+      s1 += sh[1][i];
+    }
+    red[2 * blockIdx.x] = s0;
+    red[2 * blockIdx.x + 1] = s1;
+  }
+}
+
+__device__ __forceinline__ void kv_sum_pairs(const double* red, int nb, double* s0, double* s1) {
+  __shared__ double sh[2][32];
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    a += red[2 * i];
+    b += red[2 * i + 1];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = a;
+    sh[1][w] = b;
+  }
+  __syncthreads();
+  double ta = 0.0, tb = 0.0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+    ta += sh[0][i];
+    tb += sh[1][i];
+  }
+  *s0 = ta;
+  *s1 = tb;
+}
+
+// h -= b_{i-1} old; partial <h|psi> = sum conj(h) psi (OCEAN_psi.f90:2029-2034)
+__global__ void __launch_bounds__(VAL_THREADS)
+    kv_lz1(double* __restrict__ h, const double* __restrict__ old, const double* __restrict__ psi, size_t n,
+           const double* __restrict__ rb, int it, double* __restrict__ red) {
+  const double bm = it > 0 ? -rb[it - 1] : 0.0;
+  double dr = 0.0, di = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const double hr = h[e] + bm * old[e], hi = h[n + e] + bm * old[n + e];
+    h[e] = hr;
+    h[n + e] = hi;
+    const double qr = psi[e], qi = psi[n + e];
+    dr += hr * qr + hi * qi;
+    di += hr * qi - hi * qr;
+  }
+  kv_block_pair(dr, di, red);
+}
+
+// a_{i-1} = Re<h|psi>; h -= a psi; partial |h|^2
+__global__ void __launch_bounds__(VAL_THREADS)
+    kv_lz2(const double* __restrict__ red1, int nb, double* __restrict__ h, const double* __restrict__ psi,
+           size_t n, double* __restrict__ ra, double* __restrict__ ia, int it, double* __restrict__ red2) {
+  double a, ai;
+  kv_sum_pairs(red1, nb, &a, &ai);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ra[it - 1] = a;
+    ia[it - 1] = ai;
+  }
+  const double am = -a;
+  double s = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const double r = h[e] + am * psi[e], i = h[n + e] + am * psi[n + e];
+    h[e] = r;
+    h[n + e] = i;
+    s += r * r + i * i;
+  }
+  __syncthreads();
+  kv_block_pair(s, 0.0, red2);
+}
+
+// b_i = sqrt(sum); psi_new = h / b_i in place
+__global__ void __launch_bounds__(VAL_THREADS)
+    kv_lz3(const double* __restrict__ red2, int nb, double* __restrict__ h, size_t n, double* __restrict__ rb,
+           int it) {
+  double bb, dummy;
+  kv_sum_pairs(red2, nb, &bb, &dummy);
+  const double b = sqrt(bb);
+  if (blockIdx.x == 0 && threadIdx.x == 0) rb[it] = b;
+  const double inv = 1.0 / b;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < 2 * n; e += (size_t)gridDim.x * blockDim.x)
+    h[e] *= inv;
+}
+
+// ---------------------------------------------------------------- host side
+
+int grid_for(size_t n, int threads, int cap) {
+  return (int)std::max<size_t>(1, std::min<size_t>((n + threads - 1) / threads, (size_t)cap));
+}
+
+void twiddles(const int n3[3], double2 out[3][OCN_MAX_KDIM]) {
+  const double pi = 3.1415926535897932384626433832795;
+  for (int a = 0; a < 3; ++a)
+    for (int t = 0; t < OCN_MAX_KDIM; ++t)
+      out[a][t] = t < n3[a] ? make_double2(cos(2.0 * pi * t / n3[a]), sin(2.0 * pi * t / n3[a]))
+                            : make_double2(0.0, 0.0);
+}
+
+bool cubic(const int m[3]) { return m[0] == m[1] && m[1] == m[2]; }
+bool cube_kernel_n(int n) { return n == 2 || n == 3 || n == 4 || n == 5 || n == 6 || n == 8; }
+
+template <typename R>
+size_t ladder_slab(const ocn_val_ctx* c) {
+  if (cubic(c->dims.kmesh) && cube_kernel_n(c->dims.kmesh[0]))
+    return (size_t)ocn::cube_slab<typename C2<R>::T>(c->dims.kmesh[0]);
+  return (size_t)c->dims.kmesh[0] * c->dims.kmesh[1] * (c->dims.kmesh[2] + 1);
+}
+
+template <typename R>
+size_t ladder_smem(const ocn_val_ctx* c, int ytile) {
+  return sizeof(typename C2<R>::T) *
+         (3 * OCN_MAX_KDIM + 2 * (size_t)c->nv * c->nk + (size_t)ytile * ladder_slab<R>(c));
+}
+
+template <typename R>
+using LadderFn = void (*)(const typename C2<R>::T*, const typename C2<R>::T*, const R*, typename C2<R>::T*, int,
+                          int, int, int, int, const KmeshGeom<R>, int, const typename C2<R>::T*);
+
+template <typename R>
+LadderFn<R> ladder_fn(const ocn_val_ctx* c) {
+  if (cubic(c->dims.kmesh)) switch (c->dims.kmesh[0]) {
+      case 2: return kv_ladder<R, 2>;
+      case 3: return kv_ladder<R, 3>;
+      case 4: return kv_ladder<R, 4>;
+      case 5: return kv_ladder<R, 5>;
+      case 6: return kv_ladder<R, 6>;
+      case 8: return kv_ladder<R, 8>;
+    }
+  return kv_ladder<R, 0>;
+}
+
+// y-tile from the shared-memory budget (two CTAs per SM where it fits), and
+// enough y-ranges per x-point for about two waves of CTAs.
+template <typename R>
+int plan_ladder(ocn_val_ctx* c) {
+  int ytile = 16;
+  const size_t target = std::min<size_t>(c->smem_optin, 110 * 1024);
+  while (ytile > 1 && ladder_smem<R>(c, ytile) > target) --ytile;
+  if (ladder_smem<R>(c, ytile) > c->smem_optin)
+    return vset_err(c, OCN_ERR_UNSUPPORTED,
+                    "ocn_val: Nv*Nk too large for the direct-term kernel's shared memory");
+  c->ytile = ytile;
+  c->lad_smem = ladder_smem<R>(c, ytile);
+  const int want = std::max(1, (4 * c->sm_count + c->nx - 1) / c->nx);
+  const int maxsplit = std::max(1, (c->nx + ytile - 1) / ytile);
+  c->ysplit = std::min(want, maxsplit);
+  c->yper = (c->nx + c->ysplit - 1) / c->ysplit;
+  c->ysplit = (c->nx + c->yper - 1) / c->yper;
+  cudaError_t e = cudaFuncSetAttribute(ladder_fn<R>(c), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)c->lad_smem);
+  if (e != cudaSuccess) return vcuda(c, e, "cudaFuncSetAttribute(kv_ladder)");
+  return OCN_OK;
+}
+
+size_t final_xchunk(const ocn_val_ctx* c) {
+  const size_t outs = sizeof(double2) * (size_t)c->nc * c->nv;
+  const size_t budget = outs < 48 * 1024 ? 64 * 1024 - outs : 16 * 1024;
+  size_t xc = budget / (sizeof(double2) * c->nv);
+  xc = std::max<size_t>(32, std::min<size_t>(xc, (size_t)c->nx));
+  return xc;
+}
+
+int check_ready(ocn_val_ctx* c, const int flags[3]) {
+  if (flags[0] && !c->have_e) return vset_err(c, OCN_ERR_STATE, "ocn_val: energies not set");
+  if (!c->have_allow) return vset_err(c, OCN_ERR_STATE, "ocn_val: allow mask not set");
+  if ((flags[1] || flags[2]) && !c->have_states) return vset_err(c, OCN_ERR_STATE, "ocn_val: states not set");
+  if (flags[1] && !c->have_bubble) return vset_err(c, OCN_ERR_STATE, "ocn_val: bubble not set");
+  if (flags[2] && !c->have_ladder) return vset_err(c, OCN_ERR_STATE, "ocn_val: ladder not set");
+  return OCN_OK;
+}
+
+template <typename R>
+int apply_impl(ocn_val_ctx* c, const double* d_in, double* d_out, const int flags[3], int backwards) {
+  typedef typename C2<R>::T CT;
+  const size_t n = c->npsi;
+  const int use_e = flags[0], use_x = flags[1], use_d = flags[2];
+  CT* A = static_cast<CT*>(c->d_A);
+  CT* Bp = static_cast<CT*>(c->d_Bp);
+  if (use_x || use_d) {
+    dim3 blk(32, 8), grd((c->nx + 31) / 32, (c->nk + 7) / 8);
+    const size_t sm = sizeof(double2) * 8 * VAL_CC * c->nv;
+    if (c->nv <= 4)
+      kv_amat<R, 4><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, c->d_con, c->d_val, c->nc, c->nv,
+                                                 c->nk, c->nx, c->d_lp, A);
+    else if (c->nv <= 8)
+      kv_amat<R, 8><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, c->d_con, c->d_val, c->nc, c->nv,
+                                                 c->nk, c->nx, c->d_lp, A);
+    else if (c->nv <= 16)
+      kv_amat<R, 16><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, c->d_con, c->d_val, c->nc, c->nv,
+                                                  c->nk, c->nx, c->d_lp, A);
+    else
+      kv_amat<R, 32><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, c->d_con, c->d_val, c->nc, c->nv,
+                                                  c->nk, c->nx, c->d_lp, A);
+    ++c->launches;
+    VCUDA(c, cudaGetLastError());
+  }
+  if (use_x) {
+    kv_bub_reduce<<<(c->nx + 255) / 256, 256, 0, c->stream>>>(c->d_lp, c->nk, c->nx, c->d_s);
+    const KmeshGeom<double> gx = ocn::kmesh_geom<double>(c->dims.xmesh, 1);
+    kv_bub_fft<<<1, VAL_THREADS, ocn::kmesh_smem(gx), c->stream>>>(c->d_s, c->d_bub, c->nx, gx, c->d_twx);
+    c->launches += 2;
+    VCUDA(c, cudaGetLastError());
+  }
+  if (use_d) {
+    KmeshGeom<R> g = ocn::kmesh_geom<R>(c->dims.kmesh, c->ytile);
+    g.slab = (int)ladder_slab<R>(c);
+    const CT* tw;
+    if constexpr (sizeof(R) == 4) tw = c->d_twk32;
+    else tw = c->d_twk;
+    ladder_fn<R>(c)<<<dim3(c->nx, c->ysplit), VAL_THREADS, c->lad_smem, c->stream>>>(
+        A, static_cast<const CT*>(c->d_valT), static_cast<const R*>(c->d_lad), Bp, c->nv, c->nk, c->nx, c->ytile,
+        c->yper, g, g.slab, tw);
+    ++c->launches;
+    VCUDA(c, cudaGetLastError());
+  }
+  const int xc = (int)final_xchunk(c);
+  const size_t fsm = sizeof(double2) * ((size_t)c->nc * c->nv + (size_t)c->nv * xc);
+  kv_final<R><<<c->nk, VAL_THREADS, fsm, c->stream>>>(
+      d_in, d_in + n, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow, c->d_con, c->d_val, c->d_s, Bp,
+      c->ysplit, c->nc, c->nv, c->nk, c->nx, xc, use_e, use_x, use_d, backwards, d_out, d_out + n);
+  ++c->launches;
+  VCUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
+int apply_dev(ocn_val_ctx* c, const double* d_in, double* d_out, const int flags[3], int backwards) {
+  if (int rc = check_ready(c, flags)) return rc;
+  return c->mixed ? apply_impl<float>(c, d_in, d_out, flags, backwards)
+                  : apply_impl<double>(c, d_in, d_out, flags, backwards);
+}
+
+int upload(ocn_val_ctx* c, void* dst, const void* src, size_t bytes) {
+  VCUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
+  return OCN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ocn_val_create(const ocn_val_dims* d, ocn_val_ctx** out) {
+  if (!d || !out) return vset_err(nullptr, OCN_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (d->nc < 1 || d->nv < 1 || d->nv > VAL_MAX_NV)
+    return vset_err(nullptr, OCN_ERR_ARG, "ocn_val_create: need nc >= 1 and 1 <= nv <= 32");
+  for (int i = 0; i < 3; ++i) {
+    if (d->kmesh[i] < 1 || d->kmesh[i] > OCN_MAX_KDIM || d->xmesh[i] < 1 || d->xmesh[i] > OCN_MAX_KDIM)
+      return vset_err(nullptr, OCN_ERR_ARG, "ocn_val_create: mesh extents must be in 1..32");
+  }
+  if (d->precision != OCN_PREC_FP64 && d->precision != OCN_PREC_MIXED)
+    return vset_err(nullptr, OCN_ERR_ARG, "ocn_val_create: unknown precision");
+  ocn_val_ctx* c = new (std::nothrow) ocn_val_ctx();
+  if (!c) return vset_err(nullptr, OCN_ERR_ALLOC, "host allocation failed");
+  auto fail = [&](int rc) {
+    g_val_create_err = c->err;
+    ocn_val_destroy(c);
+    return rc;
+  };
+  c->dims = *d;
+  c->device = d->device;
+  c->nc = d->nc;
+  c->nv = d->nv;
+  c->nk = d->kmesh[0] * d->kmesh[1] * d->kmesh[2];
+  c->nx = d->xmesh[0] * d->xmesh[1] * d->xmesh[2];
+  c->npsi = (size_t)c->nc * c->nv * c->nk;
+  c->mixed = d->precision == OCN_PREC_MIXED;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return fail(vcuda(c, e, "cudaSetDevice"));
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(vcuda(c, e, "cudaStreamCreate"));
+  int optin = 0;
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  c->smem_optin = (size_t)optin;
+  c->red_blocks = (int)std::min<size_t>(2 * (size_t)c->sm_count, std::max<size_t>(1, (c->npsi + 511) / 512));
+  const size_t cs = c->mixed ? sizeof(float2) : sizeof(double2);
+  const size_t rs = c->mixed ? sizeof(float) : sizeof(double);
+  int rc = c->mixed ? plan_ladder<float>(c) : plan_ladder<double>(c);
+  if (rc) return fail(rc);
+  const size_t nxk = (size_t)c->nx * c->nk;
+  if ((rc = valloc(c, &c->d_er, c->npsi)) || (rc = valloc(c, &c->d_ei, c->npsi)) ||
+      (rc = valloc(c, &c->d_allow, c->npsi)) || (rc = valloc(c, &c->d_con, nxk * c->nc)) ||
+      (rc = valloc(c, &c->d_val, nxk * c->nv)) ||
+      (rc = valloc(c, reinterpret_cast<char**>(&c->d_valT), nxk * c->nv * cs)) ||
+      (rc = valloc(c, reinterpret_cast<char**>(&c->d_lad), nxk * c->nx * rs)) ||
+      (rc = valloc(c, &c->d_bub, c->nx)) || (rc = valloc(c, &c->d_twk, 3 * OCN_MAX_KDIM)) ||
+      (rc = valloc(c, &c->d_twk32, 3 * OCN_MAX_KDIM)) || (rc = valloc(c, &c->d_twx, 3 * OCN_MAX_KDIM)) ||
+      (rc = valloc(c, &c->d_lp, nxk)) || (rc = valloc(c, &c->d_s, c->nx)) ||
+      (rc = valloc(c, reinterpret_cast<char**>(&c->d_A), nxk * c->nv * cs)) ||
+      (rc = valloc(c, reinterpret_cast<char**>(&c->d_Bp), nxk * c->nv * c->ysplit * cs)) ||
+      (rc = valloc(c, &c->d_vec, 8 * c->npsi)) || (rc = valloc(c, &c->d_red, 4 * (size_t)c->red_blocks)))
+    return fail(rc);
+  double2 twk[3][OCN_MAX_KDIM], twx[3][OCN_MAX_KDIM];
+  float2 twk32[3][OCN_MAX_KDIM];
+  twiddles(d->kmesh, twk);
+  twiddles(d->xmesh, twx);
+  for (int a = 0; a < 3; ++a)
+    for (int t = 0; t < OCN_MAX_KDIM; ++t) twk32[a][t] = make_float2((float)twk[a][t].x, (float)twk[a][t].y);
+  if ((rc = upload(c, c->d_twk, twk, sizeof(twk))) || (rc = upload(c, c->d_twx, twx, sizeof(twx))) ||
+      (rc = upload(c, c->d_twk32, twk32, sizeof(twk32))))
+    return fail(rc);
+  cudaMemsetAsync(c->d_ei, 0, sizeof(double) * c->npsi, c->stream);
+  const KmeshGeom<double> gx = ocn::kmesh_geom<double>(d->xmesh, 1);
+  if (ocn::kmesh_smem(gx) > 48 * 1024) {
+    e = cudaFuncSetAttribute(kv_bub_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ocn::kmesh_smem(gx));
+    if (e != cudaSuccess) return fail(vcuda(c, e, "cudaFuncSetAttribute(kv_bub_fft)"));
+  }
+  if (sizeof(double2) * 8 * VAL_CC * c->nv > 48 * 1024) {  // Nv > 24: the 32-wide instantiation
+    e = cudaFuncSetAttribute(c->mixed ? (const void*)kv_amat<float, 32> : (const void*)kv_amat<double, 32>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(double2) * 8 * VAL_CC * c->nv));
+    if (e != cudaSuccess) return fail(vcuda(c, e, "cudaFuncSetAttribute(kv_amat)"));
+  }
+  const size_t fsm = sizeof(double2) * ((size_t)c->nc * c->nv + (size_t)c->nv * final_xchunk(c));
+  if (fsm > c->smem_optin) return fail(vset_err(c, OCN_ERR_UNSUPPORTED, "ocn_val_create: Nc*Nv too large"));
+  e = cudaFuncSetAttribute(c->mixed ? (const void*)kv_final<float> : (const void*)kv_final<double>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
+  if (e != cudaSuccess) return fail(vcuda(c, e, "cudaFuncSetAttribute(kv_final)"));
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail(vcuda(c, e, "ocn_val_create"));
+  *out = c;
+  return OCN_OK;
+}
+
+int ocn_val_destroy(ocn_val_ctx* c) {
+  if (!c) return OCN_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void* bufs[] = {c->d_er, c->d_ei, c->d_allow, c->d_con, c->d_val, c->d_valT, c->d_lad, c->d_bub,
+                  c->d_twk, c->d_twk32, c->d_twx, c->d_lp, c->d_s, c->d_A, c->d_Bp, c->d_vec, c->d_red,
+                  c->d_coef};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return OCN_OK;
+}
+
+int ocn_val_last_error(const ocn_val_ctx* c, char* buf, size_t len) {
+  if (!buf || len == 0) return OCN_ERR_ARG;
+  std::snprintf(buf, len, "%s", (c ? c->err : g_val_create_err).c_str());
+  return OCN_OK;
+}
+
+long long ocn_val_kernel_launches(const ocn_val_ctx* c) { return c ? c->launches : 0; }
+void* ocn_val_stream(ocn_val_ctx* c) { return c ? static_cast<void*>(c->stream) : nullptr; }
+
+int ocn_val_set_energies(ocn_val_ctx* c, const double* re, const double* im) {
+  if (!c || !re) return vset_err(c, OCN_ERR_ARG, "null argument");
+  cudaSetDevice(c->device);
+  if (int rc = upload(c, c->d_er, re, sizeof(double) * c->npsi)) return rc;
+  c->ei_nonzero = false;
+  if (im) {
+    for (size_t i = 0; i < c->npsi && !c->ei_nonzero; ++i) c->ei_nonzero = im[i] != 0.0;
+    if (int rc = upload(c, c->d_ei, im, sizeof(double) * c->npsi)) return rc;
+  }
+  VCUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_e = true;
+  return OCN_OK;
+}
+
+int ocn_val_set_allow(ocn_val_ctx* c, const double* allow) {
+  if (!c || !allow) return vset_err(c, OCN_ERR_ARG, "null argument");
+  cudaSetDevice(c->device);
+  if (int rc = upload(c, c->d_allow, allow, sizeof(double) * c->npsi)) return rc;
+  VCUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_allow = true;
+  return OCN_OK;
+}
+
+int ocn_val_set_bubble(ocn_val_ctx* c, const double* bubble) {
+  if (!c || !bubble) return vset_err(c, OCN_ERR_ARG, "null argument");
+  cudaSetDevice(c->device);
+  if (int rc = upload(c, c->d_bub, bubble, sizeof(double) * c->nx)) return rc;
+  VCUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_bubble = true;
+  return OCN_OK;
+}
+
+static int set_states_impl(ocn_val_ctx* c, const double* conr, const double* coni, const double* valr,
+                           const double* vali, bool on_device) {
+  if (!c || !conr || !coni || !valr || !vali) return vset_err(c, OCN_ERR_ARG, "null argument");
+  cudaSetDevice(c->device);
+  const size_t ncon = (size_t)c->nx * c->nc * c->nk, nval = (size_t)c->nx * c->nv * c->nk;
+  double* tmp = nullptr;
+  const double *cr = conr, *ci = coni, *vr = valr, *vi = vali;
+  if (!on_device) {
+    if (int rc = valloc(c, &tmp, 2 * std::max(ncon, nval))) return rc;
+    cr = tmp;
+    ci = tmp + ncon;
+  }
+  const int g = 4 * c->sm_count;
+  int rc = OCN_OK;
+  if (!on_device) {
+    if ((rc = upload(c, tmp, conr, sizeof(double) * ncon)) || (rc = upload(c, tmp + ncon, coni, sizeof(double) * ncon)))
+      goto done;
+  }
+  kv_interleave<<<g, 256, 0, c->stream>>>(cr, ci, ncon, c->d_con);
+  if (!on_device) {
+    vr = tmp;
+    vi = tmp + nval;
+    if ((rc = upload(c, tmp, valr, sizeof(double) * nval)) || (rc = upload(c, tmp + nval, vali, sizeof(double) * nval)))
+      goto done;
+  }
+  kv_interleave<<<g, 256, 0, c->stream>>>(vr, vi, nval, c->d_val);
+  if (c->mixed)
+    kv_transpose_val<float><<<g, 256, 0, c->stream>>>(c->d_val, c->nv, c->nk, c->nx,
+                                                      static_cast<float2*>(c->d_valT));
+  else
+    kv_transpose_val<double><<<g, 256, 0, c->stream>>>(c->d_val, c->nv, c->nk, c->nx,
+                                                       static_cast<double2*>(c->d_valT));
+  {
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = vcuda(c, e, "ocn_val_set_states");
+  }
+done:
+  if (tmp) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+  }
+  if (rc == OCN_OK) c->have_states = true;
+  return rc;
+}
+
+int ocn_val_set_states(ocn_val_ctx* c, const double* conr, const double* coni, const double* valr,
+                       const double* vali) {
+  return set_states_impl(c, conr, coni, valr, vali, false);
+}
+
+int ocn_val_set_states_dev(ocn_val_ctx* c, const double* conr, const double* coni, const double* valr,
+                           const double* vali) {
+  return set_states_impl(c, conr, coni, valr, vali, true);
+}
+
+static int set_ladder_impl(ocn_val_ctx* c, const double* lad, bool on_device) {
+  if (!c || !lad) return vset_err(c, OCN_ERR_ARG, "null argument");
+  cudaSetDevice(c->device);
+  const size_t n = (size_t)c->nk * c->nx * c->nx;
+  if (!c->mixed) {
+    VCUDA(c, cudaMemcpyAsync(c->d_lad, lad, sizeof(double) * n,
+                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  } else if (on_device) {
+    kv_to_float<<<4 * c->sm_count, 256, 0, c->stream>>>(lad, n, static_cast<float*>(c->d_lad));
+    VCUDA(c, cudaGetLastError());
+  } else {  // staged through a bounded device buffer
+    const size_t chunk = std::min<size_t>(n, (size_t)1 << 26);
+    double* tmp = nullptr;
+    if (int rc = valloc(c, &tmp, chunk)) return rc;
+    int rc = OCN_OK;
+    for (size_t o = 0; o < n && rc == OCN_OK; o += chunk) {
+      const size_t m = std::min(chunk, n - o);
+      rc = upload(c, tmp, lad + o, sizeof(double) * m);
+      if (rc == OCN_OK) kv_to_float<<<4 * c->sm_count, 256, 0, c->stream>>>(tmp, m, static_cast<float*>(c->d_lad) + o);
+    }
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    if (rc) return rc;
+    if (e != cudaSuccess) return vcuda(c, e, "ocn_val_set_ladder");
+  }
+  VCUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_ladder = true;
+  return OCN_OK;
+}
+
+int ocn_val_set_ladder(ocn_val_ctx* c, const double* ladder) { return set_ladder_impl(c, ladder, false); }
+int ocn_val_set_ladder_dev(ocn_val_ctx* c, const double* d_ladder) { return set_ladder_impl(c, d_ladder, true); }
+
+int ocn_val_apply_H_dev(ocn_val_ctx* c, const double* d_in, double* d_out, const int flags[3], int backwards) {
+  if (!c || !d_in || !d_out || !flags) return vset_err(c, OCN_ERR_ARG, "null argument");
+  cudaSetDevice(c->device);
+  return apply_dev(c, d_in, d_out, flags, backwards);
+}
+
+int ocn_val_apply_H(ocn_val_ctx* c, const double* in_r, const double* in_i, double* out_r, double* out_i,
+                    const int flags[3], int backwards) {
+  if (!c || !in_r || !in_i || !out_r || !out_i || !flags) return vset_err(c, OCN_ERR_ARG, "null argument");
+  cudaSetDevice(c->device);
+  const size_t n = c->npsi;
+  double* din = c->d_vec;
+  double* dout = c->d_vec + 2 * n;
+  if (int rc = upload(c, din, in_r, sizeof(double) * n)) return rc;
+  if (int rc = upload(c, din + n, in_i, sizeof(double) * n)) return rc;
+  if (int rc = apply_dev(c, din, dout, flags, backwards)) return rc;
+  VCUDA(c, cudaMemcpyAsync(out_r, dout, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  VCUDA(c, cudaMemcpyAsync(out_i, dout + n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  VCUDA(c, cudaStreamSynchronize(c->stream));
+  return OCN_OK;
+}
+
+// OCEAN_haydock_Herm_do over the valence action (OCEAN_haydock.f90:190-320,
+// 824-938); psi0 is a device vector (real plane, then imaginary plane).
+int ocn_val_haydock_dev(ocn_val_ctx* c, const double* d_psi0, int niter, const int flags[3], double* real_a,
+                        double* imag_a, double* real_b, int* niter_done) {
+  if (!c || !d_psi0 || !flags || !real_a || !imag_a || !real_b || !niter_done || niter < 1)
+    return vset_err(c, OCN_ERR_ARG, "bad argument");
+  cudaSetDevice(c->device);
+  if (int rc = check_ready(c, flags)) return rc;
+  const size_t n = c->npsi;
+  if (c->coef_cap < niter + 1) {
+    if (c->d_coef) cudaFree(c->d_coef);
+    c->d_coef = nullptr;
+    c->coef_cap = 0;
+    if (int rc = valloc(c, &c->d_coef, 3 * (size_t)(niter + 1))) return rc;
+    c->coef_cap = niter + 1;
+  }
+  double* ra = c->d_coef;
+  double* ia = ra + (niter + 1);
+  double* rb = ia + (niter + 1);
+  VCUDA(c, cudaMemsetAsync(c->d_coef, 0, sizeof(double) * 3 * (niter + 1), c->stream));
+  double* psi = c->d_vec;
+  double* h = c->d_vec + 2 * n;
+  double* old = c->d_vec + 4 * n;
+  VCUDA(c, cudaMemcpyAsync(psi, d_psi0, sizeof(double) * 2 * n, cudaMemcpyDeviceToDevice, c->stream));
+  VCUDA(c, cudaMemsetAsync(old, 0, sizeof(double) * 2 * n, c->stream));
+  const int nb = c->red_blocks;
+  for (int it = 1; it <= niter; ++it) {
+    if (int rc = apply_dev(c, psi, h, flags, 0)) return rc;
+    kv_lz1<<<nb, VAL_THREADS, 0, c->stream>>>(h, old, psi, n, rb, it, c->d_red);
+    kv_lz2<<<nb, VAL_THREADS, 0, c->stream>>>(c->d_red, nb, h, psi, n, ra, ia, it, c->d_red + 2 * nb);
+    kv_lz3<<<nb, VAL_THREADS, 0, c->stream>>>(c->d_red + 2 * nb, nb, h, n, rb, it);
+    c->launches += 3;
+    VCUDA(c, cudaGetLastError());
+    double* t = old;  // old <- psi, psi <- h (now h / b), h <- the old buffer
+    old = psi;
+    psi = h;
+    h = t;
+  }
+  VCUDA(c, cudaMemcpyAsync(real_a, ra, sizeof(double) * (niter + 1), cudaMemcpyDeviceToHost, c->stream));
+  VCUDA(c, cudaMemcpyAsync(imag_a, ia, sizeof(double) * (niter + 1), cudaMemcpyDeviceToHost, c->stream));
+  VCUDA(c, cudaMemcpyAsync(real_b, rb, sizeof(double) * (niter + 1), cudaMemcpyDeviceToHost, c->stream));
+  VCUDA(c, cudaStreamSynchronize(c->stream));
+  int done = niter;
+  for (int i = 0; i < niter; ++i)
+    if (std::isnan(real_a[i])) {
+      done = i + 1;
+      break;
+    }
+  *niter_done = done;
+  return done < niter || std::isnan(real_a[niter - 1]) ? OCN_ERR_NAN : OCN_OK;
+}
+
+int ocn_val_haydock(ocn_val_ctx* c, const double* psi0_r, const double* psi0_i, int niter, const int flags[3],
+                    double* real_a, double* imag_a, double* real_b, int* niter_done) {
+  if (!c || !psi0_r || !psi0_i) return vset_err(c, OCN_ERR_ARG, "null argument");
+  cudaSetDevice(c->device);
+  const size_t n = c->npsi;
+  double* d0 = c->d_vec + 6 * n;
+  if (int rc = upload(c, d0, psi0_r, sizeof(double) * n)) return rc;
+  if (int rc = upload(c, d0 + n, psi0_i, sizeof(double) * n)) return rc;
+  return ocn_val_haydock_dev(c, d0, niter, flags, real_a, imag_a, real_b, niter_done);
+}
+
+// AI_bubble_populate with wall_search_old_way (OCEAN_bubble.f90:238-407).
+int ocn_val_bubble_populate(const int xmesh[3], const double bvec[9], const double qinb[3], double celvol,
+                            int nkpts, double* bubble, int* ngvec) {
+  if (!xmesh || !bvec || !qinb || !bubble || nkpts < 1 || !(celvol > 0.0))
+    return vset_err(nullptr, OCN_ERR_ARG, "ocn_val_bubble_populate: bad argument");
+  const int n1 = xmesh[0], n2 = xmesh[1], n3 = xmesh[2];
+  if (n1 < 1 || n2 < 1 || n3 < 1) return vset_err(nullptr, OCN_ERR_ARG, "ocn_val_bubble_populate: bad mesh");
+  auto glen = [&](int a, int b, int cc) {  // squared length of B g (gvec_length, :38-47)
+    double s = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      const double t = bvec[i] * a + bvec[i + 3] * b + bvec[i + 6] * cc;
+      s += t * t;
+    }
+    return s;
+  };
+  auto lo = [](int n) { return (int)std::floor(-(double)n / 2.0); };
+  auto hi = [](int n) { return (int)std::ceil((double)n / 2.0); };
+  double length = HUGE_VAL;
+  for (int a = lo(n1); a <= hi(n1); ++a)
+    for (int b = lo(n2); b <= hi(n2); ++b)
+      for (int cc = lo(n3); cc <= hi(n3); ++cc)
+        if (2 * std::abs(cc) >= n3 || 2 * std::abs(b) >= n2 || 2 * std::abs(a) >= n1)
+          length = std::min(length, glen(a, b, cc));
+  double next = 0.0;
+  for (int a = lo(n1); a <= hi(n1); ++a)
+    for (int b = lo(n2); b <= hi(n2); ++b)
+      for (int cc = lo(n3); cc <= hi(n3); ++cc) {
+        const double t = glen(a, b, cc);
+        if (t < length && t > next) next = t;
+      }
+  length = 0.5 * (length + next);
+  double bmet[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int q = 0; q < 3; ++q) s += bvec[q + 3 * i] * bvec[q + 3 * j];
+      bmet[i][j] = s;
+    }
+  const double pi = 3.1415926535897932384626433832795;
+  const double g2min = 8.0 * pi * pi * pi / (celvol * (double)(n1 * n2 * n3));
+  std::fill(bubble, bubble + (size_t)n1 * n2 * n3, 0.0);
+  int count = 0;
+  for (int a = (int)std::ceil(-(double)n1 / 2.0); a <= (int)std::floor((double)n1 / 2.0); ++a)
+    for (int b = (int)std::ceil(-(double)n2 / 2.0); b <= (int)std::floor((double)n2 / 2.0); ++b)
+      for (int cc = (int)std::ceil(-(double)n3 / 2.0); cc <= (int)std::floor((double)n3 / 2.0); ++cc) {
+        const double qq[3] = {qinb[0] + a, qinb[1] + b, qinb[2] + cc};
+        double g2 = 0.0;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) g2 += qq[i] * qq[j] * bmet[i][j];
+        if (g2 < g2min) g2 = g2min;
+        const int ix = a < 0 ? a + n1 : a, iy = b < 0 ? b + n2 : b, iz = cc < 0 ? cc + n3 : cc;
+        double mul = 0.0;
+        if (glen(a, b, cc) < length) {
+          mul = 4.0 * pi / (celvol * g2 * (double)nkpts);
+          ++count;
+        }
+        bubble[iz + (size_t)n3 * (iy + (size_t)n2 * ix)] = mul;
+      }
+  bubble[0] = 0.0;
+  if (ngvec) *ngvec = count - 1;
+  return OCN_OK;
+}
+
+}  // extern "C"

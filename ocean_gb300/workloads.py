@@ -269,3 +269,202 @@ def make(name: str, seed: int = 0, nb: Optional[int] = None, kmesh=None, xmesh=N
                       mpm=mpm.reshape(-1), mhr=np.concatenate(mh_r), mhi=np.concatenate(mh_i))
         w.so_xi = 5.0 * EV2HARTREE
     return w
+
+
+# ------------------------------------------------------------------ valence BSE
+#
+# Synthetic stand-ins for the valence BSE inputs (OCEAN_val_states' real-space
+# states, OCEAN_val_energy's pair energies, OCEAN_WRR's ladder):
+#   * states per k   one QR-orthonormal complex Gaussian (Nx x (Nv + Nc)):
+#                    the first Nv columns are val(x, v, k), the rest con(x, c, k)
+#   * energies       E(c, v, k) = e_c(k) - e_v(k), e_v ~ U(-8, 0) eV and
+#                    e_c ~ U(1, 16) eV sorted per k, Hartree, Sigma'' = 0
+#   * allow          1
+#   * bubble         built by the library from the cubic cell (a = 4.0 A)
+#   * ladder(R,x,y)  W(|R + x - y|) fcn(q |R + x - y|)^2 with W = erf(r/0.5 A)/(eps r),
+#                    eps = 4, and the smoothing of OCEAN_WRR_LocalRPA
+#                    (OCEAN_WRR.f90:156, 286-304), q = (6 pi^2 / (V Nk))^(1/3);
+#                    R runs over the k-mesh's lattice vectors in FFT order
+#                    (index j -> j or j - n), and a Nyquist index of an even
+#                    mesh averages R = +n/2 and -n/2 so that
+#                    ladder(-R, y, x) = ladder(R, x, y) (the direct term is Hermitian).
+#   * psi0           complex Gaussian normalised by core_pnorm
+
+
+@dataclass
+class ValWorkload:
+    name: str
+    nc: int
+    nv: int
+    kmesh: tuple
+    xmesh: tuple
+    celvol: float
+    avec: np.ndarray          # (9,) Fortran avec(3,3), Bohr
+    bvec: np.ndarray          # (9,) Fortran bvec(3,3), Bohr^-1
+    qinb: np.ndarray          # (3,)
+    epsilon0: float
+    er: np.ndarray            # (Nc*Nv*Nk,) Fortran order (c fastest)
+    ei: np.ndarray
+    allow: np.ndarray
+    conr: Optional[np.ndarray]   # (Nx*Nc*Nk,) Fortran order (x fastest), None when on the device
+    coni: Optional[np.ndarray]
+    valr: Optional[np.ndarray]   # (Nx*Nv*Nk,)
+    vali: Optional[np.ndarray]
+    ladder: Optional[np.ndarray]  # (Nk*Nx*Nx,) Fortran ladder(k, x, y)
+    psi_r: np.ndarray
+    psi_i: np.ndarray
+    kpref: float
+    niter: int = 200
+    gam0: float = 0.2 * EV2HARTREE
+    el: float = 0.0
+    eh: float = 30.0 * EV2HARTREE
+    device_arrays: dict = field(default_factory=dict)  # torch tensors when built on a device
+
+    @property
+    def nk(self) -> int:
+        return int(np.prod(self.kmesh))
+
+    @property
+    def nx(self) -> int:
+        return int(np.prod(self.xmesh))
+
+    @property
+    def npsi(self) -> int:
+        return self.nc * self.nv * self.nk
+
+
+def _mesh_frac(mesh):
+    """Fractional positions of a mesh in its flat order (last extent fastest)."""
+    g = np.stack(np.meshgrid(*[np.arange(n) / n for n in mesh], indexing="ij"), axis=-1)
+    return g.reshape(-1, 3)
+
+
+def _lattice_images(kmesh):
+    """Per flat k index the lattice vectors R (integer, FFT order) it stands for."""
+    per_axis = []
+    for n in kmesh:
+        opts = []
+        for j in range(n):
+            if n % 2 == 0 and 2 * j == n:
+                opts.append((j, j - n))
+            else:
+                opts.append((j if j < (n + 1) // 2 else j - n,))
+        per_axis.append(opts)
+    images = []
+    for j1 in range(kmesh[0]):
+        for j2 in range(kmesh[1]):
+            for j3 in range(kmesh[2]):
+                images.append([(a, b, c) for a in per_axis[0][j1] for b in per_axis[1][j2]
+                               for c in per_axis[2][j3]])
+    return images
+
+
+def val_ladder(kmesh, xmesh, avec, celvol, epsilon0=4.0, width_angstrom=0.5, device=None, dtype=None):
+    """ladder(k, x, y) of the synthetic screened interaction as a torch tensor of
+    shape (Nx_y, Nx_x, Nk) (= Fortran ladder(k, x, y) flattened), built on `device`."""
+    import torch
+
+    dtype = dtype or torch.float64
+    nk, nx = int(np.prod(kmesh)), int(np.prod(xmesh))
+    a = width_angstrom / BOHR
+    q = (6.0 * math.pi ** 2 / (celvol * nk)) ** (1.0 / 3.0)
+    A = torch.tensor(np.asarray(avec, dtype=np.float64).reshape(3, 3, order="F"), dtype=torch.float64,
+                     device=device)
+    fx = torch.tensor(_mesh_frac(xmesh), dtype=torch.float64, device=device)
+    images = _lattice_images(kmesh)
+    nimg = max(len(i) for i in images)
+    R = np.zeros((nk, nimg, 3))
+    wts = np.zeros((nk, nimg))
+    for k, im in enumerate(images):
+        for j, r in enumerate(im):
+            R[k, j] = r
+            wts[k, j] = 1.0 / len(im)
+    R = torch.tensor(R, dtype=torch.float64, device=device)
+    wts = torch.tensor(wts, dtype=torch.float64, device=device)
+    out = torch.empty((nx, nx, nk), dtype=dtype, device=device)
+    for y in range(nx):
+        d = fx[:, None, None, :] - fx[y][None, None, None, :] + R[None, :, :, :]
+        # d: (x, k, img, 3) fractional -> Cartesian
+        cart = torch.einsum("ij,xkmj->xkmi", A, d)
+        r = torch.linalg.norm(cart, dim=-1)
+        safe = torch.where(r > 0, r, torch.ones_like(r))
+        w = torch.where(r > 0, torch.erf(safe / a) / (epsilon0 * safe),
+                        torch.full_like(r, 2.0 / (a * math.sqrt(math.pi) * epsilon0)))
+        qd = q * r
+        qs = torch.where(qd > 1e-6, qd, torch.ones_like(qd))
+        fcn = torch.where(qd > 1e-6, 3.0 * (torch.sin(qs) - qs * torch.cos(qs)) / qs ** 3, 1.0 - 0.1 * qd ** 2)
+        out[y] = ((w * fcn ** 2) * wts[None, :, :]).sum(-1).to(dtype)
+    return out
+
+
+def make_val(name: str, seed: int = 0, nc: Optional[int] = None, nv: Optional[int] = None, kmesh=None,
+             xmesh=None, device: Optional[str] = None) -> ValWorkload:
+    """Valence workloads: 'vtiny', 'vsmall' (oracle sizes), 'v2' (k-mesh 8^3,
+    x-mesh 10^3, 8 conduction and 4 valence bands: the benchmark case).
+    device: build the states and the ladder as torch tensors there (kept in
+    w.device_arrays; the numpy fields are then None)."""
+    presets = {
+        "vtiny": dict(nc=4, nv=2, kmesh=(2, 2, 2), xmesh=(3, 3, 3), niter=24),
+        "vsmall": dict(nc=6, nv=3, kmesh=(4, 4, 4), xmesh=(4, 4, 4), niter=40),
+        "vodd": dict(nc=5, nv=3, kmesh=(3, 2, 5), xmesh=(3, 4, 3), niter=30),
+        "v2": dict(nc=8, nv=4, kmesh=(8, 8, 8), xmesh=(10, 10, 10), niter=200),
+    }
+    if name not in presets:
+        raise ValueError(f"unknown valence workload {name!r}")
+    p = dict(presets[name])
+    for key, val in (("nc", nc), ("nv", nv), ("kmesh", kmesh), ("xmesh", xmesh)):
+        if val is not None:
+            p[key] = tuple(val) if key in ("kmesh", "xmesh") else val
+    km, xm = tuple(p["kmesh"]), tuple(p["xmesh"])
+    nk, nx = int(np.prod(km)), int(np.prod(xm))
+    ncb, nvb = p["nc"], p["nv"]
+    if nx < ncb + nvb:
+        raise ValueError("x-mesh too small for orthonormal states")
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a_bohr = 4.0 / BOHR
+    avec = np.zeros(9)
+    avec[0] = avec[4] = avec[8] = a_bohr
+    bvec = np.zeros(9)
+    bvec[0] = bvec[4] = bvec[8] = 2.0 * math.pi / a_bohr
+    celvol = a_bohr ** 3
+    ev = np.sort(rng.uniform(-8.0, 0.0, size=(nk, nvb)), axis=1)
+    ec = np.sort(rng.uniform(1.0, 16.0, size=(nk, ncb)), axis=1)
+    e = (ec[:, None, :] - ev[:, :, None]) * EV2HARTREE          # (k, v, c)
+    er = e.reshape(-1).copy()
+    ei = np.zeros_like(er)
+    allow = np.ones_like(er)
+    g_r = rng.standard_normal(ncb * nvb * nk)
+    g_i = rng.standard_normal(ncb * nvb * nk)
+    psi_r, psi_i, kpref = pnorm(g_r, g_i, nk, celvol)
+    w = ValWorkload(name=name, nc=ncb, nv=nvb, kmesh=km, xmesh=xm, celvol=celvol, avec=avec, bvec=bvec,
+                    qinb=np.zeros(3), epsilon0=4.0, er=er, ei=ei, allow=allow, conr=None, coni=None,
+                    valr=None, vali=None, ladder=None, psi_r=psi_r, psi_i=psi_i, kpref=kpref,
+                    niter=p["niter"])
+    if device is None:
+        st = np.empty((nk, ncb + nvb, nx), dtype=np.complex128)
+        for k in range(nk):
+            g = rng.standard_normal((nx, ncb + nvb)) + 1j * rng.standard_normal((nx, ncb + nvb))
+            qm, _ = np.linalg.qr(g)
+            st[k] = qm.T
+        val = st[:, :nvb, :]   # (k, v, x): Fortran (x, v, k) flattened
+        con = st[:, nvb:, :]
+        w.valr, w.vali = val.real.reshape(-1).copy(), val.imag.reshape(-1).copy()
+        w.conr, w.coni = con.real.reshape(-1).copy(), con.imag.reshape(-1).copy()
+        w.ladder = val_ladder(km, xm, avec, celvol, w.epsilon0).numpy().reshape(-1)
+    else:
+        import torch
+
+        gen = torch.Generator(device=device)
+        gen.manual_seed(seed)
+        st = torch.empty((nk, ncb + nvb, nx), dtype=torch.complex128, device=device)
+        for k in range(nk):
+            g = torch.complex(torch.randn((nx, ncb + nvb), generator=gen, device=device, dtype=torch.float64),
+                              torch.randn((nx, ncb + nvb), generator=gen, device=device, dtype=torch.float64))
+            qm, _ = torch.linalg.qr(g)
+            st[k] = qm.T
+        val = st[:, :nvb, :].contiguous()
+        con = st[:, nvb:, :].contiguous()
+        w.device_arrays = dict(valr=val.real.contiguous().reshape(-1), vali=val.imag.contiguous().reshape(-1),
+                               conr=con.real.contiguous().reshape(-1), coni=con.imag.contiguous().reshape(-1),
+                               ladder=val_ladder(km, xm, avec, celvol, w.epsilon0, device=device).reshape(-1))
+    return w

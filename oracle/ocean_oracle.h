@@ -127,6 +127,40 @@ int or_gmres(const or_dims* d, const or_ops* o, const double* hay_r, const doubl
 /* OCEAN_soprep without core_broaden.ipt (OCEAN_multiplet.f90:572-690). */
 int or_soprep(int core_l, double xi, double* somelr, double* someli);
 
+/* ---- valence BSE (ocean_oracle_val.cpp): one spin channel, resonant pairs */
+typedef struct {
+  int nc, nv;    /* conduction / valence bands */
+  int kmesh[3];  /* flat k index k3 fastest */
+  int xmesh[3];  /* flat x index x3 fastest */
+} or_val_dims;
+
+typedef struct {
+  const double *er, *ei;      /* (Nc, Nv, Nk) pair energies; ei may be NULL */
+  const double* allow;        /* (Nc, Nv, Nk) */
+  const double *conr, *coni;  /* (Nx, Nc, Nk) conduction states on the x-mesh */
+  const double *valr, *vali;  /* (Nx, Nv, Nk) valence states on the x-mesh */
+  const double* bubble;       /* (Nx) */
+  const double* ladder;       /* (Nk, Nx, Nx) */
+  int bande, bflag, lflag;    /* energies, exchange, screened direct */
+} or_val_ops;
+
+/* wall_search_old_way (OCEAN_bubble.f90:238-297). */
+double or_val_wall_length(const int xmesh[3], const double bvec[9]);
+/* AI_bubble_populate (OCEAN_bubble.f90:300-407). */
+int or_val_bubble_populate(const int xmesh[3], const double bvec[9], const double qinb[3], double celvol,
+                           int nkpts, double length, double* bubble);
+/* AI_bubble_act / OCEAN_ladder_act_single, accumulating into out. */
+void or_val_bubble_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi,
+                       double* outr, double* outi);
+void or_val_ladder_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi,
+                       double* outr, double* outi);
+/* OCEAN_xact valence branch + energies (OCEAN_action.f90:521-600). */
+int or_val_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, double* hr,
+               double* hi, int backwards);
+/* Hermitian Haydock over the valence action (OCEAN_haydock.f90:190-320, 824-938). */
+int or_val_haydock(const or_val_dims* d, const or_val_ops* o, const double* p0r, const double* p0i, int niter,
+                   double* real_a, double* imag_a, double* real_b, int* niter_done);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,329 @@
+// ocean_oracle_val.cpp -- CPU ORACLE for the valence BSE action (test
+// infrastructure only; never linked into the product library).  A plain FP64
+// restatement of the reference Fortran for one spin channel
+// (valence_ham_spin = 1, nspn = 1) and resonant pairs only (nbw = 1):
+//
+//   H psi = E o psi + allow o [ 2 X(allow o psi) - D(allow o psi) ]
+//
+// with the exchange ("bubble") X of OCEAN2/OCEAN_bubble.f90:420-796 and the
+// screened direct ("ladder") D of OCEAN2/OCEAN_ladder.f90:155-1004, in the
+// order of OCEAN_xact's valence branch (OCEAN2/OCEAN_action.f90:521-575,
+// 590-600).
+//
+// Layouts (Fortran order of the reference arrays, single rank):
+//   psi, E, allow   (Nc, Nv, Nk)      psi%valr/vali(c, v, k)
+//   con             (Nx, Nc, Nk)      re_con/im_con(x, c, k)
+//   val             (Nx, Nv, Nk)      re_val/im_val(x, v, k)
+//   bubble          (Nx)              bubble(x) of AI_bubble_populate
+//   ladder          (Nk, Nx, Nx)      ladder(k, x, y) after resort_ladder
+// The flat k index runs k3 fastest and the flat x index x3 fastest, the FFT
+// orders of OCEAN_ladder_init (OCEAN_ladder.f90:1599-1695) and
+// AI_bubble_prep (OCEAN_bubble.f90:67-157).
+//
+// Parity status: unpinned by reference data (the reference ships no valence
+// states, bubble or ladder files); pinned by Hermiticity, a dense-H check and
+// agreement with the cited source.
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "ocean_oracle.h"
+
+namespace {
+
+const double kPiV = 3.14159265358979323846;
+
+inline int nk_of(const or_val_dims* d) { return d->kmesh[0] * d->kmesh[1] * d->kmesh[2]; }
+inline int nx_of(const or_val_dims* d) { return d->xmesh[0] * d->xmesh[1] * d->xmesh[2]; }
+
+// gvec_length, OCEAN_bubble.f90:38-47 (the squared length |B g|^2; bvec
+// column j is the j-th reciprocal vector, b[i + 3 j] = bvec(i+1, j+1)).
+double gvec_length(const int g[3], const double* b) {
+  double s = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    const double c = b[i] * g[0] + b[i + 3] * g[1] + b[i + 6] * g[2];
+    s += c * c;
+  }
+  return s;
+}
+
+int ifloor_half(int n) { return (int)std::floor(-(double)n / 2.0); }
+int iceil_half(int n) { return (int)std::ceil((double)n / 2.0); }
+
+}  // namespace
+
+extern "C" {
+
+// wall_search_old_way, OCEAN_bubble.f90:238-297.
+double or_val_wall_length(const int xmesh[3], const double bvec[9]) {
+  double length = HUGE_VAL;
+  int g[3];
+  for (g[0] = ifloor_half(xmesh[0]); g[0] <= iceil_half(xmesh[0]); ++g[0])
+    for (g[1] = ifloor_half(xmesh[1]); g[1] <= iceil_half(xmesh[1]); ++g[1])
+      for (g[2] = ifloor_half(xmesh[2]); g[2] <= iceil_half(xmesh[2]); ++g[2])
+        if (2 * std::abs(g[2]) >= xmesh[2] || 2 * std::abs(g[1]) >= xmesh[1] || 2 * std::abs(g[0]) >= xmesh[0]) {
+          const double t = gvec_length(g, bvec);
+          if (t < length) length = t;
+        }
+  double next = 0.0;
+  for (g[0] = ifloor_half(xmesh[0]); g[0] <= iceil_half(xmesh[0]); ++g[0])
+    for (g[1] = ifloor_half(xmesh[1]); g[1] <= iceil_half(xmesh[1]); ++g[1])
+      for (g[2] = ifloor_half(xmesh[2]); g[2] <= iceil_half(xmesh[2]); ++g[2]) {
+        const double t = gvec_length(g, bvec);
+        if (t < length && t > next) next = t;
+      }
+  return 0.5 * (length + next);
+}
+
+// AI_bubble_populate, OCEAN_bubble.f90:300-407: bubble(x) on the x-mesh in
+// the FFT order (x3 fastest), G = 0 removed.  Returns the number of retained
+// G-vectors minus one, as the reference prints it.
+int or_val_bubble_populate(const int xmesh[3], const double bvec[9], const double qinb[3], double celvol,
+                           int nkpts, double length, double* bubble) {
+  const int n1 = xmesh[0], n2 = xmesh[1], n3 = xmesh[2];
+  const int nx = n1 * n2 * n3;
+  double bmet[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int c = 0; c < 3; ++c) s += bvec[c + 3 * i] * bvec[c + 3 * j];
+      bmet[i][j] = s;
+    }
+  const double floor_g2 = 8.0 * kPiV * kPiV * kPiV / (celvol * (double)nx);
+  for (int i = 0; i < nx; ++i) bubble[i] = 0.0;
+  int igvec = 0;
+  int g[3];
+  for (g[0] = (int)std::ceil(-(double)n1 / 2.0); g[0] <= (int)std::floor((double)n1 / 2.0); ++g[0])
+    for (g[1] = (int)std::ceil(-(double)n2 / 2.0); g[1] <= (int)std::floor((double)n2 / 2.0); ++g[1])
+      for (g[2] = (int)std::ceil(-(double)n3 / 2.0); g[2] <= (int)std::floor((double)n3 / 2.0); ++g[2]) {
+        double qq[3];
+        for (int i = 0; i < 3; ++i) qq[i] = qinb[i] + (double)g[i];
+        double gsqd = 0.0;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) gsqd += qq[i] * qq[j] * bmet[i][j];
+        if (gsqd < floor_g2) gsqd = floor_g2;  // vanishing q (:350-357, :364-372)
+        int ixx = 1 + g[0], iyy = 1 + g[1], izz = 1 + g[2];
+        if (ixx <= 0) ixx += n1;
+        if (iyy <= 0) iyy += n2;
+        if (izz <= 0) izz += n3;
+        double mul = 0.0;
+        if (gvec_length(g, bvec) < length) {
+          mul = 4.0 * kPiV / (celvol * gsqd * (double)nkpts);
+          ++igvec;
+        }
+        bubble[(izz - 1) + n3 * ((iyy - 1) + n2 * (ixx - 1))] = mul;  // later g overwrite (even meshes)
+      }
+  bubble[0] = 0.0;
+  return igvec - 1;
+}
+
+// A(x, v, k) = sum_c con(x, c, k) psi(c, v, k): the first DGEMM group of both
+// AI_bubble_act (OCEAN_bubble.f90:521-530) and OCEAN_ladder_act_single
+// (OCEAN_ladder.f90:317-326).
+static void val_amat(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi,
+                     std::vector<double>& ar, std::vector<double>& ai) {
+  const int nc = d->nc, nv = d->nv, nk = nk_of(d), nx = nx_of(d);
+  ar.assign((size_t)nx * nv * nk, 0.0);
+  ai.assign((size_t)nx * nv * nk, 0.0);
+  for (int k = 0; k < nk; ++k)
+    for (int v = 0; v < nv; ++v)
+      for (int c = 0; c < nc; ++c) {
+        const size_t ip = c + (size_t)nc * (v + (size_t)nv * k);
+        const double qr = pr[ip], qi = pi[ip];
+        const double* cr = o->conr + (size_t)nx * (c + (size_t)nc * k);
+        const double* ci = o->coni + (size_t)nx * (c + (size_t)nc * k);
+        double* a_r = ar.data() + (size_t)nx * (v + (size_t)nv * k);
+        double* a_i = ai.data() + (size_t)nx * (v + (size_t)nv * k);
+        for (int x = 0; x < nx; ++x) {
+          a_r[x] += cr[x] * qr - ci[x] * qi;
+          a_i[x] += ci[x] * qr + cr[x] * qi;
+        }
+      }
+}
+
+// out(c, v, k) += pref * sum_x conj(con(x, c, k)) M(x, v, k): the closing
+// DGEMM group of both terms (OCEAN_bubble.f90:742-757, OCEAN_ladder.f90:900-911).
+static void val_project(const or_val_dims* d, const or_val_ops* o, double pref, const std::vector<double>& mr,
+                        const std::vector<double>& mi, double* outr, double* outi) {
+  const int nc = d->nc, nv = d->nv, nk = nk_of(d), nx = nx_of(d);
+  for (int k = 0; k < nk; ++k)
+    for (int v = 0; v < nv; ++v)
+      for (int c = 0; c < nc; ++c) {
+        const double* cr = o->conr + (size_t)nx * (c + (size_t)nc * k);
+        const double* ci = o->coni + (size_t)nx * (c + (size_t)nc * k);
+        const double* m_r = mr.data() + (size_t)nx * (v + (size_t)nv * k);
+        const double* m_i = mi.data() + (size_t)nx * (v + (size_t)nv * k);
+        double sr = 0.0, si = 0.0;
+        for (int x = 0; x < nx; ++x) {
+          sr += cr[x] * m_r[x] + ci[x] * m_i[x];
+          si += cr[x] * m_i[x] - ci[x] * m_r[x];
+        }
+        const size_t ip = c + (size_t)nc * (v + (size_t)nv * k);
+        outr[ip] += pref * sr;
+        outi[ip] += pref * si;
+      }
+}
+
+// AI_bubble_act, OCEAN_bubble.f90:420-796 (valence_ham_spin = 1, nbw = 1):
+// l(x) = sum_{v,k} conj(val) A; s = FFT_fwd[ bubble o FFT_bwd[l] ] (neither
+// normalised, :663-665); out += 2 sum_x conj(con) s val.
+void or_val_bubble_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, double* outr,
+                       double* outi) {
+  const int nv = d->nv, nk = nk_of(d), nx = nx_of(d);
+  std::vector<double> ar, ai;
+  val_amat(d, o, pr, pi, ar, ai);
+  std::vector<double> lr(nx, 0.0), li(nx, 0.0);
+  for (int k = 0; k < nk; ++k)
+    for (int v = 0; v < nv; ++v) {
+      const size_t b = (size_t)nx * (v + (size_t)nv * k);
+      for (int x = 0; x < nx; ++x) {
+        const double vr = o->valr[b + x], vi = o->vali[b + x];
+        lr[x] += vr * ar[b + x] + vi * ai[b + x];
+        li[x] += vr * ai[b + x] - vi * ar[b + x];
+      }
+    }
+  or_fft3d(d->xmesh, lr.data(), li.data(), +1);
+  for (int x = 0; x < nx; ++x) {
+    lr[x] *= o->bubble[x];
+    li[x] *= o->bubble[x];
+  }
+  or_fft3d(d->xmesh, lr.data(), li.data(), -1);
+  std::vector<double> mr((size_t)nx * nv * nk), mi((size_t)nx * nv * nk);
+  for (int k = 0; k < nk; ++k)
+    for (int v = 0; v < nv; ++v) {
+      const size_t b = (size_t)nx * (v + (size_t)nv * k);
+      for (int x = 0; x < nx; ++x) {
+        const double vr = o->valr[b + x], vi = o->vali[b + x];
+        mr[b + x] = lr[x] * vr - li[x] * vi;
+        mi[b + x] = li[x] * vr + lr[x] * vi;
+      }
+    }
+  val_project(d, o, 2.0, mr, mi, outr, outi);
+}
+
+// OCEAN_ladder_act_single, OCEAN_ladder.f90:155-1004 (one rank, nbw = 1):
+// T(x, y, k) = sum_v A(x, v, k) conj(val(y, v, k));
+// T(x, y, .) = FFT_bwd[ ladder(., x, y) o FFT_fwd[ T(x, y, .) ] ] / Nk;
+// B(x, v, k) = sum_y T(x, y, k) val(y, v, k);  out += -1 sum_x conj(con) B.
+void or_val_ladder_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, double* outr,
+                       double* outi) {
+  const int nv = d->nv, nk = nk_of(d), nx = nx_of(d);
+  std::vector<double> ar, ai;
+  val_amat(d, o, pr, pi, ar, ai);
+  std::vector<double> br((size_t)nx * nv * nk, 0.0), bi((size_t)nx * nv * nk, 0.0);
+  std::vector<double> tr(nk), ti(nk);
+  const double inv_nk = 1.0 / (double)nk;
+  for (int y = 0; y < nx; ++y)
+    for (int x = 0; x < nx; ++x) {
+      for (int k = 0; k < nk; ++k) {
+        double sr = 0.0, si = 0.0;
+        for (int v = 0; v < nv; ++v) {
+          const size_t b = (size_t)nx * (v + (size_t)nv * k);
+          const double a_r = ar[b + x], a_i = ai[b + x];
+          const double vr = o->valr[b + y], vi = o->vali[b + y];
+          sr += a_r * vr + a_i * vi;
+          si += a_i * vr - a_r * vi;
+        }
+        tr[k] = sr;
+        ti[k] = si;
+      }
+      or_fft3d(d->kmesh, tr.data(), ti.data(), -1);
+      const double* lad = o->ladder + (size_t)nk * (x + (size_t)nx * y);
+      for (int k = 0; k < nk; ++k) {
+        tr[k] *= lad[k];
+        ti[k] *= lad[k];
+      }
+      or_fft3d(d->kmesh, tr.data(), ti.data(), +1);
+      for (int k = 0; k < nk; ++k) {
+        const double t_r = tr[k] * inv_nk, t_i = ti[k] * inv_nk;
+        for (int v = 0; v < nv; ++v) {
+          const size_t b = (size_t)nx * (v + (size_t)nv * k);
+          const double vr = o->valr[b + y], vi = o->vali[b + y];
+          br[b + x] += t_r * vr - t_i * vi;
+          bi[b + x] += t_i * vr + t_r * vi;
+        }
+      }
+    }
+  val_project(d, o, -1.0, br, bi, outr, outi);
+}
+
+// OCEAN_xact valence branch (OCEAN_action.f90:521-575) followed by
+// OCEAN_energies_act (:590-600, OCEAN_energies.f90:890-906).
+int or_val_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, double* hr,
+               double* hi, int backwards) {
+  const size_t n = (size_t)d->nc * d->nv * nk_of(d);
+  std::vector<double> qr(n), qi(n), kr(n, 0.0), ki(n, 0.0);
+  for (size_t i = 0; i < n; ++i) {
+    qr[i] = pr[i] * o->allow[i];
+    qi[i] = pi[i] * o->allow[i];
+  }
+  if (o->bflag) or_val_bubble_act(d, o, qr.data(), qi.data(), kr.data(), ki.data());
+  if (o->lflag) or_val_ladder_act(d, o, qr.data(), qi.data(), kr.data(), ki.data());
+  for (size_t i = 0; i < n; ++i) {
+    double er = 0.0, ei = 0.0;
+    if (o->bande) {
+      const double a = o->er[i], b = o->ei ? o->ei[i] : 0.0;
+      if (backwards) {
+        er = a * pr[i] + b * pi[i];
+        ei = a * pi[i] - b * pr[i];
+      } else {
+        er = a * pr[i] - b * pi[i];
+        ei = a * pi[i] + b * pr[i];
+      }
+    }
+    hr[i] = er + o->allow[i] * kr[i];
+    hi[i] = ei + o->allow[i] * ki[i];
+  }
+  return 0;
+}
+
+// The Hermitian Haydock recursion of OCEAN_haydock_Herm_do with
+// ocean_hay_ab_twoterm (OCEAN_haydock.f90:190-320, 824-938) over the valence
+// action, in the same arithmetic order as or_haydock.
+int or_val_haydock(const or_val_dims* d, const or_val_ops* o, const double* p0r, const double* p0i, int niter,
+                   double* real_a, double* imag_a, double* real_b, int* niter_done) {
+  const size_t n = (size_t)d->nc * d->nv * nk_of(d);
+  std::vector<double> psr(p0r, p0r + n), psi_(p0i, p0i + n);
+  std::vector<double> olr(n, 0.0), oli(n, 0.0), hr(n), hi(n);
+  for (int i = 0; i <= niter; ++i) real_a[i] = imag_a[i] = real_b[i] = 0.0;
+  int done = 0;
+  for (int iter = 1; iter <= niter; ++iter) {
+    or_val_act(d, o, psr.data(), psi_.data(), hr.data(), hi.data(), 0);
+    const double bm = -real_b[iter - 1];
+    for (size_t i = 0; i < n; ++i) {
+      hr[i] += bm * olr[i];
+      hi[i] += bm * oli[i];
+    }
+    double ar = 0.0, ai = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+      ar += hr[i] * psr[i] + hi[i] * psi_[i];
+      ai += hr[i] * psi_[i] - hi[i] * psr[i];
+    }
+    real_a[iter - 1] = ar;
+    for (size_t i = 0; i < n; ++i) {
+      hr[i] += -ar * psr[i];
+      hi[i] += -ar * psi_[i];
+    }
+    double bb = 0.0;
+    for (size_t i = 0; i < n; ++i) bb += hr[i] * hr[i] + hi[i] * hi[i];
+    olr = psr;
+    oli = psi_;
+    real_b[iter] = std::sqrt(bb);
+    const double inv = 1.0 / real_b[iter];
+    for (size_t i = 0; i < n; ++i) {
+      psr[i] = hr[i] * inv;
+      psi_[i] = hi[i] * inv;
+    }
+    imag_a[iter - 1] = ai;
+    done = iter;
+    if (std::isnan(real_a[iter - 1])) {
+      *niter_done = done;
+      return -1;
+    }
+  }
+  *niter_done = done;
+  return 0;
+}
+
+}  // extern "C"

@@ -43,8 +43,8 @@ class OrLrIn(C.Structure):
 
 def build(force: bool = False) -> str:
     path = os.path.join(_HERE, "liboracle.so")
-    src = os.path.join(_HERE, "ocean_oracle.cpp")
-    if force or not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("ocean_oracle.cpp", "ocean_oracle_val.cpp", "ocean_oracle.h")]
+    if force or not os.path.exists(path) or os.path.getmtime(path) < max(os.path.getmtime(f) for f in srcs):
         subprocess.check_call(["make", "-s", "-C", _HERE, "liboracle.so"])
     return path
 
@@ -57,6 +57,7 @@ def lib():
         L.or_intval.restype = C.c_double
         L.or_pnorm.restype = C.c_double
         L.or_gamfcn.restype = C.c_double
+        L.or_val_wall_length.restype = C.c_double
     return _LIB
 
 
@@ -244,3 +245,67 @@ def zhptrf_solve(ap: np.ndarray, b: np.ndarray):
         lib().or_zhptrs_u(n, apc.view(np.float64).ctypes.data_as(DP), iptr(ipiv),
                           x.view(np.float64).ctypes.data_as(DP))
     return info, ipiv, x
+
+
+# ---------------------------------------------------------------- valence BSE
+
+class OrValDims(C.Structure):
+    _fields_ = [("nc", C.c_int), ("nv", C.c_int), ("kmesh", C.c_int * 3), ("xmesh", C.c_int * 3)]
+
+
+class OrValOps(C.Structure):
+    _fields_ = [("er", DP), ("ei", DP), ("allow", DP), ("conr", DP), ("coni", DP), ("valr", DP),
+                ("vali", DP), ("bubble", DP), ("ladder", DP), ("bande", C.c_int), ("bflag", C.c_int),
+                ("lflag", C.c_int)]
+
+
+def val_wall_length(xmesh, bvec) -> float:
+    return lib().or_val_wall_length((C.c_int * 3)(*xmesh), (C.c_double * 9)(*list(bvec)))
+
+
+def val_bubble(xmesh, bvec, qinb, celvol, nkpts):
+    """AI_bubble_populate with wall_search_old_way; returns (bubble, ngvec)."""
+    n = int(np.prod(xmesh))
+    out = np.zeros(n)
+    length = val_wall_length(xmesh, bvec)
+    ng = lib().or_val_bubble_populate((C.c_int * 3)(*xmesh), (C.c_double * 9)(*list(bvec)),
+                                      (C.c_double * 3)(*list(qinb)), C.c_double(celvol), nkpts,
+                                      C.c_double(length), dptr(out))
+    return out, ng
+
+
+class OracleVal:
+    """Operator data of one valence workload (ValWorkload with host arrays)."""
+
+    def __init__(self, w, bflag=1, lflag=1, bande=1):
+        self.w = w
+        self.bubble, self.ngvec = val_bubble(w.xmesh, w.bvec, w.qinb, w.celvol, w.nk)
+        self._refs = [np.ascontiguousarray(a, dtype=np.float64) for a in
+                      (w.er, w.ei, w.allow, w.conr, w.coni, w.valr, w.vali, self.bubble, w.ladder)]
+        d = OrValDims()
+        d.nc, d.nv = w.nc, w.nv
+        d.kmesh[:] = list(w.kmesh)
+        d.xmesh[:] = list(w.xmesh)
+        self.d = d
+        o = OrValOps()
+        (o.er, o.ei, o.allow, o.conr, o.coni, o.valr, o.vali, o.bubble, o.ladder) = [dptr(a) for a in self._refs]
+        o.bande, o.bflag, o.lflag = bande, bflag, lflag
+        self.o = o
+
+    def act(self, pr, pi, backwards=False, flags=None):
+        if flags is not None:
+            self.o.bande, self.o.bflag, self.o.lflag = flags
+        hr, hi = np.zeros(self.w.npsi), np.zeros(self.w.npsi)
+        lib().or_val_act(C.byref(self.d), C.byref(self.o), dptr(np.ascontiguousarray(pr, dtype=np.float64)),
+                         dptr(np.ascontiguousarray(pi, dtype=np.float64)), dptr(hr), dptr(hi), int(bool(backwards)))
+        return hr, hi
+
+    def haydock(self, niter, pr=None, pi=None):
+        w = self.w
+        pr = np.ascontiguousarray(w.psi_r if pr is None else pr, dtype=np.float64)
+        pi = np.ascontiguousarray(w.psi_i if pi is None else pi, dtype=np.float64)
+        ra, ia, rb = np.zeros(niter + 1), np.zeros(niter + 1), np.zeros(niter + 1)
+        done = C.c_int(0)
+        rc = lib().or_val_haydock(C.byref(self.d), C.byref(self.o), dptr(pr), dptr(pi), niter, dptr(ra), dptr(ia),
+                                  dptr(rb), C.byref(done))
+        return rc, ra, ia, rb, done.value

@@ -1,0 +1,129 @@
+"""Valence BSE action and Haydock on the GPU against the oracle.
+
+Tolerances
+  * FP64 H psi vs oracle (each term alone and all together): relative 2-norm < 1e-12
+  * mixed H psi vs oracle: relative 2-norm < 1e-6 (the direct term's FP32 part
+    is a small fraction of H psi on these inputs; the term alone: < 1e-5)
+  * FP64 Haydock: first 10 a_n relative < 1e-12, b_n < 1e-12
+  * mixed Haydock: spectrum (Spect(0) column) relative < 1e-4
+  * benchmark size (v2, states and ladder built on the device): Hermiticity
+    |<y|Hx> - conj(<x|Hy>)| / |<y|Hx>| < 1e-12 (FP64), < 1e-6 (mixed), and
+    linearity H(x + 2y) = Hx + 2Hy to 1e-12 (FP64)
+"""
+import numpy as np
+import pytest
+
+from ocean_gb300 import capi
+from ocean_gb300 import workloads as WL
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def built(lib_built, oracle_lib):
+    import torch  # noqa: F401
+
+    return capi.load(lib_built), oracle_lib
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("name", ["vtiny", "vsmall", "vodd"])
+@pytest.mark.parametrize("prec", [capi.OCN_PREC_FP64, capi.OCN_PREC_MIXED])
+def test_apply_matches_oracle(built, name, prec):
+    _, O = built
+    w = WL.make_val(name, seed=11)
+    P = O.OracleVal(w)
+    ctx = capi.ValContext(w, precision=prec)
+    try:
+        rng = np.random.default_rng(2)
+        x = rng.standard_normal(w.npsi) + 1j * rng.standard_normal(w.npsi)
+        for flags in [(1, 1, 1), (1, 0, 0), (0, 1, 0), (0, 0, 1)]:
+            for back in (False, True):
+                gr, gi = ctx.apply_H(x.real, x.imag, flags=flags, backwards=back)
+                orr, oi = P.act(x.real, x.imag, backwards=back, flags=flags)
+                assert np.linalg.norm(orr + 1j * oi) > 0.0, (name, flags)
+                err = _rel(gr + 1j * gi, orr + 1j * oi)
+                if prec == capi.OCN_PREC_FP64:
+                    tol = 1e-12
+                else:
+                    tol = 1e-5 if flags == (0, 0, 1) else 1e-6
+                assert err < tol, (name, flags, back, err)
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("prec", [capi.OCN_PREC_FP64, capi.OCN_PREC_MIXED])
+def test_haydock_matches_oracle(built, prec):
+    _, O = built
+    w = WL.make_val("vsmall", seed=12)
+    P = O.OracleVal(w)
+    ctx = capi.ValContext(w, precision=prec)
+    try:
+        niter = 30
+        ra, ia, rb, done = ctx.haydock(niter)
+        rc, ora, oia, orb, odone = P.haydock(niter)
+        assert rc == 0 and done == niter == odone
+        if prec == capi.OCN_PREC_FP64:
+            assert np.max(np.abs(ra[:10] - ora[:10]) / np.abs(ora[:10])) < 1e-12
+            assert np.max(np.abs(rb[1:11] - orb[1:11]) / np.abs(orb[1:11])) < 1e-12
+        s = capi.spectrum_cf(ra, ia, rb, niter, w.kpref, w.el, w.eh, 400, w.gam0)
+        so = O.write_core(ora, oia, orb, niter, w.kpref, w.el, w.eh, 400, w.gam0)
+        assert _rel(s[:, 2], so[:, 2]) < (1e-10 if prec == capi.OCN_PREC_FP64 else 1e-4)
+    finally:
+        ctx.close()
+
+
+def test_device_entry_points_equal_host_ones(built):
+    import torch
+
+    w = WL.make_val("vodd", seed=13)
+    ctx = capi.ValContext(w, precision=capi.OCN_PREC_MIXED)
+    try:
+        hr, hi = ctx.apply_H(w.psi_r, w.psi_i)
+        d_in = torch.tensor(np.concatenate([w.psi_r, w.psi_i]), device="cuda:0")
+        d_out = torch.empty_like(d_in)
+        torch.cuda.synchronize()
+        ctx.apply_H_dev(d_in.data_ptr(), d_out.data_ptr())
+        torch.cuda.synchronize()
+        out = d_out.cpu().numpy()
+        assert np.array_equal(out[:w.npsi], hr) and np.array_equal(out[w.npsi:], hi)
+        a1 = ctx.haydock(12)
+        a2 = ctx.haydock_dev(12, d_in.data_ptr())
+        assert np.array_equal(a1[0], a2[0]) and np.array_equal(a1[2], a2[2])
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("prec", [capi.OCN_PREC_FP64, capi.OCN_PREC_MIXED])
+def test_benchmark_size_is_hermitian_and_linear(built, prec):
+    import torch
+
+    w = WL.make_val("v2", seed=14, device="cuda:0")
+    ctx = capi.ValContext(w, precision=prec)
+    try:
+        g = torch.Generator(device="cuda:0")
+        g.manual_seed(7)
+        n = w.npsi
+        x = torch.randn(2 * n, generator=g, device="cuda:0", dtype=torch.float64)
+        y = torch.randn(2 * n, generator=g, device="cuda:0", dtype=torch.float64)
+        hx, hy, hz = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
+        torch.cuda.synchronize()
+        ctx.apply_H_dev(x.data_ptr(), hx.data_ptr())
+        ctx.apply_H_dev(y.data_ptr(), hy.data_ptr())
+        z = x + 2.0 * y
+        torch.cuda.synchronize()
+        ctx.apply_H_dev(z.data_ptr(), hz.data_ptr())
+        torch.cuda.synchronize()
+        c = lambda v: torch.complex(v[:n], v[n:])  # noqa: E731
+        lhs = torch.vdot(c(y), c(hx)).item()
+        rhs = torch.vdot(c(x), c(hy)).conj().item()
+        tol = 1e-12 if prec == capi.OCN_PREC_FP64 else 1e-6
+        assert abs(lhs - rhs) / abs(lhs) < tol
+        lin = (torch.linalg.norm(c(hz) - c(hx) - 2.0 * c(hy)) / torch.linalg.norm(c(hz))).item()
+        assert lin < (1e-12 if prec == capi.OCN_PREC_FP64 else 1e-6)
+        assert torch.isfinite(hz).all()
+    finally:
+        ctx.close()

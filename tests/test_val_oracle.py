@@ -1,0 +1,103 @@
+"""CPU tests of the valence BSE pieces that need no GPU.
+
+* the library's host bubble builder (AI_bubble_populate with
+  wall_search_old_way, OCEAN_bubble.f90:238-407) is bit-identical to the
+  oracle's restatement, for even and odd meshes, zero and finite q;
+* the oracle's valence action (OCEAN_action.f90:521-600) is Hermitian, term by
+  term, on the synthetic inputs (the ladder satisfies ladder(-R,y,x) =
+  ladder(R,x,y));
+* the oracle's Haydock run over it reproduces the dense Hamiltonian's spectrum
+  edges (Ritz values of the tridiagonal, redtrid);
+* ocn_val_create rejects bad dimensions before touching a GPU.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from ocean_gb300 import capi
+from ocean_gb300 import workloads as WL
+
+
+@pytest.mark.parametrize("xmesh,qinb", [((4, 4, 4), (0, 0, 0)), ((3, 4, 5), (0, 0, 0)),
+                                        ((6, 5, 4), (0.05, 0.0, 0.02)), ((10, 10, 10), (0, 0, 0))])
+def test_bubble_matches_oracle_bit_for_bit(lib_built, oracle_lib, xmesh, qinb):
+    capi.load(lib_built)
+    O = oracle_lib
+    a = 4.0 / WL.BOHR
+    bvec = np.zeros(9)
+    bvec[0], bvec[4], bvec[8] = 2 * np.pi / a, 2 * np.pi / (1.1 * a), 2 * np.pi / (0.9 * a)
+    celvol = a ** 3 * 1.1 * 0.9
+    b_lib, n_lib = capi.val_bubble(xmesh, bvec, qinb, celvol, 64)
+    b_or, n_or = O.val_bubble(xmesh, bvec, qinb, celvol, 64)
+    assert n_lib == n_or
+    assert np.array_equal(b_lib, b_or)
+    assert b_lib[0] == 0.0 and np.all(b_lib >= 0.0) and np.count_nonzero(b_lib) > 0
+
+
+def test_bubble_is_inversion_symmetric_at_q0(lib_built):
+    capi.load(lib_built)
+    w = WL.make_val("vodd")
+    b, _ = capi.val_bubble((5, 5, 5), w.bvec, (0, 0, 0), w.celvol, w.nk)
+    B = b.reshape(5, 5, 5)
+    assert np.array_equal(B, B[(-np.arange(5)) % 5][:, (-np.arange(5)) % 5][:, :, (-np.arange(5)) % 5])
+
+
+@pytest.mark.parametrize("name", ["vtiny", "vodd", "vsmall"])
+def test_oracle_action_is_hermitian(oracle_lib, name):
+    O = oracle_lib
+    w = WL.make_val(name, seed=3)
+    P = O.OracleVal(w)
+    rng = np.random.default_rng(5)
+    n = w.npsi
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    y = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    for flags in [(1, 1, 1), (0, 1, 0), (0, 0, 1)]:
+        hx = P.act(x.real, x.imag, flags=flags)
+        hy = P.act(y.real, y.imag, flags=flags)
+        Hx, Hy = hx[0] + 1j * hx[1], hy[0] + 1j * hy[1]
+        lhs, rhs = np.vdot(y, Hx), np.conj(np.vdot(x, Hy))
+        assert abs(lhs - rhs) <= 1e-12 * abs(lhs), flags
+
+
+def test_oracle_haydock_brackets_the_dense_spectrum(oracle_lib):
+    O = oracle_lib
+    w = WL.make_val("vtiny", seed=4)
+    P = O.OracleVal(w)
+    n = w.npsi
+    H = np.zeros((n, n), dtype=complex)
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = 1.0
+        hr, hi = P.act(e, np.zeros(n))
+        H[:, j] = hr + 1j * hi
+    assert np.allclose(H, H.conj().T, atol=1e-13)
+    ev = np.linalg.eigvalsh(H)
+    niter = 40
+    rc, ra, ia, rb, done = P.haydock(niter)
+    assert rc == 0 and done == niter
+    assert np.max(np.abs(ia[:niter])) < 1e-12 * np.max(np.abs(ra[:niter]))
+    T = np.diag(ra[:niter]) + np.diag(rb[1:niter], 1) + np.diag(rb[1:niter], -1)
+    ritz = np.linalg.eigvalsh(T)
+    assert abs(ritz[0] - ev[0]) < 1e-8 and abs(ritz[-1] - ev[-1]) < 1e-8
+    assert ritz[0] >= ev[0] - 1e-10 and ritz[-1] <= ev[-1] + 1e-10
+
+
+def test_val_create_rejects_bad_dims_without_gpu(lib_built):
+    lib = capi.load(lib_built)
+    for change in [("nv", 0), ("nv", 33), ("nc", 0), ("precision", 5)]:
+        d = capi.OcnValDims()
+        d.nc, d.nv = 4, 2
+        d.kmesh[:] = [2, 2, 2]
+        d.xmesh[:] = [3, 3, 3]
+        setattr(d, change[0], change[1])
+        p = C.c_void_p()
+        assert lib.ocn_val_create(C.byref(d), C.byref(p)) == capi.OCN_ERR_ARG
+        assert not p.value
+    d = capi.OcnValDims()
+    d.nc, d.nv = 4, 2
+    d.kmesh[:] = [2, 2, 40]
+    d.xmesh[:] = [3, 3, 3]
+    p = C.c_void_p()
+    assert lib.ocn_val_create(C.byref(d), C.byref(p)) == capi.OCN_ERR_ARG
+    assert "mesh" in capi.val_last_error()
