@@ -313,6 +313,158 @@ __global__ void __launch_bounds__(VAL_THREADS)
   }
 }
 
+// N consecutive complex values; FP32 lines of even length (16-byte aligned:
+// every caller's offset is a multiple of N complex values) as 16-byte loads.
+template <typename CT, int N>
+__device__ __forceinline__ void load_line(const CT* __restrict__ p, CT (&v)[N]) {
+  if constexpr (sizeof(CT) == 8 && N % 2 == 0) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int i = 0; i < N / 2; ++i) {
+      const float4 t = __ldg(q + i);
+      v[2 * i].x = t.x;
+      v[2 * i].y = t.y;
+      v[2 * i + 1].x = t.z;
+      v[2 * i + 1].y = t.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < N; ++j) v[j] = p[j];
+  }
+}
+
+// The direct term on a cubic k-mesh N^3 (same arithmetic as kv_ladder, fewer
+// shared-memory passes): the T build is fused with the forward transform along
+// k3, the forward transform along k1, the ladder product and the backward
+// transform along k1 share one pass in registers, and the B sums of the CTA's
+// (k1 k2 line, v) pairs stay in registers across the whole y-range.
+// MAXC: (line, v) pairs per thread (N^2 nv <= MAXC * blockDim).
+template <typename R, int N, int MAXC>
+__global__ void __launch_bounds__(VAL_THREADS)
+    kv_ladder_cube(const typename C2<R>::T* __restrict__ A, const typename C2<R>::T* __restrict__ valT,
+                   const R* __restrict__ lad, typename C2<R>::T* __restrict__ Bp, int nv, int nx, int ytile, int yper,
+                   const typename C2<R>::T* __restrict__ twg) {
+  typedef typename C2<R>::T CT;
+  constexpr int NK = N * N * N, NL = N * N, P3 = N + 1;
+  constexpr int SLAB = ocn::cube_slab<CT>(N);
+  extern __shared__ __align__(16) unsigned char vsm[];
+  CT* tw = reinterpret_cast<CT*>(vsm);
+  CT* As = tw + 3 * OCN_MAX_KDIM;
+  CT* T = As + (size_t)nv * NK;
+  const int x = blockIdx.x, ys = blockIdx.y;
+  const int ybeg = ys * yper, yend = min(nx, ybeg + yper);
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
+  // As[(v N + k3) NL + line]: the lanes of the T build (consecutive k1 k2
+  // lines) read consecutive words
+  const CT* Ax = A + (size_t)x * nv * NK;
+  for (int e = threadIdx.x; e < nv * NK; e += blockDim.x) {
+    const int vv = e / NK, k = e % NK;
+    As[(vv * N + k % N) * NL + k / N] = Ax[e];
+  }
+  const int ncomb = NL * nv;
+  CT acc[MAXC][N];
+#pragma unroll
+  for (int q = 0; q < MAXC; ++q)
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      acc[q][j].x = (R)0;
+      acc[q][j].y = (R)0;
+    }
+  __syncthreads();
+  for (int y0 = ybeg; y0 < yend; y0 += ytile) {
+    const int ny = min(ytile, yend - y0);
+    // T(y, k) for a k3 line, then the forward transform along k3
+    for (int li = threadIdx.x; li < ny * NL; li += blockDim.x) {
+      const int yl = li / NL, ln = li % NL;
+      const CT* vt = valT + (size_t)(y0 + yl) * nv * NK + ln * N;
+      const CT* as = As + ln;
+      CT v[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        v[j].x = (R)0;
+        v[j].y = (R)0;
+      }
+      for (int vv = 0; vv < nv; ++vv) {
+        CT bl[N];
+        load_line<CT, N>(vt + (size_t)vv * NK, bl);
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+          const CT a = as[(vv * N + j) * NL], b = bl[j];
+          v[j].x += a.x * b.x + a.y * b.y;
+          v[j].y += a.y * b.x - a.x * b.y;
+        }
+      }
+      ocn::line_dft<CT, R, N>(v, tw + 2 * OCN_MAX_KDIM, (R)-1);
+      CT* p = T + yl * SLAB + ln * P3;
+#pragma unroll
+      for (int j = 0; j < N; ++j) p[j] = v[j];
+    }
+    __syncthreads();
+    ocn::cube_pass<R, N, 0>(T, ny, 1, tw + OCN_MAX_KDIM, (R)-1);
+    __syncthreads();
+    // forward along k1, times ladder(k, x, y), backward along k1
+    for (int li = threadIdx.x; li < ny * NL; li += blockDim.x) {
+      const int yl = li / NL, r = li % NL;
+      const int k2 = r / N, k3 = r % N;
+      CT* p = T + yl * SLAB + k2 * P3 + k3;
+      const R* w = lad + ((size_t)(y0 + yl) * nx + x) * NK + r;
+      CT v[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) v[j] = p[j * N * P3];
+      ocn::line_dft<CT, R, N>(v, tw, (R)-1);
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const R ww = w[j * NL];
+        v[j].x *= ww;
+        v[j].y *= ww;
+      }
+      ocn::line_dft<CT, R, N>(v, tw, (R)1);
+#pragma unroll
+      for (int j = 0; j < N; ++j) p[j * N * P3] = v[j];
+    }
+    __syncthreads();
+    ocn::cube_pass<R, N, 0>(T, ny, 1, tw + OCN_MAX_KDIM, (R)1);
+    __syncthreads();
+    ocn::cube_pass<R, N, 0>(T, ny, 2, tw + 2 * OCN_MAX_KDIM, (R)1);
+    __syncthreads();
+    // B(v, k) += T(y, k) val(y, v, k) for the (line, v) pairs of this thread
+#pragma unroll
+    for (int q = 0; q < MAXC; ++q) {
+      const int cb = threadIdx.x + q * VAL_THREADS;
+      if (cb < ncomb) {
+        const int ln = cb / nv, vv = cb % nv;
+        for (int yl = 0; yl < ny; ++yl) {
+          const CT* p = T + yl * SLAB + ln * P3;
+          CT bl[N];
+          load_line<CT, N>(valT + ((size_t)(y0 + yl) * nv + vv) * NK + ln * N, bl);
+#pragma unroll
+          for (int j = 0; j < N; ++j) {
+            const CT t = p[j], b = bl[j];
+            acc[q][j].x += t.x * b.x - t.y * b.y;
+            acc[q][j].y += t.y * b.x + t.x * b.y;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  const R inv = (R)1 / (R)NK;  // FFT_wrapper_single's backward normalisation
+#pragma unroll
+  for (int q = 0; q < MAXC; ++q) {
+    const int cb = threadIdx.x + q * VAL_THREADS;
+    if (cb < ncomb) {
+      const int ln = cb / nv, vv = cb % nv;
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        CT o = acc[q][j];
+        o.x *= inv;
+        o.y *= inv;
+        Bp[(((size_t)ys * NK + ln * N + j) * nv + vv) * nx + x] = o;
+      }
+    }
+  }
+}
+
 // out(c,v,k) = E o psi (conj E when backwards) + allow o sum_x conj(con(x,c,k))
 // M(x,v,k), M = 2 s(x) val(x,v,k) - sum_ys B_ys(x,v,k) (OCEAN_bubble.f90:742-757
 // with spin_prefac 2, OCEAN_ladder.f90:900-911 with -1, OCEAN_energies.f90:890-906).
@@ -555,15 +707,45 @@ size_t ladder_slab(const ocn_val_ctx* c) {
   return (size_t)c->dims.kmesh[0] * c->dims.kmesh[1] * (c->dims.kmesh[2] + 1);
 }
 
+// the fused cubic kernel applies when the mesh is a supported cube and each
+// thread owns at most two (line, v) pairs
+bool use_cube_kernel(const ocn_val_ctx* c) {
+  const int n = c->dims.kmesh[0];
+  return cubic(c->dims.kmesh) && cube_kernel_n(n) && n * n * c->nv <= 2 * VAL_THREADS;
+}
+
 template <typename R>
 size_t ladder_smem(const ocn_val_ctx* c, int ytile) {
+  const size_t bs = use_cube_kernel(c) ? 0 : (size_t)c->nv * c->nk;  // the cubic kernel sums B in registers
   return sizeof(typename C2<R>::T) *
-         (3 * OCN_MAX_KDIM + 2 * (size_t)c->nv * c->nk + (size_t)ytile * ladder_slab<R>(c));
+         (3 * OCN_MAX_KDIM + (size_t)c->nv * c->nk + bs + (size_t)ytile * ladder_slab<R>(c));
 }
 
 template <typename R>
 using LadderFn = void (*)(const typename C2<R>::T*, const typename C2<R>::T*, const R*, typename C2<R>::T*, int,
                           int, int, int, int, const KmeshGeom<R>, int, const typename C2<R>::T*);
+
+template <typename R>
+using LadderCubeFn = void (*)(const typename C2<R>::T*, const typename C2<R>::T*, const R*, typename C2<R>::T*,
+                              int, int, int, int, const typename C2<R>::T*);
+
+template <typename R, int N>
+LadderCubeFn<R> cube_fn2(const ocn_val_ctx* c) {
+  return N * N * c->nv <= VAL_THREADS ? kv_ladder_cube<R, N, 1> : kv_ladder_cube<R, N, 2>;
+}
+
+template <typename R>
+LadderCubeFn<R> ladder_cube_fn(const ocn_val_ctx* c) {
+  switch (c->dims.kmesh[0]) {
+    case 2: return cube_fn2<R, 2>(c);
+    case 3: return cube_fn2<R, 3>(c);
+    case 4: return cube_fn2<R, 4>(c);
+    case 5: return cube_fn2<R, 5>(c);
+    case 6: return cube_fn2<R, 6>(c);
+    case 8: return cube_fn2<R, 8>(c);
+  }
+  return nullptr;
+}
 
 template <typename R>
 LadderFn<R> ladder_fn(const ocn_val_ctx* c) {
@@ -583,21 +765,36 @@ LadderFn<R> ladder_fn(const ocn_val_ctx* c) {
 template <typename R>
 int plan_ladder(ocn_val_ctx* c) {
   int ytile = 16;
-  const size_t target = std::min<size_t>(c->smem_optin, 110 * 1024);
+  const size_t target = std::min<size_t>(c->smem_optin, use_cube_kernel(c) ? 56 * 1024 : 110 * 1024);
   while (ytile > 1 && ladder_smem<R>(c, ytile) > target) --ytile;
   if (ladder_smem<R>(c, ytile) > c->smem_optin)
     return vset_err(c, OCN_ERR_UNSUPPORTED,
                     "ocn_val: Nv*Nk too large for the direct-term kernel's shared memory");
   c->ytile = ytile;
   c->lad_smem = ladder_smem<R>(c, ytile);
-  const int want = std::max(1, (4 * c->sm_count + c->nx - 1) / c->nx);
-  const int maxsplit = std::max(1, (c->nx + ytile - 1) / ytile);
-  c->ysplit = std::min(want, maxsplit);
-  c->yper = (c->nx + c->ysplit - 1) / c->ysplit;
-  c->ysplit = (c->nx + c->yper - 1) / c->yper;
-  cudaError_t e = cudaFuncSetAttribute(ladder_fn<R>(c), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)c->lad_smem);
+  const bool cube = use_cube_kernel(c);
+  const void* fn = cube ? (const void*)ladder_cube_fn<R>(c) : (const void*)ladder_fn<R>(c);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->lad_smem);
   if (e != cudaSuccess) return vcuda(c, e, "cudaFuncSetAttribute(kv_ladder)");
+  int per_sm = 1;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, VAL_THREADS, c->lad_smem);
+  if (e != cudaSuccess) return vcuda(c, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor(kv_ladder)");
+  // y-ranges per x-point: the split (up to 8, ranges no shorter than a tile)
+  // whose CTA count fills the last wave best
+  const double slots = (double)std::max(1, per_sm) * c->sm_count;
+  const int maxsplit = std::max(1, std::min(8, c->nx / ytile));
+  int best = 1;
+  double best_eff = 0.0;
+  for (int sp = 1; sp <= maxsplit; ++sp) {
+    const double waves = (double)c->nx * sp / slots;
+    const double eff = waves / std::ceil(waves);
+    if (eff > best_eff + 0.02) {
+      best_eff = eff;
+      best = sp;
+    }
+  }
+  c->yper = (c->nx + best - 1) / best;
+  c->ysplit = (c->nx + c->yper - 1) / c->yper;
   return OCN_OK;
 }
 
@@ -656,9 +853,14 @@ int apply_impl(ocn_val_ctx* c, const double* d_in, double* d_out, const int flag
     const CT* tw;
     if constexpr (sizeof(R) == 4) tw = c->d_twk32;
     else tw = c->d_twk;
-    ladder_fn<R>(c)<<<dim3(c->nx, c->ysplit), VAL_THREADS, c->lad_smem, c->stream>>>(
-        A, static_cast<const CT*>(c->d_valT), static_cast<const R*>(c->d_lad), Bp, c->nv, c->nk, c->nx, c->ytile,
-        c->yper, g, g.slab, tw);
+    if (use_cube_kernel(c))
+      ladder_cube_fn<R>(c)<<<dim3(c->nx, c->ysplit), VAL_THREADS, c->lad_smem, c->stream>>>(
+          A, static_cast<const CT*>(c->d_valT), static_cast<const R*>(c->d_lad), Bp, c->nv, c->nx, c->ytile,
+          c->yper, tw);
+    else
+      ladder_fn<R>(c)<<<dim3(c->nx, c->ysplit), VAL_THREADS, c->lad_smem, c->stream>>>(
+          A, static_cast<const CT*>(c->d_valT), static_cast<const R*>(c->d_lad), Bp, c->nv, c->nk, c->nx,
+          c->ytile, c->yper, g, g.slab, tw);
     ++c->launches;
     VCUDA(c, cudaGetLastError());
   }
