@@ -82,6 +82,7 @@ struct ocn_val_ctx {
   int coef_cap = 0;
   int red_blocks = 1;
   int ytile = 1, ysplit = 1, yper = 1;
+  int xper = 1;  // x-points per CTA of the cubic direct-term kernel
   size_t lad_smem = 0;
   long long launches = 0;
   std::string err;
@@ -333,14 +334,16 @@ __device__ __forceinline__ void load_line(const CT* __restrict__ p, CT (&v)[N]) 
   }
 }
 
-// The direct term on a cubic k-mesh N^3 (same arithmetic as kv_ladder, fewer
-// shared-memory passes): the T build is fused with the forward transform along
-// k3, the forward transform along k1, the ladder product and the backward
-// transform along k1 share one pass in registers, and the B sums of the CTA's
-// (k1 k2 line, v) pairs stay in registers across the whole y-range.
+// The direct term on a cubic k-mesh N^3 for X x-points per CTA (same
+// arithmetic as kv_ladder, fewer shared-memory passes): the T build is fused
+// with the forward transform along k3 (one val line serves all X x-points),
+// the forward transform along k1, the ladder product and the backward
+// transform along k1 share one pass in registers, and the backward transform
+// along k3 is redone in registers by each thread of the B sum, whose (k1 k2
+// line, v) pairs stay in registers across the whole y-range.
 // MAXC: (line, v) pairs per thread (N^2 nv <= MAXC * blockDim).
-template <typename R, int N, int MAXC>
-__global__ void __launch_bounds__(VAL_THREADS)
+template <typename R, int N, int MAXC, int X>
+__global__ void __launch_bounds__(VAL_THREADS, sizeof(R) == 4 ? (X == 1 ? 4 : 3) : 2)
     kv_ladder_cube(const typename C2<R>::T* __restrict__ A, const typename C2<R>::T* __restrict__ valT,
                    const R* __restrict__ lad, typename C2<R>::T* __restrict__ Bp, int nv, int nx, int ytile, int yper,
                    const typename C2<R>::T* __restrict__ twg) {
@@ -349,65 +352,81 @@ __global__ void __launch_bounds__(VAL_THREADS)
   constexpr int SLAB = ocn::cube_slab<CT>(N);
   extern __shared__ __align__(16) unsigned char vsm[];
   CT* tw = reinterpret_cast<CT*>(vsm);
-  CT* As = tw + 3 * OCN_MAX_KDIM;
-  CT* T = As + (size_t)nv * NK;
-  const int x = blockIdx.x, ys = blockIdx.y;
+  CT* As = tw + 3 * OCN_MAX_KDIM;        // [xi][(v N + k3) NL + line]
+  CT* T = As + (size_t)X * nv * NK;      // slab (yl X + xi)
+  const int x0 = blockIdx.x * X, ys = blockIdx.y;
   const int ybeg = ys * yper, yend = min(nx, ybeg + yper);
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
-  // As[(v N + k3) NL + line]: the lanes of the T build (consecutive k1 k2
-  // lines) read consecutive words
-  const CT* Ax = A + (size_t)x * nv * NK;
-  for (int e = threadIdx.x; e < nv * NK; e += blockDim.x) {
-    const int vv = e / NK, k = e % NK;
-    As[(vv * N + k % N) * NL + k / N] = Ax[e];
+  // the lanes of the T build (consecutive k1 k2 lines) read consecutive words;
+  // an x-point past the mesh (odd Nx) is staged as zeros and never stored
+  for (int e = threadIdx.x; e < X * nv * NK; e += blockDim.x) {
+    const int xi = e / (nv * NK), r = e % (nv * NK);
+    const int vv = r / NK, k = r % NK;
+    CT a;
+    a.x = (R)0;
+    a.y = (R)0;
+    if (x0 + xi < nx) a = A[(size_t)(x0 + xi) * nv * NK + r];
+    As[xi * nv * NK + (vv * N + k % N) * NL + k / N] = a;
   }
   const int ncomb = NL * nv;
-  CT acc[MAXC][N];
+  CT acc[MAXC][X][N];
 #pragma unroll
   for (int q = 0; q < MAXC; ++q)
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-      acc[q][j].x = (R)0;
-      acc[q][j].y = (R)0;
-    }
+    for (int xi = 0; xi < X; ++xi)
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        acc[q][xi][j].x = (R)0;
+        acc[q][xi][j].y = (R)0;
+      }
   __syncthreads();
   for (int y0 = ybeg; y0 < yend; y0 += ytile) {
     const int ny = min(ytile, yend - y0);
-    // T(y, k) for a k3 line, then the forward transform along k3
+    // T(x, y, k) for a k3 line, then the forward transform along k3
     for (int li = threadIdx.x; li < ny * NL; li += blockDim.x) {
       const int yl = li / NL, ln = li % NL;
       const CT* vt = valT + (size_t)(y0 + yl) * nv * NK + ln * N;
-      const CT* as = As + ln;
-      CT v[N];
+      CT v[X][N];
 #pragma unroll
-      for (int j = 0; j < N; ++j) {
-        v[j].x = (R)0;
-        v[j].y = (R)0;
-      }
+      for (int xi = 0; xi < X; ++xi)
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+          v[xi][j].x = (R)0;
+          v[xi][j].y = (R)0;
+        }
       for (int vv = 0; vv < nv; ++vv) {
         CT bl[N];
         load_line<CT, N>(vt + (size_t)vv * NK, bl);
 #pragma unroll
-        for (int j = 0; j < N; ++j) {
-          const CT a = as[(vv * N + j) * NL], b = bl[j];
-          v[j].x += a.x * b.x + a.y * b.y;
-          v[j].y += a.y * b.x - a.x * b.y;
+        for (int xi = 0; xi < X; ++xi) {
+          const CT* as = As + xi * nv * NK + ln;
+#pragma unroll
+          for (int j = 0; j < N; ++j) {
+            const CT a = as[(vv * N + j) * NL], b = bl[j];
+            v[xi][j].x += a.x * b.x + a.y * b.y;
+            v[xi][j].y += a.y * b.x - a.x * b.y;
+          }
         }
       }
-      ocn::line_dft<CT, R, N>(v, tw + 2 * OCN_MAX_KDIM, (R)-1);
-      CT* p = T + yl * SLAB + ln * P3;
 #pragma unroll
-      for (int j = 0; j < N; ++j) p[j] = v[j];
+      for (int xi = 0; xi < X; ++xi) {
+        ocn::line_dft<CT, R, N>(v[xi], tw + 2 * OCN_MAX_KDIM, (R)-1);
+        CT* p = T + (yl * X + xi) * SLAB + ln * P3;
+#pragma unroll
+        for (int j = 0; j < N; ++j) p[j] = v[xi][j];
+      }
     }
     __syncthreads();
-    ocn::cube_pass<R, N, 0>(T, ny, 1, tw + OCN_MAX_KDIM, (R)-1);
+    ocn::cube_pass<R, N, 0>(T, ny * X, 1, tw + OCN_MAX_KDIM, (R)-1);
     __syncthreads();
     // forward along k1, times ladder(k, x, y), backward along k1
-    for (int li = threadIdx.x; li < ny * NL; li += blockDim.x) {
-      const int yl = li / NL, r = li % NL;
+    for (int li = threadIdx.x; li < ny * X * NL; li += blockDim.x) {
+      const int sl = li / NL, r = li % NL;
+      const int yl = sl / X, xi = sl % X;
       const int k2 = r / N, k3 = r % N;
-      CT* p = T + yl * SLAB + k2 * P3 + k3;
-      const R* w = lad + ((size_t)(y0 + yl) * nx + x) * NK + r;
+      CT* p = T + sl * SLAB + k2 * P3 + k3;
+      const int xx = min(x0 + xi, nx - 1);  // a padding x-point reads a valid row and is never stored
+      const R* w = lad + ((size_t)(y0 + yl) * nx + xx) * NK + r;
       CT v[N];
 #pragma unroll
       for (int j = 0; j < N; ++j) v[j] = p[j * N * P3];
@@ -423,25 +442,29 @@ __global__ void __launch_bounds__(VAL_THREADS)
       for (int j = 0; j < N; ++j) p[j * N * P3] = v[j];
     }
     __syncthreads();
-    ocn::cube_pass<R, N, 0>(T, ny, 1, tw + OCN_MAX_KDIM, (R)1);
+    ocn::cube_pass<R, N, 0>(T, ny * X, 1, tw + OCN_MAX_KDIM, (R)1);
     __syncthreads();
-    ocn::cube_pass<R, N, 0>(T, ny, 2, tw + 2 * OCN_MAX_KDIM, (R)1);
-    __syncthreads();
-    // B(v, k) += T(y, k) val(y, v, k) for the (line, v) pairs of this thread
+    // backward along k3 in registers, then B(x, v, k) += T(x, y, k) val(y, v, k)
 #pragma unroll
     for (int q = 0; q < MAXC; ++q) {
       const int cb = threadIdx.x + q * VAL_THREADS;
       if (cb < ncomb) {
         const int ln = cb / nv, vv = cb % nv;
         for (int yl = 0; yl < ny; ++yl) {
-          const CT* p = T + yl * SLAB + ln * P3;
           CT bl[N];
           load_line<CT, N>(valT + ((size_t)(y0 + yl) * nv + vv) * NK + ln * N, bl);
 #pragma unroll
-          for (int j = 0; j < N; ++j) {
-            const CT t = p[j], b = bl[j];
-            acc[q][j].x += t.x * b.x - t.y * b.y;
-            acc[q][j].y += t.y * b.x + t.x * b.y;
+          for (int xi = 0; xi < X; ++xi) {
+            const CT* p = T + (yl * X + xi) * SLAB + ln * P3;
+            CT t[N];
+#pragma unroll
+            for (int j = 0; j < N; ++j) t[j] = p[j];
+            ocn::line_dft<CT, R, N>(t, tw + 2 * OCN_MAX_KDIM, (R)1);
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+              acc[q][xi][j].x += t[j].x * bl[j].x - t[j].y * bl[j].y;
+              acc[q][xi][j].y += t[j].y * bl[j].x + t[j].x * bl[j].y;
+            }
           }
         }
       }
@@ -455,11 +478,15 @@ __global__ void __launch_bounds__(VAL_THREADS)
     if (cb < ncomb) {
       const int ln = cb / nv, vv = cb % nv;
 #pragma unroll
-      for (int j = 0; j < N; ++j) {
-        CT o = acc[q][j];
-        o.x *= inv;
-        o.y *= inv;
-        Bp[(((size_t)ys * NK + ln * N + j) * nv + vv) * nx + x] = o;
+      for (int xi = 0; xi < X; ++xi) {
+        if (x0 + xi >= nx) continue;
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+          CT o = acc[q][xi][j];
+          o.x *= inv;
+          o.y *= inv;
+          Bp[(((size_t)ys * NK + ln * N + j) * nv + vv) * nx + x0 + xi] = o;
+        }
       }
     }
   }
@@ -716,9 +743,11 @@ bool use_cube_kernel(const ocn_val_ctx* c) {
 
 template <typename R>
 size_t ladder_smem(const ocn_val_ctx* c, int ytile) {
-  const size_t bs = use_cube_kernel(c) ? 0 : (size_t)c->nv * c->nk;  // the cubic kernel sums B in registers
+  if (use_cube_kernel(c))  // X x-points' A and ytile * X transforms; B sums live in registers
+    return sizeof(typename C2<R>::T) * (3 * OCN_MAX_KDIM + (size_t)c->xper * c->nv * c->nk +
+                                        (size_t)ytile * c->xper * ladder_slab<R>(c));
   return sizeof(typename C2<R>::T) *
-         (3 * OCN_MAX_KDIM + (size_t)c->nv * c->nk + bs + (size_t)ytile * ladder_slab<R>(c));
+         (3 * OCN_MAX_KDIM + 2 * (size_t)c->nv * c->nk + (size_t)ytile * ladder_slab<R>(c));
 }
 
 template <typename R>
@@ -731,7 +760,9 @@ using LadderCubeFn = void (*)(const typename C2<R>::T*, const typename C2<R>::T*
 
 template <typename R, int N>
 LadderCubeFn<R> cube_fn2(const ocn_val_ctx* c) {
-  return N * N * c->nv <= VAL_THREADS ? kv_ladder_cube<R, N, 1> : kv_ladder_cube<R, N, 2>;
+  const bool one = N * N * c->nv <= VAL_THREADS;
+  if (c->xper == 2) return one ? kv_ladder_cube<R, N, 1, 2> : kv_ladder_cube<R, N, 2, 2>;
+  return one ? kv_ladder_cube<R, N, 1, 1> : kv_ladder_cube<R, N, 2, 1>;
 }
 
 template <typename R>
@@ -765,7 +796,12 @@ LadderFn<R> ladder_fn(const ocn_val_ctx* c) {
 template <typename R>
 int plan_ladder(ocn_val_ctx* c) {
   int ytile = 16;
-  const size_t target = std::min<size_t>(c->smem_optin, use_cube_kernel(c) ? 56 * 1024 : 110 * 1024);
+  // cubic kernel: two x-points per CTA and the largest y-tile that leaves two
+  // CTAs per SM (measured on the 8^3 k-mesh, 10^3 x-mesh case: 5.9 ms per
+  // H psi with one x-point and 56 KB, 5.2 ms with two and 56 KB, 5.0 ms with
+  // two and 110 KB)
+  c->xper = (use_cube_kernel(c) && c->nx >= 2) ? 2 : 1;
+  const size_t target = std::min<size_t>(c->smem_optin, 110 * 1024);
   while (ytile > 1 && ladder_smem<R>(c, ytile) > target) --ytile;
   if (ladder_smem<R>(c, ytile) > c->smem_optin)
     return vset_err(c, OCN_ERR_UNSUPPORTED,
@@ -783,10 +819,11 @@ int plan_ladder(ocn_val_ctx* c) {
   // whose CTA count fills the last wave best
   const double slots = (double)std::max(1, per_sm) * c->sm_count;
   const int maxsplit = std::max(1, std::min(8, c->nx / ytile));
+  const int nxb = (c->nx + c->xper - 1) / c->xper;
   int best = 1;
   double best_eff = 0.0;
   for (int sp = 1; sp <= maxsplit; ++sp) {
-    const double waves = (double)c->nx * sp / slots;
+    const double waves = (double)nxb * sp / slots;
     const double eff = waves / std::ceil(waves);
     if (eff > best_eff + 0.02) {
       best_eff = eff;
@@ -854,7 +891,7 @@ int apply_impl(ocn_val_ctx* c, const double* d_in, double* d_out, const int flag
     if constexpr (sizeof(R) == 4) tw = c->d_twk32;
     else tw = c->d_twk;
     if (use_cube_kernel(c))
-      ladder_cube_fn<R>(c)<<<dim3(c->nx, c->ysplit), VAL_THREADS, c->lad_smem, c->stream>>>(
+      ladder_cube_fn<R>(c)<<<dim3((c->nx + c->xper - 1) / c->xper, c->ysplit), VAL_THREADS, c->lad_smem, c->stream>>>(
           A, static_cast<const CT*>(c->d_valT), static_cast<const R*>(c->d_lad), Bp, c->nv, c->nx, c->ytile,
           c->yper, tw);
     else
