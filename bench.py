@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -57,6 +58,9 @@ def parse():
     ap.add_argument("--nonherm-steps", type=int, default=60,
                     help="steps of the non-Hermitian (two-sided Lanczos) leg on the main workload with a "
                          "lifetime Sigma'' on the bands, both precisions; 0 = off")
+    ap.add_argument("--valence-steps", type=int, default=40,
+                    help="Lanczos steps of the valence BSE leg (8^3 k, 10^3 x, 8+4 bands; exchange + screened "
+                         "direct), both precisions, with the oracle timed on a y-slab; 0 = off")
     ap.add_argument("--batch", type=int, default=64,
                     help="instances of the batched uneven-Haydock leg (3 polarisations each); 0 = off")
     ap.add_argument("--adjoint-omega", type=int, default=400,
@@ -311,6 +315,86 @@ def run_small(args, torch, capi, WL, local):
     for name in ("mixed", "fp64"):
         out[name]["spectral_error_vs_oracle"] = float(np.linalg.norm(spec[name][:, 2] - so[:, 2]) /
                                                       np.linalg.norm(so[:, 2]))
+    return out
+
+
+def run_valence(args, torch, capi, WL, local):
+    """Valence BSE (exchange + screened direct + pair energies) on the v2 case:
+    Haydock H*psi/s of both precisions, the spectral error of the mixed run, the
+    direct term's kernel rate, and the oracle's H*psi time estimated from the
+    exchange part plus a timed y-slab of the direct term (scaled to all y)."""
+    import dataclasses
+    import time
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    dev = f"cuda:{local}"
+    w = WL.make_val("v2", seed=0, device=dev)
+    niter = args.valence_steps
+    nk, nx, nv = w.nk, w.nx, w.nv
+    out = {"workload": f"v2: k-mesh {'x'.join(map(str, w.kmesh))}, x-mesh {'x'.join(map(str, w.xmesh))}, "
+                       f"{w.nc} conduction + {nv} valence bands, exchange + screened direct",
+           "steps": niter}
+    d0 = torch.tensor(np.concatenate([w.psi_r, w.psi_i]), device=dev)
+    spec = {}
+    for name, prec in (("mixed", capi.OCN_PREC_MIXED), ("fp64", capi.OCN_PREC_FP64)):
+        ctx = capi.ValContext(w, precision=prec, device=local)
+        ctx.haydock_dev(3, d0.data_ptr())
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ra, ia, rb, done = ctx.haydock_dev(niter, d0.data_ptr())
+        dt = time.perf_counter() - t0
+        # the direct term alone: H psi with and without it, CUDA events on the context stream
+        st = torch.cuda.ExternalStream(ctx.stream)
+        hx = torch.empty_like(d0)
+        ms = {}
+        for key, flags in (("all", (1, 1, 1)), ("no_direct", (1, 1, 0))):
+            reps = 5 if name == "mixed" else 2
+            ctx.apply_H_dev(d0.data_ptr(), hx.data_ptr(), flags=flags)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                ctx.apply_H_dev(d0.data_ptr(), hx.data_ptr(), flags=flags)
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms[key] = e0.elapsed_time(e1) / reps
+        ctx.close()
+        spec[name] = capi.spectrum_cf(ra, ia, rb, done, w.kpref, w.el, w.eh, args.ne, w.gam0)
+        direct_ms = ms["all"] - ms["no_direct"]
+        # algorithmic work of the direct term per H psi: T build and B sums
+        # (8 nv nk flops each per (x, y)), two k-mesh FFTs (5 nk log2 nk each),
+        # the ladder product (2 nk); ladder bytes nx^2 nk in the term's precision
+        flops = nx * nx * (16.0 * nv * nk + 10.0 * nk * math.log2(nk) + 2.0 * nk)
+        lad_bytes = nx * nx * nk * (4 if name == "mixed" else 8)
+        out[name] = {"value": niter / dt, "unit": UNIT, "ms_per_hpsi": dt * 1e3 / niter,
+                     "hpsi_ms_events": ms["all"], "direct_term_ms": direct_ms,
+                     "direct_term_tflops": flops / (direct_ms * 1e-3) / 1e12,
+                     "direct_term_ladder_gbs": lad_bytes / (direct_ms * 1e-3) / 1e9}
+    out["spectral_error_mixed_vs_fp64"] = float(np.linalg.norm(spec["mixed"][:, 2] - spec["fp64"][:, 2]) /
+                                                np.linalg.norm(spec["fp64"][:, 2]))
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    # CPU: the oracle's exchange + energies on the whole problem, and the direct
+    # term on ny_s of the nx y-points (scaled by nx / ny_s); one core
+    a = w.device_arrays
+    wh = dataclasses.replace(w, conr=a["conr"].cpu().numpy(), coni=a["coni"].cpu().numpy(),
+                             valr=a["valr"].cpu().numpy(), vali=a["vali"].cpu().numpy(), ladder=None)
+    ny_s = 4
+    slab = a["ladder"].reshape(nx, nx * nk)[:ny_s].cpu().numpy().reshape(-1)
+    P = O.OracleVal(wh, bande=1, bflag=1, lflag=0)
+    t0 = time.perf_counter()
+    P.act(w.psi_r, w.psi_i)
+    t_x = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    P.ladder_slab(w.psi_r, w.psi_i, 0, ny_s, slab)
+    t_s = time.perf_counter() - t0
+    t_hpsi = t_x + t_s * nx / ny_s
+    out["cpu_oracle"] = {"value": 1.0 / t_hpsi, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"exchange + energies on the whole case ({t_x:.2f} s) and the direct term "
+                                   f"on {ny_s} of {nx} y-points ({t_s:.2f} s), scaled to all y"}
+    out["speedup_mixed_vs_cpu_oracle"] = out["mixed"]["value"] / out["cpu_oracle"]["value"]
+    del a, w
+    torch.cuda.empty_cache()
     return out
 
 
@@ -608,6 +692,11 @@ def run_ours(args, ws, rank, local, pg):
     if rank == 0 and args.nonherm_steps > 0 and prec == capi.OCN_PREC_MIXED:
         nh = run_nonherm(args, torch, capi, w, local)
 
+    # ---- valence leg: exchange + screened direct terms on the v2 case, both precisions
+    val = None
+    if rank == 0 and args.valence_steps > 0 and prec == capi.OCN_PREC_MIXED:
+        val = run_valence(args, torch, capi, WL, local)
+
     # ---- batched leg: independent uneven instances (k-mesh n^3, n in {4,5,6,8};
     #      bands U{24..128}; 1s or 2p; x-mesh 8^3..12^3), 3 polarisations each,
     #      500 Lanczos steps, all advanced by one graph launch per 3 steps
@@ -713,7 +802,8 @@ def run_ours(args, ws, rank, local, pg):
                            w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
             "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
             "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "adjoint": adj, "batch": bat,
-            "multiplet": mlt, "nonherm": nh, "c1": small, "roofline": roof, "cpu_baseline": cpu,
+            "multiplet": mlt, "nonherm": nh, "valence": val, "c1": small, "roofline": roof,
+            "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
                     "d2h_bytes_per_step": 3 * (niter + 1) * 8 + (ne + 1) * 9 * 8},
             "gpu_launches": launches, "clocks": clocks, "kernel_ms": kt}

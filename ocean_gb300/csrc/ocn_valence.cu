@@ -66,6 +66,8 @@ struct ocn_val_ctx {
   double* d_allow = nullptr;
   double2* d_con = nullptr;   // [k][c][x]
   double2* d_val = nullptr;   // [k][v][x]
+  float2* d_con32 = nullptr;  // FP32 copies (mixed precision)
+  float2* d_val32 = nullptr;
   void* d_valT = nullptr;     // [y][v][k], double2 or float2
   void* d_lad = nullptr;      // [y][x][k], double or float
   double* d_bub = nullptr;    // [x]
@@ -119,106 +121,166 @@ int valloc(ocn_val_ctx* c, T** p, size_t count) {
 
 // A(x,v,k) = sum_c con(x,c,k) (allow o psi)(c,v,k) (OCEAN_bubble.f90:521-530,
 // OCEAN_ladder.f90:317-326) and the exchange partial
-// l_k(x) = sum_v conj(val(x,v,k)) A(x,v,k) (OCEAN_bubble.f90:568-580).
+// l_k(x) = sum_v conj(val(x,v,k)) A(x,v,k) (OCEAN_bubble.f90:568-580), summed
+// over the block's 8 k-points (in k order) into lp[k / 8][x].
 // Block: 32 x-points by 8 k-points; lanes along x read con rows coalesced.
+// R: arithmetic and state precision (FP32 copies of con/val in mixed mode).
 template <typename R, int MAXV>
 __global__ void __launch_bounds__(VAL_THREADS)
     kv_amat(const double* __restrict__ pr, const double* __restrict__ pi, const double* __restrict__ allow,
-            const double2* __restrict__ con, const double2* __restrict__ val, int nc, int nv, int nk, int nx,
-            double2* __restrict__ lp, typename C2<R>::T* __restrict__ A) {
+            const typename C2<R>::T* __restrict__ con, const typename C2<R>::T* __restrict__ val, int nc, int nv,
+            int nk, int nx, double2* __restrict__ lp, typename C2<R>::T* __restrict__ A) {
   typedef typename C2<R>::T CT;
-  extern __shared__ double2 qs[];  // [kl][cl][v]
+  extern __shared__ __align__(16) unsigned char amsm[];
+  CT* qs = reinterpret_cast<CT*>(amsm);  // [kl][cl][v]
+  __shared__ double2 lred[8][32];
   const int xl = threadIdx.x, kl = threadIdx.y;
   const int tid = kl * 32 + xl;
   const int x = blockIdx.x * 32 + xl, k0 = blockIdx.y * 8, k = k0 + kl;
-  double2 acc[MAXV];
+  CT acc[MAXV];
 #pragma unroll
-  for (int v = 0; v < MAXV; ++v) acc[v] = make_double2(0.0, 0.0);
+  for (int v = 0; v < MAXV; ++v) {
+    acc[v].x = (R)0;
+    acc[v].y = (R)0;
+  }
   for (int c0 = 0; c0 < nc; c0 += VAL_CC) {
     const int cn = min(VAL_CC, nc - c0);
     __syncthreads();
     for (int e = tid; e < 8 * VAL_CC * nv; e += VAL_THREADS) {
       const int kk = e / (VAL_CC * nv), r = e % (VAL_CC * nv);
       const int cl = r / nv, v = r % nv;
-      double2 q = make_double2(0.0, 0.0);
+      CT q;
+      q.x = (R)0;
+      q.y = (R)0;
       if (k0 + kk < nk && cl < cn) {
         const size_t idx = (size_t)(c0 + cl) + (size_t)nc * (v + (size_t)nv * (k0 + kk));
         const double m = allow[idx];
-        q = make_double2(pr[idx] * m, pi[idx] * m);
+        q.x = (R)(pr[idx] * m);
+        q.y = (R)(pi[idx] * m);
       }
       qs[e] = q;
     }
     __syncthreads();
     if (x < nx && k < nk) {
       for (int cl = 0; cl < cn; ++cl) {
-        const double2 cv = con[((size_t)k * nc + c0 + cl) * nx + x];
-        const double2* q = qs + (kl * VAL_CC + cl) * nv;
+        const CT cv = con[((size_t)k * nc + c0 + cl) * nx + x];
+        const CT* q = qs + (kl * VAL_CC + cl) * nv;
 #pragma unroll
         for (int v = 0; v < MAXV; ++v)
           if (v < nv) {
-            const double2 qq = q[v];
+            const CT qq = q[v];
             acc[v].x += cv.x * qq.x - cv.y * qq.y;
             acc[v].y += cv.y * qq.x + cv.x * qq.y;
           }
       }
     }
   }
+  R lr = (R)0, li = (R)0;
   if (x < nx && k < nk) {
-    double lr = 0.0, li = 0.0;
 #pragma unroll
     for (int v = 0; v < MAXV; ++v)
       if (v < nv) {
-        const double2 vv = val[((size_t)k * nv + v) * nx + x];
+        const CT vv = val[((size_t)k * nv + v) * nx + x];
         lr += vv.x * acc[v].x + vv.y * acc[v].y;
         li += vv.x * acc[v].y - vv.y * acc[v].x;
-        CT a;
-        a.x = (R)acc[v].x;
-        a.y = (R)acc[v].y;
-        A[((size_t)x * nv + v) * nk + k] = a;
+        A[((size_t)x * nv + v) * nk + k] = acc[v];
       }
-    lp[(size_t)k * nx + x] = make_double2(lr, li);
+  }
+  lred[kl][xl] = make_double2((double)lr, (double)li);
+  __syncthreads();
+  if (kl == 0 && x < nx) {
+    double sr = 0.0, si = 0.0;
+    for (int i = 0; i < 8; ++i) {
+      sr += lred[i][xl].x;
+      si += lred[i][xl].y;
+    }
+    lp[(size_t)blockIdx.y * nx + x] = make_double2(sr, si);
   }
 }
 
-// l(x) = sum_k l_k(x), k in order.
-__global__ void kv_bub_reduce(const double2* __restrict__ lp, int nk, int nx, double2* __restrict__ l) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= nx) return;
+// l(x) = sum_b lp[b][x] over the nkb k-blocks: 32 slices per x-point, each a
+// strided sum in b order, then the slices in order.
+__global__ void __launch_bounds__(1024) kv_bub_reduce(const double2* __restrict__ lp, int nkb, int nx,
+                                                      double2* __restrict__ l) {
+  __shared__ double2 part[32][33];
+  const int xl = threadIdx.x, sl = threadIdx.y;
+  const int x = blockIdx.x * 32 + xl;
   double sr = 0.0, si = 0.0;
-  for (int k = 0; k < nk; ++k) {
-    const double2 t = lp[(size_t)k * nx + x];
-    sr += t.x;
-    si += t.y;
+  if (x < nx)
+    for (int b = sl; b < nkb; b += 32) {
+      const double2 t = lp[(size_t)b * nx + x];
+      sr += t.x;
+      si += t.y;
+    }
+  part[sl][xl] = make_double2(sr, si);
+  __syncthreads();
+  if (sl == 0 && x < nx) {
+    double tr = 0.0, ti = 0.0;
+    for (int i = 0; i < 32; ++i) {
+      tr += part[i][xl].x;
+      ti += part[i][xl].y;
+    }
+    l[x] = make_double2(tr, ti);
   }
-  l[x] = make_double2(sr, si);
+}
+
+// One pass along `ax` of a 3-D DFT over the whole mesh, one output element per
+// thread (out of place): out(m) = sum_j in(j) w^(j m), w = exp(sgn 2 pi i / n_ax).
+__device__ __forceinline__ void xmesh_pass(const double2* __restrict__ in, double2* __restrict__ out, const int n[3],
+                                           int ax, const double2* __restrict__ tw, double sgn) {
+  const int nx = n[0] * n[1] * n[2];
+  const int st = ax == 2 ? 1 : (ax == 1 ? n[2] : n[1] * n[2]);
+  const int na = n[ax];
+  for (int o = threadIdx.x; o < nx; o += blockDim.x) {
+    const int m = (o / st) % na;
+    const double2* line = in + (o - m * st);
+    double sr = 0.0, si = 0.0;
+    int t = 0;
+    for (int j = 0; j < na; ++j) {
+      const double2 v = line[j * st];
+      const double2 w = tw[t];
+      const double wy = sgn * w.y;
+      sr += v.x * w.x - v.y * wy;
+      si += v.x * wy + v.y * w.x;
+      t += m;
+      if (t >= na) t -= na;
+    }
+    out[o] = make_double2(sr, si);
+  }
 }
 
 // s = FFT_fwd[ bubble o FFT_bwd[ l ] ] on the x-mesh, neither normalised
 // (OCEAN_bubble.f90:663-665; FFTW signs +1 backward, -1 forward,
-// Modules/FFT_wrapper.f90:24-25).  One CTA; the mesh is a few thousand points.
-__global__ void kv_bub_fft(double2* __restrict__ l, const double* __restrict__ bub, int nx,
-                           const KmeshGeom<double> g, const double2* __restrict__ twg) {
+// Modules/FFT_wrapper.f90:24-25).  One CTA of 1024 threads, ping-pong buffers.
+__global__ void __launch_bounds__(1024) kv_bub_fft(double2* __restrict__ l, const double* __restrict__ bub,
+                                                   const int3 mesh, const double2* __restrict__ twg) {
   extern __shared__ double2 sm[];
+  const int n[3] = {mesh.x, mesh.y, mesh.z};
+  const int nx = n[0] * n[1] * n[2];
   double2* tw = sm;
-  double2* buf = sm + 3 * OCN_MAX_KDIM;
+  double2* b0 = sm + 3 * OCN_MAX_KDIM;
+  double2* b1 = b0 + nx;
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
-  for (int x = threadIdx.x; x < nx; x += blockDim.x) buf[ocn::kpad(g, x)] = l[x];
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) b0[x] = l[x];
   __syncthreads();
-  for (int ax = 0; ax < 3; ++ax) {
-    ocn::dft_pass<double>(buf, g, ax, tw + ax * OCN_MAX_KDIM, 1.0);
-    __syncthreads();
-  }
+  xmesh_pass(b0, b1, n, 0, tw, 1.0);
+  __syncthreads();
+  xmesh_pass(b1, b0, n, 1, tw + OCN_MAX_KDIM, 1.0);
+  __syncthreads();
+  xmesh_pass(b0, b1, n, 2, tw + 2 * OCN_MAX_KDIM, 1.0);
+  __syncthreads();
   for (int x = threadIdx.x; x < nx; x += blockDim.x) {
-    double2& v = buf[ocn::kpad(g, x)];
-    v.x *= bub[x];
-    v.y *= bub[x];
+    b1[x].x *= bub[x];
+    b1[x].y *= bub[x];
   }
   __syncthreads();
-  for (int ax = 0; ax < 3; ++ax) {
-    ocn::dft_pass<double>(buf, g, ax, tw + ax * OCN_MAX_KDIM, -1.0);
-    __syncthreads();
-  }
-  for (int x = threadIdx.x; x < nx; x += blockDim.x) l[x] = buf[ocn::kpad(g, x)];
+  xmesh_pass(b1, b0, n, 0, tw, -1.0);
+  __syncthreads();
+  xmesh_pass(b0, b1, n, 1, tw + OCN_MAX_KDIM, -1.0);
+  __syncthreads();
+  xmesh_pass(b1, b0, n, 2, tw + 2 * OCN_MAX_KDIM, -1.0);
+  __syncthreads();
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) l[x] = b0[x];
 }
 
 // Direct term for the x-point of this CTA and the y-range blockIdx.y
@@ -339,8 +401,8 @@ __device__ __forceinline__ void load_line(const CT* __restrict__ p, CT (&v)[N]) 
 // with the forward transform along k3 (one val line serves all X x-points),
 // the forward transform along k1, the ladder product and the backward
 // transform along k1 share one pass in registers, and the backward transform
-// along k3 is redone in registers by each thread of the B sum, whose (k1 k2
-// line, v) pairs stay in registers across the whole y-range.
+// along k3 is redone in registers by each thread of the B sum (FP32), whose
+// (k1 k2 line, v) pairs stay in registers across the whole y-range.
 // MAXC: (line, v) pairs per thread (N^2 nv <= MAXC * blockDim).
 template <typename R, int N, int MAXC, int X>
 __global__ void __launch_bounds__(VAL_THREADS, sizeof(R) == 4 ? (X == 1 ? 4 : 3) : 2)
@@ -350,6 +412,10 @@ __global__ void __launch_bounds__(VAL_THREADS, sizeof(R) == 4 ? (X == 1 ? 4 : 3)
   typedef typename C2<R>::T CT;
   constexpr int NK = N * N * N, NL = N * N, P3 = N + 1;
   constexpr int SLAB = ocn::cube_slab<CT>(N);
+  // FP32: the last backward transform is redone by each of the nv threads of a
+  // line in the B sum (saves a shared-memory pass); FP64 is FP64-pipe bound,
+  // so there it stays one shared pass (85 ms against 104 ms per H psi)
+  constexpr bool FUSE_K3 = sizeof(R) == 4;
   extern __shared__ __align__(16) unsigned char vsm[];
   CT* tw = reinterpret_cast<CT*>(vsm);
   CT* As = tw + 3 * OCN_MAX_KDIM;        // [xi][(v N + k3) NL + line]
@@ -444,7 +510,11 @@ __global__ void __launch_bounds__(VAL_THREADS, sizeof(R) == 4 ? (X == 1 ? 4 : 3)
     __syncthreads();
     ocn::cube_pass<R, N, 0>(T, ny * X, 1, tw + OCN_MAX_KDIM, (R)1);
     __syncthreads();
-    // backward along k3 in registers, then B(x, v, k) += T(x, y, k) val(y, v, k)
+    if constexpr (!FUSE_K3) {
+      ocn::cube_pass<R, N, 0>(T, ny * X, 2, tw + 2 * OCN_MAX_KDIM, (R)1);
+      __syncthreads();
+    }
+    // backward along k3 (in registers when fused), then B(x, v, k) += T(x, y, k) val(y, v, k)
 #pragma unroll
     for (int q = 0; q < MAXC; ++q) {
       const int cb = threadIdx.x + q * VAL_THREADS;
@@ -459,7 +529,7 @@ __global__ void __launch_bounds__(VAL_THREADS, sizeof(R) == 4 ? (X == 1 ? 4 : 3)
             CT t[N];
 #pragma unroll
             for (int j = 0; j < N; ++j) t[j] = p[j];
-            ocn::line_dft<CT, R, N>(t, tw + 2 * OCN_MAX_KDIM, (R)1);
+            if constexpr (FUSE_K3) ocn::line_dft<CT, R, N>(t, tw + 2 * OCN_MAX_KDIM, (R)1);
 #pragma unroll
             for (int j = 0; j < N; ++j) {
               acc[q][xi][j].x += t[j].x * bl[j].x - t[j].y * bl[j].y;
@@ -499,14 +569,14 @@ __global__ void __launch_bounds__(VAL_THREADS, sizeof(R) == 4 ? (X == 1 ? 4 : 3)
 template <typename R>
 __global__ void __launch_bounds__(VAL_THREADS)
     kv_final(const double* __restrict__ pr, const double* __restrict__ pi, const double* __restrict__ er,
-             const double* __restrict__ ei, const double* __restrict__ allow, const double2* __restrict__ con,
-             const double2* __restrict__ val, const double2* __restrict__ s, const typename C2<R>::T* __restrict__ Bp,
-             int nysplit, int nc, int nv, int nk, int nx, int xchunk, int use_e, int use_x, int use_d, int backwards,
-             double* __restrict__ outr, double* __restrict__ outi) {
+             const double* __restrict__ ei, const double* __restrict__ allow, const typename C2<R>::T* __restrict__ con,
+             const typename C2<R>::T* __restrict__ val, const double2* __restrict__ s,
+             const typename C2<R>::T* __restrict__ Bp, int nysplit, int nc, int nv, int nk, int nx, int xchunk,
+             int use_e, int use_x, int use_d, int backwards, double* __restrict__ outr, double* __restrict__ outi) {
   typedef typename C2<R>::T CT;
   extern __shared__ double2 fsm[];
-  double2* accs = fsm;               // [c + nc v]
-  double2* M = fsm + (size_t)nc * nv;  // [v][xl]
+  double2* accs = fsm;                                   // [c + nc v]
+  CT* M = reinterpret_cast<CT*>(fsm + (size_t)nc * nv);  // [v][xl]
   const int k = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nout = nc * nv;
@@ -517,32 +587,37 @@ __global__ void __launch_bounds__(VAL_THREADS)
       __syncthreads();
       for (int e = threadIdx.x; e < nv * xn; e += blockDim.x) {
         const int v = e / xn, xl = e % xn, x = x0 + xl;
-        double mr = 0.0, mi = 0.0;
+        R mr = (R)0, mi = (R)0;
         if (use_x) {
-          const double2 vv = val[((size_t)k * nv + v) * nx + x];
-          const double2 ss = s[x];
-          mr = 2.0 * (ss.x * vv.x - ss.y * vv.y);
-          mi = 2.0 * (ss.y * vv.x + ss.x * vv.y);
+          const CT vv = val[((size_t)k * nv + v) * nx + x];
+          const double2 sd = s[x];
+          const R sx = (R)sd.x, sy = (R)sd.y;
+          mr = (R)2 * (sx * vv.x - sy * vv.y);
+          mi = (R)2 * (sy * vv.x + sx * vv.y);
         }
         if (use_d)
           for (int ys = 0; ys < nysplit; ++ys) {
             const CT b = Bp[(((size_t)ys * nk + k) * nv + v) * nx + x];
-            mr -= (double)b.x;
-            mi -= (double)b.y;
+            mr -= b.x;
+            mi -= b.y;
           }
-        M[(size_t)v * xchunk + xl] = make_double2(mr, mi);
+        CT mm;
+        mm.x = mr;
+        mm.y = mi;
+        M[(size_t)v * xchunk + xl] = mm;
       }
       __syncthreads();
       for (int o = warp; o < nout; o += VAL_FIN_WARPS) {
         const int c = o % nc, v = o / nc;
-        const double2* cr = con + ((size_t)k * nc + c) * nx + x0;
-        const double2* mv = M + (size_t)v * xchunk;
-        double sr = 0.0, si = 0.0;
+        const CT* cr = con + ((size_t)k * nc + c) * nx + x0;
+        const CT* mv = M + (size_t)v * xchunk;
+        R pr_ = (R)0, pi_ = (R)0;
         for (int xl = lane; xl < xn; xl += 32) {
-          const double2 cc = cr[xl], m = mv[xl];
-          sr += cc.x * m.x + cc.y * m.y;
-          si += cc.x * m.y - cc.y * m.x;
+          const CT cc = cr[xl], m = mv[xl];
+          pr_ += cc.x * m.x + cc.y * m.y;
+          pi_ += cc.x * m.y - cc.y * m.x;
         }
+        double sr = (double)pr_, si = (double)pi_;
         for (int off = 16; off > 0; off >>= 1) {
           sr += __shfl_down_sync(0xffffffffu, sr, off);
           si += __shfl_down_sync(0xffffffffu, si, off);
@@ -796,11 +871,11 @@ LadderFn<R> ladder_fn(const ocn_val_ctx* c) {
 template <typename R>
 int plan_ladder(ocn_val_ctx* c) {
   int ytile = 16;
-  // cubic kernel: two x-points per CTA and the largest y-tile that leaves two
-  // CTAs per SM (measured on the 8^3 k-mesh, 10^3 x-mesh case: 5.9 ms per
-  // H psi with one x-point and 56 KB, 5.2 ms with two and 56 KB, 5.0 ms with
-  // two and 110 KB)
-  c->xper = (use_cube_kernel(c) && c->nx >= 2) ? 2 : 1;
+  // cubic kernel: in FP32 two x-points per CTA and the largest y-tile that
+  // leaves two CTAs per SM (measured on the 8^3 k-mesh, 10^3 x-mesh case: 5.9 ms
+  // per H psi with one x-point and 56 KB, 5.2 ms with two and 56 KB, 5.0 ms with
+  // two and 110 KB); in FP64 two x-points spill registers (85 -> 104 ms), so one
+  c->xper = (use_cube_kernel(c) && c->nx >= 2 && sizeof(R) == 4) ? 2 : 1;
   const size_t target = std::min<size_t>(c->smem_optin, 110 * 1024);
   while (ytile > 1 && ladder_smem<R>(c, ytile) > target) --ytile;
   if (ladder_smem<R>(c, ytile) > c->smem_optin)
@@ -843,6 +918,13 @@ size_t final_xchunk(const ocn_val_ctx* c) {
   return xc;
 }
 
+size_t final_smem(const ocn_val_ctx* c) {
+  const size_t ct = c->mixed ? sizeof(float2) : sizeof(double2);
+  return sizeof(double2) * (size_t)c->nc * c->nv + ct * (size_t)c->nv * final_xchunk(c);
+}
+
+size_t bub_fft_smem(const ocn_val_ctx* c) { return sizeof(double2) * (3 * OCN_MAX_KDIM + 2 * (size_t)c->nx); }
+
 int check_ready(ocn_val_ctx* c, const int flags[3]) {
   if (flags[0] && !c->have_e) return vset_err(c, OCN_ERR_STATE, "ocn_val: energies not set");
   if (!c->have_allow) return vset_err(c, OCN_ERR_STATE, "ocn_val: allow mask not set");
@@ -859,28 +941,30 @@ int apply_impl(ocn_val_ctx* c, const double* d_in, double* d_out, const int flag
   const int use_e = flags[0], use_x = flags[1], use_d = flags[2];
   CT* A = static_cast<CT*>(c->d_A);
   CT* Bp = static_cast<CT*>(c->d_Bp);
+  const CT* con = c->mixed ? reinterpret_cast<const CT*>(c->d_con32) : reinterpret_cast<const CT*>(c->d_con);
+  const CT* val = c->mixed ? reinterpret_cast<const CT*>(c->d_val32) : reinterpret_cast<const CT*>(c->d_val);
   if (use_x || use_d) {
     dim3 blk(32, 8), grd((c->nx + 31) / 32, (c->nk + 7) / 8);
-    const size_t sm = sizeof(double2) * 8 * VAL_CC * c->nv;
+    const size_t sm = sizeof(CT) * 8 * VAL_CC * c->nv;
     if (c->nv <= 4)
-      kv_amat<R, 4><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, c->d_con, c->d_val, c->nc, c->nv,
+      kv_amat<R, 4><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, con, val, c->nc, c->nv,
                                                  c->nk, c->nx, c->d_lp, A);
     else if (c->nv <= 8)
-      kv_amat<R, 8><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, c->d_con, c->d_val, c->nc, c->nv,
+      kv_amat<R, 8><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, con, val, c->nc, c->nv,
                                                  c->nk, c->nx, c->d_lp, A);
     else if (c->nv <= 16)
-      kv_amat<R, 16><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, c->d_con, c->d_val, c->nc, c->nv,
+      kv_amat<R, 16><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, con, val, c->nc, c->nv,
                                                   c->nk, c->nx, c->d_lp, A);
     else
-      kv_amat<R, 32><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, c->d_con, c->d_val, c->nc, c->nv,
+      kv_amat<R, 32><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, con, val, c->nc, c->nv,
                                                   c->nk, c->nx, c->d_lp, A);
     ++c->launches;
     VCUDA(c, cudaGetLastError());
   }
   if (use_x) {
-    kv_bub_reduce<<<(c->nx + 255) / 256, 256, 0, c->stream>>>(c->d_lp, c->nk, c->nx, c->d_s);
-    const KmeshGeom<double> gx = ocn::kmesh_geom<double>(c->dims.xmesh, 1);
-    kv_bub_fft<<<1, VAL_THREADS, ocn::kmesh_smem(gx), c->stream>>>(c->d_s, c->d_bub, c->nx, gx, c->d_twx);
+    kv_bub_reduce<<<(c->nx + 31) / 32, dim3(32, 32), 0, c->stream>>>(c->d_lp, (c->nk + 7) / 8, c->nx, c->d_s);
+    kv_bub_fft<<<1, 1024, bub_fft_smem(c), c->stream>>>(
+        c->d_s, c->d_bub, make_int3(c->dims.xmesh[0], c->dims.xmesh[1], c->dims.xmesh[2]), c->d_twx);
     c->launches += 2;
     VCUDA(c, cudaGetLastError());
   }
@@ -902,9 +986,9 @@ int apply_impl(ocn_val_ctx* c, const double* d_in, double* d_out, const int flag
     VCUDA(c, cudaGetLastError());
   }
   const int xc = (int)final_xchunk(c);
-  const size_t fsm = sizeof(double2) * ((size_t)c->nc * c->nv + (size_t)c->nv * xc);
+  const size_t fsm = final_smem(c);
   kv_final<R><<<c->nk, VAL_THREADS, fsm, c->stream>>>(
-      d_in, d_in + n, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow, c->d_con, c->d_val, c->d_s, Bp,
+      d_in, d_in + n, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow, con, val, c->d_s, Bp,
       c->ysplit, c->nc, c->nv, c->nk, c->nx, xc, use_e, use_x, use_d, backwards, d_out, d_out + n);
   ++c->launches;
   VCUDA(c, cudaGetLastError());
@@ -973,10 +1057,12 @@ int ocn_val_create(const ocn_val_dims* d, ocn_val_ctx** out) {
       (rc = valloc(c, reinterpret_cast<char**>(&c->d_lad), nxk * c->nx * rs)) ||
       (rc = valloc(c, &c->d_bub, c->nx)) || (rc = valloc(c, &c->d_twk, 3 * OCN_MAX_KDIM)) ||
       (rc = valloc(c, &c->d_twk32, 3 * OCN_MAX_KDIM)) || (rc = valloc(c, &c->d_twx, 3 * OCN_MAX_KDIM)) ||
-      (rc = valloc(c, &c->d_lp, nxk)) || (rc = valloc(c, &c->d_s, c->nx)) ||
+      (rc = valloc(c, &c->d_lp, (size_t)c->nx * ((c->nk + 7) / 8))) || (rc = valloc(c, &c->d_s, c->nx)) ||
       (rc = valloc(c, reinterpret_cast<char**>(&c->d_A), nxk * c->nv * cs)) ||
       (rc = valloc(c, reinterpret_cast<char**>(&c->d_Bp), nxk * c->nv * c->ysplit * cs)) ||
       (rc = valloc(c, &c->d_vec, 8 * c->npsi)) || (rc = valloc(c, &c->d_red, 4 * (size_t)c->red_blocks)))
+    return fail(rc);
+  if (c->mixed && ((rc = valloc(c, &c->d_con32, nxk * c->nc)) || (rc = valloc(c, &c->d_val32, nxk * c->nv))))
     return fail(rc);
   double2 twk[3][OCN_MAX_KDIM], twx[3][OCN_MAX_KDIM];
   float2 twk32[3][OCN_MAX_KDIM];
@@ -988,17 +1074,19 @@ int ocn_val_create(const ocn_val_dims* d, ocn_val_ctx** out) {
       (rc = upload(c, c->d_twk32, twk32, sizeof(twk32))))
     return fail(rc);
   cudaMemsetAsync(c->d_ei, 0, sizeof(double) * c->npsi, c->stream);
-  const KmeshGeom<double> gx = ocn::kmesh_geom<double>(d->xmesh, 1);
-  if (ocn::kmesh_smem(gx) > 48 * 1024) {
-    e = cudaFuncSetAttribute(kv_bub_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ocn::kmesh_smem(gx));
+  if (bub_fft_smem(c) > c->smem_optin)
+    return fail(vset_err(c, OCN_ERR_UNSUPPORTED, "ocn_val_create: x-mesh too large for the exchange transform"));
+  if (bub_fft_smem(c) > 48 * 1024) {
+    e = cudaFuncSetAttribute(kv_bub_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bub_fft_smem(c));
     if (e != cudaSuccess) return fail(vcuda(c, e, "cudaFuncSetAttribute(kv_bub_fft)"));
   }
-  if (sizeof(double2) * 8 * VAL_CC * c->nv > 48 * 1024) {  // Nv > 24: the 32-wide instantiation
-    e = cudaFuncSetAttribute(c->mixed ? (const void*)kv_amat<float, 32> : (const void*)kv_amat<double, 32>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(double2) * 8 * VAL_CC * c->nv));
+  // dynamic + 4 KB static above the default 48 KB: Nv > 22, the 32-wide instantiation
+  if (sizeof(double2) * 8 * VAL_CC * c->nv + 4096 > 48 * 1024 && !c->mixed) {
+    e = cudaFuncSetAttribute(kv_amat<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(double2) * 8 * VAL_CC * c->nv));
     if (e != cudaSuccess) return fail(vcuda(c, e, "cudaFuncSetAttribute(kv_amat)"));
   }
-  const size_t fsm = sizeof(double2) * ((size_t)c->nc * c->nv + (size_t)c->nv * final_xchunk(c));
+  const size_t fsm = final_smem(c);
   if (fsm > c->smem_optin) return fail(vset_err(c, OCN_ERR_UNSUPPORTED, "ocn_val_create: Nc*Nv too large"));
   e = cudaFuncSetAttribute(c->mixed ? (const void*)kv_final<float> : (const void*)kv_final<double>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
@@ -1013,7 +1101,7 @@ int ocn_val_destroy(ocn_val_ctx* c) {
   if (!c) return OCN_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void* bufs[] = {c->d_er, c->d_ei, c->d_allow, c->d_con, c->d_val, c->d_valT, c->d_lad, c->d_bub,
+  void* bufs[] = {c->d_er, c->d_ei, c->d_allow, c->d_con, c->d_val, c->d_con32, c->d_val32, c->d_valT, c->d_lad, c->d_bub,
                   c->d_twk, c->d_twk32, c->d_twx, c->d_lp, c->d_s, c->d_A, c->d_Bp, c->d_vec, c->d_red,
                   c->d_coef};
   for (void* p : bufs)
@@ -1090,9 +1178,14 @@ static int set_states_impl(ocn_val_ctx* c, const double* conr, const double* con
       goto done;
   }
   kv_interleave<<<g, 256, 0, c->stream>>>(vr, vi, nval, c->d_val);
-  if (c->mixed)
+  if (c->mixed) {
     kv_transpose_val<float><<<g, 256, 0, c->stream>>>(c->d_val, c->nv, c->nk, c->nx,
                                                       static_cast<float2*>(c->d_valT));
+    kv_to_float<<<g, 256, 0, c->stream>>>(reinterpret_cast<const double*>(c->d_con), 2 * ncon,
+                                          reinterpret_cast<float*>(c->d_con32));
+    kv_to_float<<<g, 256, 0, c->stream>>>(reinterpret_cast<const double*>(c->d_val), 2 * nval,
+                                          reinterpret_cast<float*>(c->d_val32));
+  }
   else
     kv_transpose_val<double><<<g, 256, 0, c->stream>>>(c->d_val, c->nv, c->nk, c->nx,
                                                        static_cast<double2*>(c->d_valT));

@@ -154,6 +154,9 @@ void or_val_bubble_act(const or_val_dims* d, const or_val_ops* o, const double* 
                        double* outr, double* outi);
 void or_val_ladder_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi,
                        double* outr, double* outi);
+/* The direct term's part from y in [y0, y1), lad_slab = ladder(., ., y0..y1-1). */
+void or_val_ladder_slab(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, int y0,
+                        int y1, const double* lad_slab, double* outr, double* outi);
 /* OCEAN_xact valence branch + energies (OCEAN_action.f90:521-600). */
 int or_val_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, double* hr,
                double* hi, int backwards);

@@ -206,15 +206,26 @@ void or_val_bubble_act(const or_val_dims* d, const or_val_ops* o, const double* 
 // T(x, y, k) = sum_v A(x, v, k) conj(val(y, v, k));
 // T(x, y, .) = FFT_bwd[ ladder(., x, y) o FFT_fwd[ T(x, y, .) ] ] / Nk;
 // B(x, v, k) = sum_y T(x, y, k) val(y, v, k);  out += -1 sum_x conj(con) B.
+// The part of the direct term from y in [y0, y1); lad holds ladder(., ., y) for
+// those y only (lad[nk (x + nx (y - y0)) + k]).  Summing the parts over a
+// partition of the y-range gives or_val_ladder_act up to the order of the sums.
+void or_val_ladder_slab(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, int y0, int y1,
+                        const double* lad_slab, double* outr, double* outi);
+
 void or_val_ladder_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, double* outr,
                        double* outi) {
+  or_val_ladder_slab(d, o, pr, pi, 0, nx_of(d), o->ladder, outr, outi);
+}
+
+void or_val_ladder_slab(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, int y0, int y1,
+                        const double* lad_slab, double* outr, double* outi) {
   const int nv = d->nv, nk = nk_of(d), nx = nx_of(d);
   std::vector<double> ar, ai;
   val_amat(d, o, pr, pi, ar, ai);
   std::vector<double> br((size_t)nx * nv * nk, 0.0), bi((size_t)nx * nv * nk, 0.0);
   std::vector<double> tr(nk), ti(nk);
   const double inv_nk = 1.0 / (double)nk;
-  for (int y = 0; y < nx; ++y)
+  for (int y = y0; y < y1; ++y)
     for (int x = 0; x < nx; ++x) {
       for (int k = 0; k < nk; ++k) {
         double sr = 0.0, si = 0.0;
@@ -229,7 +240,7 @@ void or_val_ladder_act(const or_val_dims* d, const or_val_ops* o, const double* 
         ti[k] = si;
       }
       or_fft3d(d->kmesh, tr.data(), ti.data(), -1);
-      const double* lad = o->ladder + (size_t)nk * (x + (size_t)nx * y);
+      const double* lad = lad_slab + (size_t)nk * (x + (size_t)nx * (y - y0));
       for (int k = 0; k < nk; ++k) {
         tr[k] *= lad[k];
         ti[k] *= lad[k];

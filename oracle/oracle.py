@@ -275,10 +275,13 @@ def val_bubble(xmesh, bvec, qinb, celvol, nkpts):
 
 
 class OracleVal:
-    """Operator data of one valence workload (ValWorkload with host arrays)."""
+    """Operator data of one valence workload (ValWorkload with host arrays; the
+    ladder may be None when only slabs are timed)."""
 
     def __init__(self, w, bflag=1, lflag=1, bande=1):
         self.w = w
+        if w.ladder is None:
+            w = __import__("dataclasses").replace(w, ladder=np.zeros(1))
         self.bubble, self.ngvec = val_bubble(w.xmesh, w.bvec, w.qinb, w.celvol, w.nk)
         self._refs = [np.ascontiguousarray(a, dtype=np.float64) for a in
                       (w.er, w.ei, w.allow, w.conr, w.coni, w.valr, w.vali, self.bubble, w.ladder)]
@@ -309,3 +312,11 @@ class OracleVal:
         rc = lib().or_val_haydock(C.byref(self.d), C.byref(self.o), dptr(pr), dptr(pi), niter, dptr(ra), dptr(ia),
                                   dptr(rb), C.byref(done))
         return rc, ra, ia, rb, done.value
+
+    def ladder_slab(self, pr, pi, y0, y1, lad_slab):
+        """Direct-term contribution of y in [y0, y1) (lad_slab: ladder rows of those y)."""
+        hr, hi = np.zeros(self.w.npsi), np.zeros(self.w.npsi)
+        lib().or_val_ladder_slab(C.byref(self.d), C.byref(self.o), dptr(np.ascontiguousarray(pr, dtype=np.float64)),
+                                 dptr(np.ascontiguousarray(pi, dtype=np.float64)), int(y0), int(y1),
+                                 dptr(np.ascontiguousarray(lad_slab, dtype=np.float64)), dptr(hr), dptr(hi))
+        return hr, hi

@@ -2,8 +2,8 @@
 
 Tolerances
   * FP64 H psi vs oracle (each term alone and all together): relative 2-norm < 1e-12
-  * mixed H psi vs oracle: relative 2-norm < 1e-6 (the direct term's FP32 part
-    is a small fraction of H psi on these inputs; the term alone: < 1e-5)
+  * mixed H psi vs oracle: relative 2-norm < 1e-6 (the FP32 interaction terms
+    are a small fraction of H psi on these inputs; each term alone: < 1e-5)
   * FP64 Haydock: first 10 a_n relative < 1e-12, b_n < 1e-12
   * mixed Haydock: spectrum (Spect(0) column) relative < 1e-4
   * benchmark size (v2, states and ladder built on the device): Hermiticity
@@ -48,8 +48,8 @@ def test_apply_matches_oracle(built, name, prec):
                 err = _rel(gr + 1j * gi, orr + 1j * oi)
                 if prec == capi.OCN_PREC_FP64:
                     tol = 1e-12
-                else:
-                    tol = 1e-5 if flags == (0, 0, 1) else 1e-6
+                else:  # FP32 interaction terms: each alone to 1e-5, with the energies to 1e-6
+                    tol = 1e-5 if flags in ((0, 1, 0), (0, 0, 1)) else 1e-6
                 assert err < tol, (name, flags, back, err)
     finally:
         ctx.close()
