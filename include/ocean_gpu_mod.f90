@@ -63,6 +63,10 @@ module ocean_gpu_mod
   public :: ocn_set_bloch, ocn_lr_init, ocn_soprep, ocn_apply_H, ocn_haydock, ocn_spectrum_cf
   public :: ocn_gmres, ocn_redtrid
 
+  type, bind(C) :: ocn_val_dims
+    integer(c_int) :: nc, nv, kmesh(3), xmesh(3), precision, device
+  end type
+
   interface
     integer(c_int) function ocn_ctx_create(dims, ctx) bind(C, name="ocn_ctx_create")
       import :: c_int, c_ptr, ocn_dims
@@ -167,6 +171,60 @@ module ocean_gpu_mod
       integer(c_int), value :: n
       real(c_double), intent(in) :: real_a(0:*), real_b(0:*)
       real(c_double), intent(out) :: w(*)
+    end function
+    ! ---- valence BSE (one spin channel, resonant pairs)
+    integer(c_int) function ocn_val_create(dims, ctx) bind(C, name="ocn_val_create")
+      import :: c_int, c_ptr, ocn_val_dims
+      type(ocn_val_dims), intent(in) :: dims
+      type(c_ptr), intent(out) :: ctx
+    end function
+    integer(c_int) function ocn_val_destroy(ctx) bind(C, name="ocn_val_destroy")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function ocn_val_set_energies(ctx, re, im) bind(C, name="ocn_val_set_energies")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: re(*), im(*)
+    end function
+    integer(c_int) function ocn_val_set_allow(ctx, allow) bind(C, name="ocn_val_set_allow")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: allow(*)
+    end function
+    integer(c_int) function ocn_val_set_states(ctx, con_r, con_i, val_r, val_i) bind(C, name="ocn_val_set_states")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: con_r(*), con_i(*), val_r(*), val_i(*)
+    end function
+    integer(c_int) function ocn_val_set_bubble(ctx, bubble) bind(C, name="ocn_val_set_bubble")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: bubble(*)
+    end function
+    integer(c_int) function ocn_val_set_ladder(ctx, ladder) bind(C, name="ocn_val_set_ladder")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: ladder(*)
+    end function
+    integer(c_int) function ocn_val_apply_H(ctx, in_r, in_i, out_r, out_i, flags, backwards) &
+        bind(C, name="ocn_val_apply_H")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: in_r(*), in_i(*)
+      real(c_double), intent(out) :: out_r(*), out_i(*)
+      integer(c_int), intent(in) :: flags(3)
+      integer(c_int), value :: backwards
+    end function
+    integer(c_int) function ocn_val_haydock(ctx, psi0_r, psi0_i, niter, flags, real_a, imag_a, real_b, &
+        niter_done) bind(C, name="ocn_val_haydock")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: psi0_r(*), psi0_i(*)
+      integer(c_int), value :: niter
+      integer(c_int), intent(in) :: flags(3)
+      real(c_double), intent(out) :: real_a(0:*), imag_a(0:*), real_b(0:*)
+      integer(c_int), intent(out) :: niter_done
     end function
   end interface
 end module ocean_gpu_mod
