@@ -61,6 +61,10 @@ def parse():
     ap.add_argument("--valence-steps", type=int, default=40,
                     help="Lanczos steps of the valence BSE leg (8^3 k, 10^3 x, 8+4 bands; exchange + screened "
                          "direct), both precisions, with the oracle timed on a y-slab; 0 = off")
+    ap.add_argument("--valence-xmesh", type=int, default=10,
+                    help="x-mesh extent n (n^3 points) of the valence leg (10 = the v2 case)")
+    ap.add_argument("--valence-only", action="store_true",
+                    help="run the valence leg alone and print its JSON object (profiling)")
     ap.add_argument("--batch", type=int, default=64,
                     help="instances of the batched uneven-Haydock leg (3 polarisations each); 0 = off")
     ap.add_argument("--adjoint-omega", type=int, default=400,
@@ -330,7 +334,8 @@ def run_valence(args, torch, capi, WL, local):
     import oracle as O
 
     dev = f"cuda:{local}"
-    w = WL.make_val("v2", seed=0, device=dev)
+    xm = args.valence_xmesh
+    w = WL.make_val("v2", seed=0, device=dev, xmesh=(xm, xm, xm))
     niter = args.valence_steps
     nk, nx, nv = w.nk, w.nx, w.nv
     out = {"workload": f"v2: k-mesh {'x'.join(map(str, w.kmesh))}, x-mesh {'x'.join(map(str, w.xmesh))}, "
@@ -815,6 +820,15 @@ def main():
     ws, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, ws, rank, pg)
+    elif args.valence_only:
+        import torch
+
+        from ocean_gb300 import capi
+        from ocean_gb300 import workloads as WL
+
+        capi.load()
+        if rank == 0:
+            print(json.dumps({"valence": run_valence(args, torch, capi, WL, local)}), flush=True)
     else:
         run_ours(args, ws, rank, local, pg)
     if pg is not None:
