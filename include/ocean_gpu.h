@@ -572,6 +572,30 @@ int ocn_val_haydock(ocn_val_ctx* ctx, const double* psi0_r, const double* psi0_i
 int ocn_val_haydock_dev(ocn_val_ctx* ctx, const double* d_psi0, int niter, const int flags[3], double* real_a,
                         double* imag_a, double* real_b, int* niter_done);
 
+/* write_val (OCEAN_haydock.f90:1706-1799), the spectrum of a valence run
+ * (haydump's 'VAL'/'RXS' branch, file "opcons"): ne rows at the midpoints
+ * el + (eh - el)(2r+1)/(2 ne) (Hartree), each 8 values
+ *   omega (eV), eps1, eps2, Re(n) - 1, Im(n), mu (1/cm), R, epsinv
+ * with eps = 1 - fact/al [- fact/be when semi_tda], fact = kpref (2/val_ham_spin)
+ * ucvol (integer division), al/be the resonant / anti-resonant continued
+ * fractions with the square-root terminator at the real energy, backf: z and
+ * the energy squared (the backward-pair form).  imag_a/imag_b/real_c/imag_c may
+ * be NULL (Hermitian run: c = b, imaginary parts 0).  Evaluated on the GPU,
+ * FP64.  out: ne * 8. */
+typedef struct {
+  double kpref, ucvol;
+  double el, eh, gam0;  /* Hartree */
+  int ne, val_ham_spin, semi_tda, backf;
+} ocn_val_cf_params;
+
+int ocn_val_spectrum(const double* real_a, const double* imag_a, const double* real_b, const double* imag_b,
+                     const double* real_c, const double* imag_c, int iter, const ocn_val_cf_params* p, double* out);
+/* write_val's optical constants (:1778-1795) for given eps at energies omega
+ * (Hartree); out: n * 8 in the column order above.  Host only. */
+int ocn_val_optical_constants(int n, const double* omega, const double* eps_re, const double* eps_im, double* out);
+/* The "opcons" file write_val writes: its header and '(8(1E24.16,1X))' rows. */
+int ocn_write_opcons(const char* path, int ne, const double* rows);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,6 +89,7 @@ EXPORTS = [
     "ocn_val_set_energies", "ocn_val_set_allow", "ocn_val_set_states", "ocn_val_set_states_dev",
     "ocn_val_set_bubble", "ocn_val_set_ladder", "ocn_val_set_ladder_dev", "ocn_val_bubble_populate",
     "ocn_val_apply_H", "ocn_val_apply_H_dev", "ocn_val_haydock", "ocn_val_haydock_dev",
+    "ocn_val_spectrum", "ocn_val_optical_constants", "ocn_write_opcons",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -741,3 +742,34 @@ class ValContext:
         self._chk(self.lib.ocn_val_haydock_dev(self.ptr, C.c_void_p(d_psi0), niter, (C.c_int * 3)(*flags),
                                                _dp(ra), _dp(ia), _dp(rb), C.byref(done)))
         return ra, ia, rb, done.value
+
+
+class OcnValCfParams(C.Structure):
+    _fields_ = [("kpref", C.c_double), ("ucvol", C.c_double), ("el", C.c_double), ("eh", C.c_double),
+                ("gam0", C.c_double), ("ne", C.c_int), ("val_ham_spin", C.c_int), ("semi_tda", C.c_int),
+                ("backf", C.c_int)]
+
+
+def val_spectrum(ra, ia, rb, iteration: int, kpref: float, ucvol: float, el: float, eh: float, ne: int,
+                 gam0: float, val_ham_spin: int = 1, semi_tda: bool = False, backf: bool = False,
+                 ib=None, rc=None, ic=None):
+    """write_val rows (ne x 8: omega eV, eps1, eps2, Re n - 1, Im n, mu, R, epsinv) on the GPU."""
+    p = OcnValCfParams(kpref, ucvol, el, eh, gam0, ne, val_ham_spin, int(bool(semi_tda)), int(bool(backf)))
+    out = np.zeros(ne * 8)
+    opt = [None if a is None else _f64(a) for a in (ia, ib, rc, ic)]
+    ptr = [None if a is None else _dp(a) for a in opt]
+    check(load().ocn_val_spectrum(_dp(_f64(ra)), ptr[0], _dp(_f64(rb)), ptr[1], ptr[2], ptr[3], int(iteration),
+                                  C.byref(p), _dp(out)))
+    return out.reshape(ne, 8)
+
+
+def val_optical_constants(omega_ha, eps_re, eps_im):
+    om, er, ei = _f64(omega_ha), _f64(eps_re), _f64(eps_im)
+    out = np.zeros(len(om) * 8)
+    check(load().ocn_val_optical_constants(len(om), _dp(om), _dp(er), _dp(ei), _dp(out)))
+    return out.reshape(len(om), 8)
+
+
+def write_opcons(path: str, rows):
+    r = _f64(np.asarray(rows).reshape(-1))
+    check(load().ocn_write_opcons(path.encode(), len(r) // 8, _dp(r)))

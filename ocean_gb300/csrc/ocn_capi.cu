@@ -1221,6 +1221,22 @@ int ocn_spectrum_cf_bc(const double* real_a, const double* imag_a, const double*
   return rc;
 }
 
+int ocn_val_spectrum(const double* real_a, const double* imag_a, const double* real_b, const double* imag_b,
+                     const double* real_c, const double* imag_c, int iter, const ocn_val_cf_params* p, double* out) {
+  if (!real_a || !real_b || !p || !out) return set_err(nullptr, OCN_ERR_ARG, "null argument");
+  std::string err;
+  int rc = val_spectrum_eval(real_a, imag_a, real_b, imag_b, real_c, imag_c, iter, p, out, &err);
+  if (rc) set_err(nullptr, rc, err);
+  return rc;
+}
+
+int ocn_val_optical_constants(int n, const double* omega, const double* eps_re, const double* eps_im, double* out) {
+  if (n < 0 || (n > 0 && (!omega || !eps_re || !eps_im || !out)))
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_val_optical_constants: bad argument");
+  for (int i = 0; i < n; ++i) val_optical_host(omega[i], eps_re[i], eps_im[i], out + 8 * (size_t)i);
+  return OCN_OK;
+}
+
 int ocn_spectrum_cf(const double* real_a, const double* imag_a, const double* real_b, int iter,
                     double kpref, const ocn_cf_params* p, double* out) {
   if (!real_a || !real_b || !p || !out) return set_err(nullptr, OCN_ERR_ARG, "null argument");

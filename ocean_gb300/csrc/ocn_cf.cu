@@ -149,7 +149,139 @@ __global__ void k_cf_points(const double* __restrict__ ra, const double* __restr
   sk[i] = prefactor * kpref * dr / (dr * dr + di * di);
 }
 
+// ---- write_val (OCEAN_haydock.f90:1706-1799): the valence dielectric function
+
+constexpr double kAlphaInv = 137.035999177;
+
+__host__ __device__ inline void csqrt_hd(double x, double y, double* rx, double* ry) {
+  if (x == 0.0 && y == 0.0) {
+    *rx = 0.0;
+    *ry = y;
+    return;
+  }
+  const double t = sqrt((fabs(x) + sqrt(x * x + y * y)) * 0.5);
+  if (x >= 0.0) {
+    *rx = t;
+    *ry = y / (2.0 * t);
+  } else {
+    *rx = fabs(y) / (2.0 * t);
+    *ry = copysign(t, y);
+  }
+}
+
+// The optical constants write_val prints for one energy (Hartree) and eps
+// (:1778-1795): omega (eV), eps1, eps2, Re(n) - 1, Im(n), mu (1/cm), R, epsinv,
+// n = sqrt(eps) (principal), R = |(n-1)/(n+1)|^2, mu = 2 omega Im(n) / (bohr
+// alphainv 1000), epsinv = Im(eps) / |eps|^2.
+__host__ __device__ inline void val_optical(double ere, double er, double ei, double* o) {
+  const double lossf = ei / (er * er + ei * ei);
+  double nr, ni;
+  csqrt_hd(er, ei, &nr, &ni);
+  const double ar = nr - 1.0, br = nr + 1.0;
+  const double reflct = (ar * ar + ni * ni) / (br * br + ni * ni);
+  const double mu = 2.0 * ere * kHa2eV * ni / (kBohr * kAlphaInv * 1000.0);
+  o[0] = ere * kHa2eV;
+  o[1] = er;
+  o[2] = ei;
+  o[3] = nr - 1.0;
+  o[4] = ni;
+  o[5] = mu;
+  o[6] = reflct;
+  o[7] = lossf;
+}
+
+// b_j c_j as write_val forms it: cmplx(real_b, imag_b, DP) * cmplx(real_c, -imag_c, DP),
+// FP64 (c = b real in the Hermitian run).
+__device__ __forceinline__ cplx bc_val(const double* __restrict__ rb, const BcArrays& q, int j) {
+  const double a = rb[j], b = q.ib ? q.ib[j] : 0.0;
+  const double c = q.rc ? q.rc[j] : a, d = q.ic ? -q.ic[j] : 0.0;
+  return {a * c - b * d, a * d + b * c};
+}
+
+// One output row per thread: energies at the midpoints el + (eh - el)(2r+1)/(2 ne),
+// the square-root terminator at the real energy, the resonant (al) and
+// anti-resonant (be) fractions, eps = 1 - fact/al (- fact/be with semiTDA).
+__global__ void k_write_val(const double* __restrict__ ra, const double* __restrict__ ia,
+                            const double* __restrict__ rb, const BcArrays q, int iter, double fact, double el,
+                            double eh, int ne, double gam0, int semi_tda, int backf, double* __restrict__ out) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= ne) return;
+  const int ie = 2 * row + 1;
+  double ere = el + (eh - el) * (double)ie / (double)(2 * ne);
+  cplx ct = {ere, gam0};
+  if (backf) {
+    ct = {ct.x * ct.x - ct.y * ct.y, ct.x * ct.y + ct.y * ct.x};
+    ere = ere * ere;
+  }
+  const double an = ra[iter - 1];
+  double sx, sy;
+  csqrt_hd((ere - an) * (ere - an) - 4.0 * rb[iter] * rb[iter], 0.0, &sx, &sy);
+  const cplx rp = {0.5 * (ere - an + sx), 0.5 * sy};
+  const cplx rm = {0.5 * (ere - an - sx), 0.5 * (-sy)};
+  const cplx rrr = rp.y < 0.0 ? rp : rm;
+  cplx al = {ct.x - an - rrr.x, ct.y - rrr.y};
+  cplx be = {-ct.x - an - rrr.x, -ct.y - rrr.y};
+  for (int i = iter - 1; i >= 0; --i) {
+    const double ai = ia ? ia[i] : 0.0;
+    const cplx bc = bc_val(rb, q, i + 1);
+    const cplx qa = cdiv_smith(bc, al), qb = cdiv_smith(bc, be);
+    al = {ct.x - ra[i] - qa.x, ct.y - ai - qa.y};
+    be = {-ct.x - ra[i] - qb.x, -ct.y - ai - qb.y};
+  }
+  const cplx fa = cdiv_smith({fact, 0.0}, al);
+  cplx eps = {1.0 - fa.x, -fa.y};
+  if (semi_tda) {
+    const cplx fb = cdiv_smith({fact, 0.0}, be);
+    eps = {eps.x - fb.x, eps.y - fb.y};
+  }
+  if (backf) ere = sqrt(ere);
+  val_optical(ere, eps.x, eps.y, out + 8 * (size_t)row);
+}
+
 }  // namespace
+
+void val_optical_host(double ere, double er, double ei, double* o) { val_optical(ere, er, ei, o); }
+
+int val_spectrum_eval(const double* ra, const double* ia, const double* rb, const double* ib, const double* rc,
+                      const double* ic, int iter, const ocn_val_cf_params* p, double* out, std::string* err) {
+  if (iter < 1 || p->ne < 1 || (p->val_ham_spin != 1 && p->val_ham_spin != 2)) {
+    if (err) *err = "ocn_val_spectrum: iter and ne must be >= 1, val_ham_spin 1 or 2";
+    return OCN_ERR_ARG;
+  }
+  const size_t nco = (size_t)iter + 1;
+  std::vector<void*> owned;
+  cudaError_t e = cudaSuccess;
+  auto dup = [&](const double* h) -> double* {
+    if (!h) return nullptr;
+    void* q = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&q, nco * sizeof(double));
+    if (e != cudaSuccess) return nullptr;
+    owned.push_back(q);
+    e = cudaMemcpy(q, h, nco * sizeof(double), cudaMemcpyHostToDevice);
+    return static_cast<double*>(q);
+  };
+  double* d_ra = dup(ra);
+  double* d_ia = dup(ia);
+  double* d_rb = dup(rb);
+  BcArrays dq{dup(ib), dup(rc), dup(ic)};
+  double* d_out = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&d_out), (size_t)p->ne * 8 * sizeof(double));
+  if (e == cudaSuccess) {
+    owned.push_back(d_out);
+    // fact = kpref * real(2 / val_ham_spin, DP) * ucvol (integer division, :1715)
+    const double fact = p->kpref * (double)(2 / p->val_ham_spin) * p->ucvol;
+    k_write_val<<<(p->ne + 63) / 64, 64>>>(d_ra, d_ia, d_rb, dq, iter, fact, p->el, p->eh, p->ne, p->gam0,
+                                          p->semi_tda, p->backf, d_out);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d_out, (size_t)p->ne * 8 * sizeof(double), cudaMemcpyDeviceToHost);
+  for (void* q : owned) cudaFree(q);
+  if (e != cudaSuccess) {
+    if (err) *err = std::string("ocn_val_spectrum: ") + cudaGetErrorString(e);
+    return OCN_ERR_CUDA;
+  }
+  return OCN_OK;
+}
 
 int cf_eval(const double* ra, const double* ia, const double* rb, int iter, double kpref,
             const ocn_cf_params* p, double* out, std::string* err, const double* ib, const double* rc,

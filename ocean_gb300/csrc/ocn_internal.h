@@ -301,6 +301,9 @@ int vec_fill(ocn_ctx* c, double* x, double vr, double vi);
 int cf_eval(const double* ra, const double* ia, const double* rb, int iter, double kpref,
             const ocn_cf_params* p, double* out, std::string* err,
             const double* ib = nullptr, const double* rc = nullptr, const double* ic = nullptr);
+int val_spectrum_eval(const double* ra, const double* ia, const double* rb, const double* ib, const double* rc,
+                      const double* ic, int iter, const ocn_val_cf_params* p, double* out, std::string* err);
+void val_optical_host(double ere, double er, double ei, double* o);
 int cf_eval_noalloc(const double* ra, const double* ia, const double* rb, int iter, double kpref,
                     const ocn_cf_params* p, double* out, std::string* err);
 

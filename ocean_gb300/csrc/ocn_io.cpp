@@ -396,6 +396,23 @@ int ocn_write_absspct(const char* path, int iter, double gam0, double kpref, dou
   return close_out(f, path);
 }
 
+int ocn_write_opcons(const char* path, int ne, const double* rows) {
+  if (ne < 0 || (ne > 0 && !rows)) return set_err(nullptr, OCN_ERR_ARG, "ocn_write_opcons: bad argument");
+  FILE* f;
+  int rc = open_out(path, &f);
+  if (rc) return rc;
+  // write_val (OCEAN_haydock.f90:1717-1719,1797): "(a)" header, '(8(1E24.16,1X))' rows
+  put(f, "#   omega (eV)      epsilon_1       epsilon_2       n               kappa           mu (cm^(-1))    R"
+         "               epsinv");
+  std::string line;
+  for (int r = 0; r < ne; ++r) {
+    line.clear();
+    for (int j = 0; j < 8; ++j) line += (j ? " " : "") + fmt_e(rows[(size_t)r * 8 + j], 24, 16);
+    put(f, line);  // the trailing 1x of the last item writes nothing
+  }
+  return close_out(f, path);
+}
+
 int ocn_write_abs_gmres(const char* path, int nomega, const double* energies_ev, const double* out_re,
                         const double* out_im, const double* rel_err, const int* iters) {
   if (nomega < 0 || !energies_ev || !out_re || !out_im || !rel_err || !iters)

@@ -885,6 +885,59 @@ int or_write_core_bc(const double* ra, const double* ia, const double* rb, const
   return 0;
 }
 
+// write_val, OCEAN_haydock.f90:1706-1799: the valence dielectric function and
+// optical constants, ne rows of (omega eV, eps1, eps2, Re n - 1, Im n, mu, R,
+// epsinv).  b_j c_j = cmplx(real_b, imag_b, DP) * cmplx(real_c, -imag_c, DP).
+int or_write_val(const double* ra, const double* ia, const double* rb, const double* ib, const double* rc,
+                 const double* ic, int iter, double kpref, double ucvol, int val_ham_spin, int semi_tda, int backf,
+                 double el, double eh, int ne, double gam0, double* out) {
+  if (iter < 1 || ne < 1 || (val_ham_spin != 1 && val_ham_spin != 2)) return -1;
+  const double h2e = 27.211386245980, bohr = 0.529177210544, alphainv = 137.035999177;
+  const double fact = kpref * (double)(2 / val_ham_spin) * ucvol;
+  for (int r = 0; r < ne; ++r) {
+    const int ie = 2 * r + 1;
+    double ere = el + (eh - el) * (double)ie / (double)(2 * ne);
+    cd ctmp(ere, gam0);
+    if (backf) {
+      ctmp = cmul(ctmp, ctmp);
+      ere = ere * ere;
+    }
+    const double an = ra[iter - 1];
+    const cd arg = csqrt_p(cd((ere - an) * (ere - an) - 4.0 * rb[iter] * rb[iter], 0.0));
+    const cd rp = (cd(ere - an, 0.0) + arg) * 0.5;
+    const cd rm = (cd(ere - an, 0.0) - arg) * 0.5;
+    const cd rrr = rp.imag() < 0.0 ? rp : rm;
+    cd al = ctmp - an - rrr;
+    cd be = -ctmp - an - rrr;
+    for (int i = iter - 1; i >= 0; --i) {
+      const double a = rb[i + 1], b = ib ? ib[i + 1] : 0.0;
+      const double c = rc ? rc[i + 1] : a, dd = ic ? -ic[i + 1] : 0.0;
+      const cd bc(a * c - b * dd, a * dd + b * c);
+      const cd ai(ra[i], ia ? ia[i] : 0.0);
+      al = ctmp - ai - cdiv(bc, al);
+      be = -ctmp - ai - cdiv(bc, be);
+    }
+    cd eps = cd(1.0, 0.0) - cdiv(cd(fact, 0.0), al);
+    if (semi_tda) eps -= cdiv(cd(fact, 0.0), be);
+    if (backf) ere = std::sqrt(ere);
+    const double reeps = eps.real(), imeps = eps.imag();
+    const double lossf = imeps / (reeps * reeps + imeps * imeps);
+    const cd refrac = csqrt_p(eps);
+    const double reflct = std::norm(cdiv(refrac - 1.0, refrac + 1.0));
+    const double mu = 2.0 * ere * h2e * refrac.imag() / (bohr * alphainv * 1000.0);
+    double* o = out + 8 * (size_t)r;
+    o[0] = ere * h2e;
+    o[1] = reeps;
+    o[2] = imeps;
+    o[3] = refrac.real() - 1.0;
+    o[4] = refrac.imag();
+    o[5] = mu;
+    o[6] = reflct;
+    o[7] = lossf;
+  }
+  return 0;
+}
+
 // calc_spect_core, OCEAN_haydock.f90:1991-2027.
 int or_calc_spect_core(const double* ra, const double* ia, const double* rb, int iter, double kpref,
                        double el, double eh, int ne, double gam0, double ebase, double* out) {

@@ -107,6 +107,10 @@ int or_write_core(const double* real_a, const double* imag_a, const double* real
 int or_write_core_bc(const double* real_a, const double* imag_a, const double* real_b, const double* imag_b,
                      const double* real_c, const double* imag_c, int iter, double kpref, double el, double eh,
                      int ne, double gam0, double ebase, double ucvol, double* out);
+/* write_val (OCEAN_haydock.f90:1706-1799). out ne*8. */
+int or_write_val(const double* real_a, const double* imag_a, const double* real_b, const double* imag_b,
+                 const double* real_c, const double* imag_c, int iter, double kpref, double ucvol, int val_ham_spin,
+                 int semi_tda, int backf, double el, double eh, int ne, double gam0, double* out);
 /* calc_spect_core (OCEAN_haydock.f90:1991-2027). out ne*3. */
 int or_calc_spect_core(const double* real_a, const double* imag_a, const double* real_b, int iter,
                        double kpref, double el, double eh, int ne, double gam0, double ebase,

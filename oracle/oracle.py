@@ -219,6 +219,19 @@ def write_core_bc(ra, ia, rb, ib, rc, ic, it, kpref, el, eh, ne, gam0, ebase=0.0
     return out.reshape(ne + 1, 9)
 
 
+def write_val(ra, ia, rb, it, kpref, ucvol, el, eh, ne, gam0, val_ham_spin=1, semi_tda=False, backf=False,
+              ib=None, rc=None, ic=None):
+    """write_val rows (ne x 8) of a valence run."""
+    out = np.zeros(ne * 8)
+    arr = [None if x is None else dptr(np.ascontiguousarray(x, dtype=np.float64)) for x in (ia, ib, rc, ic)]
+    rc_ = lib().or_write_val(dptr(np.ascontiguousarray(ra, dtype=np.float64)), arr[0],
+                             dptr(np.ascontiguousarray(rb, dtype=np.float64)), arr[1], arr[2], arr[3], it,
+                             C.c_double(kpref), C.c_double(ucvol), val_ham_spin, int(bool(semi_tda)),
+                             int(bool(backf)), C.c_double(el), C.c_double(eh), ne, C.c_double(gam0), dptr(out))
+    assert rc_ == 0
+    return out.reshape(ne, 8)
+
+
 def redtrid(n, ra, rb):
     w = np.zeros(n + 1)
     rc = lib().or_redtrid(n, dptr(np.ascontiguousarray(ra, dtype=np.float64)),

@@ -127,3 +127,48 @@ def test_benchmark_size_is_hermitian_and_linear(built, prec):
         assert torch.isfinite(hz).all()
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("semi_tda,backf,cplx", [(False, False, False), (True, False, False), (True, True, False),
+                                                 (False, False, True)])
+def test_val_spectrum_matches_oracle(built, semi_tda, backf, cplx):
+    """write_val on the GPU against the oracle: 1e-13 relative per column."""
+    _, O = built
+    rng = np.random.default_rng(21)
+    n = 60
+    ra = rng.uniform(0.1, 0.9, n + 1)
+    rb = np.concatenate([[0.0], rng.uniform(0.02, 0.2, n)])
+    ia = ib = rc = ic = None
+    if cplx:
+        ia = rng.uniform(-0.01, 0.01, n + 1)
+        ib = rng.uniform(-0.02, 0.02, n + 1)
+        rc = rb * rng.uniform(0.9, 1.1, n + 1)
+        ic = rng.uniform(-0.02, 0.02, n + 1)
+    args = (n, 0.7, 270.0, 0.0, 1.3, 500, 0.01)
+    g = capi.val_spectrum(ra, ia, rb, *args, val_ham_spin=1, semi_tda=semi_tda, backf=backf, ib=ib, rc=rc, ic=ic)
+    o = O.write_val(ra, ia, rb, *args, 1, semi_tda, backf, ib=ib, rc=rc, ic=ic)
+    for j in range(8):
+        err = np.abs(g[:, j] - o[:, j]) / np.maximum(np.abs(o[:, j]), 1e-300)
+        assert np.max(err) < 1e-13, (j, np.max(err))
+
+
+@pytest.mark.parametrize("prec", [capi.OCN_PREC_FP64, capi.OCN_PREC_MIXED])
+def test_valence_haydock_spectrum_end_to_end(built, prec):
+    """Haydock over the valence action, then write_val: GPU against the oracle's
+    whole run (eps2 column, relative 2-norm 1e-10 FP64, 1e-4 mixed)."""
+    _, O = built
+    w = WL.make_val("vsmall", seed=23)
+    ctx = capi.ValContext(w, precision=prec)
+    try:
+        niter = 30
+        ra, ia, rb, done = ctx.haydock(niter)
+    finally:
+        ctx.close()
+    P = O.OracleVal(w)
+    rc, ora, oia, orb, _ = P.haydock(niter)
+    assert rc == 0 and done == niter
+    args = (niter, w.kpref, w.celvol, w.el, w.eh, 400, w.gam0)
+    g = capi.val_spectrum(ra, ia, rb, *args, semi_tda=True)
+    o = O.write_val(ora, oia, orb, *args, 1, True)
+    err = np.linalg.norm(g[:, 2] - o[:, 2]) / np.linalg.norm(o[:, 2])
+    assert err < (1e-10 if prec == capi.OCN_PREC_FP64 else 1e-4), err

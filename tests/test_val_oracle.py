@@ -101,3 +101,76 @@ def test_val_create_rejects_bad_dims_without_gpu(lib_built):
     p = C.c_void_p()
     assert lib.ocn_val_create(C.byref(d), C.byref(p)) == capi.OCN_ERR_ARG
     assert "mesh" in capi.val_last_error()
+
+
+# ---- write_val (the valence spectrum, file "opcons") against EXAMPLE/Si_valence
+
+# EXAMPLE/Si_valence/opcons: 2000 rows, spect_range {2000 0 20} eV (Si.in); the
+# fixture keeps every OPCONS_STRIDE-th row (tests/golden/make_opcons_fixture.py)
+OPCONS_STRIDE = 5
+OPCONS_NE = 2000
+
+
+def _opcons_rows():
+    import os
+
+    from conftest import ROOT
+
+    path = os.path.join(ROOT, "tests", "golden", "opcons_Si_valence_rows.txt")
+    return [l.rstrip("\n") for l in open(path)]
+
+
+def test_opcons_grid_and_optical_constants_match_the_reference(lib_built):
+    capi.load(lib_built)
+    lines = _opcons_rows()
+    vals = np.array([[float(x) for x in l.split()] for l in lines[1:]])
+    ne = OPCONS_NE
+    rows = np.arange(0, ne, OPCONS_STRIDE)
+    assert len(vals) == len(rows)
+    el, eh = 0.0 * WL.EV2HARTREE, 20.0 * WL.EV2HARTREE
+    omega = el + (eh - el) * (2 * rows + 1) / (2 * ne)
+    out = capi.val_optical_constants(omega, vals[:, 1], vals[:, 2])
+    # the energy grid (midpoints) and the columns that are pure functions of eps
+    assert np.max(np.abs(out[:, 0] - vals[:, 0]) / vals[:, 0]) < 1e-13
+    for j in (3, 4, 6, 7):
+        ref = vals[:, j]
+        err = np.abs(out[:, j] - ref) / np.maximum(np.abs(ref), 1e-300)
+        assert np.max(err) < 1e-13, (j, np.max(err))
+    # mu carries the physical constants, which the file's OCEAN version rounded
+    # differently (5e-11 relative)
+    nz = vals[:, 5] != 0
+    assert np.max(np.abs(out[nz, 5] - vals[nz, 5]) / np.abs(vals[nz, 5])) < 1e-9
+
+
+def test_opcons_writer_is_byte_identical(lib_built, tmp_path):
+    capi.load(lib_built)
+    lines = _opcons_rows()
+    vals = np.array([[float(x) for x in l.split()] for l in lines[1:]])
+    path = str(tmp_path / "opcons")
+    capi.write_opcons(path, vals)
+    assert open(path).read().splitlines() == lines
+
+
+@pytest.mark.parametrize("semi_tda", [False, True])
+def test_oracle_write_val_is_the_resolvent(oracle_lib, semi_tda):
+    """With a vanishing last b the terminator drops out and eps is
+    1 - fact [G(z) (+ G'(-z))] of the tridiagonal matrix (dense solve)."""
+    O = oracle_lib
+    rng = np.random.default_rng(8)
+    n = 30
+    ra = np.concatenate([rng.uniform(0.1, 0.9, n), [0.0]])
+    rb = np.concatenate([[0.0], rng.uniform(0.02, 0.1, n - 1), [1e-12]])
+    kpref, ucvol, gam0, ne = 0.7, 270.0, 0.01, 50
+    el, eh = 0.05, 1.2
+    out = O.write_val(ra, None, rb, n, kpref, ucvol, el, eh, ne, gam0, 1, semi_tda)
+    T = np.diag(ra[:n]) + np.diag(rb[1:n], 1) + np.diag(rb[1:n], -1)
+    fact = kpref * 2 * ucvol
+    e1 = np.zeros(n)
+    e1[0] = 1.0
+    for r in range(ne):
+        om = el + (eh - el) * (2 * r + 1) / (2 * ne)
+        z = om + 1j * gam0
+        eps = 1.0 - fact * np.linalg.solve(z * np.eye(n) - T, e1)[0]
+        if semi_tda:
+            eps -= fact * np.linalg.solve(-z * np.eye(n) - T, e1)[0]
+        assert abs(out[r, 1] + 1j * out[r, 2] - eps) < 1e-9 * abs(eps), r
