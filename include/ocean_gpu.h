@@ -504,17 +504,20 @@ int ocn_timing_reset(ocn_ctx* ctx);
 int ocn_timing_read(ocn_ctx* ctx, long long counts[6], double ms[6]);
 
 /* ------------------------------------------------------- valence BSE
- * The valence branch of OCEAN_xact (OCEAN_action.f90:521-600) for one spin
- * channel (valence_ham_spin = 1, nspn = 1) and resonant pairs (nbw = 1):
+ * The valence branch of OCEAN_xact (OCEAN_action.f90:521-600) for resonant
+ * pairs (nbw = 1), valence_ham_spin 1 or 2 and one or two DFT spins:
  *   H psi = E o psi + allow o [ 2 X(allow o psi) - D(allow o psi) ]
  * X: AI_bubble_act (OCEAN_bubble.f90:420-796); D: OCEAN_ladder_act_single
  * (OCEAN_ladder.f90:155-1004).  Replaces those routines and the module state
  * they read (re/im_con, re/im_val of OCEAN_val_states, p_energy and allow of
  * OCEAN_energies, bubble of OCEAN_bubble, ladder of OCEAN_ladder).
  * Layouts are the reference's Fortran orders:
- *   psi, energies, allow  (Nc, Nv, Nk)   psi%valr / valr(c, v, k)
- *   con                   (Nx, Nc, Nk)   re_con / im_con(x, c, k)
- *   val                   (Nx, Nv, Nk)   re_val / im_val(x, v, k)
+ *   psi, energies, allow  (Nc, Nv, Nk, vspin^2)  psi%valr(c, v, k, ibeta)
+ *   con                   (Nx, Nc, Nk, nspn)     re_con / im_con(x, c, k, spin)
+ *   val                   (Nx, Nv, Nk, nspn)     re_val / im_val(x, v, k, spin)
+ * ibeta = (i - 1) vspin + j pairs valence spin i with conduction spin j
+ * (OCEAN_ladder.f90:118-133); the exchange couples the same-spin blocks
+ * (OCEAN_bubble.f90:509-760, spin_prefac 2 for one spin, 1 for two).
  *   bubble                (Nx)
  *   ladder                (Nk, Nx, Nx)   ladder(k, x, y) after resort_ladder
  * with the flat k index k3 fastest and the flat x index x3 fastest (the FFT
@@ -530,6 +533,8 @@ typedef struct {
   int xmesh[3];   /* x-mesh of the states, bubble and ladder (each 1..32) */
   int precision;  /* OCN_PREC_FP64 or OCN_PREC_MIXED */
   int device;     /* CUDA device ordinal */
+  int nspn;       /* DFT spins of con/val: 1 (0 reads as 1) or 2 */
+  int vspin;      /* valence_ham_spin: 1 (0 reads as 1) or 2 */
 } ocn_val_dims;
 
 int ocn_val_create(const ocn_val_dims* dims, ocn_val_ctx** out);

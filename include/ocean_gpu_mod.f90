@@ -64,7 +64,7 @@ module ocean_gpu_mod
   public :: ocn_gmres, ocn_redtrid
 
   type, bind(C) :: ocn_val_dims
-    integer(c_int) :: nc, nv, kmesh(3), xmesh(3), precision, device
+    integer(c_int) :: nc, nv, kmesh(3), xmesh(3), precision, device, nspn, vspin
   end type
 
   interface

@@ -635,7 +635,7 @@ def pnorm(pr, pi, nkpts: int, celvol: float):
 
 class OcnValDims(C.Structure):
     _fields_ = [("nc", C.c_int), ("nv", C.c_int), ("kmesh", C.c_int * 3), ("xmesh", C.c_int * 3),
-                ("precision", C.c_int), ("device", C.c_int)]
+                ("precision", C.c_int), ("device", C.c_int), ("nspn", C.c_int), ("vspin", C.c_int)]
 
 
 def val_last_error(ctx=None) -> str:
@@ -670,6 +670,8 @@ class ValContext:
         d.xmesh[:] = list(w.xmesh)
         d.precision = precision
         d.device = device
+        d.nspn = getattr(w, "nspn", 1)
+        d.vspin = getattr(w, "vspin", 1)
         self.ptr = C.c_void_p()
         rc = lib.ocn_val_create(C.byref(d), C.byref(self.ptr))
         if rc != 0:

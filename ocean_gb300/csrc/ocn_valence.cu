@@ -4,8 +4,8 @@
 //
 // X: exchange ("bubble", OCEAN2/OCEAN_bubble.f90:420-796); D: screened direct
 // ("ladder", OCEAN2/OCEAN_ladder.f90:155-1004); order of OCEAN_xact's valence
-// branch (OCEAN2/OCEAN_action.f90:521-600).  One spin channel
-// (valence_ham_spin = 1) and resonant pairs (nbw = 1).
+// branch (OCEAN2/OCEAN_action.f90:521-600).  valence_ham_spin 1 or 2 (psi in 1
+// or 4 spin blocks), one or two DFT spins, resonant pairs (nbw = 1).
 //
 // Both terms start from A(x,v,k) = sum_c con(x,c,k) psi(c,v,k) and end with
 // out(c,v,k) = sum_x conj(con(x,c,k)) M(x,v,k), so one kernel builds A (and the
@@ -57,7 +57,9 @@ struct ocn_val_ctx {
   size_t smem_optin = 0;
   ocn_val_dims dims{};
   int nc = 0, nv = 0, nk = 0, nx = 0;
-  size_t npsi = 0;
+  int nspn = 1, vspin = 1;  // DFT spins of the states; valence_ham_spin (vspin^2 psi blocks)
+  size_t npsi = 0;          // all blocks
+  size_t nb1 = 0;           // one block: Nc Nv Nk
   int mixed = 0;
   bool have_e = false, have_allow = false, have_states = false, have_bubble = false, have_ladder = false;
   bool ei_nonzero = false;
@@ -563,8 +565,8 @@ __global__ void __launch_bounds__(VAL_THREADS, sizeof(R) == 4 ? (X == 1 ? 4 : 3)
 }
 
 // out(c,v,k) = E o psi (conj E when backwards) + allow o sum_x conj(con(x,c,k))
-// M(x,v,k), M = 2 s(x) val(x,v,k) - sum_ys B_ys(x,v,k) (OCEAN_bubble.f90:742-757
-// with spin_prefac 2, OCEAN_ladder.f90:900-911 with -1, OCEAN_energies.f90:890-906).
+// M(x,v,k), M = xpref s(x) val(x,v,k) - sum_ys B_ys(x,v,k) (OCEAN_bubble.f90:742-757
+// with xpref = spin_prefac, OCEAN_ladder.f90:900-911 with -1, OCEAN_energies.f90:890-906).
 // One CTA per k; a warp owns (c,v) outputs and its lanes run over x.
 template <typename R>
 __global__ void __launch_bounds__(VAL_THREADS)
@@ -572,7 +574,8 @@ __global__ void __launch_bounds__(VAL_THREADS)
              const double* __restrict__ ei, const double* __restrict__ allow, const typename C2<R>::T* __restrict__ con,
              const typename C2<R>::T* __restrict__ val, const double2* __restrict__ s,
              const typename C2<R>::T* __restrict__ Bp, int nysplit, int nc, int nv, int nk, int nx, int xchunk,
-             int use_e, int use_x, int use_d, int backwards, double* __restrict__ outr, double* __restrict__ outi) {
+             int use_e, int use_x, int use_d, int backwards, double xpref, double* __restrict__ outr,
+             double* __restrict__ outi) {
   typedef typename C2<R>::T CT;
   extern __shared__ double2 fsm[];
   double2* accs = fsm;                                   // [c + nc v]
@@ -592,8 +595,8 @@ __global__ void __launch_bounds__(VAL_THREADS)
           const CT vv = val[((size_t)k * nv + v) * nx + x];
           const double2 sd = s[x];
           const R sx = (R)sd.x, sy = (R)sd.y;
-          mr = (R)2 * (sx * vv.x - sy * vv.y);
-          mi = (R)2 * (sy * vv.x + sx * vv.y);
+          mr = (R)xpref * (sx * vv.x - sy * vv.y);
+          mi = (R)xpref * (sy * vv.x + sx * vv.y);
         }
         if (use_d)
           for (int ys = 0; ys < nysplit; ++ys) {
@@ -934,64 +937,95 @@ int check_ready(ocn_val_ctx* c, const int flags[3]) {
   return OCN_OK;
 }
 
+// psi holds vspin^2 blocks in the order ibeta = (i - 1) vspin + j of
+// OCEAN_ladder_act (OCEAN_ladder.f90:118-133; i the valence spin, j the
+// conduction spin, each DFT spin = min(spin, nspn)).  The direct term acts on
+// every block; the exchange sums the same-spin blocks (i, i) into one l and
+// feeds s back to each of them with spin_prefac 2 (one spin) or 1 (two),
+// OCEAN_bubble.f90:465-470,509-760.
 template <typename R>
 int apply_impl(ocn_val_ctx* c, const double* d_in, double* d_out, const int flags[3], int backwards) {
   typedef typename C2<R>::T CT;
-  const size_t n = c->npsi;
+  const size_t n = c->npsi, nb1 = c->nb1;
+  const int vs = c->vspin, ns = c->nspn;
   const int use_e = flags[0], use_x = flags[1], use_d = flags[2];
+  const size_t nxk = (size_t)c->nx * c->nk;
+  const size_t lp_blk = (size_t)c->nx * ((c->nk + 7) / 8), bp_blk = nxk * c->nv * c->ysplit;
   CT* A = static_cast<CT*>(c->d_A);
   CT* Bp = static_cast<CT*>(c->d_Bp);
-  const CT* con = c->mixed ? reinterpret_cast<const CT*>(c->d_con32) : reinterpret_cast<const CT*>(c->d_con);
-  const CT* val = c->mixed ? reinterpret_cast<const CT*>(c->d_val32) : reinterpret_cast<const CT*>(c->d_val);
-  if (use_x || use_d) {
-    dim3 blk(32, 8), grd((c->nx + 31) / 32, (c->nk + 7) / 8);
-    const size_t sm = sizeof(CT) * 8 * VAL_CC * c->nv;
-    if (c->nv <= 4)
-      kv_amat<R, 4><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, con, val, c->nc, c->nv,
-                                                 c->nk, c->nx, c->d_lp, A);
-    else if (c->nv <= 8)
-      kv_amat<R, 8><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, con, val, c->nc, c->nv,
-                                                 c->nk, c->nx, c->d_lp, A);
-    else if (c->nv <= 16)
-      kv_amat<R, 16><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, con, val, c->nc, c->nv,
-                                                  c->nk, c->nx, c->d_lp, A);
-    else
-      kv_amat<R, 32><<<grd, blk, sm, c->stream>>>(d_in, d_in + n, c->d_allow, con, val, c->nc, c->nv,
-                                                  c->nk, c->nx, c->d_lp, A);
-    ++c->launches;
-    VCUDA(c, cudaGetLastError());
-  }
+  const CT* con0 = c->mixed ? reinterpret_cast<const CT*>(c->d_con32) : reinterpret_cast<const CT*>(c->d_con);
+  const CT* val0 = c->mixed ? reinterpret_cast<const CT*>(c->d_val32) : reinterpret_cast<const CT*>(c->d_val);
+  const CT* valT0 = static_cast<const CT*>(c->d_valT);
+  auto con_s = [&](int sp) { return con0 + (size_t)sp * nxk * c->nc; };
+  auto val_s = [&](int sp) { return val0 + (size_t)sp * nxk * c->nv; };
+  auto valT_s = [&](int sp) { return valT0 + (size_t)sp * nxk * c->nv; };
+  for (int iv = 0; iv < vs; ++iv)
+    for (int jc = 0; jc < vs; ++jc) {
+      const int b = iv * vs + jc;
+      const bool diag = iv == jc;
+      if (!(use_d || (use_x && diag))) continue;
+      const int sc = std::min(jc, ns - 1), sv = std::min(iv, ns - 1);
+      // exchange partials of a same-spin block in slot iv; other blocks' go to the spare slot vs
+      double2* lp = c->d_lp + (diag ? iv : vs) * lp_blk;
+      const double* pr = d_in + b * nb1;
+      const double* pi = d_in + n + b * nb1;
+      const double* al = c->d_allow + b * nb1;
+      dim3 blk(32, 8), grd((c->nx + 31) / 32, (c->nk + 7) / 8);
+      const size_t sm = sizeof(CT) * 8 * VAL_CC * c->nv;
+      if (c->nv <= 4)
+        kv_amat<R, 4><<<grd, blk, sm, c->stream>>>(pr, pi, al, con_s(sc), val_s(sv), c->nc, c->nv, c->nk, c->nx,
+                                                   lp, A);
+      else if (c->nv <= 8)
+        kv_amat<R, 8><<<grd, blk, sm, c->stream>>>(pr, pi, al, con_s(sc), val_s(sv), c->nc, c->nv, c->nk, c->nx,
+                                                   lp, A);
+      else if (c->nv <= 16)
+        kv_amat<R, 16><<<grd, blk, sm, c->stream>>>(pr, pi, al, con_s(sc), val_s(sv), c->nc, c->nv, c->nk, c->nx,
+                                                    lp, A);
+      else
+        kv_amat<R, 32><<<grd, blk, sm, c->stream>>>(pr, pi, al, con_s(sc), val_s(sv), c->nc, c->nv, c->nk, c->nx,
+                                                    lp, A);
+      ++c->launches;
+      VCUDA(c, cudaGetLastError());
+      if (use_d) {
+        KmeshGeom<R> g = ocn::kmesh_geom<R>(c->dims.kmesh, c->ytile);
+        g.slab = (int)ladder_slab<R>(c);
+        const CT* tw;
+        if constexpr (sizeof(R) == 4) tw = c->d_twk32;
+        else tw = c->d_twk;
+        if (use_cube_kernel(c))
+          ladder_cube_fn<R>(c)<<<dim3((c->nx + c->xper - 1) / c->xper, c->ysplit), VAL_THREADS, c->lad_smem,
+                                 c->stream>>>(A, valT_s(sv), static_cast<const R*>(c->d_lad), Bp + b * bp_blk, c->nv,
+                                              c->nx, c->ytile, c->yper, tw);
+        else
+          ladder_fn<R>(c)<<<dim3(c->nx, c->ysplit), VAL_THREADS, c->lad_smem, c->stream>>>(
+              A, valT_s(sv), static_cast<const R*>(c->d_lad), Bp + b * bp_blk, c->nv, c->nk, c->nx, c->ytile,
+              c->yper, g, g.slab, tw);
+        ++c->launches;
+        VCUDA(c, cudaGetLastError());
+      }
+    }
   if (use_x) {
-    kv_bub_reduce<<<(c->nx + 31) / 32, dim3(32, 32), 0, c->stream>>>(c->d_lp, (c->nk + 7) / 8, c->nx, c->d_s);
+    kv_bub_reduce<<<(c->nx + 31) / 32, dim3(32, 32), 0, c->stream>>>(c->d_lp, vs * ((c->nk + 7) / 8), c->nx,
+                                                                      c->d_s);
     kv_bub_fft<<<1, 1024, bub_fft_smem(c), c->stream>>>(
         c->d_s, c->d_bub, make_int3(c->dims.xmesh[0], c->dims.xmesh[1], c->dims.xmesh[2]), c->d_twx);
     c->launches += 2;
     VCUDA(c, cudaGetLastError());
   }
-  if (use_d) {
-    KmeshGeom<R> g = ocn::kmesh_geom<R>(c->dims.kmesh, c->ytile);
-    g.slab = (int)ladder_slab<R>(c);
-    const CT* tw;
-    if constexpr (sizeof(R) == 4) tw = c->d_twk32;
-    else tw = c->d_twk;
-    if (use_cube_kernel(c))
-      ladder_cube_fn<R>(c)<<<dim3((c->nx + c->xper - 1) / c->xper, c->ysplit), VAL_THREADS, c->lad_smem, c->stream>>>(
-          A, static_cast<const CT*>(c->d_valT), static_cast<const R*>(c->d_lad), Bp, c->nv, c->nx, c->ytile,
-          c->yper, tw);
-    else
-      ladder_fn<R>(c)<<<dim3(c->nx, c->ysplit), VAL_THREADS, c->lad_smem, c->stream>>>(
-          A, static_cast<const CT*>(c->d_valT), static_cast<const R*>(c->d_lad), Bp, c->nv, c->nk, c->nx,
-          c->ytile, c->yper, g, g.slab, tw);
-    ++c->launches;
-    VCUDA(c, cudaGetLastError());
-  }
   const int xc = (int)final_xchunk(c);
   const size_t fsm = final_smem(c);
-  kv_final<R><<<c->nk, VAL_THREADS, fsm, c->stream>>>(
-      d_in, d_in + n, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow, con, val, c->d_s, Bp,
-      c->ysplit, c->nc, c->nv, c->nk, c->nx, xc, use_e, use_x, use_d, backwards, d_out, d_out + n);
-  ++c->launches;
-  VCUDA(c, cudaGetLastError());
+  const double xpref = vs == 1 ? 2.0 : 1.0;
+  for (int iv = 0; iv < vs; ++iv)
+    for (int jc = 0; jc < vs; ++jc) {
+      const int b = iv * vs + jc;
+      const int sc = std::min(jc, ns - 1), sv = std::min(iv, ns - 1);
+      kv_final<R><<<c->nk, VAL_THREADS, fsm, c->stream>>>(
+          d_in + b * nb1, d_in + n + b * nb1, c->d_er + b * nb1, c->ei_nonzero ? c->d_ei + b * nb1 : nullptr,
+          c->d_allow + b * nb1, con_s(sc), val_s(sv), c->d_s, Bp + b * bp_blk, c->ysplit, c->nc, c->nv, c->nk,
+          c->nx, xc, use_e, use_x && iv == jc, use_d, backwards, xpref, d_out + b * nb1, d_out + n + b * nb1);
+      ++c->launches;
+      VCUDA(c, cudaGetLastError());
+    }
   return OCN_OK;
 }
 
@@ -1021,6 +1055,8 @@ int ocn_val_create(const ocn_val_dims* d, ocn_val_ctx** out) {
   }
   if (d->precision != OCN_PREC_FP64 && d->precision != OCN_PREC_MIXED)
     return vset_err(nullptr, OCN_ERR_ARG, "ocn_val_create: unknown precision");
+  if (d->nspn < 0 || d->nspn > 2 || d->vspin < 0 || d->vspin > 2)
+    return vset_err(nullptr, OCN_ERR_ARG, "ocn_val_create: nspn and vspin must be 1 or 2");
   ocn_val_ctx* c = new (std::nothrow) ocn_val_ctx();
   if (!c) return vset_err(nullptr, OCN_ERR_ALLOC, "host allocation failed");
   auto fail = [&](int rc) {
@@ -1034,7 +1070,10 @@ int ocn_val_create(const ocn_val_dims* d, ocn_val_ctx** out) {
   c->nv = d->nv;
   c->nk = d->kmesh[0] * d->kmesh[1] * d->kmesh[2];
   c->nx = d->xmesh[0] * d->xmesh[1] * d->xmesh[2];
-  c->npsi = (size_t)c->nc * c->nv * c->nk;
+  c->nspn = d->nspn > 1 ? 2 : 1;
+  c->vspin = d->vspin > 1 ? 2 : 1;
+  c->nb1 = (size_t)c->nc * c->nv * c->nk;
+  c->npsi = c->nb1 * c->vspin * c->vspin;
   c->mixed = d->precision == OCN_PREC_MIXED;
   cudaError_t e = cudaSetDevice(c->device);
   if (e != cudaSuccess) return fail(vcuda(c, e, "cudaSetDevice"));
@@ -1051,18 +1090,20 @@ int ocn_val_create(const ocn_val_dims* d, ocn_val_ctx** out) {
   if (rc) return fail(rc);
   const size_t nxk = (size_t)c->nx * c->nk;
   if ((rc = valloc(c, &c->d_er, c->npsi)) || (rc = valloc(c, &c->d_ei, c->npsi)) ||
-      (rc = valloc(c, &c->d_allow, c->npsi)) || (rc = valloc(c, &c->d_con, nxk * c->nc)) ||
-      (rc = valloc(c, &c->d_val, nxk * c->nv)) ||
-      (rc = valloc(c, reinterpret_cast<char**>(&c->d_valT), nxk * c->nv * cs)) ||
+      (rc = valloc(c, &c->d_allow, c->npsi)) || (rc = valloc(c, &c->d_con, nxk * c->nc * c->nspn)) ||
+      (rc = valloc(c, &c->d_val, nxk * c->nv * c->nspn)) ||
+      (rc = valloc(c, reinterpret_cast<char**>(&c->d_valT), nxk * c->nv * c->nspn * cs)) ||
       (rc = valloc(c, reinterpret_cast<char**>(&c->d_lad), nxk * c->nx * rs)) ||
       (rc = valloc(c, &c->d_bub, c->nx)) || (rc = valloc(c, &c->d_twk, 3 * OCN_MAX_KDIM)) ||
       (rc = valloc(c, &c->d_twk32, 3 * OCN_MAX_KDIM)) || (rc = valloc(c, &c->d_twx, 3 * OCN_MAX_KDIM)) ||
-      (rc = valloc(c, &c->d_lp, (size_t)c->nx * ((c->nk + 7) / 8))) || (rc = valloc(c, &c->d_s, c->nx)) ||
-      (rc = valloc(c, reinterpret_cast<char**>(&c->d_A), nxk * c->nv * cs)) ||
-      (rc = valloc(c, reinterpret_cast<char**>(&c->d_Bp), nxk * c->nv * c->ysplit * cs)) ||
+      (rc = valloc(c, &c->d_lp, (size_t)(c->vspin + 1) * c->nx * ((c->nk + 7) / 8))) ||
+      (rc = valloc(c, &c->d_s, c->nx)) || (rc = valloc(c, reinterpret_cast<char**>(&c->d_A), nxk * c->nv * cs)) ||
+      (rc = valloc(c, reinterpret_cast<char**>(&c->d_Bp),
+                   nxk * c->nv * c->ysplit * cs * c->vspin * c->vspin)) ||
       (rc = valloc(c, &c->d_vec, 8 * c->npsi)) || (rc = valloc(c, &c->d_red, 4 * (size_t)c->red_blocks)))
     return fail(rc);
-  if (c->mixed && ((rc = valloc(c, &c->d_con32, nxk * c->nc)) || (rc = valloc(c, &c->d_val32, nxk * c->nv))))
+  if (c->mixed && ((rc = valloc(c, &c->d_con32, nxk * c->nc * c->nspn)) ||
+                   (rc = valloc(c, &c->d_val32, nxk * c->nv * c->nspn))))
     return fail(rc);
   double2 twk[3][OCN_MAX_KDIM], twx[3][OCN_MAX_KDIM];
   float2 twk32[3][OCN_MAX_KDIM];
@@ -1156,7 +1197,8 @@ static int set_states_impl(ocn_val_ctx* c, const double* conr, const double* con
                            const double* vali, bool on_device) {
   if (!c || !conr || !coni || !valr || !vali) return vset_err(c, OCN_ERR_ARG, "null argument");
   cudaSetDevice(c->device);
-  const size_t ncon = (size_t)c->nx * c->nc * c->nk, nval = (size_t)c->nx * c->nv * c->nk;
+  const size_t ncon = (size_t)c->nx * c->nc * c->nk * c->nspn, nval = (size_t)c->nx * c->nv * c->nk * c->nspn;
+  const size_t nval1 = nval / c->nspn;
   double* tmp = nullptr;
   const double *cr = conr, *ci = coni, *vr = valr, *vi = vali;
   if (!on_device) {
@@ -1179,16 +1221,18 @@ static int set_states_impl(ocn_val_ctx* c, const double* conr, const double* con
   }
   kv_interleave<<<g, 256, 0, c->stream>>>(vr, vi, nval, c->d_val);
   if (c->mixed) {
-    kv_transpose_val<float><<<g, 256, 0, c->stream>>>(c->d_val, c->nv, c->nk, c->nx,
-                                                      static_cast<float2*>(c->d_valT));
+    for (int sp = 0; sp < c->nspn; ++sp)
+      kv_transpose_val<float><<<g, 256, 0, c->stream>>>(c->d_val + sp * nval1, c->nv, c->nk, c->nx,
+                                                        static_cast<float2*>(c->d_valT) + sp * nval1);
     kv_to_float<<<g, 256, 0, c->stream>>>(reinterpret_cast<const double*>(c->d_con), 2 * ncon,
                                           reinterpret_cast<float*>(c->d_con32));
     kv_to_float<<<g, 256, 0, c->stream>>>(reinterpret_cast<const double*>(c->d_val), 2 * nval,
                                           reinterpret_cast<float*>(c->d_val32));
   }
   else
-    kv_transpose_val<double><<<g, 256, 0, c->stream>>>(c->d_val, c->nv, c->nk, c->nx,
-                                                       static_cast<double2*>(c->d_valT));
+    for (int sp = 0; sp < c->nspn; ++sp)
+      kv_transpose_val<double><<<g, 256, 0, c->stream>>>(c->d_val + sp * nval1, c->nv, c->nk, c->nx,
+                                                         static_cast<double2*>(c->d_valT) + sp * nval1);
   {
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

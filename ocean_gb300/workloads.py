@@ -319,6 +319,8 @@ class ValWorkload:
     el: float = 0.0
     eh: float = 30.0 * EV2HARTREE
     device_arrays: dict = field(default_factory=dict)  # torch tensors when built on a device
+    nspn: int = 1              # DFT spins of the states
+    vspin: int = 1             # valence_ham_spin: psi has vspin^2 spin blocks
 
     @property
     def nk(self) -> int:
@@ -330,7 +332,7 @@ class ValWorkload:
 
     @property
     def npsi(self) -> int:
-        return self.nc * self.nv * self.nk
+        return self.nc * self.nv * self.nk * self.vspin * self.vspin
 
 
 def _mesh_frac(mesh):
@@ -398,11 +400,15 @@ def val_ladder(kmesh, xmesh, avec, celvol, epsilon0=4.0, width_angstrom=0.5, dev
 
 
 def make_val(name: str, seed: int = 0, nc: Optional[int] = None, nv: Optional[int] = None, kmesh=None,
-             xmesh=None, device: Optional[str] = None) -> ValWorkload:
+             xmesh=None, device: Optional[str] = None, nspn: int = 1, vspin: int = 1) -> ValWorkload:
     """Valence workloads: 'vtiny', 'vsmall' (oracle sizes), 'v2' (k-mesh 8^3,
     x-mesh 10^3, 8 conduction and 4 valence bands: the benchmark case).
     device: build the states and the ladder as torch tensors there (kept in
-    w.device_arrays; the numpy fields are then None)."""
+    w.device_arrays; the numpy fields are then None).  nspn: DFT spins (states
+    and band energies per spin); vspin: valence_ham_spin (psi gets vspin^2
+    blocks, block (i, j) pairing valence spin i with conduction spin j)."""
+    if nspn not in (1, 2) or vspin not in (1, 2):
+        raise ValueError("nspn and vspin must be 1 or 2")
     presets = {
         "vtiny": dict(nc=4, nv=2, kmesh=(2, 2, 2), xmesh=(3, 3, 3), niter=24),
         "vsmall": dict(nc=6, nv=3, kmesh=(4, 4, 4), xmesh=(4, 4, 4), niter=40),
@@ -427,27 +433,32 @@ def make_val(name: str, seed: int = 0, nc: Optional[int] = None, nv: Optional[in
     bvec = np.zeros(9)
     bvec[0] = bvec[4] = bvec[8] = 2.0 * math.pi / a_bohr
     celvol = a_bohr ** 3
-    ev = np.sort(rng.uniform(-8.0, 0.0, size=(nk, nvb)), axis=1)
-    ec = np.sort(rng.uniform(1.0, 16.0, size=(nk, ncb)), axis=1)
-    e = (ec[:, None, :] - ev[:, :, None]) * EV2HARTREE          # (k, v, c)
-    er = e.reshape(-1).copy()
+    ev = np.sort(rng.uniform(-8.0, 0.0, size=(nspn, nk, nvb)), axis=2)
+    ec = np.sort(rng.uniform(1.0, 16.0, size=(nspn, nk, ncb)), axis=2)
+    blocks = []
+    for iv in range(vspin):          # ibeta = (i - 1) vspin + j: valence spin outer
+        for jc in range(vspin):
+            sv, sc = min(iv, nspn - 1), min(jc, nspn - 1)
+            blocks.append((ec[sc][:, None, :] - ev[sv][:, :, None]) * EV2HARTREE)  # (k, v, c)
+    er = np.concatenate([b.reshape(-1) for b in blocks])
     ei = np.zeros_like(er)
     allow = np.ones_like(er)
-    g_r = rng.standard_normal(ncb * nvb * nk)
-    g_i = rng.standard_normal(ncb * nvb * nk)
+    g_r = rng.standard_normal(er.size)
+    g_i = rng.standard_normal(er.size)
     psi_r, psi_i, kpref = pnorm(g_r, g_i, nk, celvol)
     w = ValWorkload(name=name, nc=ncb, nv=nvb, kmesh=km, xmesh=xm, celvol=celvol, avec=avec, bvec=bvec,
                     qinb=np.zeros(3), epsilon0=4.0, er=er, ei=ei, allow=allow, conr=None, coni=None,
                     valr=None, vali=None, ladder=None, psi_r=psi_r, psi_i=psi_i, kpref=kpref,
-                    niter=p["niter"])
+                    niter=p["niter"], nspn=nspn, vspin=vspin)
     if device is None:
-        st = np.empty((nk, ncb + nvb, nx), dtype=np.complex128)
-        for k in range(nk):
-            g = rng.standard_normal((nx, ncb + nvb)) + 1j * rng.standard_normal((nx, ncb + nvb))
-            qm, _ = np.linalg.qr(g)
-            st[k] = qm.T
-        val = st[:, :nvb, :]   # (k, v, x): Fortran (x, v, k) flattened
-        con = st[:, nvb:, :]
+        st = np.empty((nspn, nk, ncb + nvb, nx), dtype=np.complex128)
+        for sp in range(nspn):
+            for k in range(nk):
+                g = rng.standard_normal((nx, ncb + nvb)) + 1j * rng.standard_normal((nx, ncb + nvb))
+                qm, _ = np.linalg.qr(g)
+                st[sp, k] = qm.T
+        val = st[:, :, :nvb, :]   # (s, k, v, x): Fortran (x, v, k, s) flattened
+        con = st[:, :, nvb:, :]
         w.valr, w.vali = val.real.reshape(-1).copy(), val.imag.reshape(-1).copy()
         w.conr, w.coni = con.real.reshape(-1).copy(), con.imag.reshape(-1).copy()
         w.ladder = val_ladder(km, xm, avec, celvol, w.epsilon0).numpy().reshape(-1)
@@ -456,14 +467,15 @@ def make_val(name: str, seed: int = 0, nc: Optional[int] = None, nv: Optional[in
 
         gen = torch.Generator(device=device)
         gen.manual_seed(seed)
-        st = torch.empty((nk, ncb + nvb, nx), dtype=torch.complex128, device=device)
-        for k in range(nk):
-            g = torch.complex(torch.randn((nx, ncb + nvb), generator=gen, device=device, dtype=torch.float64),
-                              torch.randn((nx, ncb + nvb), generator=gen, device=device, dtype=torch.float64))
-            qm, _ = torch.linalg.qr(g)
-            st[k] = qm.T
-        val = st[:, :nvb, :].contiguous()
-        con = st[:, nvb:, :].contiguous()
+        st = torch.empty((nspn, nk, ncb + nvb, nx), dtype=torch.complex128, device=device)
+        for sp in range(nspn):
+            for k in range(nk):
+                g = torch.complex(torch.randn((nx, ncb + nvb), generator=gen, device=device, dtype=torch.float64),
+                                  torch.randn((nx, ncb + nvb), generator=gen, device=device, dtype=torch.float64))
+                qm, _ = torch.linalg.qr(g)
+                st[sp, k] = qm.T
+        val = st[:, :, :nvb, :].contiguous()
+        con = st[:, :, nvb:, :].contiguous()
         w.device_arrays = dict(valr=val.real.contiguous().reshape(-1), vali=val.imag.contiguous().reshape(-1),
                                conr=con.real.contiguous().reshape(-1), coni=con.imag.contiguous().reshape(-1),
                                ladder=val_ladder(km, xm, avec, celvol, w.epsilon0, device=device).reshape(-1))

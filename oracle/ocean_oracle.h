@@ -136,6 +136,8 @@ typedef struct {
   int nc, nv;    /* conduction / valence bands */
   int kmesh[3];  /* flat k index k3 fastest */
   int xmesh[3];  /* flat x index x3 fastest */
+  int nspn;      /* DFT spins of con/val (0 or 1: one) */
+  int vspin;     /* valence_ham_spin (0 or 1: one; 2: psi has 4 spin blocks) */
 } or_val_dims;
 
 typedef struct {

@@ -1,7 +1,7 @@
 // ocean_oracle_val.cpp -- CPU ORACLE for the valence BSE action (test
 // infrastructure only; never linked into the product library).  A plain FP64
-// restatement of the reference Fortran for one spin channel
-// (valence_ham_spin = 1, nspn = 1) and resonant pairs only (nbw = 1):
+// restatement of the reference Fortran for resonant pairs (nbw = 1), one or two
+// valence-Hamiltonian spins (valence_ham_spin) and DFT spins (nspn):
 //
 //   H psi = E o psi + allow o [ 2 X(allow o psi) - D(allow o psi) ]
 //
@@ -11,9 +11,9 @@
 // 590-600).
 //
 // Layouts (Fortran order of the reference arrays, single rank):
-//   psi, E, allow   (Nc, Nv, Nk)      psi%valr/vali(c, v, k)
-//   con             (Nx, Nc, Nk)      re_con/im_con(x, c, k)
-//   val             (Nx, Nv, Nk)      re_val/im_val(x, v, k)
+//   psi, E, allow   (Nc, Nv, Nk, vs^2) psi%valr/vali(c, v, k, ibeta)
+//   con             (Nx, Nc, Nk, nspn) re_con/im_con(x, c, k, spin)
+//   val             (Nx, Nv, Nk, nspn) re_val/im_val(x, v, k, spin)
 //   bubble          (Nx)              bubble(x) of AI_bubble_populate
 //   ladder          (Nk, Nx, Nx)      ladder(k, x, y) after resort_ladder
 // The flat k index runs k3 fastest and the flat x index x3 fastest, the FFT
@@ -23,6 +23,7 @@
 // Parity status: unpinned by reference data (the reference ships no valence
 // states, bubble or ladder files); pinned by Hermiticity, a dense-H check and
 // agreement with the cited source.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -165,15 +166,16 @@ static void val_project(const or_val_dims* d, const or_val_ops* o, double pref, 
       }
 }
 
-// AI_bubble_act, OCEAN_bubble.f90:420-796 (valence_ham_spin = 1, nbw = 1):
-// l(x) = sum_{v,k} conj(val) A; s = FFT_fwd[ bubble o FFT_bwd[l] ] (neither
-// normalised, :663-665); out += 2 sum_x conj(con) s val.
-void or_val_bubble_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, double* outr,
-                       double* outi) {
+// AI_bubble_act, OCEAN_bubble.f90:420-796 (nbw = 1), in two halves:
+// l(x) += sum_{v,k} conj(val) A for one same-spin block (:509-580), and, after
+// s = FFT_fwd[ bubble o FFT_bwd[l] ] (neither normalised, :663-665),
+// out += pref sum_x conj(con) s val for one same-spin block (:687-760);
+// pref = spin_prefac, 2 for valence_ham_spin = 1 and 1 for 2 (:465-470).
+static void bubble_l(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi,
+                     std::vector<double>& lr, std::vector<double>& li) {
   const int nv = d->nv, nk = nk_of(d), nx = nx_of(d);
   std::vector<double> ar, ai;
   val_amat(d, o, pr, pi, ar, ai);
-  std::vector<double> lr(nx, 0.0), li(nx, 0.0);
   for (int k = 0; k < nk; ++k)
     for (int v = 0; v < nv; ++v) {
       const size_t b = (size_t)nx * (v + (size_t)nv * k);
@@ -183,12 +185,21 @@ void or_val_bubble_act(const or_val_dims* d, const or_val_ops* o, const double* 
         li[x] += vr * ai[b + x] - vi * ar[b + x];
       }
     }
+}
+
+static void bubble_s(const or_val_dims* d, const or_val_ops* o, std::vector<double>& lr, std::vector<double>& li) {
+  const int nx = nx_of(d);
   or_fft3d(d->xmesh, lr.data(), li.data(), +1);
   for (int x = 0; x < nx; ++x) {
     lr[x] *= o->bubble[x];
     li[x] *= o->bubble[x];
   }
   or_fft3d(d->xmesh, lr.data(), li.data(), -1);
+}
+
+static void bubble_project(const or_val_dims* d, const or_val_ops* o, double pref, const std::vector<double>& lr,
+                           const std::vector<double>& li, double* outr, double* outi) {
+  const int nv = d->nv, nk = nk_of(d), nx = nx_of(d);
   std::vector<double> mr((size_t)nx * nv * nk), mi((size_t)nx * nv * nk);
   for (int k = 0; k < nk; ++k)
     for (int v = 0; v < nv; ++v) {
@@ -199,7 +210,16 @@ void or_val_bubble_act(const or_val_dims* d, const or_val_ops* o, const double* 
         mi[b + x] = li[x] * vr + lr[x] * vi;
       }
     }
-  val_project(d, o, 2.0, mr, mi, outr, outi);
+  val_project(d, o, pref, mr, mi, outr, outi);
+}
+
+// One spin channel (valence_ham_spin = 1): spin_prefac 2.
+void or_val_bubble_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, double* outr,
+                       double* outi) {
+  std::vector<double> lr(nx_of(d), 0.0), li(nx_of(d), 0.0);
+  bubble_l(d, o, pr, pi, lr, li);
+  bubble_s(d, o, lr, li);
+  bubble_project(d, o, 2.0, lr, li, outr, outi);
 }
 
 // OCEAN_ladder_act_single, OCEAN_ladder.f90:155-1004 (one rank, nbw = 1):
@@ -259,18 +279,61 @@ void or_val_ladder_slab(const or_val_dims* d, const or_val_ops* o, const double*
   val_project(d, o, -1.0, br, bi, outr, outi);
 }
 
+// The operator data seen by one (valence spin, conduction spin) pair: con of
+// the conduction spin, val of the valence spin (DFT spin index = min(spin,
+// nspn), OCEAN_ladder.f90:118-133, OCEAN_bubble.f90:511-512).
+static or_val_ops spin_view(const or_val_dims* d, const or_val_ops* o, int cs, int vs) {
+  const size_t nxk = (size_t)nx_of(d) * nk_of(d);
+  or_val_ops v = *o;
+  v.conr = o->conr + (size_t)cs * nxk * d->nc;
+  v.coni = o->coni + (size_t)cs * nxk * d->nc;
+  v.valr = o->valr + (size_t)vs * nxk * d->nv;
+  v.vali = o->vali + (size_t)vs * nxk * d->nv;
+  return v;
+}
+
+static int vspin_of(const or_val_dims* d) { return d->vspin > 1 ? 2 : 1; }
+static int nspn_of(const or_val_dims* d) { return d->nspn > 1 ? 2 : 1; }
+
 // OCEAN_xact valence branch (OCEAN_action.f90:521-575) followed by
-// OCEAN_energies_act (:590-600, OCEAN_energies.f90:890-906).
+// OCEAN_energies_act (:590-600, OCEAN_energies.f90:890-906).  psi holds
+// valence_ham_spin^2 blocks (Nc, Nv, Nk) in the order ibeta = (i - 1) vs + j
+// of OCEAN_ladder_act (i the valence spin, j the conduction spin).  The
+// exchange sums the same-spin blocks (ispn, ispn) into one l and feeds it back
+// to each of them; the direct term acts on every block.
 int or_val_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, double* hr,
                double* hi, int backwards) {
-  const size_t n = (size_t)d->nc * d->nv * nk_of(d);
+  const int vs = vspin_of(d), ns = nspn_of(d);
+  const size_t nb1 = (size_t)d->nc * d->nv * nk_of(d), n = nb1 * vs * vs;
   std::vector<double> qr(n), qi(n), kr(n, 0.0), ki(n, 0.0);
   for (size_t i = 0; i < n; ++i) {
     qr[i] = pr[i] * o->allow[i];
     qi[i] = pi[i] * o->allow[i];
   }
-  if (o->bflag) or_val_bubble_act(d, o, qr.data(), qi.data(), kr.data(), ki.data());
-  if (o->lflag) or_val_ladder_act(d, o, qr.data(), qi.data(), kr.data(), ki.data());
+  if (o->bflag) {
+    std::vector<double> lr(nx_of(d), 0.0), li(nx_of(d), 0.0);
+    for (int is = 0; is < vs; ++is) {
+      const int ds = std::min(is, ns - 1);
+      const or_val_ops v = spin_view(d, o, ds, ds);
+      const size_t off = nb1 * (size_t)(is * vs + is);
+      bubble_l(d, &v, qr.data() + off, qi.data() + off, lr, li);
+    }
+    bubble_s(d, o, lr, li);
+    const double pref = vs == 1 ? 2.0 : 1.0;
+    for (int js = 0; js < vs; ++js) {
+      const int ds = std::min(js, ns - 1);
+      const or_val_ops v = spin_view(d, o, ds, ds);
+      const size_t off = nb1 * (size_t)(js * vs + js);
+      bubble_project(d, &v, pref, lr, li, kr.data() + off, ki.data() + off);
+    }
+  }
+  if (o->lflag)
+    for (int iv = 0; iv < vs; ++iv)
+      for (int jc = 0; jc < vs; ++jc) {
+        const or_val_ops v = spin_view(d, o, std::min(jc, ns - 1), std::min(iv, ns - 1));
+        const size_t off = nb1 * (size_t)(iv * vs + jc);
+        or_val_ladder_act(d, &v, qr.data() + off, qi.data() + off, kr.data() + off, ki.data() + off);
+      }
   for (size_t i = 0; i < n; ++i) {
     double er = 0.0, ei = 0.0;
     if (o->bande) {
@@ -294,7 +357,7 @@ int or_val_act(const or_val_dims* d, const or_val_ops* o, const double* pr, cons
 // action, in the same arithmetic order as or_haydock.
 int or_val_haydock(const or_val_dims* d, const or_val_ops* o, const double* p0r, const double* p0i, int niter,
                    double* real_a, double* imag_a, double* real_b, int* niter_done) {
-  const size_t n = (size_t)d->nc * d->nv * nk_of(d);
+  const size_t n = (size_t)d->nc * d->nv * nk_of(d) * vspin_of(d) * vspin_of(d);
   std::vector<double> psr(p0r, p0r + n), psi_(p0i, p0i + n);
   std::vector<double> olr(n, 0.0), oli(n, 0.0), hr(n), hi(n);
   for (int i = 0; i <= niter; ++i) real_a[i] = imag_a[i] = real_b[i] = 0.0;

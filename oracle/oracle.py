@@ -263,7 +263,8 @@ def zhptrf_solve(ap: np.ndarray, b: np.ndarray):
 # ---------------------------------------------------------------- valence BSE
 
 class OrValDims(C.Structure):
-    _fields_ = [("nc", C.c_int), ("nv", C.c_int), ("kmesh", C.c_int * 3), ("xmesh", C.c_int * 3)]
+    _fields_ = [("nc", C.c_int), ("nv", C.c_int), ("kmesh", C.c_int * 3), ("xmesh", C.c_int * 3),
+                ("nspn", C.c_int), ("vspin", C.c_int)]
 
 
 class OrValOps(C.Structure):
@@ -302,6 +303,8 @@ class OracleVal:
         d.nc, d.nv = w.nc, w.nv
         d.kmesh[:] = list(w.kmesh)
         d.xmesh[:] = list(w.xmesh)
+        d.nspn = getattr(w, "nspn", 1)
+        d.vspin = getattr(w, "vspin", 1)
         self.d = d
         o = OrValOps()
         (o.er, o.ei, o.allow, o.conr, o.coni, o.valr, o.vali, o.bubble, o.ladder) = [dptr(a) for a in self._refs]
@@ -309,11 +312,18 @@ class OracleVal:
         self.o = o
 
     def act(self, pr, pi, backwards=False, flags=None):
+        """H psi; flags = (bande, bflag, lflag) for this call only (default: the
+        flags the problem was built with)."""
+        saved = (self.o.bande, self.o.bflag, self.o.lflag)
         if flags is not None:
             self.o.bande, self.o.bflag, self.o.lflag = flags
         hr, hi = np.zeros(self.w.npsi), np.zeros(self.w.npsi)
-        lib().or_val_act(C.byref(self.d), C.byref(self.o), dptr(np.ascontiguousarray(pr, dtype=np.float64)),
-                         dptr(np.ascontiguousarray(pi, dtype=np.float64)), dptr(hr), dptr(hi), int(bool(backwards)))
+        try:
+            lib().or_val_act(C.byref(self.d), C.byref(self.o), dptr(np.ascontiguousarray(pr, dtype=np.float64)),
+                             dptr(np.ascontiguousarray(pi, dtype=np.float64)), dptr(hr), dptr(hi),
+                             int(bool(backwards)))
+        finally:
+            self.o.bande, self.o.bflag, self.o.lflag = saved
         return hr, hi
 
     def haydock(self, niter, pr=None, pi=None):

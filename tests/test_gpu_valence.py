@@ -172,3 +172,27 @@ def test_valence_haydock_spectrum_end_to_end(built, prec):
     o = O.write_val(ora, oia, orb, *args, 1, True)
     err = np.linalg.norm(g[:, 2] - o[:, 2]) / np.linalg.norm(o[:, 2])
     assert err < (1e-10 if prec == capi.OCN_PREC_FP64 else 1e-4), err
+
+
+@pytest.mark.parametrize("nspn,vspin", [(1, 2), (2, 2), (2, 1)])
+@pytest.mark.parametrize("prec", [capi.OCN_PREC_FP64, capi.OCN_PREC_MIXED])
+def test_spin_blocks_match_oracle(built, nspn, vspin, prec):
+    _, O = built
+    w = WL.make_val("vsmall", seed=31, nspn=nspn, vspin=vspin)
+    P = O.OracleVal(w)
+    ctx = capi.ValContext(w, precision=prec)
+    try:
+        rng = np.random.default_rng(3)
+        x = rng.standard_normal(w.npsi) + 1j * rng.standard_normal(w.npsi)
+        for flags in [(1, 1, 1), (0, 1, 0), (0, 0, 1)]:
+            gr, gi = ctx.apply_H(x.real, x.imag, flags=flags)
+            orr, oi = P.act(x.real, x.imag, flags=flags)
+            err = _rel(gr + 1j * gi, orr + 1j * oi)
+            tol = 1e-12 if prec == capi.OCN_PREC_FP64 else (1e-6 if flags == (1, 1, 1) else 1e-5)
+            assert err < tol, (flags, err)
+        ra, ia, rb, done = ctx.haydock(20)
+        rc, ora, oia, orb, _ = P.haydock(20)
+        if prec == capi.OCN_PREC_FP64:
+            assert np.max(np.abs(ra[:10] - ora[:10]) / np.abs(ora[:10])) < 1e-12
+    finally:
+        ctx.close()

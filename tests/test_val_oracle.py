@@ -85,7 +85,7 @@ def test_oracle_haydock_brackets_the_dense_spectrum(oracle_lib):
 
 def test_val_create_rejects_bad_dims_without_gpu(lib_built):
     lib = capi.load(lib_built)
-    for change in [("nv", 0), ("nv", 33), ("nc", 0), ("precision", 5)]:
+    for change in [("nv", 0), ("nv", 33), ("nc", 0), ("precision", 5), ("nspn", 3), ("vspin", -1)]:
         d = capi.OcnValDims()
         d.nc, d.nv = 4, 2
         d.kmesh[:] = [2, 2, 2]
@@ -174,3 +174,44 @@ def test_oracle_write_val_is_the_resolvent(oracle_lib, semi_tda):
         if semi_tda:
             eps -= fact * np.linalg.solve(-z * np.eye(n) - T, e1)[0]
         assert abs(out[r, 1] + 1j * out[r, 2] - eps) < 1e-9 * abs(eps), r
+
+
+@pytest.mark.parametrize("nspn,vspin", [(1, 2), (2, 2), (2, 1)])
+def test_oracle_spin_blocks_hermitian(oracle_lib, nspn, vspin):
+    O = oracle_lib
+    w = WL.make_val("vtiny", seed=6, nspn=nspn, vspin=vspin)
+    assert w.npsi == w.nc * w.nv * w.nk * vspin * vspin
+    P = O.OracleVal(w)
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(w.npsi) + 1j * rng.standard_normal(w.npsi)
+    y = rng.standard_normal(w.npsi) + 1j * rng.standard_normal(w.npsi)
+    hx, hy = P.act(x.real, x.imag), P.act(y.real, y.imag)
+    lhs = np.vdot(y, hx[0] + 1j * hx[1])
+    rhs = np.conj(np.vdot(x, hy[0] + 1j * hy[1]))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_oracle_singlet_reduces_to_one_spin_channel(oracle_lib):
+    """valence_ham_spin = 2 with one DFT spin: a singlet psi (blocks up-up =
+    down-down = z, spin-flip blocks 0) maps to a singlet whose up-up block is
+    the one-channel action on z (exchange: two blocks at spin_prefac 1 = one
+    block at 2), and the spin-flip blocks get nothing."""
+    import dataclasses
+
+    O = oracle_lib
+    w2 = WL.make_val("vsmall", seed=7, nspn=1, vspin=2)
+    nb1 = w2.npsi // 4
+    w1 = dataclasses.replace(w2, vspin=1, er=w2.er[:nb1].copy(), ei=w2.ei[:nb1].copy(),
+                             allow=w2.allow[:nb1].copy(), psi_r=w2.psi_r[:nb1].copy(), psi_i=w2.psi_i[:nb1].copy())
+    rng = np.random.default_rng(4)
+    z = rng.standard_normal(nb1) + 1j * rng.standard_normal(nb1)
+    psi = np.zeros(w2.npsi, complex)
+    psi[:nb1] = z
+    psi[3 * nb1:] = z
+    h2 = O.OracleVal(w2).act(psi.real, psi.imag)
+    h1 = O.OracleVal(w1).act(z.real, z.imag)
+    H2 = h2[0] + 1j * h2[1]
+    H1 = h1[0] + 1j * h1[1]
+    assert np.max(np.abs(H2[:nb1] - H1)) < 1e-13 * np.max(np.abs(H1))
+    assert np.max(np.abs(H2[3 * nb1:] - H1)) < 1e-13 * np.max(np.abs(H1))
+    assert np.max(np.abs(H2[nb1:3 * nb1])) == 0.0
