@@ -506,8 +506,9 @@ int ocn_timing_read(ocn_ctx* ctx, long long counts[6], double ms[6]);
 /* ------------------------------------------------------- valence BSE
  * The valence branch of OCEAN_xact (OCEAN_action.f90:521-600) for resonant
  * pairs (nbw = 1), valence_ham_spin 1 or 2 and one or two DFT spins:
- *   H psi = E o psi + allow o [ 2 X(allow o psi) - D(allow o psi) ]
- * X: AI_bubble_act (OCEAN_bubble.f90:420-796); D: OCEAN_ladder_act_single
+ *   H psi = E o psi + allow o [ 2 X(allow o psi) - D(allow o psi) (+ 2 F(allow o psi)) ]
+ * X: AI_bubble_act (OCEAN_bubble.f90:420-796); F: OCEAN_fxc_act when a kernel
+ * is set (OCEAN_fxc.f90:127-322); D: OCEAN_ladder_act_single
  * (OCEAN_ladder.f90:155-1004).  Replaces those routines and the module state
  * they read (re/im_con, re/im_val of OCEAN_val_states, p_energy and allow of
  * OCEAN_energies, bubble of OCEAN_bubble, ladder of OCEAN_ladder).
@@ -553,6 +554,14 @@ int ocn_val_set_states_dev(ocn_val_ctx* ctx, const double* con_r, const double* 
 int ocn_val_set_bubble(ocn_val_ctx* ctx, const double* bubble);
 int ocn_val_set_ladder(ocn_val_ctx* ctx, const double* ladder);
 int ocn_val_set_ladder_dev(ocn_val_ctx* ctx, const double* d_ladder);
+
+/* The ALDA f_xc term (OCEAN_fxc_act, OCEAN_fxc.f90:127-322; aldaf): on while a
+ * kernel fxc(Nx) is set (NULL: off); valence_ham_spin = 1 only, as the
+ * reference (else OCN_ERR_UNSUPPORTED).  ocn_val_fxc_from_rho builds it from
+ * the density on the x-mesh (OCEAN_fxc_prep with cacorr, :35-123,333-470).
+ * Host only; rho in the x-mesh order. */
+int ocn_val_set_fxc(ocn_val_ctx* ctx, const double* fxc);
+int ocn_val_fxc_from_rho(int nx, const double* rho, double celvol, int nkpts, double* fxc);
 
 /* bubble(x) from the cell (AI_bubble_populate with wall_search_old_way,
  * OCEAN_bubble.f90:238-407): bvec column-major (bvec[i + 3 j] = bvec(i+1, j+1),

@@ -207,6 +207,11 @@ module ocean_gpu_mod
       type(c_ptr), value :: ctx
       real(c_double), intent(in) :: ladder(*)
     end function
+    integer(c_int) function ocn_val_set_fxc(ctx, fxc) bind(C, name="ocn_val_set_fxc")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: fxc(*)
+    end function
     integer(c_int) function ocn_val_apply_H(ctx, in_r, in_i, out_r, out_i, flags, backwards) &
         bind(C, name="ocn_val_apply_H")
       import :: c_int, c_ptr, c_double

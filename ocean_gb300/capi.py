@@ -89,7 +89,8 @@ EXPORTS = [
     "ocn_val_set_energies", "ocn_val_set_allow", "ocn_val_set_states", "ocn_val_set_states_dev",
     "ocn_val_set_bubble", "ocn_val_set_ladder", "ocn_val_set_ladder_dev", "ocn_val_bubble_populate",
     "ocn_val_apply_H", "ocn_val_apply_H_dev", "ocn_val_haydock", "ocn_val_haydock_dev",
-    "ocn_val_spectrum", "ocn_val_optical_constants", "ocn_write_opcons",
+    "ocn_val_spectrum", "ocn_val_optical_constants", "ocn_write_opcons", "ocn_val_set_fxc",
+    "ocn_val_fxc_from_rho",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -656,6 +657,16 @@ def val_bubble(xmesh, bvec, qinb, celvol: float, nkpts: int):
     return out, ng.value
 
 
+def val_fxc_from_rho(rho, celvol: float, nkpts: int):
+    """OCEAN_fxc_prep's ALDA kernel on the x-mesh (host code of the library)."""
+    r = _f64(rho)
+    out = np.zeros(len(r))
+    rc = load().ocn_val_fxc_from_rho(len(r), _dp(r), C.c_double(celvol), int(nkpts), _dp(out))
+    if rc != 0:
+        raise OcnError(rc, val_last_error())
+    return out
+
+
 class ValContext:
     """One valence BSE problem on one GPU: the module state of OCEAN_val_states,
     OCEAN_val_energy, OCEAN_bubble and OCEAN_ladder, and the valence action."""
@@ -681,6 +692,9 @@ class ValContext:
             self._chk(lib.ocn_val_set_allow(self.ptr, _dp(_f64(w.allow))))
             self.bubble, self.ngvec = val_bubble(w.xmesh, w.bvec, w.qinb, w.celvol, w.nk)
             self._chk(lib.ocn_val_set_bubble(self.ptr, _dp(self.bubble)))
+            if getattr(w, "rho", None) is not None:
+                self.fxc = val_fxc_from_rho(w.rho, w.celvol, w.nk)
+                self._chk(lib.ocn_val_set_fxc(self.ptr, _dp(self.fxc)))
             if w.conr is not None:
                 self._chk(lib.ocn_val_set_states(self.ptr, _dp(_f64(w.conr)), _dp(_f64(w.coni)),
                                                  _dp(_f64(w.valr)), _dp(_f64(w.vali))))

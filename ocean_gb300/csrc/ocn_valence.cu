@@ -73,6 +73,8 @@ struct ocn_val_ctx {
   void* d_valT = nullptr;     // [y][v][k], double2 or float2
   void* d_lad = nullptr;      // [y][x][k], double or float
   double* d_bub = nullptr;    // [x]
+  double* d_fxc = nullptr;    // [x] ALDA kernel; set: the f_xc term is on (OCEAN_fxc_act)
+  bool have_fxc = false;
   double2* d_twk = nullptr;   // exp(+2 pi i t / n_axis) for the k-mesh, [axis][t]
   float2* d_twk32 = nullptr;
   double2* d_twx = nullptr;   // same for the x-mesh
@@ -254,14 +256,24 @@ __device__ __forceinline__ void xmesh_pass(const double2* __restrict__ in, doubl
 // s = FFT_fwd[ bubble o FFT_bwd[ l ] ] on the x-mesh, neither normalised
 // (OCEAN_bubble.f90:663-665; FFTW signs +1 backward, -1 forward,
 // Modules/FFT_wrapper.f90:24-25).  One CTA of 1024 threads, ping-pong buffers.
+// With fxc (the ALDA kernel, OCEAN_fxc_act, OCEAN_fxc.f90:250-253) the local
+// term fxc(x) l(x) is added to s; without use_x only that term is formed.
 __global__ void __launch_bounds__(1024) kv_bub_fft(double2* __restrict__ l, const double* __restrict__ bub,
-                                                   const int3 mesh, const double2* __restrict__ twg) {
+                                                   const double* __restrict__ fxc, int use_x, const int3 mesh,
+                                                   const double2* __restrict__ twg) {
   extern __shared__ double2 sm[];
   const int n[3] = {mesh.x, mesh.y, mesh.z};
   const int nx = n[0] * n[1] * n[2];
   double2* tw = sm;
   double2* b0 = sm + 3 * OCN_MAX_KDIM;
   double2* b1 = b0 + nx;
+  if (!use_x) {  // the local term alone; each x read and written by one thread
+    for (int x = threadIdx.x; x < nx; x += blockDim.x) {
+      const double2 v = l[x];
+      l[x] = make_double2(fxc[x] * v.x, fxc[x] * v.y);
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
   for (int x = threadIdx.x; x < nx; x += blockDim.x) b0[x] = l[x];
   __syncthreads();
@@ -282,7 +294,15 @@ __global__ void __launch_bounds__(1024) kv_bub_fft(double2* __restrict__ l, cons
   __syncthreads();
   xmesh_pass(b1, b0, n, 2, tw + 2 * OCN_MAX_KDIM, -1.0);
   __syncthreads();
-  for (int x = threadIdx.x; x < nx; x += blockDim.x) l[x] = b0[x];
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) {
+    double2 v = b0[x];
+    if (fxc) {  // l[x] still holds this thread's input value
+      const double2 u = l[x];
+      v.x += fxc[x] * u.x;
+      v.y += fxc[x] * u.y;
+    }
+    l[x] = v;
+  }
 }
 
 // Direct term for the x-point of this CTA and the y-range blockIdx.y
@@ -934,6 +954,7 @@ int check_ready(ocn_val_ctx* c, const int flags[3]) {
   if ((flags[1] || flags[2]) && !c->have_states) return vset_err(c, OCN_ERR_STATE, "ocn_val: states not set");
   if (flags[1] && !c->have_bubble) return vset_err(c, OCN_ERR_STATE, "ocn_val: bubble not set");
   if (flags[2] && !c->have_ladder) return vset_err(c, OCN_ERR_STATE, "ocn_val: ladder not set");
+  if (c->have_fxc && !c->have_states) return vset_err(c, OCN_ERR_STATE, "ocn_val: states not set");
   return OCN_OK;
 }
 
@@ -949,6 +970,8 @@ int apply_impl(ocn_val_ctx* c, const double* d_in, double* d_out, const int flag
   const size_t n = c->npsi, nb1 = c->nb1;
   const int vs = c->vspin, ns = c->nspn;
   const int use_e = flags[0], use_x = flags[1], use_d = flags[2];
+  const int use_f = c->have_fxc ? 1 : 0;  // aldaf: on whenever the kernel is set
+  const int use_l = use_x || use_f;       // the exchange-like terms need l(x)
   const size_t nxk = (size_t)c->nx * c->nk;
   const size_t lp_blk = (size_t)c->nx * ((c->nk + 7) / 8), bp_blk = nxk * c->nv * c->ysplit;
   CT* A = static_cast<CT*>(c->d_A);
@@ -963,7 +986,7 @@ int apply_impl(ocn_val_ctx* c, const double* d_in, double* d_out, const int flag
     for (int jc = 0; jc < vs; ++jc) {
       const int b = iv * vs + jc;
       const bool diag = iv == jc;
-      if (!(use_d || (use_x && diag))) continue;
+      if (!(use_d || (use_l && diag))) continue;
       const int sc = std::min(jc, ns - 1), sv = std::min(iv, ns - 1);
       // exchange partials of a same-spin block in slot iv; other blocks' go to the spare slot vs
       double2* lp = c->d_lp + (diag ? iv : vs) * lp_blk;
@@ -1004,11 +1027,12 @@ int apply_impl(ocn_val_ctx* c, const double* d_in, double* d_out, const int flag
         VCUDA(c, cudaGetLastError());
       }
     }
-  if (use_x) {
+  if (use_l) {
     kv_bub_reduce<<<(c->nx + 31) / 32, dim3(32, 32), 0, c->stream>>>(c->d_lp, vs * ((c->nk + 7) / 8), c->nx,
                                                                       c->d_s);
     kv_bub_fft<<<1, 1024, bub_fft_smem(c), c->stream>>>(
-        c->d_s, c->d_bub, make_int3(c->dims.xmesh[0], c->dims.xmesh[1], c->dims.xmesh[2]), c->d_twx);
+        c->d_s, c->d_bub, use_f ? c->d_fxc : nullptr, use_x,
+        make_int3(c->dims.xmesh[0], c->dims.xmesh[1], c->dims.xmesh[2]), c->d_twx);
     c->launches += 2;
     VCUDA(c, cudaGetLastError());
   }
@@ -1022,7 +1046,7 @@ int apply_impl(ocn_val_ctx* c, const double* d_in, double* d_out, const int flag
       kv_final<R><<<c->nk, VAL_THREADS, fsm, c->stream>>>(
           d_in + b * nb1, d_in + n + b * nb1, c->d_er + b * nb1, c->ei_nonzero ? c->d_ei + b * nb1 : nullptr,
           c->d_allow + b * nb1, con_s(sc), val_s(sv), c->d_s, Bp + b * bp_blk, c->ysplit, c->nc, c->nv, c->nk,
-          c->nx, xc, use_e, use_x && iv == jc, use_d, backwards, xpref, d_out + b * nb1, d_out + n + b * nb1);
+          c->nx, xc, use_e, use_l && iv == jc, use_d, backwards, xpref, d_out + b * nb1, d_out + n + b * nb1);
       ++c->launches;
       VCUDA(c, cudaGetLastError());
     }
@@ -1094,7 +1118,7 @@ int ocn_val_create(const ocn_val_dims* d, ocn_val_ctx** out) {
       (rc = valloc(c, &c->d_val, nxk * c->nv * c->nspn)) ||
       (rc = valloc(c, reinterpret_cast<char**>(&c->d_valT), nxk * c->nv * c->nspn * cs)) ||
       (rc = valloc(c, reinterpret_cast<char**>(&c->d_lad), nxk * c->nx * rs)) ||
-      (rc = valloc(c, &c->d_bub, c->nx)) || (rc = valloc(c, &c->d_twk, 3 * OCN_MAX_KDIM)) ||
+      (rc = valloc(c, &c->d_bub, c->nx)) || (rc = valloc(c, &c->d_fxc, c->nx)) || (rc = valloc(c, &c->d_twk, 3 * OCN_MAX_KDIM)) ||
       (rc = valloc(c, &c->d_twk32, 3 * OCN_MAX_KDIM)) || (rc = valloc(c, &c->d_twx, 3 * OCN_MAX_KDIM)) ||
       (rc = valloc(c, &c->d_lp, (size_t)(c->vspin + 1) * c->nx * ((c->nk + 7) / 8))) ||
       (rc = valloc(c, &c->d_s, c->nx)) || (rc = valloc(c, reinterpret_cast<char**>(&c->d_A), nxk * c->nv * cs)) ||
@@ -1143,7 +1167,7 @@ int ocn_val_destroy(ocn_val_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_er, c->d_ei, c->d_allow, c->d_con, c->d_val, c->d_con32, c->d_val32, c->d_valT, c->d_lad, c->d_bub,
-                  c->d_twk, c->d_twk32, c->d_twx, c->d_lp, c->d_s, c->d_A, c->d_Bp, c->d_vec, c->d_red,
+                  c->d_fxc, c->d_twk, c->d_twk32, c->d_twx, c->d_lp, c->d_s, c->d_A, c->d_Bp, c->d_vec, c->d_red,
                   c->d_coef};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -1190,6 +1214,23 @@ int ocn_val_set_bubble(ocn_val_ctx* c, const double* bubble) {
   if (int rc = upload(c, c->d_bub, bubble, sizeof(double) * c->nx)) return rc;
   VCUDA(c, cudaStreamSynchronize(c->stream));
   c->have_bubble = true;
+  return OCN_OK;
+}
+
+// OCEAN_fxc_prep's kernel (set by the caller, e.g. from ocn_val_fxc_from_rho);
+// NULL switches the f_xc term off.  One valence-Hamiltonian spin only, as
+// OCEAN_fxc_act (OCEAN_fxc.f90:154-159).
+int ocn_val_set_fxc(ocn_val_ctx* c, const double* fxc) {
+  if (!c) return vset_err(c, OCN_ERR_ARG, "null argument");
+  if (!fxc) {
+    c->have_fxc = false;
+    return OCN_OK;
+  }
+  if (c->vspin != 1) return vset_err(c, OCN_ERR_UNSUPPORTED, "ocn_val_set_fxc: f_xc needs valence_ham_spin = 1");
+  cudaSetDevice(c->device);
+  if (int rc = upload(c, c->d_fxc, fxc, sizeof(double) * c->nx)) return rc;
+  VCUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_fxc = true;
   return OCN_OK;
 }
 
@@ -1373,6 +1414,51 @@ int ocn_val_haydock(ocn_val_ctx* c, const double* psi0_r, const double* psi0_i, 
   if (int rc = upload(c, d0, psi0_r, sizeof(double) * n)) return rc;
   if (int rc = upload(c, d0 + n, psi0_i, sizeof(double) * n)) return rc;
   return ocn_val_haydock_dev(c, d0, niter, flags, real_a, imag_a, real_b, niter_done);
+}
+
+// Local-density exchange and correlation energies per electron of an
+// unpolarised, non-relativistic gas, as cacorr forms them (OCEAN_fxc.f90:333-470):
+// Slater exchange and the Ceperley-Alder correlation in the Perdew-Zunger
+// (Phys. Rev. B 23, 5048) parametrisation, zeta = 0.
+static void lda_energies(double n, double* ex, double* ec) {
+  if (n < 0.00000001) {
+    *ex = 0.0;
+    *ec = 0.0;
+    return;
+  }
+  const double pi = 3.1415926535897932384626433832795;
+  const double third = 1.0 / 3.0;
+  const double rs = std::pow(3.0 / (4.0 * pi * n), third);
+  const double spin_n = n / 2.0;                                   // each spin channel
+  const double e1 = -1.5 * std::pow(0.75 / pi, third) * std::pow(spin_n, third);
+  *ex = (spin_n * e1 + spin_n * e1) / n;
+  if (rs >= 1.0) {
+    *ec = -0.1423 / (1.0 + 1.0529 * std::sqrt(rs) + 0.3334 * rs);
+  } else {
+    const double lrs = std::log(rs);
+    *ec = 0.0311 * lrs + (-0.048) + 0.002 * (rs * lrs) + (-0.0116) * rs;
+  }
+}
+
+// OCEAN_fxc_prep (OCEAN_fxc.f90:35-123): f_xc(x) = second derivative of
+// n (ex + ec) at n = rho(x) by the five-point rule with step n/100, times
+// Nx / (Nk V).  rho in the x-mesh order (x3 fastest).  Host only.
+int ocn_val_fxc_from_rho(int nx, const double* rho, double celvol, int nkpts, double* fxc) {
+  if (nx < 1 || !rho || !fxc || nkpts < 1 || !(celvol > 0.0))
+    return vset_err(nullptr, OCN_ERR_ARG, "ocn_val_fxc_from_rho: bad argument");
+  for (int i = 0; i < nx; ++i) {
+    const double n = rho[i], dn = 0.01 * n;
+    const double pts[5] = {n + 2 * dn, n + dn, n, n - dn, n - 2 * dn};
+    double f[5];
+    for (int j = 0; j < 5; ++j) {
+      double ex, ec;
+      lda_energies(pts[j], &ex, &ec);
+      f[j] = pts[j] * (ex + ec);
+    }
+    fxc[i] = (16.0 * (f[3] + f[1]) - (f[4] + f[0]) - 30.0 * f[2]) / (12.0 * dn * dn) * (double)nx /
+             ((double)nkpts * celvol);
+  }
+  return OCN_OK;
 }
 
 // AI_bubble_populate with wall_search_old_way (OCEAN_bubble.f90:238-407).

@@ -321,6 +321,7 @@ class ValWorkload:
     device_arrays: dict = field(default_factory=dict)  # torch tensors when built on a device
     nspn: int = 1              # DFT spins of the states
     vspin: int = 1             # valence_ham_spin: psi has vspin^2 spin blocks
+    rho: Optional[np.ndarray] = None  # (Nx) valence density (electrons / Bohr^3); set: the f_xc term is on
 
     @property
     def nk(self) -> int:
@@ -400,7 +401,8 @@ def val_ladder(kmesh, xmesh, avec, celvol, epsilon0=4.0, width_angstrom=0.5, dev
 
 
 def make_val(name: str, seed: int = 0, nc: Optional[int] = None, nv: Optional[int] = None, kmesh=None,
-             xmesh=None, device: Optional[str] = None, nspn: int = 1, vspin: int = 1) -> ValWorkload:
+             xmesh=None, device: Optional[str] = None, nspn: int = 1, vspin: int = 1,
+             with_fxc: bool = False) -> ValWorkload:
     """Valence workloads: 'vtiny', 'vsmall' (oracle sizes), 'v2' (k-mesh 8^3,
     x-mesh 10^3, 8 conduction and 4 valence bands: the benchmark case).
     device: build the states and the ladder as torch tensors there (kept in
@@ -450,6 +452,10 @@ def make_val(name: str, seed: int = 0, nc: Optional[int] = None, nv: Optional[in
                     qinb=np.zeros(3), epsilon0=4.0, er=er, ei=ei, allow=allow, conr=None, coni=None,
                     valr=None, vali=None, ladder=None, psi_r=psi_r, psi_i=psi_i, kpref=kpref,
                     niter=p["niter"], nspn=nspn, vspin=vspin)
+    if with_fxc:  # a smooth density with the mean of 8 valence electrons per cell
+        f = _mesh_frac(xm)
+        shape = 1.0 + 0.5 * np.prod(np.cos(2.0 * math.pi * f), axis=1)
+        w.rho = 8.0 / celvol * shape / shape.mean()
     if device is None:
         st = np.empty((nspn, nk, ncb + nvb, nx), dtype=np.complex128)
         for sp in range(nspn):

@@ -148,7 +148,11 @@ typedef struct {
   const double* bubble;       /* (Nx) */
   const double* ladder;       /* (Nk, Nx, Nx) */
   int bande, bflag, lflag;    /* energies, exchange, screened direct */
+  const double* fxc;          /* (Nx) ALDA kernel, NULL = off (aldaf) */
 } or_val_ops;
+
+/* OCEAN_fxc_prep (OCEAN_fxc.f90:35-123) with cacorr (:333-470). */
+void or_val_fxc_from_rho(int nx, const double* rho, double celvol, int nkpts, double* fxc);
 
 /* wall_search_old_way (OCEAN_bubble.f90:238-297). */
 double or_val_wall_length(const int xmesh[3], const double bvec[9]);

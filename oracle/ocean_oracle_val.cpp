@@ -279,6 +279,49 @@ void or_val_ladder_slab(const or_val_dims* d, const or_val_ops* o, const double*
   val_project(d, o, -1.0, br, bi, outr, outi);
 }
 
+// cacorr (OCEAN_fxc.f90:333-470) for the unpolarised, non-relativistic gas it
+// is called with (xn1 = xn2 = n/2, rel = 0): Slater exchange per particle and
+// the Ceperley-Alder correlation in the Perdew-Zunger parametrisation (Phys.
+// Rev. B 23, 5048); zeta = 0 selects the unpolarised fit.
+static void lda_ex_ec(double n, double* ex, double* ec) {
+  const double pi = kPiV;
+  if (n < 0.00000001) {
+    *ex = 0.0;
+    *ec = 0.0;
+    return;
+  }
+  const double third = 1.0 / 3.0;
+  const double rs = std::pow(3.0 / (4.0 * pi * n), third);
+  const double half = n / 2.0;
+  const double ex1 = -1.5 * std::pow(0.75 / pi, third) * std::pow(half, third);
+  *ex = (half * ex1 + half * ex1) / n;
+  if (rs >= 1.0) {
+    const double rr = std::sqrt(rs);
+    *ec = -0.1423 / (1.0 + 1.0529 * rr + 0.3334 * rs);
+  } else {
+    const double lr = std::log(rs);
+    *ec = 0.0311 * lr + (-0.048) + 0.002 * (rs * lr) + (-0.0116) * rs;
+  }
+}
+
+// OCEAN_fxc_prep (OCEAN_fxc.f90:35-123): f_xc(x) = d^2[n (ex + ec)]/dn^2 by the
+// five-point rule with step dn = n/100, times Nx / (Nk V); rho in the x-mesh
+// order (x3 fastest, the rho(iz, iy, ix) loop).
+void or_val_fxc_from_rho(int nx, const double* rho, double celvol, int nkpts, double* fxc) {
+  for (int i = 0; i < nx; ++i) {
+    const double n = rho[i], dn = 0.01 * n;
+    const double ns[5] = {n + 2 * dn, n + dn, n, n - dn, n - 2 * dn};
+    double v[5];
+    for (int j = 0; j < 5; ++j) {
+      double ex, ec;
+      lda_ex_ec(ns[j], &ex, &ec);
+      v[j] = ns[j] * (ex + ec);
+    }
+    fxc[i] = (16.0 * (v[3] + v[1]) - (v[4] + v[0]) - 30.0 * v[2]) / (12.0 * dn * dn) * (double)nx /
+             ((double)nkpts * celvol);
+  }
+}
+
 // The operator data seen by one (valence spin, conduction spin) pair: con of
 // the conduction spin, val of the valence spin (DFT spin index = min(spin,
 // nspn), OCEAN_ladder.f90:118-133, OCEAN_bubble.f90:511-512).
@@ -326,6 +369,16 @@ int or_val_act(const or_val_dims* d, const or_val_ops* o, const double* pr, cons
       const size_t off = nb1 * (size_t)(js * vs + js);
       bubble_project(d, &v, pref, lr, li, kr.data() + off, ki.data() + off);
     }
+  }
+  if (o->fxc && vs == 1) {  // OCEAN_fxc_act (OCEAN_fxc.f90:127-322): phi = fxc l, spin_prefac 2
+    std::vector<double> lr(nx_of(d), 0.0), li(nx_of(d), 0.0);
+    const or_val_ops v = spin_view(d, o, 0, 0);
+    bubble_l(d, &v, qr.data(), qi.data(), lr, li);
+    for (int x = 0; x < nx_of(d); ++x) {
+      lr[x] *= o->fxc[x];
+      li[x] *= o->fxc[x];
+    }
+    bubble_project(d, &v, 2.0, lr, li, kr.data(), ki.data());
   }
   if (o->lflag)
     for (int iv = 0; iv < vs; ++iv)

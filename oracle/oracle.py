@@ -270,7 +270,14 @@ class OrValDims(C.Structure):
 class OrValOps(C.Structure):
     _fields_ = [("er", DP), ("ei", DP), ("allow", DP), ("conr", DP), ("coni", DP), ("valr", DP),
                 ("vali", DP), ("bubble", DP), ("ladder", DP), ("bande", C.c_int), ("bflag", C.c_int),
-                ("lflag", C.c_int)]
+                ("lflag", C.c_int), ("fxc", DP)]
+
+
+def val_fxc_from_rho(rho, celvol, nkpts):
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    out = np.zeros(len(rho))
+    lib().or_val_fxc_from_rho(len(rho), dptr(rho), C.c_double(celvol), int(nkpts), dptr(out))
+    return out
 
 
 def val_wall_length(xmesh, bvec) -> float:
@@ -309,6 +316,10 @@ class OracleVal:
         o = OrValOps()
         (o.er, o.ei, o.allow, o.conr, o.coni, o.valr, o.vali, o.bubble, o.ladder) = [dptr(a) for a in self._refs]
         o.bande, o.bflag, o.lflag = bande, bflag, lflag
+        self.fxc = None
+        if getattr(w, "rho", None) is not None:
+            self.fxc = val_fxc_from_rho(w.rho, w.celvol, w.nk)
+            o.fxc = dptr(self.fxc)
         self.o = o
 
     def act(self, pr, pi, backwards=False, flags=None):

@@ -196,3 +196,40 @@ def test_spin_blocks_match_oracle(built, nspn, vspin, prec):
             assert np.max(np.abs(ra[:10] - ora[:10]) / np.abs(ora[:10])) < 1e-12
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("prec", [capi.OCN_PREC_FP64, capi.OCN_PREC_MIXED])
+def test_fxc_term_matches_oracle(built, prec):
+    _, O = built
+    w = WL.make_val("vsmall", seed=41, with_fxc=True)
+    P = O.OracleVal(w)
+    ctx = capi.ValContext(w, precision=prec)
+    try:
+        rng = np.random.default_rng(4)
+        x = rng.standard_normal(w.npsi) + 1j * rng.standard_normal(w.npsi)
+        for flags in [(0, 0, 0), (0, 1, 0), (1, 1, 1)]:
+            gr, gi = ctx.apply_H(x.real, x.imag, flags=flags)
+            orr, oi = P.act(x.real, x.imag, flags=flags)
+            err = _rel(gr + 1j * gi, orr + 1j * oi)
+            tol = 1e-12 if prec == capi.OCN_PREC_FP64 else (1e-6 if flags == (1, 1, 1) else 1e-5)
+            assert err < tol, (flags, err)
+        import ctypes as C
+
+        ctx._chk(ctx.lib.ocn_val_set_fxc(ctx.ptr, None))  # off again: the exchange alone
+        gr, gi = ctx.apply_H(x.real, x.imag, flags=(0, 1, 0))
+        P0 = O.OracleVal(__import__("dataclasses").replace(w, rho=None))
+        orr, oi = P0.act(x.real, x.imag, flags=(0, 1, 0))
+        assert _rel(gr + 1j * gi, orr + 1j * oi) < (1e-12 if prec == capi.OCN_PREC_FP64 else 1e-5)
+    finally:
+        ctx.close()
+
+
+def test_fxc_refuses_two_spins(built):
+    w = WL.make_val("vtiny", seed=1, vspin=2)
+    ctx = capi.ValContext(w)
+    try:
+        with pytest.raises(capi.OcnError) as e:
+            ctx._chk(ctx.lib.ocn_val_set_fxc(ctx.ptr, capi._dp(np.ones(w.nx))))
+        assert e.value.code == 9962
+    finally:
+        ctx.close()

@@ -215,3 +215,31 @@ def test_oracle_singlet_reduces_to_one_spin_channel(oracle_lib):
     assert np.max(np.abs(H2[:nb1] - H1)) < 1e-13 * np.max(np.abs(H1))
     assert np.max(np.abs(H2[3 * nb1:] - H1)) < 1e-13 * np.max(np.abs(H1))
     assert np.max(np.abs(H2[nb1:3 * nb1])) == 0.0
+
+
+def test_fxc_kernel_matches_oracle_bit_for_bit(lib_built, oracle_lib):
+    """OCEAN_fxc_prep's ALDA kernel (five-point second derivative of n(ex + ec),
+    Perdew-Zunger correlation): library host code against the oracle."""
+    capi.load(lib_built)
+    O = oracle_lib
+    w = WL.make_val("vsmall", with_fxc=True)
+    rho = np.concatenate([w.rho, [1e-9, 0.003, 0.5, 3.0]])  # both sides of rs = 1 and the cutoff
+    a = capi.val_fxc_from_rho(rho[:-4].copy(), w.celvol, w.nk)
+    b = O.val_fxc_from_rho(rho[:-4].copy(), w.celvol, w.nk)
+    assert np.array_equal(a, b) and np.all(a < 0.0)
+    a2 = capi.val_fxc_from_rho(rho, w.celvol, w.nk)
+    b2 = O.val_fxc_from_rho(rho, w.celvol, w.nk)
+    assert np.array_equal(a2, b2)
+
+
+def test_oracle_fxc_term_is_hermitian(oracle_lib):
+    O = oracle_lib
+    w = WL.make_val("vodd", seed=2, with_fxc=True)
+    P = O.OracleVal(w)
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal(w.npsi) + 1j * rng.standard_normal(w.npsi)
+    y = rng.standard_normal(w.npsi) + 1j * rng.standard_normal(w.npsi)
+    hx, hy = P.act(x.real, x.imag, flags=(0, 0, 0)), P.act(y.real, y.imag, flags=(0, 0, 0))
+    lhs = np.vdot(y, hx[0] + 1j * hx[1])
+    rhs = np.conj(np.vdot(x, hy[0] + 1j * hy[1]))
+    assert abs(lhs) > 0 and abs(lhs - rhs) <= 1e-12 * abs(lhs)
