@@ -233,3 +233,35 @@ def test_fxc_refuses_two_spins(built):
         assert e.value.code == 9962
     finally:
         ctx.close()
+
+
+def test_state_and_argument_errors(built):
+    """Missing operator data and bad arguments return status codes (no abort)."""
+    import ctypes as C
+
+    lib, _ = built
+    w = WL.make_val("vtiny", seed=2)
+    d = capi.OcnValDims()
+    d.nc, d.nv = w.nc, w.nv
+    d.kmesh[:] = list(w.kmesh)
+    d.xmesh[:] = list(w.xmesh)
+    p = C.c_void_p()
+    assert lib.ocn_val_create(C.byref(d), C.byref(p)) == 0
+    try:
+        n = w.npsi
+        a = np.zeros(n)
+        flags = (C.c_int * 3)(1, 1, 1)
+        rc = lib.ocn_val_apply_H(p, capi._dp(a), capi._dp(a), capi._dp(a), capi._dp(a), flags, 0)
+        assert rc == capi.OCN_ERR_STATE and "not set" in capi.val_last_error(p)
+        assert lib.ocn_val_set_energies(p, None, None) == capi.OCN_ERR_ARG
+        assert lib.ocn_val_set_allow(p, capi._dp(np.ones(n))) == 0
+        only_e = (C.c_int * 3)(1, 0, 0)
+        rc = lib.ocn_val_apply_H(p, capi._dp(a), capi._dp(a), capi._dp(a), capi._dp(a), only_e, 0)
+        assert rc == capi.OCN_ERR_STATE  # energies still missing
+        ra, ia, rb = np.zeros(5), np.zeros(5), np.zeros(5)
+        done = C.c_int(0)
+        rc = lib.ocn_val_haydock(p, capi._dp(a), capi._dp(a), 0, flags, capi._dp(ra), capi._dp(ia), capi._dp(rb),
+                                 C.byref(done))
+        assert rc == capi.OCN_ERR_ARG
+    finally:
+        lib.ocn_val_destroy(p)
