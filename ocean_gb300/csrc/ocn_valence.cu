@@ -427,7 +427,7 @@ __device__ __forceinline__ void load_line(const CT* __restrict__ p, CT (&v)[N]) 
 // (k1 k2 line, v) pairs stay in registers across the whole y-range.
 // MAXC: (line, v) pairs per thread (N^2 nv <= MAXC * blockDim).
 template <typename R, int N, int MAXC, int X>
-__global__ void __launch_bounds__(VAL_THREADS, sizeof(R) == 4 ? (X == 1 ? 4 : 3) : 2)
+__global__ void __launch_bounds__(VAL_THREADS, (sizeof(R) == 4 && X == 1) ? 4 : 2)
     kv_ladder_cube(const typename C2<R>::T* __restrict__ A, const typename C2<R>::T* __restrict__ valT,
                    const R* __restrict__ lad, typename C2<R>::T* __restrict__ Bp, int nv, int nx, int ytile, int yper,
                    const typename C2<R>::T* __restrict__ twg) {
