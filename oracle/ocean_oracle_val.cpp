@@ -243,10 +243,13 @@ void or_val_ladder_slab(const or_val_dims* d, const or_val_ops* o, const double*
   std::vector<double> ar, ai;
   val_amat(d, o, pr, pi, ar, ai);
   std::vector<double> br((size_t)nx * nv * nk, 0.0), bi((size_t)nx * nv * nk, 0.0);
-  std::vector<double> tr(nk), ti(nk);
   const double inv_nk = 1.0 / (double)nk;
-  for (int y = y0; y < y1; ++y)
-    for (int x = 0; x < nx; ++x) {
+  // x-points split over threads (each thread owns B(x, ., .) of its x and adds
+  // the y in order, so the sums do not depend on the thread count)
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int x = 0; x < nx; ++x) {
+    std::vector<double> tr(nk), ti(nk);
+    for (int y = y0; y < y1; ++y) {
       for (int k = 0; k < nk; ++k) {
         double sr = 0.0, si = 0.0;
         for (int v = 0; v < nv; ++v) {
@@ -276,6 +279,7 @@ void or_val_ladder_slab(const or_val_dims* d, const or_val_ops* o, const double*
         }
       }
     }
+  }
   val_project(d, o, -1.0, br, bi, outr, outi);
 }
 
