@@ -443,6 +443,23 @@ int ocn_read_u2dat(const char* path, int nx, int ny, int nz, int nkpts, int nspn
  * *nptab is returned; otherwise up to cap samples (OCN_ERR_ARG if more). */
 int ocn_read_rpottrim(const char* path, int* nptab, double* ptab, double* rtab, int cap);
 
+/* val.u2.dat / con.u2.dat of a valence run (load_single_prefixu2dat,
+ * OCEAN_val_states.f90:421-560): stream access (no record markers), for each
+ * spin, k-point and file band [file_b0, file_b1] the complex(DP) state over
+ * the x-mesh with x1 fastest.  Bands band_lo .. band_lo + nb - 1 land in
+ * re / im(Nx, nb, nkpts, nspn) with x3 fastest: the layout ocn_val_set_states
+ * takes (val: brange(1), nbv; con: brange(3), nbc). */
+int ocn_read_val_u2(const char* path, const int xmesh[3], int nkpts, int nspn, int file_b0, int file_b1,
+                    int band_lo, int nb, double* re, double* im);
+/* Pair energies of a valence run (OCEAN_read_energies, OCEAN_val_energy.f90:
+ * 266-296, nbw = 1): out(Nc, Nv, Nk, vspin^2) = e_con(c + con_lo - 1, k, j-spin)
+ * - e_val(v + val_lo - 1, k, i-spin) from the wvfcninfo / wvfvainfo arrays
+ * (ncon_file / nval_file bands each, ocn_read_energies), 1-based band offsets
+ * (brange(3), brange(1)).  The Fermi-level, GW and allow steps of that routine
+ * are set-up left to the caller. */
+int ocn_val_pair_energies(int nc, int nv, int nkpts, int nspn, int vspin, const double* con_e, int ncon_file,
+                          int con_lo, const double* val_e, int nval_file, int val_lo, double* out);
+
 /* wvfcninfo / wvfvainfo (OCEAN_energies.f90:629-689): header (nbd, nq) or, with
  * two spins, (nbd, nq, nspn); then energies(nbd, nq, nspn) as written (the
  * pipeline's units; stubby, OCEAN_energies.f90:829-888, turns them into the

@@ -90,7 +90,7 @@ EXPORTS = [
     "ocn_val_set_bubble", "ocn_val_set_ladder", "ocn_val_set_ladder_dev", "ocn_val_bubble_populate",
     "ocn_val_apply_H", "ocn_val_apply_H_dev", "ocn_val_haydock", "ocn_val_haydock_dev",
     "ocn_val_spectrum", "ocn_val_optical_constants", "ocn_write_opcons", "ocn_val_set_fxc",
-    "ocn_val_fxc_from_rho",
+    "ocn_val_fxc_from_rho", "ocn_read_val_u2", "ocn_val_pair_energies",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -789,3 +789,19 @@ def val_optical_constants(omega_ha, eps_re, eps_im):
 def write_opcons(path: str, rows):
     r = _f64(np.asarray(rows).reshape(-1))
     check(load().ocn_write_opcons(path.encode(), len(r) // 8, _dp(r)))
+
+
+def read_val_u2(path: str, xmesh, nkpts: int, nspn: int, file_b0: int, file_b1: int, band_lo: int, nb: int):
+    """val.u2.dat / con.u2.dat -> (re, im) flat arrays in the ocn_val_set_states layout."""
+    n = int(np.prod(xmesh)) * nb * nkpts * nspn
+    re, im = np.zeros(n), np.zeros(n)
+    check(load().ocn_read_val_u2(path.encode(), (C.c_int * 3)(*xmesh), nkpts, nspn, file_b0, file_b1, band_lo, nb,
+                                 _dp(re), _dp(im)))
+    return re, im
+
+
+def val_pair_energies(nc, nv, nkpts, nspn, vspin, con_e, ncon_file, con_lo, val_e, nval_file, val_lo):
+    out = np.zeros(nc * nv * nkpts * vspin * vspin)
+    check(load().ocn_val_pair_energies(nc, nv, nkpts, nspn, vspin, _dp(_f64(con_e)), ncon_file, con_lo,
+                                       _dp(_f64(val_e)), nval_file, val_lo, _dp(out)))
+    return out

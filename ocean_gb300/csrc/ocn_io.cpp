@@ -538,6 +538,66 @@ int ocn_read_energies(const char* path, int nspn, int* nbd, int* nq, double* e, 
   return OCN_OK;
 }
 
+int ocn_read_val_u2(const char* path, const int xmesh[3], int nkpts, int nspn, int file_b0, int file_b1,
+                    int band_lo, int nb, double* re, double* im) {
+  if (!path || !xmesh || !re || !im || nkpts < 1 || nspn < 1 || nb < 1 || file_b1 < file_b0 ||
+      band_lo < file_b0 || band_lo + nb - 1 > file_b1)
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_read_val_u2: bad argument");
+  const int n1 = xmesh[0], n2 = xmesh[1], n3 = xmesh[2];
+  if (n1 < 1 || n2 < 1 || n3 < 1) return set_err(nullptr, OCN_ERR_ARG, "ocn_read_val_u2: bad mesh");
+  const size_t nx = (size_t)n1 * n2 * n3;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  // load_single_prefixu2dat (OCEAN_val_states.f90:421-560): stream access, for
+  // each spin, k-point and file band one complex(DP) array over the x-mesh with
+  // x1 fastest; bands outside [band_lo, band_lo + nb) are skipped; the arrays
+  // land in re_val / re_con(x, band, k, spin) with x3 fastest
+  std::vector<double> buf(2 * nx);
+  int rc = OCN_OK;
+  for (int sp = 0; sp < nspn && rc == OCN_OK; ++sp)
+    for (int k = 0; k < nkpts && rc == OCN_OK; ++k)
+      for (int b = file_b0; b <= file_b1 && rc == OCN_OK; ++b) {
+        if (std::fread(buf.data(), sizeof(double), 2 * nx, f) != 2 * nx) {
+          rc = set_err(nullptr, OCN_ERR_ARG, "val/con u2: file ends early");
+          break;
+        }
+        if (b < band_lo || b >= band_lo + nb) continue;
+        const size_t base = nx * ((size_t)(b - band_lo) + (size_t)nb * ((size_t)k + (size_t)nkpts * sp));
+        size_t ii = 0;
+        for (int iz = 0; iz < n3; ++iz)
+          for (int iy = 0; iy < n2; ++iy)
+            for (int ix = 0; ix < n1; ++ix, ++ii) {
+              const size_t x = (size_t)iz + (size_t)n3 * ((size_t)iy + (size_t)n2 * ix);
+              re[base + x] = buf[2 * ii];
+              im[base + x] = buf[2 * ii + 1];
+            }
+      }
+  std::fclose(f);
+  return rc;
+}
+
+int ocn_val_pair_energies(int nc, int nv, int nkpts, int nspn, int vspin, const double* con_e, int ncon_file,
+                          int con_lo, const double* val_e, int nval_file, int val_lo, double* out) {
+  if (nc < 1 || nv < 1 || nkpts < 1 || (nspn != 1 && nspn != 2) || (vspin != 1 && vspin != 2) || !con_e ||
+      !val_e || !out || con_lo < 1 || val_lo < 1 || con_lo + nc - 1 > ncon_file || val_lo + nv - 1 > nval_file)
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_val_pair_energies: bad argument");
+  // OCEAN_read_energies (OCEAN_val_energy.f90:266-296, nbw = 1): block ibeta
+  // pairs valence spin i with conduction spin j, E = e_c - e_v
+  size_t o = 0;
+  for (int i = 0; i < vspin; ++i) {
+    const int is = std::min(i, nspn - 1);
+    for (int j = 0; j < vspin; ++j) {
+      const int js = std::min(j, nspn - 1);
+      for (int k = 0; k < nkpts; ++k)
+        for (int v = 0; v < nv; ++v)
+          for (int c = 0; c < nc; ++c, ++o)
+            out[o] = con_e[(size_t)(c + con_lo - 1) + (size_t)ncon_file * ((size_t)k + (size_t)nkpts * js)] -
+                     val_e[(size_t)(v + val_lo - 1) + (size_t)nval_file * ((size_t)k + (size_t)nkpts * is)];
+    }
+  }
+  return OCN_OK;
+}
+
 int ocn_read_cks(const char* path, int stream, int nptot, int nb, int nkpts, int nspn, double* pcr, double* pci) {
   if (!path || !pcr || !pci || nptot < 1 || nb < 1 || nkpts < 1 || nspn < 1)
     return set_err(nullptr, OCN_ERR_ARG, "ocn_read_cks: bad argument");

@@ -174,3 +174,45 @@ def test_u2dat_feeds_the_library_layout(lib, tmp_path):
     _write_u2dat(p, vals, nx, ny, nz, nk, w.nspn, nb + 3, [1] * (nk * w.nspn), nb)
     re, im = capi.read_u2dat(p, nx, ny, nz, nk, w.nspn, nb + 3, 1, nb)
     assert np.array_equal(re.ravel(), w.ur) and np.array_equal(im.ravel(), w.ui)
+
+
+# ---- valence run files
+
+def test_val_u2_stream_file_layout_and_band_window(lib_built, tmp_path):
+    """val.u2.dat / con.u2.dat (load_single_prefixu2dat): x1 fastest in the file,
+    x3 fastest in the arrays; bands outside the window skipped; spins outer."""
+    capi.load(lib_built)
+    rng = np.random.default_rng(3)
+    xm, nk, nspn, fb0, fb1 = (2, 3, 4), 5, 2, 1, 6
+    nx = int(np.prod(xm))
+    data = rng.standard_normal((nspn, nk, fb1 - fb0 + 1, nx)) + 1j * rng.standard_normal((nspn, nk, fb1 - fb0 + 1, nx))
+    path = str(tmp_path / "con.u2.dat")
+    data.astype(np.complex128).tofile(path)  # stream access: no record markers
+    lo, nb = 3, 3
+    re, im = capi.read_val_u2(path, xm, nk, nspn, fb0, fb1, lo, nb)
+    got = (re + 1j * im).reshape(nspn, nk, nb, nx)
+    for s in range(nspn):
+        for k in range(nk):
+            for b in range(nb):
+                f = data[s, k, b + lo - fb0].reshape(xm[2], xm[1], xm[0])  # (iz, iy, ix), x1 fastest
+                want = np.transpose(f, (2, 1, 0)).reshape(-1)             # x3 fastest
+                assert np.array_equal(got[s, k, b], want)
+    with open(str(tmp_path / "short"), "wb") as fh:
+        fh.write(data.astype(np.complex128).tobytes()[:-16])
+    with pytest.raises(capi.OcnError):
+        capi.read_val_u2(str(tmp_path / "short"), xm, nk, nspn, fb0, fb1, lo, nb)
+
+
+def test_val_pair_energies_blocks(lib_built):
+    capi.load(lib_built)
+    rng = np.random.default_rng(4)
+    nk, nspn = 4, 2
+    ec = rng.uniform(0, 1, (nspn, nk, 10))   # (spin, k, band): Fortran e(band, k, spin)
+    ev = rng.uniform(-1, 0, (nspn, nk, 7))
+    nc, nv, clo, vlo = 3, 2, 5, 4
+    out = capi.val_pair_energies(nc, nv, nk, nspn, 2, ec.reshape(-1), 10, clo, ev.reshape(-1), 7, vlo)
+    out = out.reshape(4, nk, nv, nc)
+    for i in range(2):
+        for j in range(2):
+            want = ec[j][:, None, clo - 1:clo - 1 + nc] - ev[i][:, vlo - 1:vlo - 1 + nv, None]
+            assert np.array_equal(out[i * 2 + j], want)
