@@ -900,6 +900,8 @@ int plan_ladder(ocn_val_ctx* c) {
   // two and 110 KB); in FP64 two x-points spill registers (85 -> 104 ms), so one
   c->xper = (use_cube_kernel(c) && c->nx >= 2 && sizeof(R) == 4) ? 2 : 1;
   const size_t target = std::min<size_t>(c->smem_optin, 110 * 1024);
+  // two x-points' A must fit with at least a one-y tile, else one x-point per CTA
+  if (c->xper == 2 && ladder_smem<R>(c, 1) > c->smem_optin) c->xper = 1;
   while (ytile > 1 && ladder_smem<R>(c, ytile) > target) --ytile;
   if (ladder_smem<R>(c, ytile) > c->smem_optin)
     return vset_err(c, OCN_ERR_UNSUPPORTED,

@@ -265,3 +265,25 @@ def test_state_and_argument_errors(built):
         assert rc == capi.OCN_ERR_ARG
     finally:
         lib.ocn_val_destroy(p)
+
+
+def test_many_valence_bands_on_a_cubic_mesh(built):
+    """Nv = 16 on the 8^3 k-mesh: more (line, v) pairs than the cubic kernel
+    keeps in registers, so the generic direct-term kernel runs (A and B sums of
+    one x-point in shared memory, 131 KB in FP32) -- same results; in FP64 that
+    is 262 KB: OCN_ERR_UNSUPPORTED at creation."""
+    _, O = built
+    w = WL.make_val("vtiny", seed=51, nc=4, nv=16, kmesh=(8, 8, 8), xmesh=(4, 3, 2))
+    P = O.OracleVal(w)
+    ctx = capi.ValContext(w, precision=capi.OCN_PREC_MIXED)
+    try:
+        rng = np.random.default_rng(8)
+        x = rng.standard_normal(w.npsi) + 1j * rng.standard_normal(w.npsi)
+        gr, gi = ctx.apply_H(x.real, x.imag, flags=(0, 0, 1))
+        orr, oi = P.act(x.real, x.imag, flags=(0, 0, 1))
+        assert _rel(gr + 1j * gi, orr + 1j * oi) < 1e-5
+    finally:
+        ctx.close()
+    with pytest.raises(capi.OcnError) as e:
+        capi.ValContext(w, precision=capi.OCN_PREC_FP64)
+    assert e.value.code == 9962 and "shared memory" in str(e.value)
