@@ -243,3 +243,25 @@ def test_oracle_fxc_term_is_hermitian(oracle_lib):
     lhs = np.vdot(y, hx[0] + 1j * hx[1])
     rhs = np.conj(np.vdot(x, hy[0] + 1j * hy[1]))
     assert abs(lhs) > 0 and abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_valence_host_entry_points_reject_bad_arguments(lib_built, tmp_path):
+    """Host-side valence entry points return OCN_ERR_ARG instead of aborting."""
+    import ctypes as C
+
+    lib = capi.load(lib_built)
+    out = np.zeros(64)
+    bvec = (C.c_double * 9)(*([1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0]))
+    q = (C.c_double * 3)(0, 0, 0)
+    assert lib.ocn_val_bubble_populate((C.c_int * 3)(4, 4, 4), bvec, q, C.c_double(-1.0), 8, capi._dp(out),
+                                       None) == capi.OCN_ERR_ARG
+    assert lib.ocn_val_bubble_populate((C.c_int * 3)(4, 0, 4), bvec, q, C.c_double(1.0), 8, capi._dp(out),
+                                       None) == capi.OCN_ERR_ARG
+    with pytest.raises(capi.OcnError):
+        capi.val_pair_energies(2, 2, 1, 1, 1, np.zeros(3), 3, 3, np.zeros(3), 3, 1)  # conduction window past the file
+    with pytest.raises(capi.OcnError):
+        capi.val_fxc_from_rho(np.ones(4), -1.0, 8)
+    with pytest.raises(capi.OcnError):
+        capi.read_val_u2(str(tmp_path / "missing"), (2, 2, 2), 1, 1, 1, 2, 1, 2)
+    assert lib.ocn_val_optical_constants(-1, None, None, None, None) == capi.OCN_ERR_ARG
+    assert lib.ocn_write_opcons(str(tmp_path / "x").encode(), 1, None) == capi.OCN_ERR_ARG
