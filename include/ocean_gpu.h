@@ -303,6 +303,9 @@ int ocn_spectrum_cf_bc(const double* real_a, const double* imag_a, const double*
  * 3*(OCN_CF_NOALLOC_MAX_ITER+1) + 10*(OCN_CF_NOALLOC_MAX_NE+1) doubles (736 KiB).
  * Runs on the calling thread's current device; the first call on a device looks
  * up that array's address (set-up), so make it before any stream capture.
+ * The address is kept for the life of the process: do not call this entry
+ * point on a device after cudaDeviceReset (the module may be reloaded at
+ * another address).
  * iter > OCN_CF_NOALLOC_MAX_ITER, ne > OCN_CF_NOALLOC_MAX_NE and Voigt broadening
  * (gam_gauss > gam0/10) return OCN_ERR_ARG.  Nothing must be zeroed first.  Calls
  * that overlap on one device share the array and race: serialise them.  Same
@@ -509,6 +512,14 @@ long long ocn_kernel_launches(const ocn_ctx* ctx);
 int ocn_autotune(ocn_ctx* ctx, int nv, int reps, double* best_ms, double* current_ms, int tiles[7]);
 int ocn_set_tiles(ocn_ctx* ctx, const int tiles[7]);
 int ocn_get_tiles(const ocn_ctx* ctx, int tiles[7]);
+
+/* Test hook for the bounded waits of the tensor-core contractions (no
+ * counterpart in the reference).  on = 1: the long-range contractions' load
+ * warp issues no loads, so the MMA warp's first bounded wait (about 1 s) runs
+ * out with no copy or MMA in flight; the kernel records it, frees its tensor
+ * memory and returns, and the call reports OCN_ERR_TIMEOUT.  on = 0 restores
+ * normal operation; the context stays usable.  Mixed precision only. */
+int ocn_test_starve_tc(ocn_ctx* ctx, int on);
 
 /* Per-kernel device timing with CUDA events recorded on the context stream
  * (replaces the wall-clock buckets of OCEAN_timekeeper, OCEAN_timekeeper.f90:13-168).

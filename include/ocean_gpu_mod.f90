@@ -1,7 +1,7 @@
 ! ocean_gpu_mod.f90 -- iso_c_binding interface to libocean_gpu.so for ocean.x.
 !
 ! A maintainer adds this module to OCEAN2/ and calls the wrappers from
-! OCEAN_action.f90 / OCEAN_haydock.f90 / OCEAN_gmres.f90 (see INTEGRATION.md).
+! OCEAN_action.f90 / OCEAN_haydock.f90 / OCEAN_gmres.f90 in place of the CPU calls.
 ! Not compiled in this repository (no Fortran compiler here); the C ABI it binds
 ! is tested from C/Python.
 module ocean_gpu_mod

@@ -90,7 +90,7 @@ EXPORTS = [
     "ocn_val_set_bubble", "ocn_val_set_ladder", "ocn_val_set_ladder_dev", "ocn_val_bubble_populate",
     "ocn_val_apply_H", "ocn_val_apply_H_dev", "ocn_val_haydock", "ocn_val_haydock_dev",
     "ocn_val_spectrum", "ocn_val_optical_constants", "ocn_write_opcons", "ocn_val_set_fxc",
-    "ocn_val_fxc_from_rho", "ocn_read_val_u2", "ocn_val_pair_energies",
+    "ocn_val_fxc_from_rho", "ocn_read_val_u2", "ocn_val_pair_energies", "ocn_test_starve_tc",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -308,6 +308,11 @@ class Context:
 
     def timing(self, on: bool = True):
         self._chk(self.lib.ocn_timing_enable(self.ptr, int(on)))
+
+    def starve_tc(self, on: bool = True):
+        """Test hook: the tensor-core contractions' load warp issues nothing, so
+        their bounded waits run out and calls report OCN_ERR_TIMEOUT."""
+        self._chk(self.lib.ocn_test_starve_tc(self.ptr, int(on)))
 
     def timing_reset(self):
         self._chk(self.lib.ocn_timing_reset(self.ptr))

@@ -165,6 +165,16 @@ int ocn_set_tiles(ocn_ctx* c, const int tiles[7]) {
   return mixed_configure(c, tiles);
 }
 
+int ocn_test_starve_tc(ocn_ctx* c, int on) {
+  if (!c) return OCN_ERR_ARG;
+  if (c->dims.precision != OCN_PREC_MIXED || !c->mixed)
+    return set_err(c, OCN_ERR_UNSUPPORTED, "ocn_test_starve_tc: mixed-precision contexts only");
+  cudaSetDevice(c->device);
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+  drop_haydock_graph(c);  // a captured graph holds the launch parameters
+  return mixed_set_starve(c, on);
+}
+
 int ocn_get_tiles(const ocn_ctx* c, int tiles[7]) {
   if (!c || !tiles) return OCN_ERR_ARG;
   return c->mixed ? mixed_config(c, tiles) : OCN_ERR_UNSUPPORTED;

@@ -429,7 +429,10 @@ constexpr size_t kNaDoubles = 3 * kNaCoef + 10 * kNaRows;  // 94,221 doubles = 7
 static __device__ __align__(256) double g_cf_scratch[kNaDoubles];
 
 // Device address of g_cf_scratch per device, looked up once with that device
-// current (the first call on a device does the set-up).
+// current (the first call on a device does the set-up).  The cached address
+// belongs to the device's primary context as it was at set-up; after
+// cudaDeviceReset the module may load at another address, so the entry point
+// is not to be used on a device after a reset (stated in the header).
 constexpr int kNaMaxDevices = 64;
 std::atomic<double*> g_cf_scratch_ptr[kNaMaxDevices] = {};
 

@@ -320,6 +320,7 @@ int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vst
 int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rstride, double* h,
                     double* rb, size_t cstride, const int* itp);
 int mixed_check(ocn_ctx* c);       // reads and clears the device timeout flag
+int mixed_set_starve(ocn_ctx* c, int on);  // test hook of ocn_test_starve_tc
 // multiplet on the tensor cores: operands from c->mult (after ocn_set_mult), and
 // the action's multiplet term of nv vectors into its d_accpart slices
 int mixed_set_mult(ocn_ctx* c);

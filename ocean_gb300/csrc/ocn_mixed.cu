@@ -74,6 +74,8 @@ struct TcParams {
   int koff;      // added to k for the A operand: spin s of a spin-polarised problem at s*Nk
   int spin;      // -1: write every alpha; 0/1: only alpha with alpha mod 2 == spin
   int estg;      // launch-wide: mode-1 outputs staged per warp in shared memory, stored coalesced
+  int starve;    // launch-wide test hook: the producer issues no loads, so the MMA warp's
+                 // first bounded wait runs out with nothing in flight (OCN_ERR_TIMEOUT path)
 };
 
 // Tensor maps of a group launch (kernel parameter space, 384 bytes per problem).
@@ -276,7 +278,7 @@ __device__ __forceinline__ void lr_tc_body(const TcParams& p, const Src& src) {
       int armed_phase[TC_MAX_STAGES];
       for (int s = 0; s < TC_MAX_STAGES; ++s) armed_phase[s] = -1;
       bool ok = true;
-      for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
+      for (int t = blockIdx.x; t < p.ntiles && ok && !p.starve; t += gridDim.x) {
         int lt;
         const int ii = src.inst(t, &lt);
         const TcParams& tp = src.par(ii);
@@ -1316,6 +1318,13 @@ int mixed_set_bloch(ocn_ctx* c) {
   c->launches += 1;
   OCN_CUDA(c, cudaStreamSynchronize(c->stream));
   m->ready = true;
+  return OCN_OK;
+}
+
+int mixed_set_starve(ocn_ctx* c, int on) {
+  MixedLR* m = c->mixed;
+  if (!m || !m->ready) return set_err(c, OCN_ERR_STATE, "mixed-precision operands not built");
+  m->g1.starve = m->g2.starve = on ? 1 : 0;
   return OCN_OK;
 }
 

@@ -889,6 +889,20 @@ LadderFn<R> ladder_fn(const ocn_val_ctx* c) {
   return kv_ladder<R, 0>;
 }
 
+// The dynamic shared-memory limit of a kernel is process-wide state of the
+// device, shared by every context. It is raised once to the device's opt-in
+// maximum (less the kernel's static shared memory) and never lowered, so a
+// context created later with smaller sizes cannot take room away from an
+// earlier, larger one; each launch still asks only for what it needs.
+cudaError_t raise_smem_limit(const void* fn, size_t optin) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, fn);
+  if (e != cudaSuccess) return e;
+  const size_t room = optin > a.sharedSizeBytes ? optin - a.sharedSizeBytes : 0;
+  if ((size_t)a.maxDynamicSharedSizeBytes >= room) return cudaSuccess;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)room);
+}
+
 // y-tile from the shared-memory budget (two CTAs per SM where it fits), and
 // enough y-ranges per x-point for about two waves of CTAs.
 template <typename R>
@@ -910,7 +924,7 @@ int plan_ladder(ocn_val_ctx* c) {
   c->lad_smem = ladder_smem<R>(c, ytile);
   const bool cube = use_cube_kernel(c);
   const void* fn = cube ? (const void*)ladder_cube_fn<R>(c) : (const void*)ladder_fn<R>(c);
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c->lad_smem);
+  cudaError_t e = raise_smem_limit(fn, c->smem_optin);
   if (e != cudaSuccess) return vcuda(c, e, "cudaFuncSetAttribute(kv_ladder)");
   int per_sm = 1;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, VAL_THREADS, c->lad_smem);
@@ -1143,20 +1157,16 @@ int ocn_val_create(const ocn_val_dims* d, ocn_val_ctx** out) {
   cudaMemsetAsync(c->d_ei, 0, sizeof(double) * c->npsi, c->stream);
   if (bub_fft_smem(c) > c->smem_optin)
     return fail(vset_err(c, OCN_ERR_UNSUPPORTED, "ocn_val_create: x-mesh too large for the exchange transform"));
-  if (bub_fft_smem(c) > 48 * 1024) {
-    e = cudaFuncSetAttribute(kv_bub_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bub_fft_smem(c));
-    if (e != cudaSuccess) return fail(vcuda(c, e, "cudaFuncSetAttribute(kv_bub_fft)"));
-  }
+  e = raise_smem_limit((const void*)kv_bub_fft, c->smem_optin);
+  if (e != cudaSuccess) return fail(vcuda(c, e, "cudaFuncSetAttribute(kv_bub_fft)"));
   // dynamic + 4 KB static above the default 48 KB: Nv > 22, the 32-wide instantiation
-  if (sizeof(double2) * 8 * VAL_CC * c->nv + 4096 > 48 * 1024 && !c->mixed) {
-    e = cudaFuncSetAttribute(kv_amat<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(sizeof(double2) * 8 * VAL_CC * c->nv));
-    if (e != cudaSuccess) return fail(vcuda(c, e, "cudaFuncSetAttribute(kv_amat)"));
-  }
+  if (sizeof(double2) * 8 * VAL_CC * c->nv + 4096 > c->smem_optin && !c->mixed)
+    return fail(vset_err(c, OCN_ERR_UNSUPPORTED, "ocn_val_create: Nv too large for the pair contraction"));
+  e = raise_smem_limit((const void*)kv_amat<double, 32>, c->smem_optin);
+  if (e != cudaSuccess) return fail(vcuda(c, e, "cudaFuncSetAttribute(kv_amat)"));
   const size_t fsm = final_smem(c);
   if (fsm > c->smem_optin) return fail(vset_err(c, OCN_ERR_UNSUPPORTED, "ocn_val_create: Nc*Nv too large"));
-  e = cudaFuncSetAttribute(c->mixed ? (const void*)kv_final<float> : (const void*)kv_final<double>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
+  e = raise_smem_limit(c->mixed ? (const void*)kv_final<float> : (const void*)kv_final<double>, c->smem_optin);
   if (e != cudaSuccess) return fail(vcuda(c, e, "cudaFuncSetAttribute(kv_final)"));
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return fail(vcuda(c, e, "ocn_val_create"));

@@ -11,14 +11,17 @@ Text fixtures (verbatim bytes, for the byte-compatibility tests of the writers):
   cu_abslanc_01.txt       : abslanc_Cu.0001_1s_01 whole
   cu_absspct_01_rows.txt  : absspct_Cu.0001_1s_01, its two header records and
                             the same kept rows
-Run from the repository root: python tests/golden/make_golden.py [reference_root]
+Run from the repository root: python tests/golden/make_golden.py <reference_root>
+(the root of an OCEAN v3.2.1 source tree).
 """
 import os
 import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_golden.py <reference_root>")
+REF = sys.argv[1]
 RES = os.path.join(REF, "EXAMPLE", "Cu_TwoPhoton", "Results")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cu_twophoton_kat.npz")
 

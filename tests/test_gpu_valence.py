@@ -287,3 +287,26 @@ def test_many_valence_bands_on_a_cubic_mesh(built):
     with pytest.raises(capi.OcnError) as e:
         capi.ValContext(w, precision=capi.OCN_PREC_FP64)
     assert e.value.code == 9962 and "shared memory" in str(e.value)
+
+
+@pytest.mark.parametrize("prec", [capi.OCN_PREC_FP64, capi.OCN_PREC_MIXED])
+def test_smaller_context_keeps_larger_one_working(built, prec):
+    """Kernel shared-memory limits are process-wide: a small context created
+    while a large one is alive must not shrink them under the large one."""
+    _, O = built
+    big = WL.make_val("vsmall", seed=21, nv=4, kmesh=(8, 8, 8))
+    small = WL.make_val("vtiny", seed=22)
+    cb = capi.ValContext(big, precision=prec)
+    try:
+        r1 = cb.apply_H(big.psi_r, big.psi_i)
+        cs = capi.ValContext(small, precision=prec)
+        try:
+            cs.apply_H(small.psi_r, small.psi_i)
+            r2 = cb.apply_H(big.psi_r, big.psi_i)
+        finally:
+            cs.close()
+        assert np.array_equal(r1[0], r2[0]) and np.array_equal(r1[1], r2[1])
+        orr, oi = O.OracleVal(big).act(big.psi_r, big.psi_i)
+        assert _rel(r2[0] + 1j * r2[1], orr + 1j * oi) < (1e-12 if prec == capi.OCN_PREC_FP64 else 1e-6)
+    finally:
+        cb.close()
