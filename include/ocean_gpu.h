@@ -332,13 +332,28 @@ typedef struct {
 /* OCEAN_gmres_do_recycle (OCEAN_gmres.f90:508-908) with update_gmres (:241-344),
  * make_recycle (:207-239), set_initial_vector (:1213-1283) and
  * OCEAN_psi_min_set_prec (OCEAN_psi.f90:2907-2994).  hay_vec is the normalised
- * psi0 (host planes); energies[nomega] in eV as in bse.in.  For each energy writes
+ * psi0 (host planes); energies[nomega] in eV as in bse.in.  The recycled P
+ * updates at a new energy run as one P x P projection built from Gram matrices
+ * of the basis kept across energies (equal in exact arithmetic).  Mixed-
+ * precision contexts form the Gram dots and basis updates in double-float
+ * (binary32 pairs, 48-bit significands); the solve stays FP64.  Writes, per energy,
  *   out_re[i] = 1 - Re<b|x>*kpref, out_im[i] = -Im<b|x>*kpref,
  *   rel_err[i] = -|g|^2/Im<b|x>, iters[i] = complete_iter
  * (the abs.gmres columns, OCEAN_gmres.f90:864-869).  Any output may be NULL. */
 int ocn_gmres(ocn_ctx* ctx, const double* hay_r, const double* hay_i, double kpref,
               const double* energies_ev, int nomega, const ocn_gmres_params* p,
               double* out_re, double* out_im, double* rel_err, int* iters);
+
+/* Energy lanes of the GMRES sweep of this context (no counterpart in the
+ * reference; default 1 = its single sweep, OCEAN_gmres.f90:613-884).  With
+ * nlanes > 1, ocn_gmres, ocn_gmres_dev and ocn_gmres_vjp split the energy list
+ * into nlanes contiguous chunks; each chunk is the reference's recycled sweep
+ * from x = 0 at its first energy, and the chunks advance together so that one
+ * block action (ocn_apply_H_block; up to nvec vectors per launch set on
+ * mixed-precision contexts) serves all of them.  Results agree with the single
+ * sweep within the convergence tolerance; iteration counts differ.  nlanes in
+ * 1..64, else OCN_ERR_ARG. */
+int ocn_gmres_set_lanes(ocn_ctx* ctx, int nlanes);
 
 /* Same with psi0 in device memory (d_hay: real plane then imaginary plane, npsi
  * each).  d_x (device, may be NULL) receives the solution x of every energy:

@@ -26,6 +26,7 @@ SOURCES = {
     "ocn_capi.cu": [],
     "ocn_kernels.cu": [],
     "ocn_cf.cu": ["-fmad=false"],
+    "ocn_gmres.cu": [],
     "ocn_mixed.cu": [],
     "ocn_valence.cu": [],
     "ocn_setup.cpp": [],

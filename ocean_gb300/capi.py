@@ -91,6 +91,7 @@ EXPORTS = [
     "ocn_val_apply_H", "ocn_val_apply_H_dev", "ocn_val_haydock", "ocn_val_haydock_dev",
     "ocn_val_spectrum", "ocn_val_optical_constants", "ocn_write_opcons", "ocn_val_set_fxc",
     "ocn_val_fxc_from_rho", "ocn_read_val_u2", "ocn_val_pair_energies", "ocn_test_starve_tc",
+    "ocn_gmres_set_lanes",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -426,6 +427,10 @@ class Context:
         p.convergence = tol
         p.max_restarts = max_restarts
         return p
+
+    def set_gmres_lanes(self, nlanes: int):
+        """Energy lanes of the GMRES sweeps of this context (1: the reference's single sweep)."""
+        self._chk(self.lib.ocn_gmres_set_lanes(self.ptr, int(nlanes)))
 
     def gmres_dev(self, d_hay: int, energies_ev, depth=80, resolution=None, preconditioner=None, tol=1e-6,
                   max_restarts=50, kpref=None, d_x: int = 0):

@@ -52,6 +52,8 @@ int require(ocn_ctx* c) {
   return OCN_OK;
 }
 
+}  // namespace
+
 // H*psi on device vectors (OCEAN_xact, OCEAN_action.f90:286-618).
 int apply_H_impl(ocn_ctx* c, const double* ir, const double* ii, double* orr, double* oi,
                  const int* hflag_in, int backwards) {
@@ -85,7 +87,7 @@ int apply_H_impl(ocn_ctx* c, const double* ir, const double* ii, double* orr, do
 // the Bloch functions once for the block; the FP64 path acts vector by vector.
 // back_each (may be NULL): the backwards switch of each vector (H or H^dagger).
 int apply_H_block_impl(ocn_ctx* c, int nv, const double* in, double* out, const int* hflag_in,
-                       int backwards, const int* back_each = nullptr) {
+                       int backwards, const int* back_each) {
   const size_t n = c->npsi;
   if (nv < 1 || nv > c->nvec) return set_err(c, OCN_ERR_ARG, "block size must be in 1..nvec");
   if (c->dims.precision != OCN_PREC_MIXED) {
@@ -122,7 +124,6 @@ int apply_H_block_impl(ocn_ctx* c, int nv, const double* in, double* out, const 
   return rc;
 }
 
-}  // namespace
 }  // namespace ocn
 
 using namespace ocn;
@@ -1270,288 +1271,58 @@ int ocn_redtrid(int n, const double* real_a, const double* real_b, double* w) {
   return redtrid_eigs(n, real_a, real_b, w) ? OCN_ERR_SOLVE : OCN_OK;
 }
 
-// ------------------------------------------------------------------- GMRES
-
-namespace {
-
-// Cholesky factor L (L L^H = C) of the Hermitian positive-definite Gram matrix
-// C_ij = <au_i|au_j>, grown one row at a time: update_gmres appends row cur-1
-// of C on each call (OCEAN_gmres.f90:262-300) and restarts from row 0 whenever
-// the basis changes, so rows 0..cur-2 of L stay valid.  Each entry follows
-// L_ij = (C_ij - sum_{k<j} L_ik conj(L_jk)) / L_jj with k ascending, the same
-// arithmetic as a full factorisation.
-struct GramCholesky {
-  typedef std::complex<double> cd;
-  int depth = 0;
-  std::vector<cd> L;  // row-major depth x depth, lower
-  void init(int d) {
-    depth = d;
-    L.assign((size_t)d * d, cd(0.0, 0.0));
-  }
-  // up: packed upper triangle of C (C_ij, i <= j, at i + j(j+1)/2)
-  int add_row(int i, const std::vector<cd>& up) {
-    cd* Li = L.data() + (size_t)i * depth;
-    for (int j = 0; j < i; ++j) {
-      cd v = std::conj(up[(size_t)j + (size_t)i * (i + 1) / 2]);  // C_ij, i > j
-      const cd* Lj = L.data() + (size_t)j * depth;
-      for (int k = 0; k < j; ++k) v -= Li[k] * std::conj(Lj[k]);
-      Li[j] = v / Lj[j].real();
-    }
-    double d = up[(size_t)i + (size_t)i * (i + 1) / 2].real();
-    for (int k = 0; k < i; ++k) d -= std::norm(Li[k]);
-    if (!(d > 0.0)) return i + 1;
-    Li[i] = std::sqrt(d);
-    return 0;
-  }
-  // C x = b with the first n rows of L
-  void solve(int n, std::vector<cd>& b) const {
-    for (int i = 0; i < n; ++i) {  // L y = b
-      cd s = b[i];
-      for (int k = 0; k < i; ++k) s -= L[(size_t)i * depth + k] * b[k];
-      b[i] = s / L[(size_t)i * depth + i].real();
-    }
-    for (int i = n - 1; i >= 0; --i) {  // L^H x = y
-      cd s = b[i];
-      for (int k = i + 1; k < n; ++k) s -= std::conj(L[(size_t)k * depth + i]) * b[k];
-      b[i] = s / L[(size_t)i * depth + i].real();
-    }
-  }
-};
-
-struct Gmres {
-  ocn_ctx* c;
-  size_t n;
-  int depth;
-  std::vector<double*> u, au;
-  double** d_ul = nullptr;
-  double** d_aul = nullptr;
-  double* d_part = nullptr;
-  double* d_out = nullptr;
-  double2* d_coef = nullptr;
-  std::vector<std::complex<double>> cmat;
-  GramCholesky chol;
-  long long hpsi = 0;
-
-  int H(const double* in, double* out) {
-    ++hpsi;
-    return apply_H_impl(c, in, in + n, out, out + n, nullptr, 0);
-  }
-  // |g|^2 and <rhs|x> with one read-back (the convergence test of OCEAN_gmres.f90:820-842)
-  int residual(const double* g, const double* rhs, const double* x, double* gval, double* rval, double* ival) {
-    int rc;
-    if ((rc = vec_dot_dev(c, g, g, c->d_scal)) || (rc = vec_dot_dev(c, rhs, x, c->d_scal + 2))) return rc;
-    double h[4];
-    OCN_CUDA(c, cudaMemcpyAsync(h, c->d_scal, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    OCN_CUDA(c, cudaStreamSynchronize(c->stream));
-    *gval = h[0];
-    *rval = h[2];
-    *ival = h[3];
-    return OCN_OK;
-  }
-  // update_gmres (OCEAN_gmres.f90:241-344)
-  int update(int cur, double* g, double* x, double* ax) {
-    int rc = vec_multidot_dev(c, const_cast<const double* const*>(d_aul), cur, au[cur - 1], g, d_part, d_out);
-    if (rc) return rc;
-    std::vector<double> h(4 * (size_t)cur);
-    OCN_CUDA(c, cudaMemcpyAsync(h.data(), d_out, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    OCN_CUDA(c, cudaStreamSynchronize(c->stream));
-    const size_t start = (size_t)cur * (cur - 1) / 2;
-    for (int j = 0; j < cur; ++j) {
-      // c_matrix(iter + iter_start) = conj(<au_cur|au_iter>); the diagonal is the norm
-      if (j == cur - 1) cmat[start + j] = std::complex<double>(h[4 * j], 0.0);
-      else cmat[start + j] = std::complex<double>(h[4 * j], -h[4 * j + 1]);
-    }
-    std::vector<std::complex<double>> coef(cur);
-    for (int j = 0; j < cur; ++j) coef[j] = -std::complex<double>(h[4 * j + 2], h[4 * j + 3]);
-    if (chol.add_row(cur - 1, cmat)) return set_err(c, OCN_ERR_SOLVE, "GMRES Gram matrix not positive definite");
-    chol.solve(cur, coef);
-    std::vector<double2> hc(cur);
-    for (int j = 0; j < cur; ++j) hc[j] = make_double2(coef[j].real(), coef[j].imag());
-    OCN_CUDA(c, cudaMemcpyAsync(d_coef, hc.data(), cur * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
-    return vec_update_dev(c, cur, d_coef, const_cast<const double* const*>(d_ul),
-                          const_cast<const double* const*>(d_aul), x, ax);
-  }
-};
-
-// Called with each energy's solution x (device, re|im planes) once it has converged.
-typedef std::function<int(int step, const double* x)> GmresHook;
-
-// OCEAN_gmres_do_recycle over the energy list; hay_r/hay_i are host or device
-// planes as `kind` says.  adjoint: solve (w - i Gamma - H) y = b instead, with
-// the preconditioner's damping and the convergence test's sign flipped to match.
-int gmres_run(ocn_ctx* c, const double* hay_r, const double* hay_i, cudaMemcpyKind kind, double kpref,
-              const double* elist, int nomega, const ocn_gmres_params* p, double* out_re, double* out_im,
-              double* rel_err, int* iters, const GmresHook* on_x, bool adjoint = false) {
-  const double zs = adjoint ? -1.0 : 1.0;
-  const double res = zs * p->resolution, gprc = zs * p->preconditioner;
-  if (!c || !hay_r || !hay_i || !elist || nomega < 1 || !p || p->depth < 1) return OCN_ERR_ARG;
-  if (p->depth > 1024) return set_err(c, OCN_ERR_ARG, "gmres depth must be <= 1024");
-  cudaSetDevice(c->device);
-  int rc = require(c);
-  if (rc) return rc;
-  const double ev2ha = 0.036749322175666;
-  Gmres G;
-  G.c = c;
-  G.n = c->npsi;
-  G.depth = p->depth;
-  const size_t n = c->npsi;
-  const int nfixed = 8;  // rhs x ax hpsi1 g pcdiv ones spare
-  double* pool = nullptr;
-  if ((rc = dev_alloc(c, &pool, (size_t)(nfixed + 2 * p->depth) * 2 * n))) return rc;
-  auto V = [&](int i) { return pool + (size_t)i * 2 * n; };
-  double *rhs = V(0), *x = V(1), *ax = V(2), *hpsi1 = V(3), *g = V(4), *pcdiv = V(5), *ones = V(6);
-  for (int j = 0; j < p->depth; ++j) {
-    G.u.push_back(V(nfixed + j));
-    G.au.push_back(V(nfixed + p->depth + j));
-  }
-  std::vector<void*> owned{pool};
-  auto cleanup = [&]() {
-    for (void* q : owned) cudaFree(q);
-  };
-  if ((rc = dev_alloc(c, &G.d_ul, p->depth)) || (owned.push_back(G.d_ul), false) ||
-      (rc = dev_alloc(c, &G.d_aul, p->depth)) || (owned.push_back(G.d_aul), false) ||
-      (rc = dev_alloc(c, &G.d_part, (size_t)c->red_blocks * p->depth * 4)) ||
-      (owned.push_back(G.d_part), false) || (rc = dev_alloc(c, &G.d_out, (size_t)p->depth * 4)) ||
-      (owned.push_back(G.d_out), false) || (rc = dev_alloc(c, &G.d_coef, p->depth)) ||
-      (owned.push_back(G.d_coef), false)) {
-    cleanup();
-    return rc;
-  }
-  G.cmat.assign((size_t)p->depth * (p->depth + 1) / 2, std::complex<double>(0.0, 0.0));
-  G.chol.init(p->depth);
-  cudaError_t e = cudaMemcpyAsync(G.d_ul, G.u.data(), p->depth * sizeof(double*), cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(G.d_aul, G.au.data(), p->depth * sizeof(double*), cudaMemcpyHostToDevice, c->stream);
-  // psi_rhs = sfact(hay_vec): allow o hay (OCEAN_gmres.f90:586)
-  if (e == cudaSuccess) e = cudaMemcpyAsync(g, hay_r, n * sizeof(double), kind, c->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(g + n, hay_i, n * sizeof(double), kind, c->stream);
-  if (e != cudaSuccess) {
-    cleanup();
-    return cuda_fail(c, e, "ocn_gmres upload");
-  }
-  auto run = [&]() -> int {
-    int r;
-    if ((r = vec_mask_copy(c, g, rhs))) return r;
-    if ((r = vec_fill(c, ones, 1.0, 0.0))) return r;
-    if ((r = G.H(ones, hpsi1))) return r;  // H * (1,0), :600-608
-    int global_iter = 0, prev_iter = 0;
-    double prev_energy = -1.0e308;
-    double rval = 0.0, ival = 0.0, gval = 0.0;
-    for (int step = 0; step < nomega; ++step) {
-      int complete_iter = 0;
-      const double ener = elist[step] * ev2ha;
-      bool converged = false;
-      if (prev_iter == 0) {
-        prev_energy = ener;
-        if ((r = vec_set_prec(c, ener, gprc, hpsi1, pcdiv))) return r;
-      }
-      // set_initial_vector: keep x for step > 0 (force_reuse_x, OCEAN_gmres.f90:24-27,1232-1241)
-      auto initial = [&]() -> int {
-        int q;
-        if (step > 0) {
-          if ((q = G.H(x, ax))) return q;
-          if ((q = vec_axmy(c, x, ax, ener, res))) return q;
-        } else {
-          if ((q = vec_fill(c, x, 0.0, 0.0))) return q;
-          if ((q = vec_fill(c, ax, 0.0, 0.0))) return q;
-        }
-        return vec_axmz(c, ax, g, rhs);
-      };
-      if (prev_iter == 0) {
-        if ((r = initial())) return r;
-        if ((r = G.residual(g, rhs, x, &gval, &rval, &ival))) return r;
-      } else {
-        const double delta = elist[step] * ev2ha - elist[step - 1] * ev2ha;  // make_recycle
-        for (int j = 0; j < prev_iter; ++j)
-          if ((r = vec_axpy(c, delta, 0.0, G.u[j], G.au[j]))) return r;
-        if ((r = initial())) return r;
-        for (int it = 1; it <= prev_iter; ++it) {
-          if ((r = G.update(it, g, x, ax))) return r;
-          if ((r = vec_axmz(c, ax, g, rhs))) return r;
-        }
-        if ((r = G.residual(g, rhs, x, &gval, &rval, &ival))) return r;
-        if (gval < p->convergence) {
-          const double rel = -zs * gval / ival;
-          if (rel < 0.001 || gval < p->convergence / 10.0) converged = true;
-        }
-        if (!converged && std::fabs(prev_energy - ener) > p->preconditioner / 4.0) {
-          prev_iter = 0;
-          prev_energy = ener;
-          if ((r = vec_set_prec(c, ener, gprc, hpsi1, pcdiv))) return r;
-        }
-      }
-      int restarts = 0;
-      while (!converged) {
-        for (int it = prev_iter + 1; it <= p->depth; ++it) {
-          ++complete_iter;
-          ++global_iter;
-          double* pg = G.u[it - 1];
-          double* apg = G.au[it - 1];
-          if ((r = vec_mul(c, g, pcdiv, pg))) return r;
-          if ((r = G.H(pg, apg))) return r;
-          if ((r = vec_axmy(c, pg, apg, ener, res))) return r;
-          if ((r = G.update(it, g, x, ax))) return r;
-          if (it == p->depth) {
-            if ((r = G.H(x, ax))) return r;
-            if ((r = vec_axmy(c, x, ax, ener, res))) return r;
-            if (ener != prev_energy) {
-              if ((r = vec_set_prec(c, ener, gprc, hpsi1, pcdiv))) return r;
-              prev_energy = ener;
-            }
-            prev_iter = 0;
-          }
-          if ((r = vec_axmz(c, ax, g, rhs))) return r;
-          if ((r = G.residual(g, rhs, x, &gval, &rval, &ival))) return r;
-          if (gval < p->convergence) {
-            const double rel = -zs * gval / ival;
-            if (rel < 0.001 || gval < p->convergence / 10.0) {
-              prev_iter = (it == p->depth) ? 0 : it;
-              converged = true;
-              break;
-            }
-          }
-        }
-        if (converged) break;
-        if (++restarts > std::max(0, p->max_restarts))
-          return set_err(c, OCN_ERR_NOCONV, "GMRES restart cap reached");
-      }
-      if (out_re) out_re[step] = 1.0 - rval * kpref;
-      if (out_im) out_im[step] = -ival * kpref;
-      if (rel_err) rel_err[step] = -gval / ival;
-      if (iters) iters[step] = complete_iter;
-      if (on_x && (r = (*on_x)(step, x))) return r;
-    }
-    return OCN_OK;
-  };
-  rc = run();
-  e = cudaStreamSynchronize(c->stream);
-  cleanup();
-  if (e != cudaSuccess) return cuda_fail(c, e, "ocn_gmres");
-  if (rc == OCN_OK && c->mixed) rc = mixed_check(c);
-  return rc;
+int ocn_gmres_set_lanes(ocn_ctx* c, int nlanes) {
+  if (!c) return OCN_ERR_ARG;
+  if (nlanes < 1 || nlanes > 64) return set_err(c, OCN_ERR_ARG, "ocn_gmres_set_lanes: nlanes must be in 1..64");
+  c->gmres_lanes = nlanes;
+  return OCN_OK;
 }
 
+namespace {
+int gmres_check(ocn_ctx* c, const double* elist, int nomega, const ocn_gmres_params* p) {
+  if (!elist || nomega < 1 || !p || p->depth < 1) return set_err(c, OCN_ERR_ARG, "ocn_gmres: bad argument");
+  if (p->depth > 1024) return set_err(c, OCN_ERR_ARG, "gmres depth must be <= 1024");
+  cudaSetDevice(c->device);
+  return require(c);
+}
 }  // namespace
 
 int ocn_gmres(ocn_ctx* c, const double* hay_r, const double* hay_i, double kpref, const double* elist,
               int nomega, const ocn_gmres_params* p, double* out_re, double* out_im, double* rel_err,
               int* iters) {
-  return gmres_run(c, hay_r, hay_i, cudaMemcpyHostToDevice, kpref, elist, nomega, p, out_re, out_im, rel_err,
-                   iters, nullptr);
+  if (!c || !hay_r || !hay_i) return OCN_ERR_ARG;
+  int rc = gmres_check(c, elist, nomega, p);
+  if (rc) return rc;
+  const size_t n = c->npsi;
+  double* d_hay = nullptr;
+  if ((rc = dev_alloc(c, &d_hay, 2 * n))) return rc;
+  cudaError_t e = cudaMemcpyAsync(d_hay, hay_r, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_hay + n, hay_i, n * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) {
+    cudaFree(d_hay);
+    return cuda_fail(c, e, "ocn_gmres upload");
+  }
+  rc = gmres_solve(c, d_hay, kpref, elist, nomega, p, c->gmres_lanes, out_re, out_im, rel_err, iters, nullptr,
+                   false);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(d_hay);
+  return rc;
 }
 
 int ocn_gmres_dev(ocn_ctx* c, const double* d_hay, double kpref, const double* elist, int nomega,
                   const ocn_gmres_params* p, double* out_re, double* out_im, double* rel_err, int* iters,
                   double* d_x) {
   if (!c || !d_hay) return OCN_ERR_ARG;
+  int rc = gmres_check(c, elist, nomega, p);
+  if (rc) return rc;
   const size_t n = c->npsi;
   GmresHook keep = [&](int step, const double* x) -> int {
     OCN_CUDA(c, cudaMemcpyAsync(d_x + (size_t)step * 2 * n, x, 2 * n * sizeof(double), cudaMemcpyDeviceToDevice,
                                 c->stream));
     return OCN_OK;
   };
-  return gmres_run(c, d_hay, d_hay + n, cudaMemcpyDeviceToDevice, kpref, elist, nomega, p, out_re, out_im,
-                   rel_err, iters, d_x ? &keep : nullptr);
+  return gmres_solve(c, d_hay, kpref, elist, nomega, p, c->gmres_lanes, out_re, out_im, rel_err, iters,
+                     d_x ? &keep : nullptr, false);
 }
 
 int ocn_gmres_vjp(ocn_ctx* c, const double* d_hay, double kpref, const double* elist, int nomega,
@@ -1589,8 +1360,10 @@ int ocn_gmres_vjp(ocn_ctx* c, const double* d_hay, double kpref, const double* e
     gs += a * yx[0] + b * yx[1];
     return lr_wgrad_fp64(c, x, y, phi, a, b, d_gW);
   };
-  rc = gmres_run(c, d_hay, d_hay + n, cudaMemcpyDeviceToDevice, kpref, elist, nomega, p, nullptr, nullptr,
-                 nullptr, nullptr, &pair, true);
+  rc = gmres_check(c, elist, nomega, p);
+  if (rc == OCN_OK)
+    rc = gmres_solve(c, d_hay, kpref, elist, nomega, p, c->gmres_lanes, nullptr, nullptr, nullptr, nullptr, &pair,
+                     true);
   e = cudaStreamSynchronize(c->stream);
   cudaFree(phi);
   if (rc) return rc;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -139,6 +140,8 @@ struct ocn_ctx {
   ocn::MixedLR* mixed = nullptr;
 
   ocn::Timing timing;
+
+  int gmres_lanes = 1;         // energy lanes of the GMRES sweep (ocn_gmres_set_lanes)
 
   // Haydock loop: persistent buffers and the captured 3-iteration CUDA graph
   double* hay_vec = nullptr;   // old | psi | h, each 2*npsi
@@ -281,12 +284,24 @@ int lr_group_norm(LrGroup* g, int rot, cudaStream_t s);
 int lr_group_launches(const LrGroup* g);
 void lr_group_destroy(LrGroup* g);
 
+// ---- the action and the GMRES sweep (ocn_capi.cu, ocn_gmres.cu)
+// H*psi on device planes (OCEAN_xact); hflag NULL: the context's switches
+int apply_H_impl(ocn_ctx* c, const double* ir, const double* ii, double* orr, double* oi, const int* hflag_in,
+                 int backwards);
+// H on a block of nv <= nvec vectors (vector v at in + 2 v npsi)
+int apply_H_block_impl(ocn_ctx* c, int nv, const double* in, double* out, const int* hflag_in, int backwards,
+                       const int* back_each = nullptr);
+typedef std::function<int(int step, const double* x)> GmresHook;
+// OCEAN_gmres_do_recycle over the energy list in nlanes lanes; d_rhs: device
+// planes of the right-hand side before the allow mask.  on_x: called with each
+// energy's solution (device planes) once it has converged.  adjoint: solve
+// (w - i Gamma - H) y = b instead.
+int gmres_solve(ocn_ctx* c, const double* d_rhs, double kpref, const double* elist, int nomega,
+                const ocn_gmres_params* p, int nlanes, double* out_re, double* out_im, double* rel_err,
+                int* iters, const GmresHook* on_x, bool adjoint);
+
 // BLAS-1 helpers for GMRES (ocn_kernels.cu); vectors are [re plane | im plane]
 int vec_dot_dev(ocn_ctx* c, const double* p, const double* q, double* d_out);
-int vec_multidot_dev(ocn_ctx* c, const double* const* d_vecs, int nvec, const double* au_cur,
-                     const double* g, double* d_part, double* d_out);
-int vec_update_dev(ocn_ctx* c, int nvec, const double2* d_coef, const double* const* d_ul,
-                   const double* const* d_aul, double* x, double* ax);
 int vec_axmy(ocn_ctx* c, const double* x, double* y, double rv, double iv);
 int vec_axmz(ocn_ctx* c, const double* x, double* y, const double* z);
 int vec_axpy(ocn_ctx* c, double ar, double ai, const double* x, double* y);

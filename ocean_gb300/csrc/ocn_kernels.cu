@@ -740,101 +740,6 @@ __global__ void k_reduce_final(const double* __restrict__ red, int nblk, double*
   }
 }
 
-// Gram row of update_gmres (OCEAN_gmres.f90:270-283) in one pass:
-// part[blk][j] = { <au_cur|au_j> (re, im), <au_j|g> (re, im) } for j < nvec.
-// Gram row of update_gmres (OCEAN_gmres.f90:262-300): for vector j = blockIdx.y,
-// partial sums over element chunk blockIdx.x of <au_j|au_cur> and <au_j|g>.
-// One (vector, chunk) per CTA keeps every CTA streaming a long contiguous range;
-// au_cur and g are re-read per vector from L2.
-__global__ void k_multidot(const double* const* __restrict__ vecs, int nvec,
-                           const double* __restrict__ au_cur, const double* __restrict__ g,
-                           size_t n, double* __restrict__ part) {
-  __shared__ double sh[4][32];
-  const int j = blockIdx.y;
-  const double* __restrict__ v = vecs[j];
-  const size_t chunk = (n + gridDim.x - 1) / gridDim.x;
-  const size_t e0 = blockIdx.x * chunk;
-  const size_t e1 = (e0 + chunk < n) ? e0 + chunk : n;
-  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-#pragma unroll 4
-  for (size_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-    const double cr = au_cur[e], ci = au_cur[n + e];
-    const double vr = v[e], vi = v[n + e];
-    const double gr = g[e], gi = g[n + e];
-    s0 += cr * vr + ci * vi;
-    s1 += cr * vi - ci * vr;
-    s2 += vr * gr + vi * gi;
-    s3 += vr * gi - vi * gr;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    s0 += __shfl_down_sync(0xffffffffu, s0, o);
-    s1 += __shfl_down_sync(0xffffffffu, s1, o);
-    s2 += __shfl_down_sync(0xffffffffu, s2, o);
-    s3 += __shfl_down_sync(0xffffffffu, s3, o);
-  }
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) {
-    sh[0][w] = s0;
-    sh[1][w] = s1;
-    sh[2][w] = s2;
-    sh[3][w] = s3;
-  }
-  __syncthreads();
-  if (threadIdx.x < 4) {
-    double t = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += sh[threadIdx.x][i];
-    part[((size_t)blockIdx.x * nvec + j) * 4 + threadIdx.x] = t;
-  }
-}
-// One warp per output: lane l sums chunks l, l+32, ... in order, then a fixed
-// shuffle tree (deterministic; the chunk partials are L2-resident).
-__global__ void k_multidot_reduce(const double* __restrict__ part, int nblk, int nvec,
-                                  double* __restrict__ out) {
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (i >= nvec * 4) return;
-  double s = 0.0;
-  for (int b = lane; b < nblk; b += 32) s += part[(size_t)b * nvec * 4 + i];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) out[i] = s;
-}
-// x += sum_j c_j u_j, ax += sum_j c_j au_j   (OCEAN_gmres.f90:336-341, in j order)
-// x += sum_j c_j u_j, ax += sum_j c_j au_j (OCEAN_gmres.f90:312-322).  The
-// coefficients and vector addresses are staged in shared memory; the j loop is
-// unrolled so that several vectors' loads are in flight per thread.
-__global__ void k_update(int nvec, const double2* __restrict__ coef, const double* const* __restrict__ ul,
-                         const double* const* __restrict__ aul, double* __restrict__ x,
-                         double* __restrict__ ax, size_t n) {
-  extern __shared__ unsigned char upd_sm[];
-  double2* sc = reinterpret_cast<double2*>(upd_sm);
-  const double** su = reinterpret_cast<const double**>(sc + nvec);
-  const double** sa = su + nvec;
-  for (int j = threadIdx.x; j < nvec; j += blockDim.x) {
-    sc[j] = coef[j];
-    su[j] = ul[j];
-    sa[j] = aul[j];
-  }
-  __syncthreads();
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
-       e += (size_t)gridDim.x * blockDim.x) {
-    double xr = x[e], xi = x[n + e], yr = ax[e], yi = ax[n + e];
-#pragma unroll 4
-    for (int j = 0; j < nvec; ++j) {
-      const double2 c = sc[j];
-      const double* u = su[j];
-      const double* au = sa[j];
-      const double ur = u[e], ui = u[n + e], vr = au[e], vi = au[n + e];
-      xr += c.x * ur - c.y * ui;
-      xi += c.x * ui + c.y * ur;
-      yr += c.x * vr - c.y * vi;
-      yi += c.x * vi + c.y * vr;
-    }
-    x[e] = xr;
-    x[n + e] = xi;
-    ax[e] = yr;
-    ax[n + e] = yi;
-  }
-}
 
 typedef decltype(&k_combine<4, false>) CombineFn;
 CombineFn combine_kernel(int na, int use_so) {
@@ -1165,27 +1070,6 @@ int vec_dot_dev(ocn_ctx* c, const double* p, const double* q, double* d_out) {
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   k_reduce_final<<<1, 256, 0, c->stream>>>(c->d_red, nblk, d_out);
-  ++c->launches;
-  OCN_CUDA(c, cudaGetLastError());
-  return OCN_OK;
-}
-int vec_multidot_dev(ocn_ctx* c, const double* const* d_vecs, int nvec, const double* au_cur,
-                     const double* g, double* d_part, double* d_out) {
-  // about eight CTAs per SM in total, at least 16 chunks per vector
-  const int nblk = std::max(16, std::min(c->red_blocks, (8 * c->sm_count + nvec - 1) / nvec));
-  k_multidot<<<dim3(nblk, nvec), 256, 0, c->stream>>>(d_vecs, nvec, au_cur, g, c->npsi, d_part);
-  ++c->launches;
-  OCN_CUDA(c, cudaGetLastError());
-  k_multidot_reduce<<<(nvec * 4 + 7) / 8, 256, 0, c->stream>>>(d_part, nblk, nvec, d_out);
-  ++c->launches;
-  OCN_CUDA(c, cudaGetLastError());
-  return OCN_OK;
-}
-int vec_update_dev(ocn_ctx* c, int nvec, const double2* d_coef, const double* const* d_ul,
-                   const double* const* d_aul, double* x, double* ax) {
-  const size_t sm = (size_t)nvec * (sizeof(double2) + 2 * sizeof(double*));
-  k_update<<<grid_for(c->npsi, 256, 4 * c->sm_count), 256, sm, c->stream>>>(nvec, d_coef, d_ul, d_aul, x,
-                                                                             ax, c->npsi);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;

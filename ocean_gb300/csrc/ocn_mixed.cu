@@ -927,6 +927,15 @@ int alloc(ocn_ctx* c, T** p, size_t n) {
 
 }  // namespace
 
+// Transforms per CTA of the cubic k-mesh step for ntot = Na * nv transforms:
+// the configured count when it divides ntot, else all of them; reduced to one
+// vector's Na (which always divides ntot) when that would not fit in shared memory.
+int cube_tc(const MixedLR* m, int kn, int na, int ntot) {
+  int tc = (m->cfg[4] > 0 && ntot % m->cfg[4] == 0) ? m->cfg[4] : ntot;
+  if (kmesh_cube_smem<float>(kn, tc) > 227u * 1024u) tc = na;
+  return tc;
+}
+
 int mixed_init(ocn_ctx* c) {
   if (c->nspn != 1 && c->nspn != 2) return set_err(c, OCN_ERR_UNSUPPORTED, "nspn must be 1 or 2");
   const int nb = c->nb, nk = c->nk, nx = c->nx, na = c->na, nvmax = c->nvec, ns = c->nspn;
@@ -934,7 +943,7 @@ int mixed_init(ocn_ctx* c) {
   if (ncol > TC_MAX_NCOL)
     return set_err(c, OCN_ERR_ARG, "nvec too large: 4*nalpha*nvec must be <= 256");
   const bool cube = kmesh_cube_supported(c->dims.kmesh);
-  const size_t fsm = cube ? kmesh_cube_smem<float>(c->dims.kmesh[0], na * nvmax)
+  const size_t fsm = cube ? kmesh_cube_smem<float>(c->dims.kmesh[0], na)
                           : kmesh_smem(kmesh_geom<float>(c->dims.kmesh, na * nvmax));
   if (fsm > 227u * 1024u)
     return set_err(c, OCN_ERR_ARG, "nvec*nalpha*Nk too large for the shared-memory k-mesh transform");
@@ -1389,7 +1398,7 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
     if (m->cube) {
       // transforms per CTA: all of the x-point, or a slice (tile parameter 5)
       const int ntot = na * nv;
-      const int tc = (m->cfg[4] > 0 && ntot % m->cfg[4] == 0) ? m->cfg[4] : ntot;
+      const int tc = cube_tc(m, c->dims.kmesh[0], na, ntot);
       CubeFnF f;
       OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], tc, f);
       const int th = m->cfg[5] ? m->cfg[5] : 128;
@@ -1563,9 +1572,9 @@ int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out) {
     ocn_ctx* c = mem[i].c;
     const MixedLR* m = c->mixed;
     const int ntot = c->na * mem[i].nv;
-    const int tc = (m->cfg[4] > 0 && ntot % m->cfg[4] == 0) ? m->cfg[4] : ntot;
-    const int th = m->cfg[5] ? m->cfg[5] : 128;
     const int kn = c->dims.kmesh[0];
+    const int tc = cube_tc(m, kn, c->na, ntot);
+    const int th = m->cfg[5] ? m->cfg[5] : 128;
     LrGroup::FftClass* cls = nullptr;
     for (auto& f : g->fft)
       if (f.kn == kn && f.tc == tc && f.th == th) cls = &f;
