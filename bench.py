@@ -71,9 +71,15 @@ def parse():
                     help="energies of the adjoint-gradient leg (GMRES forward + reverse); 0 = off")
     ap.add_argument("--gmres-omega", type=int, default=200,
                     help="energies of the GMRES leg (0 disables it)")
-    ap.add_argument("--gmres-fp64-omega", type=int, default=8,
-                    help="energies (a spread subset of the GMRES leg's) solved by both precisions for the "
+    ap.add_argument("--gmres-fp64-omega", type=int, default=50,
+                    help="energies (every k-th of the GMRES leg's) solved by both precisions for the "
                          "FP64 comparison; 0 = off")
+    ap.add_argument("--gmres-lanes", type=int, default=16,
+                    help="energy lanes of the GMRES leg (one block action serves all lanes); the single "
+                         "reference-order sweep is timed beside it")
+    ap.add_argument("--oracle-steps", type=int, default=200,
+                    help="Lanczos steps of the main workload run by the FP64 oracle on the host to state "
+                         "the spectral error of both GPU precisions against it; 0 = off")
     ap.add_argument("--batch-fp64", type=int, default=8,
                     help="instances of the batched set run by both precisions (100 steps) for the FP64 "
                          "comparison; 0 = off")
@@ -547,6 +553,83 @@ def run_batch(args, torch, capi, WL, local, dev, niter: int = 500, nv: int = 3):
             "fp64_subset": cmp64, "setup_s": setup_s, "shapes": shapes, "tiles": tuned}
 
 
+def oracle_check(args, ctx, w, torch, capi):
+    """The FP64 oracle's Haydock run of the main workload on the host cores and
+    the mixed GPU path's spectrum (same steps) against it."""
+    import time
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    nst = args.oracle_steps
+    ra, ia, rb, done = ctx.haydock(nst)
+    sg = capi.spectrum_cf(ra, ia, rb, done, w.kpref, w.el, w.eh, args.ne, w.gam0)
+    t0 = time.perf_counter()
+    P = O.OracleProblem(w)
+    rc, ora, oia, orb, odone = P.haydock(nst)
+    t1 = time.perf_counter()
+    so = O.write_core(ora, oia, orb, nst, w.kpref, w.el, w.eh, args.ne, w.gam0)
+    err = float(np.linalg.norm(sg[:, 2] - so[:, 2]) / np.linalg.norm(so[:, 2]))
+    return {"steps": nst, "oracle_rc": int(rc), "oracle_s": t1 - t0, "cores": os.cpu_count(),
+            "spectral_error_mixed_vs_oracle": err,
+            "first10_a_rel_mixed": float(np.max(np.abs(ra[:10] - ora[:10]) / np.abs(ora[:10]))),
+            "_spectrum": so}
+
+
+def run_gmres(args, torch, capi, w, prec, local):
+    """GMRES over the energy window: the lanes run and the single sweep."""
+    from ocean_gb300 import workloads as WL2
+
+    energies = np.linspace(w.el, w.eh, args.gmres_omega) * WL2.HARTREE2EV
+    lanes = max(1, args.gmres_lanes)
+    dev = f"cuda:{local}"
+    gctx = capi.Context(w, precision=prec, device=local, nvec=lanes if prec == capi.OCN_PREC_MIXED else 1)
+    stream = torch.cuda.ExternalStream(gctx.stream, device=dev)
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    out = {"omega_points": int(args.gmres_omega), "tolerance_g2": 1e-6, "depth": 80}
+
+    def timed(nl, es):
+        gctx.set_gmres_lanes(nl)
+        gctx.gmres(es[:2], depth=80, tol=1e-6, max_restarts=100)  # warm-up
+        l1 = gctx.launches
+        torch.cuda.synchronize()
+        g0.record(stream)
+        ore, oim, rel, its = gctx.gmres(es, depth=80, tol=1e-6, max_restarts=100)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        return g0.elapsed_time(g1), ore, oim, rel, its, gctx.launches - l1
+
+    try:
+        main_im = None
+        for tag, nl in (("lanes", lanes), ("single_sweep", 1)):
+            gms, ore, oim, rel, its, nlaunch = timed(nl, energies)
+            out[tag] = {"lanes": nl, "ms": gms, "spectra_per_s": 1000.0 / gms, "inner_iterations": int(its.sum()),
+                        "gpu_launches": nlaunch,
+                        "hpsi_per_s": (int(its.sum()) + 2 * args.gmres_omega) / (gms / 1000.0),
+                        "max_rel_error": float(np.max(np.abs(rel)))}
+            if main_im is None:
+                main_im = oim
+            else:
+                out[tag]["max_rel_diff_vs_lanes_im"] = float(np.max(np.abs(oim - main_im) / np.abs(main_im)))
+        out["ms"] = out["lanes"]["ms"]
+        out["spectra_per_s"] = out["lanes"]["spectra_per_s"]
+        if args.gmres_fp64_omega > 0 and prec == capi.OCN_PREC_MIXED:
+            # every k-th energy (recycling still applies at this spacing), solved here
+            # and again by the FP64 path with the same lanes
+            step = max(1, len(energies) // args.gmres_fp64_omega)
+            idx = np.arange(0, len(energies), step)[:args.gmres_fp64_omega]
+            sub_e = energies[idx]
+            nl = min(lanes, len(sub_e))
+            gms, sre, sim, _, sits, _ = timed(nl, sub_e)
+            out["fp64_subset"] = {"energies_ev": sub_e, "which": f"every {step}th of the {len(energies)}",
+                                  "lanes": nl, "mixed_ms": gms, "mixed_re": sre, "mixed_im": sim,
+                                  "mixed_iterations": int(sits.sum())}
+    finally:
+        gctx.close()
+    return out
+
+
 def run_ours(args, ws, rank, local, pg):
     import torch
 
@@ -616,36 +699,18 @@ def run_ours(args, ws, rank, local, pg):
     e2e_ms = max_over_ranks(pg, e2e_ms, dev)
     e2e_value = total_hpsi / (e2e_ms / 1000.0)
 
-    # ---- GMRES leg: 200 energies across the spectrum, tol 1e-6 on |g|^2, depth 80
+    # ---- oracle check: the FP64 oracle's own Haydock run on the same input, and
+    #      the spectral error of the mixed path against it (column Spect(0))
+    orc = None
+    if rank == 0 and args.oracle_steps > 0:
+        orc = oracle_check(args, ctx, w, torch, capi)
+    ctx.close()
+
+    # ---- GMRES leg: 200 energies across the spectrum, tol 1e-6 on |g|^2, depth 80,
+    #      in energy lanes (one block action per round) and as the single sweep
     gm = None
     if rank == 0 and args.gmres_omega > 0:
-        from ocean_gb300 import workloads as WL2
-
-        energies = np.linspace(w.el, w.eh, args.gmres_omega) * WL2.HARTREE2EV
-        ctx.gmres(energies[:2], depth=80, tol=1e-6, max_restarts=100)  # warm-up
-        l1 = ctx.launches
-        g0 = torch.cuda.Event(enable_timing=True)
-        g1 = torch.cuda.Event(enable_timing=True)
-        g0.record(stream)
-        ore, oim, rel, its = ctx.gmres(energies, depth=80, tol=1e-6, max_restarts=100)
-        g1.record(stream)
-        torch.cuda.synchronize()
-        gms = g0.elapsed_time(g1)
-        gm = {"omega_points": int(args.gmres_omega), "tolerance_g2": 1e-6, "depth": 80,
-              "ms": gms, "spectra_per_s": 1000.0 / gms, "inner_iterations": int(its.sum()),
-              "gpu_launches": ctx.launches - l1,
-              "hpsi_per_s": (int(its.sum()) + 2 * args.gmres_omega) / (gms / 1000.0),
-              "max_rel_error": float(np.max(np.abs(rel)))}
-        if args.gmres_fp64_omega > 0:
-            # a spread subset of the energies, solved here and again by the FP64 path below
-            sub_e = energies[np.linspace(0, len(energies) - 1, args.gmres_fp64_omega).round().astype(int)]
-            g0.record(stream)
-            sre, sim, _, sits = ctx.gmres(sub_e, depth=80, tol=1e-6, max_restarts=100)
-            g1.record(stream)
-            torch.cuda.synchronize()
-            gm["fp64_subset"] = {"energies_ev": sub_e, "mixed_ms": g0.elapsed_time(g1),
-                                 "mixed_re": sre, "mixed_im": sim, "mixed_iterations": int(sits.sum())}
-    ctx.close()
+        gm = run_gmres(args, torch, capi, w, prec, local)
 
     # ---- adjoint leg: d(spectrum)/d(W scale, W(r) table, Gamma, scissor) through
     #      GmresSpectrum, 400 energies at Gamma = 0.3 eV on the same sizes
@@ -758,6 +823,7 @@ def run_ours(args, ws, rank, local, pg):
                 "speedup_mixed_vs_fp64": value / ws / (niter / (ms64 / 1000.0))}
         if gm is not None and "fp64_subset" in gm:
             sub = gm.pop("fp64_subset")
+            c64.set_gmres_lanes(sub["lanes"])
             h0 = torch.cuda.Event(enable_timing=True)
             h1 = torch.cuda.Event(enable_timing=True)
             h0.record(s64)
@@ -765,14 +831,27 @@ def run_ours(args, ws, rank, local, pg):
             h1.record(s64)
             torch.cuda.synchronize()
             ms_g64 = h0.elapsed_time(h1)
-            # out_im is the absorption (1 - kpref Re F is out_re): both columns compared
+            # out_im is the absorption (1 - kpref Re F is out_re): both columns compared,
+            # as a 2-norm over the energies and energy by energy
             e_im = float(np.linalg.norm(sub["mixed_im"] - im64) / np.linalg.norm(im64))
             e_re = float(np.linalg.norm(sub["mixed_re"] - re64) / np.linalg.norm(re64))
-            gm["fp64_subset"] = {"omega_points": len(sub["energies_ev"]), "mixed_ms": sub["mixed_ms"],
+            m_im = float(np.max(np.abs(sub["mixed_im"] - im64) / np.abs(im64)))
+            m_re = float(np.max(np.abs(sub["mixed_re"] - re64) / np.abs(re64)))
+            gm["fp64_subset"] = {"omega_points": len(sub["energies_ev"]), "lanes": sub["lanes"],
+                                 "energies": sub["which"], "mixed_ms": sub["mixed_ms"],
                                  "fp64_ms": ms_g64, "speedup_mixed_vs_fp64": ms_g64 / sub["mixed_ms"],
                                  "mixed_iterations": sub["mixed_iterations"], "fp64_iterations": int(its64.sum()),
-                                 "spectral_error_im": e_im, "spectral_error_re": e_re}
+                                 "spectral_error_im": e_im, "spectral_error_re": e_re,
+                                 "max_rel_error_im_per_energy": m_im, "max_rel_error_re_per_energy": m_re}
+        if orc is not None:
+            ra, ia, rb, done = c64.haydock_dev(orc["steps"], pr_ptr, pi_ptr)
+            s64o = capi.spectrum_cf(ra, ia, rb, done, w.kpref, w.el, w.eh, ne, w.gam0)
+            so = orc["_spectrum"]
+            orc["spectral_error_fp64_vs_oracle"] = float(np.linalg.norm(s64o[:, 2] - so[:, 2]) /
+                                                         np.linalg.norm(so[:, 2]))
         c64.close()
+    if orc is not None:
+        orc.pop("_spectrum", None)
     if gm is not None and "mixed_re" in gm.get("fp64_subset", {}):
         gm.pop("fp64_subset")  # no FP64 run to compare with
     # dominant kernel and its roofline
@@ -807,7 +886,7 @@ def run_ours(args, ws, rank, local, pg):
                        "l2": "inputs larger than L2 (u2 %.2f GB per contraction operand)" % (
                            w.nb * w.nk * w.nx * (16 if args.precision == 'fp64' else 8) / 1e9)},
             "spectra_per_s": args.steps * ws / (dev_ms / 1000.0),
-            "fp64_gpu": fp64, "gmres": gm, "block_haydock": blk, "adjoint": adj, "batch": bat,
+            "fp64_gpu": fp64, "oracle_check": orc, "gmres": gm, "block_haydock": blk, "adjoint": adj, "batch": bat,
             "multiplet": mlt, "nonherm": nh, "valence": val, "c1": small, "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 8,
