@@ -315,6 +315,30 @@ int ocn_spectrum_cf_bc(const double* real_a, const double* imag_a, const double*
 int ocn_spectrum_cf_noalloc(const double* real_a, const double* imag_a, const double* real_b,
                             int iter, double kpref, const ocn_cf_params* p, double* out);
 
+/* Haydock early exit: the haydockconv.ipt test of OCEAN_haydock_Herm_do
+ * (OCEAN_haydock.f90:268-292, check_convergence :1608-1661, calc_spect_core
+ * :1991-2027; switched on by OCEAN_system.f90:452-462).  After every Lanczos
+ * step it > spacing the run compares the spectra of it and it - spacing steps
+ * on ne midpoints (column Spect(0)) by relArea = 2 sum|s1 - s2| / (sum|s1| +
+ * sum|s2|); the run stops at the first step whose relArea and the previous
+ * step's are both below the threshold (*niter_done = that step; coefficients
+ * beyond it are returned as 0).  The test runs on the device inside the
+ * captured Lanczos graph; the host reads the relArea of each step every 30
+ * steps, so up to 30 steps beyond the stop are computed and discarded. */
+typedef struct {
+  double threshold;      /* haydockConvergeThreshold; <= 0 switches the test off */
+  int spacing;           /* haydockConvergeSpacing (>= 1) */
+  int ne;                /* energy points of the test spectra (bse.in ne) */
+  double el, eh, gam0;   /* bse.in energy window and broadening, Hartree */
+  double kpref;          /* hay_vec%kpref of the run */
+} ocn_haydock_conv;
+/* Sets (p != NULL, threshold > 0) or clears the test for this context's
+ * single-chain Haydock runs (ocn_haydock, ocn_haydock_dev); block and batched
+ * runs ignore it. */
+int ocn_set_haydock_conv(ocn_ctx* ctx, const ocn_haydock_conv* p);
+/* haydockconv.ipt: "threshold spacing", list-directed (OCEAN_system.f90:452-458). */
+int ocn_read_haydockconv(const char* path, double* threshold, int* spacing);
+
 /* redtrid (OCEAN_haydock.f90:2273-2316): eigenvalues (ascending) of the (n+1)x(n+1)
  * tridiagonal Lanczos matrix; host FP64. */
 int ocn_redtrid(int n, const double* real_a, const double* real_b, double* w /* n+1 */);

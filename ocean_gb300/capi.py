@@ -64,6 +64,11 @@ class OcnGmresParams(C.Structure):
                 ("convergence", C.c_double), ("max_restarts", C.c_int)]
 
 
+class OcnHaydockConv(C.Structure):
+    _fields_ = [("threshold", C.c_double), ("spacing", C.c_int), ("ne", C.c_int), ("el", C.c_double),
+                ("eh", C.c_double), ("gam0", C.c_double), ("kpref", C.c_double)]
+
+
 class OcnBseIn(C.Structure):
     _fields_ = [("dumi", C.c_int), ("dumf", C.c_double), ("style", C.c_char * 8), ("niter", C.c_int),
                 ("ne", C.c_int), ("el", C.c_double), ("eh", C.c_double), ("gam0", C.c_double),
@@ -91,7 +96,7 @@ EXPORTS = [
     "ocn_val_apply_H", "ocn_val_apply_H_dev", "ocn_val_haydock", "ocn_val_haydock_dev",
     "ocn_val_spectrum", "ocn_val_optical_constants", "ocn_write_opcons", "ocn_val_set_fxc",
     "ocn_val_fxc_from_rho", "ocn_read_val_u2", "ocn_val_pair_energies", "ocn_test_starve_tc",
-    "ocn_gmres_set_lanes",
+    "ocn_gmres_set_lanes", "ocn_set_haydock_conv", "ocn_read_haydockconv",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -428,6 +433,20 @@ class Context:
         p.max_restarts = max_restarts
         return p
 
+    def set_haydock_conv(self, threshold: float, spacing: int = 1, ne: int = 200, el=None, eh=None, gam0=None,
+                         kpref=None):
+        """haydockconv.ipt early exit for single-chain Haydock runs (threshold <= 0: off)."""
+        w = self.w
+        p = OcnHaydockConv()
+        p.threshold = threshold
+        p.spacing = spacing
+        p.ne = ne
+        p.el = w.el if el is None else el
+        p.eh = w.eh if eh is None else eh
+        p.gam0 = w.gam0 if gam0 is None else gam0
+        p.kpref = w.kpref if kpref is None else kpref
+        self._chk(self.lib.ocn_set_haydock_conv(self.ptr, C.byref(p)))
+
     def set_gmres_lanes(self, nlanes: int):
         """Energy lanes of the GMRES sweeps of this context (1: the reference's single sweep)."""
         self._chk(self.lib.ocn_gmres_set_lanes(self.ptr, int(nlanes)))
@@ -521,6 +540,14 @@ def spectrum_cf_noalloc(ra, ia, rb, iteration: int, kpref: float, el: float, eh:
     check(lib.ocn_spectrum_cf_noalloc(_dp(_f64(ra)), ia_p, _dp(_f64(rb)), iteration, C.c_double(kpref),
                                       C.byref(p), _dp(out)))
     return out.reshape(ne + 1, 9)
+
+
+def read_haydockconv(path: str):
+    """haydockconv.ipt: (threshold, spacing)."""
+    lib = load()
+    t, sp = C.c_double(0.0), C.c_int(0)
+    check(lib.ocn_read_haydockconv(path.encode(), C.byref(t), C.byref(sp)))
+    return t.value, sp.value
 
 
 def read_bse_in(path: str) -> dict:

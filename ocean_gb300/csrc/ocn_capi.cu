@@ -319,7 +319,8 @@ int ocn_ctx_destroy(ocn_ctx* c) {
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->hay_exec) cudaGraphExecDestroy(c->hay_exec);
-  for (void* p : {(void*)c->hay_vec, (void*)c->hay_coef, (void*)c->d_iter})
+  for (void* p : {(void*)c->hay_vec, (void*)c->hay_coef, (void*)c->d_iter, (void*)c->d_conv_sp,
+                  (void*)c->d_conv_rel})
     if (p) cudaFree(p);
   for (auto& ge : c->graph_events) {
     cudaEventDestroy(ge.second.first);
@@ -668,7 +669,9 @@ int haydock_iteration(ocn_ctx* c, int nv, double* old, double* psi, double* h, d
                                                : lr_apply_fp64(c, psi, psi + n);
     if (rc) return rc;
   }
-  return lanczos_launch(c, nv, old, psi, h, ra, ia, rb, cstride, c->d_iter);
+  rc = lanczos_launch(c, nv, old, psi, h, ra, ia, rb, cstride, c->d_iter);
+  if (rc == OCN_OK && c->conv_on && nv == 1) rc = conv_check_launch(c, ra, ia, rb, c->d_iter);
+  return rc;
 }
 
 void drop_haydock_graph(ocn_ctx* c) {
@@ -693,6 +696,16 @@ unsigned long long haydock_key(const ocn_ctx* c, int nv) {
   k ^= (unsigned long long)(c->ei_nonzero ? 1 : 0) << 7;
   for (int i = 0; i < 6; ++i) k ^= (unsigned long long)(c->sys.nhflag[i] & 1) << (8 + i);
   k ^= (unsigned long long)nv << 16;
+  if (c->conv_on && nv == 1) {  // the convergence test's launch parameters are part of the graph
+    const double v[5] = {c->conv.el, c->conv.eh, c->conv.gam0, c->conv.kpref, (double)c->conv.ne};
+    for (int i = 0; i < 5; ++i) {
+      unsigned long long b;
+      std::memcpy(&b, &v[i], 8);
+      k ^= (b * 0x9E3779B97F4A7C15ull) >> (i + 1);
+    }
+    k ^= ((unsigned long long)c->conv.spacing << 24) ^ (1ull << 23);
+    k ^= reinterpret_cast<uintptr_t>(c->d_conv_sp) ^ (reinterpret_cast<uintptr_t>(c->d_conv_rel) << 3);
+  }
   return k;
 }
 
@@ -749,9 +762,40 @@ int haydock_prepare(ocn_ctx* c, int nv, const double* p0r, const double* p0i, si
                           cudaMemcpyDeviceToDevice, c->stream);
   }
   if (e != cudaSuccess) return cuda_fail(c, e, "ocn_haydock setup");
+  if (c->conv_on && nv == 1) {  // early-exit test buffers (relArea per iteration, two spectra)
+    if (c->conv_cap_ne < c->conv.ne || c->conv_cap_iter < c->hay_cap) {
+      drop_haydock_graph(c);
+      if (c->d_conv_sp) cudaFree(c->d_conv_sp);
+      if (c->d_conv_rel) cudaFree(c->d_conv_rel);
+      c->d_conv_sp = c->d_conv_rel = nullptr;
+      c->conv_cap_ne = c->conv_cap_iter = 0;
+      if ((rc = dev_alloc(c, &c->d_conv_sp, 2 * (size_t)c->conv.ne)) ||
+          (rc = dev_alloc(c, &c->d_conv_rel, (size_t)c->hay_cap + 1)))
+        return rc;
+      c->conv_cap_ne = c->conv.ne;
+      c->conv_cap_iter = c->hay_cap;
+    }
+    OCN_CUDA(c, cudaMemsetAsync(c->d_conv_rel, 0, ((size_t)c->hay_cap + 1) * sizeof(double), c->stream));
+  }
   if (c->dims.precision == OCN_PREC_MIXED && (rc = mixed_prep_b1(c, R->buf[1], R->buf[1] + n, 2 * n, nv)))
     return rc;
   return OCN_OK;
+}
+
+// The early-exit rule (OCEAN_haydock.f90:268-292) over relArea values of
+// iterations from..to (rel indexed by iteration); prev carries prevConv
+// across calls.  Returns the stopping iteration or 0.
+int conv_stop(const ocn_ctx* c, const std::vector<double>& rel, int from, int to, bool* prev) {
+  for (int it = from; it <= to; ++it) {
+    if (it <= c->conv.spacing) continue;
+    if (rel[it] < c->conv.threshold) {
+      if (*prev) return it;
+      *prev = true;
+    } else {
+      *prev = false;
+    }
+  }
+  return 0;
 }
 
 // Captures three iterations, which rotate (old, psi, h) back to their starting
@@ -848,7 +892,14 @@ int haydock_finish(ocn_ctx* c, const HayRun& R, int done, bool graph_timing, dou
 // nv Lanczos chains from device psi0 planes (chain v: p0r + v*vstride, p0i + v*vstride).
 // Coefficients land in host arrays real_a/imag_a/real_b + v*(niter+1).
 int haydock_run(ocn_ctx* c, int nv, const double* p0r, const double* p0i, size_t vstride, int niter,
-                double* real_a, double* imag_a, double* real_b, int* niter_done) {
+                double* real_a, double* imag_a, double* real_b, int* niter_done, bool allow_conv = false) {
+  const bool conv_saved = c->conv_on;
+  c->conv_on = conv_saved && allow_conv && nv == 1;  // the early exit is for single-chain runs
+  struct Restore {
+    ocn_ctx* c;
+    bool v;
+    ~Restore() { c->conv_on = v; }
+  } restore{c, conv_saved};
   HayRun R;
   int rc = haydock_prepare(c, nv, p0r, p0i, vstride, niter, &R);
   if (rc) return rc;
@@ -867,14 +918,38 @@ int haydock_run(ocn_ctx* c, int nv, const double* p0r, const double* p0i, size_t
       }
       c->hay_key = key;
     }
-    for (int g = 0; g < ngraph; ++g) {
-      OCN_CUDA(c, cudaGraphLaunch(c->hay_exec, c->stream));
-      c->launches += c->hay_graph_kernels;
-    }
   }
-  int done = 3 * ngraph;
-  rc = haydock_remainder(c, R, done, &done);
-  const int rf = haydock_finish(c, R, done, ngraph > 0, real_a, imag_a, real_b, niter_done);
+  const bool conv = c->conv_on && nv == 1;
+  std::vector<double> rel(conv ? (size_t)niter + 1 : 0, 0.0);
+  bool prev = false;
+  int checked = 0, stop = 0;
+  // early exit: read the relArea of the steps so far and apply the rule
+  auto poll = [&](int upto) -> int {
+    OCN_CUDA(c, cudaMemcpyAsync(rel.data() + checked + 1, c->d_conv_rel + checked + 1,
+                                (size_t)(upto - checked) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+    stop = conv_stop(c, rel, checked + 1, upto, &prev);
+    checked = upto;
+    return OCN_OK;
+  };
+  int done = 0;
+  for (int g = 0; g < ngraph && !stop; ++g) {
+    OCN_CUDA(c, cudaGraphLaunch(c->hay_exec, c->stream));
+    c->launches += c->hay_graph_kernels;
+    done += 3;
+    if (conv && (g % 10 == 9 || g == ngraph - 1) && (rc = poll(done))) return rc;
+  }
+  if (!stop) {
+    rc = haydock_remainder(c, R, done, &done);
+    if (rc == OCN_OK && conv && done > checked) rc = poll(done);
+  }
+  const int rf = haydock_finish(c, R, stop ? stop : done, ngraph > 0, real_a, imag_a, real_b, niter_done);
+  if (stop && rf == OCN_OK && rc == OCN_OK)  // the steps computed past the stop are not part of the run
+    for (int i = stop; i <= niter; ++i) {
+      real_a[i] = 0.0;
+      if (imag_a) imag_a[i] = 0.0;
+      if (i > stop) real_b[i] = 0.0;
+    }
   return rc ? rc : rf;
 }
 
@@ -899,11 +974,28 @@ int haydock_block_impl(ocn_ctx* c, int nv, const double* d_psi0, int niter, doub
 
 }  // namespace
 
+int ocn_set_haydock_conv(ocn_ctx* c, const ocn_haydock_conv* p) {
+  if (!c) return OCN_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!p || !(p->threshold > 0.0)) {
+    if (c->conv_on) drop_haydock_graph(c);
+    c->conv_on = false;
+    return OCN_OK;
+  }
+  if (p->spacing < 1 || p->ne < 1 || !(p->eh > p->el) || !(p->gam0 >= 0.0))
+    return set_err(c, OCN_ERR_ARG, "ocn_set_haydock_conv: spacing >= 1, ne >= 1, eh > el, gam0 >= 0 required");
+  OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+  drop_haydock_graph(c);
+  c->conv = *p;
+  c->conv_on = true;
+  return OCN_OK;
+}
+
 int ocn_haydock_dev(ocn_ctx* c, const double* p0r, const double* p0i, int niter, double* real_a,
                     double* imag_a, double* real_b, int* niter_done) {
   if (!c || !p0r || !p0i || niter < 1 || !real_a || !real_b) return OCN_ERR_ARG;
   cudaSetDevice(c->device);
-  return haydock_run(c, 1, p0r, p0i, 0, niter, real_a, imag_a, real_b, niter_done);
+  return haydock_run(c, 1, p0r, p0i, 0, niter, real_a, imag_a, real_b, niter_done, true);
 }
 
 int ocn_haydock(ocn_ctx* c, const double* p0r, const double* p0i, int niter, double* real_a,

@@ -133,6 +133,42 @@ __global__ void k_write_core(const double* __restrict__ ra, const double* __rest
   r[8] = spct * tpacm4;
 }
 
+// check_convergence (OCEAN_haydock.f90:1608-1661) after the Lanczos step that
+// brought the device counter to it = *itp: calc_spect_core's column 3
+// (:1991-2027) at it and at it - spacing steps on the ne midpoints
+// el + (eh - el)(2i+1)/(2 ne), one thread per (spectrum, point).
+__global__ void k_conv_spect(const double* __restrict__ ra, const double* __restrict__ ia,
+                             const double* __restrict__ rb, const int* __restrict__ itp, int spacing, double kpref,
+                             double el, double eh, int ne, double gam0, double* __restrict__ sp) {
+  const int it = *itp;
+  if (it <= spacing) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 2 * ne) return;
+  const int which = i / ne, ie = i - which * ne;
+  const double e = el + (eh - el) * (double)(2 * ie + 1) / (double)(2 * ne);
+  const cplx d = cf_delta(ra, ia, rb, BcArrays{nullptr, nullptr, nullptr}, which ? it - spacing : it, e, gam0);
+  const double dr = d.x, di = fabs(d.y);
+  sp[i] = kpref * di / (dr * dr + di * di);
+}
+// relArea = 2 sum|sp1 - sp2| / (sum|sp1| + sum|sp2|) summed in energy order by
+// one thread, as the reference does (:1640-1652); rel[it] (0 when it <= spacing).
+__global__ void k_conv_rel(const double* __restrict__ sp, int ne, const int* __restrict__ itp, int spacing,
+                           double* __restrict__ rel) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int it = *itp;
+  if (it <= spacing) {
+    rel[it] = 0.0;
+    return;
+  }
+  double d = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int i = 0; i < ne; ++i) {
+    d += fabs(sp[i] - sp[ne + i]);
+    a1 += fabs(sp[i]);
+    a2 += fabs(sp[ne + i]);
+  }
+  rel[it] = 2.0 * d / (a1 + a2);
+}
+
 // Voigt variant: Lorentzian spectrum on the fine grid e_i = el + (i - nstep)*estep
 // (each fine point of write_core_Voigt evaluated once), with damping gam[i].
 __global__ void k_cf_points(const double* __restrict__ ra, const double* __restrict__ ia,
@@ -241,6 +277,18 @@ __global__ void k_write_val(const double* __restrict__ ra, const double* __restr
 }  // namespace
 
 void val_optical_host(double ere, double er, double ei, double* o) { val_optical(ere, er, ei, o); }
+
+int conv_check_launch(ocn_ctx* c, const double* ra, const double* ia, const double* rb, const int* itp) {
+  const ocn_haydock_conv& p = c->conv;
+  k_conv_spect<<<(2 * p.ne + 127) / 128, 128, 0, c->stream>>>(ra, ia, rb, itp, p.spacing, p.kpref, p.el, p.eh,
+                                                               p.ne, p.gam0, c->d_conv_sp);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  k_conv_rel<<<1, 32, 0, c->stream>>>(c->d_conv_sp, p.ne, itp, p.spacing, c->d_conv_rel);
+  ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
 
 int val_spectrum_eval(const double* ra, const double* ia, const double* rb, const double* ib, const double* rc,
                       const double* ic, int iter, const ocn_val_cf_params* p, double* out, std::string* err) {

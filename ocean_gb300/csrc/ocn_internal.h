@@ -143,6 +143,13 @@ struct ocn_ctx {
 
   int gmres_lanes = 1;         // energy lanes of the GMRES sweep (ocn_gmres_set_lanes)
 
+  // Haydock early exit (haydockconv.ipt): test parameters and device buffers
+  bool conv_on = false;
+  ocn_haydock_conv conv{};
+  double* d_conv_sp = nullptr;   // 2*ne: the two test spectra
+  double* d_conv_rel = nullptr;  // relArea per iteration (hay_cap + 1)
+  int conv_cap_ne = 0, conv_cap_iter = 0;
+
   // Haydock loop: persistent buffers and the captured 3-iteration CUDA graph
   double* hay_vec = nullptr;   // old | psi | h, each 2*npsi
   double* hay_coef = nullptr;  // real_a | imag_a | real_b, each hay_cap+1
@@ -319,6 +326,8 @@ int cf_eval(const double* ra, const double* ia, const double* rb, int iter, doub
 int val_spectrum_eval(const double* ra, const double* ia, const double* rb, const double* ib, const double* rc,
                       const double* ic, int iter, const ocn_val_cf_params* p, double* out, std::string* err);
 void val_optical_host(double ere, double er, double ei, double* o);
+// check_convergence after the Lanczos step that set *itp (graph-capturable)
+int conv_check_launch(ocn_ctx* c, const double* ra, const double* ia, const double* rb, const int* itp);
 int cf_eval_noalloc(const double* ra, const double* ia, const double* rb, int iter, double kpref,
                     const ocn_cf_params* p, double* out, std::string* err);
 

@@ -345,6 +345,18 @@ int ocn_read_bse_in(const char* path, ocn_bse_in* out, double* energies, int cap
   return OCN_OK;
 }
 
+int ocn_read_haydockconv(const char* path, double* threshold, int* spacing) {
+  if (!path || !threshold || !spacing) return set_err(nullptr, OCN_ERR_ARG, "ocn_read_haydockconv: null argument");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  std::vector<std::string> v;
+  // read(99, *) haydockConvergeThreshold, haydockConvergeSpacing (OCEAN_system.f90:455)
+  const bool ok = ld_read(f, 2, &v) && ld_real(v[0], threshold) && ld_int(v[1], spacing);
+  std::fclose(f);
+  if (!ok) return set_err(nullptr, OCN_ERR_ARG, "haydockconv.ipt: expected a real and an integer");
+  return OCN_OK;
+}
+
 int ocn_write_abslanc(const char* path, int n, double kpref, const double* real_a, const double* imag_a,
                       const double* real_b, const double* imag_b, const double* real_c, const double* imag_c,
                       const double* eigs) {

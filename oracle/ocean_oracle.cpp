@@ -952,6 +952,110 @@ int or_calc_spect_core(const double* ra, const double* ia, const double* rb, int
   return 0;
 }
 
+// check_convergence (OCEAN_haydock.f90:1608-1661), core branch: the calc_spect_core
+// spectra of iter1 and iter2 steps on the ne midpoints; relArea =
+// 2 sum|sp1 - sp2| / (sum|sp1| + sum|sp2|), maxDiff = max|sp1 - sp2| (column 3,
+// sums in energy order).
+int or_check_convergence(const double* ra, const double* ia, const double* rb, int iter1, int iter2, double kpref,
+                         double el, double eh, int ne, double gam0, double* max_diff, double* rel_area) {
+  std::vector<double> sp1(3 * (size_t)ne), sp2(3 * (size_t)ne);
+  or_calc_spect_core(ra, ia, rb, iter1, kpref, el, eh, ne, gam0, 0.0, sp1.data());
+  or_calc_spect_core(ra, ia, rb, iter2, kpref, el, eh, ne, gam0, 0.0, sp2.data());
+  double md = 0.0, rel = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int i = 0; i < ne; ++i) {
+    const double diff = std::fabs(sp1[3 * i + 2] - sp2[3 * i + 2]);
+    if (diff > md) md = diff;
+    rel += diff;
+    a1 += std::fabs(sp1[3 * i + 2]);
+    a2 += std::fabs(sp2[3 * i + 2]);
+  }
+  *max_diff = md;
+  *rel_area = 2.0 * rel / (a1 + a2);
+  return 0;
+}
+
+// Stopping iteration of the early exit of OCEAN_haydock_Herm_do
+// (OCEAN_haydock.f90:268-292) from the relArea of each iteration
+// (rel[iter], iter = spacing+1 .. niter): the first iter whose relArea and the
+// previous iteration's are both below the threshold (prevConv), else niter.
+int or_early_exit_iter(const double* rel, int niter, int spacing, double threshold) {
+  bool prev = false;
+  for (int iter = 1; iter <= niter; ++iter) {
+    if (threshold > 0.0 && iter > spacing) {
+      if (rel[iter] < threshold) {
+        if (prev) return iter;
+        prev = true;
+      } else {
+        prev = false;
+      }
+    }
+  }
+  return niter;
+}
+
+// OCEAN_haydock_Herm_do with haydockconv.ipt (earlyExit): the Lanczos run of
+// or_haydock, with check_convergence after every step beyond the spacing;
+// rel_out[iter] (may be NULL) receives each relArea (0 where not checked).
+int or_haydock_conv(const or_dims* d, const or_ops* o, const double* p0r, const double* p0i, int niter,
+                    double threshold, int spacing, double kpref, double el, double eh, int ne, double gam0,
+                    double* real_a, double* imag_a, double* real_b, double* rel_out, int* niter_done) {
+  const size_t n = (size_t)d->nb * nk_of(d) * d->na;
+  std::vector<double> psr(p0r, p0r + n), psi_(p0i, p0i + n);
+  std::vector<double> olr(n, 0.0), oli(n, 0.0), hr(n), hi(n);
+  for (int i = 0; i <= niter; ++i) real_a[i] = imag_a[i] = real_b[i] = 0.0;
+  if (rel_out)
+    for (int i = 0; i <= niter; ++i) rel_out[i] = 0.0;
+  bool prev = false;
+  int done = 0;
+  for (int iter = 1; iter <= niter; ++iter) {
+    or_xact(d, o, psr.data(), psi_.data(), hr.data(), hi.data(), nullptr, 0);
+    double bm = -real_b[iter - 1];
+    for (size_t i = 0; i < n; ++i) {
+      hr[i] += bm * olr[i];
+      hi[i] += bm * oli[i];
+    }
+    double ar = 0.0, ai = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+      ar += hr[i] * psr[i] + hi[i] * psi_[i];
+      ai += hr[i] * psi_[i] - hi[i] * psr[i];
+    }
+    real_a[iter - 1] = ar;
+    for (size_t i = 0; i < n; ++i) {
+      hr[i] += -ar * psr[i];
+      hi[i] += -ar * psi_[i];
+    }
+    double bb = 0.0;
+    for (size_t i = 0; i < n; ++i) bb += hr[i] * hr[i] + hi[i] * hi[i];
+    olr = psr;
+    oli = psi_;
+    real_b[iter] = std::sqrt(bb);
+    double inv = 1.0 / real_b[iter];
+    for (size_t i = 0; i < n; ++i) {
+      psr[i] = hr[i] * inv;
+      psi_[i] = hi[i] * inv;
+    }
+    imag_a[iter - 1] = ai;
+    done = iter;
+    if (std::isnan(real_a[iter - 1])) {
+      *niter_done = done;
+      return -1;
+    }
+    if (threshold > 0.0 && iter > spacing) {
+      double md, rel;
+      or_check_convergence(real_a, imag_a, real_b, iter, iter - spacing, kpref, el, eh, ne, gam0, &md, &rel);
+      if (rel_out) rel_out[iter] = rel;
+      if (rel < threshold) {
+        if (prev) break;
+        prev = true;
+      } else {
+        prev = false;
+      }
+    }
+  }
+  *niter_done = done;
+  return 0;
+}
+
 // redtrid (OCEAN_haydock.f90:2273-2316): eigenvalues of the (n+1)x(n+1) Hermitian
 // tridiagonal with diagonal real_a(0:n) and off-diagonal real_b(1:n).  elsch
 // (EISPACK htridi + tqlrat) is restated as the equivalent symmetric tridiagonal

@@ -115,6 +115,17 @@ int or_write_val(const double* real_a, const double* imag_a, const double* real_
 int or_calc_spect_core(const double* real_a, const double* imag_a, const double* real_b, int iter,
                        double kpref, double el, double eh, int ne, double gam0, double ebase,
                        double* out);
+/* check_convergence (OCEAN_haydock.f90:1608-1661), core branch. */
+int or_check_convergence(const double* real_a, const double* imag_a, const double* real_b, int iter1, int iter2,
+                         double kpref, double el, double eh, int ne, double gam0, double* max_diff,
+                         double* rel_area);
+/* The early-exit rule of OCEAN_haydock_Herm_do (OCEAN_haydock.f90:268-292) on
+ * per-iteration relArea values rel[0..niter]. */
+int or_early_exit_iter(const double* rel, int niter, int spacing, double threshold);
+/* Hermitian Haydock with the haydockconv.ipt early exit. */
+int or_haydock_conv(const or_dims* d, const or_ops* o, const double* p0r, const double* p0i, int niter,
+                    double threshold, int spacing, double kpref, double el, double eh, int ne, double gam0,
+                    double* real_a, double* imag_a, double* real_b, double* rel_out, int* niter_done);
 /* gamfcn (CNBSE/zcmsnmult/zf90/gamfcn.f90:8-42). */
 double or_gamfcn(double e, double n, double e0);
 /* redtrid eigenvalues (OCEAN_haydock.f90:2273-2316). */

@@ -170,6 +170,24 @@ class OracleProblem:
                               dptr(ra), dptr(ia), dptr(rb), C.byref(done))
         return rc, ra, ia, rb, done.value
 
+    def haydock_conv(self, niter, threshold, spacing, ne, el=None, eh=None, gam0=None, pr=None, pi=None):
+        """Haydock with the haydockconv.ipt early exit (OCEAN_haydock.f90:268-292,
+        check_convergence :1608-1661): returns rc, a, ia, b, niter_actual and the
+        relArea of each checked iteration."""
+        w = self.w
+        pr = w.psi_r if pr is None else pr
+        pi = w.psi_i if pi is None else pi
+        el = w.el if el is None else el
+        eh = w.eh if eh is None else eh
+        gam0 = w.gam0 if gam0 is None else gam0
+        ra, ia, rb, rel = (np.zeros(niter + 1) for _ in range(4))
+        done = C.c_int(0)
+        rc = lib().or_haydock_conv(C.byref(self.d), C.byref(self.o), dptr(np.ascontiguousarray(pr)),
+                                   dptr(np.ascontiguousarray(pi)), niter, C.c_double(threshold), int(spacing),
+                                   C.c_double(w.kpref), C.c_double(el), C.c_double(eh), int(ne), C.c_double(gam0),
+                                   dptr(ra), dptr(ia), dptr(rb), dptr(rel), C.byref(done))
+        return rc, ra, ia, rb, done.value, rel
+
     def haydock_nonherm(self, niter, pr=None, pi=None):
         """Two-sided Lanczos (OCEAN_haydock.f90:53-164,1250-1433): complex a, b, c."""
         w = self.w
@@ -196,6 +214,32 @@ class OracleProblem:
                             C.c_double(gprc), C.c_double(ffff), max_restarts, dptr(ore), dptr(oim),
                             dptr(rel), iptr(its), C.byref(tot))
         return rc, ore, oim, rel, its, tot.value
+
+
+def calc_spect_core(ra, ia, rb, it, kpref, el, eh, ne, gam0, ebase=0.0):
+    """calc_spect_core (OCEAN_haydock.f90:1991-2027): ne x 3 (energy, Re, Im part columns)."""
+    out = np.zeros(ne * 3)
+    lib().or_calc_spect_core(dptr(np.ascontiguousarray(ra, dtype=np.float64)),
+                             dptr(np.ascontiguousarray(ia, dtype=np.float64)),
+                             dptr(np.ascontiguousarray(rb, dtype=np.float64)), it, C.c_double(kpref),
+                             C.c_double(el), C.c_double(eh), ne, C.c_double(gam0), C.c_double(ebase), dptr(out))
+    return out.reshape(ne, 3)
+
+
+def check_convergence(ra, ia, rb, iter1, iter2, kpref, el, eh, ne, gam0):
+    """check_convergence (OCEAN_haydock.f90:1608-1661): (maxDiff, relArea)."""
+    md, rel = C.c_double(0.0), C.c_double(0.0)
+    lib().or_check_convergence(dptr(np.ascontiguousarray(ra, dtype=np.float64)),
+                               dptr(np.ascontiguousarray(ia, dtype=np.float64)),
+                               dptr(np.ascontiguousarray(rb, dtype=np.float64)), iter1, iter2, C.c_double(kpref),
+                               C.c_double(el), C.c_double(eh), ne, C.c_double(gam0), C.byref(md), C.byref(rel))
+    return md.value, rel.value
+
+
+def early_exit_iter(rel, niter, spacing, threshold):
+    """The stopping iteration of the early exit for per-iteration relArea values."""
+    return int(lib().or_early_exit_iter(dptr(np.ascontiguousarray(rel, dtype=np.float64)), niter, int(spacing),
+                                        C.c_double(threshold)))
 
 
 def write_core(ra, ia, rb, it, kpref, el, eh, ne, gam0, ebase=0.0, gam_gauss=0.0, ucvol=1.0,

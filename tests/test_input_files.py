@@ -216,3 +216,19 @@ def test_val_pair_energies_blocks(lib_built):
         for j in range(2):
             want = ec[j][:, None, clo - 1:clo - 1 + nc] - ev[i][:, vlo - 1:vlo - 1 + nv, None]
             assert np.array_equal(out[i * 2 + j], want)
+
+
+def test_read_haydockconv(tmp_path, lib_built):
+    """haydockconv.ipt holds the early-exit threshold and spacing, read
+    list-directed (OCEAN_system.f90:452-458)."""
+    from ocean_gb300 import capi
+
+    capi.load(lib_built)
+    p = tmp_path / "haydockconv.ipt"
+    p.write_text("  1.0d-3   5\n")
+    assert capi.read_haydockconv(str(p)) == (1.0e-3, 5)
+    p.write_text("0.02, 10 ! threshold, spacing\n")
+    assert capi.read_haydockconv(str(p)) == (0.02, 10)
+    p.write_text("0.02\n")
+    with pytest.raises(capi.OcnError):
+        capi.read_haydockconv(str(p))

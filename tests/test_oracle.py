@@ -273,3 +273,79 @@ def test_two_sided_lanczos_spectrum_is_the_adjoint_resolvent(oracle_lib):
         z = w.el + (w.eh - w.el) * r / ne + 1j * w.gam0
         ex[r] = w.kpref * abs(np.vdot(v0, np.linalg.solve(z * np.eye(n) - A.conj().T, v0)).imag)
     assert np.linalg.norm(s[:, 2] - ex) < 1e-5 * np.linalg.norm(ex)
+
+
+@pytest.mark.parametrize("photon", [1, 4])
+def test_calc_spect_core_is_write_core_on_the_midpoints(oracle_lib, kat, photon):
+    """calc_spect_core (OCEAN_haydock.f90:1991-2027) evaluates write_core's
+    fraction on the ne midpoints el + (eh - el)(2i+1)/(2ne): on the reference's
+    own Lanczos coefficients it equals, bit for bit, the odd rows of write_core
+    at 2 ne (which is pinned to the golden absspct files)."""
+    O = oracle_lib
+    p = f"p{photon}"
+    n = int(kat[p + "_n"])
+    kp = float(kat[p + "_kpref"])
+    el, eh = float(kat["el_ev"]) * WL.EV2HARTREE, float(kat["eh_ev"]) * WL.EV2HARTREE
+    gam = float(kat["gam0_ev"]) * WL.EV2HARTREE
+    ne = 400
+    ra, rb = kat[p + "_real_a"], kat[p + "_real_b"]
+    ia = np.zeros_like(ra)
+    sp = O.calc_spect_core(ra, ia, rb, n, kp, el, eh, ne, gam)
+    wc = O.write_core(ra, ia, rb, n, kp, el, eh, 2 * ne, gam)
+    assert np.array_equal(sp[:, 2], wc[1::2, 2])
+    assert np.array_equal(sp[:, 1], wc[1::2, 4])
+    assert np.array_equal(sp[:, 0], wc[1::2, 0])
+
+
+def test_check_convergence_rel_area(oracle_lib, kat):
+    """relArea = 2 sum|sp1 - sp2| / (sum|sp1| + sum|sp2|) over calc_spect_core's
+    column 3, maxDiff its largest term (OCEAN_haydock.f90:1640-1652)."""
+    O = oracle_lib
+    n = int(kat["p1_n"])
+    ra, rb = kat["p1_real_a"], kat["p1_real_b"]
+    ia = np.zeros_like(ra)
+    kp = float(kat["p1_kpref"])
+    el, eh, gam = -1.0, 2.5, 0.05
+    md, rel = O.check_convergence(ra, ia, rb, 150, 140, kp, el, eh, 300, gam)
+    s1 = O.calc_spect_core(ra, ia, rb, 150, kp, el, eh, 300, gam)[:, 2]
+    s2 = O.calc_spect_core(ra, ia, rb, 140, kp, el, eh, 300, gam)[:, 2]
+    d, a1, a2 = 0.0, 0.0, 0.0
+    for i in range(300):
+        d += abs(s1[i] - s2[i])
+        a1 += abs(s1[i])
+        a2 += abs(s2[i])
+    assert rel == 2.0 * d / (a1 + a2)
+    assert md == np.max(np.abs(s1 - s2))
+    assert n >= 150
+
+
+def test_early_exit_two_in_a_row(oracle_lib):
+    """The early exit stops at the first iteration whose relArea and the
+    previous one's are both below the threshold (prevConv,
+    OCEAN_haydock.f90:275-290); a single pass is not enough."""
+    O = oracle_lib
+    rel = np.array([0, 0, 0, 0.5, 0.01, 0.5, 0.01, 0.02, 0.001, 0.001])
+    assert O.early_exit_iter(rel, 9, 2, 0.05) == 7
+    assert O.early_exit_iter(rel, 9, 2, 0.005) == 9      # 8 and 9 pass
+    assert O.early_exit_iter(rel, 9, 2, 0.0) == 9        # off
+    assert O.early_exit_iter(rel, 6, 2, 0.05) == 6       # never twice in a row up to 6
+
+
+def test_haydock_early_exit_matches_plain_run(tiny_problem, oracle_lib):
+    """The early-exit run computes the same coefficients as the plain run up to
+    its stopping iteration, which is the rule's answer on the relArea of each
+    iteration recomputed from the plain run's coefficients."""
+    O = oracle_lib
+    w, P = tiny_problem
+    niter, spacing, ne = 24, 3, 200
+    rc, ra, ia, rb, done = P.haydock(niter)
+    rels = np.zeros(niter + 1)
+    for it in range(spacing + 1, niter + 1):
+        rels[it] = O.check_convergence(ra, ia, rb, it, it - spacing, w.kpref, w.el, w.eh, ne, w.gam0)[1]
+    thr = float(np.sort(rels[spacing + 1:])[niter // 2])  # some threshold that is met part-way
+    stop = O.early_exit_iter(rels, niter, spacing, thr)
+    assert spacing + 2 <= stop < niter
+    rc2, ra2, ia2, rb2, done2, rel2 = P.haydock_conv(niter, thr, spacing, ne)
+    assert rc2 == 0 and done2 == stop
+    assert np.array_equal(ra2[:stop], ra[:stop]) and np.array_equal(rb2[:stop + 1], rb[:stop + 1])
+    assert np.array_equal(rel2[spacing + 1:stop + 1], rels[spacing + 1:stop + 1])
