@@ -480,6 +480,26 @@ int ocn_output_filename(const char* kind, const char* calc_type, const char* eln
 int ocn_read_u2dat(const char* path, int nx, int ny, int nz, int nkpts, int nspn, int nband_file,
                    const int* first, int nfirst, int nbd, double* re, double* im);
 
+/* u2par.dat, the 'new' Bloch-state format (load_new_u2, OCEAN_bloch.f90:697-996,
+ * chosen by bloch_type = 'new'): a raw complex(DP) array without record frames;
+ * the states of (k-point, spin) start at element (k + spin*nkpts)*width3*Nx
+ * (width3 = the third line of obf_control), the first[] bands of each are
+ * skipped (first as in ocn_read_u2dat) and nbd bands read, each band over the
+ * x-mesh with iz fastest.  Output as ocn_read_u2dat: re_bloch_state(nbd,
+ * nkpts, Nx, nspn), x = ix + nx*(iy + ny*iz). */
+int ocn_read_u2par(const char* path, const int xmesh[3], int nkpts, int nspn, int width3, const int* first,
+                   int nfirst, int nbd, double* re, double* im);
+/* con.u2.dat of a core-level run, the 'par' route that ocean.x takes whenever
+ * con.u2.dat exists (OCEAN_bloch.f90:481-482; single_load_prefixu2dat :998-1115;
+ * val.u2.dat for XES): stream access, per spin, k-point and file band one
+ * complex(DP) array over the Nx x-points in the states' order; bands_in_file
+ * bands per k-point (brange(4) - brange(3) + 1), the first nbd kept.  Output as
+ * ocn_read_u2dat. */
+int ocn_read_con_u2(const char* path, int nxpts, int nkpts, int nspn, int bands_in_file, int nbd, double* re,
+                    double* im);
+/* obf_control: the three widths of the 'new' format (OCEAN_bloch.f90:722-727). */
+int ocn_read_obf_control(const char* path, int width[3]);
+
 /* rpottrim.z<El><idx>_n<nn>l<ll> (long_range.f90:1689-1698): a header record
  * (a word, nptab) then nptab records ptab rtab.  With ptab and rtab NULL only
  * *nptab is returned; otherwise up to cap samples (OCN_ERR_ARG if more). */

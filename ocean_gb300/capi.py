@@ -97,6 +97,7 @@ EXPORTS = [
     "ocn_val_spectrum", "ocn_val_optical_constants", "ocn_write_opcons", "ocn_val_set_fxc",
     "ocn_val_fxc_from_rho", "ocn_read_val_u2", "ocn_val_pair_energies", "ocn_test_starve_tc",
     "ocn_gmres_set_lanes", "ocn_set_haydock_conv", "ocn_read_haydockconv",
+    "ocn_read_u2par", "ocn_read_con_u2", "ocn_read_obf_control",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -607,6 +608,55 @@ def read_u2dat(path: str, nx: int, ny: int, nz: int, nkpts: int, nspn: int, nban
     check(load().ocn_read_u2dat(path.encode(), nx, ny, nz, nkpts, nspn, nband_file, f.ctypes.data_as(IP), len(f),
                                 nbd, _dp(re), _dp(im)))
     return re, im
+
+
+def read_u2par(path: str, xmesh, nkpts: int, nspn: int, width3: int, first, nbd: int):
+    """u2par.dat ('new' format) -> (re, im) shaped like read_u2dat's."""
+    f = np.ascontiguousarray(np.atleast_1d(first), dtype=np.int32)
+    nxyz = int(np.prod(xmesh))
+    re = np.zeros((nspn, nxyz, nkpts, nbd))
+    im = np.zeros_like(re)
+    check(load().ocn_read_u2par(path.encode(), (C.c_int * 3)(*xmesh), nkpts, nspn, int(width3),
+                                f.ctypes.data_as(IP), len(f), nbd, _dp(re), _dp(im)))
+    return re, im
+
+
+def read_con_u2(path: str, nxpts: int, nkpts: int, nspn: int, bands_in_file: int, nbd: int):
+    """con.u2.dat of a core run ('par' route) -> (re, im) shaped like read_u2dat's."""
+    re = np.zeros((nspn, nxpts, nkpts, nbd))
+    im = np.zeros_like(re)
+    check(load().ocn_read_con_u2(path.encode(), nxpts, nkpts, nspn, bands_in_file, nbd, _dp(re), _dp(im)))
+    return re, im
+
+
+def read_obf_control(path: str):
+    w = (C.c_int * 3)()
+    check(load().ocn_read_obf_control(path.encode(), w))
+    return tuple(w)
+
+
+def load_bloch_states(run_dir: str, xmesh, nkpts: int, nspn: int, nbd: int, first=0, bands_in_file=None,
+                      calc_type: str = "XAS"):
+    """The Bloch states of a core-level run directory, chosen as ocean.x chooses
+    (OCEAN_bloch.f90:470-482): con.u2.dat (val.u2.dat for XES) present -> the
+    'par' stream file; else bloch_type 'new' -> u2par.dat with obf_control's
+    widths; else u2.dat ('old').  bands_in_file: bands per k-point in the 'par'
+    file (brange(4) - brange(3) + 1) or in u2.dat; first: the skipped bands of
+    the 'old' and 'new' formats.  Returns (format, re, im)."""
+    par = os.path.join(run_dir, "val.u2.dat" if calc_type == "XES" else "con.u2.dat")
+    if os.path.exists(par):
+        nb_file = nbd if bands_in_file is None else bands_in_file
+        return ("par",) + read_con_u2(par, int(np.prod(xmesh)), nkpts, nspn, nb_file, nbd)
+    btype = "old"
+    bt = os.path.join(run_dir, "bloch_type")
+    if os.path.exists(bt):
+        with open(bt) as fh:
+            btype = fh.read().split()[0].strip("'\"")
+    if btype == "new":
+        width = read_obf_control(os.path.join(run_dir, "obf_control"))
+        return ("new",) + read_u2par(os.path.join(run_dir, "u2par.dat"), xmesh, nkpts, nspn, width[2], first, nbd)
+    nb_file = nbd if bands_in_file is None else bands_in_file
+    return ("old",) + read_u2dat(os.path.join(run_dir, "u2.dat"), *xmesh, nkpts, nspn, nb_file, first, nbd)
 
 
 def read_rpottrim(path: str):

@@ -503,6 +503,91 @@ int ocn_read_u2dat(const char* path, int nx, int ny, int nz, int nkpts, int nspn
   return OCN_OK;
 }
 
+int ocn_read_u2par(const char* path, const int xmesh[3], int nkpts, int nspn, int width3, const int* first,
+                   int nfirst, int nbd, double* re, double* im) {
+  if (!path || !xmesh || !first || !re || !im || nkpts < 1 || nspn < 1 || nbd < 1 || width3 < nbd ||
+      (nfirst != 1 && nfirst != nkpts * nspn))
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_read_u2par: bad argument");
+  const int n1 = xmesh[0], n2 = xmesh[1], n3 = xmesh[2];
+  if (n1 < 1 || n2 < 1 || n3 < 1) return set_err(nullptr, OCN_ERR_ARG, "ocn_read_u2par: bad mesh");
+  const size_t nx = (size_t)n1 * n2 * n3;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  // load_new_u2 (OCEAN_bloch.f90:697-996): a raw array of complex(DP); the states
+  // of (k-point iq, spin) start at element ((iq-1) + (ispn-1) nkpts) width(3) Nx,
+  // the first ivh2 bands are skipped, and each band is u2_buf(iz, iy, ix) with iz
+  // fastest; it lands in re_bloch_state(band, iq, x, spin), x = ix + nx(iy + ny iz)
+  std::vector<double> buf(2 * nx * (size_t)nbd);
+  int rc = OCN_OK;
+  for (int sp = 0; sp < nspn && rc == OCN_OK; ++sp)
+    for (int k = 0; k < nkpts && rc == OCN_OK; ++k) {
+      const int f0 = first[nfirst == 1 ? 0 : k + nkpts * sp];
+      if (f0 < 0 || f0 + nbd > width3) {
+        rc = set_err(nullptr, OCN_ERR_ARG, "u2par.dat: band window outside width(3)");
+        break;
+      }
+      const long long off = (((long long)k + (long long)sp * nkpts) * width3 + f0) * (long long)nx * 16;
+      if (std::fseek(f, (long)off, SEEK_SET) != 0 || std::fread(buf.data(), sizeof(double), buf.size(), f) != buf.size()) {
+        rc = set_err(nullptr, OCN_ERR_ARG, "u2par.dat: file ends early");
+        break;
+      }
+      size_t ii = 0;
+      for (int b = 0; b < nbd; ++b)
+        for (int ix = 0; ix < n1; ++ix)
+          for (int iy = 0; iy < n2; ++iy)
+            for (int iz = 0; iz < n3; ++iz, ++ii) {
+              const size_t x = (size_t)ix + (size_t)n1 * ((size_t)iy + (size_t)n2 * iz);
+              const size_t o = (size_t)b + (size_t)nbd * ((size_t)k + (size_t)nkpts * (x + nx * sp));
+              re[o] = buf[2 * ii];
+              im[o] = buf[2 * ii + 1];
+            }
+    }
+  std::fclose(f);
+  return rc;
+}
+
+int ocn_read_con_u2(const char* path, int nxpts, int nkpts, int nspn, int bands_in_file, int nbd, double* re,
+                    double* im) {
+  if (!path || !re || !im || nxpts < 1 || nkpts < 1 || nspn < 1 || nbd < 1 || bands_in_file < nbd)
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_read_con_u2: bad argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  // single_load_prefixu2dat (OCEAN_bloch.f90:998-1115): stream access, for each
+  // spin, k-point and file band one complex(DP) array over the x-mesh in the
+  // order the states use; bands beyond num_bands are read and dropped
+  const size_t nx = (size_t)nxpts;
+  std::vector<double> buf(2 * nx);
+  int rc = OCN_OK;
+  for (int sp = 0; sp < nspn && rc == OCN_OK; ++sp)
+    for (int k = 0; k < nkpts && rc == OCN_OK; ++k)
+      for (int b = 0; b < bands_in_file; ++b) {
+        if (std::fread(buf.data(), sizeof(double), 2 * nx, f) != 2 * nx) {
+          rc = set_err(nullptr, OCN_ERR_ARG, "con.u2.dat: file ends early");
+          break;
+        }
+        if (b >= nbd) continue;
+        for (size_t x = 0; x < nx; ++x) {
+          const size_t o = (size_t)b + (size_t)nbd * ((size_t)k + (size_t)nkpts * (x + nx * sp));
+          re[o] = buf[2 * x];
+          im[o] = buf[2 * x + 1];
+        }
+      }
+  std::fclose(f);
+  return rc;
+}
+
+int ocn_read_obf_control(const char* path, int width[3]) {
+  if (!path || !width) return set_err(nullptr, OCN_ERR_ARG, "ocn_read_obf_control: null argument");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  std::vector<std::string> v;
+  bool ok = true;
+  for (int i = 0; i < 3 && ok; ++i) ok = ld_read(f, 1, &v) && ld_int(v[0], &width[i]);  // three read(99,*)
+  std::fclose(f);
+  if (!ok) return set_err(nullptr, OCN_ERR_ARG, "obf_control: expected three integers");
+  return OCN_OK;
+}
+
 int ocn_read_rpottrim(const char* path, int* nptab, double* ptab, double* rtab, int cap) {
   if (!path || !nptab) return set_err(nullptr, OCN_ERR_ARG, "ocn_read_rpottrim: null argument");
   FILE* f = std::fopen(path, "r");

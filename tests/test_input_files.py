@@ -232,3 +232,80 @@ def test_read_haydockconv(tmp_path, lib_built):
     p.write_text("0.02\n")
     with pytest.raises(capi.OcnError):
         capi.read_haydockconv(str(p))
+
+
+def test_u2par_new_format_layout_and_window(lib, tmp_path):
+    """u2par.dat (load_new_u2, OCEAN_bloch.f90:697-996): raw complex(DP), each
+    (k-point, spin) block width(3) bands long, ivh2 bands skipped, iz fastest
+    within a band; lands as re_bloch_state(band, k, x, spin), x = ix + nx(iy + ny iz)."""
+    xm, nk, nspn, width3, nbd = (2, 3, 4), 3, 2, 6, 3
+    nx, ny, nz = xm
+    first = [0, 1, 2, 3, 1, 0]  # per (k-point, spin), k fastest
+    rng = np.random.default_rng(8)
+    data = rng.standard_normal((nspn, nk, width3, nx, ny, nz)) + 1j * rng.standard_normal((nspn, nk, width3, nx, ny, nz))
+    p = str(tmp_path / "u2par.dat")
+    data.astype(np.complex128).tofile(p)  # C order (..., ix, iy, iz): iz fastest, as u2_buf(iz, iy, ix, band)
+    re, im = capi.read_u2par(p, xm, nk, nspn, width3, first, nbd)
+    for s in range(nspn):
+        for q in range(nk):
+            f0 = first[q + nk * s]
+            for b in range(nbd):
+                for ix in range(nx):
+                    for iy in range(ny):
+                        for iz in range(nz):
+                            x = ix + nx * (iy + ny * iz)
+                            assert re[s, x, q, b] == data[s, q, f0 + b, ix, iy, iz].real
+                            assert im[s, x, q, b] == data[s, q, f0 + b, ix, iy, iz].imag
+    with pytest.raises(capi.OcnError):  # window beyond width(3)
+        capi.read_u2par(p, xm, nk, nspn, width3, 4, nbd)
+    with open(str(tmp_path / "short"), "wb") as fh:
+        fh.write(data.astype(np.complex128).tobytes()[:-16])
+    with pytest.raises(capi.OcnError):  # the last block's window reaches the (cut) end of the file
+        capi.read_u2par(str(tmp_path / "short"), xm, nk, nspn, width3, width3 - nbd, nbd)
+
+
+def test_run_directory_formats_feed_the_library_layout(lib, tmp_path):
+    """A workload's Bloch functions written in each of the three formats the
+    core run reads (u2.dat 'old', u2par.dat 'new' with bloch_type and
+    obf_control, con.u2.dat 'par' which wins whenever it exists) come back
+    through load_bloch_states as exactly the arrays ocn_set_bloch takes."""
+    from ocean_gb300 import workloads as WL
+
+    w = WL.make("tiny", seed=5)
+    nx, ny, nz = w.xmesh
+    nxyz, nb, nk = nx * ny * nz, w.nb, w.nk
+    u = (w.ur + 1j * w.ui).reshape(w.nspn, nxyz, nk, nb)  # [s][x][k][n]
+    xyz = [(ix, iy, iz) for ix in range(nx) for iy in range(ny) for iz in range(nz)]
+    # 'old'
+    d_old = tmp_path / "old"
+    d_old.mkdir()
+
+    def vals(s, q, b, ix, iy, iz):
+        v = u[s, ix + nx * (iy + ny * iz), q, b - 1]
+        return v.real, v.imag
+
+    _write_u2dat(str(d_old / "u2.dat"), vals, nx, ny, nz, nk, w.nspn, nb + 2, [1] * (nk * w.nspn), nb)
+    fmt, re, im = capi.load_bloch_states(str(d_old), w.xmesh, nk, w.nspn, nb, first=1, bands_in_file=nb + 2)
+    assert fmt == "old" and np.array_equal(re.ravel(), w.ur) and np.array_equal(im.ravel(), w.ui)
+    # 'new': two occupied bands skipped, width(3) = nb + 3
+    d_new = tmp_path / "new"
+    d_new.mkdir()
+    (d_new / "bloch_type").write_text("new\n")
+    (d_new / "obf_control").write_text(f"1\n1\n{nb + 3}\n")
+    blk = np.zeros((w.nspn, nk, nb + 3, nx, ny, nz), dtype=np.complex128)
+    for s in range(w.nspn):
+        for q in range(nk):
+            for (ix, iy, iz) in xyz:
+                blk[s, q, 2:2 + nb, ix, iy, iz] = u[s, ix + nx * (iy + ny * iz), q, :]
+    blk.tofile(str(d_new / "u2par.dat"))
+    fmt, re, im = capi.load_bloch_states(str(d_new), w.xmesh, nk, w.nspn, nb, first=2)
+    assert fmt == "new" and np.array_equal(re.ravel(), w.ur) and np.array_equal(im.ravel(), w.ui)
+    # 'par': con.u2.dat present (bloch_type says 'new' and is overridden), two extra bands per k
+    (d_new / "con.u2.dat").write_bytes(b"")
+    par = np.zeros((w.nspn, nk, nb + 2, nxyz), dtype=np.complex128)
+    par[:, :, :nb, :] = np.transpose(u, (0, 2, 3, 1))
+    par.tofile(str(d_new / "con.u2.dat"))
+    fmt, re, im = capi.load_bloch_states(str(d_new), w.xmesh, nk, w.nspn, nb, bands_in_file=nb + 2)
+    assert fmt == "par" and np.array_equal(re.ravel(), w.ur) and np.array_equal(im.ravel(), w.ui)
+    with pytest.raises(capi.OcnError):  # file shorter than bands_in_file promises
+        capi.load_bloch_states(str(d_new), w.xmesh, nk, w.nspn, nb, bands_in_file=nb + 3)
