@@ -171,6 +171,27 @@ int ocn_get_bloch(ocn_ctx* ctx, double* re, double* im);
 /* Multiplet projector data (OCEAN_multiplet.f90:248-570). */
 int ocn_set_mult(ocn_ctx* ctx, const ocn_mult_data* m);
 
+/* nbsemhsetup2 (OCEAN_multiplet.f90:2007-2181): the multiplet exchange
+ * matrix of one valence angular momentum lv from Slater radial integrals, on
+ * the host.  Basis (OCEAN_multiplet.f90:342-369), i = nu + np*((m_v + lv) +
+ * (2lv+1)*alpha), alpha = (core spin, core m, valence spin) with the valence
+ * spin fastest: mham = 4(2lc+1)(2lv+1)np.  F^k (k = kfl, kfl+2, .., kfh;
+ * normally 2 .. min(2lc, 2lv), 0 .. 0 for tdlda's kk files) and G^k (k = kgl,
+ * kgl+2, .., kgh; |lc-lv| .. lc+lv) are np x np column-major slices in eV with
+ * scale factors scfk / scgk; scfac multiplies all.  Writes mhr/mhi(mham, mham)
+ * in the layout ocn_mult_data.mhr takes for this l, in Hartree (the eV2Hartree
+ * of OCEAN_multiplet.f90:386-387).  The angular integrals (threey,
+ * CNBSE/zcmsnmult/zf90/newthreey.f90) are the closed-form Gaunt coefficients of
+ * the complex spherical harmonics the reference evaluates by quadrature. */
+int ocn_mult_exchange(int lc, int lv, int np, int kfl, int kfh, const double* fk, const double* scfk, int kgl,
+                      int kgh, const double* gk, const double* scgk, double scfac, double* mhr, double* mhi);
+/* threey: the integral of conj(Y_{ll,ml}) Y_{lm,mm} Y_{lr,mr} over the sphere
+ * (Y_{lm,mm} conjugated when conjug != 0). */
+double ocn_threey(int ll, int ml, int lm, int mm, int lr, int mr, int conjug);
+/* A Slater-integral file fk<lc><lv><k><add10>, gk.., kk.. (OCEAN_multiplet.f90:
+ * 2087-2120): np*np list-directed values (column order) and the scale factor. */
+int ocn_read_slater(const char* path, int np, double* f, double* scale);
+
 /* Spin-orbit matrix somelr + i someli, (Na,Na) (OCEAN_multiplet.f90:572-690). */
 int ocn_set_spin_orbit(ocn_ctx* ctx, const double* somelr, const double* someli);
 

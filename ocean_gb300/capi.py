@@ -98,6 +98,7 @@ EXPORTS = [
     "ocn_val_fxc_from_rho", "ocn_read_val_u2", "ocn_val_pair_energies", "ocn_test_starve_tc",
     "ocn_gmres_set_lanes", "ocn_set_haydock_conv", "ocn_read_haydockconv",
     "ocn_read_u2par", "ocn_read_con_u2", "ocn_read_obf_control",
+    "ocn_mult_exchange", "ocn_threey", "ocn_read_slater",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -657,6 +658,50 @@ def load_bloch_states(run_dir: str, xmesh, nkpts: int, nspn: int, nbd: int, firs
         return ("new",) + read_u2par(os.path.join(run_dir, "u2par.dat"), xmesh, nkpts, nspn, width[2], first, nbd)
     nb_file = nbd if bands_in_file is None else bands_in_file
     return ("old",) + read_u2dat(os.path.join(run_dir, "u2.dat"), *xmesh, nkpts, nspn, nb_file, first, nbd)
+
+
+def mult_exchange(lc: int, lv: int, fk: dict, gk: dict, scfk: dict = None, scgk: dict = None, scfac: float = 1.0):
+    """nbsemhsetup2: the exchange matrix of valence l = lv (Hartree, the
+    reference's (mham, mham) layout flattened) from Slater integrals in eV.
+    fk / gk: {k: (np, np) array} (F^k for k = 2..min(2lc, 2lv), G^k for
+    k = |lc-lv|..lc+lv); scfk / scgk: {k: scale} (default 1)."""
+    np_ = None
+    for d in (fk, gk):
+        for a in d.values():
+            np_ = np.asarray(a).shape[0]
+    kf = sorted(fk)
+    kg = sorted(gk)
+
+    def stack(d, ks, sc):
+        if not ks:
+            return None, None, 0, -1
+        arr = np.concatenate([np.asarray(d[k], dtype=np.float64).reshape(np_, np_).T.reshape(-1) for k in ks])
+        scl = np.array([1.0 if sc is None else sc.get(k, 1.0) for k in ks])
+        return arr, scl, ks[0], ks[-1]
+
+    fa, fs, kfl, kfh = stack(fk, kf, scfk)
+    ga, gs, kgl, kgh = stack(gk, kg, scgk)
+    mham = 4 * (2 * lc + 1) * (2 * lv + 1) * np_
+    mhr, mhi = np.zeros(mham * mham), np.zeros(mham * mham)
+    lib = load()
+    check(lib.ocn_mult_exchange(lc, lv, np_, kfl, kfh, None if fa is None else _dp(fa), None if fs is None else _dp(fs),
+                                kgl, kgh, None if ga is None else _dp(ga), None if gs is None else _dp(gs),
+                                C.c_double(scfac), _dp(mhr), _dp(mhi)))
+    return mhr, mhi
+
+
+def threey(ll, ml, lm, mm, lr, mr, conjug=False) -> float:
+    lib = load()
+    lib.ocn_threey.restype = C.c_double
+    return float(lib.ocn_threey(ll, ml, lm, mm, lr, mr, int(bool(conjug))))
+
+
+def read_slater(path: str, np_: int):
+    """fk/gk/kk file -> ((np, np) array as fk(:, :, k), scale)."""
+    f = np.zeros(np_ * np_)
+    sc = C.c_double(0.0)
+    check(load().ocn_read_slater(path.encode(), np_, _dp(f), C.byref(sc)))
+    return f.reshape(np_, np_, order="F"), sc.value
 
 
 def read_rpottrim(path: str):

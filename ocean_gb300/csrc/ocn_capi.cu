@@ -1465,6 +1465,22 @@ int ocn_gmres_vjp(ocn_ctx* c, const double* d_hay, double kpref, const double* e
   return OCN_OK;
 }
 
+int ocn_mult_exchange(int lc, int lv, int np, int kfl, int kfh, const double* fk, const double* scfk, int kgl,
+                      int kgh, const double* gk, const double* scgk, double scfac, double* mhr, double* mhi) {
+  if (lc < 0 || lc > 3 || lv < 0 || lv > 5 || np < 1 || !mhr || !mhi)
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_mult_exchange: lc in 0..3, lv in 0..5, np >= 1 required");
+  if (kfh >= kfl && (kfl < 0 || (kfl & 1) || ((kfh - kfl) & 1) || !fk || !scfk))
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_mult_exchange: F^k range must be even with fk and scfk given");
+  if (kgh >= kgl && (kgl < 0 || ((kgh - kgl) & 1) || !gk || !scgk))
+    return set_err(nullptr, OCN_ERR_ARG, "ocn_mult_exchange: G^k range must step by 2 with gk and scgk given");
+  mult_exchange_matrix(lc, lv, np, kfl, kfh, fk, scfk, kgl, kgh, gk, scgk, scfac, mhr, mhi);
+  return OCN_OK;
+}
+
+double ocn_threey(int ll, int ml, int lm, int mm, int lr, int mr, int conjug) {
+  return gaunt_threey(ll, ml, lm, mm, lr, mr, conjug);
+}
+
 int ocn_w2_vjp(const ocn_dims* d, const ocn_lr_params* p, const double* G, double* g_ptab, double* g_scale) {
   if (!d || !p || !p->rtab || !p->ptab || p->nptab < 2 || p->epsilon0 <= 0.0 || !G || !g_ptab || !g_scale)
     return set_err(nullptr, OCN_ERR_ARG, "ocn_w2_vjp: bad argument");

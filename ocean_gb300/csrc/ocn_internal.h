@@ -240,6 +240,11 @@ void w2_vjp(const ocn_dims& d, const ocn_lr_params& p, const double tau[3], cons
 void soprep(int core_l, double xi, std::vector<double>& r, std::vector<double>& i);
 int redtrid_eigs(int n, const double* ra, const double* rb, double* w);
 double gamfcn(double e, double n, double e0);
+// nbsemhsetup2 (OCEAN_multiplet.f90:2007-2181): mhr/mhi(mham, mham) of one
+// valence l, reference layout, Hartree; returns mham
+int mult_exchange_matrix(int lc, int lv, int np, int kfl, int kfh, const double* fk, const double* scfk, int kgl,
+                         int kgh, const double* gk, const double* scgk, double scfac, double* mhr, double* mhi);
+double gaunt_threey(int ll, int ml, int lm, int mm, int lr, int mr, int conjug);
 
 // ---- FP64 kernels (ocn_kernels.cu)
 int upload_twiddles(ocn_ctx* c);

@@ -588,6 +588,22 @@ int ocn_read_obf_control(const char* path, int width[3]) {
   return OCN_OK;
 }
 
+int ocn_read_slater(const char* path, int np, double* f, double* scale) {
+  if (!path || np < 1 || !f || !scale) return set_err(nullptr, OCN_ERR_ARG, "ocn_read_slater: bad argument");
+  FILE* fh = std::fopen(path, "r");
+  if (!fh) return set_err(nullptr, OCN_ERR_ARG, std::string("cannot open ") + path);
+  // read(99, *) fk(:, :, k), scfk(k) (OCEAN_multiplet.f90:2094-2097): np*np values
+  // in column order, then the scale factor
+  std::vector<std::string> v;
+  const size_t n = (size_t)np * np;
+  bool ok = ld_read(fh, n + 1, &v);
+  for (size_t i = 0; ok && i < n; ++i) ok = ld_real(v[i], &f[i]);
+  ok = ok && ld_real(v[n], scale);
+  std::fclose(fh);
+  if (!ok) return set_err(nullptr, OCN_ERR_ARG, std::string("Slater file ") + path + ": expected np*np values and a scale");
+  return OCN_OK;
+}
+
 int ocn_read_rpottrim(const char* path, int* nptab, double* ptab, double* rtab, int cap) {
   if (!path || !nptab) return set_err(nullptr, OCN_ERR_ARG, "ocn_read_rpottrim: null argument");
   FILE* f = std::fopen(path, "r");

@@ -326,4 +326,125 @@ int redtrid_eigs(int n, const double* ra, const double* rb, double* w) {
   return 0;
 }
 
+// ---- nbsemhsetup2 (OCEAN_multiplet.f90:2007-2181): the exchange matrices of
+// the multiplet term from Slater integrals and angular algebra.
+namespace {
+
+double lfact(int n) {  // log(n!)
+  return std::lgamma((double)n + 1.0);
+}
+
+// Wigner 3j symbol (j1 j2 j3; m1 m2 m3) for integer arguments (Racah's formula).
+double wigner3j(int j1, int j2, int j3, int m1, int m2, int m3) {
+  if (m1 + m2 + m3 != 0) return 0.0;
+  if (j3 < std::abs(j1 - j2) || j3 > j1 + j2) return 0.0;
+  if (std::abs(m1) > j1 || std::abs(m2) > j2 || std::abs(m3) > j3) return 0.0;
+  const double tri = 0.5 * (lfact(j1 + j2 - j3) + lfact(j1 - j2 + j3) + lfact(-j1 + j2 + j3) - lfact(j1 + j2 + j3 + 1));
+  const double pre = 0.5 * (lfact(j1 + m1) + lfact(j1 - m1) + lfact(j2 + m2) + lfact(j2 - m2) + lfact(j3 + m3) +
+                            lfact(j3 - m3));
+  const int t0 = std::max(std::max(0, j2 - j3 - m1), j1 - j3 + m2);
+  const int t1 = std::min(std::min(j1 + j2 - j3, j1 - m1), j2 + m2);
+  double sum = 0.0;
+  for (int t = t0; t <= t1; ++t) {
+    const double den = lfact(t) + lfact(j3 - j2 + t + m1) + lfact(j3 - j1 + t - m2) + lfact(j1 + j2 - j3 - t) +
+                       lfact(j1 - t - m1) + lfact(j2 - t + m2);
+    sum += ((t & 1) ? -1.0 : 1.0) * std::exp(tri + pre - den);
+  }
+  return ((j1 - j2 - m3) & 1) ? -sum : sum;
+}
+
+// threey (CNBSE/zcmsnmult/zf90/newthreey.f90): integral over the sphere of
+// conj(Y_{ll,ml}) Y_{lm,mm} Y_{lr,mr} (Y_{lm,mm} conjugated when conjug), with
+// the complex spherical harmonics of newgetylm (Condon-Shortley phase).  The
+// reference integrates it by quadrature in cos(theta) at phi = 0 (times 2 pi,
+// the phi integral of the m-selected integrand); here it is the closed form
+// (-1)^ml sqrt((2ll+1)(2lm+1)(2lr+1)/4pi) (ll lm lr; 0 0 0)(ll lm lr; -ml mm mr),
+// with conj(Y_{l,m}) = (-1)^m Y_{l,-m}.  The reference's selection rules
+// (m balance, lm in ll+lr, ll+lr-2, ..., max(|mm|, |ll-lr|)) give the same zeros.
+double threey(int ll, int ml, int lm, int mm, int lr, int mr, bool conjug) {
+  double sign = 1.0;
+  if (conjug) {
+    if (mm & 1) sign = -1.0;
+    mm = -mm;
+  }
+  if (ml != mm + mr) return 0.0;
+  if (((ll + lm + lr) & 1) != 0) return 0.0;
+  const double pi = 3.14159265358979323846;
+  const double pre = std::sqrt((2.0 * ll + 1.0) * (2.0 * lm + 1.0) * (2.0 * lr + 1.0) / (4.0 * pi));
+  const double s_ml = (ml & 1) ? -1.0 : 1.0;
+  return sign * s_ml * pre * wigner3j(ll, lm, lr, 0, 0, 0) * wigner3j(ll, lm, lr, -ml, mm, mr);
+}
+
+}  // namespace
+
+int mult_exchange_matrix(int lc, int lv, int np, int kfl, int kfh, const double* fk, const double* scfk, int kgl,
+                         int kgh, const double* gk, const double* scgk, double scfac, double* mhr, double* mhi) {
+  const int na = 4 * (2 * lc + 1);
+  const int mham = na * (2 * lv + 1) * np;
+  // the basis of OCEAN_multiplet.f90:342-369: alpha = (core spin, core m, valence
+  // spin) with the valence spin fastest, then valence m, then the radial index nu
+  // fastest of all
+  std::vector<int> cms(mham), cml(mham), vms(mham), vml(mham), vnu(mham);
+  {
+    int ii = 0;
+    for (int icms = -1; icms <= 1; icms += 2)
+      for (int icml = -lc; icml <= lc; ++icml)
+        for (int ivms = -1; ivms <= 1; ivms += 2)
+          for (int ivml = -lv; ivml <= lv; ++ivml)
+            for (int nu = 0; nu < np; ++nu, ++ii) {
+              cms[ii] = icms;  // 2 * spin
+              cml[ii] = icml;
+              vms[ii] = ivms;
+              vml[ii] = ivml;
+              vnu[ii] = nu;
+            }
+  }
+  const double pi = 3.14159265358979323846;
+  const double ev2ha = 0.036749322175666;
+  const size_t npp = (size_t)np * np;
+  for (int i2 = 0; i2 < mham; ++i2)
+    for (int i1 = 0; i1 < mham; ++i1) {
+      const int nu1 = vnu[i1], nu2 = vnu[i2];
+      double acc = 0.0;
+      if (kfh >= kfl && fk) {  // direct Slater F^k part
+        const int m1 = cml[i2], s1 = cms[i2], m2 = vml[i1], s2 = vms[i1];
+        const int m3 = cml[i1], s3 = cms[i1], m4 = vml[i2], s4 = vms[i2];
+        if (s1 == s3 && s2 == s4 && m1 + m2 == m3 + m4) {
+          const int mk = m1 - m3;
+          for (int k = kfl; k <= kfh; k += 2) {
+            if (std::abs(mk) > k) continue;
+            const int ik = (k - kfl) / 2;
+            const double ffk = scfk[ik] * fk[ik * npp + nu1 + (size_t)np * nu2] * scfac;
+            const double f1 = threey(lc, m1, k, mk, lc, m3, false);
+            const double f2 = threey(lv, m2, k, mk, lv, m4, true);
+            acc += -ffk * f1 * f2 * (4.0 * pi / (2.0 * k + 1.0));
+          }
+        }
+      }
+      if (kgh >= kgl && gk) {  // exchange Slater G^k part
+        const int m1 = cml[i2], s1 = cms[i2], m2 = vml[i1], s2 = vms[i1];
+        const int m3 = vml[i2], s3 = vms[i2], m4 = cml[i1], s4 = cms[i1];
+        if (s1 == s3 && s2 == s4 && m1 + m2 == m3 + m4) {
+          const int mk = m1 - m3;
+          for (int k = kgl; k <= kgh; k += 2) {
+            if (std::abs(mk) > k) continue;
+            const int ik = (k - kgl) / 2;
+            const double ggk = scgk[ik] * gk[ik * npp + nu1 + (size_t)np * nu2] * scfac;
+            const double f1 = threey(lc, m1, k, mk, lv, m3, false);
+            const double f2 = threey(lv, m2, k, mk, lc, m4, true);
+            acc += ggk * f1 * f2 * (4.0 * pi / (2.0 * k + 1.0));
+          }
+        }
+      }
+      // mhr_l(i1, i2), i1 fastest; eV -> Hartree as OCEAN_create_central does (:386-387)
+      mhr[(size_t)i1 + (size_t)mham * i2] = acc * ev2ha;
+      mhi[(size_t)i1 + (size_t)mham * i2] = 0.0;
+    }
+  return mham;
+}
+
+double gaunt_threey(int ll, int ml, int lm, int mm, int lr, int mr, int conjug) {
+  return threey(ll, ml, lm, mm, lr, mr, conjug != 0);
+}
+
 }  // namespace ocn

@@ -21,6 +21,11 @@ Value recipe (identical bytes are fed to the oracle and the GPU library):
                    1/(eps r) itself.  The table is positive: long_range.f90:943-961
                    subtracts conj(u) phi, which supplies the attraction.
   * psi0           complex Gaussian normalised by core_pnorm (kpref returned)
+  * multiplet      (c3) projector coefficients complex Gaussian / sqrt(Nb Nk);
+                   monopole matrices mpm and the Slater integrals F^k, G^k
+                   U(0.5, 8) eV, symmetric in the radial indices; the exchange
+                   matrices built from F^k, G^k by the library's restatement of
+                   nbsemhsetup2 (OCEAN_multiplet.f90:2007-2181)
 
 Everything is in Hartree / Bohr, the units ocean.x works in.
 """
@@ -163,6 +168,20 @@ def batch_instance(i: int, u2_device: Optional[str] = None) -> "Workload":
                 u2_device=u2_device)
 
 
+def _library():
+    """The library (built in-tree when missing): the multiplet workloads take
+    their exchange matrices from its nbsemhsetup2 restatement."""
+    from ocean_gb300 import capi
+
+    try:
+        capi.load()
+    except RuntimeError:
+        from ocean_gb300 import build
+
+        build.build()
+        capi.load()
+
+
 def make(name: str, seed: int = 0, nb: Optional[int] = None, kmesh=None, xmesh=None,
          core_l: Optional[int] = None, with_mult: Optional[bool] = None,
          u2_device: Optional[str] = None, nspn: int = 1) -> Workload:
@@ -255,15 +274,25 @@ def make(name: str, seed: int = 0, nb: Optional[int] = None, kmesh=None, xmesh=N
             npl = nproj[li]
             f = rng.uniform(0.5, 8.0, size=(npl, npl))
             mpm[li, :npl, :npl] = 0.5 * (f + f.T) * EV2HARTREE
+        # exchange matrices from Slater radial integrals F^k, G^k ~ U(0.5, 8) eV
+        # (symmetric in the two radial indices) through nbsemhsetup2's angular
+        # algebra (OCEAN_multiplet.f90:2007-2181), as the library builds them
+        from ocean_gb300 import capi
+
+        _library()
         mh_r, mh_i = [], []
         for li, l in enumerate(range(lmin, lmax + 1)):
-            mham = na * (2 * l + 1) * nproj[li]
-            gmat = (rng.uniform(0.5, 8.0, size=(mham, mham)) *
-                    np.exp(2j * math.pi * rng.uniform(size=(mham, mham))))
-            h = 0.5 * (gmat + gmat.conj().T) * EV2HARTREE / math.sqrt(mham)
-            # row ii contiguous: C order of an (ii, jj) array
-            mh_r.append(h.real.reshape(-1))
-            mh_i.append(h.imag.reshape(-1))
+            npl = nproj[li]
+
+            def slater():
+                a = rng.uniform(0.5, 8.0, size=(npl, npl))
+                return 0.5 * (a + a.T)
+
+            fk = {k: slater() for k in range(2, min(2 * lc, 2 * l) + 1, 2)}
+            gk = {k: slater() for k in range(abs(lc - l), lc + l + 1, 2)}
+            mr, mi = capi.mult_exchange(lc, l, fk, gk)
+            mh_r.append(mr)
+            mh_i.append(mi)
         w.mult = dict(lmin=lmin, lmax=lmax, nproj=np.array(nproj, dtype=np.int32), npmax=npmax,
                       mpcr=mpcr.reshape(-1), mpci=mpci.reshape(-1),
                       mpm=mpm.reshape(-1), mhr=np.concatenate(mh_r), mhi=np.concatenate(mh_i))

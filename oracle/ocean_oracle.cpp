@@ -1056,6 +1056,187 @@ int or_haydock_conv(const or_dims* d, const or_ops* o, const double* p0r, const 
   return 0;
 }
 
+// ---- nbsemhsetup2 (OCEAN_multiplet.f90:2007-2181) with threey
+// (CNBSE/zcmsnmult/zf90/newthreey.f90), newgetylm and newgetprefs.
+
+}  // extern "C"
+
+namespace {
+
+// Gauss-Legendre nodes and weights on [-1, 1] (the role of the Pquadrature file;
+// weights rescaled to sum to 2 as nbsemhsetup2 does).
+void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < n; ++i) {
+    double z = std::cos(pi * (i + 0.75) / (n + 0.5));
+    double dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int l = 2; l <= n; ++l) {
+        const double p2 = ((2.0 * l - 1.0) * z * p1 - (l - 1.0) * p0) / l;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    x[i] = z;
+    w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+  double su = 0.0;
+  for (double v : w) su += v;
+  for (double& v : w) v = v * 2.0 / su;
+}
+
+// newgetylm at (x, y, z) on the unit sphere: prefs(l,|m|) f(l,|m|)(u) (x + i y)^m,
+// m < 0: times (-(x - i y))^|m|; f = (-1)^m d^m P_l / du^m (the table of newgetylm),
+// prefs = sqrt((2l+1)/(4 pi) (l-|m|)!/(l+|m|)!) (newgetprefs).
+cd ylm_ref(int l, int m, double x, double y, double z) {
+  const double pi = 3.14159265358979323846;
+  const int am = std::abs(m);
+  // m-th derivative of P_l at u = z: coefficients of P_l by the three-term recurrence
+  std::vector<std::vector<double>> P(l + 1, std::vector<double>(l + 1, 0.0));
+  P[0][0] = 1.0;
+  if (l >= 1) P[1][1] = 1.0;
+  for (int n = 2; n <= l; ++n)
+    for (int k = 0; k <= n; ++k) {
+      double v = 0.0;
+      if (k >= 1) v += (2.0 * n - 1.0) * P[n - 1][k - 1];
+      v -= (n - 1.0) * P[n - 2][k];
+      P[n][k] = v / n;
+    }
+  double f = 0.0;
+  for (int k = am; k <= l; ++k) {
+    double c = P[l][k];
+    for (int j = 0; j < am; ++j) c *= (double)(k - j);
+    f += c * std::pow(z, k - am);
+  }
+  if (am & 1) f = -f;
+  double pref = (2.0 * l + 1.0) / (4.0 * pi);
+  for (int j = 1; j <= am; ++j) pref /= (double)((l - j + 1) * (l + j));
+  cd y0(std::sqrt(pref) * f, 0.0);
+  for (int j = 0; j < am; ++j) y0 *= (m > 0) ? cd(x, y) : -cd(x, -y);
+  return y0;
+}
+
+cd threey_ref(int ll, int ml, int lmid, int mmid, int lr, int mr, bool conjug, const std::vector<double>& xq,
+              const std::vector<double>& wq) {
+  const double pi = 3.14159265358979323846;
+  cd i0(0.0, 0.0);
+  const bool mdo = conjug ? (ml == mr - mmid) : (ml == mr + mmid);
+  bool ldo = false;
+  for (int j = ll + lr; j >= std::max(std::abs(mmid), std::abs(ll - lr)); j -= 2)
+    if (j == lmid) ldo = true;
+  if (!(ldo && mdo)) return i0;
+  for (size_t j = 0; j < xq.size(); ++j) {  // phi = 0
+    const double ct = xq[j], st = std::sqrt(1.0 - ct * ct);
+    const cd yl = ylm_ref(ll, ml, st, 0.0, ct);
+    cd ym = ylm_ref(lmid, mmid, st, 0.0, ct);
+    if (conjug) ym = std::conj(ym);
+    const cd yr = ylm_ref(lr, mr, st, 0.0, ct);
+    i0 += wq[j] * std::conj(yl) * ym * yr;
+  }
+  return i0 * (2.0 * pi);
+}
+
+}  // namespace
+
+extern "C" {
+
+double or_threey(int ll, int ml, int lm, int mm, int lr, int mr, int conjug, int npt) {
+  std::vector<double> xq, wq;
+  gauss_legendre(npt, xq, wq);
+  return threey_ref(ll, ml, lm, mm, lr, mr, conjug != 0, xq, wq).real();
+}
+
+int or_nbsemhsetup2(int lc, int lv, int np, int kfl, int kfh, const double* fk, const double* scfk, int kgl,
+                    int kgh, const double* gk, const double* scgk, double scfac, int npt, double* mhr_out,
+                    double* mhi_out) {
+  std::vector<double> xq, wq;
+  gauss_legendre(npt, xq, wq);
+  const int nalpha = 4 * (2 * lc + 1);
+  const int mham = nalpha * (2 * lv + 1) * np;
+  // hcms, hcml, hvms, hvml, hvnu of OCEAN_multiplet.f90:342-369
+  std::vector<double> cms(mham), cml(mham), vms(mham), vml(mham);
+  std::vector<int> vnu(mham);
+  std::vector<double> acms, acml, avms;
+  for (int icms = -1; icms <= 1; icms += 2)
+    for (int icml = -lc; icml <= lc; ++icml)
+      for (int ivms = -1; ivms <= 1; ivms += 2) {
+        acms.push_back(0.5 * icms);
+        acml.push_back(icml);
+        avms.push_back(0.5 * ivms);
+      }
+  int ii = 0;
+  for (int ic = 0; ic < nalpha; ++ic)
+    for (int ivml = -lv; ivml <= lv; ++ivml)
+      for (int nu = 1; nu <= np; ++nu, ++ii) {
+        cms[ii] = acms[ic];
+        cml[ii] = acml[ic];
+        vms[ii] = avms[ic];
+        vml[ii] = ivml;
+        vnu[ii] = nu;
+      }
+  const double pi = 4.0 * std::atan(1.0);
+  const size_t npp = (size_t)np * np;
+  auto nint = [](double v) { return (int)std::lround(v); };
+  for (int i1 = 0; i1 < mham; ++i1) {
+    const int nu1 = vnu[i1] - 1;
+    for (int i2 = 0; i2 < mham; ++i2) {
+      const int nu2 = vnu[i2] - 1;
+      double mr = 0.0, mi = 0.0;
+      if (kfh >= kfl) {
+        const int l1 = lc, m1 = nint(cml[i2]), s1 = nint(2 * cms[i2]);
+        const int l2 = lv, m2 = nint(vml[i1]), s2 = nint(2 * vms[i1]);
+        const int l3 = lc, m3 = nint(cml[i1]), s3 = nint(2 * cms[i1]);
+        const int l4 = lv, m4 = nint(vml[i2]), s4 = nint(2 * vms[i2]);
+        if (s1 == s3 && s2 == s4) {
+          const int mk = m1 - m3;
+          if (m1 + m2 == m3 + m4)
+            for (int k = kfl; k <= kfh; k += 2)
+              if (std::abs(mk) <= k) {
+                const int ik = (k - kfl) / 2;
+                const double ffk = scfk[ik] * fk[ik * npp + nu1 + (size_t)np * nu2] * scfac;
+                const cd f1 = threey_ref(l1, m1, k, mk, l3, m3, false, xq, wq);
+                const cd f2 = threey_ref(l2, m2, k, mk, l4, m4, true, xq, wq);
+                const cd ct = -ffk * f1 * f2 * (4 * pi / (2 * k + 1));
+                mr += ct.real();
+                mi += ct.imag();
+              }
+        }
+      }
+      if (kgh >= kgl) {
+        const int l1 = lc, m1 = nint(cml[i2]), s1 = nint(2 * cms[i2]);
+        const int l2 = lv, m2 = nint(vml[i1]), s2 = nint(2 * vms[i1]);
+        const int l3 = lv, m3 = nint(vml[i2]), s3 = nint(2 * vms[i2]);
+        const int l4 = lc, m4 = nint(cml[i1]), s4 = nint(2 * cms[i1]);
+        if (s1 == s3 && s2 == s4) {
+          const int mk = m1 - m3;
+          if (m1 + m2 == m3 + m4)
+            for (int k = kgl; k <= kgh; k += 2)
+              if (std::abs(mk) <= k) {
+                const int ik = (k - kgl) / 2;
+                const double ggk = scgk[ik] * gk[ik * npp + nu1 + (size_t)np * nu2] * scfac;
+                const cd f1 = threey_ref(l1, m1, k, mk, l3, m3, false, xq, wq);
+                const cd f2 = threey_ref(l2, m2, k, mk, l4, m4, true, xq, wq);
+                const cd ct = ggk * f1 * f2 * (4 * pi / (2 * k + 1));
+                mr += ct.real();
+                mi += ct.imag();
+              }
+        }
+      }
+      // mhr_l(i1, i2) then the eV -> Hartree of OCEAN_create_central (:386-387)
+      mhr_out[(size_t)i1 + (size_t)mham * i2] = mr * kEV2Ha;
+      mhi_out[(size_t)i1 + (size_t)mham * i2] = mi * kEV2Ha;
+    }
+  }
+  return mham;
+}
+
 // redtrid (OCEAN_haydock.f90:2273-2316): eigenvalues of the (n+1)x(n+1) Hermitian
 // tridiagonal with diagonal real_a(0:n) and off-diagonal real_b(1:n).  elsch
 // (EISPACK htridi + tqlrat) is restated as the equivalent symmetric tridiagonal

@@ -126,6 +126,12 @@ int or_early_exit_iter(const double* rel, int niter, int spacing, double thresho
 int or_haydock_conv(const or_dims* d, const or_ops* o, const double* p0r, const double* p0i, int niter,
                     double threshold, int spacing, double kpref, double el, double eh, int ne, double gam0,
                     double* real_a, double* imag_a, double* real_b, double* rel_out, int* niter_done);
+/* nbsemhsetup2 (OCEAN_multiplet.f90:2007-2181) with threey by npt-point
+ * Gauss-Legendre quadrature; mhr/mhi(mham, mham), Hartree. */
+int or_nbsemhsetup2(int lc, int lv, int np, int kfl, int kfh, const double* fk, const double* scfk, int kgl,
+                    int kgh, const double* gk, const double* scgk, double scfac, int npt, double* mhr,
+                    double* mhi);
+double or_threey(int ll, int ml, int lm, int mm, int lr, int mr, int conjug, int npt);
 /* gamfcn (CNBSE/zcmsnmult/zf90/gamfcn.f90:8-42). */
 double or_gamfcn(double e, double n, double e0);
 /* redtrid eigenvalues (OCEAN_haydock.f90:2273-2316). */

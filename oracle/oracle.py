@@ -57,6 +57,7 @@ def lib():
         L.or_intval.restype = C.c_double
         L.or_pnorm.restype = C.c_double
         L.or_gamfcn.restype = C.c_double
+        L.or_threey.restype = C.c_double
         L.or_val_wall_length.restype = C.c_double
     return _LIB
 
@@ -240,6 +241,37 @@ def early_exit_iter(rel, niter, spacing, threshold):
     """The stopping iteration of the early exit for per-iteration relArea values."""
     return int(lib().or_early_exit_iter(dptr(np.ascontiguousarray(rel, dtype=np.float64)), niter, int(spacing),
                                         C.c_double(threshold)))
+
+
+def nbsemhsetup2(lc, lv, fk, gk, scfk=None, scgk=None, scfac=1.0, npt=16):
+    """The exchange matrix of valence l = lv (OCEAN_multiplet.f90:2007-2181),
+    threey by npt-point Gauss-Legendre quadrature: (mhr, mhi) flat, (mham,
+    mham) with i1 fastest, Hartree.  fk / gk: {k: (np, np) array} in eV."""
+    npr = None
+    for d in (fk, gk):
+        for a in d.values():
+            npr = np.asarray(a).shape[0]
+
+    def stack(d, sc):
+        ks = sorted(d)
+        if not ks:
+            return None, None, 0, -1
+        arr = np.concatenate([np.asarray(d[k], dtype=np.float64).T.reshape(-1) for k in ks])
+        scl = np.array([1.0 if sc is None else sc.get(k, 1.0) for k in ks])
+        return arr, scl, ks[0], ks[-1]
+
+    fa, fs, kfl, kfh = stack(fk, scfk)
+    ga, gs, kgl, kgh = stack(gk, scgk)
+    mham = 4 * (2 * lc + 1) * (2 * lv + 1) * npr
+    mhr, mhi = np.zeros(mham * mham), np.zeros(mham * mham)
+    lib().or_nbsemhsetup2(lc, lv, npr, kfl, kfh, None if fa is None else dptr(fa), None if fs is None else dptr(fs),
+                          kgl, kgh, None if ga is None else dptr(ga), None if gs is None else dptr(gs),
+                          C.c_double(scfac), npt, dptr(mhr), dptr(mhi))
+    return mhr, mhi
+
+
+def threey(ll, ml, lm, mm, lr, mr, conjug=False, npt=16):
+    return float(lib().or_threey(ll, ml, lm, mm, lr, mr, int(bool(conjug)), npt))
 
 
 def write_core(ra, ia, rb, it, kpref, el, eh, ne, gam0, ebase=0.0, gam_gauss=0.0, ucvol=1.0,

@@ -17,7 +17,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_symbols():
     txt = open(os.path.join(ROOT, "include", "ocean_gpu.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*|long long|void\*)\s+(ocn_\w+)\(", txt,
+    return sorted(set(re.findall(r"^\s*(?:int|double|const char\*|long long|void\*)\s+(ocn_\w+)\(", txt,
                                  re.M)))
 
 
