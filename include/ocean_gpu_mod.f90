@@ -61,7 +61,13 @@ module ocean_gpu_mod
 
   public :: ocn_ctx_create, ocn_ctx_destroy, ocn_set_system, ocn_set_energies, ocn_set_allow
   public :: ocn_set_bloch, ocn_lr_init, ocn_soprep, ocn_apply_H, ocn_haydock, ocn_spectrum_cf
-  public :: ocn_gmres, ocn_redtrid
+  public :: ocn_gmres, ocn_redtrid, ocn_gmres_set_lanes, ocn_set_haydock_conv, ocn_mult_exchange
+
+  type, bind(C), public :: ocn_haydock_conv
+    real(c_double) :: threshold
+    integer(c_int) :: spacing, ne
+    real(c_double) :: el, eh, gam0, kpref
+  end type
 
   type, bind(C) :: ocn_val_dims
     integer(c_int) :: nc, nv, kmesh(3), xmesh(3), precision, device, nspn, vspin
@@ -165,6 +171,26 @@ module ocean_gpu_mod
       type(ocn_gmres_params), intent(in) :: p
       real(c_double), intent(out) :: out_re(*), out_im(*), rel_err(*)
       integer(c_int), intent(out) :: iters(*)
+    end function
+    integer(c_int) function ocn_gmres_set_lanes(ctx, nlanes) bind(C, name="ocn_gmres_set_lanes")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nlanes
+    end function
+    ! haydockconv.ipt present (sys%earlyExit): set before OCEAN_haydock_do's run
+    integer(c_int) function ocn_set_haydock_conv(ctx, p) bind(C, name="ocn_set_haydock_conv")
+      import :: c_int, c_ptr, ocn_haydock_conv
+      type(c_ptr), value :: ctx
+      type(ocn_haydock_conv), intent(in) :: p
+    end function
+    ! nbsemhsetup2 for one lv: mhr_l / mhi_l(mham, mham) in Hartree
+    integer(c_int) function ocn_mult_exchange(lc, lv, np, kfl, kfh, fk, scfk, kgl, kgh, gk, scgk, scfac, &
+        mhr, mhi) bind(C, name="ocn_mult_exchange")
+      import :: c_int, c_double
+      integer(c_int), value :: lc, lv, np, kfl, kfh, kgl, kgh
+      real(c_double), intent(in) :: fk(*), scfk(*), gk(*), scgk(*)
+      real(c_double), value :: scfac
+      real(c_double), intent(out) :: mhr(*), mhi(*)
     end function
     integer(c_int) function ocn_redtrid(n, real_a, real_b, w) bind(C, name="ocn_redtrid")
       import :: c_int, c_double
