@@ -689,6 +689,15 @@ int ocn_val_apply_H_dev(ocn_val_ctx* ctx, const double* d_in, double* d_out, con
 /* OCEAN_haydock_Herm_do with ocean_hay_ab_twoterm over the valence action
  * (OCEAN_haydock.f90:190-320, 824-938): arrays of niter+1; OCN_ERR_NAN on a NaN
  * a_n.  psi0 is used as given (normalise it first, core_pnorm). */
+/* OCEAN_gmres_do_recycle over the valence action (OCEAN_gmres.f90:508-908 with
+ * the have_val branches :544-548, :603-606): rhs = allow o psi0, the
+ * preconditioner from H (allow o 1), outputs as ocn_gmres with kpref replaced
+ * by fact = kpref * 2 * celvol.  flags as ocn_val_apply_H (NULL: all terms).
+ * The single recycled sweep; mixed-precision contexts form the Gram dots in
+ * double-float as ocn_gmres does. */
+int ocn_val_gmres(ocn_val_ctx* ctx, const double* hay_r, const double* hay_i, double kpref, double celvol,
+                  const double* energies_ev, int nomega, const ocn_gmres_params* p, const int flags[3],
+                  double* out_re, double* out_im, double* rel_err, int* iters);
 int ocn_val_haydock(ocn_val_ctx* ctx, const double* psi0_r, const double* psi0_i, int niter, const int flags[3],
                     double* real_a, double* imag_a, double* real_b, int* niter_done);
 int ocn_val_haydock_dev(ocn_val_ctx* ctx, const double* d_psi0, int niter, const int flags[3], double* real_a,

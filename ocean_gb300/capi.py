@@ -98,7 +98,7 @@ EXPORTS = [
     "ocn_val_fxc_from_rho", "ocn_read_val_u2", "ocn_val_pair_energies", "ocn_test_starve_tc",
     "ocn_gmres_set_lanes", "ocn_set_haydock_conv", "ocn_read_haydockconv",
     "ocn_read_u2par", "ocn_read_con_u2", "ocn_read_obf_control",
-    "ocn_mult_exchange", "ocn_threey", "ocn_read_slater",
+    "ocn_mult_exchange", "ocn_threey", "ocn_read_slater", "ocn_val_gmres",
 ]
 
 TIMED_CLASSES = ["lr_band_to_x", "lr_kmesh_transform", "lr_x_to_band", "lr_prep", "multiplet",
@@ -873,6 +873,25 @@ class ValContext:
     def apply_H_dev(self, d_in: int, d_out: int, flags=(1, 1, 1), backwards=False):
         self._chk(self.lib.ocn_val_apply_H_dev(self.ptr, C.c_void_p(d_in), C.c_void_p(d_out),
                                                (C.c_int * 3)(*flags), int(bool(backwards))))
+
+    def gmres(self, energies_ev, depth=80, resolution=None, preconditioner=0.5, tol=1e-6, max_restarts=50,
+              flags=(1, 1, 1)):
+        """GMRES over the valence action (ocn_val_gmres): out_re, out_im, rel_err, iters."""
+        w = self.w
+        e = _f64(energies_ev)
+        n = len(e)
+        p = OcnGmresParams()
+        p.depth = depth
+        p.resolution = w.gam0 if resolution is None else resolution
+        p.preconditioner = preconditioner
+        p.convergence = tol
+        p.max_restarts = max_restarts
+        ore, oim, rel = np.zeros(n), np.zeros(n), np.zeros(n)
+        its = np.zeros(n, dtype=np.int32)
+        self._chk(self.lib.ocn_val_gmres(self.ptr, _dp(_f64(w.psi_r)), _dp(_f64(w.psi_i)), C.c_double(w.kpref),
+                                         C.c_double(w.celvol), _dp(e), n, C.byref(p), (C.c_int * 3)(*flags),
+                                         _dp(ore), _dp(oim), _dp(rel), its.ctypes.data_as(IP)))
+        return ore, oim, rel, its
 
     def haydock(self, niter: int, pr=None, pi=None, flags=(1, 1, 1)):
         w = self.w

@@ -389,6 +389,37 @@ __global__ void __launch_bounds__(GM_THREADS)
   block_reduce_out<false, 3>(acc, shr, red + (size_t)blockIdx.x * 3, 3);
 }
 
+// pcdiv = (E - (h_r + i(h_i + g))) / ((E - h)^2 + g^2), the Lorentzian
+// preconditioner of OCEAN_psi_min_set_prec (OCEAN_psi.f90:2961-2965), h = H*1.
+__global__ void k_gm_set_prec(double energy, double gprc, const double* __restrict__ h, double* __restrict__ out,
+                              size_t n) {
+  const double g2 = gprc * gprc;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const double hr = h[e], hi = h[n + e];
+    const double er = energy - hr, ei = -hi;
+    const double dr = er * er - ei * ei + g2, di = 2.0 * er * ei;
+    const double nr = energy - hr, ni = -(hi + gprc);
+    const double den = dr * dr + di * di;
+    out[e] = (nr * dr + ni * di) / den;
+    out[n + e] = (ni * dr - nr * di) / den;
+  }
+}
+// out = allow o in (both planes); in == NULL: out = allow o (1, 0)
+__global__ void k_gm_mask(const double* __restrict__ in, const double* __restrict__ allow, double* __restrict__ out,
+                          size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const double m = allow[e];
+    out[e] = in ? m * in[e] : m;
+    out[n + e] = in ? m * in[n + e] : 0.0;
+  }
+}
+__global__ void k_gm_ones(double* __restrict__ out, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    out[e] = 1.0;
+    out[n + e] = 0.0;
+  }
+}
+
 // out[i] = sum_b part[b*nout + i] for i < nout, one warp per output (lanes take
 // b = lane, lane+32, ... in order, then a fixed shuffle tree).
 __global__ void k_gm_reduce(const double* __restrict__ part, int nblk, int nout, double* __restrict__ out) {
@@ -463,9 +494,9 @@ Coef16 pack_coef(bool dfmt, cd c) {
   return o;
 }
 
-int grid_n(const ocn_ctx* c, size_t n) {
+int grid_n(int sm_count, size_t n) {
   const size_t b = (n + GM_THREADS - 1) / GM_THREADS;
-  return (int)std::max<size_t>(1, std::min<size_t>(b, (size_t)4 * c->sm_count));
+  return (int)std::max<size_t>(1, std::min<size_t>(b, (size_t)4 * sm_count));
 }
 
 enum LaneWait { LW_RUN, LW_H, LW_RB, LW_DONE };
@@ -512,17 +543,24 @@ struct Lane {
 
 }  // namespace
 
-// Multi-lane recycled GMRES over energies (see the file comment).
-int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* elist, int nomega,
-                const ocn_gmres_params* p, int nlanes, double* out_re, double* out_im, double* rel_err,
-                int* iters, const GmresHook* on_x, bool adjoint) {
+#define GM_CUDA(call)                                                                          \
+  do {                                                                                         \
+    cudaError_t _e = (call);                                                                   \
+    if (_e != cudaSuccess) return op.err(OCN_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+// Multi-lane recycled GMRES over energies (see the file comment) for any action.
+int gmres_solve_op(const GmresOp& op, const double* d_rhs_in, double kpref, const double* elist, int nomega,
+                   const ocn_gmres_params* p, int nlanes, double* out_re, double* out_im, double* rel_err,
+                   int* iters, const GmresHook* on_x, bool adjoint) {
   const double zs = adjoint ? -1.0 : 1.0;
   const double res = zs * p->resolution, gprc = zs * p->preconditioner;
-  const size_t n = c->npsi;
+  const size_t n = op.n;
   const int depth = p->depth;
-  const bool dfmt = c->dims.precision == OCN_PREC_MIXED;
+  const bool dfmt = op.dfmt;
   const int L = std::max(1, std::min(nlanes, nomega));
-  const int SM = c->sm_count;
+  const int SM = op.sm_count;
+  cudaStream_t stream = op.stream;
   // Gram / recycle chunking: about GM_CTAS_PER_SM CTAs per SM over all basis vectors
   const size_t nchunk_max =
       std::max<size_t>(8, std::min<size_t>((n + 255) / 256, (size_t)GM_CTAS_PER_SM * SM));
@@ -538,7 +576,7 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
   };
   auto alloc = [&](size_t bytes, void** q) -> int {
     cudaError_t e = cudaMalloc(q, bytes);
-    if (e != cudaSuccess) return set_err(c, OCN_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess) return op.err(OCN_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     owned.push_back(*q);
     return OCN_OK;
   };
@@ -582,7 +620,7 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
     cudaError_t e = cudaMallocHost((void**)&host_pool, (size_t)L * host_bytes);
     if (e != cudaSuccess) {
       host_pool = nullptr;
-      rc = set_err(c, OCN_ERR_ALLOC, "cudaMallocHost (GMRES read-back)");
+      rc = op.err(OCN_ERR_ALLOC, "cudaMallocHost (GMRES read-back)");
     }
   }
   if (rc) {
@@ -595,16 +633,16 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
   }
 
   auto launched = [&]() -> int {
-    ++c->launches;
-    OCN_CUDA(c, cudaGetLastError());
+    ++*op.launches;
+    GM_CUDA(cudaGetLastError());
     return OCN_OK;
   };
   auto reduce_to = [&](const double* part, int nblk, int nout, double* dout) -> int {
-    k_gm_reduce<<<(nout * 32 + 255) / 256, 256, 0, c->stream>>>(part, nblk, nout, dout);
+    k_gm_reduce<<<(nout * 32 + 255) / 256, 256, 0, stream>>>(part, nblk, nout, dout);
     return launched();
   };
   auto readback = [&](Lane& ln, const double* dsrc, int count) -> int {
-    OCN_CUDA(c, cudaMemcpyAsync(ln.host, dsrc, count * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    GM_CUDA(cudaMemcpyAsync(ln.host, dsrc, count * sizeof(double), cudaMemcpyDeviceToHost, stream));
     ln.wait = LW_RB;
     return OCN_OK;
   };
@@ -615,17 +653,17 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
                           bool want) -> int {
     if (nvec > 0) {
       for (int j = 0; j < nvec; ++j) ln.hcoef[j] = pack_coef(dfmt, cf[j]);
-      OCN_CUDA(c, cudaMemcpyAsync(ln.coef, ln.hcoef, nvec * sizeof(Coef16), cudaMemcpyHostToDevice, c->stream));
+      GM_CUDA(cudaMemcpyAsync(ln.coef, ln.hcoef, nvec * sizeof(Coef16), cudaMemcpyHostToDevice, stream));
     }
-    const int gb = grid_n(c, n);
+    const int gb = grid_n(SM, n);
     double* red = want ? ln.part : nullptr;
     const size_t smem = (size_t)std::max(1, nvec) * 16;
     if (dfmt)
-      k_gm_combine<true><<<gb, GM_THREADS, smem, c->stream>>>(reinterpret_cast<const float4*>(vb), nvec,
+      k_gm_combine<true><<<gb, GM_THREADS, smem, stream>>>(reinterpret_cast<const float4*>(vb), nvec,
                                                              reinterpret_cast<const float4*>(ln.coef), y, n,
                                                              rhs, red);
     else
-      k_gm_combine<false><<<gb, GM_THREADS, smem, c->stream>>>(reinterpret_cast<const double2*>(vb), nvec,
+      k_gm_combine<false><<<gb, GM_THREADS, smem, stream>>>(reinterpret_cast<const double2*>(vb), nvec,
                                                               reinterpret_cast<const double2*>(ln.coef), y, n,
                                                               rhs, red);
     int q = launched();
@@ -640,14 +678,14 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
     return q;
   };
   auto resid = [&](Lane& ln, const double* t, bool zero_x, bool want_gs) -> int {
-    const int gb = grid_n(c, n);
+    const int gb = grid_n(SM, n);
     const double* xp = zero_x ? nullptr : ln.x;
     if (dfmt)
-      k_gm_resid<true><<<gb, GM_THREADS, 0, c->stream>>>(xp, t, rhs, n, ln.ener, res, ln.g,
+      k_gm_resid<true><<<gb, GM_THREADS, 0, stream>>>(xp, t, rhs, n, ln.ener, res, ln.g,
                                                          want_gs ? reinterpret_cast<float4*>(ln.gs) : nullptr,
                                                          ln.part);
     else
-      k_gm_resid<false><<<gb, GM_THREADS, 0, c->stream>>>(xp, t, rhs, n, ln.ener, res, ln.g,
+      k_gm_resid<false><<<gb, GM_THREADS, 0, stream>>>(xp, t, rhs, n, ln.ener, res, ln.g,
                                                           want_gs ? reinterpret_cast<double2*>(ln.gs) : nullptr,
                                                           ln.part);
     int q = launched();
@@ -656,7 +694,8 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
   };
   auto set_prec = [&](Lane& ln) -> int {
     ln.prev_energy = ln.ener;
-    return vec_set_prec(c, ln.ener, gprc, hpsi1, ln.pcdiv);
+    k_gm_set_prec<<<grid_n(SM, n), GM_THREADS, 0, stream>>>(ln.ener, gprc, hpsi1, ln.pcdiv, n);
+    return launched();
   };
   int nreq = 0;
   std::vector<Lane*> hq;
@@ -665,7 +704,7 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
     ln.hin = hin + (size_t)ln.slot * 2 * n;
     ln.hout = hout + (size_t)ln.slot * 2 * n;
     if (src)
-      OCN_CUDA(c, cudaMemcpyAsync(ln.hin, src, 2 * n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+      GM_CUDA(cudaMemcpyAsync(ln.hin, src, 2 * n * sizeof(double), cudaMemcpyDeviceToDevice, stream));
     hq.push_back(&ln);
     ln.wait = LW_H;
     return OCN_OK;
@@ -697,7 +736,7 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
     if (ln.restarted) {
       ln.restarted = false;
       if (++ln.restarts > std::max(0, p->max_restarts))
-        return set_err(c, OCN_ERR_NOCONV, "GMRES restart cap reached");
+        return op.err(OCN_ERR_NOCONV, "GMRES restart cap reached");
     }
     ln.ph = LP_ITER;
     return OCN_OK;
@@ -725,7 +764,7 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
           if (ln.P == 0 && (q = set_prec(ln))) return q;
           if (ln.P == 0) {
             if (ln.s == ln.s0) {  // set_initial_vector at the lane's first energy: x = 0, g = -b
-              OCN_CUDA(c, cudaMemsetAsync(ln.x, 0, 2 * n * sizeof(double), c->stream));
+              GM_CUDA(cudaMemsetAsync(ln.x, 0, 2 * n * sizeof(double), stream));
               if ((q = resid(ln, nullptr, true, false))) return q;
               ln.xpend = false;
               ln.ph = LP_ITER;
@@ -751,11 +790,11 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
           const size_t chunk = (n + nch - 1) / nch;
           const dim3 grid((unsigned)nch, (unsigned)ng);
           if (dfmt)
-            k_gm_recycle<true><<<grid, GM_THREADS, 0, c->stream>>>(
+            k_gm_recycle<true><<<grid, GM_THREADS, 0, stream>>>(
                 reinterpret_cast<const float4*>(ln.ub), reinterpret_cast<float4*>(ln.aub), ln.P, n, chunk, dw,
                 reinterpret_cast<const float4*>(ln.gs), ln.part);
           else
-            k_gm_recycle<false><<<grid, GM_THREADS, 0, c->stream>>>(
+            k_gm_recycle<false><<<grid, GM_THREADS, 0, stream>>>(
                 reinterpret_cast<const double2*>(ln.ub), reinterpret_cast<double2*>(ln.aub), ln.P, n, chunk, dw,
                 reinterpret_cast<const double2*>(ln.gs), ln.part);
           if ((q = launched()) || (q = reduce_to(ln.part, (int)nch, 2 * ln.P, ln.out))) return q;
@@ -774,7 +813,7 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
           // the recycled solve (the P updates of :667-677 in one projection)
           for (int i = 0; i < ln.P; ++i)
             if (ln.chol.add_row(i, ln.C))
-              return set_err(c, OCN_ERR_SOLVE, "GMRES Gram matrix not positive definite");
+              return op.err(OCN_ERR_SOLVE, "GMRES Gram matrix not positive definite");
           ln.r.assign(ln.P, cd(0.0, 0.0));
           for (int j = 0; j < ln.P; ++j) ln.r[j] = -cd(ln.host[2 * j], ln.host[2 * j + 1]);
           ln.chol.solve(ln.P, ln.r);
@@ -826,13 +865,13 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
           const size_t eb = n * 16;
           // the preconditioned residual goes straight into this lane's H slot
           double* pg = hin + (size_t)nreq * 2 * n;
-          const int gb = grid_n(c, n);
+          const int gb = grid_n(SM, n);
           if (dfmt)
-            k_gm_prec<true><<<gb, GM_THREADS, 0, c->stream>>>(ln.g, ln.pcdiv, n, pg,
+            k_gm_prec<true><<<gb, GM_THREADS, 0, stream>>>(ln.g, ln.pcdiv, n, pg,
                                                               reinterpret_cast<float4*>(ln.ub + (size_t)m * eb),
                                                               reinterpret_cast<float4*>(ln.gs));
           else
-            k_gm_prec<false><<<gb, GM_THREADS, 0, c->stream>>>(ln.g, ln.pcdiv, n, pg,
+            k_gm_prec<false><<<gb, GM_THREADS, 0, stream>>>(ln.g, ln.pcdiv, n, pg,
                                                                reinterpret_cast<double2*>(ln.ub + (size_t)m * eb),
                                                                reinterpret_cast<double2*>(ln.gs));
           if ((q = launched())) return q;
@@ -842,12 +881,12 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
         case LP_ITER_H: {
           const int m = ln.it - 1;
           const size_t eb = n * 16;
-          const int gb = grid_n(c, n);
+          const int gb = grid_n(SM, n);
           if (dfmt)
-            k_gm_form<true><<<gb, GM_THREADS, 0, c->stream>>>(ln.hin, ln.hout, n, ln.ener, res,
+            k_gm_form<true><<<gb, GM_THREADS, 0, stream>>>(ln.hin, ln.hout, n, ln.ener, res,
                                                               reinterpret_cast<float4*>(ln.aub + (size_t)m * eb));
           else
-            k_gm_form<false><<<gb, GM_THREADS, 0, c->stream>>>(ln.hin, ln.hout, n, ln.ener, res,
+            k_gm_form<false><<<gb, GM_THREADS, 0, stream>>>(ln.hin, ln.hout, n, ln.ener, res,
                                                                reinterpret_cast<double2*>(ln.aub + (size_t)m * eb));
           if ((q = launched())) return q;
           const int ng = m + 1;
@@ -856,11 +895,11 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
           const size_t chunk = (n + nch - 1) / nch;
           const dim3 grid((unsigned)nch, (unsigned)ng);
           if (dfmt)
-            k_gm_gram<true><<<grid, GM_THREADS, 0, c->stream>>>(
+            k_gm_gram<true><<<grid, GM_THREADS, 0, stream>>>(
                 reinterpret_cast<const float4*>(ln.ub), reinterpret_cast<const float4*>(ln.aub), m, n, chunk,
                 reinterpret_cast<const float4*>(ln.gs), ln.part);
           else
-            k_gm_gram<false><<<grid, GM_THREADS, 0, c->stream>>>(
+            k_gm_gram<false><<<grid, GM_THREADS, 0, stream>>>(
                 reinterpret_cast<const double2*>(ln.ub), reinterpret_cast<const double2*>(ln.aub), m, n, chunk,
                 reinterpret_cast<const double2*>(ln.gs), ln.part);
           if ((q = launched()) || (q = reduce_to(ln.part, (int)nch, (m + 1) * GM_NQ, ln.out))) return q;
@@ -882,7 +921,7 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
           }
           ln.C[(size_t)m * depth + m] = cd(ln.C[(size_t)m * depth + m].real(), 0.0);
           ln.S[(size_t)m * depth + m] = cd(ln.S[(size_t)m * depth + m].real(), 0.0);
-          if (ln.chol.add_row(m, ln.C)) return set_err(c, OCN_ERR_SOLVE, "GMRES Gram matrix not positive definite");
+          if (ln.chol.add_row(m, ln.C)) return op.err(OCN_ERR_SOLVE, "GMRES Gram matrix not positive definite");
           ln.r.assign(m + 1, cd(0.0, 0.0));
           for (int j = 0; j <= m; ++j) ln.r[j] = -cd(h[(size_t)j * GM_NQ + 8], h[(size_t)j * GM_NQ + 9]);
           ln.chol.solve(m + 1, ln.r);
@@ -917,10 +956,16 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
   // ---- the sweep
   auto run = [&]() -> int {
     int q;
-    // rhs = allow o hay (OCEAN_gmres.f90:586); hpsi1 = H (1, 0) (:600-608)
-    if ((q = vec_mask_copy(c, d_rhs_in, rhs))) return q;
-    if ((q = vec_fill(c, ones, 1.0, 0.0))) return q;
-    if ((q = apply_H_impl(c, ones, ones + n, hpsi1, hpsi1 + n, nullptr, 0))) return q;
+    // rhs = allow o hay (OCEAN_gmres.f90:586); hpsi1 = H (1, 0) (:600-608), with
+    // the valence run's allow on the ones first (:603-606)
+    k_gm_mask<<<grid_n(SM, n), GM_THREADS, 0, stream>>>(d_rhs_in, op.allow, rhs, n);
+    if ((q = launched())) return q;
+    if (op.mask_ones)
+      k_gm_mask<<<grid_n(SM, n), GM_THREADS, 0, stream>>>(nullptr, op.allow, ones, n);
+    else
+      k_gm_ones<<<grid_n(SM, n), GM_THREADS, 0, stream>>>(ones, n);
+    if ((q = launched())) return q;
+    if ((q = op.H(ones, hpsi1))) return q;
     for (;;) {
       bool any_rb = false, all_done = true;
       for (Lane& ln : lanes) {
@@ -932,21 +977,21 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
       }
       if (all_done) break;
       if (any_rb) {
-        OCN_CUDA(c, cudaStreamSynchronize(c->stream));
+        GM_CUDA(cudaStreamSynchronize(stream));
         for (Lane& ln : lanes)
           if (ln.wait == LW_RB) ln.wait = LW_RUN;
         continue;
       }
       // every lane waits for H (or is done): one block action over the slots
-      if (hq.empty()) return set_err(c, OCN_ERR_STATE, "GMRES scheduler stalled");
+      if (hq.empty()) return op.err(OCN_ERR_STATE, "GMRES scheduler stalled");
       const int nv = (int)hq.size();
-      if (nv == 1) {
-        if ((q = apply_H_impl(c, hin, hin + n, hout, hout + n, nullptr, 0))) return q;
+      if (nv == 1 || !op.Hblock) {
+        for (int v = 0; v < nv; ++v)
+          if ((q = op.H(hin + (size_t)v * 2 * n, hout + (size_t)v * 2 * n))) return q;
       } else {
-        for (int v0 = 0; v0 < nv; v0 += c->nvec) {
-          const int nb = std::min(c->nvec, nv - v0);
-          if ((q = apply_H_block_impl(c, nb, hin + (size_t)v0 * 2 * n, hout + (size_t)v0 * 2 * n, nullptr, 0)))
-            return q;
+        for (int v0 = 0; v0 < nv; v0 += op.nvec) {
+          const int nb = std::min(op.nvec, nv - v0);
+          if ((q = op.Hblock(nb, hin + (size_t)v0 * 2 * n, hout + (size_t)v0 * 2 * n))) return q;
         }
       }
       for (Lane* lp : hq) lp->wait = LW_RUN;
@@ -956,12 +1001,32 @@ int gmres_solve(ocn_ctx* c, const double* d_rhs_in, double kpref, const double* 
     return OCN_OK;
   };
   rc = run();
-  cudaError_t e = cudaStreamSynchronize(c->stream);
+  cudaError_t e = cudaStreamSynchronize(stream);
   cleanup();
   if (rc) return rc;
-  if (e != cudaSuccess) return cuda_fail(c, e, "ocn_gmres");
-  if (c->mixed) rc = mixed_check(c);
+  if (e != cudaSuccess) return op.err(OCN_ERR_CUDA, std::string("ocn_gmres: ") + cudaGetErrorString(e));
+  if (op.finish) rc = op.finish();
   return rc;
+}
+
+int gmres_solve(ocn_ctx* c, const double* d_rhs, double kpref, const double* elist, int nomega,
+                const ocn_gmres_params* p, int nlanes, double* out_re, double* out_im, double* rel_err,
+                int* iters, const GmresHook* on_x, bool adjoint) {
+  GmresOp op;
+  op.n = c->npsi;
+  op.dfmt = c->dims.precision == OCN_PREC_MIXED;
+  op.sm_count = c->sm_count;
+  op.stream = c->stream;
+  op.launches = &c->launches;
+  op.nvec = c->nvec;
+  op.allow = c->d_allow;
+  op.mask_ones = false;
+  const size_t n = c->npsi;
+  op.H = [c, n](const double* in, double* out) { return apply_H_impl(c, in, in + n, out, out + n, nullptr, 0); };
+  op.Hblock = [c](int nv, const double* in, double* out) { return apply_H_block_impl(c, nv, in, out, nullptr, 0); };
+  op.err = [c](int code, const std::string& msg) { return set_err(c, code, msg); };
+  if (c->mixed) op.finish = [c]() { return mixed_check(c); };
+  return gmres_solve_op(op, d_rhs, kpref, elist, nomega, p, nlanes, out_re, out_im, rel_err, iters, on_x, adjoint);
 }
 
 }  // namespace ocn

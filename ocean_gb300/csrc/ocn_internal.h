@@ -304,6 +304,24 @@ int apply_H_impl(ocn_ctx* c, const double* ir, const double* ii, double* orr, do
 int apply_H_block_impl(ocn_ctx* c, int nv, const double* in, double* out, const int* hflag_in, int backwards,
                        const int* back_each = nullptr);
 typedef std::function<int(int step, const double* x)> GmresHook;
+// The action and context a GMRES sweep runs on (core or valence).
+struct GmresOp {
+  size_t n = 0;                  // complex values per vector (planes of n doubles)
+  bool dfmt = false;             // double-float basis (mixed-precision contexts)
+  int sm_count = 1;
+  cudaStream_t stream = nullptr;
+  long long* launches = nullptr;
+  int nvec = 1;                  // vectors per block action
+  const double* allow = nullptr; // device allow mask (n)
+  bool mask_ones = false;        // preconditioner from H (allow o 1) (valence runs)
+  std::function<int(const double*, double*)> H;             // device planes in, out
+  std::function<int(int, const double*, double*)> Hblock;   // nv vectors at stride 2n (may be empty)
+  std::function<int(int, const std::string&)> err;          // records an error, returns the code
+  std::function<int()> finish;                              // after the sweep (may be empty)
+};
+int gmres_solve_op(const GmresOp& op, const double* d_rhs, double kpref, const double* elist, int nomega,
+                   const ocn_gmres_params* p, int nlanes, double* out_re, double* out_im, double* rel_err,
+                   int* iters, const GmresHook* on_x, bool adjoint);
 // OCEAN_gmres_do_recycle over the energy list in nlanes lanes; d_rhs: device
 // planes of the right-hand side before the allow mask.  on_x: called with each
 // energy's solution (device planes) once it has converged.  adjoint: solve

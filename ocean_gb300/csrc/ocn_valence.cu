@@ -1417,6 +1417,42 @@ int ocn_val_haydock_dev(ocn_val_ctx* c, const double* d_psi0, int niter, const i
   return done < niter || std::isnan(real_a[niter - 1]) ? OCN_ERR_NAN : OCN_OK;
 }
 
+int ocn_val_gmres(ocn_val_ctx* c, const double* hay_r, const double* hay_i, double kpref, double celvol,
+                  const double* energies_ev, int nomega, const ocn_gmres_params* p, const int flags[3],
+                  double* out_re, double* out_im, double* rel_err, int* iters) {
+  if (!c || !hay_r || !hay_i || !energies_ev || nomega < 1 || !p || p->depth < 1 || p->depth > 1024)
+    return vset_err(c, OCN_ERR_ARG, "ocn_val_gmres: bad argument");
+  cudaSetDevice(c->device);
+  int fl[3] = {1, 1, 1};
+  if (flags)
+    for (int i = 0; i < 3; ++i) fl[i] = flags[i];
+  if (int rc = check_ready(c, fl)) return rc;
+  const size_t n = c->npsi;
+  double* d_hay = nullptr;
+  if (int rc = valloc(c, &d_hay, 2 * n)) return rc;
+  int rc = upload(c, d_hay, hay_r, sizeof(double) * n);
+  if (rc == OCN_OK) rc = upload(c, d_hay + n, hay_i, sizeof(double) * n);
+  if (rc == OCN_OK) {
+    ocn::GmresOp op;
+    op.n = n;
+    op.dfmt = c->mixed != 0;
+    op.sm_count = c->sm_count;
+    op.stream = c->stream;
+    op.launches = &c->launches;
+    op.nvec = 1;
+    op.allow = c->d_allow;
+    op.mask_ones = true;  // OCEAN_energies_allow_full on the ones (OCEAN_gmres.f90:603-606)
+    op.H = [c, &fl](const double* in, double* out) { return apply_dev(c, in, out, fl, 0); };
+    op.err = [c](int code, const std::string& msg) { return vset_err(c, code, msg); };
+    // fact = kpref 2 celvol for a valence run (OCEAN_gmres.f90:544-548)
+    rc = ocn::gmres_solve_op(op, d_hay, kpref * 2.0 * celvol, energies_ev, nomega, p, 1, out_re, out_im, rel_err,
+                             iters, nullptr, false);
+  }
+  cudaStreamSynchronize(c->stream);
+  cudaFree(d_hay);
+  return rc;
+}
+
 int ocn_val_haydock(ocn_val_ctx* c, const double* psi0_r, const double* psi0_i, int niter, const int flags[3],
                     double* real_a, double* imag_a, double* real_b, int* niter_done) {
   if (!c || !psi0_r || !psi0_i) return vset_err(c, OCN_ERR_ARG, "null argument");

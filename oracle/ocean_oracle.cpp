@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <functional>
 #include <cstring>
 #include <vector>
 #ifdef _OPENMP
@@ -1528,14 +1529,13 @@ void set_prec(double energy, double gprc, const Vec& h, Vec& out) {
 }
 
 struct GmresState {
-  const or_dims* d;
-  const or_ops* o;
+  std::function<void(const double*, const double*, double*, double*)> act;  // OCEAN_xact
   int depth;
   std::vector<Vec> u, au;
   std::vector<cd> cmat;  // packed upper, module-global c_matrix
   long long hpsi = 0;
   void H(const Vec& in, Vec& out) {
-    or_xact(d, o, in.r.data(), in.i.data(), out.r.data(), out.i.data(), nullptr, 0);
+    act(in.r.data(), in.i.data(), out.r.data(), out.i.data());
     ++hpsi;
   }
   // update_gmres, OCEAN_gmres.f90:241-344
@@ -1571,26 +1571,36 @@ struct GmresState {
 
 // OCEAN_gmres_do_recycle, OCEAN_gmres.f90:508-908 (core, bwflg = F, loud = T,
 // do_precondition = allow_reuse_x = force_reuse_x = allow_recycle = T per :24-27).
-int or_gmres(const or_dims* d, const or_ops* o, const double* hay_r, const double* hay_i,
-             double kpref, const double* elist, int nomega, int depth, double gres, double gprc,
-             double ffff, int max_restarts, double* out_re, double* out_im, double* rel_err,
-             int* iters, int* total_hpsi) {
-  const size_t n = (size_t)d->nb * nk_of(d) * d->na;
+}  // extern "C"
+
+namespace {
+
+// OCEAN_gmres_do_recycle (OCEAN_gmres.f90:508-908) over an action on vectors of
+// n complex values; allow: the sfact / allow mask (rhs = allow o hay, :586; with
+// mask_ones the H*1 of the preconditioner is H(allow o 1), the valence branch
+// :603-606); fact scales the output columns (kpref, or kpref 2 celvol for a
+// valence run, :544-548).
+int gmres_generic(size_t n, const double* allow, bool mask_ones,
+                  const std::function<void(const double*, const double*, double*, double*)>& act,
+                  const double* hay_r, const double* hay_i, double fact, const double* elist, int nomega, int depth,
+                  double gres, double gprc, double ffff, int max_restarts, double* out_re, double* out_im,
+                  double* rel_err, int* iters, int* total_hpsi) {
   GmresState st;
-  st.d = d;
-  st.o = o;
+  st.act = act;
   st.depth = depth;
   st.u.assign(depth, Vec(n));
   st.au.assign(depth, Vec(n));
   st.cmat.assign((size_t)depth * (depth + 1) / 2, cd(0.0, 0.0));
   Vec x(n), ax(n), hpsi1(n), g(n), pcdiv(n), rhs(n);
   for (size_t j = 0; j < n; ++j) {  // sfact_copy: allow%i (= allow for core) o hay_vec
-    rhs.r[j] = o->allow[j] * hay_r[j];
-    rhs.i[j] = o->allow[j] * hay_i[j];
+    rhs.r[j] = allow[j] * hay_r[j];
+    rhs.i[j] = allow[j] * hay_i[j];
   }
-  for (size_t j = 0; j < n; ++j) { x.r[j] = 1.0; x.i[j] = 0.0; }  // psi_one_full
+  for (size_t j = 0; j < n; ++j) {  // psi_one_full (then allow_full for valence)
+    x.r[j] = mask_ones ? allow[j] : 1.0;
+    x.i[j] = 0.0;
+  }
   st.H(x, hpsi1);
-  const double fact = kpref;
   int global_iter = 0, prev_iter = 0;
   double prev_energy = -1.0e308;
   double rval = 0, ival = 0, gval = 0;
@@ -1689,6 +1699,33 @@ int or_gmres(const or_dims* d, const or_ops* o, const double* hay_r, const doubl
   }
   if (total_hpsi) *total_hpsi = (int)st.hpsi;
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int or_gmres(const or_dims* d, const or_ops* o, const double* hay_r, const double* hay_i,
+             double kpref, const double* elist, int nomega, int depth, double gres, double gprc,
+             double ffff, int max_restarts, double* out_re, double* out_im, double* rel_err,
+             int* iters, int* total_hpsi) {
+  const size_t n = (size_t)d->nb * nk_of(d) * d->na;
+  auto act = [&](const double* pr, const double* pi, double* hr, double* hi) {
+    or_xact(d, o, pr, pi, hr, hi, nullptr, 0);
+  };
+  return gmres_generic(n, o->allow, false, act, hay_r, hay_i, kpref, elist, nomega, depth, gres, gprc, ffff,
+                       max_restarts, out_re, out_im, rel_err, iters, total_hpsi);
+}
+
+// GMRES over a caller-supplied action (the valence action of ocean_oracle_val.cpp).
+int or_gmres_with(size_t n, const double* allow, int mask_ones,
+                  void (*act)(void* user, const double* pr, const double* pi, double* hr, double* hi), void* user,
+                  const double* hay_r, const double* hay_i, double fact, const double* elist, int nomega, int depth,
+                  double gres, double gprc, double ffff, int max_restarts, double* out_re, double* out_im,
+                  double* rel_err, int* iters, int* total_hpsi) {
+  auto f = [&](const double* pr, const double* pi, double* hr, double* hi) { act(user, pr, pi, hr, hi); };
+  return gmres_generic(n, allow, mask_ones != 0, f, hay_r, hay_i, fact, elist, nomega, depth, gres, gprc, ffff,
+                       max_restarts, out_re, out_im, rel_err, iters, total_hpsi);
 }
 
 // OCEAN_soprep without core_broaden.ipt (OCEAN_multiplet.f90:572-690), jimel

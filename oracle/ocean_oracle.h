@@ -19,6 +19,8 @@
 #ifndef OCEAN_ORACLE_H
 #define OCEAN_ORACLE_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -187,6 +189,16 @@ void or_val_ladder_slab(const or_val_dims* d, const or_val_ops* o, const double*
 /* OCEAN_xact valence branch + energies (OCEAN_action.f90:521-600). */
 int or_val_act(const or_val_dims* d, const or_val_ops* o, const double* pr, const double* pi, double* hr,
                double* hi, int backwards);
+/* GMRES (OCEAN_gmres_do_recycle) over a caller-supplied action on n complex values. */
+int or_gmres_with(size_t n, const double* allow, int mask_ones,
+                  void (*act)(void* user, const double* pr, const double* pi, double* hr, double* hi), void* user,
+                  const double* hay_r, const double* hay_i, double fact, const double* elist, int nomega, int depth,
+                  double gres, double gprc, double ffff, int max_restarts, double* out_re, double* out_im,
+                  double* rel_err, int* iters, int* total_hpsi);
+/* GMRES over the valence action (OCEAN_gmres.f90:508-908, have_val branches). */
+int or_val_gmres(const or_val_dims* d, const or_val_ops* o, const double* hay_r, const double* hay_i, double kpref,
+                 double celvol, const double* elist, int nomega, int depth, double gres, double gprc, double ffff,
+                 int max_restarts, double* out_re, double* out_im, double* rel_err, int* iters, int* total_hpsi);
 /* Hermitian Haydock over the valence action (OCEAN_haydock.f90:190-320, 824-938). */
 int or_val_haydock(const or_val_dims* d, const or_val_ops* o, const double* p0r, const double* p0i, int niter,
                    double* real_a, double* imag_a, double* real_b, int* niter_done);

@@ -409,6 +409,25 @@ int or_val_act(const or_val_dims* d, const or_val_ops* o, const double* pr, cons
   return 0;
 }
 
+// OCEAN_gmres_do_recycle over the valence action (the have_val branches of
+// OCEAN_gmres.f90:544-548, 603-606): rhs = allow o hay, the preconditioner from
+// H (allow o 1), and the output scaled by fact = kpref 2 celvol.
+int or_val_gmres(const or_val_dims* d, const or_val_ops* o, const double* hay_r, const double* hay_i, double kpref,
+                 double celvol, const double* elist, int nomega, int depth, double gres, double gprc, double ffff,
+                 int max_restarts, double* out_re, double* out_im, double* rel_err, int* iters, int* total_hpsi) {
+  const size_t n = (size_t)d->nc * d->nv * nk_of(d) * vspin_of(d) * vspin_of(d);
+  struct U {
+    const or_val_dims* d;
+    const or_val_ops* o;
+  } u{d, o};
+  auto act = [](void* user, const double* pr, const double* pi, double* hr, double* hi) {
+    const U* q = static_cast<const U*>(user);
+    or_val_act(q->d, q->o, pr, pi, hr, hi, 0);
+  };
+  return or_gmres_with(n, o->allow, 1, act, &u, hay_r, hay_i, kpref * 2.0 * celvol, elist, nomega, depth, gres,
+                       gprc, ffff, max_restarts, out_re, out_im, rel_err, iters, total_hpsi);
+}
+
 // The Hermitian Haydock recursion of OCEAN_haydock_Herm_do with
 // ocean_hay_ab_twoterm (OCEAN_haydock.f90:190-320, 824-938) over the valence
 // action, in the same arithmetic order as or_haydock.

@@ -423,6 +423,21 @@ class OracleVal:
                                   dptr(rb), C.byref(done))
         return rc, ra, ia, rb, done.value
 
+    def gmres(self, energies_ev, depth=80, gres=None, gprc=0.5, ffff=1e-6, max_restarts=50):
+        """GMRES over the valence action (OCEAN_gmres.f90:508-908, have_val)."""
+        w = self.w
+        e = np.ascontiguousarray(energies_ev, dtype=np.float64)
+        n = len(e)
+        gres = w.gam0 if gres is None else gres
+        ore, oim, rel = np.zeros(n), np.zeros(n), np.zeros(n)
+        its = np.zeros(n, dtype=np.int32)
+        tot = C.c_int(0)
+        rc = lib().or_val_gmres(C.byref(self.d), C.byref(self.o), dptr(np.ascontiguousarray(w.psi_r)),
+                                dptr(np.ascontiguousarray(w.psi_i)), C.c_double(w.kpref), C.c_double(w.celvol),
+                                dptr(e), n, depth, C.c_double(gres), C.c_double(gprc), C.c_double(ffff),
+                                max_restarts, dptr(ore), dptr(oim), dptr(rel), iptr(its), C.byref(tot))
+        return rc, ore, oim, rel, its, tot.value
+
     def ladder_slab(self, pr, pi, y0, y1, lad_slab):
         """Direct-term contribution of y in [y0, y1) (lad_slab: ladder rows of those y)."""
         hr, hi = np.zeros(self.w.npsi), np.zeros(self.w.npsi)

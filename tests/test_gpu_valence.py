@@ -310,3 +310,28 @@ def test_smaller_context_keeps_larger_one_working(built, prec):
         assert _rel(r2[0] + 1j * r2[1], orr + 1j * oi) < (1e-12 if prec == capi.OCN_PREC_FP64 else 1e-6)
     finally:
         cb.close()
+
+
+@pytest.mark.parametrize("prec", [capi.OCN_PREC_FP64, capi.OCN_PREC_MIXED])
+def test_valence_gmres_matches_oracle(built, prec):
+    """GMRES over the valence action (ocn_val_gmres; OCEAN_gmres.f90:508-908 with
+    the have_val branches) against the oracle's sweep: FP64 within 1e-8 at a
+    tight tolerance (the same iteration counts within one), mixed within 1e-4
+    at a tolerance above its precision floor."""
+    _, O = built
+    w = WL.make_val("vsmall", seed=32)
+    P = O.OracleVal(w)
+    E = np.array([6.0, 6.2, 6.4, 11.0])
+    tol = 1e-20 if prec == capi.OCN_PREC_FP64 else 1e-10
+    ctx = capi.ValContext(w, precision=prec)
+    try:
+        ore, oim, rel, its = ctx.gmres(E, depth=16, tol=tol, max_restarts=500)
+    finally:
+        ctx.close()
+    rc, ore2, oim2, rel2, its2, tot = P.gmres(E, depth=16, ffff=1e-20, max_restarts=500)
+    assert rc == 0
+    bar = 1e-8 if prec == capi.OCN_PREC_FP64 else 1e-4
+    assert np.max(np.abs(oim - oim2) / np.abs(oim2)) < bar
+    assert np.max(np.abs(ore - ore2) / np.abs(ore2)) < bar
+    if prec == capi.OCN_PREC_FP64:
+        assert np.max(np.abs(its - its2)) <= 1

@@ -265,3 +265,30 @@ def test_valence_host_entry_points_reject_bad_arguments(lib_built, tmp_path):
         capi.read_val_u2(str(tmp_path / "missing"), (2, 2, 2), 1, 1, 1, 2, 1, 2)
     assert lib.ocn_val_optical_constants(-1, None, None, None, None) == capi.OCN_ERR_ARG
     assert lib.ocn_write_opcons(str(tmp_path / "x").encode(), 1, None) == capi.OCN_ERR_ARG
+
+
+def test_valence_gmres_matches_dense_solve(oracle_lib):
+    """GMRES over the valence action (OCEAN_gmres.f90:508-908, have_val) solves
+    ((w + i G) - H) x = allow o psi0 at tight tolerance: <b|x> against a dense
+    solve of the same action, and the outputs scaled by fact = kpref 2 celvol."""
+    O = oracle_lib
+    w = WL.make_val("vtiny", seed=31)
+    P = O.OracleVal(w)
+    n = w.npsi
+    H = np.zeros((n, n), complex)
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = 1.0
+        hr, hi = P.act(e, np.zeros(n))
+        H[:, j] = hr + 1j * hi
+    E = np.array([5.0, 5.2, 9.0])
+    rc, ore, oim, rel, its, tot = P.gmres(E, depth=12, ffff=1e-22, max_restarts=400)
+    assert rc == 0
+    b = w.allow * (w.psi_r + 1j * w.psi_i)
+    fact = w.kpref * 2.0 * w.celvol
+    for i, ev in enumerate(E):
+        z = ev * WL.EV2HARTREE + 1j * w.gam0
+        x = np.linalg.solve(z * np.eye(n) - H, b)
+        f = np.vdot(b, x)
+        assert abs((1.0 - f.real * fact) - ore[i]) < 1e-9 * abs(ore[i])
+        assert abs(-f.imag * fact - oim[i]) < 1e-9 * abs(oim[i])
