@@ -882,7 +882,7 @@ def run_ours(args, ws, rank, local, pg):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "bf16x2-split+f32 (contractions), f64 (vectors)",
+            "dtype": "f64" if args.precision == "fp64" else "bf16x2-split+f32 (contractions), f32x2 double-float (Lanczos vectors), f64 (coefficients)",
             "data": "synthetic (seeded; u2 QR-orthonormal complex Gaussian, U(0,30) eV bands, "
                     "erf(r/0.5A)/(4r) W table)",
             "config": {"workload": f"{args.workload}: {describe(w)}, "

@@ -315,7 +315,8 @@ int ocn_ctx_destroy(ocn_ctx* c) {
   void* bufs[] = {c->d_er, c->d_ei, c->d_allow, c->d_u, c->d_W, c->d_tw, c->d_so, c->d_phi, c->d_acc,
                   c->d_accpart, c->d_vec, c->d_red, c->d_scal, c->mult.mpc, c->mult.mpm, c->mult.mh,
                   c->mult.p_l, c->mult.p_m, c->mult.p_nu, c->mult.d_pfirst, c->mult.d_nproj,
-                  c->mult.d_jbeg, c->mult.amp, c->mult.amp_part, c->mult.hamp};
+                  c->mult.d_jbeg, c->mult.amp, c->mult.amp_part, c->mult.hamp, c->d_er_df, c->d_ei_df,
+                  c->d_allow_f, c->d_so_f};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->hay_exec) cudaGraphExecDestroy(c->hay_exec);
@@ -657,6 +658,8 @@ int haydock_iteration(ocn_ctx* c, int nv, double* old, double* psi, double* h, d
     if (c->mult_parts > 0) {  // tensor cores; the psi operand was built with the last normalisation
       if ((rc = mult_apply_mixed(c, psi, psi + n, 2 * n, nv, true))) return rc;
     } else {
+      if (mixed_parts(c))  // the FP64 multiplet kernels cannot read the double-float vectors
+        return set_err(c, OCN_ERR_STATE, "mixed-precision multiplet operands not built");
       if ((rc = zero_acc(c, nv))) return rc;
       for (int v = 0; v < nv; ++v)
         if ((rc = mult_apply(c, psi + 2 * v * n, psi + 2 * v * n + n, c->d_acc + 2 * v * n))) return rc;
@@ -777,8 +780,15 @@ int haydock_prepare(ocn_ctx* c, int nv, const double* p0r, const double* p0i, si
     }
     OCN_CUDA(c, cudaMemsetAsync(c->d_conv_rel, 0, ((size_t)c->hay_cap + 1) * sizeof(double), c->stream));
   }
-  if (c->dims.precision == OCN_PREC_MIXED && (rc = mixed_prep_b1(c, R->buf[1], R->buf[1] + n, 2 * n, nv)))
-    return rc;
+  if (mixed_parts(c)) {
+    // first psi operand from the FP64 start vectors, then the loop's double-float form
+    if ((rc = mixed_prep_b1(c, R->buf[1], R->buf[1] + n, 2 * n, nv))) return rc;
+    if (!c->d_er_df && ((rc = dev_alloc(c, &c->d_er_df, n)) || (rc = dev_alloc(c, &c->d_ei_df, n)) ||
+                        (rc = dev_alloc(c, &c->d_allow_f, n)) ||
+                        (rc = dev_alloc(c, &c->d_so_f, (size_t)c->na * c->na))))
+      return rc;
+    if ((rc = haydock_to_df(c, R->buf[1], nv))) return rc;
+  }
   return OCN_OK;
 }
 

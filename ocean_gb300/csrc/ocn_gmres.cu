@@ -46,6 +46,7 @@
 #include <functional>
 #include <vector>
 
+#include "ocn_df.cuh"
 #include "ocn_internal.h"
 
 namespace ocn {
@@ -58,42 +59,7 @@ constexpr int GM_THREADS = 256;
 constexpr int GM_CTAS_PER_SM = 4;  // target CTAs per SM of the Gram and recycle passes
 constexpr int GM_NQ = 10;          // real sums per basis vector in the Gram pass
 
-// ------------------------------------------------------------ double-float
-
-struct df {
-  float h, l;
-};
-
-__device__ __forceinline__ df df_split(double v) {
-  const float h = __double2float_rn(v);
-  const float l = __double2float_rn(v - (double)h);
-  return {h, l};
-}
-
-// (sh, sl) += a * b with the product's rounding error and the sum's rounding
-// error carried in sl (TwoProduct by FMA, TwoSum); no operation is contracted.
-__device__ __forceinline__ void df_fma(float& sh, float& sl, df a, df b) {
-  const float p = __fmul_rn(a.h, b.h);
-  float e = __fmaf_rn(a.h, b.h, -p);
-  e = __fmaf_rn(a.h, b.l, e);
-  e = __fmaf_rn(a.l, b.h, e);
-  const float s = __fadd_rn(sh, p);
-  const float bb = __fsub_rn(s, sh);
-  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-  sh = s;
-  sl = __fadd_rn(sl, __fadd_rn(err, e));
-}
-
-// (ah, al) += (bh, bl), renormalised
-__device__ __forceinline__ void df_add(float& ah, float& al, float bh, float bl) {
-  const float s = __fadd_rn(ah, bh);
-  const float bb = __fsub_rn(s, ah);
-  const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
-  const float lo = __fadd_rn(__fadd_rn(al, bl), err);
-  const float h = __fadd_rn(s, lo);
-  al = __fsub_rn(lo, __fsub_rn(h, s));
-  ah = h;
-}
+// double-float helpers: ocn_df.cuh
 
 // Element and accumulator policies of the two basis formats.
 template <bool DF>

@@ -41,6 +41,9 @@ struct CombineArgs {
   const int* itp;
   double* red;
   BlockStrides bs;
+  const float2 *er_df, *ei_df;  // double-float loop (mixed precision): operator copies
+  const float* allow_f;
+  const float2* so_f;
   int nv;    // vectors of this context; blocks beyond it return at once
   int nblk;  // blocks per vector of this context (its own launches' grid); blocks beyond return
 };
@@ -110,6 +113,11 @@ struct ocn_ctx {
   double* d_er = nullptr;    // energies (npsi)
   double* d_ei = nullptr;
   double* d_allow = nullptr;
+  // operator copies of the mixed-precision (double-float) Haydock loop, rebuilt per run
+  float2* d_er_df = nullptr;
+  float2* d_ei_df = nullptr;
+  float* d_allow_f = nullptr;
+  float2* d_so_f = nullptr;
   double2* d_u = nullptr;    // phased Bloch functions, [s][x][k][n] complex (reference order)
   double* d_W = nullptr;     // (Nk, Nx): W[x*Nk + k]
   double2* d_tw = nullptr;   // k-mesh twiddles exp(+2 pi i t / n_axis), [axis][t] (3 x OCN_MAX_KDIM)
@@ -251,7 +259,8 @@ int upload_twiddles(ocn_ctx* c);
 int lr_apply_fp64(ocn_ctx* c, const double* d_pr, const double* d_pi);  // adds into d_acc
 int mult_apply(ocn_ctx* c, const double* d_pr, const double* d_pi, double* acc);  // adds into acc
 int mult_hamp(ocn_ctx* c, const double2* amp, double2* hamp);  // one vector, [p][a]
-void active_parts(const ocn_ctx* c, const int* hflag, const double** base, int* count);
+// base: binary32 partials on the mixed path, FP64 otherwise
+void active_parts(const ocn_ctx* c, const int* hflag, const void** base, int* count);
 int phase_bloch(ocn_ctx* c, const double* d_ur, const double* d_ui, const double* d_cos,
                 const double* d_sin);
 // out = E o in + A o acc + SO in   (acc already holds H_fg + H_lr of A o in), for nv
@@ -364,6 +373,9 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
                    bool b1_ready = false);
 int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vstride, int nv);
 // b_i = sqrt(partials), psi = h / b_i, and the psi operand of the next action (nv chains)
+// Tensor-core partials (binary32) and the double-float Haydock vectors: mixed precision.
+inline bool mixed_parts(const ocn_ctx* c) { return c->dims.precision == OCN_PREC_MIXED && c->mixed != nullptr; }
+int haydock_to_df(ocn_ctx* c, double* buf, int nv);
 int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rstride, double* h,
                     double* rb, size_t cstride, const int* itp);
 int mixed_check(ocn_ctx* c);       // reads and clears the device timeout flag

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <new>
 
+#include "ocn_df.cuh"
 #include "ocn_internal.h"
 #include "ocn_kmesh_dft.cuh"
 
@@ -216,11 +217,13 @@ __global__ void k_lr_gemm2_fp64(const double2* __restrict__ u, const double2* __
 //             + sum_jc S(ic,jc) psi(n,k,jc)        (OCEAN_action.f90:337-372,596-608)
 // Optionally fused with the first Lanczos stage (ocean_hay_ab_twoterm,
 // OCEAN_haydock.f90:848-860): out -= b_{i-1} old, partial <out|psi>.
-template <int NA, bool SO>
+// PT: element type of the long-range / multiplet partials (double on the FP64
+// path, float from the tensor-core contractions).
+template <int NA, bool SO, typename PT>
 __device__ __forceinline__ void combine_body(const double* __restrict__ pr, const double* __restrict__ pi,
                           const double* __restrict__ er, const double* __restrict__ ei,
                           const double* __restrict__ allow, const double* __restrict__ acc,
-                          const double* __restrict__ part, int nparts, const double2* __restrict__ so,
+                          const PT* __restrict__ part, int nparts, const double2* __restrict__ so,
                           double* __restrict__ outr, double* __restrict__ outi, int nbk, int na,
                           size_t npsi, int use_e0, int use_so, int backwards,
                           const double* __restrict__ oldr, const double* __restrict__ oldi,
@@ -258,8 +261,8 @@ __device__ __forceinline__ void combine_body(const double* __restrict__ pr, cons
       fi = acc[npsi + idx];
     }
     for (int s = 0; s < nparts; ++s) {
-      fr += part[(size_t)s * bs.part + idx];
-      fi += part[(size_t)s * bs.part + npsi + idx];
+      fr += (double)part[(size_t)s * bs.part + idx];
+      fi += (double)part[(size_t)s * bs.part + npsi + idx];
     }
     const double m = allow[idx];
     fr *= m;
@@ -326,17 +329,182 @@ __device__ __forceinline__ void combine_body(const double* __restrict__ pr, cons
 }
 
 
-template <int NA, bool SO>
+template <int NA, bool SO, typename PT>
 __global__ void __launch_bounds__(LZ_THREADS)
     k_combine(const double* __restrict__ pr, const double* __restrict__ pi, const double* __restrict__ er,
               const double* __restrict__ ei, const double* __restrict__ allow, const double* __restrict__ acc,
-              const double* __restrict__ part, int nparts, const double2* __restrict__ so,
+              const void* __restrict__ part, int nparts, const double2* __restrict__ so,
               double* __restrict__ outr, double* __restrict__ outi, int nbk, int na, size_t npsi, int use_e0,
               int use_so, int backwards, const double* __restrict__ oldr, const double* __restrict__ oldi,
               const double* __restrict__ rb_base, const int* __restrict__ itp, double* __restrict__ red,
               const BlockStrides bs) {
-  combine_body<NA, SO>(pr, pi, er, ei, allow, acc, part, nparts, so, outr, outi, nbk, na, npsi, use_e0, use_so,
-                       backwards, oldr, oldi, rb_base, itp, red, bs, blockIdx.x, blockIdx.y, gridDim.x);
+  combine_body<NA, SO, PT>(pr, pi, er, ei, allow, acc, static_cast<const PT*>(part), nparts, so, outr, outi, nbk, na,
+                           npsi, use_e0, use_so, backwards, oldr, oldi, rb_base, itp, red, bs, blockIdx.x,
+                           blockIdx.y, gridDim.x);
+}
+
+// ------------------------------------------- double-float Lanczos step (mixed precision)
+// The mixed-precision Haydock loop keeps its vectors as double-float planes
+// (ocn_df.cuh): a float2 (h, l) per real value, at the offsets of the FP64
+// layout.  The operator data are double-float / binary32 copies (energies,
+// masks, spin-orbit matrix) and the long-range / multiplet partials are the
+// binary32 outputs of the tensor-core contractions; every per-element operation
+// runs on the FP32 pipe.  Reduction partials are double-float pairs in the
+// (double-sized) partial arrays; a, b are recorded in FP64.
+
+// Deterministic block reduction of K double-float sums; thread 0 writes them to
+// out[0..K-1].  sh: 32 float2 per sum.
+template <int K>
+__device__ __forceinline__ void block_reduce_df(df (&v)[K], float2 (*sh)[32], float2* __restrict__ out) {
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+    for (int o = 16; o > 0; o >>= 1) {
+      const float bh = __shfl_down_sync(0xffffffffu, v[j].h, o);
+      const float bl = __shfl_down_sync(0xffffffffu, v[j].l, o);
+      v[j] = df_add(v[j], df{bh, bl});
+    }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0)
+#pragma unroll
+    for (int j = 0; j < K; ++j) sh[j][w] = make_float2(v[j].h, v[j].l);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      df t{0.0f, 0.0f};
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t = df_add(t, df{sh[j][i].x, sh[j][i].y});
+      out[j] = make_float2(t.h, t.l);
+    }
+  }
+}
+
+// Sum of nblk double-float partial pairs, in the same order in every thread of
+// every block.
+__device__ __forceinline__ void reduce_pairs_df(const float2* __restrict__ red, int nblk, df* s0, df* s1) {
+  __shared__ float2 sh[2][32];
+  df a{0.0f, 0.0f}, b{0.0f, 0.0f};
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
+    a = df_add(a, df{red[2 * i].x, red[2 * i].y});
+    b = df_add(b, df{red[2 * i + 1].x, red[2 * i + 1].y});
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a = df_add(a, df{__shfl_down_sync(0xffffffffu, a.h, o), __shfl_down_sync(0xffffffffu, a.l, o)});
+    b = df_add(b, df{__shfl_down_sync(0xffffffffu, b.h, o), __shfl_down_sync(0xffffffffu, b.l, o)});
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) {
+    sh[0][w] = make_float2(a.h, a.l);
+    sh[1][w] = make_float2(b.h, b.l);
+  }
+  __syncthreads();
+  df ta{0.0f, 0.0f}, tb{0.0f, 0.0f};
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+    ta = df_add(ta, df{sh[0][i].x, sh[0][i].y});
+    tb = df_add(tb, df{sh[1][i].x, sh[1][i].y});
+  }
+  *s0 = ta;
+  *s1 = tb;
+}
+
+// combine + first Lanczos stage (as combine_body with the Lanczos fields set,
+// OCEAN_action.f90:337-372 then OCEAN_haydock.f90:848-860): h = E o psi + allow o
+// (partials) + S psi - b_{i-1} old, and the block partial of <h|psi>.
+template <int NA, bool SO>
+__device__ __forceinline__ void combine_df_body(const float2* __restrict__ pr, const float2* __restrict__ pi,
+                                                const float2* __restrict__ er, const float2* __restrict__ ei,
+                                                const float* __restrict__ allow, const float* __restrict__ part,
+                                                int nparts, const float2* __restrict__ so, float2* __restrict__ outr,
+                                                float2* __restrict__ outi, int nbk, size_t npsi, int use_e0,
+                                                const float2* __restrict__ oldr, const float2* __restrict__ oldi,
+                                                const double* __restrict__ rb_base, const int* __restrict__ itp,
+                                                float2* __restrict__ red, const BlockStrides bs, int bx, int by,
+                                                int nbx) {
+  __shared__ float2 sh[2][32];
+  __shared__ float2 s_bm;
+  const size_t v = by;
+  pr += v * bs.vec;
+  pi += v * bs.vec;
+  outr += v * bs.vec;
+  outi += v * bs.vec;
+  oldr += v * bs.vec;
+  oldi += v * bs.vec;
+  part += v * 2 * npsi;
+  rb_base += v * bs.coef;
+  red += v * bs.red;
+  if (threadIdx.x == 0) {
+    const df b = df_split(-rb_base[*itp - 1]);  // -b_{i-1}
+    s_bm = make_float2(b.h, b.l);
+  }
+  __syncthreads();
+  const df bm{s_bm.x, s_bm.y};
+  df dr{0.0f, 0.0f}, di{0.0f, 0.0f};
+  const size_t nall = (size_t)nbk * NA;
+  for (size_t idx = bx * (size_t)blockDim.x + threadIdx.x; idx < nall; idx += (size_t)nbx * blockDim.x) {
+    const int ic = (int)(idx / (size_t)nbk);
+    const size_t e = idx - (size_t)ic * nbk;
+    const df qr = df_ld(pr, idx), qi = df_ld(pi, idx);
+    df fr{0.0f, 0.0f}, fi{0.0f, 0.0f};
+    for (int s = 0; s < nparts; ++s) {
+      fr = df_add(fr, part[(size_t)s * bs.part + idx]);
+      fi = df_add(fi, part[(size_t)s * bs.part + npsi + idx]);
+    }
+    const float m = allow[idx];
+    fr = df_mul(fr, m);
+    fi = df_mul(fi, m);
+    if (SO) {
+#pragma unroll
+      for (int jc = 0; jc < NA; ++jc) {
+        const float2 sv = so[jc * NA + ic];
+        const size_t j = e + (size_t)nbk * jc;
+        const df qr2 = df_ld(pr, j), qi2 = df_ld(pi, j);
+        fr = df_add(fr, df_mul(qr2, sv.x));
+        fr = df_add(fr, df_mul(qi2, -sv.y));
+        fi = df_add(fi, df_mul(qi2, sv.x));
+        fi = df_add(fi, df_mul(qr2, sv.y));
+      }
+    }
+    df hr = fr, hi = fi;
+    if (use_e0) {
+      const df a = df_ld(er, idx);
+      hr = df_add(hr, df_mul(a, qr));
+      hi = df_add(hi, df_mul(a, qi));
+      if (ei) {
+        const df b = df_ld(ei, idx);
+        hr = df_add(hr, df_neg(df_mul(b, qi)));
+        hi = df_add(hi, df_mul(b, qr));
+      }
+    }
+    hr = df_add(hr, df_mul(bm, df_ld(oldr, idx)));
+    hi = df_add(hi, df_mul(bm, df_ld(oldi, idx)));
+    // psi_dot(hpsi, psi): sum conj(h) psi
+    df_fma(dr.h, dr.l, hr, qr);
+    df_fma(dr.h, dr.l, hi, qi);
+    df_fma(di.h, di.l, hr, qi);
+    df_fma(di.h, di.l, df_neg(hi), qr);
+    df_st(outr, idx, hr);
+    df_st(outi, idx, hi);
+  }
+  df q[2] = {dr, di};
+  float2 tot[2];
+  block_reduce_df<2>(q, sh, tot);
+  if (threadIdx.x == 0) {
+    red[2 * bx] = tot[0];
+    red[2 * bx + 1] = tot[1];
+  }
+}
+
+template <int NA, bool SO>
+__global__ void __launch_bounds__(LZ_THREADS)
+    k_combine_df(const float2* __restrict__ pr, const float2* __restrict__ pi, const float2* __restrict__ er,
+                 const float2* __restrict__ ei, const float* __restrict__ allow, const float* __restrict__ part,
+                 int nparts, const float2* __restrict__ so, float2* __restrict__ outr, float2* __restrict__ outi,
+                 int nbk, size_t npsi, int use_e0, const float2* __restrict__ oldr, const float2* __restrict__ oldi,
+                 const double* __restrict__ rb_base, const int* __restrict__ itp, float2* __restrict__ red,
+                 const BlockStrides bs) {
+  combine_df_body<NA, SO>(pr, pi, er, ei, allow, part, nparts, so, outr, outi, nbk, npsi, use_e0, oldr, oldi, rb_base,
+                          itp, red, bs, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
 // The combine + first Lanczos stage of several contexts of one (Na, spin-orbit)
@@ -344,12 +512,99 @@ __global__ void __launch_bounds__(LZ_THREADS)
 // contexts); every context keeps the block partition (and so the reduction
 // order) of its own launches.
 template <int NA, bool SO>
-__global__ void __launch_bounds__(LZ_THREADS) k_combine_group(const CombineArgs* __restrict__ tab) {
+__global__ void __launch_bounds__(LZ_THREADS) k_combine_df_group(const CombineArgs* __restrict__ tab) {
   const CombineArgs& a = tab[blockIdx.z];
   if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
-  combine_body<NA, SO>(a.pr, a.pi, a.er, a.ei, a.allow, a.acc, a.part, a.nparts, a.so, a.outr, a.outi, a.nbk,
-                       a.na, a.npsi, a.use_e0, a.use_so, a.backwards, a.oldr, a.oldi, a.rb_base, a.itp, a.red,
-                       a.bs, blockIdx.x, blockIdx.y, a.nblk);
+  combine_df_body<NA, SO>(reinterpret_cast<const float2*>(a.pr), reinterpret_cast<const float2*>(a.pi), a.er_df,
+                          a.ei_df, a.allow_f, reinterpret_cast<const float*>(a.part), a.nparts, a.so_f,
+                          reinterpret_cast<float2*>(a.outr), reinterpret_cast<float2*>(a.outi), a.nbk, a.npsi,
+                          a.use_e0, reinterpret_cast<const float2*>(a.oldr), reinterpret_cast<const float2*>(a.oldi),
+                          a.rb_base, a.itp, reinterpret_cast<float2*>(a.red), a.bs, blockIdx.x, blockIdx.y, a.nblk);
+}
+
+// Lanczos stage 2 (OCEAN_haydock.f90:862-878): a_{i-1} = Re<h|psi>; h -= a psi; partial |h|^2.
+__device__ __forceinline__ void lanczos2_df_body(const float2* __restrict__ red1, int nblk, float2* __restrict__ hr,
+                                                 float2* __restrict__ hi, const float2* __restrict__ pr,
+                                                 const float2* __restrict__ pi, size_t n, float2* __restrict__ red2,
+                                                 double* __restrict__ ra_base, double* __restrict__ ia_base,
+                                                 const int* __restrict__ itp, const BlockStrides bs, int bx, int by,
+                                                 int nbx) {
+  __shared__ float2 sh[1][32];
+  const size_t v = by;
+  red1 += v * bs.red;
+  red2 += v * bs.red;
+  hr += v * bs.vec;
+  hi += v * bs.vec;
+  pr += v * bs.vec;
+  pi += v * bs.vec;
+  ra_base += v * bs.coef;
+  ia_base += v * bs.coef;
+  df a, ia;
+  reduce_pairs_df(red1, nblk, &a, &ia);
+  if (bx == 0 && threadIdx.x == 0) {
+    const int it = *itp;
+    ra_base[it - 1] = df_value(a);
+    ia_base[it - 1] = df_value(ia);
+  }
+  const df am = df_neg(a);
+  df s[1] = {df{0.0f, 0.0f}};
+  for (size_t e = bx * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)nbx * blockDim.x) {
+    const df r = df_add(df_ld(hr, e), df_mul(am, df_ld(pr, e)));
+    const df i = df_add(df_ld(hi, e), df_mul(am, df_ld(pi, e)));
+    df_st(hr, e, r);
+    df_st(hi, e, i);
+    df_fma(s[0].h, s[0].l, r, r);
+    df_fma(s[0].h, s[0].l, i, i);
+  }
+  float2 tot[1];
+  block_reduce_df<1>(s, sh, tot);
+  if (threadIdx.x == 0) {
+    red2[2 * bx] = tot[0];
+    red2[2 * bx + 1] = make_float2(0.0f, 0.0f);
+  }
+}
+
+__global__ void __launch_bounds__(LZ_THREADS)
+    k_lanczos2_df(const float2* __restrict__ red1, int nblk, float2* __restrict__ hr, float2* __restrict__ hi,
+                  const float2* __restrict__ pr, const float2* __restrict__ pi, size_t n, float2* __restrict__ red2,
+                  double* __restrict__ ra_base, double* __restrict__ ia_base, const int* __restrict__ itp,
+                  const BlockStrides bs) {
+  lanczos2_df_body(red1, nblk, hr, hi, pr, pi, n, red2, ra_base, ia_base, itp, bs, blockIdx.x, blockIdx.y,
+                   gridDim.x);
+}
+
+__global__ void __launch_bounds__(LZ_THREADS) k_lanczos2_df_group(const Lanczos2Args* __restrict__ tab) {
+  const Lanczos2Args& a = tab[blockIdx.z];
+  if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
+  lanczos2_df_body(reinterpret_cast<const float2*>(a.red1), a.nblk, reinterpret_cast<float2*>(a.hr),
+                   reinterpret_cast<float2*>(a.hi), reinterpret_cast<const float2*>(a.pr),
+                   reinterpret_cast<const float2*>(a.pi), a.n, reinterpret_cast<float2*>(a.red2), a.ra_base,
+                   a.ia_base, a.itp, a.bs, blockIdx.x, blockIdx.y, a.nblk);
+}
+
+// Operator data of the double-float loop, from the FP64 copies: energies as
+// double-float, the mask and the spin-orbit matrix as binary32.
+__global__ void k_df_operators(const double* __restrict__ er, const double* __restrict__ ei,
+                               const double* __restrict__ allow, const double2* __restrict__ so, float2* __restrict__ erd,
+                               float2* __restrict__ eid, float* __restrict__ allowf, float2* __restrict__ sof, size_t n,
+                               int nso) {
+  const size_t m = n > (size_t)nso ? n : (size_t)nso;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < m; i += (size_t)gridDim.x * blockDim.x) {
+    if (i < n) {
+      df_st(erd, i, df_split(er[i]));
+      df_st(eid, i, df_split(ei[i]));
+      allowf[i] = (float)allow[i];
+    }
+    if (i < (size_t)nso) sof[i] = make_float2((float)so[i].x, (float)so[i].y);
+  }
+}
+
+// FP64 values -> double-float in place (element i keeps its 8 bytes)
+__global__ void k_to_df_inplace(double* __restrict__ v, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const df d = df_split(v[i]);
+    reinterpret_cast<float2*>(v)[i] = make_float2(d.h, d.l);
+  }
 }
 
 // Sum of nb partial pairs in a fixed order, done identically by every block.
@@ -457,12 +712,6 @@ __global__ void __launch_bounds__(LZ_THREADS)
   lanczos2_body(red1, nblk, hr, hi, pr, pi, n, red2, ra_base, ia_base, itp, bs, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
-__global__ void __launch_bounds__(LZ_THREADS) k_lanczos2_group(const Lanczos2Args* __restrict__ tab) {
-  const Lanczos2Args& a = tab[blockIdx.z];
-  if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
-  lanczos2_body(a.red1, a.nblk, a.hr, a.hi, a.pr, a.pi, a.n, a.red2, a.ra_base, a.ia_base, a.itp, a.bs,
-                blockIdx.x, blockIdx.y, a.nblk);
-}
 
 // Lanczos stage 3: b_i = sqrt(sum); psi_new = h / b_i (in place in h).
 __global__ void __launch_bounds__(LZ_THREADS) k_lanczos3(const double* __restrict__ red2, int nblk, double* __restrict__ hr,
@@ -741,10 +990,20 @@ __global__ void k_reduce_final(const double* __restrict__ red, int nblk, double*
 }
 
 
-typedef decltype(&k_combine<4, false>) CombineFn;
-CombineFn combine_kernel(int na, int use_so) {
-  if (na == 4) return use_so ? k_combine<4, true> : k_combine<4, false>;
-  return use_so ? k_combine<12, true> : k_combine<12, false>;
+typedef decltype(&k_combine<4, false, double>) CombineFn;
+// f32_parts: the partials come from the tensor-core contractions (mixed precision)
+CombineFn combine_kernel(int na, int use_so, bool f32_parts) {
+  if (f32_parts) {
+    if (na == 4) return use_so ? k_combine<4, true, float> : k_combine<4, false, float>;
+    return use_so ? k_combine<12, true, float> : k_combine<12, false, float>;
+  }
+  if (na == 4) return use_so ? k_combine<4, true, double> : k_combine<4, false, double>;
+  return use_so ? k_combine<12, true, double> : k_combine<12, false, double>;
+}
+typedef decltype(&k_combine_df<4, false>) CombineDfFn;
+CombineDfFn combine_df_kernel(int na, int use_so) {
+  if (na == 4) return use_so ? k_combine_df<4, true> : k_combine_df<4, false>;
+  return use_so ? k_combine_df<12, true> : k_combine_df<12, false>;
 }
 
 inline int grid_for(size_t n, int block, int cap) {
@@ -895,10 +1154,12 @@ int mult_hamp(ocn_ctx* c, const double2* amp, double2* hamp) {
 
 // Slices of d_accpart that hold terms of the current action: the long-range
 // K-split partials, followed (mixed precision) by the multiplet's.
-void active_parts(const ocn_ctx* c, const int* hf, const double** base, int* count) {
+void active_parts(const ocn_ctx* c, const int* hf, const void** base, int* count) {
   const bool lr = c->sys.long_range && hf[0] == 1;
   const bool mm = c->mult_parts > 0 && c->sys.mult && hf[4] == 1 && c->have_mult;
-  *base = c->d_accpart + (lr ? 0 : (size_t)c->lr_xsplit * c->part_stride);
+  const size_t off = lr ? 0 : (size_t)c->lr_xsplit * c->part_stride;  // elements
+  if (mixed_parts(c)) *base = reinterpret_cast<const float*>(c->d_accpart) + off;
+  else *base = c->d_accpart + off;
   *count = (lr ? c->lr_xsplit : 0) + (mm ? c->mult_parts : 0);
 }
 
@@ -945,17 +1206,19 @@ int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* 
             size_t vstride, const int* hflag, int backwards, int v0) {
   const int nbk = c->nb * c->nk;
   const int use_so = (c->sys.mult && hflag[5] == 1 && c->have_so) ? 1 : 0;
-  const double* parts;
+  const void* parts;
   int nparts;
   active_parts(c, hflag, &parts, &nparts);
   const BlockStrides bs = {vstride, c->part_stride, 0, 0};
-  auto kern = combine_kernel(c->na, use_so);
+  const bool f32 = mixed_parts(c);
+  auto kern = combine_kernel(c->na, use_so, f32);
   dim3 grid(grid_for(c->npsi, LZ_THREADS, 4 * c->sm_count), nv);
   // vector v0 of the block: its long-range partials and multiplet accumulator
-  parts += (size_t)v0 * 2 * c->npsi;
+  const void* pv = f32 ? static_cast<const void*>(static_cast<const float*>(parts) + (size_t)v0 * 2 * c->npsi)
+                       : static_cast<const void*>(static_cast<const double*>(parts) + (size_t)v0 * 2 * c->npsi);
   kern<<<grid, LZ_THREADS, 0, c->stream>>>(
       d_pr, d_pi, c->d_er, c->ei_nonzero ? c->d_ei : nullptr, c->d_allow,
-      c->acc_valid ? c->d_acc + (size_t)v0 * vstride : nullptr, parts, nparts,
+      c->acc_valid ? c->d_acc + (size_t)v0 * vstride : nullptr, pv, nparts,
       c->d_so, d_or, d_oi, nbk, c->na, c->npsi, c->sys.e0, use_so, backwards, nullptr, nullptr,
       nullptr, nullptr, nullptr, bs);
   ++c->launches;
@@ -966,21 +1229,42 @@ int combine(ocn_ctx* c, int nv, const double* d_pr, const double* d_pi, double* 
 // Fused combine + ocean_hay_ab_twoterm for iteration i = *itp of nv chains:
 // reads b_{i-1} from rb, writes a_{i-1}, Im a_{i-1} and b_i
 // (OCEAN_haydock.f90:848-889).  old/psi/h are block bases (vector stride 2*npsi),
-// ra/ia/rb coefficient bases with cstride between chains.
+// ra/ia/rb coefficient bases with cstride between chains.  Mixed precision: the
+// vectors are double-float planes (haydock_to_df) and the step runs on the FP32
+// pipe; FP64: the reference's arithmetic in FP64.
 int lanczos_launch(ocn_ctx* c, int nv, const double* old, const double* psi, double* h, double* ra,
                    double* ia, double* rb, size_t cstride, const int* itp) {
   const int nbk = c->nb * c->nk;
   const size_t n = c->npsi;
   const int* hf = c->sys.nhflag;
   const int use_so = (c->sys.mult && hf[5] == 1 && c->have_so) ? 1 : 0;
-  const double* parts;
+  const void* parts;
   int nparts;
   active_parts(c, hf, &parts, &nparts);
   const int nblk = c->red_blocks;
   const BlockStrides bs = {2 * n, c->part_stride, cstride, (size_t)4 * nblk};
   TimedScope ts(c, T_LANCZOS);
   dim3 grid(nblk, nv);
-  auto kern = combine_kernel(c->na, use_so);
+  if (mixed_parts(c)) {
+    typedef const float2* cf2;
+    auto kd = combine_df_kernel(c->na, use_so);
+    kd<<<grid, LZ_THREADS, 0, c->stream>>>(
+        reinterpret_cast<cf2>(psi), reinterpret_cast<cf2>(psi + n), c->d_er_df, c->ei_nonzero ? c->d_ei_df : nullptr,
+        c->d_allow_f, static_cast<const float*>(parts), nparts, c->d_so_f, reinterpret_cast<float2*>(h),
+        reinterpret_cast<float2*>(h + n), nbk, n, c->sys.e0, reinterpret_cast<cf2>(old), reinterpret_cast<cf2>(old + n),
+        rb, itp, reinterpret_cast<float2*>(c->d_red), bs);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+    k_lanczos2_df<<<grid, LZ_THREADS, 0, c->stream>>>(
+        reinterpret_cast<cf2>(c->d_red), nblk, reinterpret_cast<float2*>(h), reinterpret_cast<float2*>(h + n),
+        reinterpret_cast<cf2>(psi), reinterpret_cast<cf2>(psi + n), n, reinterpret_cast<float2*>(c->d_red + 2 * nblk),
+        ra, ia, itp, bs);
+    ++c->launches;
+    OCN_CUDA(c, cudaGetLastError());
+    // b_i, psi = h / b_i and the next psi operand
+    return mixed_norm_prep(c, nv, c->d_red + 2 * nblk, nblk, bs.red, h, rb, cstride, itp);
+  }
+  auto kern = combine_kernel(c->na, use_so, false);
   kern<<<grid, LZ_THREADS, 0, c->stream>>>(psi, psi + n, c->d_er, c->ei_nonzero ? c->d_ei : nullptr,
                                     c->d_allow, c->acc_valid ? c->d_acc : nullptr, parts,
                                     nparts, c->d_so, h, h + n, nbk, c->na, n, c->sys.e0, use_so, 0,
@@ -991,10 +1275,22 @@ int lanczos_launch(ocn_ctx* c, int nv, const double* old, const double* psi, dou
                                           ra, ia, itp, bs);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
-  if (c->dims.precision == OCN_PREC_MIXED && c->mixed)  // also builds the next psi operand
-    return mixed_norm_prep(c, nv, c->d_red + 2 * nblk, nblk, bs.red, h, rb, cstride, itp);
   k_lanczos3<<<grid, LZ_THREADS, 0, c->stream>>>(c->d_red + 2 * nblk, nblk, h, h + n, n, rb, itp, bs);
   ++c->launches;
+  OCN_CUDA(c, cudaGetLastError());
+  return OCN_OK;
+}
+
+// The double-float operator copies (allocated by the caller) and the first
+// vectors of a mixed-precision Haydock run: nv chains of FP64 planes at buf
+// (vector stride 2n) converted in place.
+int haydock_to_df(ocn_ctx* c, double* buf, int nv) {
+  const size_t n = c->npsi;
+  const int nso = c->na * c->na;
+  k_df_operators<<<grid_for(std::max(n, (size_t)nso), 256, 4 * c->sm_count), 256, 0, c->stream>>>(
+      c->d_er, c->d_ei, c->d_allow, c->d_so, c->d_er_df, c->d_ei_df, c->d_allow_f, c->d_so_f, n, nso);
+  k_to_df_inplace<<<grid_for(2 * n * nv, 256, 4 * c->sm_count), 256, 0, c->stream>>>(buf, 2 * n * nv);
+  c->launches += 2;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;
 }
@@ -1101,7 +1397,8 @@ void lz_group_destroy(LzGroup* g) {
 }
 
 // The records of lanczos_launch for every member and each of the three buffer
-// rotations of a captured three-iteration graph.
+// rotations of a captured three-iteration graph (grouped members are mixed
+// precision: double-float vectors).
 int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out) {
   *out = nullptr;
   if (mem.empty()) return OCN_ERR_ARG;
@@ -1142,7 +1439,7 @@ int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out) {
       const double* psi = b.buf[(r + 1) % 3];
       double* h = b.buf[(r + 2) % 3];
       const int* hf = c->sys.nhflag;
-      const double* parts;
+      const void* parts;  // binary32 partials (grouped members are mixed precision)
       int nparts;
       active_parts(c, hf, &parts, &nparts);
       const int nblk = c->red_blocks;
@@ -1154,7 +1451,7 @@ int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out) {
       a.ei = c->ei_nonzero ? c->d_ei : nullptr;
       a.allow = c->d_allow;
       a.acc = nullptr;  // grouped members have no multiplet term
-      a.part = parts;
+      a.part = static_cast<const double*>(parts);  // read as binary32 by k_combine_df_group
       a.nparts = nparts;
       a.so = c->d_so;
       a.outr = h;
@@ -1171,6 +1468,10 @@ int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out) {
       a.itp = c->d_iter;
       a.red = c->d_red;
       a.bs = bs;
+      a.er_df = c->d_er_df;
+      a.ei_df = c->ei_nonzero ? c->d_ei_df : nullptr;
+      a.allow_f = c->d_allow_f;
+      a.so_f = c->d_so_f;
       a.nv = b.nv;
       a.nblk = nblk;
       Lanczos2Args& l = la[i];
@@ -1222,16 +1523,16 @@ int lz_group_step(LzGroup* g, int rot, cudaStream_t s) {
     const dim3 gc(g->nblk, g->nvmax, k.count);
     const CombineArgs* t = g->d_comb[rot] + k.first;
     if (k.na == 4) {
-      if (k.so) k_combine_group<4, true><<<gc, LZ_THREADS, 0, s>>>(t);
-      else k_combine_group<4, false><<<gc, LZ_THREADS, 0, s>>>(t);
+      if (k.so) k_combine_df_group<4, true><<<gc, LZ_THREADS, 0, s>>>(t);
+      else k_combine_df_group<4, false><<<gc, LZ_THREADS, 0, s>>>(t);
     } else {
-      if (k.so) k_combine_group<12, true><<<gc, LZ_THREADS, 0, s>>>(t);
-      else k_combine_group<12, false><<<gc, LZ_THREADS, 0, s>>>(t);
+      if (k.so) k_combine_df_group<12, true><<<gc, LZ_THREADS, 0, s>>>(t);
+      else k_combine_df_group<12, false><<<gc, LZ_THREADS, 0, s>>>(t);
     }
     if (cudaGetLastError() != cudaSuccess) return OCN_ERR_CUDA;
   }
   const dim3 grid(g->nblk, g->nvmax, g->n);
-  k_lanczos2_group<<<grid, LZ_THREADS, 0, s>>>(g->d_lz2[rot]);
+  k_lanczos2_df_group<<<grid, LZ_THREADS, 0, s>>>(g->d_lz2[rot]);
   return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
 }
 

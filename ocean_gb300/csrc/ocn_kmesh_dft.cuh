@@ -288,11 +288,12 @@ __device__ __forceinline__ void cube_pass(typename C2<R>::T* buf, int nt_rt, int
 
 // nt transforms of the x-point (alpha, or (vector, alpha) for a block of psi):
 // transform t of k-point k at phi[(k*nx + x)*ld + t], ld >= nt (a CTA may own a
-// slice of the transforms of its x-point).
+// slice of the transforms of its x-point).  Leaves Nk * phi'(k) of transform t
+// in buf[t*SLAB + (k/N)*(N+1) + k%N] (not yet divided by Nk); ends with a barrier.
 template <typename R, int N, int NTC>
-__device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R* __restrict__ W, int nx,
-                                    int x, int nt_rt, int ld, typename C2<R>::T* buf,
-                                    const typename C2<R>::T* __restrict__ tw) {
+__device__ void kmesh_cube_transform(const typename C2<R>::T* __restrict__ phi, const R* __restrict__ W, int nx,
+                                     int x, int nt_rt, int ld, typename C2<R>::T* buf,
+                                     const typename C2<R>::T* __restrict__ tw) {
   typedef typename C2<R>::T CT;
   const int nt = NTC ? NTC : nt_rt;
   constexpr int NK = N * N * N;
@@ -339,6 +340,18 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
     cube_pass<R, N, NTC>(buf, nt, ax, tw + ax * OCN_MAX_KDIM, (R)-1);
     __syncthreads();
   }
+}
+
+// The transformed planes of kmesh_cube_transform, divided by Nk, back into phi.
+template <typename R, int N, int NTC>
+__device__ void kmesh_cube_store(typename C2<R>::T* __restrict__ phi, int nx, int x, int nt_rt, int ld,
+                                 const typename C2<R>::T* buf) {
+  typedef typename C2<R>::T CT;
+  const int nt = NTC ? NTC : nt_rt;
+  constexpr int NK = N * N * N;
+  constexpr int P3 = N + 1;
+  constexpr int SLAB = cube_slab<CT>(N);
+  const int dt = blockDim.x % nt, dk = blockDim.x / nt;
   const R norm = (R)1 / (R)NK;
   if constexpr (NTC > 0) {
     for (int e = threadIdx.x; e < NTC * NK; e += blockDim.x) {
@@ -365,6 +378,14 @@ __device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R
       }
     }
   }
+}
+
+template <typename R, int N, int NTC>
+__device__ void kmesh_convolve_cube(typename C2<R>::T* __restrict__ phi, const R* __restrict__ W, int nx,
+                                    int x, int nt_rt, int ld, typename C2<R>::T* buf,
+                                    const typename C2<R>::T* __restrict__ tw) {
+  kmesh_cube_transform<R, N, NTC>(phi, W, nx, x, nt_rt, ld, buf, tw);
+  kmesh_cube_store<R, N, NTC>(phi, nx, x, nt_rt, ld, buf);
 }
 
 // dL/dW of the long-range term for the x-point of this CTA, from the band-to-x
@@ -441,11 +462,12 @@ inline bool kmesh_cube_supported(const int kmesh[3]) {
   } while (0)
 
 // Whole k-mesh step for the x-point of this CTA.  phi layout [k][x][a].
-// twiddles: tw + ax*OCN_MAX_KDIM.
+// twiddles: tw + ax*OCN_MAX_KDIM.  kmesh_transform leaves Nk * phi'(k) of
+// transform a in buf[a*g.slab + kpad(g, k)] and ends with a barrier.
 template <typename R>
-__device__ void kmesh_convolve(typename C2<R>::T* __restrict__ phi, const R* __restrict__ W, int nx, int x,
-                               const KmeshGeom<R>& g, typename C2<R>::T* buf,
-                               const typename C2<R>::T* __restrict__ tw) {
+__device__ void kmesh_transform(const typename C2<R>::T* __restrict__ phi, const R* __restrict__ W, int nx, int x,
+                                const KmeshGeom<R>& g, typename C2<R>::T* buf,
+                                const typename C2<R>::T* __restrict__ tw) {
   typedef typename C2<R>::T CT;
   const int tot = g.na * g.nk;
   for (int k = threadIdx.x; k < g.nk; k += blockDim.x) {
@@ -470,6 +492,14 @@ __device__ void kmesh_convolve(typename C2<R>::T* __restrict__ phi, const R* __r
     dft_pass<R>(buf, g, ax, tw + ax * OCN_MAX_KDIM, (R)-1);
     __syncthreads();
   }
+}
+
+template <typename R>
+__device__ void kmesh_convolve(typename C2<R>::T* __restrict__ phi, const R* __restrict__ W, int nx, int x,
+                               const KmeshGeom<R>& g, typename C2<R>::T* buf,
+                               const typename C2<R>::T* __restrict__ tw) {
+  typedef typename C2<R>::T CT;
+  kmesh_transform<R>(phi, W, nx, x, g, buf, tw);
   const R norm = (R)1 / (R)g.nk;
   for (int k = threadIdx.x; k < g.nk; k += blockDim.x) {
     CT* dst = phi + ((size_t)k * nx + x) * g.na;

@@ -16,11 +16,14 @@
 // D[:, j + 2Na] is the full product.  MMA shape: M = 128 rows, N = 4 Na nvmax,
 // K = 16 per instruction.  Every byte of u2 read from HBM serves all nv vectors.
 //
-// Operands live in HBM as bf16 tiles read by TMA with 128-byte swizzling:
+// Operands live in HBM as bf16 tiles read by TMA:
 //   UA_s [k][x][K1]  (K1 = 2 Nb)      A of the band -> x contraction, built once
-//   UB_s [k][n][K2]  (K2 = 2 Nx)      A of the x -> band contraction, built once
+//   UB_s [k][n][K2]                   A of the x -> band contraction, built once
 //   B1   [k][j][K1]                   psi operand, rebuilt per action
-//   B2   [k][j][K2]                   phi' operand, rebuilt per action
+//   B2   [k][K2][j]                   phi' operand, MN-major, written by the k-mesh transform
+// with K2 = (x/64)*128 + c*64 + x%64 (both c halves of a 64-x block in consecutive
+// 64-wide K chunks).  A operands and B1 are K-major with 128-byte swizzling; B2 is
+// read in 16-column boxes with 32-byte swizzling.
 // The GEMM kernel is persistent and warp-specialised: warp 0 issues TMA loads,
 // warp 1 issues tcgen05.mma and owns the tensor-memory allocation, warps 2-5 drain
 // the double-buffered accumulator.  Every mbarrier wait is bounded in time; on
@@ -37,6 +40,7 @@
 #include <new>
 #include <string>
 
+#include "ocn_df.cuh"
 #include "ocn_internal.h"
 #include "ocn_kmesh_dft.cuh"
 
@@ -67,7 +71,7 @@ struct TcParams {
   uint32_t idesc;
   uint32_t tcols;
   float2* phi;   // mode 1 output [k][x][v*Na + a]
-  double* part;  // mode 2 output [split][v][re|im][npsi]
+  float* part;   // mode 2 output [split][v][re|im][npsi] (binary32: the accumulator's own precision)
   size_t npsi;
   int* err;
   int bshared;   // B operand has one k slice shared by every k (multiplet back-projection)
@@ -76,6 +80,7 @@ struct TcParams {
   int estg;      // launch-wide: mode-1 outputs staged per warp in shared memory, stored coalesced
   int starve;    // launch-wide test hook: the producer issues no loads, so the MMA warp's
                  // first bounded wait runs out with nothing in flight (OCN_ERR_TIMEOUT path)
+  int bmn;       // B is MN-major in SW32 boxes of 16 columns by 64 K rows (B2 of the x -> band contraction)
 };
 
 // Tensor maps of a group launch (kernel parameter space, 384 bytes per problem).
@@ -141,6 +146,14 @@ __device__ __forceinline__ void tc_fence_after() {
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
          ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// MN-major operand tile with 32-byte swizzling, as TMA writes boxes of 64 K-rows
+// by 16 MN-elements (32 bytes): 8-row K groups 256 bytes apart (stride byte
+// offset), consecutive 16-element MN atoms 2048 bytes apart (leading byte offset).
+__device__ __forceinline__ uint64_t sw32_mn_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(2048 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)6 << 61);
 }
 
 __device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
@@ -292,7 +305,12 @@ __device__ __forceinline__ void lr_tc_body(const TcParams& p, const Src& src) {
           mbar_expect_tx(full0 + 8 * stage, 2 * a_bytes + (uint32_t)tp.ncol * TC_BK * 2);
           tma_load_3d(sbase, src.map(ii, 0), full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + tp.koff);
           tma_load_3d(sbase + a_bytes, src.map(ii, 1), full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + tp.koff);
-          tma_load_3d(sbase + 2 * a_bytes, src.map(ii, 2), full0 + 8 * stage, c * TC_BK, 0, tp.bshared ? 0 : ti.k);
+          if (tp.bmn) {
+            for (int j = 0; j < tp.ncol / 16; ++j)
+              tma_load_3d(sbase + 2 * a_bytes + j * 2048, src.map(ii, 2), full0 + 8 * stage, 16 * j, c * TC_BK, ti.k);
+          } else {
+            tma_load_3d(sbase + 2 * a_bytes, src.map(ii, 2), full0 + 8 * stage, c * TC_BK, 0, tp.bshared ? 0 : ti.k);
+          }
           armed_phase[stage] = (int)phase;
           if (++stage == (uint32_t)S) {
             stage = 0;
@@ -340,7 +358,8 @@ __device__ __forceinline__ void lr_tc_body(const TcParams& p, const Src& src) {
           const uint32_t sa = su32(smem + stage * stage_bytes);
 #pragma unroll
           for (int kk = 0; kk < TC_BK / 16; ++kk) {
-            const uint64_t bd = sw128_desc(sa + 2 * a_bytes + kk * 32);
+            const uint64_t bd =
+                tp.bmn ? sw32_mn_desc(sa + 2 * a_bytes + kk * 512) : sw128_desc(sa + 2 * a_bytes + kk * 32);
             umma_bf16(dt, sw128_desc(sa + kk * 32), bd, tp.idesc, (c > ti.c0 || kk > 0) ? 1u : 0u);
             umma_bf16(dt, sw128_desc(sa + a_bytes + kk * 32), bd, tp.idesc, 1u);
           }
@@ -406,13 +425,13 @@ __device__ __forceinline__ void lr_tc_body(const TcParams& p, const Src& src) {
         } else {
           const int n = ti.row0 + row;
           if (n < tp.nb) {
-            double* pr = tp.part + ((size_t)ti.sp * tp.nvmax + vv) * 2 * tp.npsi;
-            double* pim = pr + tp.npsi;
+            float* pr = tp.part + ((size_t)ti.sp * tp.nvmax + vv) * 2 * tp.npsi;
+            float* pim = pr + tp.npsi;
             for (int a = 0; a < na; ++a) {
               if (tp.spin >= 0 && (a & 1) != tp.spin) continue;
               const size_t idx = (size_t)n + (size_t)tp.nb * ((size_t)ti.k + (size_t)tp.nk * a);
-              pr[idx] = -((double)v[a] + (double)v[2 * na + a]);
-              pim[idx] = -((double)v[na + a] + (double)v[3 * na + a]);
+              pr[idx] = -(v[a] + v[2 * na + a]);
+              pim[idx] = -(v[na + a] + v[3 * na + a]);
             }
           }
         }
@@ -475,6 +494,10 @@ __device__ __forceinline__ void split_bf16(float v, __nv_bfloat16& hi, __nv_bflo
   hi = __float2bfloat16_rn(v);
   lo = __float2bfloat16_rn(v - __bfloat162float(hi));
 }
+// two BF16 values as one 32-bit word, a at the lower address
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b) {
+  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
 
 // UA_s[k][x][K1]: K < Nb -> Re u(n=K), else Im u(n=K-Nb)   (from u [x][k][n])
 __global__ void k_build_ua(const double2* __restrict__ u, __nv_bfloat16* __restrict__ hi,
@@ -497,7 +520,8 @@ __global__ void k_build_ua(const double2* __restrict__ u, __nv_bfloat16* __restr
   }
 }
 
-// UB_s[k][n][K2]: K2 < Nx -> Re u(n, x=K2), else Im u(n, x=K2-Nx)
+// UB_s[k][n][K2]: K2 = (x/64)*128 + c*64 + x%64 -> Re u(n, x) (c = 0), Im u(n, x) (c = 1);
+// the padding of a partial last 64-x block is never written (zero since allocation)
 __global__ void k_build_ub(const double2* __restrict__ u, __nv_bfloat16* __restrict__ hi,
                            __nv_bfloat16* __restrict__ lo, int nb, int nk, int nx, int p2) {
   const long long total = (long long)nk * nb * 2 * nx;
@@ -512,7 +536,7 @@ __global__ void k_build_ub(const double2* __restrict__ u, __nv_bfloat16* __restr
     const float v = (float)(K < nx ? z.x : z.y);
     __nv_bfloat16 h, l;
     split_bf16(v, h, l);
-    const size_t o = ((size_t)k * nb + n) * p2 + K;
+    const size_t o = ((size_t)k * nb + n) * p2 + ((x >> 6) << 7) + (K < nx ? 0 : 64) + (x & 63);
     hi[o] = h;
     lo[o] = l;
   }
@@ -657,30 +681,39 @@ __global__ void k_prep_b3(const double2* __restrict__ hamp, __nv_bfloat16* __res
 }
 
 // Lanczos normalisation fused with the next action's psi operand
-// (OCEAN_haydock.f90:880-889 then long_range.f90:897-906): for chain v =
-// blockIdx.y, b_i = sqrt(sum of partials), psi = h / b_i written in place, and
-// B1 rows of vector v built from allow o psi.  One thread per (n, k) covers
-// both K = n and K = Nb + n for every alpha.
+// (OCEAN_haydock.f90:880-889 then long_range.f90:897-906), on the double-float
+// vectors of the mixed-precision loop: for chain v = blockIdx.y, b_i = sqrt(sum of
+// the double-float partials) (formed in FP64 by one thread, broadcast as a
+// double-float 1/b_i), psi = h / b_i written in place, and B1 rows of vector v
+// built from allow o psi.  One thread per (n, k) covers both K = n and K = Nb + n
+// for every alpha.
 __device__ __forceinline__ void norm_prep_body(const double* __restrict__ red2, int nblk, size_t rstride,
                             double* __restrict__ hbase, size_t vstride, size_t npsi,
-                            const double* __restrict__ allow, __nv_bfloat16* __restrict__ b1, int nb,
+                            const float* __restrict__ allow, __nv_bfloat16* __restrict__ b1, int nb,
                             int nk, int na, int ncol, int p1, double* __restrict__ rb_base,
                             size_t cstride, const int* __restrict__ itp, int bx, int by, int nbx) {
-  __shared__ double sh[32];
+  __shared__ float2 sh[32];
+  __shared__ float2 s_inv;
   const int vv = by;
-  const double* red = red2 + (size_t)vv * rstride;
-  double s = 0.0;
-  for (int i = threadIdx.x; i < nblk; i += blockDim.x) s += red[2 * i];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  const float2* red = reinterpret_cast<const float2*>(red2 + (size_t)vv * rstride);
+  df s{0.0f, 0.0f};
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) s = df_add(s, df{red[2 * i].x, red[2 * i].y});
+  for (int o = 16; o > 0; o >>= 1)
+    s = df_add(s, df{__shfl_down_sync(0xffffffffu, s.h, o), __shfl_down_sync(0xffffffffu, s.l, o)});
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = make_float2(s.h, s.l);
   __syncthreads();
-  double bb = 0.0;
-  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) bb += sh[i];
-  const double b = sqrt(bb);
-  if (bx == 0 && threadIdx.x == 0) rb_base[(size_t)vv * cstride + *itp] = b;
-  const double inv = 1.0 / b;
-  double* hr = hbase + (size_t)vv * vstride;
-  double* hi = hr + npsi;
+  if (threadIdx.x == 0) {
+    df bb{0.0f, 0.0f};
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) bb = df_add(bb, df{sh[i].x, sh[i].y});
+    const double b = sqrt(df_value(bb));
+    if (bx == 0) rb_base[(size_t)vv * cstride + *itp] = b;
+    const df inv = df_split(1.0 / b);
+    s_inv = make_float2(inv.h, inv.l);
+  }
+  __syncthreads();
+  const df inv{s_inv.x, s_inv.y};
+  float2* hr = reinterpret_cast<float2*>(hbase + (size_t)vv * vstride);
+  float2* hi = hr + npsi;
   const int g4 = 4 * na;
   const int total = nb * nk;
   for (int i = bx * blockDim.x + threadIdx.x; i < total; i += nbx * blockDim.x) {
@@ -689,11 +722,11 @@ __device__ __forceinline__ void norm_prep_body(const double* __restrict__ red2, 
     __nv_bfloat16* base = b1 + (size_t)k * ncol * p1 + (size_t)vv * g4 * p1;
     for (int a = 0; a < na; ++a) {
       const size_t idx = (size_t)i + (size_t)total * a;
-      const double r = hr[idx] * inv, im = hi[idx] * inv;
-      hr[idx] = r;
-      hi[idx] = im;
-      const double m = allow[idx];
-      const float qr = (float)(r * m), qi = (float)(im * m);
+      const df r = df_mul(df_ld(hr, idx), inv), im = df_mul(df_ld(hi, idx), inv);
+      df_st(hr, idx, r);
+      df_st(hi, idx, im);
+      const float m = allow[idx];
+      const float qr = df_to_float(r) * m, qi = df_to_float(im) * m;
       __nv_bfloat16 h0, l0, h1, l1, h2, l2;
       split_bf16(qr, h0, l0);
       split_bf16(qi, h1, l1);
@@ -713,7 +746,7 @@ __device__ __forceinline__ void norm_prep_body(const double* __restrict__ red2, 
 
 __global__ void __launch_bounds__(LZ_THREADS)
     k_norm_prep(const double* __restrict__ red2, int nblk, size_t rstride, double* __restrict__ hbase,
-                size_t vstride, size_t npsi, const double* __restrict__ allow, __nv_bfloat16* __restrict__ b1,
+                size_t vstride, size_t npsi, const float* __restrict__ allow, __nv_bfloat16* __restrict__ b1,
                 int nb, int nk, int na, int ncol, int p1, double* __restrict__ rb_base, size_t cstride,
                 const int* __restrict__ itp) {
   norm_prep_body(red2, nblk, rstride, hbase, vstride, npsi, allow, b1, nb, nk, na, ncol, p1, rb_base, cstride, itp,
@@ -726,7 +759,7 @@ struct NormGroupArgs {
   size_t rstride;
   double* hbase;
   size_t vstride, npsi;
-  const double* allow;
+  const float* allow;
   __nv_bfloat16* b1;
   int nb, nk, na, ncol, p1;
   double* rb_base;
@@ -742,50 +775,6 @@ __global__ void __launch_bounds__(LZ_THREADS) k_norm_prep_group(const NormGroupA
                  a.p1, a.rb_base, a.cstride, a.itp, blockIdx.x, blockIdx.y, a.nblk);
 }
 
-// B2[k][v*4Na + j][K2] from phi'[k][x][v*Na + a]:
-//   part 0 (Re out): K=(0,x) -> Re phi', K=(1,x) -> Im phi'
-//   part 1 (Im out): K=(0,x) -> Im phi', K=(1,x) -> -Re phi'
-__device__ __forceinline__ void prep_b2_body(const float2* __restrict__ phi, __nv_bfloat16* __restrict__ b2,
-                                             int nk, int nx, int na, int nv, int ncol, int p2, int bx, int nbx) {
-  const int total = nk * nx;
-  const int g4 = 4 * na;
-  const int nt = na * nv;
-  for (int i = bx * blockDim.x + threadIdx.x; i < total; i += nbx * blockDim.x) {
-    const int x = i % nx;
-    const int k = i / nx;
-    for (int t = 0; t < nt; ++t) {
-      const int vv = t / na, a = t % na;
-      __nv_bfloat16* base = b2 + (size_t)k * ncol * p2 + (size_t)vv * g4 * p2;
-      const float2 f = phi[((size_t)k * nx + x) * nt + t];
-      __nv_bfloat16 hr, lr, hi, li, hn, ln;
-      split_bf16(f.x, hr, lr);
-      split_bf16(f.y, hi, li);
-      split_bf16(-f.x, hn, ln);
-      // part 0
-      base[(size_t)(a)*p2 + x] = hr;
-      base[(size_t)(a)*p2 + nx + x] = hi;
-      base[(size_t)(2 * na + a) * p2 + x] = lr;
-      base[(size_t)(2 * na + a) * p2 + nx + x] = li;
-      // part 1
-      base[(size_t)(na + a) * p2 + x] = hi;
-      base[(size_t)(na + a) * p2 + nx + x] = hn;
-      base[(size_t)(3 * na + a) * p2 + x] = li;
-      base[(size_t)(3 * na + a) * p2 + nx + x] = ln;
-    }
-  }
-}
-
-__global__ void k_prep_b2(const float2* __restrict__ phi, __nv_bfloat16* __restrict__ b2, int nk, int nx,
-                          int na, int nv, int ncol, int p2) {
-  prep_b2_body(phi, b2, nk, nx, na, nv, ncol, p2, blockIdx.x, gridDim.x);
-}
-
-struct B2GroupArgs {
-  const float2* phi;
-  __nv_bfloat16* b2;
-  int nk, nx, na, nv, ncol, p2;
-  int cta0, nctas;  // this context's CTAs in the grouped grid
-};
 // The last of n records whose first CTA is <= b (records ordered by cta0).
 template <class A>
 __device__ __forceinline__ int group_find(const A* __restrict__ tab, int n, int b) {
@@ -797,56 +786,114 @@ __device__ __forceinline__ int group_find(const A* __restrict__ tab, int n, int 
   }
   return lo;
 }
-__global__ void k_prep_b2_group(const B2GroupArgs* __restrict__ tab, int n) {
-  const B2GroupArgs& a = tab[group_find(tab, n, blockIdx.x)];
-  prep_b2_body(a.phi, a.b2, a.nk, a.nx, a.na, a.nv, a.ncol, a.p2, blockIdx.x - a.cta0, a.nctas);
+
+// B2 rows of the x-point of this CTA, written straight from the transformed
+// planes (no phi' round trip through HBM).  B2 is MN-major: B2[k][K2][col],
+// K2 = (x/64)*128 + c*64 + x%64, col = v*4Na + s*2Na + part*Na + a, and
+//   part 0 (Re out): c = 0 -> Re phi', c = 1 -> Im phi'
+//   part 1 (Im out): c = 0 -> Im phi', c = 1 -> -Re phi'
+// with s = 0 / 1 the high / low BF16 half.  The CTA holds transforms t0 .. t0+nt-1
+// of its x-point (nt a multiple of Na, so whole vectors); get(t, k) = Nk phi'(k).
+// One thread per (k, c, vector) writes the vector's 4 Na columns (8 Na bytes).
+template <class Get>
+__device__ __forceinline__ void store_b2_rows(const Get& get, float norm, __nv_bfloat16* __restrict__ b2, int nk,
+                                              int x, int na, int t0, int nt, int ncol, int k2ext) {
+  const int nvl = nt / na, v0 = t0 / na;
+  const int row_x = ((x >> 6) << 7) + (x & 63);
+  const int items = nk * 2 * nvl;
+  for (int e = threadIdx.x; e < items; e += blockDim.x) {
+    const int vl = e % nvl;
+    const int c = (e / nvl) & 1;
+    const int k = e / (2 * nvl);
+    __nv_bfloat16* dst = b2 + ((size_t)k * k2ext + row_x + 64 * c) * ncol + (size_t)(v0 + vl) * 4 * na;
+    for (int a0 = 0; a0 < na; a0 += 4) {
+      // columns (s, part, a0..a0+3): four runs of 4 BF16
+      __nv_bfloat16 h[2][4], l[2][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float2 f = get(vl * na + a0 + q, k);
+        const float re = f.x * norm, im = f.y * norm;
+        split_bf16(c == 0 ? re : im, h[0][q], l[0][q]);
+        split_bf16(c == 0 ? im : -re, h[1][q], l[1][q]);
+      }
+      uint2 w[2][2];
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        w[0][part] = make_uint2(pack_bf16(h[part][0], h[part][1]), pack_bf16(h[part][2], h[part][3]));
+        w[1][part] = make_uint2(pack_bf16(l[part][0], l[part][1]), pack_bf16(l[part][2], l[part][3]));
+      }
+      if (na == 4) {  // (s, 0) and (s, 1) adjacent: one 16-byte store per half
+        *reinterpret_cast<uint4*>(dst) = make_uint4(w[0][0].x, w[0][0].y, w[0][1].x, w[0][1].y);
+        *reinterpret_cast<uint4*>(dst + 8) = make_uint4(w[1][0].x, w[1][0].y, w[1][1].x, w[1][1].y);
+      } else {
+#pragma unroll
+        for (int sp = 0; sp < 2; ++sp)
+#pragma unroll
+          for (int part = 0; part < 2; ++part)
+            *reinterpret_cast<uint2*>(dst + sp * 2 * na + part * na + a0) = w[sp][part];
+      }
+    }
+  }
 }
 
-// FP32 k-mesh transform, one CTA per x-point (ocn_kmesh_dft.cuh): generic meshes
-__global__ void k_lr_fft_w_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx,
-                               const KmeshGeom<float> g, const float2* __restrict__ twg) {
+// FP32 k-mesh transform of one x-point per CTA (ocn_kmesh_dft.cuh), B2 rows out: generic meshes
+__global__ void k_fft_b2(const float2* __restrict__ phi, const float* __restrict__ W, int nx,
+                         const KmeshGeom<float> g, const float2* __restrict__ twg, __nv_bfloat16* __restrict__ b2,
+                         int na, int ncol, int k2ext) {
   extern __shared__ float2 fsm[];
   float2* tw = fsm;
   float2* buf = fsm + 3 * OCN_MAX_KDIM;
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
   __syncthreads();
-  kmesh_convolve<float>(phi, W, nx, blockIdx.x, g, buf, tw);
+  kmesh_transform<float>(phi, W, nx, blockIdx.x, g, buf, tw);
+  const auto get = [&](int t, int k) { return buf[t * g.slab + kpad(g, k)]; };
+  store_b2_rows(get, 1.0f / (float)g.nk, b2, g.nk, blockIdx.x, na, 0, g.na, ncol, k2ext);
 }
 
-// cubic meshes, nt transforms per x-point (NTC: nt fixed at compile time, or 0)
+// cubic meshes: nt transforms (a slice of the ld of the x-point) per CTA
 template <int N, int NTC>
-__global__ void k_fft_cube_f32(float2* __restrict__ phi, const float* __restrict__ W, int nx, int nt, int ld,
-                               const float2* __restrict__ twg) {
+__device__ __forceinline__ void fft_b2_cube_body(const float2* __restrict__ phi, const float* __restrict__ W, int nx,
+                                                 int x, int slice, int nt, int ld, const float2* __restrict__ twg,
+                                                 __nv_bfloat16* __restrict__ b2, int na, int ncol, int k2ext) {
   extern __shared__ float2 fsm[];
   float2* tw = fsm;
   float2* buf = fsm + 3 * OCN_MAX_KDIM;
   for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
   __syncthreads();
-  // blockIdx.y: which slice of nt transforms (of ld per x-point) this CTA owns
-  kmesh_convolve_cube<float, N, NTC>(phi + (size_t)blockIdx.y * nt, W, nx, blockIdx.x, nt, ld, buf, tw);
+  const int t0 = slice * (NTC ? NTC : nt);
+  kmesh_cube_transform<float, N, NTC>(phi + t0, W, nx, x, nt, ld, buf, tw);
+  constexpr int P3 = N + 1;
+  constexpr int SLAB = cube_slab<float2>(N);
+  const auto get = [&](int t, int k) { return buf[t * SLAB + (k / N) * P3 + k % N]; };
+  store_b2_rows(get, 1.0f / (float)(N * N * N), b2, N * N * N, x, na, t0, NTC ? NTC : nt, ncol, k2ext);
 }
-typedef void (*CubeFnF)(float2*, const float*, int, int, int, const float2*);
+template <int N, int NTC>
+__global__ void k_fft_b2_cube(const float2* __restrict__ phi, const float* __restrict__ W, int nx, int nt, int ld,
+                              const float2* __restrict__ twg, __nv_bfloat16* __restrict__ b2, int na, int ncol,
+                              int k2ext) {
+  fft_b2_cube_body<N, NTC>(phi, W, nx, blockIdx.x, blockIdx.y, nt, ld, twg, b2, na, ncol, k2ext);
+}
+typedef void (*CubeFnB2)(const float2*, const float*, int, int, int, const float2*, __nv_bfloat16*, int, int, int);
 
+// The transforms of several contexts of one instantiation class (mesh, slice
+// size) in one launch.
 struct FftGroupArgs {
-  float2* phi;
+  const float2* phi;
   const float* W;
   int nx, nt, ld;  // x-points, transforms per CTA, transforms per x-point
   const float2* tw;
+  __nv_bfloat16* b2;
+  int na, ncol, k2ext;
   int cta0;        // first CTA of this context; its CTAs are (slice, x) = divmod(local, nx)
 };
 template <int N, int NTC>
-__global__ void k_fft_cube_f32_group(const FftGroupArgs* __restrict__ tab, int n) {
+__global__ void k_fft_b2_cube_group(const FftGroupArgs* __restrict__ tab, int n) {
   const FftGroupArgs& a = tab[group_find(tab, n, blockIdx.x)];
   const int local = blockIdx.x - a.cta0;
-  const int x = local % a.nx, slice = local / a.nx;
-  extern __shared__ float2 fsm[];
-  float2* tw = fsm;
-  float2* buf = fsm + 3 * OCN_MAX_KDIM;
-  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = a.tw[i];
-  __syncthreads();
-  kmesh_convolve_cube<float, N, NTC>(a.phi + (size_t)slice * a.nt, a.W, a.nx, x, a.nt, a.ld, buf, tw);
+  fft_b2_cube_body<N, NTC>(a.phi, a.W, a.nx, local % a.nx, local / a.nx, a.nt, a.ld, a.tw, a.b2, a.na, a.ncol,
+                           a.k2ext);
 }
-typedef void (*CubeFnGroupF)(const FftGroupArgs*, int);
+typedef void (*CubeFnB2Group)(const FftGroupArgs*, int);
 
 __global__ void k_w_to_f32(const double* __restrict__ W, float* __restrict__ Wf, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -861,7 +908,8 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
 }  // namespace
 
 struct MixedLR {
-  int p1 = 0, p2 = 0, ncol = 0, nvmax = 1;
+  int p1 = 0, ncol = 0, nvmax = 1;
+  int p2 = 0;  // K2 extent of UB rows and B2: 128 per 64-x block
   __nv_bfloat16 *ua_hi = nullptr, *ua_lo = nullptr, *ub_hi = nullptr, *ub_lo = nullptr;
   __nv_bfloat16 *b1 = nullptr, *b2 = nullptr;
   float2* phi = nullptr;
@@ -872,7 +920,7 @@ struct MixedLR {
   TcParams g1{}, g2{};
   int grid1 = 1, grid2 = 1;
   size_t smem_bytes = 0;
-  bool cube = false;        // cubic k-mesh: k_fft_cube_f32 instantiations apply
+  bool cube = false;        // cubic k-mesh: k_fft_b2_cube instantiations apply
   size_t stage_bytes = 0;   // shared memory of one pipeline stage
   int max_stages = 1;       // deepest pipeline that fits the shared-memory budget
   int cfg[7] = {0, 0, 0, 0, 0, 0, 0};  // stages, GEMM2 K splits (requested), grid caps of GEMM1 / GEMM2,
@@ -918,6 +966,20 @@ int encode3d(ocn_ctx* c, EncodeTiledFn fn, CUtensorMap* m, void* base, uint64_t 
   return OCN_OK;
 }
 
+// B2[k][K2][col] as 16-column by 64-row boxes with 32-byte swizzling (MN-major B)
+int encode_b_mn(ocn_ctx* c, EncodeTiledFn fn, CUtensorMap* m, void* base, uint64_t ncol, uint64_t rows,
+                uint64_t outer) {
+  const cuuint64_t dims[3] = {ncol, rows, outer};
+  const cuuint64_t strides[2] = {ncol * 2, ncol * 2 * rows};
+  const cuuint32_t box[3] = {16, (cuuint32_t)TC_BK, 1};
+  const cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_err(c, OCN_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return OCN_OK;
+}
+
 template <typename T>
 int alloc(ocn_ctx* c, T** p, size_t n) {
   cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
@@ -928,10 +990,12 @@ int alloc(ocn_ctx* c, T** p, size_t n) {
 }  // namespace
 
 // Transforms per CTA of the cubic k-mesh step for ntot = Na * nv transforms:
-// the configured count when it divides ntot, else all of them; reduced to one
-// vector's Na (which always divides ntot) when that would not fit in shared memory.
+// the configured count when it is a whole number of vectors (a multiple of Na
+// dividing ntot: a CTA writes whole B2 column blocks), else all of them; reduced
+// to one vector's Na when that would not fit in shared memory.
 int cube_tc(const MixedLR* m, int kn, int na, int ntot) {
-  int tc = (m->cfg[4] > 0 && ntot % m->cfg[4] == 0) ? m->cfg[4] : ntot;
+  const int q = m->cfg[4];
+  int tc = (q > 0 && q % na == 0 && ntot % q == 0) ? q : ntot;
   if (kmesh_cube_smem<float>(kn, tc) > 227u * 1024u) tc = na;
   return tc;
 }
@@ -953,7 +1017,8 @@ int mixed_init(ocn_ctx* c) {
   m->nvmax = nvmax;
   m->ncol = ncol;
   m->p1 = (2 * nb + 7) / 8 * 8;
-  m->p2 = (2 * nx + 7) / 8 * 8;
+  const int nxc = (nx + TC_BK - 1) / TC_BK;  // 64-x blocks
+  m->p2 = 2 * nxc * TC_BK;
   int rc;
   // u2 operands of both valence spins, spin-major: spin s at outer index s*Nk + k
   if ((rc = alloc(c, &m->ua_hi, (size_t)ns * nk * nx * m->p1)) ||
@@ -968,6 +1033,9 @@ int mixed_init(ocn_ctx* c) {
   // operand rows of vectors outside the current block keep finite (zero) values
   OCN_CUDA(c, cudaMemset(m->b1, 0, (size_t)nk * ncol * m->p1 * 2));
   OCN_CUDA(c, cudaMemset(m->b2, 0, (size_t)nk * ncol * m->p2 * 2));
+  // the padding of a partial last 64-x block stays zero
+  OCN_CUDA(c, cudaMemset(m->ub_hi, 0, (size_t)ns * nk * nb * m->p2 * 2));
+  OCN_CUDA(c, cudaMemset(m->ub_lo, 0, (size_t)ns * nk * nb * m->p2 * 2));
 
   void* fnp = nullptr;
   cudaDriverEntryPointQueryResult q;
@@ -977,9 +1045,9 @@ int mixed_init(ocn_ctx* c) {
   if ((rc = encode3d(c, fn, &m->tm_ua_hi, m->ua_hi, 2 * nb, nx, (uint64_t)ns * nk, m->p1, TC_BM)) ||
       (rc = encode3d(c, fn, &m->tm_ua_lo, m->ua_lo, 2 * nb, nx, (uint64_t)ns * nk, m->p1, TC_BM)) ||
       (rc = encode3d(c, fn, &m->tm_b1, m->b1, 2 * nb, ncol, nk, m->p1, ncol)) ||
-      (rc = encode3d(c, fn, &m->tm_ub_hi, m->ub_hi, 2 * nx, nb, (uint64_t)ns * nk, m->p2, TC_BM)) ||
-      (rc = encode3d(c, fn, &m->tm_ub_lo, m->ub_lo, 2 * nx, nb, (uint64_t)ns * nk, m->p2, TC_BM)) ||
-      (rc = encode3d(c, fn, &m->tm_b2, m->b2, 2 * nx, ncol, nk, m->p2, ncol)))
+      (rc = encode3d(c, fn, &m->tm_ub_hi, m->ub_hi, m->p2, nb, (uint64_t)ns * nk, m->p2, TC_BM)) ||
+      (rc = encode3d(c, fn, &m->tm_ub_lo, m->ub_lo, m->p2, nb, (uint64_t)ns * nk, m->p2, TC_BM)) ||
+      (rc = encode_b_mn(c, fn, &m->tm_b2, m->b2, ncol, m->p2, nk)))
     return rc;
 
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(ncol >> 3) << 17) |
@@ -1009,8 +1077,10 @@ int mixed_init(ocn_ctx* c) {
   TcParams& g2 = m->g2;
   g2 = g1;
   g2.mode = 2;
-  g2.nch = (2 * nx + TC_BK - 1) / TC_BK;
+  g2.nch = 2 * nxc;
   g2.mt2 = (nb + TC_BM - 1) / TC_BM;
+  g2.bmn = 1;
+  g2.idesc = idesc | (1u << 16);  // B MN-major
   m->stage_bytes = stage_bytes;
   m->max_stages = stages;
   c->part_stride = (size_t)nvmax * 2 * c->npsi;
@@ -1027,12 +1097,12 @@ int mixed_init(ocn_ctx* c) {
   const int cfg[7] = {st_def, ks, c->sm_count, c->sm_count, 0, 256, nvmax > 1 ? 1 : 0};
   if ((rc = mixed_configure(c, cfg))) return rc;
   if (int rc_ = allow_max_smem(c, k_lr_tc)) return rc_;
-  if (int rc_ = allow_max_smem(c, k_lr_fft_w_f32)) return rc_;
+  if (int rc_ = allow_max_smem(c, k_fft_b2)) return rc_;
   if (cube) {
     // the three instantiations a call can select (nt = 4, 12, other)
     for (int nt : {4, 12, 1}) {
-      CubeFnF f;
-      OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], nt, f);
+      CubeFnB2 f;
+      OCN_CUBE_DISPATCH(k_fft_b2_cube, c->dims.kmesh[0], nt, f);
       if (int rc_ = allow_max_smem(c, f)) return rc_;
     }
     m->cube = true;
@@ -1079,9 +1149,9 @@ int mixed_configure(ocn_ctx* c, const int cfg[7]) {
     c->d_accpart = np;
     m->part_cap = need;
   }
-  g2.part = c->d_accpart;
+  g2.part = reinterpret_cast<float*>(c->d_accpart);
   c->lr_xsplit = g2.ks2;
-  m->gm2.part = c->d_accpart + (size_t)g2.ks2 * c->part_stride;
+  m->gm2.part = reinterpret_cast<float*>(c->d_accpart) + (size_t)g2.ks2 * c->part_stride;
   m->smem_bytes = 1024 + (size_t)cfg[0] * m->stage_bytes + 256;
   {  // band->x outputs staged for coalesced stores when the pipeline leaves room
     const size_t eb = estg_bytes(m->ncol);
@@ -1248,6 +1318,8 @@ int mixed_set_mult(ocn_ctx* c) {
   b.ks2 = 1;
   b.ntiles = nk * b.mt2;
   b.bshared = 1;
+  b.bmn = 0;  // B3 is K-major
+  b.idesc = m->g1.idesc;
   c->mult_parts = 1;
   if ((rc = mixed_configure(c, m->cfg))) return rc;  // partial-sum room, multiplet grids
   OCN_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1353,7 +1425,7 @@ int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rst
                     double* rb, size_t cstride, const int* itp) {
   MixedLR* m = c->mixed;  // timed as part of the enclosing Lanczos step
   dim3 grid(nblk, nv);
-  k_norm_prep<<<grid, LZ_THREADS, 0, c->stream>>>(red2, nblk, rstride, h, 2 * c->npsi, c->npsi, c->d_allow, m->b1,
+  k_norm_prep<<<grid, LZ_THREADS, 0, c->stream>>>(red2, nblk, rstride, h, 2 * c->npsi, c->npsi, c->d_allow_f, m->b1,
                                            c->nb, c->nk, c->na, m->ncol, m->p1, rb, cstride, itp);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
@@ -1394,28 +1466,20 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
     }
   }
   {
-    TimedScope ts(c, T_LR_FFT);
+    TimedScope ts(c, T_LR_FFT);  // the k-mesh transform writes the x -> band operand B2 directly
     if (m->cube) {
       // transforms per CTA: all of the x-point, or a slice (tile parameter 5)
       const int ntot = na * nv;
       const int tc = cube_tc(m, c->dims.kmesh[0], na, ntot);
-      CubeFnF f;
-      OCN_CUBE_DISPATCH(k_fft_cube_f32, c->dims.kmesh[0], tc, f);
+      CubeFnB2 f;
+      OCN_CUBE_DISPATCH(k_fft_b2_cube, c->dims.kmesh[0], tc, f);
       const int th = m->cfg[5] ? m->cfg[5] : 128;
-      f<<<dim3(nx, ntot / tc), th, kmesh_cube_smem<float>(c->dims.kmesh[0], tc), c->stream>>>(m->phi, m->Wf, nx, tc,
-                                                                                             ntot, m->twf);
+      f<<<dim3(nx, ntot / tc), th, kmesh_cube_smem<float>(c->dims.kmesh[0], tc), c->stream>>>(
+          m->phi, m->Wf, nx, tc, ntot, m->twf, m->b2, na, m->ncol, m->p2);
     } else {
       const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na * nv);
-      k_lr_fft_w_f32<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g, m->twf);
+      k_fft_b2<<<nx, 256, kmesh_smem(g), c->stream>>>(m->phi, m->Wf, nx, g, m->twf, m->b2, na, m->ncol, m->p2);
     }
-    ++c->launches;
-    OCN_CUDA(c, cudaGetLastError());
-  }
-  {
-    TimedScope ts(c, T_LR_PREP);
-    const int total = nk * nx;
-    k_prep_b2<<<std::min((total + 255) / 256, 8 * c->sm_count), 256, 0, c->stream>>>(m->phi, m->b2, nk, nx,
-                                                                                       na, nv, m->ncol, m->p2);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
   }
@@ -1443,18 +1507,16 @@ struct LrGroup {
     int ninst = 0, grid = 0;
     size_t smem = 0;
   };
+  std::vector<TcLaunch> g1, g2;
+  // k-mesh transforms with B2 out, one launch per instantiation class
   struct FftClass {
-    CubeFnGroupF f = nullptr;
-    int kn = 0, tc = 0, th = 0;
+    CubeFnB2Group f = nullptr;
+    int kn = 0, tc = 0, th = 0, nctas = 0;
     size_t smem = 0;
     std::vector<FftGroupArgs> h;
     FftGroupArgs* d = nullptr;
-    int nctas = 0;
   };
-  std::vector<TcLaunch> g1, g2;
   std::vector<FftClass> fft;
-  B2GroupArgs* d_b2 = nullptr;
-  int b2ctas = 0;
   NormGroupArgs* d_norm[3] = {nullptr, nullptr, nullptr};
   int n = 0, nvmax = 1, nblk = 0;
 };
@@ -1478,7 +1540,6 @@ void lr_group_destroy(LrGroup* g) {
     }
   for (auto& f : g->fft)
     if (f.d) cudaFree(f.d);
-  if (g->d_b2) cudaFree(g->d_b2);
   for (int r = 0; r < 3; ++r)
     if (g->d_norm[r]) cudaFree(g->d_norm[r]);
   delete g;
@@ -1567,7 +1628,7 @@ int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out) {
       if ((rc = upload(c0, &L.d_tab, tab)) == OCN_OK) rc = upload(c0, &L.d_tile0, tile0);
     }
   }
-  // k-mesh transforms, by instantiation class
+  // k-mesh transforms with the B2 rows out: one launch for every context
   for (size_t i = 0; i < mem.size() && rc == OCN_OK; ++i) {
     ocn_ctx* c = mem[i].c;
     const MixedLR* m = c->mixed;
@@ -1585,29 +1646,15 @@ int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out) {
       cls->tc = tc;
       cls->th = th;
       cls->smem = kmesh_cube_smem<float>(kn, tc);
-      OCN_CUBE_DISPATCH(k_fft_cube_f32_group, kn, tc, cls->f);
+      OCN_CUBE_DISPATCH(k_fft_b2_cube_group, kn, tc, cls->f);
       if (!cls->f) rc = set_err(c0, OCN_ERR_UNSUPPORTED, "no cubic transform for this k-mesh");
       else rc = allow_max_smem(c0, cls->f);
     }
-    FftGroupArgs a{m->phi, m->Wf, c->nx, tc, ntot, m->twf, cls->nctas};
-    cls->h.push_back(a);
+    cls->h.push_back(FftGroupArgs{m->phi, m->Wf, c->nx, tc, ntot, m->twf, m->b2, c->na, m->ncol, m->p2, cls->nctas});
     cls->nctas += c->nx * (ntot / tc);
   }
   for (auto& f : g->fft)
     if (rc == OCN_OK) rc = upload(c0, &f.d, f.h);
-  // phi' -> split-BF16 operand of the x->band contraction
-  if (rc == OCN_OK) {
-    std::vector<B2GroupArgs> b2;
-    for (const BatchMember& b : mem) {
-      const ocn_ctx* c = b.c;
-      const MixedLR* m = c->mixed;
-      const int total = c->nk * c->nx;
-      const int ctas = std::min((total + 255) / 256, 8 * c->sm_count);
-      b2.push_back(B2GroupArgs{m->phi, m->b2, c->nk, c->nx, c->na, b.nv, m->ncol, m->p2, g->b2ctas, ctas});
-      g->b2ctas += ctas;
-    }
-    rc = upload(c0, &g->d_b2, b2);
-  }
   // normalisation + next psi operand, per buffer rotation
   for (int r = 0; r < 3 && rc == OCN_OK; ++r) {
     std::vector<NormGroupArgs> nt;
@@ -1621,7 +1668,7 @@ int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out) {
       a.hbase = b.buf[(r + 2) % 3];
       a.vstride = 2 * c->npsi;
       a.npsi = c->npsi;
-      a.allow = c->d_allow;
+      a.allow = c->d_allow_f;
       a.b1 = m->b1;
       a.nb = c->nb;
       a.nk = c->nk;
@@ -1645,13 +1692,12 @@ int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out) {
 }
 
 // Kernels one lr_group_apply + lr_group_norm launch.
-int lr_group_launches(const LrGroup* g) { return (int)(g->g1.size() + g->g2.size() + g->fft.size()) + 2; }
+int lr_group_launches(const LrGroup* g) { return (int)(g->g1.size() + g->g2.size() + g->fft.size()) + 1; }
 
 int lr_group_apply(LrGroup* g, cudaStream_t s) {
   for (auto& L : g->g1)
     k_lr_tc_group<<<L.grid, TC_THREADS, L.smem, s>>>(L.maps, L.p, L.d_tab, L.d_tile0, L.ninst);
   for (auto& f : g->fft) f.f<<<f.nctas, f.th, f.smem, s>>>(f.d, (int)f.h.size());
-  k_prep_b2_group<<<g->b2ctas, 256, 0, s>>>(g->d_b2, g->n);
   for (auto& L : g->g2)
     k_lr_tc_group<<<L.grid, TC_THREADS, L.smem, s>>>(L.maps, L.p, L.d_tab, L.d_tile0, L.ninst);
   return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
