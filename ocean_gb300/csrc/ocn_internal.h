@@ -14,6 +14,7 @@
 #define OCN_MAX_KDIM 32     // largest k-mesh extent along one axis handled by the FFT kernels
 #define OCN_MAX_NK 4096     // largest k-mesh size (shared-memory FFT)
 #define LZ_THREADS 256      // threads of the Lanczos-step kernels
+#define LZ_DF_THREADS 512   // threads of the double-float (mixed-precision) Lanczos-step kernels
 
 namespace ocn {
 

@@ -496,7 +496,7 @@ __device__ __forceinline__ void combine_df_body(const float2* __restrict__ pr, c
 }
 
 template <int NA, bool SO>
-__global__ void __launch_bounds__(LZ_THREADS)
+__global__ void __launch_bounds__(LZ_DF_THREADS)
     k_combine_df(const float2* __restrict__ pr, const float2* __restrict__ pi, const float2* __restrict__ er,
                  const float2* __restrict__ ei, const float* __restrict__ allow, const float* __restrict__ part,
                  int nparts, const float2* __restrict__ so, float2* __restrict__ outr, float2* __restrict__ outi,
@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(LZ_THREADS)
 // contexts); every context keeps the block partition (and so the reduction
 // order) of its own launches.
 template <int NA, bool SO>
-__global__ void __launch_bounds__(LZ_THREADS) k_combine_df_group(const CombineArgs* __restrict__ tab) {
+__global__ void __launch_bounds__(LZ_DF_THREADS) k_combine_df_group(const CombineArgs* __restrict__ tab) {
   const CombineArgs& a = tab[blockIdx.z];
   if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
   combine_df_body<NA, SO>(reinterpret_cast<const float2*>(a.pr), reinterpret_cast<const float2*>(a.pi), a.er_df,
@@ -564,7 +564,7 @@ __device__ __forceinline__ void lanczos2_df_body(const float2* __restrict__ red1
   }
 }
 
-__global__ void __launch_bounds__(LZ_THREADS)
+__global__ void __launch_bounds__(LZ_DF_THREADS)
     k_lanczos2_df(const float2* __restrict__ red1, int nblk, float2* __restrict__ hr, float2* __restrict__ hi,
                   const float2* __restrict__ pr, const float2* __restrict__ pi, size_t n, float2* __restrict__ red2,
                   double* __restrict__ ra_base, double* __restrict__ ia_base, const int* __restrict__ itp,
@@ -573,7 +573,7 @@ __global__ void __launch_bounds__(LZ_THREADS)
                    gridDim.x);
 }
 
-__global__ void __launch_bounds__(LZ_THREADS) k_lanczos2_df_group(const Lanczos2Args* __restrict__ tab) {
+__global__ void __launch_bounds__(LZ_DF_THREADS) k_lanczos2_df_group(const Lanczos2Args* __restrict__ tab) {
   const Lanczos2Args& a = tab[blockIdx.z];
   if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
   lanczos2_df_body(reinterpret_cast<const float2*>(a.red1), a.nblk, reinterpret_cast<float2*>(a.hr),
@@ -1248,14 +1248,14 @@ int lanczos_launch(ocn_ctx* c, int nv, const double* old, const double* psi, dou
   if (mixed_parts(c)) {
     typedef const float2* cf2;
     auto kd = combine_df_kernel(c->na, use_so);
-    kd<<<grid, LZ_THREADS, 0, c->stream>>>(
+    kd<<<grid, LZ_DF_THREADS, 0, c->stream>>>(
         reinterpret_cast<cf2>(psi), reinterpret_cast<cf2>(psi + n), c->d_er_df, c->ei_nonzero ? c->d_ei_df : nullptr,
         c->d_allow_f, static_cast<const float*>(parts), nparts, c->d_so_f, reinterpret_cast<float2*>(h),
         reinterpret_cast<float2*>(h + n), nbk, n, c->sys.e0, reinterpret_cast<cf2>(old), reinterpret_cast<cf2>(old + n),
         rb, itp, reinterpret_cast<float2*>(c->d_red), bs);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
-    k_lanczos2_df<<<grid, LZ_THREADS, 0, c->stream>>>(
+    k_lanczos2_df<<<grid, LZ_DF_THREADS, 0, c->stream>>>(
         reinterpret_cast<cf2>(c->d_red), nblk, reinterpret_cast<float2*>(h), reinterpret_cast<float2*>(h + n),
         reinterpret_cast<cf2>(psi), reinterpret_cast<cf2>(psi + n), n, reinterpret_cast<float2*>(c->d_red + 2 * nblk),
         ra, ia, itp, bs);
@@ -1523,16 +1523,16 @@ int lz_group_step(LzGroup* g, int rot, cudaStream_t s) {
     const dim3 gc(g->nblk, g->nvmax, k.count);
     const CombineArgs* t = g->d_comb[rot] + k.first;
     if (k.na == 4) {
-      if (k.so) k_combine_df_group<4, true><<<gc, LZ_THREADS, 0, s>>>(t);
-      else k_combine_df_group<4, false><<<gc, LZ_THREADS, 0, s>>>(t);
+      if (k.so) k_combine_df_group<4, true><<<gc, LZ_DF_THREADS, 0, s>>>(t);
+      else k_combine_df_group<4, false><<<gc, LZ_DF_THREADS, 0, s>>>(t);
     } else {
-      if (k.so) k_combine_df_group<12, true><<<gc, LZ_THREADS, 0, s>>>(t);
-      else k_combine_df_group<12, false><<<gc, LZ_THREADS, 0, s>>>(t);
+      if (k.so) k_combine_df_group<12, true><<<gc, LZ_DF_THREADS, 0, s>>>(t);
+      else k_combine_df_group<12, false><<<gc, LZ_DF_THREADS, 0, s>>>(t);
     }
     if (cudaGetLastError() != cudaSuccess) return OCN_ERR_CUDA;
   }
   const dim3 grid(g->nblk, g->nvmax, g->n);
-  k_lanczos2_df_group<<<grid, LZ_THREADS, 0, s>>>(g->d_lz2[rot]);
+  k_lanczos2_df_group<<<grid, LZ_DF_THREADS, 0, s>>>(g->d_lz2[rot]);
   return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
 }
 

@@ -744,7 +744,7 @@ __device__ __forceinline__ void norm_prep_body(const double* __restrict__ red2, 
   }
 }
 
-__global__ void __launch_bounds__(LZ_THREADS)
+__global__ void __launch_bounds__(LZ_DF_THREADS)
     k_norm_prep(const double* __restrict__ red2, int nblk, size_t rstride, double* __restrict__ hbase,
                 size_t vstride, size_t npsi, const float* __restrict__ allow, __nv_bfloat16* __restrict__ b1,
                 int nb, int nk, int na, int ncol, int p1, double* __restrict__ rb_base, size_t cstride,
@@ -768,7 +768,7 @@ struct NormGroupArgs {
   int nv;
 };
 // grid (blocks per context, largest block of vectors, contexts)
-__global__ void __launch_bounds__(LZ_THREADS) k_norm_prep_group(const NormGroupArgs* __restrict__ tab) {
+__global__ void __launch_bounds__(LZ_DF_THREADS) k_norm_prep_group(const NormGroupArgs* __restrict__ tab) {
   const NormGroupArgs& a = tab[blockIdx.z];
   if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
   norm_prep_body(a.red2, a.nblk, a.rstride, a.hbase, a.vstride, a.npsi, a.allow, a.b1, a.nb, a.nk, a.na, a.ncol,
@@ -795,7 +795,59 @@ __device__ __forceinline__ int group_find(const A* __restrict__ tab, int n, int 
 // with s = 0 / 1 the high / low BF16 half.  The CTA holds transforms t0 .. t0+nt-1
 // of its x-point (nt a multiple of Na, so whole vectors); get(t, k) = Nk phi'(k).
 // One thread per (k, c, vector) writes the vector's 4 Na columns (8 Na bytes).
+// One vector's 4 NA columns of row (k, c), transforms tb .. tb+NA-1: built in
+// registers, stored as NA/2 16-byte words.
+template <int NA, class Get>
+__device__ __forceinline__ void b2_row(const Get& get, float norm, __nv_bfloat16* __restrict__ dst, int tb, int k,
+                                       int c) {
+  uint32_t pk[2 * NA];  // column j = s*2NA + part*NA + a in half j%2 of pk[j/2]
+#pragma unroll
+  for (int a = 0; a < NA; a += 2) {
+    __nv_bfloat16 h[2][2], l[2][2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const float2 f = get(tb + a + q, k);
+      const float re = f.x * norm, im = f.y * norm;
+      split_bf16(c == 0 ? re : im, h[0][q], l[0][q]);
+      split_bf16(c == 0 ? im : -re, h[1][q], l[1][q]);
+    }
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+      pk[(part * NA + a) / 2] = pack_bf16(h[part][0], h[part][1]);
+      pk[(2 * NA + part * NA + a) / 2] = pack_bf16(l[part][0], l[part][1]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NA / 2; ++q)
+    reinterpret_cast<uint4*>(dst)[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+}
+
+// Any Na (a multiple of 4): runs of 4 BF16 per (s, part, 4 alphas).
 template <class Get>
+__device__ __forceinline__ void b2_row_any(const Get& get, float norm, __nv_bfloat16* __restrict__ dst, int tb,
+                                           int na, int k, int c) {
+  for (int a0 = 0; a0 < na; a0 += 4) {
+    __nv_bfloat16 h[2][4], l[2][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float2 f = get(tb + a0 + q, k);
+      const float re = f.x * norm, im = f.y * norm;
+      split_bf16(c == 0 ? re : im, h[0][q], l[0][q]);
+      split_bf16(c == 0 ? im : -re, h[1][q], l[1][q]);
+    }
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+      *reinterpret_cast<uint2*>(dst + part * na + a0) =
+          make_uint2(pack_bf16(h[part][0], h[part][1]), pack_bf16(h[part][2], h[part][3]));
+      *reinterpret_cast<uint2*>(dst + 2 * na + part * na + a0) =
+          make_uint2(pack_bf16(l[part][0], l[part][1]), pack_bf16(l[part][2], l[part][3]));
+    }
+  }
+}
+
+// NTC: transforms per CTA when known at compile time (a multiple of Na), which
+// bounds the Na the kernel instantiation can meet (and so its registers).
+template <int NTC, class Get>
 __device__ __forceinline__ void store_b2_rows(const Get& get, float norm, __nv_bfloat16* __restrict__ b2, int nk,
                                               int x, int na, int t0, int nt, int ncol, int k2ext) {
   const int nvl = nt / na, v0 = t0 / na;
@@ -806,33 +858,9 @@ __device__ __forceinline__ void store_b2_rows(const Get& get, float norm, __nv_b
     const int c = (e / nvl) & 1;
     const int k = e / (2 * nvl);
     __nv_bfloat16* dst = b2 + ((size_t)k * k2ext + row_x + 64 * c) * ncol + (size_t)(v0 + vl) * 4 * na;
-    for (int a0 = 0; a0 < na; a0 += 4) {
-      // columns (s, part, a0..a0+3): four runs of 4 BF16
-      __nv_bfloat16 h[2][4], l[2][4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float2 f = get(vl * na + a0 + q, k);
-        const float re = f.x * norm, im = f.y * norm;
-        split_bf16(c == 0 ? re : im, h[0][q], l[0][q]);
-        split_bf16(c == 0 ? im : -re, h[1][q], l[1][q]);
-      }
-      uint2 w[2][2];
-#pragma unroll
-      for (int part = 0; part < 2; ++part) {
-        w[0][part] = make_uint2(pack_bf16(h[part][0], h[part][1]), pack_bf16(h[part][2], h[part][3]));
-        w[1][part] = make_uint2(pack_bf16(l[part][0], l[part][1]), pack_bf16(l[part][2], l[part][3]));
-      }
-      if (na == 4) {  // (s, 0) and (s, 1) adjacent: one 16-byte store per half
-        *reinterpret_cast<uint4*>(dst) = make_uint4(w[0][0].x, w[0][0].y, w[0][1].x, w[0][1].y);
-        *reinterpret_cast<uint4*>(dst + 8) = make_uint4(w[1][0].x, w[1][0].y, w[1][1].x, w[1][1].y);
-      } else {
-#pragma unroll
-        for (int sp = 0; sp < 2; ++sp)
-#pragma unroll
-          for (int part = 0; part < 2; ++part)
-            *reinterpret_cast<uint2*>(dst + sp * 2 * na + part * na + a0) = w[sp][part];
-      }
-    }
+    if (NTC == 4 || na == 4) b2_row<4>(get, norm, dst, vl * na, k, c);
+    else if (na == 12) b2_row<12>(get, norm, dst, vl * na, k, c);
+    else b2_row_any(get, norm, dst, vl * na, na, k, c);
   }
 }
 
@@ -847,25 +875,142 @@ __global__ void k_fft_b2(const float2* __restrict__ phi, const float* __restrict
   __syncthreads();
   kmesh_transform<float>(phi, W, nx, blockIdx.x, g, buf, tw);
   const auto get = [&](int t, int k) { return buf[t * g.slab + kpad(g, k)]; };
-  store_b2_rows(get, 1.0f / (float)g.nk, b2, g.nk, blockIdx.x, na, 0, g.na, ncol, k2ext);
+  store_b2_rows<0>(get, 1.0f / (float)g.nk, b2, g.nk, blockIdx.x, na, 0, g.na, ncol, k2ext);
 }
 
 // cubic meshes: nt transforms (a slice of the ld of the x-point) per CTA
+// Cubic k-mesh transform of the nt transforms (a multiple of 4) of x-point x
+// owned by this CTA, B2 rows out, in five phases over shared memory (four
+// barriers):
+//   A  per (k2, k3, group of 4 transforms): the N values along k1 of each, read
+//      from phi as 32-byte rows (a k-point's 4 transforms are adjacent), backward
+//      DFT along k1, into the padded planes;
+//   B  backward DFT along k2;
+//   C  backward DFT along k3, x W(x, k), forward DFT along k3 (one line in registers);
+//   D  forward DFT along k2;
+//   E  per (k2, k3, group of 4): forward DFT along k1 in registers, / Nk, and the
+//      B2 columns of the 4 transforms for the N k-points of the line.
+// The same separable transform as kmesh_cube_transform (backward = +i), with the
+// W pass and the first / last passes fused.
+template <int N>
+__host__ __device__ constexpr size_t fft_b2_smem_elems(int nt) {
+  return 3 * OCN_MAX_KDIM + (N * N * N + 1) / 2 + (size_t)nt * cube_slab<float2>(N);
+}
+inline size_t fft_b2_smem(int n, int nt) {
+  switch (n) {
+    case 2: return sizeof(float2) * fft_b2_smem_elems<2>(nt);
+    case 3: return sizeof(float2) * fft_b2_smem_elems<3>(nt);
+    case 4: return sizeof(float2) * fft_b2_smem_elems<4>(nt);
+    case 5: return sizeof(float2) * fft_b2_smem_elems<5>(nt);
+    case 6: return sizeof(float2) * fft_b2_smem_elems<6>(nt);
+    default: return sizeof(float2) * fft_b2_smem_elems<8>(nt);
+  }
+}
+
 template <int N, int NTC>
 __device__ __forceinline__ void fft_b2_cube_body(const float2* __restrict__ phi, const float* __restrict__ W, int nx,
-                                                 int x, int slice, int nt, int ld, const float2* __restrict__ twg,
+                                                 int x, int slice, int nt_rt, int ld, const float2* __restrict__ twg,
                                                  __nv_bfloat16* __restrict__ b2, int na, int ncol, int k2ext) {
-  extern __shared__ float2 fsm[];
-  float2* tw = fsm;
-  float2* buf = fsm + 3 * OCN_MAX_KDIM;
-  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
-  __syncthreads();
-  const int t0 = slice * (NTC ? NTC : nt);
-  kmesh_cube_transform<float, N, NTC>(phi + t0, W, nx, x, nt, ld, buf, tw);
-  constexpr int P3 = N + 1;
+  constexpr int N2 = N * N, NK = N * N * N, P3 = N + 1;
   constexpr int SLAB = cube_slab<float2>(N);
-  const auto get = [&](int t, int k) { return buf[t * SLAB + (k / N) * P3 + k % N]; };
-  store_b2_rows(get, 1.0f / (float)(N * N * N), b2, N * N * N, x, na, t0, NTC ? NTC : nt, ncol, k2ext);
+  const int nt = NTC ? NTC : nt_rt;
+  extern __shared__ float2 fsm[];
+  float2* tw = fsm;                                               // [axis][t]
+  float* ws = reinterpret_cast<float*>(fsm + 3 * OCN_MAX_KDIM);  // W(x, k)
+  float2* buf = fsm + 3 * OCN_MAX_KDIM + (NK + 1) / 2;
+  for (int i = threadIdx.x; i < 3 * OCN_MAX_KDIM; i += blockDim.x) tw[i] = twg[i];
+  for (int i = threadIdx.x; i < NK; i += blockDim.x) ws[i] = W[(size_t)x * NK + i];
+  __syncthreads();
+  const int t0 = slice * nt;
+  // line tasks (r = k2*N + k3, t) with t fastest: the 4 lanes of a group hold the
+  // 4 transforms t = 4g .. 4g+3 of one (k2, k3) line
+  const int tasks = N2 * nt;
+  // A: load + backward DFT along k1
+  for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+    const int r = task / nt, t = task - r * nt;
+    float2 v[N];
+#pragma unroll
+    for (int k1 = 0; k1 < N; ++k1) v[k1] = phi[((size_t)(k1 * N2 + r) * nx + x) * ld + t0 + t];
+    line_dft<float2, float, N>(v, tw, 1.0f);
+    float2* dst = buf + t * SLAB + (r / N) * P3 + r % N;
+#pragma unroll
+    for (int k1 = 0; k1 < N; ++k1) dst[k1 * N * P3] = v[k1];
+  }
+  __syncthreads();
+  // B: backward along k2
+  cube_pass<float, N, NTC>(buf, nt, 1, tw + OCN_MAX_KDIM, 1.0f);
+  __syncthreads();
+  // C: along k3: backward, x W, forward
+  for (int l = threadIdx.x; l < nt * N2; l += blockDim.x) {
+    const int t = l / N2, r = l - t * N2;  // r = k1*N + k2
+    float2* p = buf + t * SLAB + r * P3;
+    float2 v[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) v[j] = p[j];
+    line_dft<float2, float, N>(v, tw + 2 * OCN_MAX_KDIM, 1.0f);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const float wv = ws[r * N + j];
+      v[j].x *= wv;
+      v[j].y *= wv;
+    }
+    line_dft<float2, float, N>(v, tw + 2 * OCN_MAX_KDIM, -1.0f);
+#pragma unroll
+    for (int j = 0; j < N; ++j) p[j] = v[j];
+  }
+  __syncthreads();
+  // D: forward along k2
+  cube_pass<float, N, NTC>(buf, nt, 1, tw + OCN_MAX_KDIM, -1.0f);
+  __syncthreads();
+  // E: forward along k1 and the B2 columns.  Lane q of a group of 4 writes word q
+  // = (split s, part) = (q / 2, q % 2) of the group's 4 alphas: for Na = 4 the 4
+  // lanes write one 32-byte row segment.  Every lane of the warp takes part in
+  // the shuffles (tasks is a multiple of 4; idle lanes carry zeros).
+  const float norm = 1.0f / (float)NK;
+  const int row_x = ((x >> 6) << 7) + (x & 63);
+  const int lane = threadIdx.x & 31, q = lane & 3, s = q >> 1, part = q & 1;
+  for (int base = 0; base < tasks; base += blockDim.x) {
+    const int task = base + threadIdx.x;
+    const bool on = task < tasks;
+    const int r = on ? task / nt : 0, t = on ? task - r * nt : 0;
+    float2 v[N];
+    if (on) {
+      const float2* src = buf + t * SLAB + (r / N) * P3 + r % N;
+#pragma unroll
+      for (int k1 = 0; k1 < N; ++k1) v[k1] = src[k1 * N * P3];
+      line_dft<float2, float, N>(v, tw, -1.0f);
+    } else {
+#pragma unroll
+      for (int k1 = 0; k1 < N; ++k1) v[k1] = make_float2(0.0f, 0.0f);
+    }
+    const int tg = t0 + (t & ~3), vv = tg / na, a0 = tg - vv * na;
+    __nv_bfloat16* col = b2 + (size_t)vv * 4 * na + s * 2 * na + part * na + a0;
+#pragma unroll
+    for (int k1 = 0; k1 < N; ++k1) {
+      float2 f[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        f[j].x = __shfl_sync(0xffffffffu, v[k1].x, (lane & ~3) + j);
+        f[j].y = __shfl_sync(0xffffffffu, v[k1].y, (lane & ~3) + j);
+      }
+      if (!on) continue;
+      const size_t k = (size_t)k1 * N2 + r;
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        __nv_bfloat16 e[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float re = f[j].x * norm, im = f[j].y * norm;
+          const float val = part == 0 ? (c == 0 ? re : im) : (c == 0 ? im : -re);
+          __nv_bfloat16 hv, lv;
+          split_bf16(val, hv, lv);
+          e[j] = s == 0 ? hv : lv;
+        }
+        *reinterpret_cast<uint2*>(col + (k * k2ext + row_x + 64 * c) * ncol) =
+            make_uint2(pack_bf16(e[0], e[1]), pack_bf16(e[2], e[3]));
+      }
+    }
+  }
 }
 template <int N, int NTC>
 __global__ void k_fft_b2_cube(const float2* __restrict__ phi, const float* __restrict__ W, int nx, int nt, int ld,
@@ -996,7 +1141,7 @@ int alloc(ocn_ctx* c, T** p, size_t n) {
 int cube_tc(const MixedLR* m, int kn, int na, int ntot) {
   const int q = m->cfg[4];
   int tc = (q > 0 && q % na == 0 && ntot % q == 0) ? q : ntot;
-  if (kmesh_cube_smem<float>(kn, tc) > 227u * 1024u) tc = na;
+  if (fft_b2_smem(kn, tc) > 227u * 1024u) tc = na;
   return tc;
 }
 
@@ -1007,7 +1152,7 @@ int mixed_init(ocn_ctx* c) {
   if (ncol > TC_MAX_NCOL)
     return set_err(c, OCN_ERR_ARG, "nvec too large: 4*nalpha*nvec must be <= 256");
   const bool cube = kmesh_cube_supported(c->dims.kmesh);
-  const size_t fsm = cube ? kmesh_cube_smem<float>(c->dims.kmesh[0], na)
+  const size_t fsm = cube ? fft_b2_smem(c->dims.kmesh[0], na)
                           : kmesh_smem(kmesh_geom<float>(c->dims.kmesh, na * nvmax));
   if (fsm > 227u * 1024u)
     return set_err(c, OCN_ERR_ARG, "nvec*nalpha*Nk too large for the shared-memory k-mesh transform");
@@ -1425,7 +1570,7 @@ int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rst
                     double* rb, size_t cstride, const int* itp) {
   MixedLR* m = c->mixed;  // timed as part of the enclosing Lanczos step
   dim3 grid(nblk, nv);
-  k_norm_prep<<<grid, LZ_THREADS, 0, c->stream>>>(red2, nblk, rstride, h, 2 * c->npsi, c->npsi, c->d_allow_f, m->b1,
+  k_norm_prep<<<grid, LZ_DF_THREADS, 0, c->stream>>>(red2, nblk, rstride, h, 2 * c->npsi, c->npsi, c->d_allow_f, m->b1,
                                            c->nb, c->nk, c->na, m->ncol, m->p1, rb, cstride, itp);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
@@ -1474,7 +1619,7 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
       CubeFnB2 f;
       OCN_CUBE_DISPATCH(k_fft_b2_cube, c->dims.kmesh[0], tc, f);
       const int th = m->cfg[5] ? m->cfg[5] : 128;
-      f<<<dim3(nx, ntot / tc), th, kmesh_cube_smem<float>(c->dims.kmesh[0], tc), c->stream>>>(
+      f<<<dim3(nx, ntot / tc), th, fft_b2_smem(c->dims.kmesh[0], tc), c->stream>>>(
           m->phi, m->Wf, nx, tc, ntot, m->twf, m->b2, na, m->ncol, m->p2);
     } else {
       const KmeshGeom<float> g = kmesh_geom<float>(c->dims.kmesh, na * nv);
@@ -1645,7 +1790,7 @@ int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out) {
       cls->kn = kn;
       cls->tc = tc;
       cls->th = th;
-      cls->smem = kmesh_cube_smem<float>(kn, tc);
+      cls->smem = fft_b2_smem(kn, tc);
       OCN_CUBE_DISPATCH(k_fft_b2_cube_group, kn, tc, cls->f);
       if (!cls->f) rc = set_err(c0, OCN_ERR_UNSUPPORTED, "no cubic transform for this k-mesh");
       else rc = allow_max_smem(c0, cls->f);
@@ -1704,7 +1849,7 @@ int lr_group_apply(LrGroup* g, cudaStream_t s) {
 }
 
 int lr_group_norm(LrGroup* g, int rot, cudaStream_t s) {
-  k_norm_prep_group<<<dim3(g->nblk, g->nvmax, g->n), LZ_THREADS, 0, s>>>(g->d_norm[rot]);
+  k_norm_prep_group<<<dim3(g->nblk, g->nvmax, g->n), LZ_DF_THREADS, 0, s>>>(g->d_norm[rot]);
   return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
 }
 
