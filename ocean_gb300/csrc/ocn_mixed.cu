@@ -81,6 +81,7 @@ struct TcParams {
   int starve;    // launch-wide test hook: the producer issues no loads, so the MMA warp's
                  // first bounded wait runs out with nothing in flight (OCN_ERR_TIMEOUT path)
   int bmn;       // B is MN-major in SW32 boxes of 16 columns by 64 K rows (B2 of the x -> band contraction)
+  int achunk;    // A is stored chunk-major, [k][K chunk][row][64] (UB): every A box is one contiguous run
 };
 
 // Tensor maps of a group launch (kernel parameter space, 384 bytes per problem).
@@ -131,6 +132,15 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
       "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int c0, int c1,
+                                            int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5, %6}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
       : "memory");
 }
 
@@ -303,8 +313,13 @@ __device__ __forceinline__ void lr_tc_body(const TcParams& p, const Src& src) {
           }
           const uint32_t sbase = su32(smem + stage * stage_bytes);
           mbar_expect_tx(full0 + 8 * stage, 2 * a_bytes + (uint32_t)tp.ncol * TC_BK * 2);
-          tma_load_3d(sbase, src.map(ii, 0), full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + tp.koff);
-          tma_load_3d(sbase + a_bytes, src.map(ii, 1), full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + tp.koff);
+          if (tp.achunk) {  // (K in chunk, row, chunk, k)
+            tma_load_4d(sbase, src.map(ii, 0), full0 + 8 * stage, 0, ti.row0, c, ti.k + tp.koff);
+            tma_load_4d(sbase + a_bytes, src.map(ii, 1), full0 + 8 * stage, 0, ti.row0, c, ti.k + tp.koff);
+          } else {
+            tma_load_3d(sbase, src.map(ii, 0), full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + tp.koff);
+            tma_load_3d(sbase + a_bytes, src.map(ii, 1), full0 + 8 * stage, c * TC_BK, ti.row0, ti.k + tp.koff);
+          }
           if (tp.bmn) {
             for (int j = 0; j < tp.ncol / 16; ++j)
               tma_load_3d(sbase + 2 * a_bytes + j * 2048, src.map(ii, 2), full0 + 8 * stage, 16 * j, c * TC_BK, ti.k);
@@ -520,8 +535,9 @@ __global__ void k_build_ua(const double2* __restrict__ u, __nv_bfloat16* __restr
   }
 }
 
-// UB_s[k][n][K2]: K2 = (x/64)*128 + c*64 + x%64 -> Re u(n, x) (c = 0), Im u(n, x) (c = 1);
-// the padding of a partial last 64-x block is never written (zero since allocation)
+// UB_s[k][j][n][K2 % 64], chunk j = K2 / 64 with K2 = (x/64)*128 + c*64 + x%64 -> Re u(n, x)
+// (c = 0), Im u(n, x) (c = 1): chunk-major, so a 128-band x 64 box is contiguous.  The
+// padding of a partial last 64-x block is never written (zero since allocation).
 __global__ void k_build_ub(const double2* __restrict__ u, __nv_bfloat16* __restrict__ hi,
                            __nv_bfloat16* __restrict__ lo, int nb, int nk, int nx, int p2) {
   const long long total = (long long)nk * nb * 2 * nx;
@@ -536,7 +552,8 @@ __global__ void k_build_ub(const double2* __restrict__ u, __nv_bfloat16* __restr
     const float v = (float)(K < nx ? z.x : z.y);
     __nv_bfloat16 h, l;
     split_bf16(v, h, l);
-    const size_t o = ((size_t)k * nb + n) * p2 + ((x >> 6) << 7) + (K < nx ? 0 : 64) + (x & 63);
+    const int K2 = ((x >> 6) << 7) + (K < nx ? 0 : 64) + (x & 63);
+    const size_t o = (((size_t)k * (p2 >> 6) + (K2 >> 6)) * nb + n) * 64 + (K2 & 63);
     hi[o] = h;
     lo[o] = l;
   }
@@ -1111,6 +1128,22 @@ int encode3d(ocn_ctx* c, EncodeTiledFn fn, CUtensorMap* m, void* base, uint64_t 
   return OCN_OK;
 }
 
+// A stored chunk-major, [outer][chunk][row][64]: 64 x 128-row boxes with 128-byte
+// swizzling, each one contiguous run of memory
+int encode_a_chunked(ocn_ctx* c, EncodeTiledFn fn, CUtensorMap* m, void* base, uint64_t rows, uint64_t nchunk,
+                     uint64_t outer) {
+  const cuuint64_t dims[4] = {(cuuint64_t)TC_BK, rows, nchunk, outer};
+  const cuuint64_t strides[3] = {(cuuint64_t)TC_BK * 2, (cuuint64_t)TC_BK * 2 * rows,
+                                 (cuuint64_t)TC_BK * 2 * rows * nchunk};
+  const cuuint32_t box[4] = {(cuuint32_t)TC_BK, (cuuint32_t)TC_BM, 1, 1};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, base, dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_err(c, OCN_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return OCN_OK;
+}
+
 // B2[k][K2][col] as 16-column by 64-row boxes with 32-byte swizzling (MN-major B)
 int encode_b_mn(ocn_ctx* c, EncodeTiledFn fn, CUtensorMap* m, void* base, uint64_t ncol, uint64_t rows,
                 uint64_t outer) {
@@ -1190,8 +1223,8 @@ int mixed_init(ocn_ctx* c) {
   if ((rc = encode3d(c, fn, &m->tm_ua_hi, m->ua_hi, 2 * nb, nx, (uint64_t)ns * nk, m->p1, TC_BM)) ||
       (rc = encode3d(c, fn, &m->tm_ua_lo, m->ua_lo, 2 * nb, nx, (uint64_t)ns * nk, m->p1, TC_BM)) ||
       (rc = encode3d(c, fn, &m->tm_b1, m->b1, 2 * nb, ncol, nk, m->p1, ncol)) ||
-      (rc = encode3d(c, fn, &m->tm_ub_hi, m->ub_hi, m->p2, nb, (uint64_t)ns * nk, m->p2, TC_BM)) ||
-      (rc = encode3d(c, fn, &m->tm_ub_lo, m->ub_lo, m->p2, nb, (uint64_t)ns * nk, m->p2, TC_BM)) ||
+      (rc = encode_a_chunked(c, fn, &m->tm_ub_hi, m->ub_hi, nb, m->p2 / TC_BK, (uint64_t)ns * nk)) ||
+      (rc = encode_a_chunked(c, fn, &m->tm_ub_lo, m->ub_lo, nb, m->p2 / TC_BK, (uint64_t)ns * nk)) ||
       (rc = encode_b_mn(c, fn, &m->tm_b2, m->b2, ncol, m->p2, nk)))
     return rc;
 
@@ -1225,6 +1258,7 @@ int mixed_init(ocn_ctx* c) {
   g2.nch = 2 * nxc;
   g2.mt2 = (nb + TC_BM - 1) / TC_BM;
   g2.bmn = 1;
+  g2.achunk = 1;
   g2.idesc = idesc | (1u << 16);  // B MN-major
   m->stage_bytes = stage_bytes;
   m->max_stages = stages;
@@ -1464,6 +1498,7 @@ int mixed_set_mult(ocn_ctx* c) {
   b.ntiles = nk * b.mt2;
   b.bshared = 1;
   b.bmn = 0;  // B3 is K-major
+  b.achunk = 0;
   b.idesc = m->g1.idesc;
   c->mult_parts = 1;
   if ((rc = mixed_configure(c, m->cfg))) return rc;  // partial-sum room, multiplet grids
