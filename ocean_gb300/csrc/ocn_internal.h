@@ -48,18 +48,6 @@ struct CombineArgs {
   int nv;    // vectors of this context; blocks beyond it return at once
   int nblk;  // blocks per vector of this context (its own launches' grid); blocks beyond return
 };
-struct Lanczos2Args {
-  const double* red1;
-  int nblk;
-  double *hr, *hi;
-  const double *pr, *pi;
-  size_t n;
-  double* red2;
-  double *ra_base, *ia_base;
-  const int* itp;
-  BlockStrides bs;
-  int nv;
-};
 
 // Kernel classes timed with CUDA events on the context stream when timing is on.
 enum TimedClass { T_LR_GEMM1 = 0, T_LR_FFT, T_LR_GEMM2, T_LR_PREP, T_MULT, T_LANCZOS, T_NCLASS };
@@ -377,8 +365,10 @@ int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vst
 // Tensor-core partials (binary32) and the double-float Haydock vectors: mixed precision.
 inline bool mixed_parts(const ocn_ctx* c) { return c->dims.precision == OCN_PREC_MIXED && c->mixed != nullptr; }
 int haydock_to_df(ocn_ctx* c, double* buf, int nv);
-int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rstride, double* h,
-                    double* rb, size_t cstride, const int* itp);
+// Lanczos stage 2 and the normalisation of nv double-float chains from the combine
+// partials: a_{i-1}, b_i, psi = (h - a psi) / b_i in place of h, and the next psi operand
+int mixed_norm_prep(ocn_ctx* c, int nv, const double* psi, double* h, double* ra, double* ia, double* rb,
+                    size_t cstride, const int* itp);
 int mixed_check(ocn_ctx* c);       // reads and clears the device timeout flag
 int mixed_set_starve(ocn_ctx* c, int on);  // test hook of ocn_test_starve_tc
 // multiplet on the tensor cores: operands from c->mult (after ocn_set_mult), and

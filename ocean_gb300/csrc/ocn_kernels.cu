@@ -410,7 +410,9 @@ __device__ __forceinline__ void reduce_pairs_df(const float2* __restrict__ red, 
 
 // combine + first Lanczos stage (as combine_body with the Lanczos fields set,
 // OCEAN_action.f90:337-372 then OCEAN_haydock.f90:848-860): h = E o psi + allow o
-// (partials) + S psi - b_{i-1} old, and the block partial of <h|psi>.
+// (partials) + S psi - b_{i-1} old, and the block partials of <h|psi> (red[2 bx],
+// red[2 bx + 1]) and of |h|^2, |psi|^2 (red[2 nbx + 2 bx], red[2 nbx + 2 bx + 1]),
+// from which the normalisation forms b_i without another pass over h.
 template <int NA, bool SO>
 __device__ __forceinline__ void combine_df_body(const float2* __restrict__ pr, const float2* __restrict__ pi,
                                                 const float2* __restrict__ er, const float2* __restrict__ ei,
@@ -421,7 +423,7 @@ __device__ __forceinline__ void combine_df_body(const float2* __restrict__ pr, c
                                                 const double* __restrict__ rb_base, const int* __restrict__ itp,
                                                 float2* __restrict__ red, const BlockStrides bs, int bx, int by,
                                                 int nbx) {
-  __shared__ float2 sh[2][32];
+  __shared__ float2 sh[4][32];
   __shared__ float2 s_bm;
   const size_t v = by;
   pr += v * bs.vec;
@@ -439,7 +441,7 @@ __device__ __forceinline__ void combine_df_body(const float2* __restrict__ pr, c
   }
   __syncthreads();
   const df bm{s_bm.x, s_bm.y};
-  df dr{0.0f, 0.0f}, di{0.0f, 0.0f};
+  df dr{0.0f, 0.0f}, di{0.0f, 0.0f}, hh{0.0f, 0.0f}, pp{0.0f, 0.0f};
   const size_t nall = (size_t)nbk * NA;
   for (size_t idx = bx * (size_t)blockDim.x + threadIdx.x; idx < nall; idx += (size_t)nbx * blockDim.x) {
     const int ic = (int)(idx / (size_t)nbk);
@@ -483,15 +485,21 @@ __device__ __forceinline__ void combine_df_body(const float2* __restrict__ pr, c
     df_fma(dr.h, dr.l, hi, qi);
     df_fma(di.h, di.l, hr, qi);
     df_fma(di.h, di.l, df_neg(hi), qr);
+    df_fma(hh.h, hh.l, hr, hr);
+    df_fma(hh.h, hh.l, hi, hi);
+    df_fma(pp.h, pp.l, qr, qr);
+    df_fma(pp.h, pp.l, qi, qi);
     df_st(outr, idx, hr);
     df_st(outi, idx, hi);
   }
-  df q[2] = {dr, di};
-  float2 tot[2];
-  block_reduce_df<2>(q, sh, tot);
+  df q[4] = {dr, di, hh, pp};
+  float2 tot[4];
+  block_reduce_df<4>(q, sh, tot);
   if (threadIdx.x == 0) {
     red[2 * bx] = tot[0];
     red[2 * bx + 1] = tot[1];
+    red[2 * nbx + 2 * bx] = tot[2];
+    red[2 * nbx + 2 * bx + 1] = tot[3];
   }
 }
 
@@ -520,66 +528,6 @@ __global__ void __launch_bounds__(LZ_DF_THREADS) k_combine_df_group(const Combin
                           reinterpret_cast<float2*>(a.outr), reinterpret_cast<float2*>(a.outi), a.nbk, a.npsi,
                           a.use_e0, reinterpret_cast<const float2*>(a.oldr), reinterpret_cast<const float2*>(a.oldi),
                           a.rb_base, a.itp, reinterpret_cast<float2*>(a.red), a.bs, blockIdx.x, blockIdx.y, a.nblk);
-}
-
-// Lanczos stage 2 (OCEAN_haydock.f90:862-878): a_{i-1} = Re<h|psi>; h -= a psi; partial |h|^2.
-__device__ __forceinline__ void lanczos2_df_body(const float2* __restrict__ red1, int nblk, float2* __restrict__ hr,
-                                                 float2* __restrict__ hi, const float2* __restrict__ pr,
-                                                 const float2* __restrict__ pi, size_t n, float2* __restrict__ red2,
-                                                 double* __restrict__ ra_base, double* __restrict__ ia_base,
-                                                 const int* __restrict__ itp, const BlockStrides bs, int bx, int by,
-                                                 int nbx) {
-  __shared__ float2 sh[1][32];
-  const size_t v = by;
-  red1 += v * bs.red;
-  red2 += v * bs.red;
-  hr += v * bs.vec;
-  hi += v * bs.vec;
-  pr += v * bs.vec;
-  pi += v * bs.vec;
-  ra_base += v * bs.coef;
-  ia_base += v * bs.coef;
-  df a, ia;
-  reduce_pairs_df(red1, nblk, &a, &ia);
-  if (bx == 0 && threadIdx.x == 0) {
-    const int it = *itp;
-    ra_base[it - 1] = df_value(a);
-    ia_base[it - 1] = df_value(ia);
-  }
-  const df am = df_neg(a);
-  df s[1] = {df{0.0f, 0.0f}};
-  for (size_t e = bx * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)nbx * blockDim.x) {
-    const df r = df_add(df_ld(hr, e), df_mul(am, df_ld(pr, e)));
-    const df i = df_add(df_ld(hi, e), df_mul(am, df_ld(pi, e)));
-    df_st(hr, e, r);
-    df_st(hi, e, i);
-    df_fma(s[0].h, s[0].l, r, r);
-    df_fma(s[0].h, s[0].l, i, i);
-  }
-  float2 tot[1];
-  block_reduce_df<1>(s, sh, tot);
-  if (threadIdx.x == 0) {
-    red2[2 * bx] = tot[0];
-    red2[2 * bx + 1] = make_float2(0.0f, 0.0f);
-  }
-}
-
-__global__ void __launch_bounds__(LZ_DF_THREADS)
-    k_lanczos2_df(const float2* __restrict__ red1, int nblk, float2* __restrict__ hr, float2* __restrict__ hi,
-                  const float2* __restrict__ pr, const float2* __restrict__ pi, size_t n, float2* __restrict__ red2,
-                  double* __restrict__ ra_base, double* __restrict__ ia_base, const int* __restrict__ itp,
-                  const BlockStrides bs) {
-  lanczos2_df_body(red1, nblk, hr, hi, pr, pi, n, red2, ra_base, ia_base, itp, bs, blockIdx.x, blockIdx.y,
-                   gridDim.x);
-}
-
-__global__ void __launch_bounds__(LZ_DF_THREADS) k_lanczos2_df_group(const Lanczos2Args* __restrict__ tab) {
-  const Lanczos2Args& a = tab[blockIdx.z];
-  if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
-  lanczos2_df_body(reinterpret_cast<const float2*>(a.red1), a.nblk, reinterpret_cast<float2*>(a.hr),
-                   reinterpret_cast<float2*>(a.hi), reinterpret_cast<const float2*>(a.pr),
-                   reinterpret_cast<const float2*>(a.pi), a.n, reinterpret_cast<float2*>(a.red2), a.ra_base,
-                   a.ia_base, a.itp, a.bs, blockIdx.x, blockIdx.y, a.nblk);
 }
 
 // Operator data of the double-float loop, from the FP64 copies: energies as
@@ -1255,14 +1203,8 @@ int lanczos_launch(ocn_ctx* c, int nv, const double* old, const double* psi, dou
         rb, itp, reinterpret_cast<float2*>(c->d_red), bs);
     ++c->launches;
     OCN_CUDA(c, cudaGetLastError());
-    k_lanczos2_df<<<grid, LZ_DF_THREADS, 0, c->stream>>>(
-        reinterpret_cast<cf2>(c->d_red), nblk, reinterpret_cast<float2*>(h), reinterpret_cast<float2*>(h + n),
-        reinterpret_cast<cf2>(psi), reinterpret_cast<cf2>(psi + n), n, reinterpret_cast<float2*>(c->d_red + 2 * nblk),
-        ra, ia, itp, bs);
-    ++c->launches;
-    OCN_CUDA(c, cudaGetLastError());
-    // b_i, psi = h / b_i and the next psi operand
-    return mixed_norm_prep(c, nv, c->d_red + 2 * nblk, nblk, bs.red, h, rb, cstride, itp);
+    // a_{i-1}, b_i, psi = (h - a psi) / b_i and the next psi operand
+    return mixed_norm_prep(c, nv, psi, h, ra, ia, rb, cstride, itp);
   }
   auto kern = combine_kernel(c->na, use_so, false);
   kern<<<grid, LZ_THREADS, 0, c->stream>>>(psi, psi + n, c->d_er, c->ei_nonzero ? c->d_ei : nullptr,
@@ -1382,7 +1324,6 @@ struct LzGroup {
   std::vector<Cls> cls;
   std::vector<int> order;  // member index of each record
   CombineArgs* d_comb[3] = {nullptr, nullptr, nullptr};
-  Lanczos2Args* d_lz2[3] = {nullptr, nullptr, nullptr};
   int** d_iters = nullptr;
 };
 
@@ -1390,7 +1331,6 @@ void lz_group_destroy(LzGroup* g) {
   if (!g) return;
   for (int r = 0; r < 3; ++r) {
     if (g->d_comb[r]) cudaFree(g->d_comb[r]);
-    if (g->d_lz2[r]) cudaFree(g->d_lz2[r]);
   }
   if (g->d_iters) cudaFree(g->d_iters);
   delete g;
@@ -1409,7 +1349,6 @@ int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out) {
   g->nblk = c0->red_blocks;
   std::vector<int*> iters;
   std::vector<CombineArgs> ca(mem.size());
-  std::vector<Lanczos2Args> la(mem.size());
   int rc = OCN_OK;
   for (const BatchMember& b : mem) {
     g->nvmax = std::max(g->nvmax, b.nv);
@@ -1474,25 +1413,9 @@ int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out) {
       a.so_f = c->d_so_f;
       a.nv = b.nv;
       a.nblk = nblk;
-      Lanczos2Args& l = la[i];
-      l.red1 = c->d_red;
-      l.nblk = nblk;
-      l.hr = h;
-      l.hi = h + n;
-      l.pr = psi;
-      l.pi = psi + n;
-      l.n = n;
-      l.red2 = c->d_red + 2 * nblk;
-      l.ra_base = b.ra;
-      l.ia_base = b.ia;
-      l.itp = c->d_iter;
-      l.bs = bs;
-      l.nv = b.nv;
     }
     cudaError_t e = cudaMalloc(&g->d_comb[r], ca.size() * sizeof(CombineArgs));
-    if (e == cudaSuccess) e = cudaMalloc(&g->d_lz2[r], la.size() * sizeof(Lanczos2Args));
     if (e == cudaSuccess) e = cudaMemcpy(g->d_comb[r], ca.data(), ca.size() * sizeof(CombineArgs), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(g->d_lz2[r], la.data(), la.size() * sizeof(Lanczos2Args), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) rc = cuda_fail(c0, e, "batched Lanczos tables");
   }
   if (rc == OCN_OK) {
@@ -1509,7 +1432,7 @@ int lz_group_create(const std::vector<BatchMember>& mem, LzGroup** out) {
 }
 
 // Kernels of one lz_group_advance + lz_group_step.
-int lz_group_launches(const LzGroup* g) { return 2 + (int)g->cls.size(); }
+int lz_group_launches(const LzGroup* g) { return 1 + (int)g->cls.size(); }
 
 int lz_group_advance(LzGroup* g, cudaStream_t s) {
   k_advance_group<<<(g->n + 127) / 128, 128, 0, s>>>(g->d_iters, g->n);
@@ -1531,9 +1454,7 @@ int lz_group_step(LzGroup* g, int rot, cudaStream_t s) {
     }
     if (cudaGetLastError() != cudaSuccess) return OCN_ERR_CUDA;
   }
-  const dim3 grid(g->nblk, g->nvmax, g->n);
-  k_lanczos2_df_group<<<grid, LZ_DF_THREADS, 0, s>>>(g->d_lz2[rot]);
-  return cudaGetLastError() == cudaSuccess ? OCN_OK : OCN_ERR_CUDA;
+  return OCN_OK;
 }
 
 }  // namespace ocn

@@ -697,40 +697,63 @@ __global__ void k_prep_b3(const double2* __restrict__ hamp, __nv_bfloat16* __res
   base[(size_t)(3 * na + a) * p3 + np + p] = nl;
 }
 
-// Lanczos normalisation fused with the next action's psi operand
-// (OCEAN_haydock.f90:880-889 then long_range.f90:897-906), on the double-float
-// vectors of the mixed-precision loop: for chain v = blockIdx.y, b_i = sqrt(sum of
-// the double-float partials) (formed in FP64 by one thread, broadcast as a
-// double-float 1/b_i), psi = h / b_i written in place, and B1 rows of vector v
-// built from allow o psi.  One thread per (n, k) covers both K = n and K = Nb + n
-// for every alpha.
-__device__ __forceinline__ void norm_prep_body(const double* __restrict__ red2, int nblk, size_t rstride,
-                            double* __restrict__ hbase, size_t vstride, size_t npsi,
-                            const float* __restrict__ allow, __nv_bfloat16* __restrict__ b1, int nb,
-                            int nk, int na, int ncol, int p1, double* __restrict__ rb_base,
-                            size_t cstride, const int* __restrict__ itp, int bx, int by, int nbx) {
-  __shared__ float2 sh[32];
-  __shared__ float2 s_inv;
+// Lanczos stage 2 and normalisation fused with the next action's psi operand
+// (OCEAN_haydock.f90:862-889 then long_range.f90:897-906), on the double-float
+// vectors of the mixed-precision loop, for chain v = blockIdx.y: from the
+// combine's double-float partials, a + i ia = <h|psi> and b_i^2 = |h - a psi|^2 =
+// |h|^2 - 2 a Re<h|psi> + a^2 |psi|^2 (formed in FP64 by one thread and broadcast,
+// so h is read once); psi = (h - a psi) / b_i written in place of h, and B1 rows of
+// vector v built from allow o psi.  One thread per (n, k) covers both K = n and
+// K = Nb + n for every alpha.  Every CTA sums the partials in the same order.
+__device__ __forceinline__ void norm_prep_body(const double* __restrict__ red1, int nblk, size_t rstride,
+                            double* __restrict__ hbase, const double* __restrict__ pbase, size_t vstride,
+                            size_t npsi, const float* __restrict__ allow, __nv_bfloat16* __restrict__ b1, int nb,
+                            int nk, int na, int ncol, int p1, double* __restrict__ ra_base,
+                            double* __restrict__ ia_base, double* __restrict__ rb_base, size_t cstride,
+                            const int* __restrict__ itp, int bx, int by, int nbx) {
+  __shared__ float2 sh[4][32];
+  __shared__ float2 s_am, s_inv;
   const int vv = by;
-  const float2* red = reinterpret_cast<const float2*>(red2 + (size_t)vv * rstride);
-  df s{0.0f, 0.0f};
-  for (int i = threadIdx.x; i < nblk; i += blockDim.x) s = df_add(s, df{red[2 * i].x, red[2 * i].y});
-  for (int o = 16; o > 0; o >>= 1)
-    s = df_add(s, df{__shfl_down_sync(0xffffffffu, s.h, o), __shfl_down_sync(0xffffffffu, s.l, o)});
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = make_float2(s.h, s.l);
+  const float2* r1 = reinterpret_cast<const float2*>(red1 + (size_t)vv * rstride);  // <h|psi> pairs
+  const float2* r2 = r1 + 2 * nblk;                                                // |h|^2, |psi|^2 pairs
+  df q[4] = {df{0.0f, 0.0f}, df{0.0f, 0.0f}, df{0.0f, 0.0f}, df{0.0f, 0.0f}};
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) {
+    q[0] = df_add(q[0], df{r1[2 * i].x, r1[2 * i].y});
+    q[1] = df_add(q[1], df{r1[2 * i + 1].x, r1[2 * i + 1].y});
+    q[2] = df_add(q[2], df{r2[2 * i].x, r2[2 * i].y});
+    q[3] = df_add(q[3], df{r2[2 * i + 1].x, r2[2 * i + 1].y});
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    for (int o = 16; o > 0; o >>= 1)
+      q[j] = df_add(q[j], df{__shfl_down_sync(0xffffffffu, q[j].h, o), __shfl_down_sync(0xffffffffu, q[j].l, o)});
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) sh[j][threadIdx.x >> 5] = make_float2(q[j].h, q[j].l);
   __syncthreads();
   if (threadIdx.x == 0) {
-    df bb{0.0f, 0.0f};
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) bb = df_add(bb, df{sh[i].x, sh[i].y});
-    const double b = sqrt(df_value(bb));
-    if (bx == 0) rb_base[(size_t)vv * cstride + *itp] = b;
-    const df inv = df_split(1.0 / b);
+    df t[4] = {df{0.0f, 0.0f}, df{0.0f, 0.0f}, df{0.0f, 0.0f}, df{0.0f, 0.0f}};
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) t[j] = df_add(t[j], df{sh[j][i].x, sh[j][i].y});
+    const double a = df_value(t[0]), hh = df_value(t[2]), pp = df_value(t[3]);
+    const double b = sqrt(hh - 2.0 * a * a + a * a * pp);
+    if (bx == 0) {
+      const int it = *itp;
+      ra_base[(size_t)vv * cstride + it - 1] = a;
+      ia_base[(size_t)vv * cstride + it - 1] = df_value(t[1]);
+      rb_base[(size_t)vv * cstride + it] = b;
+    }
+    const df am = df_neg(t[0]), inv = df_split(1.0 / b);
+    s_am = make_float2(am.h, am.l);
     s_inv = make_float2(inv.h, inv.l);
   }
   __syncthreads();
-  const df inv{s_inv.x, s_inv.y};
+  const df am{s_am.x, s_am.y}, inv{s_inv.x, s_inv.y};
   float2* hr = reinterpret_cast<float2*>(hbase + (size_t)vv * vstride);
   float2* hi = hr + npsi;
+  const float2* pr = reinterpret_cast<const float2*>(pbase + (size_t)vv * vstride);
+  const float2* pi = pr + npsi;
   const int g4 = 4 * na;
   const int total = nb * nk;
   for (int i = bx * blockDim.x + threadIdx.x; i < total; i += nbx * blockDim.x) {
@@ -739,7 +762,8 @@ __device__ __forceinline__ void norm_prep_body(const double* __restrict__ red2, 
     __nv_bfloat16* base = b1 + (size_t)k * ncol * p1 + (size_t)vv * g4 * p1;
     for (int a = 0; a < na; ++a) {
       const size_t idx = (size_t)i + (size_t)total * a;
-      const df r = df_mul(df_ld(hr, idx), inv), im = df_mul(df_ld(hi, idx), inv);
+      const df r = df_mul(df_add(df_ld(hr, idx), df_mul(am, df_ld(pr, idx))), inv);
+      const df im = df_mul(df_add(df_ld(hi, idx), df_mul(am, df_ld(pi, idx))), inv);
       df_st(hr, idx, r);
       df_st(hi, idx, im);
       const float m = allow[idx];
@@ -762,24 +786,26 @@ __device__ __forceinline__ void norm_prep_body(const double* __restrict__ red2, 
 }
 
 __global__ void __launch_bounds__(LZ_DF_THREADS)
-    k_norm_prep(const double* __restrict__ red2, int nblk, size_t rstride, double* __restrict__ hbase,
-                size_t vstride, size_t npsi, const float* __restrict__ allow, __nv_bfloat16* __restrict__ b1,
-                int nb, int nk, int na, int ncol, int p1, double* __restrict__ rb_base, size_t cstride,
+    k_norm_prep(const double* __restrict__ red1, int nblk, size_t rstride, double* __restrict__ hbase,
+                const double* __restrict__ pbase, size_t vstride, size_t npsi, const float* __restrict__ allow,
+                __nv_bfloat16* __restrict__ b1, int nb, int nk, int na, int ncol, int p1, double* __restrict__ ra_base,
+                double* __restrict__ ia_base, double* __restrict__ rb_base, size_t cstride,
                 const int* __restrict__ itp) {
-  norm_prep_body(red2, nblk, rstride, hbase, vstride, npsi, allow, b1, nb, nk, na, ncol, p1, rb_base, cstride, itp,
-                 blockIdx.x, blockIdx.y, gridDim.x);
+  norm_prep_body(red1, nblk, rstride, hbase, pbase, vstride, npsi, allow, b1, nb, nk, na, ncol, p1, ra_base, ia_base,
+                 rb_base, cstride, itp, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
 struct NormGroupArgs {
-  const double* red2;
+  const double* red1;
   int nblk;
   size_t rstride;
   double* hbase;
+  const double* pbase;
   size_t vstride, npsi;
   const float* allow;
   __nv_bfloat16* b1;
   int nb, nk, na, ncol, p1;
-  double* rb_base;
+  double *ra_base, *ia_base, *rb_base;
   size_t cstride;
   const int* itp;
   int nv;
@@ -788,9 +814,10 @@ struct NormGroupArgs {
 __global__ void __launch_bounds__(LZ_DF_THREADS) k_norm_prep_group(const NormGroupArgs* __restrict__ tab) {
   const NormGroupArgs& a = tab[blockIdx.z];
   if ((int)blockIdx.y >= a.nv || (int)blockIdx.x >= a.nblk) return;
-  norm_prep_body(a.red2, a.nblk, a.rstride, a.hbase, a.vstride, a.npsi, a.allow, a.b1, a.nb, a.nk, a.na, a.ncol,
-                 a.p1, a.rb_base, a.cstride, a.itp, blockIdx.x, blockIdx.y, a.nblk);
+  norm_prep_body(a.red1, a.nblk, a.rstride, a.hbase, a.pbase, a.vstride, a.npsi, a.allow, a.b1, a.nb, a.nk, a.na,
+                 a.ncol, a.p1, a.ra_base, a.ia_base, a.rb_base, a.cstride, a.itp, blockIdx.x, blockIdx.y, a.nblk);
 }
+
 
 // The last of n records whose first CTA is <= b (records ordered by cta0).
 template <class A>
@@ -1601,12 +1628,14 @@ int mixed_check(ocn_ctx* c) {
   return OCN_OK;
 }
 
-int mixed_norm_prep(ocn_ctx* c, int nv, const double* red2, int nblk, size_t rstride, double* h,
-                    double* rb, size_t cstride, const int* itp) {
+int mixed_norm_prep(ocn_ctx* c, int nv, const double* psi, double* h, double* ra, double* ia, double* rb,
+                    size_t cstride, const int* itp) {
   MixedLR* m = c->mixed;  // timed as part of the enclosing Lanczos step
+  const int nblk = c->red_blocks;
   dim3 grid(nblk, nv);
-  k_norm_prep<<<grid, LZ_DF_THREADS, 0, c->stream>>>(red2, nblk, rstride, h, 2 * c->npsi, c->npsi, c->d_allow_f, m->b1,
-                                           c->nb, c->nk, c->na, m->ncol, m->p1, rb, cstride, itp);
+  k_norm_prep<<<grid, LZ_DF_THREADS, 0, c->stream>>>(c->d_red, nblk, (size_t)4 * nblk, h, psi, 2 * c->npsi, c->npsi,
+                                                      c->d_allow_f, m->b1, c->nb, c->nk, c->na, m->ncol, m->p1, ra,
+                                                      ia, rb, cstride, itp);
   ++c->launches;
   OCN_CUDA(c, cudaGetLastError());
   return OCN_OK;
@@ -1835,17 +1864,18 @@ int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out) {
   }
   for (auto& f : g->fft)
     if (rc == OCN_OK) rc = upload(c0, &f.d, f.h);
-  // normalisation + next psi operand, per buffer rotation
+  // Lanczos stage 2 + normalisation + next psi operand, per buffer rotation
   for (int r = 0; r < 3 && rc == OCN_OK; ++r) {
     std::vector<NormGroupArgs> nt;
     for (const BatchMember& b : mem) {
       const ocn_ctx* c = b.c;
       const MixedLR* m = c->mixed;
       NormGroupArgs a;
-      a.red2 = c->d_red + 2 * c->red_blocks;
+      a.red1 = c->d_red;
       a.nblk = c->red_blocks;
       a.rstride = (size_t)4 * c->red_blocks;
       a.hbase = b.buf[(r + 2) % 3];
+      a.pbase = b.buf[(r + 1) % 3];
       a.vstride = 2 * c->npsi;
       a.npsi = c->npsi;
       a.allow = c->d_allow_f;
@@ -1855,6 +1885,8 @@ int lr_group_create(const std::vector<BatchMember>& mem, LrGroup** out) {
       a.na = c->na;
       a.ncol = m->ncol;
       a.p1 = m->p1;
+      a.ra_base = b.ra;
+      a.ia_base = b.ia;
       a.rb_base = b.rb;
       a.cstride = b.cstride;
       a.itp = c->d_iter;
