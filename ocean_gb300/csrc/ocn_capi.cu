@@ -652,7 +652,9 @@ int haydock_iteration(ocn_ctx* c, int nv, double* old, double* psi, double* h, d
                       double* rb, size_t cstride) {
   const size_t n = c->npsi;
   int rc;
-  if ((rc = advance_iter(c, c->d_iter))) return rc;
+  // mixed precision: the step's first tensor-core launch advances the iteration counter
+  if (mixed_parts(c)) mixed_defer_advance(c, c->d_iter);
+  else if ((rc = advance_iter(c, c->d_iter))) return rc;
   c->acc_valid = false;
   if (c->sys.mult && c->sys.nhflag[4] == 1 && c->have_mult) {
     if (c->mult_parts > 0) {  // tensor cores; the psi operand was built with the last normalisation
@@ -672,6 +674,7 @@ int haydock_iteration(ocn_ctx* c, int nv, double* old, double* psi, double* h, d
                                                : lr_apply_fp64(c, psi, psi + n);
     if (rc) return rc;
   }
+  if (mixed_take_advance(c) && (rc = advance_iter(c, c->d_iter))) return rc;  // no term ran a contraction
   rc = lanczos_launch(c, nv, old, psi, h, ra, ia, rb, cstride, c->d_iter);
   if (rc == OCN_OK && c->conv_on && nv == 1) rc = conv_check_launch(c, ra, ia, rb, c->d_iter);
   return rc;
@@ -781,6 +784,7 @@ int haydock_prepare(ocn_ctx* c, int nv, const double* p0r, const double* p0i, si
     OCN_CUDA(c, cudaMemsetAsync(c->d_conv_rel, 0, ((size_t)c->hay_cap + 1) * sizeof(double), c->stream));
   }
   if (mixed_parts(c)) {
+    mixed_take_advance(c);  // no request of an earlier, failed step carries over
     // first psi operand from the FP64 start vectors, then the loop's double-float form
     if ((rc = mixed_prep_b1(c, R->buf[1], R->buf[1] + n, 2 * n, nv))) return rc;
     if (!c->d_er_df && ((rc = dev_alloc(c, &c->d_er_df, n)) || (rc = dev_alloc(c, &c->d_ei_df, n)) ||

@@ -361,6 +361,8 @@ int mixed_set_bloch(ocn_ctx* c);   // builds split-BF16 layouts from d_u
 int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vstride, int nv,
                    bool b1_ready = false);
 int mixed_prep_b1(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vstride, int nv);
+void mixed_defer_advance(ocn_ctx* c, int* itp);  // the next band -> x launch adds 1 to *itp
+bool mixed_take_advance(ocn_ctx* c);             // true (and cleared) if no launch took the request
 // b_i = sqrt(partials), psi = h / b_i, and the psi operand of the next action (nv chains)
 // Tensor-core partials (binary32) and the double-float Haydock vectors: mixed precision.
 inline bool mixed_parts(const ocn_ctx* c) { return c->dims.precision == OCN_PREC_MIXED && c->mixed != nullptr; }

@@ -82,6 +82,7 @@ struct TcParams {
                  // first bounded wait runs out with nothing in flight (OCN_ERR_TIMEOUT path)
   int bmn;       // B is MN-major in SW32 boxes of 16 columns by 64 K rows (B2 of the x -> band contraction)
   int achunk;    // A is stored chunk-major, [k][K chunk][row][64] (UB): every A box is one contiguous run
+  int* inc;      // launch-wide: non-null, block 0 adds 1 to it (the Haydock iteration counter; saves a launch)
 };
 
 // Tensor maps of a group launch (kernel parameter space, 384 bytes per problem).
@@ -271,6 +272,7 @@ __device__ __forceinline__ void lr_tc_body(const TcParams& p, const Src& src) {
   const uint32_t tfull0 = su32(bars + 2 * TC_MAX_STAGES), tempty0 = su32(bars + 2 * TC_MAX_STAGES + 2);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (p.inc && blockIdx.x == 0 && threadIdx.x == 0) *p.inc += 1;  // nothing in this launch reads it
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(full0 + 8 * s, 1);
@@ -1128,6 +1130,7 @@ struct MixedLR {
   TcParams gm1{}, gm2{};
   int gridm1 = 0, gridm2 = 0;
   bool ready = false;
+  int* pending_inc = nullptr;  // set by a Haydock step: the next band -> x launch advances this counter
 };
 
 namespace {
@@ -1553,6 +1556,8 @@ int mult_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t 
   for (int s = 0; s < ns; ++s) {
     a.koff = s * c->nk;
     a.spin = ns == 2 ? s : -1;
+    a.inc = m->pending_inc;
+    m->pending_inc = nullptr;
     k_lr_tc<<<m->gridm1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ma_hi, m->tm_ma_lo, m->tm_b1, a);
     ++c->launches;
   }
@@ -1607,6 +1612,18 @@ int mixed_set_bloch(ocn_ctx* c) {
   OCN_CUDA(c, cudaStreamSynchronize(c->stream));
   m->ready = true;
   return OCN_OK;
+}
+
+// The iteration counter of a Haydock step, advanced by the step's first
+// tensor-core launch (band -> x or the multiplet amplitudes) instead of a launch
+// of its own; mixed_take_advance reports (and clears) a request no launch took.
+void mixed_defer_advance(ocn_ctx* c, int* itp) {
+  if (c->mixed) c->mixed->pending_inc = itp;
+}
+bool mixed_take_advance(ocn_ctx* c) {
+  if (!c->mixed || !c->mixed->pending_inc) return false;
+  c->mixed->pending_inc = nullptr;
+  return true;
 }
 
 int mixed_set_starve(ocn_ctx* c, int on) {
@@ -1669,6 +1686,8 @@ int lr_apply_mixed(ocn_ctx* c, const double* d_pr, const double* d_pi, size_t vs
     for (int s = 0; s < ns; ++s) {
       g1.koff = s * nk;
       g1.spin = ns == 2 ? s : -1;
+      g1.inc = m->pending_inc;  // the first launch of a Haydock step advances its iteration counter
+      m->pending_inc = nullptr;
       k_lr_tc<<<m->grid1, TC_THREADS, m->smem_bytes, c->stream>>>(m->tm_ua_hi, m->tm_ua_lo, m->tm_b1, g1);
       ++c->launches;
       OCN_CUDA(c, cudaGetLastError());
