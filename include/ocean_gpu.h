@@ -225,7 +225,9 @@ int ocn_apply_H_block(ocn_ctx* ctx, int nv, const double* in_r, const double* in
  * OCEAN_psi.f90:5589-5638).  Writes real_a[0..niter], imag_a[0..niter],
  * real_b[0..niter] (index 0 of b unused = 0, a[niter] = 0 as in the reference's
  * zero-initialised arrays).  *niter_done = iterations completed.
- * Returns OCN_ERR_NAN if an a_n is NaN (checked after the loop).  Host buffers. */
+ * Returns OCN_ERR_NAN if an a_n is NaN (checked after the loop).  Host buffers.
+ * Mixed-precision contexts keep the Lanczos vectors in double-float (binary32
+ * pairs, ~48 significant bits) on the device; a, b are formed and returned in FP64. */
 int ocn_haydock(ocn_ctx* ctx, const double* psi0_r, const double* psi0_i, int niter,
                 double* real_a, double* imag_a, double* real_b, int* niter_done);
 

@@ -369,12 +369,14 @@ __device__ __forceinline__ void block_reduce_df(df (&v)[K], float2 (*sh)[32], fl
 #pragma unroll
     for (int j = 0; j < K; ++j) sh[j][w] = make_float2(v[j].h, v[j].l);
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (w == 0) {  // the warp partials, summed by a fixed shuffle tree
+    const int nw = (int)(blockDim.x >> 5);
 #pragma unroll
     for (int j = 0; j < K; ++j) {
-      df t{0.0f, 0.0f};
-      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t = df_add(t, df{sh[j][i].x, sh[j][i].y});
-      out[j] = make_float2(t.h, t.l);
+      df t = l < nw ? df{sh[j][l].x, sh[j][l].y} : df{0.0f, 0.0f};
+      for (int o = 16; o > 0; o >>= 1)
+        t = df_add(t, df{__shfl_down_sync(0xffffffffu, t.h, o), __shfl_down_sync(0xffffffffu, t.l, o)});
+      if (l == 0) out[j] = make_float2(t.h, t.l);
     }
   }
 }
@@ -424,7 +426,6 @@ __device__ __forceinline__ void combine_df_body(const float2* __restrict__ pr, c
                                                 float2* __restrict__ red, const BlockStrides bs, int bx, int by,
                                                 int nbx) {
   __shared__ float2 sh[4][32];
-  __shared__ float2 s_bm;
   const size_t v = by;
   pr += v * bs.vec;
   pi += v * bs.vec;
@@ -435,12 +436,11 @@ __device__ __forceinline__ void combine_df_body(const float2* __restrict__ pr, c
   part += v * 2 * npsi;
   rb_base += v * bs.coef;
   red += v * bs.red;
-  if (threadIdx.x == 0) {
-    const df b = df_split(-rb_base[*itp - 1]);  // -b_{i-1}
-    s_bm = make_float2(b.h, b.l);
-  }
-  __syncthreads();
-  const df bm{s_bm.x, s_bm.y};
+  // -b_{i-1}, formed by each warp's lane 0 (no block barrier before the element loop)
+  df bm{0.0f, 0.0f};
+  if ((threadIdx.x & 31) == 0) bm = df_split(-rb_base[*itp - 1]);
+  bm.h = __shfl_sync(0xffffffffu, bm.h, 0);
+  bm.l = __shfl_sync(0xffffffffu, bm.l, 0);
   df dr{0.0f, 0.0f}, di{0.0f, 0.0f}, hh{0.0f, 0.0f}, pp{0.0f, 0.0f};
   const size_t nall = (size_t)nbk * NA;
   for (size_t idx = bx * (size_t)blockDim.x + threadIdx.x; idx < nall; idx += (size_t)nbx * blockDim.x) {

@@ -733,11 +733,17 @@ __device__ __forceinline__ void norm_prep_body(const double* __restrict__ red1, 
 #pragma unroll
     for (int j = 0; j < 4; ++j) sh[j][threadIdx.x >> 5] = make_float2(q[j].h, q[j].l);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    df t[4] = {df{0.0f, 0.0f}, df{0.0f, 0.0f}, df{0.0f, 0.0f}, df{0.0f, 0.0f}};
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i)
+  df t[4] = {df{0.0f, 0.0f}, df{0.0f, 0.0f}, df{0.0f, 0.0f}, df{0.0f, 0.0f}};
+  if (threadIdx.x < 32) {  // warp 0 adds the warp partials by a fixed shuffle tree
+    const int nw = (int)(blockDim.x >> 5), l = threadIdx.x;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) t[j] = df_add(t[j], df{sh[j][i].x, sh[j][i].y});
+    for (int j = 0; j < 4; ++j) {
+      t[j] = l < nw ? df{sh[j][l].x, sh[j][l].y} : df{0.0f, 0.0f};
+      for (int o = 16; o > 0; o >>= 1)
+        t[j] = df_add(t[j], df{__shfl_down_sync(0xffffffffu, t[j].h, o), __shfl_down_sync(0xffffffffu, t[j].l, o)});
+    }
+  }
+  if (threadIdx.x == 0) {
     const double a = df_value(t[0]), hh = df_value(t[2]), pp = df_value(t[3]);
     const double b = sqrt(hh - 2.0 * a * a + a * a * pp);
     if (bx == 0) {
