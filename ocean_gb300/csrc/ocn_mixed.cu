@@ -18,7 +18,8 @@
 //
 // Operands live in HBM as bf16 tiles read by TMA:
 //   UA_s [k][x][K1]  (K1 = 2 Nb)      A of the band -> x contraction, built once
-//   UB_s [k][n][K2]                   A of the x -> band contraction, built once
+//   UB_s [k][K2/64][n][64]            A of the x -> band contraction, built once, chunk-major
+//                                     (each 128-band x 64 TMA box is one contiguous run)
 //   B1   [k][j][K1]                   psi operand, rebuilt per action
 //   B2   [k][K2][j]                   phi' operand, MN-major, written by the k-mesh transform
 // with K2 = (x/64)*128 + c*64 + x%64 (both c halves of a 64-x block in consecutive
