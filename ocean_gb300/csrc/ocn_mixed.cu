@@ -644,35 +644,36 @@ __global__ void k_build_mb(const double2* __restrict__ mpc, __nv_bfloat16* __res
   }
 }
 
-// amp[v][p][a] = sum_k amp_part[k][p][v*Na + a], summed in FP64: a CTA owns
+// amp[v][p][a] = sum_k amp_part[k][p][v*Na + a], summed in double-float: a CTA owns
 // 32 consecutive (p, t) outputs (coalesced along t) and its AMP_KGROUPS warps
 // split the k range (warp w takes k = w, w + AMP_KGROUPS, ...); warp 0 adds
 // the group partials in order (deterministic).
 constexpr int AMP_KGROUPS = 32;
 __global__ void __launch_bounds__(32 * AMP_KGROUPS)
     k_amp_reduce_f32(const float2* __restrict__ part, double2* __restrict__ amp, int nk, int np, int na, int nv) {
-  __shared__ double2 sh[AMP_KGROUPS][32];
+  __shared__ float4 sh[AMP_KGROUPS][32];  // double-float (re h, re l, im h, im l)
   const int nt = na * nv;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int i = blockIdx.x * 32 + lane;
-  double sr = 0.0, si = 0.0;
+  df sr{0.0f, 0.0f}, si{0.0f, 0.0f};  // exact sums of the binary32 terms to ~48 bits, on the FP32 pipe
   if (i < np * nt)
     for (int k = w; k < nk; k += AMP_KGROUPS) {
       const float2 f = part[(size_t)k * np * nt + i];
-      sr += (double)f.x;
-      si += (double)f.y;
+      sr = df_add(sr, f.x);
+      si = df_add(si, f.y);
     }
-  sh[w][lane] = make_double2(sr, si);
+  sh[w][lane] = make_float4(sr.h, sr.l, si.h, si.l);
   __syncthreads();
   if (w == 0 && i < np * nt) {
-    double tr = 0.0, ti = 0.0;
+    df tr{0.0f, 0.0f}, ti{0.0f, 0.0f};
     for (int g = 0; g < AMP_KGROUPS; ++g) {
-      tr += sh[g][lane].x;
-      ti += sh[g][lane].y;
+      const float4 q = sh[g][lane];
+      tr = df_add(tr, df{q.x, q.y});
+      ti = df_add(ti, df{q.z, q.w});
     }
     const int p = i / nt, t = i % nt;
     const int v = t / na, a = t % na;
-    amp[((size_t)v * np + p) * na + a] = make_double2(tr, ti);
+    amp[((size_t)v * np + p) * na + a] = make_double2(df_value(tr), df_value(ti));
   }
 }
 
